@@ -1,0 +1,164 @@
+// ref_shim.cpp -- C entry points into the reference's own signal-matrix code.
+//
+// TEST INFRASTRUCTURE ONLY.  The Makefile in this directory compiles this
+// file together with the reference's unmodified sources (read in place from
+// the reference checkout, never copied) into oracle/_ref/libopsecref.so.  It
+// is used to pin the oracle restatement and to generate golden vectors; the
+// GPU library never links it.
+//
+// The reference spherical survey links against HEALPix map readers
+// (chealpix.c needs cfitsio, which is absent); the three symbols it names are
+// stubbed below because the separation function never calls them.
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "BoxSurvey.h"
+#include "Cell.h"
+#include "Model.h"
+#include "QSpline.h"
+#include "SeparationFunc.h"
+#include "SphericalSurvey.h"
+#include "Spline.h"
+#include "TestModel.h"
+#include "XiFunc.h"
+#include "cfg.h"
+#include "sig.h"
+
+extern "C" {
+float* read_healpix_map(const char*, long*, char*, char*) { return NULL; }
+void ang2pix_nest(long, double, double, long* ip) { *ip = 0; }
+void ang2pix_ring(long, double, double, long* ip) { *ip = 0; }
+}
+
+namespace {
+
+// Same behaviour as the reference's RealSpaceXi (RealModel.cpp:19-30):
+// xi(p1,p2) = F(sep.r(p1,p2)) for a QSpline F.
+struct TableXi : public XiFuncImpl {
+    QSpline F;
+    explicit TableXi(const QSpline& f) : F(f) {}
+    double xi(const Point& p1, const Point& p2, const SeparationFunc& sep) { return F(sep.r(p1, p2)); }
+};
+
+Survey* make_survey(int coordsys, const double* grid, const int* n, double L) {
+    if (coordsys == CoordSysCartesian) {
+        Survey* s = new BoxSurvey("none", 1.0, L);
+        s->XMin = grid[0]; s->XMax = grid[1];
+        s->YMin = grid[2]; s->YMax = grid[3];
+        s->ZMin = grid[4]; s->ZMax = grid[5];
+        s->Nx = n[0]; s->Ny = n[1]; s->Nz = n[2];
+        return s;
+    }
+    Config cfg = cfg_new();
+    cfg_set_double(cfg, "RMin", grid[0]);
+    cfg_set_double(cfg, "RMax", grid[1]);
+    cfg_set_double(cfg, "MuMin", grid[2]);
+    cfg_set_double(cfg, "MuMuin", grid[2]);
+    cfg_set_double(cfg, "MuMax", grid[3]);
+    cfg_set_double(cfg, "PhiMin", grid[4]);
+    cfg_set_double(cfg, "PhiMax", grid[5]);
+    cfg_set_int(cfg, "Nr", n[0]);
+    cfg_set_int(cfg, "Nmu", n[1]);
+    cfg_set_int(cfg, "Nphi", n[2]);
+    cfg_set(cfg, "galfile", "none");
+    cfg_set(cfg, "maskfile", "none");
+    cfg_set(cfg, "radial", "none");
+    Survey* s = new SphericalSurvey(cfg);
+    cfg_destroy(cfg);
+    // Survey.cpp:32 requires the key MuMin but :39 reads the key MuMuin; both are set above
+    s->MuMin = grid[2];
+    return s;
+}
+
+void to_cell(const double* c, Cell& cell) {
+    memset(&cell, 0, sizeof(Cell));
+    cell.min1 = c[0]; cell.max1 = c[1];
+    cell.min2 = c[2]; cell.max2 = c[3];
+    cell.min3 = c[4]; cell.max3 = c[5];
+}
+
+}  // namespace
+
+extern "C" {
+
+// xi(r) = RealModel::GetXi for a tabulated P(k) (RealModel.cpp:98-108), or
+// the band derivative GetXiDeriv (RealModel.cpp:110-127) when band_kmax > band_kmin.
+void ref_xi_table(int npk, const double* pk_k, const double* pk_P, double band_kmin, double band_kmax,
+                  int n1, int n2, double r1, double r2, double* r_out, double* xi_out) {
+    std::vector<double> r = QSpline::MakeArray(n1, n2, r1, r2);
+    if (band_kmax > band_kmin) {
+        Spline one = ConstantSpline(1, band_kmin, band_kmax);
+        ComputeXiLM(0, 2, one, n1 + n2, &r[0], xi_out, 8192, band_kmin, band_kmax);
+    } else {
+        Spline pk = CubicSpline(npk, pk_k, pk_P);
+        ComputeXiLM(0, 2, pk, n1 + n2, &r[0], xi_out);
+    }
+    for (int i = 0; i < n1 + n2; i++) r_out[i] = r[i];
+}
+
+double ref_cspline_eval(int npk, const double* pk_k, const double* pk_P, double k) {
+    Spline pk = CubicSpline(npk, pk_k, pk_P);
+    return pk(k);
+}
+
+void ref_qspline_eval(int n1, int n2, const double* x, const double* y, int m, const double* r, double* out) {
+    QSpline q(n1, n2, x, y);
+    for (int i = 0; i < m; i++) out[i] = q(r[i]);
+}
+
+double ref_sep(int coordsys, double L, const double* p1, const double* p2) {
+    double grid[6] = {0, 1, -1, 1, 0, 2 * M_PI};
+    int n[3] = {1, 1, 1};
+    Survey* s = make_survey(coordsys, grid, n, L);
+    SeparationFunc sep = s->GetSeparationFunction();
+    Point a = {p1[0], p1[1], p1[2]};
+    Point b = {p2[0], p2[1], p2[2]};
+    double r = sep.r(a, b);
+    delete s;
+    return r;
+}
+
+// One adaptive-cubature cell-pair integral (sig.cpp:419-482) with a
+// tabulated xi (kind 0) or a TestModel correlation function (kind 1
+// exponential, 2 gaussian: TestModel.cpp:13-25).
+double ref_signal_pair(int coordsys, double L, const double* c1, const double* c2, int kind, double A, double b,
+                       int n1, int n2, const double* x, const double* y, double epsrel, double epsabs,
+                       double* err) {
+    double grid[6] = {0, 1, -1, 1, 0, 2 * M_PI};
+    int n[3] = {1, 1, 1};
+    Survey* s = make_survey(coordsys, grid, n, L);
+    SeparationFunc sep = s->GetSeparationFunction();
+    XiFunc xi;
+    if (kind == 0)
+        xi = XiFunc(new TableXi(QSpline(n1, n2, x, y)));
+    else {
+        TestModel m(kind == 1 ? 0 : 1, A, b);
+        xi = m.GetXi();
+    }
+    Cell a, bb;
+    to_cell(c1, a);
+    to_cell(c2, bb);
+    double v = (coordsys == CoordSysCartesian) ? ComputeSignalC(a, bb, xi, sep, epsrel, epsabs, err)
+                                               : ComputeSignalS(a, bb, xi, sep, epsrel, epsabs, err);
+    delete s;
+    return v;
+}
+
+// ComputeSignalMatrixBlock (sig.cpp:50-213) over the full grid of cells,
+// cells[i] = {a, d1, d2, d3, bounds..., Veff, Nbar} in the reference layout.
+void ref_signal_block(int coordsys, const double* grid, const int* n, double L, int ncells, const void* cells,
+                      int nrows, const int* rows, int ncols, const int* cols, double* s, int lld, int n1, int n2,
+                      const double* x, const double* y, double epsrel, double epsabs) {
+    Survey* sv = make_survey(coordsys, grid, n, L);
+    XiFunc xi(new TableXi(QSpline(n1, n2, x, y)));
+    std::vector<int> r(rows, rows + nrows), c(cols, cols + ncols);
+    ComputeSignalMatrixBlock(ncells, r, c, s, lld, xi, sv, (const Cell*)cells, epsrel, epsabs);
+    delete sv;
+}
+
+int ref_sizeof_cell() { return (int)sizeof(Cell); }
+
+}  // extern "C"

@@ -1,0 +1,199 @@
+"""The FP64 oracle against the reference's own outputs (golden vectors made by
+tests/golden/make_golden.py from the reference sources) and against the known
+answers of the reference's test suite (code/opsec/tests)."""
+import math
+
+import numpy as np
+import pytest
+
+import oracle as O
+from opsec_gpu import synth
+
+
+def test_xi_tables_match_reference(golden):
+    bands = golden["bands_sel"]
+    T = O.xi_tables(golden["pk_k"], golden["pk_P"], bands, O.LAYOUT_REFERENCE)
+    X, _ = O.r_grid(O.LAYOUT_REFERENCE)
+    np.testing.assert_array_equal(X, golden["xi_r"])
+    ref = golden["xi_tables"]
+    for t in range(ref.shape[0]):
+        assert np.max(np.abs(T[t] - ref[t])) <= 1e-14 * np.max(np.abs(ref[t]))
+
+
+def test_cspline_and_qspline_match_reference(golden):
+    spl = O.CubicSpline(golden["pk_k"], golden["pk_P"])
+    np.testing.assert_array_equal(spl(golden["cspline_k"]), golden["cspline_P"])
+    np.testing.assert_array_equal(O.qspline_eval(golden["xi_tables"][0], golden["qspline_r"]), golden["qspline_xi"])
+
+
+def test_separations_match_reference(golden):
+    L = O.lib()
+    for a, b, ref in zip(golden["sep_box_p1"], golden["sep_box_p2"], golden["sep_box"]):
+        assert L.orc_sep_box(a.copy(), b.copy(), float(golden["sep_box_L"])) == ref
+    # testBoxSurvey.cpp:15-24 known answers
+    assert abs(golden["sep_box"][0] - math.sqrt(3 * 40 * 40)) < 1e-10
+    assert abs(golden["sep_box"][1] - math.sqrt(2 * 40 * 40 + 20 * 20)) < 1e-10
+    for a, b, ref in zip(golden["sep_sph_p1"], golden["sep_sph_p2"], golden["sep_sph"]):
+        assert L.orc_sep_sph(a.copy(), b.copy()) == ref
+
+
+def test_genz_malik_port_matches_reference_cubature(golden):
+    Y = golden["xi_tables"][0]
+    for cs, c1, c2, ref in zip(golden["pair_coordsys"], golden["pair_c1"], golden["pair_c2"], golden["pair_val"]):
+        L = 600.0 if cs == 1 else 0.0
+        v, err, nev = O.gm_pair(int(cs), L, c1, c2, Y)
+        assert abs(v - ref) <= 1e-13 * abs(ref), (cs, v, ref)
+
+
+def test_reference_gaussian_known_answer(golden):
+    """testsig.cpp:41-66.  The reference's adaptive value misses the analytic
+    answer by 6.3e-4 (the test's own bound, 5 epsrel = 5e-5, fails); the port
+    reproduces the reference value."""
+    L, A, b = float(golden["gauss_box_L"]), float(golden["gauss_box_A"]), float(golden["gauss_box_b"])
+    exact = math.erf(L / (2 * math.sqrt(2) * (1 / math.sqrt(2)))) ** 3 / L ** 3
+    ref = float(golden["gauss_box_Q"])
+    assert abs(ref - exact) / exact < 1e-3
+    c = np.array([0, L, 0, L, 0, L], dtype=np.float64)
+    v, _, _ = O.gm_pair(1, L, c, c, None, kind=2, A=A, b=b, abs_bound=1e-5, rel_bound=1e-12)
+    assert abs(v - ref) <= 1e-12 * ref
+
+
+def test_gauss_rule_known_answers():
+    """Constant xi gives Q = 1 exactly (testsig.cpp:19-39); the periodic
+    Gaussian case converges to erf(L/(2 sqrt2 sigma))^3 / L^3 as the Gauss
+    order grows (tolerances are the observed convergence of the rule)."""
+    c1 = np.array([0.0, 1.0, 0.0, 1.0, 0.0, 1.0])
+    c2 = np.array([1.0, 1.5, 1.0, 1.5, 1.0, 1.5])
+    q = O.q_pairs(1, 1000.0, c1, c2, kinds=[1], A=[1.0], b=[0.0])
+    assert abs(q[0, 0] - 1.0) < 1e-14
+    L = 10.0
+    sigma = 1 / math.sqrt(2)
+    A = (2 * math.pi * sigma ** 2) ** -1.5
+    b = 1 / (2 * sigma ** 2)
+    exact = math.erf(L / (2 * math.sqrt(2) * sigma)) ** 3 / L ** 3
+    c = np.array([0, L, 0, L, 0, L], dtype=np.float64)
+    errs = {}
+    for ng in (4, 8, 12):
+        v = O.q_pairs(1, L, c, c, kinds=[2], A=[A], b=[b], ng=ng)[0, 0]
+        errs[ng] = abs(v - exact) / exact
+    assert errs[8] < errs[4] and errs[12] < errs[8]
+    assert errs[12] < 0.05
+
+
+def _block_from_port(golden, name):
+    cells = golden[f"block_{name}_cells"]
+    sv = synth.Survey(1 if name == "box" else 2, golden[f"block_{name}_bounds"], golden[f"block_{name}_n"],
+                      float(golden[f"block_{name}_L"]))
+    Y = golden["xi_tables"][0]
+    b = O.cell_bounds(cells)
+    n = cells.size
+    S = np.zeros((n, n))
+    # the reference integrates the lower-index cell first (sig.cpp:116-117,199-200)
+    a_idx, b_idx = np.triu_indices(n)
+    vals = O.gm_pairs(sv.coordsys, sv.L, b[a_idx], b[b_idx], Y)
+    S[a_idx, b_idx] = vals
+    S[b_idx, a_idx] = vals
+    return sv, cells, S
+
+
+@pytest.mark.parametrize("name", ["box", "sph"])
+def test_signal_block_matches_reference(golden, name):
+    """Full blocks through the port, normalised by sqrt(Nbar_a Nbar_b): equal to
+    the reference's cached block (sig.cpp:82-213) to rounding, which pins the
+    symmetry keys -- the reference reuses one integral per key."""
+    sv, cells, Q = _block_from_port(golden, name)
+    nb = np.sqrt(cells["Nbar"])
+    S = nb[:, None] * Q * nb[None, :]
+    ref = golden[f"block_{name}_S"]
+    scale = np.max(np.abs(ref))
+    # per-pair integrals vs one cached integral per key differ by the
+    # adaptive rule's own error (abs bound 1e-5 on Q)
+    assert np.max(np.abs(S - ref)) <= 2e-5 * np.max(nb) ** 2 + 1e-12 * scale
+    # exact check of the key structure: entries sharing a key are identical in the reference
+    idx = O.key_index(sv, cells)
+    for k in np.unique(idx)[:50]:
+        m = idx == k
+        vals = (ref / (nb[:, None] * nb[None, :]))[m]
+        assert np.max(np.abs(vals - vals[0])) <= 1e-12 * max(abs(vals[0]), 1e-300)
+
+
+def test_key_folding_and_symmetry():
+    sv, cells = synth.shell_survey(2, 3, 6)
+    Y = O.xi_tables(*synth.pk_table(), synth.band_edges(1, 0.0, 0.1), O.LAYOUT_REFERENCE)
+    kf = O.keys_all(sv, fold=True)
+    ku = O.keys_all(sv, fold=False)
+    Qf = O.qtable_keys(sv, kf, Y)
+    Qu = O.qtable_keys(sv, ku, Y)
+    Sf = O.signal_matrix(sv, cells, Qf[:, 0], fold=True)
+    Su = O.signal_matrix(sv, cells, Qu[:, 0], fold=False)
+    assert np.max(np.abs(Sf - Su)) <= 1e-12 * np.max(np.abs(Su))
+    assert np.array_equal(Su, Su.T)
+
+
+def test_matrix_known_answers():
+    """testMyMatrix.cpp:67-104: inverse and sqrtm known values."""
+    A = np.array([[1, 1, 2], [2, 4, -3], [3, 6, -5]], dtype=np.float64)
+    Binv = np.array([[2, -17, 11], [-1, 11, -7], [0, 3, -2]], dtype=np.float64)
+    np.testing.assert_allclose(np.linalg.inv(A), Binv, atol=1e-10)
+    X = np.array([[5, -4, 1, 0, 0], [-4, 6, -4, 1, 0], [1, -4, 6, -4, 1], [0, 1, -4, 6, -4], [0, 0, 1, -4, 5]],
+                 dtype=np.float64)
+    w, V = np.linalg.eigh(X)
+    Y = (V * np.sqrt(w)) @ V.T
+    T = 2 * np.eye(5) - np.eye(5, k=1) - np.eye(5, k=-1)
+    np.testing.assert_allclose(Y, T, atol=1e-10)
+
+
+def test_packed_index_order():
+    """k = j(j+1)/2 + i, i <= j: the order comma writes (comma-scalapack.cpp:257-265)
+    and PackedMatrixIndex::update walks (MyMatrix.hpp:46-65)."""
+    i, j = O.packed_ij(5)
+    walk = []
+    ii = jj = 0
+    for _ in range(15):
+        walk.append((ii, jj))
+        ii += 1
+        if ii > jj:
+            jj += 1
+            ii = 0
+    assert list(zip(i, j)) == walk
+
+
+def test_fisher_identities():
+    rng = np.random.default_rng(0)
+    M, nb = 30, 4
+    evals = np.sort(rng.uniform(0.1, 5.0, M))[::-1]
+    Dfull = [(lambda A: A + A.T)(rng.standard_normal((M, M))) for _ in range(nb)]
+    Dp = np.stack([O.pack_upper(D) for D in Dfull])
+    y = rng.standard_normal(M)
+    prior = rng.uniform(0.5, 2.0, nb)
+    F, f, q = O.fisher(evals, Dp, y, prior)
+    Ci = np.diag(1 / (1 + evals))
+    Cm = np.diag(1 + evals)
+    for p in range(nb):
+        for r in range(nb):
+            assert abs(F[p, r] - 0.5 * np.trace(Ci @ Dfull[p] @ Ci @ Dfull[r])) < 1e-10 * abs(F[p, r]) + 1e-12
+        Rm = Cm - sum(prior[n] * Dfull[n] for n in range(nb))
+        assert abs(f[p] - 0.5 * np.trace(Ci @ Dfull[p] @ Ci @ Rm)) < 1e-10 * (abs(f[p]) + 1)
+        assert abs(q[p] - 0.5 * y @ Ci @ Dfull[p] @ Ci @ y) < 1e-10 * (abs(q[p]) + 1)
+    # f_p = 1/2 sum_i w_i D_p,ii - sum_n F_pn p_n
+    w = 1 / (1 + evals)
+    diag = np.stack([np.diag(D) for D in Dfull])
+    np.testing.assert_allclose(f, 0.5 * diag @ w - F @ prior, rtol=1e-10, atol=1e-10)
+
+
+@pytest.mark.parametrize("mixing", ["inverse", "inverse-sqrt", "identity"])
+def test_epilogue_storage_order(mixing):
+    """The as-executed epilogue equals the textbook one transposed where
+    estimate-mpi's multiply() reads the wrong storage flag; for the default
+    mixing (inverse) both agree to rounding."""
+    rng = np.random.default_rng(1)
+    A = rng.standard_normal((6, 6))
+    F = A @ A.T + 6 * np.eye(6)
+    q, f = rng.standard_normal(6), rng.standard_normal(6)
+    e = O.estimate_epilogue(F, q, f, mixing)
+    m = O.estimate_epilogue_math(F, q, f, mixing)
+    np.testing.assert_allclose(e["phat"], m["phat"], rtol=1e-12, atol=1e-12)
+    np.testing.assert_allclose(e["W"], m["W"].T, rtol=1e-12, atol=1e-12)
+    if mixing == "inverse":
+        np.testing.assert_allclose(e["pcov"], m["pcov"], rtol=1e-10, atol=1e-12)
+    np.testing.assert_allclose(e["pcov"], e["M"].T @ e["M"] @ F, rtol=1e-12)
