@@ -1,0 +1,131 @@
+/* opsec_gpu.h -- C ABI of the GB300 Fisher-build engine.
+ *
+ * One context = one GPU (the current CUDA device at opsec_gpu_create), one
+ * stream, device memory owned by the context.  Every entry point returns
+ * OPSEC_OK (0) or a negative OPSEC_ERR_* code; opsec_gpu_last_error() gives
+ * the message.  Calls are synchronous on return and not thread-safe on one
+ * context.  All host arrays are owned by the caller; all outputs are double.
+ *
+ * Each entry point names the reference interface it replaces (paths inside
+ * jwgcarlson/OPSEC, code/opsec/src/).
+ */
+#ifndef OPSEC_GPU_H
+#define OPSEC_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define OPSEC_OK 0
+#define OPSEC_ERR_CONFIG (-1)  /* missing or invalid configuration option   */
+#define OPSEC_ERR_ARG (-2)     /* invalid argument (size, pointer, index)    */
+#define OPSEC_ERR_CUDA (-3)    /* CUDA runtime or library failure            */
+#define OPSEC_ERR_NOMEM (-4)   /* device or host allocation failed           */
+#define OPSEC_ERR_FILE (-5)    /* file missing, unreadable or malformed      */
+#define OPSEC_ERR_NUMERIC (-6) /* non-finite input, eigensolver failure, singular Fisher matrix */
+#define OPSEC_ERR_STATE (-7)   /* call made before its inputs exist          */
+
+/* Mixing matrix choices of estimate-mpi.cpp:33-37. */
+#define OPSEC_MIXING_INVERSE 0
+#define OPSEC_MIXING_INVERSE_SQRT 1
+#define OPSEC_MIXING_IDENTITY 2
+
+/* A basis cell, byte-for-byte the reference's Cell ("4i8d", Cell.h:74-99). */
+typedef struct opsec_cell {
+    int a;          /* index within the list of cells   */
+    int d1, d2, d3; /* grid index (x,y,z) or (r,mu,phi)  */
+    double min1, max1, min2, max2, min3, max3;
+    double Veff;
+    double Nbar;
+} opsec_cell;
+
+typedef struct opsec_gpu opsec_gpu;
+
+/* Parse key=value configuration text (the syntax of cfg.c:238-295; '#'
+ * comments, optional quotes) and set up model and survey.  Replaces
+ * opsec_init (opsec.c:19-56), InitializeModel (Model.cpp:26-51) and
+ * InitializeSurvey (Survey.cpp:140-165).  Recognised keys: coordsys,
+ * survey.type, survey.{XMin..ZMax,Nx,Ny,Nz,L} or survey.{RMin..PhiMax,
+ * MuMuin,Nr,Nmu,Nphi}, model=RealModel, RealModel.pkfile,
+ * RealModel.{Nbands,kmin,kmax} or RealModel.bands, Nmodes, mixing; and the
+ * engine's own xi.{n1,n2,r1,r2} (xi-table layout, default 512,256,200,20000
+ * as RealModel.cpp:99-102) and sig.gauss (Gauss points per cell axis, 1-6,
+ * default 4). */
+int opsec_gpu_create(opsec_gpu** ctx, const char* cfg_text);
+
+/* Supply P(k) as arrays instead of RealModel.pkfile (RealModel.cpp:33-40:
+ * CubicSpline(pkfile)). */
+int opsec_gpu_set_pk(opsec_gpu* ctx, int n, const double* k, const double* P);
+
+/* Model::NumParams and Model::GetParam for every band (RealModel.cpp:81-96). */
+int opsec_gpu_num_params(opsec_gpu* ctx, int* nparams);
+int opsec_gpu_get_params(opsec_gpu* ctx, double* params);
+
+/* xi tables of RealModel::GetXi / GetXiDeriv (RealModel.cpp:98-127): row 0
+ * is xi(r), row 1+p the derivative for band p, each xi_n1+xi_n2 values on the
+ * r grid of QSpline::MakeArray (QSpline.cpp:6-17).  r_out (n) and xi_out
+ * ((1+Nbands) x n) may be NULL. */
+int opsec_gpu_xi_tables(opsec_gpu* ctx, int* n, double* r_out, double* xi_out);
+
+/* Replace one xi table by caller values on the same r grid (n = xi.n1 +
+ * xi.n2): the plug-in point of a custom correlation function, as an
+ * XiFuncImpl subclass is in the reference (XiFunc.h:36-44).  table 0 is xi,
+ * 1+p the derivative for band p.  Replaced tables persist until the next
+ * opsec_gpu_set_pk. */
+int opsec_gpu_set_xi_table(opsec_gpu* ctx, int table, int n, const double* values);
+
+/* A block of the signal matrix, S_ab = sqrt(Nbar_a Nbar_b) Q_ab, written
+ * row-major s[i*lld + j] for i < nrows, j < ncols (lld <= 0: lld = ncols).
+ * table = 0 for xi (klt), 1+p for the derivative with respect to band p
+ * (comma).  Replaces ComputeSignalMatrixBlock (sig.cpp:50-70). */
+int opsec_gpu_signal_block(opsec_gpu* ctx, int ncells, const opsec_cell* cells, int nrows, const int* rows,
+                           int ncols, const int* cols, double* s, int lld, int table);
+
+/* Top-nmodes eigenpairs of the signal matrix, eigenvalues descending, modes
+ * written mode-major (modes[i*ncells + a]).  *nconv = number of converged
+ * modes.  Replaces klt's solve and write loop (klt.cpp:173-248). */
+int opsec_gpu_klt(opsec_gpu* ctx, int ncells, const opsec_cell* cells, int nmodes, double* evals, double* modes,
+                  int* nconv);
+
+/* Packed derivative matrices C_p = B^T S_p B for every band, band after
+ * band, each the upper triangle column by column (nmodes(nmodes+1)/2
+ * values).  modes as written by opsec_gpu_klt.  Replaces the band loop of
+ * comma (comma-scalapack.cpp:228-265). */
+int opsec_gpu_comma(opsec_gpu* ctx, int ncells, const opsec_cell* cells, int nmodes, const double* modes,
+                    double* cov_packed);
+
+/* Pixel values y_i = sum_a B_ia (N_a - Nbar_a)/sqrt(Nbar_a) from weighted
+ * counts per cell.  Replaces dot.cpp:131-152. */
+int opsec_gpu_dot(opsec_gpu* ctx, int ncells, const opsec_cell* cells, const double* counts, int nmodes,
+                  const double* modes, double* y);
+
+/* Fisher matrix, bias, quadratic estimates and the estfile records of
+ * estimate (estimate-mpi.cpp:480-641, one-rank semantics).  Outputs (any may
+ * be NULL): phat (Nb), pcov, F, W, M (Nb x Nb, row-major), q (Nb; written as
+ * q - f as the reference does), f (Nb). */
+int opsec_gpu_estimate(opsec_gpu* ctx, int nmodes, const double* evals, const double* cov_packed, const double* y,
+                       int mixing, double* phat, double* pcov, double* F, double* W, double* M, double* q,
+                       double* f);
+
+/* The whole path with every intermediate resident on the GPU: cells and
+ * counts in, KL eigenvalues and estfile records out (klt -> comma -> dot ->
+ * estimate).  evals (nmodes) and any output may be NULL. */
+int opsec_gpu_fisher_build(opsec_gpu* ctx, int ncells, const opsec_cell* cells, const double* counts, int nmodes,
+                           int mixing, double* evals, double* phat, double* pcov, double* F, double* W, double* M,
+                           double* q, double* f);
+
+/* Milliseconds spent in each stage of the last opsec_gpu_fisher_build
+ * (CUDA events): xi tables, cubature, eigensolve, projection, Fisher.
+ * times must hold 5 values. */
+int opsec_gpu_stage_times(const opsec_gpu* ctx, double* times);
+
+/* Number of kernels this context has launched since creation. */
+long long opsec_gpu_launch_count(const opsec_gpu* ctx);
+
+const char* opsec_gpu_last_error(const opsec_gpu* ctx);
+void opsec_gpu_destroy(opsec_gpu* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* OPSEC_GPU_H */

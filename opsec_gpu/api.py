@@ -1,0 +1,236 @@
+"""Python binding of the C ABI (include/opsec_gpu.h) over ctypes.
+
+The names follow the reference programs and routines they replace:
+``klt`` (code/opsec/src/klt.cpp), ``comma`` (comma-scalapack.cpp), ``dot``
+(dot.cpp), ``estimate`` (estimate-mpi.cpp) and ``signal_block``
+(ComputeSignalMatrixBlock, sig.cpp:50-70).  Errors raise OpsecError with the
+library's status code; there is no CPU fallback -- a missing library raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from .synth import CELL_DTYPE
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libopsec_gpu.so")
+
+OK = 0
+ERR = {-1: "CONFIG", -2: "ARG", -3: "CUDA", -4: "NOMEM", -5: "FILE", -6: "NUMERIC", -7: "STATE"}
+MIXING = {"inverse": 0, "inverse-sqrt": 1, "identity": 2}
+STAGES = ("xi_tables", "cubature", "eigensolve", "projection", "fisher")
+
+_lib = None
+
+
+class OpsecError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"OPSEC_ERR_{ERR.get(code, code)}: {msg}")
+        self.code = code
+
+
+def load():
+    """Load libopsec_gpu.so; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: build it with `python -m opsec_gpu.build`")
+    L = C.CDLL(LIB_PATH)
+    vp, ip, dp = C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double)
+    L.opsec_gpu_create.argtypes = [C.POINTER(vp), C.c_char_p]
+    L.opsec_gpu_set_pk.argtypes = [vp, C.c_int, dp, dp]
+    L.opsec_gpu_set_xi_table.argtypes = [vp, C.c_int, C.c_int, dp]
+    L.opsec_gpu_num_params.argtypes = [vp, ip]
+    L.opsec_gpu_get_params.argtypes = [vp, dp]
+    L.opsec_gpu_xi_tables.argtypes = [vp, ip, dp, dp]
+    L.opsec_gpu_signal_block.argtypes = [vp, C.c_int, vp, C.c_int, ip, C.c_int, ip, dp, C.c_int, C.c_int]
+    L.opsec_gpu_klt.argtypes = [vp, C.c_int, vp, C.c_int, dp, dp, ip]
+    L.opsec_gpu_comma.argtypes = [vp, C.c_int, vp, C.c_int, dp, dp]
+    L.opsec_gpu_dot.argtypes = [vp, C.c_int, vp, dp, C.c_int, dp, dp]
+    L.opsec_gpu_estimate.argtypes = [vp, C.c_int, dp, dp, dp, C.c_int] + [dp] * 7
+    L.opsec_gpu_fisher_build.argtypes = [vp, C.c_int, vp, dp, C.c_int, C.c_int] + [dp] * 8
+    L.opsec_gpu_stage_times.argtypes = [vp, dp]
+    L.opsec_gpu_launch_count.argtypes = [vp]
+    L.opsec_gpu_launch_count.restype = C.c_longlong
+    L.opsec_gpu_last_error.argtypes = [vp]
+    L.opsec_gpu_last_error.restype = C.c_char_p
+    L.opsec_gpu_destroy.argtypes = [vp]
+    _lib = L
+    return L
+
+
+def _d(a):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _i(a):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _cells(cells):
+    c = np.ascontiguousarray(cells)
+    if c.dtype != CELL_DTYPE:
+        raise TypeError("cells must use opsec_gpu.synth.CELL_DTYPE (the reference Cell layout)")
+    return c
+
+
+def make_config(survey, bands=None, nbands=None, kmin=None, kmax=None, nmodes=None, pkfile=None, layout=None,
+                gauss=None, mixing=None, extra=()):
+    """key = value text in the reference's configuration vocabulary."""
+    lines = list(survey.config_lines())
+    lines.append("model = RealModel")
+    if pkfile:
+        lines.append(f"RealModel.pkfile = {pkfile}")
+    if bands is not None:
+        lines.append("RealModel.bands = " + " ".join(f"{lo!r} {hi!r}" for lo, hi in bands))
+    else:
+        lines += [f"RealModel.Nbands = {nbands}", f"RealModel.kmin = {kmin!r}", f"RealModel.kmax = {kmax!r}"]
+    if nmodes is not None:
+        lines.append(f"Nmodes = {nmodes}")
+    if layout is not None:
+        n1, n2, r1, r2 = layout
+        lines += [f"xi.n1 = {n1}", f"xi.n2 = {n2}", f"xi.r1 = {r1!r}", f"xi.r2 = {r2!r}"]
+    if gauss is not None:
+        lines.append(f"sig.gauss = {gauss}")
+    if mixing is not None:
+        lines.append(f"mixing = {mixing}")
+    lines += list(extra)
+    return "\n".join(lines) + "\n"
+
+
+class Engine:
+    """One GPU context (the current CUDA device)."""
+
+    def __init__(self, cfg_text: str):
+        self._L = load()
+        self._h = C.c_void_p()
+        rc = self._L.opsec_gpu_create(C.byref(self._h), cfg_text.encode())
+        if rc != OK:
+            msg = self._L.opsec_gpu_last_error(self._h).decode() if self._h else ""
+            self._L.opsec_gpu_destroy(self._h)
+            self._h = None
+            raise OpsecError(rc, msg)
+
+    def _check(self, rc):
+        if rc != OK:
+            raise OpsecError(rc, self._L.opsec_gpu_last_error(self._h).decode())
+
+    def close(self):
+        if self._h:
+            self._L.opsec_gpu_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- model
+    def set_pk(self, k, P):
+        k, P = _f64(k), _f64(P)
+        self._check(self._L.opsec_gpu_set_pk(self._h, k.size, _d(k), _d(P)))
+
+    def num_params(self):
+        n = C.c_int()
+        self._check(self._L.opsec_gpu_num_params(self._h, C.byref(n)))
+        return n.value
+
+    def get_params(self):
+        p = np.zeros(self.num_params())
+        self._check(self._L.opsec_gpu_get_params(self._h, _d(p)))
+        return p
+
+    def xi_tables(self):
+        n = C.c_int()
+        self._check(self._L.opsec_gpu_xi_tables(self._h, C.byref(n), None, None))
+        r = np.zeros(n.value)
+        xi = np.zeros((1 + self.num_params(), n.value))
+        self._check(self._L.opsec_gpu_xi_tables(self._h, C.byref(n), _d(r), _d(xi)))
+        return r, xi
+
+    def set_xi_table(self, table, values):
+        v = _f64(values)
+        self._check(self._L.opsec_gpu_set_xi_table(self._h, table, v.size, _d(v)))
+
+    # -- the path
+    def signal_block(self, cells, rows=None, cols=None, table=0, lld=0):
+        cells = _cells(cells)
+        rows = np.arange(cells.size, dtype=np.int32) if rows is None else np.ascontiguousarray(rows, dtype=np.int32)
+        cols = np.arange(cells.size, dtype=np.int32) if cols is None else np.ascontiguousarray(cols, dtype=np.int32)
+        ld = lld if lld > 0 else cols.size
+        s = np.zeros((rows.size, ld))
+        self._check(self._L.opsec_gpu_signal_block(self._h, cells.size, cells.ctypes.data, rows.size, _i(rows),
+                                                   cols.size, _i(cols), _d(s), ld, table))
+        return s[:, : cols.size]
+
+    def klt(self, cells, nmodes):
+        cells = _cells(cells)
+        ev = np.zeros(nmodes)
+        modes = np.zeros((nmodes, cells.size))
+        nconv = C.c_int()
+        self._check(self._L.opsec_gpu_klt(self._h, cells.size, cells.ctypes.data, nmodes, _d(ev), _d(modes),
+                                          C.byref(nconv)))
+        return ev, modes
+
+    def comma(self, cells, modes):
+        cells = _cells(cells)
+        modes = _f64(modes)
+        M = modes.shape[0]
+        out = np.zeros((self.num_params(), M * (M + 1) // 2))
+        self._check(self._L.opsec_gpu_comma(self._h, cells.size, cells.ctypes.data, M, _d(modes), _d(out)))
+        return out
+
+    def dot(self, cells, counts, modes):
+        cells = _cells(cells)
+        modes, counts = _f64(modes), _f64(counts)
+        y = np.zeros(modes.shape[0])
+        self._check(self._L.opsec_gpu_dot(self._h, cells.size, cells.ctypes.data, _d(counts), modes.shape[0],
+                                          _d(modes), _d(y)))
+        return y
+
+    def _records(self):
+        nb = self.num_params()
+        return {"phat": np.zeros(nb), "pcov": np.zeros((nb, nb)), "F": np.zeros((nb, nb)), "W": np.zeros((nb, nb)),
+                "M": np.zeros((nb, nb)), "q": np.zeros(nb), "f": np.zeros(nb)}
+
+    def estimate(self, evals, cov, y, mixing="inverse"):
+        evals, cov, y = _f64(evals), _f64(cov), _f64(y)
+        r = self._records()
+        self._check(self._L.opsec_gpu_estimate(self._h, evals.size, _d(evals), _d(cov), _d(y), MIXING[mixing],
+                                               _d(r["phat"]), _d(r["pcov"]), _d(r["F"]), _d(r["W"]), _d(r["M"]),
+                                               _d(r["q"]), _d(r["f"])))
+        return r
+
+    def fisher_build(self, cells, counts, nmodes, mixing="inverse", want_evals=True):
+        cells = _cells(cells)
+        counts = _f64(counts)
+        r = self._records()
+        ev = np.zeros(nmodes) if want_evals else None
+        self._check(self._L.opsec_gpu_fisher_build(self._h, cells.size, cells.ctypes.data, _d(counts), nmodes,
+                                                   MIXING[mixing], _d(ev), _d(r["phat"]), _d(r["pcov"]), _d(r["F"]),
+                                                   _d(r["W"]), _d(r["M"]), _d(r["q"]), _d(r["f"])))
+        r["evals"] = ev
+        return r
+
+    def stage_times(self):
+        t = np.zeros(5)
+        self._check(self._L.opsec_gpu_stage_times(self._h, _d(t)))
+        return dict(zip(STAGES, t))
+
+    def launch_count(self):
+        return int(self._L.opsec_gpu_launch_count(self._h))

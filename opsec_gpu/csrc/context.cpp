@@ -1,0 +1,1090 @@
+// context.cpp -- host side of the engine: configuration, model and survey
+// setup, device-resident pipeline, and the C ABI of include/opsec_gpu.h.
+#include <cuda_runtime.h>
+#include <cusolverDn.h>
+
+#include <algorithm>
+#include <cerrno>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <new>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "engine.h"
+
+namespace opsec {
+
+void launch_project_simt(const ProjectArgs& a, cudaStream_t s, long long* launches);
+bool project_tc_supported(const ProjectArgs& a);
+void launch_project_tc(const ProjectArgs& a, cudaStream_t s, long long* launches);
+size_t project_tc_work_bytes(const ProjectArgs& a);
+void launch_fisher64(const FisherArgs& a, const double* Dp64, cudaStream_t s, long long* launches);
+void launch_reverse_modes(int n, int m, int lda, const double* A, const double* w, double* modes, double* evals,
+                          cudaStream_t s, long long* launches);
+
+[[noreturn]] void fail(int code, const std::string& msg) { throw Error{code, msg}; }
+
+void cuda_check(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) {
+        if (e == cudaErrorMemoryAllocation) fail(OPSEC_ERR_NOMEM, std::string(what) + ": out of device memory");
+        fail(OPSEC_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    }
+}
+
+static void solver_check(cusolverStatus_t st, const char* what) {
+    if (st != CUSOLVER_STATUS_SUCCESS) fail(OPSEC_ERR_CUDA, std::string(what) + ": cuSOLVER status " + std::to_string((int)st));
+}
+
+template <class T>
+void DevBuf<T>::alloc(size_t count) {
+    if (count <= n && p) return;
+    release();
+    if (count == 0) return;
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&p), sizeof(T) * count);
+    if (e != cudaSuccess) {
+        p = nullptr;
+        n = 0;
+        cudaGetLastError();
+        fail(OPSEC_ERR_NOMEM, "cudaMalloc of " + std::to_string(sizeof(T) * count) + " bytes failed");
+    }
+    n = count;
+}
+
+template <class T>
+void DevBuf<T>::release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+}
+
+template struct DevBuf<double>;
+template struct DevBuf<float>;
+template struct DevBuf<int>;
+template struct DevBuf<unsigned char>;
+
+bool Geometry::full_sky() const { return coordsys == 2 && std::fabs(b[5] - b[4] - 2 * M_PI) < 1e-12; }
+
+// ---------------------------------------------------------------- config
+// key = value lines, '#' comments, surrounding quotes stripped (cfg.c:238-295).
+static std::map<std::string, std::string> parse_config(const char* text) {
+    std::map<std::string, std::string> kv;
+    if (!text) return kv;
+    std::istringstream in(text);
+    std::string line;
+    while (std::getline(in, line)) {
+        size_t p = line.find_first_not_of(" \t\r\n");
+        if (p == std::string::npos || line[p] == '#') continue;
+        size_t eq = line.find('=', p);
+        if (eq == std::string::npos || eq == p) fail(OPSEC_ERR_CONFIG, "not a key = value line: '" + line + "'");
+        std::string key = line.substr(p, eq - p);
+        key.erase(key.find_last_not_of(" \t") + 1);
+        std::string val = line.substr(eq + 1);
+        size_t vb = val.find_first_not_of(" \t\r\n");
+        val = (vb == std::string::npos) ? std::string() : val.substr(vb);
+        val.erase(val.find_last_not_of(" \t\r\n") + 1);
+        if (val.size() >= 2 && ((val.front() == '"' && val.back() == '"') || (val.front() == '\'' && val.back() == '\'')))
+            val = val.substr(1, val.size() - 2);
+        kv[key] = val;
+    }
+    return kv;
+}
+
+static double to_double(const std::string& key, const std::string& v) {
+    char* end = nullptr;
+    errno = 0;
+    double d = std::strtod(v.c_str(), &end);
+    if (end == v.c_str() || errno == ERANGE || !std::isfinite(d)) fail(OPSEC_ERR_CONFIG, "option " + key + " = '" + v + "' is not a number");
+    return d;
+}
+
+static int to_int(const std::string& key, const std::string& v) {
+    char* end = nullptr;
+    long x = std::strtol(v.c_str(), &end, 10);
+    if (end == v.c_str() || *end != '\0') fail(OPSEC_ERR_CONFIG, "option " + key + " = '" + v + "' is not an integer");
+    return (int)x;
+}
+
+// ---------------------------------------------------------------- host math
+// fmm cubic spline coefficients (Spline.cpp:258-330).
+static void cspline_coeffs(const std::vector<double>& X, const std::vector<double>& Y, std::vector<double>& b,
+                           std::vector<double>& c, std::vector<double>& d) {
+    const int N = (int)X.size();
+    b.assign(N, 0);
+    c.assign(N, 0);
+    d.assign(N, 0);
+    if (N == 2) {
+        b[0] = b[1] = (Y[1] - Y[0]) / (X[1] - X[0]);
+        return;
+    }
+    d[0] = X[1] - X[0];
+    c[1] = (Y[1] - Y[0]) / d[0];
+    for (int i = 1; i < N - 1; i++) {
+        d[i] = X[i + 1] - X[i];
+        b[i] = 2 * (d[i - 1] + d[i]);
+        c[i + 1] = (Y[i + 1] - Y[i]) / d[i];
+        c[i] = c[i + 1] - c[i];
+    }
+    b[0] = -d[0];
+    b[N - 1] = -d[N - 2];
+    c[0] = 0;
+    c[N - 1] = 0;
+    if (N > 3) {
+        c[0] = c[2] / (X[3] - X[1]) - c[1] / (X[2] - X[0]);
+        c[N - 1] = c[N - 2] / (X[N - 1] - X[N - 3]) - c[N - 3] / (X[N - 2] - X[N - 4]);
+        c[0] = c[0] * d[0] * d[0] / (X[3] - X[0]);
+        c[N - 1] = -c[N - 1] * d[N - 2] * d[N - 2] / (X[N - 1] - X[N - 4]);
+    }
+    for (int i = 1; i < N; i++) {
+        double t = d[i - 1] / b[i - 1];
+        b[i] -= t * d[i - 1];
+        c[i] -= t * c[i - 1];
+    }
+    c[N - 1] = c[N - 1] / b[N - 1];
+    for (int j = 0; j < N - 1; j++) {
+        int i = N - j - 2;
+        c[i] = (c[i] - d[i] * c[i + 1]) / b[i];
+    }
+    b[N - 1] = (Y[N - 1] - Y[N - 2]) / d[N - 2] + d[N - 2] * (c[N - 2] + 2 * c[N - 1]);
+    for (int i = 0; i < N - 1; i++) {
+        b[i] = (Y[i + 1] - Y[i]) / d[i] - d[i] * (c[i + 1] + 2 * c[i]);
+        d[i] = (c[i + 1] - c[i]) / d[i];
+        c[i] = 3 * c[i];
+    }
+    c[N - 1] = 3 * c[N - 1];
+    d[N - 1] = d[N - 2];
+}
+
+static int lookup_index(double x, int N, const double* X) {
+    double I = (N - 1) * (x - X[0]) / (X[N - 1] - X[0]);
+    int i = std::min(std::max((int)I, 0), N - 2);
+    int ilo = 0, ihi = N - 2;
+    while (ilo < ihi) {
+        if (x < X[i]) {
+            ihi = i - 1;
+            i = (ilo + ihi) / 2;
+        } else if (x > X[i + 1]) {
+            ilo = i + 1;
+            i = (ilo + ihi) / 2;
+        } else
+            break;
+    }
+    return i;
+}
+
+// Gauss-Legendre nodes and weights on [0,1] (Newton on the Legendre recurrence).
+static void gauss_legendre01(int n, std::vector<double>& u, std::vector<double>& w) {
+    u.assign(n, 0.5);
+    w.assign(n, 1.0);
+    if (n == 1) return;
+    for (int i = 0; i < (n + 1) / 2; i++) {
+        double x = std::cos(M_PI * (i + 0.75) / (n + 0.5));
+        double p0 = 1, p1 = x, dp = 1;
+        for (int it = 0; it < 100; it++) {
+            p0 = 1;
+            p1 = x;
+            for (int k = 2; k <= n; k++) {
+                double p2 = ((2 * k - 1) * x * p1 - (k - 1) * p0) / k;
+                p0 = p1;
+                p1 = p2;
+            }
+            dp = n * (x * p1 - p0) / (x * x - 1);
+            double dx = p1 / dp;
+            x -= dx;
+            if (std::fabs(dx) <= 1e-15 * std::fabs(x)) break;
+        }
+        p0 = 1;
+        p1 = x;
+        for (int k = 2; k <= n; k++) {
+            double p2 = ((2 * k - 1) * x * p1 - (k - 1) * p0) / k;
+            p0 = p1;
+            p1 = p2;
+        }
+        dp = n * (x * p1 - p0) / (x * x - 1);
+        double wt = 2 / ((1 - x * x) * dp * dp);
+        u[i] = 0.5 * (1 - x);
+        u[n - 1 - i] = 0.5 * (1 + x);
+        w[i] = w[n - 1 - i] = 0.5 * wt;
+    }
+}
+
+}  // namespace opsec
+
+using namespace opsec;
+
+// ---------------------------------------------------------------- context
+struct opsec_gpu {
+    std::string err;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cusolverDnHandle_t solver = nullptr;
+    long long launches = 0;
+    double stage_ms[5] = {0, 0, 0, 0, 0};
+    std::string warning;
+
+    // configuration
+    Geometry geo;
+    XiLayout xl;
+    int ng = 4;
+    int nmodes_cfg = 0;
+    int mixing = OPSEC_MIXING_INVERSE;
+    std::string projection = "auto";
+    std::vector<double> pk_k, pk_P;
+    std::vector<double> band_lo, band_hi;
+
+    // device state
+    bool tables_ok = false, q_ok = false, qsq_ok = false;
+    bool custom_xi = false;  // a table was replaced through opsec_gpu_set_xi_table
+    KeySpace ks;
+    DevBuf<double> xi64, r_grid, scratch, pk_dev;
+    DevBuf<float> xi32;
+    DevBuf<double> Q;      // [ntab][nkeys]
+    DevBuf<float> Qsq;     // [ntab][nsquare]
+    DevBuf<double> nodes;  // node tables for the cubature kernel
+    DevBuf<int> cell_i;    // d1,d2,d3 then h,f,g per cell
+    DevBuf<double> nbar;
+    DevBuf<int> rc;        // rows/cols for signal blocks
+    DevBuf<double> sblock;
+    DevBuf<double> S;      // dense S or azimuthal blocks
+    DevBuf<double> W;      // eigenvalues
+    DevBuf<double> work;   // solver workspace
+    DevBuf<int> info;
+    DevBuf<int> sel;
+    DevBuf<double> evals, modes, Bs, y, counts, prior, fout, partial, est;
+    DevBuf<float> Dp;
+    DevBuf<double> Dp64;
+    DevBuf<unsigned char> pwork;
+    DevBuf<int> status;
+    int ncells_loaded = 0;
+
+    int ntab() const { return 1 + (int)band_lo.size(); }
+};
+
+namespace {
+
+template <class F>
+int guard(opsec_gpu* ctx, F&& f) {
+    if (!ctx) return OPSEC_ERR_ARG;
+    try {
+        ctx->err.clear();
+        if (ctx->device >= 0) OPSEC_CUDA(cudaSetDevice(ctx->device));
+        f();
+        return OPSEC_OK;
+    } catch (const Error& e) {
+        ctx->err = e.msg;
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        ctx->err = "host allocation failed";
+        return OPSEC_ERR_NOMEM;
+    } catch (const std::exception& e) {
+        ctx->err = e.what();
+        return OPSEC_ERR_ARG;
+    }
+}
+
+void load_pkfile(opsec_gpu* c, const std::string& path) {
+    // Spline.cpp:48-90 LoadData: skip blank and '#' lines, columns 1 and 2
+    FILE* fp = std::fopen(path.c_str(), "r");
+    if (!fp) fail(OPSEC_ERR_FILE, "could not read pkfile '" + path + "'");
+    char buf[4096];
+    std::vector<double> k, P;
+    while (std::fgets(buf, sizeof buf, fp)) {
+        if (buf[0] == '\0' || buf[0] == '#' || buf[0] == '\n') continue;
+        char* e1 = nullptr;
+        double a = std::strtod(buf, &e1);
+        char* e2 = nullptr;
+        double b = std::strtod(e1, &e2);
+        if (e1 == buf || e2 == e1) continue;
+        k.push_back(a);
+        P.push_back(b);
+    }
+    std::fclose(fp);
+    if (k.size() < 2) fail(OPSEC_ERR_FILE, "pkfile '" + path + "' holds fewer than two points");
+    c->pk_k = k;
+    c->pk_P = P;
+}
+
+void configure(opsec_gpu* c, const std::map<std::string, std::string>& kv) {
+    auto has = [&](const std::string& k) { return kv.count(k) > 0; };
+    auto get = [&](const std::string& k) -> const std::string& {
+        auto it = kv.find(k);
+        if (it == kv.end()) fail(OPSEC_ERR_CONFIG, "missing configuration option " + k);
+        return it->second;
+    };
+    // survey (Survey.cpp:12-60, InitializeSurvey Survey.cpp:140-165)
+    std::string type = has("survey.type") ? get("survey.type") : "";
+    std::string cs = has("coordsys") ? get("coordsys") : "";
+    if (type == "BoxSurvey" || (type.empty() && cs == "cartesian")) {
+        c->geo.coordsys = 1;
+        const char* names[6] = {"XMin", "XMax", "YMin", "YMax", "ZMin", "ZMax"};
+        const char* ns[3] = {"Nx", "Ny", "Nz"};
+        for (int i = 0; i < 6; i++) c->geo.b[i] = to_double(names[i], get(std::string("survey.") + names[i]));
+        for (int i = 0; i < 3; i++) c->geo.n[i] = to_int(ns[i], get(std::string("survey.") + ns[i]));
+        // BoxSurvey separation is periodic with period L (BoxSurvey.cpp:19-37); L <= 0 = open box
+        c->geo.L = has("survey.L") ? to_double("survey.L", get("survey.L")) : 0.0;
+        if (has("survey.periodic") && get("survey.periodic") == "0") c->geo.L = 0.0;
+    } else if (type == "SphericalSurvey" || (type.empty() && cs == "spherical")) {
+        c->geo.coordsys = 2;
+        c->geo.b[0] = to_double("RMin", get("survey.RMin"));
+        c->geo.b[1] = to_double("RMax", get("survey.RMax"));
+        // Survey.cpp:39 reads MuMin from the key "MuMuin"; it wins when present
+        c->geo.b[2] = has("survey.MuMuin") ? to_double("MuMuin", get("survey.MuMuin"))
+                                           : to_double("MuMin", get("survey.MuMin"));
+        c->geo.b[3] = to_double("MuMax", get("survey.MuMax"));
+        c->geo.b[4] = to_double("PhiMin", get("survey.PhiMin"));
+        c->geo.b[5] = to_double("PhiMax", get("survey.PhiMax"));
+        c->geo.n[0] = to_int("Nr", get("survey.Nr"));
+        c->geo.n[1] = to_int("Nmu", get("survey.Nmu"));
+        c->geo.n[2] = to_int("Nphi", get("survey.Nphi"));
+    } else {
+        fail(OPSEC_ERR_CONFIG, "survey.type must be BoxSurvey or SphericalSurvey (got '" + type + "')");
+    }
+    for (int i = 0; i < 3; i++) {
+        if (c->geo.n[i] <= 0) fail(OPSEC_ERR_CONFIG, "survey grid sizes must be positive");
+        if (!(c->geo.b[2 * i] < c->geo.b[2 * i + 1])) fail(OPSEC_ERR_CONFIG, "survey bounds must satisfy Min < Max");
+    }
+    if (c->geo.coordsys == 2 && (c->geo.b[0] < 0 || c->geo.b[2] < -1 || c->geo.b[3] > 1))
+        fail(OPSEC_ERR_CONFIG, "spherical bounds need RMin >= 0 and -1 <= MuMin < MuMax <= 1");
+
+    // model (Model.cpp:26-51, RealModel.cpp:33-79)
+    if (has("model") && get("model") != "RealModel")
+        fail(OPSEC_ERR_CONFIG, "model must be RealModel (got '" + get("model") + "')");
+    if (has("RealModel.pkfile")) load_pkfile(c, get("RealModel.pkfile"));
+    if (has("RealModel.bands")) {
+        std::istringstream in(get("RealModel.bands"));
+        std::vector<double> v;
+        std::string tok;
+        while (in >> tok) {
+            for (char& ch : tok)
+                if (ch == ',') ch = ' ';
+            std::istringstream t2(tok);
+            double x;
+            while (t2 >> x) v.push_back(x);
+        }
+        if (v.size() % 2) v.pop_back();  // RealModel.cpp:49-52 drops an odd trailing value
+        for (size_t i = 0; i + 1 < v.size(); i += 2) {
+            c->band_lo.push_back(v[i]);
+            c->band_hi.push_back(v[i + 1]);
+        }
+    } else if (has("RealModel.Nbands")) {
+        int nb = to_int("Nbands", get("RealModel.Nbands"));
+        double kmin = to_double("kmin", get("RealModel.kmin"));
+        double kmax = to_double("kmax", get("RealModel.kmax"));
+        if (nb <= 0) fail(OPSEC_ERR_CONFIG, "RealModel.Nbands must be positive");
+        for (int n = 0; n < nb; n++) {
+            c->band_lo.push_back(kmin + n * (kmax - kmin) / nb);
+            c->band_hi.push_back(kmin + (n + 1) * (kmax - kmin) / nb);
+        }
+    } else {
+        fail(OPSEC_ERR_CONFIG, "k-bands not specified (RealModel.bands or RealModel.Nbands,kmin,kmax)");
+    }
+    for (size_t i = 0; i < c->band_lo.size(); i++)
+        if (!(c->band_lo[i] < c->band_hi[i]) || c->band_lo[i] < 0)
+            fail(OPSEC_ERR_CONFIG, "band " + std::to_string(i) + " has kmin >= kmax or kmin < 0");
+
+    if (has("Nmodes")) c->nmodes_cfg = to_int("Nmodes", get("Nmodes"));
+    if (has("mixing")) {
+        const std::string& m = get("mixing");
+        if (m == "inverse") c->mixing = OPSEC_MIXING_INVERSE;
+        else if (m == "inverse-sqrt") c->mixing = OPSEC_MIXING_INVERSE_SQRT;
+        else if (m == "identity") c->mixing = OPSEC_MIXING_IDENTITY;
+        else fail(OPSEC_ERR_CONFIG, "mixing must be inverse, inverse-sqrt or identity");
+    }
+    if (has("xi.n1")) c->xl.n1 = to_int("xi.n1", get("xi.n1"));
+    if (has("xi.n2")) c->xl.n2 = to_int("xi.n2", get("xi.n2"));
+    if (has("xi.r1")) c->xl.r1 = to_double("xi.r1", get("xi.r1"));
+    if (has("xi.r2")) c->xl.r2 = to_double("xi.r2", get("xi.r2"));
+    if (c->xl.n1 < 1 || c->xl.n2 < 2 || !(c->xl.r1 > 0) || !(c->xl.r2 > c->xl.r1))
+        fail(OPSEC_ERR_CONFIG, "xi table layout needs n1 >= 1, n2 >= 2, 0 < r1 < r2");
+    if (has("sig.gauss")) c->ng = to_int("sig.gauss", get("sig.gauss"));
+    if (c->ng < 1 || c->ng > 6) fail(OPSEC_ERR_CONFIG, "sig.gauss must be between 1 and 6");
+    if (has("projection")) c->projection = get("projection");
+}
+
+void sync(opsec_gpu* c) { OPSEC_CUDA(cudaStreamSynchronize(c->stream)); }
+
+// ---------------------------------------------------------------- stages
+void build_tables(opsec_gpu* c) {
+    if (c->tables_ok) return;
+    if (c->pk_k.size() < 2) fail(OPSEC_ERR_STATE, "no P(k): set RealModel.pkfile or call opsec_gpu_set_pk");
+    const int n = c->xl.n(), ntab = c->ntab(), nb = ntab - 1;
+    // r grid exactly as QSpline::MakeArray (QSpline.cpp:6-17)
+    std::vector<double> r(n);
+    for (int i = 0; i < c->xl.n1; i++) r[i] = i * c->xl.r1 / c->xl.n1;
+    for (int j = 0; j < c->xl.n2; j++) r[c->xl.n1 + j] = c->xl.r1 * std::exp(j * std::log(c->xl.r2 / c->xl.r1) / (c->xl.n2 - 1));
+    std::vector<double> b, cc, d;
+    cspline_coeffs(c->pk_k, c->pk_P, b, cc, d);
+    const int npk = (int)c->pk_k.size();
+    std::vector<double> host;
+    host.insert(host.end(), c->pk_k.begin(), c->pk_k.end());
+    host.insert(host.end(), c->pk_P.begin(), c->pk_P.end());
+    host.insert(host.end(), b.begin(), b.end());
+    host.insert(host.end(), cc.begin(), cc.end());
+    host.insert(host.end(), d.begin(), d.end());
+    host.insert(host.end(), c->band_lo.begin(), c->band_lo.end());
+    host.insert(host.end(), c->band_hi.begin(), c->band_hi.end());
+    c->pk_dev.alloc(host.size());
+    OPSEC_CUDA(cudaMemcpyAsync(c->pk_dev.p, host.data(), sizeof(double) * host.size(), cudaMemcpyHostToDevice, c->stream));
+    c->r_grid.alloc(n);
+    OPSEC_CUDA(cudaMemcpyAsync(c->r_grid.p, r.data(), sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+    c->xi64.alloc((size_t)ntab * n);
+    c->xi32.alloc((size_t)ntab * n);
+    c->scratch.alloc((size_t)32769 + (size_t)nb * 8193);
+    XiTableArgs a;
+    a.xl = c->xl;
+    a.nbands = nb;
+    a.pk_x = c->pk_dev.p;
+    a.pk_y = a.pk_x + npk;
+    a.pk_b = a.pk_y + npk;
+    a.pk_c = a.pk_b + npk;
+    a.pk_d = a.pk_c + npk;
+    a.band_lo = a.pk_d + npk;
+    a.band_hi = a.band_lo + nb;
+    a.npk = npk;
+    a.r = c->r_grid.p;
+    a.xi64 = c->xi64.p;
+    a.xi32 = c->xi32.p;
+    a.scratch = c->scratch.p;
+    launch_xi_tables(a, c->stream, &c->launches);
+    sync(c);  // host arrays above go out of scope
+    c->tables_ok = true;
+}
+
+void setup_keys(opsec_gpu* c) {
+    KeySpace& ks = c->ks;
+    ks.coordsys = c->geo.coordsys;
+    ks.N1 = c->geo.n[0];
+    ks.N2 = c->geo.n[1];
+    ks.N3 = c->geo.n[2];
+    if (ks.coordsys == 1) {
+        ks.nkeys = (long long)ks.N1 * ks.N2 * ks.N3;
+        ks.nsquare = ks.nkeys;
+    } else {
+        ks.H = ks.N1 * ks.N2;
+        ks.fold = c->geo.full_sky();
+        ks.nf = ks.fold ? ks.N3 / 2 + 1 : ks.N3;
+        ks.nkeys = (long long)ks.H * (ks.H + 1) / 2 * ks.nf;
+        ks.nsquare = (long long)ks.H * ks.H * ks.nf;
+    }
+}
+
+void build_q(opsec_gpu* c) {
+    if (c->q_ok) return;
+    build_tables(c);
+    setup_keys(c);
+    const int ng = c->ng;
+    std::vector<double> u, w;
+    gauss_legendre01(ng, u, w);
+    const Geometry& g = c->geo;
+    // per-axis node tables, computed with the reference's cell bounds (Survey.cpp:80-97)
+    auto edge_lo = [&](int ax, int dd) { return g.b[2 * ax] + dd * (g.b[2 * ax + 1] - g.b[2 * ax]) / g.n[ax]; };
+    auto edge_hi = [&](int ax, int dd) { return g.b[2 * ax] + (dd + 1) * (g.b[2 * ax + 1] - g.b[2 * ax]) / g.n[ax]; };
+    std::vector<double> w_h(w), n1((size_t)g.n[0] * ng), n2((size_t)g.n[1] * ng), s2((size_t)g.n[1] * ng),
+        n3((size_t)g.n[2] * ng), cp((size_t)g.n[2] * ng), sp((size_t)g.n[2] * ng);
+    for (int ax = 0; ax < 3; ax++)
+        for (int dd = 0; dd < g.n[ax]; dd++) {
+            double lo = edge_lo(ax, dd), hi = edge_hi(ax, dd);
+            for (int i = 0; i < ng; i++) {
+                size_t o = (size_t)dd * ng + i;
+                if (g.coordsys == 1) {
+                    double x = (1 - u[i]) * lo + u[i] * hi;  // sig.cpp:401-406
+                    (ax == 0 ? n1 : ax == 1 ? n2 : n3)[o] = x;
+                } else if (ax == 0) {
+                    n1[o] = std::cbrt((1 - u[i]) * (lo * lo * lo) + u[i] * (hi * hi * hi));  // sig.cpp:453-454
+                } else if (ax == 1) {
+                    double mu = (1 - u[i]) * lo + u[i] * hi;
+                    n2[o] = mu;
+                    s2[o] = std::sqrt(std::fmax(1 - mu * mu, 0.0));
+                } else {
+                    double phi = (1 - u[i]) * lo + u[i] * hi;
+                    n3[o] = phi;
+                    cp[o] = std::cos(phi);
+                    sp[o] = std::sin(phi);
+                }
+            }
+        }
+    std::vector<double> all;
+    size_t off_w = all.size();
+    all.insert(all.end(), w_h.begin(), w_h.end());
+    size_t off1 = all.size();
+    all.insert(all.end(), n1.begin(), n1.end());
+    size_t off2 = all.size();
+    all.insert(all.end(), n2.begin(), n2.end());
+    size_t offs = all.size();
+    all.insert(all.end(), s2.begin(), s2.end());
+    size_t off3 = all.size();
+    all.insert(all.end(), n3.begin(), n3.end());
+    size_t offc = all.size();
+    all.insert(all.end(), cp.begin(), cp.end());
+    size_t offsn = all.size();
+    all.insert(all.end(), sp.begin(), sp.end());
+    c->nodes.alloc(all.size());
+    OPSEC_CUDA(cudaMemcpyAsync(c->nodes.p, all.data(), sizeof(double) * all.size(), cudaMemcpyHostToDevice, c->stream));
+    c->Q.alloc((size_t)c->ntab() * c->ks.nkeys);
+    CubatureArgs a;
+    a.coordsys = g.coordsys;
+    a.L = g.coordsys == 1 ? g.L : 0.0;
+    a.ks = c->ks;
+    a.ng = ng;
+    a.np = ng * ng * ng;
+    a.w = c->nodes.p + off_w;
+    a.node1 = c->nodes.p + off1;
+    a.node2 = c->nodes.p + off2;
+    a.snode2 = c->nodes.p + offs;
+    a.node3 = c->nodes.p + off3;
+    a.cphi = c->nodes.p + offc;
+    a.sphi = c->nodes.p + offsn;
+    a.xl = c->xl;
+    a.ntab = c->ntab();
+    a.tab32 = c->xi32.p;
+    a.Q = c->Q.p;
+    launch_cubature(a, c->stream, &c->launches);
+    sync(c);
+    c->q_ok = true;
+}
+
+void build_qsq(opsec_gpu* c) {
+    if (c->qsq_ok) return;
+    build_q(c);
+    c->Qsq.alloc((size_t)c->ntab() * c->ks.nsquare);
+    launch_expand_q(c->ks, c->ntab(), c->Q.p, c->Qsq.p, c->stream, &c->launches);
+    c->qsq_ok = true;
+}
+
+// Validate cells against the survey grid and upload their indices and Nbar.
+void load_cells(opsec_gpu* c, int ncells, const opsec_cell* cells) {
+    if (ncells <= 0 || !cells) fail(OPSEC_ERR_ARG, "no cells");
+    const Geometry& g = c->geo;
+    std::vector<int> idx((size_t)6 * ncells);
+    std::vector<double> nb(ncells);
+    for (int a = 0; a < ncells; a++) {
+        const opsec_cell& cl = cells[a];
+        if (cl.d1 < 0 || cl.d1 >= g.n[0] || cl.d2 < 0 || cl.d2 >= g.n[1] || cl.d3 < 0 || cl.d3 >= g.n[2])
+            fail(OPSEC_ERR_ARG, "cell " + std::to_string(a) + " has a grid index outside the survey grid");
+        if (!(cl.Nbar > 0) || !std::isfinite(cl.Nbar))
+            fail(OPSEC_ERR_NUMERIC, "cell " + std::to_string(a) + " has Nbar <= 0 or non-finite");
+        const double lo1 = g.b[0] + cl.d1 * (g.b[1] - g.b[0]) / g.n[0];
+        const double lo3 = g.b[4] + cl.d3 * (g.b[5] - g.b[4]) / g.n[2];
+        if (std::fabs(cl.min1 - lo1) > 1e-9 * (std::fabs(lo1) + std::fabs(g.b[1] - g.b[0])) ||
+            std::fabs(cl.min3 - lo3) > 1e-9 * (std::fabs(lo3) + std::fabs(g.b[5] - g.b[4])))
+            fail(OPSEC_ERR_CONFIG, "cell " + std::to_string(a) + " bounds do not match the survey grid");
+        idx[a] = cl.d1;
+        idx[ncells + a] = cl.d2;
+        idx[2 * (size_t)ncells + a] = cl.d3;
+        if (g.coordsys == 2) {
+            idx[3 * (size_t)ncells + a] = cl.d1 * g.n[1] + cl.d2;
+            idx[4 * (size_t)ncells + a] = cl.d3;
+            idx[5 * (size_t)ncells + a] = 0;
+        } else {
+            idx[3 * (size_t)ncells + a] = cl.d1;
+            idx[4 * (size_t)ncells + a] = cl.d2;
+            idx[5 * (size_t)ncells + a] = cl.d3;
+        }
+        nb[a] = cl.Nbar;
+    }
+    c->cell_i.alloc(idx.size());
+    c->nbar.alloc(ncells);
+    OPSEC_CUDA(cudaMemcpyAsync(c->cell_i.p, idx.data(), sizeof(int) * idx.size(), cudaMemcpyHostToDevice, c->stream));
+    OPSEC_CUDA(cudaMemcpyAsync(c->nbar.p, nb.data(), sizeof(double) * ncells, cudaMemcpyHostToDevice, c->stream));
+    sync(c);
+    c->ncells_loaded = ncells;
+}
+
+CellKeyInfo cell_info(opsec_gpu* c) {
+    const size_t n = c->ncells_loaded;
+    return CellKeyInfo{c->cell_i.p, c->cell_i.p + n, c->cell_i.p + 2 * n, c->nbar.p};
+}
+
+// True when S is block-circulant in phi: full-sky spherical grid, every cell
+// present in grid order, Nbar constant along each arc.
+bool azimuthal_ok(opsec_gpu* c, int ncells, const opsec_cell* cells) {
+    const Geometry& g = c->geo;
+    if (g.coordsys != 2 || !g.full_sky()) return false;
+    if ((long long)ncells != (long long)g.n[0] * g.n[1] * g.n[2]) return false;
+    const int Nphi = g.n[2];
+    for (int a = 0; a < ncells; a++) {
+        const opsec_cell& cl = cells[a];
+        if ((cl.d1 * g.n[1] + cl.d2) * Nphi + cl.d3 != a) return false;
+        const double ref = cells[a - cl.d3].Nbar;
+        if (std::fabs(cl.Nbar - ref) > 1e-12 * ref) return false;
+    }
+    return true;
+}
+
+void cusolver_stream(opsec_gpu* c) {
+    if (!c->solver) solver_check(cusolverDnCreate(&c->solver), "cusolverDnCreate");
+    solver_check(cusolverDnSetStream(c->solver, c->stream), "cusolverDnSetStream");
+}
+
+void check_info(opsec_gpu* c, int count) {
+    std::vector<int> h(count);
+    OPSEC_CUDA(cudaMemcpyAsync(h.data(), c->info.p, sizeof(int) * count, cudaMemcpyDeviceToHost, c->stream));
+    sync(c);
+    for (int i = 0; i < count; i++)
+        if (h[i] != 0) fail(OPSEC_ERR_NUMERIC, "eigensolver failed (info " + std::to_string(h[i]) + ")");
+}
+
+// Top-M eigenpairs of S into c->evals / c->modes (mode-major).  Returns nconv.
+int eigensolve(opsec_gpu* c, int ncells, const opsec_cell* cells, int M) {
+    build_q(c);
+    load_cells(c, ncells, cells);
+    if (M <= 0 || M > ncells) fail(OPSEC_ERR_ARG, "Nmodes must be in [1, Ncells]");
+    cusolver_stream(c);
+    c->evals.alloc(M);
+    c->modes.alloc((size_t)M * ncells);
+    c->warning.clear();
+    if (azimuthal_ok(c, ncells, cells)) {
+        const KeySpace& ks = c->ks;
+        const int H = ks.H, Nphi = ks.N3, nm = Nphi / 2 + 1;
+        std::vector<double> nba(H);
+        for (int h = 0; h < H; h++) nba[h] = cells[(size_t)h * Nphi].Nbar;
+        DevBuf<double> d_nba;
+        d_nba.alloc(H);
+        OPSEC_CUDA(cudaMemcpyAsync(d_nba.p, nba.data(), sizeof(double) * H, cudaMemcpyHostToDevice, c->stream));
+        c->S.alloc((size_t)nm * H * H);
+        launch_azimuthal_blocks(ks, c->Q.p, d_nba.p, nm, c->S.p, c->stream, &c->launches);
+        c->W.alloc((size_t)nm * H);
+        c->info.alloc(nm);
+        int lwork = 0;
+        solver_check(cusolverDnDsyevd_bufferSize(c->solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, H, c->S.p,
+                                                 H, c->W.p, &lwork),
+                     "syevd_bufferSize");
+        c->work.alloc((size_t)lwork);
+        for (int m = 0; m < nm; m++)
+            solver_check(cusolverDnDsyevd(c->solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, H,
+                                          c->S.p + (size_t)m * H * H, H, c->W.p + (size_t)m * H, c->work.p, lwork,
+                                          c->info.p + m),
+                         "syevd");
+        check_info(c, nm);
+        std::vector<double> w((size_t)nm * H);
+        OPSEC_CUDA(cudaMemcpyAsync(w.data(), c->W.p, sizeof(double) * w.size(), cudaMemcpyDeviceToHost, c->stream));
+        sync(c);
+        struct Ent {
+            double lam;
+            int m, idx, kind;
+        };
+        std::vector<Ent> ent;
+        ent.reserve((size_t)H * Nphi);
+        for (int m = 0; m < nm; m++)
+            for (int i = 0; i < H; i++) {
+                double lam = w[(size_t)m * H + i];
+                if (m == 0)
+                    ent.push_back({lam, m, i, 0});
+                else if (2 * m == Nphi)
+                    ent.push_back({lam, m, i, 3});
+                else {
+                    ent.push_back({lam, m, i, 1});
+                    ent.push_back({lam, m, i, 2});
+                }
+            }
+        std::stable_sort(ent.begin(), ent.end(), [](const Ent& x, const Ent& y) {
+            if (x.lam != y.lam) return x.lam > y.lam;
+            if (x.m != y.m) return x.m < y.m;
+            if (x.idx != y.idx) return x.idx < y.idx;
+            return x.kind < y.kind;
+        });
+        if (M < (int)ent.size() && ent[M - 1].kind == 1 && ent[M].kind == 2 && ent[M].m == ent[M - 1].m &&
+            ent[M].idx == ent[M - 1].idx)
+            c->warning = "Nmodes splits a degenerate (cos, sin) pair of azimuthal order m=" + std::to_string(ent[M].m);
+        std::vector<int> sel((size_t)3 * M);
+        std::vector<double> ev(M);
+        for (int i = 0; i < M; i++) {
+            sel[i] = ent[i].m;
+            sel[M + i] = ent[i].idx;
+            sel[2 * M + i] = ent[i].kind;
+            ev[i] = ent[i].lam;
+        }
+        c->sel.alloc(sel.size());
+        OPSEC_CUDA(cudaMemcpyAsync(c->sel.p, sel.data(), sizeof(int) * sel.size(), cudaMemcpyHostToDevice, c->stream));
+        OPSEC_CUDA(cudaMemcpyAsync(c->evals.p, ev.data(), sizeof(double) * M, cudaMemcpyHostToDevice, c->stream));
+        launch_assemble_modes(H, Nphi, M, c->sel.p, c->sel.p + M, c->sel.p + 2 * M, c->S.p, c->modes.p, c->stream,
+                              &c->launches);
+        sync(c);
+        return M;
+    }
+    // dense path: S in FP64, top-M by syevdx (klt.cpp:173-248 via PARPACK there)
+    const int N = ncells;
+    c->S.alloc((size_t)N * N);
+    std::vector<int> all(N);
+    for (int i = 0; i < N; i++) all[i] = i;
+    c->rc.alloc(N);
+    OPSEC_CUDA(cudaMemcpyAsync(c->rc.p, all.data(), sizeof(int) * N, cudaMemcpyHostToDevice, c->stream));
+    launch_signal_block(c->ks, cell_info(c), c->Q.p, N, c->rc.p, N, c->rc.p, c->S.p, N, c->stream, &c->launches);
+    c->W.alloc(N);
+    c->info.alloc(1);
+    int lwork = 0, meig = 0;
+    solver_check(cusolverDnDsyevdx_bufferSize(c->solver, CUSOLVER_EIG_MODE_VECTOR, CUSOLVER_EIG_RANGE_I,
+                                              CUBLAS_FILL_MODE_LOWER, N, c->S.p, N, 0.0, 0.0, N - M + 1, N, &meig,
+                                              c->W.p, &lwork),
+                 "syevdx_bufferSize");
+    c->work.alloc((size_t)lwork);
+    solver_check(cusolverDnDsyevdx(c->solver, CUSOLVER_EIG_MODE_VECTOR, CUSOLVER_EIG_RANGE_I, CUBLAS_FILL_MODE_LOWER,
+                                   N, c->S.p, N, 0.0, 0.0, N - M + 1, N, &meig, c->W.p, c->work.p, lwork, c->info.p),
+                 "syevdx");
+    check_info(c, 1);
+    if (meig < M) fail(OPSEC_ERR_NUMERIC, "eigensolver returned fewer modes than requested");
+    launch_reverse_modes(N, M, N, c->S.p, c->W.p, c->modes.p, c->evals.p, c->stream, &c->launches);
+    sync(c);
+    return M;
+}
+
+void project_all(opsec_gpu* c, int ncells, int M) {
+    build_qsq(c);
+    const int nb = c->ntab() - 1;
+    c->Bs.alloc((size_t)M * ncells);
+    launch_scale_modes(ncells, M, c->modes.p, c->nbar.p, c->Bs.p, c->stream, &c->launches);
+    const size_t K = (size_t)M * (M + 1) / 2;
+    c->Dp.alloc(K * nb);
+    ProjectArgs a;
+    a.ks = c->ks;
+    a.ncells = ncells;
+    a.nmodes = M;
+    a.nbands = nb;
+    a.cell_h = c->cell_i.p + 3 * (size_t)ncells;
+    a.cell_f = c->cell_i.p + 4 * (size_t)ncells;
+    a.cell_g = c->cell_i.p + 5 * (size_t)ncells;
+    a.Qsq = c->Qsq.p;
+    a.Bs = c->Bs.p;
+    a.Dp = c->Dp.p;
+    bool tc = (c->projection != "simt") && project_tc_supported(a);
+    if (c->projection == "tc" && !tc) fail(OPSEC_ERR_CONFIG, "projection=tc requested but the shape is not supported");
+    size_t wb = tc ? project_tc_work_bytes(a) : sizeof(float) * (size_t)M * ncells;
+    c->pwork.alloc(wb);
+    a.work = c->pwork.p;
+    a.work_bytes = wb;
+    if (tc)
+        launch_project_tc(a, c->stream, &c->launches);
+    else
+        launch_project_simt(a, c->stream, &c->launches);
+}
+
+std::vector<double> priors(opsec_gpu* c) {
+    // RealModel::GetParam: mean of P(k) on 256 midpoints of the band (RealModel.cpp:85-96)
+    std::vector<double> b, cc, d;
+    cspline_coeffs(c->pk_k, c->pk_P, b, cc, d);
+    const int N = (int)c->pk_k.size();
+    const double* X = c->pk_k.data();
+    std::vector<double> p(c->band_lo.size());
+    for (size_t n = 0; n < p.size(); n++) {
+        double sum = 0;
+        for (int i = 0; i < 256; i++) {
+            double k = c->band_lo[n] + (i + 0.5) * (c->band_hi[n] - c->band_lo[n]) / 256;
+            double v = 0;
+            if (!(k < X[0] || k >= X[N - 1])) {
+                int j = lookup_index(k, N, X);
+                double u = k - X[j];
+                v = c->pk_P[j] + b[j] * u + cc[j] * u * u + d[j] * u * u * u;
+            }
+            sum += v;
+        }
+        p[n] = sum / 256;
+    }
+    return p;
+}
+
+// F, f, q then the epilogue; records copied to the host outputs
+void fisher_and_epilogue(opsec_gpu* c, int M, const float* Dp32, const double* Dp64, int mixing, double* phat,
+                         double* pcov, double* F, double* W, double* Mx, double* q, double* f) {
+    const int nb = c->ntab() - 1;
+    std::vector<double> pr = priors(c);
+    c->prior.alloc(nb);
+    OPSEC_CUDA(cudaMemcpyAsync(c->prior.p, pr.data(), sizeof(double) * nb, cudaMemcpyHostToDevice, c->stream));
+    FisherArgs a;
+    a.nmodes = M;
+    a.nbands = nb;
+    a.Dp = Dp32;
+    a.evals = c->evals.p;
+    a.y = c->y.p;
+    a.prior = c->prior.p;
+    a.nblocks = fisher_blocks(M);
+    const int nout = nb * (nb + 1) / 2 + 2 * nb;
+    c->partial.alloc((size_t)a.nblocks * nout);
+    a.partial = c->partial.p;
+    c->fout.alloc((size_t)nb * nb + 2 * nb);
+    a.out = c->fout.p;
+    if (Dp64)
+        launch_fisher64(a, Dp64, c->stream, &c->launches);
+    else
+        launch_fisher(a, c->stream, &c->launches);
+    const size_t nrec = (size_t)nb + 4 * (size_t)nb * nb + 2 * nb;
+    c->est.alloc(nrec);
+    c->status.alloc(1);
+    launch_epilogue(nb, mixing, c->fout.p, c->est.p, c->status.p, c->stream, &c->launches);
+    std::vector<double> h(nrec);
+    int st = 0;
+    OPSEC_CUDA(cudaMemcpyAsync(h.data(), c->est.p, sizeof(double) * nrec, cudaMemcpyDeviceToHost, c->stream));
+    OPSEC_CUDA(cudaMemcpyAsync(&st, c->status.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    sync(c);
+    if (st != 0) fail(OPSEC_ERR_NUMERIC, "Fisher matrix is singular");
+    const size_t n2 = (size_t)nb * nb;
+    const double* src = h.data();
+    if (phat) std::memcpy(phat, src, sizeof(double) * nb);
+    src += nb;
+    if (pcov) std::memcpy(pcov, src, sizeof(double) * n2);
+    src += n2;
+    if (F) std::memcpy(F, src, sizeof(double) * n2);
+    src += n2;
+    if (W) std::memcpy(W, src, sizeof(double) * n2);
+    src += n2;
+    if (Mx) std::memcpy(Mx, src, sizeof(double) * n2);
+    src += n2;
+    if (q) std::memcpy(q, src, sizeof(double) * nb);
+    src += nb;
+    if (f) std::memcpy(f, src, sizeof(double) * nb);
+}
+
+struct StageTimer {
+    opsec_gpu* c;
+    cudaEvent_t ev[6];
+    int n = 0;
+    explicit StageTimer(opsec_gpu* cc) : c(cc) {
+        for (auto& e : ev) OPSEC_CUDA(cudaEventCreate(&e));
+    }
+    void mark() { OPSEC_CUDA(cudaEventRecord(ev[n++], c->stream)); }
+    void finish() {
+        OPSEC_CUDA(cudaEventSynchronize(ev[n - 1]));
+        for (int i = 0; i + 1 < n && i < 5; i++) {
+            float ms = 0;
+            OPSEC_CUDA(cudaEventElapsedTime(&ms, ev[i], ev[i + 1]));
+            c->stage_ms[i] = ms;
+        }
+    }
+    ~StageTimer() {
+        for (auto& e : ev) cudaEventDestroy(e);
+    }
+};
+
+}  // namespace
+
+// ---------------------------------------------------------------- C ABI
+extern "C" {
+
+int opsec_gpu_create(opsec_gpu** out, const char* cfg_text) {
+    if (!out) return OPSEC_ERR_ARG;
+    *out = nullptr;
+    opsec_gpu* c = new (std::nothrow) opsec_gpu();
+    if (!c) return OPSEC_ERR_NOMEM;
+    c->device = -1;
+    int rc = guard(c, [&] {
+        int dev = 0;
+        OPSEC_CUDA(cudaGetDevice(&dev));
+        c->device = dev;
+        configure(c, parse_config(cfg_text));
+        OPSEC_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    });
+    *out = c;  // returned even on error so that opsec_gpu_last_error can report it
+    return rc;
+}
+
+int opsec_gpu_set_pk(opsec_gpu* c, int n, const double* k, const double* P) {
+    return guard(c, [&] {
+        if (n < 2 || !k || !P) fail(OPSEC_ERR_ARG, "P(k) needs at least two points");
+        for (int i = 0; i < n; i++) {
+            if (!std::isfinite(k[i]) || !std::isfinite(P[i])) fail(OPSEC_ERR_NUMERIC, "P(k) has non-finite values");
+            if (i && !(k[i] > k[i - 1])) fail(OPSEC_ERR_ARG, "P(k) abscissae must increase");
+        }
+        c->pk_k.assign(k, k + n);
+        c->pk_P.assign(P, P + n);
+        c->tables_ok = c->q_ok = c->qsq_ok = false;
+        c->custom_xi = false;
+    });
+}
+
+int opsec_gpu_set_xi_table(opsec_gpu* c, int table, int n, const double* values) {
+    return guard(c, [&] {
+        if (table < 0 || table >= c->ntab()) fail(OPSEC_ERR_ARG, "table index out of range");
+        if (n != c->xl.n() || !values) fail(OPSEC_ERR_ARG, "table length must equal xi.n1 + xi.n2");
+        for (int i = 0; i < n; i++)
+            if (!std::isfinite(values[i])) fail(OPSEC_ERR_NUMERIC, "non-finite xi value");
+        build_tables(c);
+        std::vector<float> v32(values, values + n);
+        OPSEC_CUDA(cudaMemcpyAsync(c->xi64.p + (size_t)table * n, values, sizeof(double) * n, cudaMemcpyHostToDevice,
+                                   c->stream));
+        OPSEC_CUDA(cudaMemcpyAsync(c->xi32.p + (size_t)table * n, v32.data(), sizeof(float) * n, cudaMemcpyHostToDevice,
+                                   c->stream));
+        sync(c);
+        c->custom_xi = true;
+        c->q_ok = c->qsq_ok = false;
+    });
+}
+
+int opsec_gpu_num_params(opsec_gpu* c, int* np) {
+    return guard(c, [&] {
+        if (!np) fail(OPSEC_ERR_ARG, "null output");
+        *np = (int)c->band_lo.size();
+    });
+}
+
+int opsec_gpu_get_params(opsec_gpu* c, double* p) {
+    return guard(c, [&] {
+        if (!p) fail(OPSEC_ERR_ARG, "null output");
+        if (c->pk_k.size() < 2) fail(OPSEC_ERR_STATE, "no P(k)");
+        std::vector<double> v = priors(c);
+        std::memcpy(p, v.data(), sizeof(double) * v.size());
+    });
+}
+
+int opsec_gpu_xi_tables(opsec_gpu* c, int* n, double* r_out, double* xi_out) {
+    return guard(c, [&] {
+        build_tables(c);
+        const int nx = c->xl.n();
+        if (n) *n = nx;
+        if (r_out) OPSEC_CUDA(cudaMemcpyAsync(r_out, c->r_grid.p, sizeof(double) * nx, cudaMemcpyDeviceToHost, c->stream));
+        if (xi_out)
+            OPSEC_CUDA(cudaMemcpyAsync(xi_out, c->xi64.p, sizeof(double) * nx * c->ntab(), cudaMemcpyDeviceToHost,
+                                       c->stream));
+        sync(c);
+    });
+}
+
+int opsec_gpu_signal_block(opsec_gpu* c, int ncells, const opsec_cell* cells, int nrows, const int* rows, int ncols,
+                           const int* cols, double* s, int lld, int table) {
+    return guard(c, [&] {
+        if (nrows < 0 || ncols < 0 || (nrows && !rows) || (ncols && !cols) || (nrows && ncols && !s))
+            fail(OPSEC_ERR_ARG, "invalid block arguments");
+        if (lld <= 0) lld = ncols;
+        if (lld < ncols) fail(OPSEC_ERR_ARG, "lld < ncols");  // sig.cpp:57-61
+        if (table < 0 || table >= c->ntab()) fail(OPSEC_ERR_ARG, "table index out of range");
+        for (int i = 0; i < nrows; i++)
+            if (rows[i] < 0 || rows[i] >= ncells) fail(OPSEC_ERR_ARG, "row index out of range");
+        for (int j = 0; j < ncols; j++)
+            if (cols[j] < 0 || cols[j] >= ncells) fail(OPSEC_ERR_ARG, "column index out of range");
+        if (nrows == 0 || ncols == 0) return;
+        build_q(c);
+        load_cells(c, ncells, cells);
+        c->rc.alloc((size_t)nrows + ncols);
+        OPSEC_CUDA(cudaMemcpyAsync(c->rc.p, rows, sizeof(int) * nrows, cudaMemcpyHostToDevice, c->stream));
+        OPSEC_CUDA(cudaMemcpyAsync(c->rc.p + nrows, cols, sizeof(int) * ncols, cudaMemcpyHostToDevice, c->stream));
+        c->sblock.alloc((size_t)nrows * lld);
+        launch_signal_block(c->ks, cell_info(c), c->Q.p + (size_t)table * c->ks.nkeys, nrows, c->rc.p, ncols,
+                            c->rc.p + nrows, c->sblock.p, lld, c->stream, &c->launches);
+        OPSEC_CUDA(cudaMemcpyAsync(s, c->sblock.p, sizeof(double) * ((size_t)(nrows - 1) * lld + ncols),
+                                   cudaMemcpyDeviceToHost, c->stream));
+        sync(c);
+    });
+}
+
+int opsec_gpu_klt(opsec_gpu* c, int ncells, const opsec_cell* cells, int nmodes, double* evals, double* modes,
+                  int* nconv) {
+    return guard(c, [&] {
+        int n = eigensolve(c, ncells, cells, nmodes);
+        if (evals) OPSEC_CUDA(cudaMemcpyAsync(evals, c->evals.p, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+        if (modes)
+            OPSEC_CUDA(cudaMemcpyAsync(modes, c->modes.p, sizeof(double) * (size_t)n * ncells, cudaMemcpyDeviceToHost,
+                                       c->stream));
+        sync(c);
+        if (nconv) *nconv = n;
+    });
+}
+
+int opsec_gpu_comma(opsec_gpu* c, int ncells, const opsec_cell* cells, int nmodes, const double* modes,
+                    double* cov_packed) {
+    return guard(c, [&] {
+        if (nmodes <= 0 || nmodes > ncells || !modes || !cov_packed) fail(OPSEC_ERR_ARG, "invalid comma arguments");
+        build_qsq(c);
+        load_cells(c, ncells, cells);
+        c->modes.alloc((size_t)nmodes * ncells);
+        OPSEC_CUDA(cudaMemcpyAsync(c->modes.p, modes, sizeof(double) * (size_t)nmodes * ncells, cudaMemcpyHostToDevice,
+                                   c->stream));
+        project_all(c, ncells, nmodes);
+        const size_t K = (size_t)nmodes * (nmodes + 1) / 2, tot = K * (c->ntab() - 1);
+        c->Dp64.alloc(tot);
+        launch_widen(tot, c->Dp.p, c->Dp64.p, c->stream, &c->launches);
+        OPSEC_CUDA(cudaMemcpyAsync(cov_packed, c->Dp64.p, sizeof(double) * tot, cudaMemcpyDeviceToHost, c->stream));
+        sync(c);
+    });
+}
+
+int opsec_gpu_dot(opsec_gpu* c, int ncells, const opsec_cell* cells, const double* counts, int nmodes,
+                  const double* modes, double* y) {
+    return guard(c, [&] {
+        if (nmodes <= 0 || !counts || !modes || !y) fail(OPSEC_ERR_ARG, "invalid dot arguments");
+        load_cells(c, ncells, cells);
+        c->modes.alloc((size_t)nmodes * ncells);
+        c->counts.alloc(ncells);
+        c->y.alloc(nmodes);
+        OPSEC_CUDA(cudaMemcpyAsync(c->modes.p, modes, sizeof(double) * (size_t)nmodes * ncells, cudaMemcpyHostToDevice,
+                                   c->stream));
+        OPSEC_CUDA(cudaMemcpyAsync(c->counts.p, counts, sizeof(double) * ncells, cudaMemcpyHostToDevice, c->stream));
+        launch_dot(ncells, nmodes, c->modes.p, c->counts.p, c->nbar.p, c->y.p, c->stream, &c->launches);
+        OPSEC_CUDA(cudaMemcpyAsync(y, c->y.p, sizeof(double) * nmodes, cudaMemcpyDeviceToHost, c->stream));
+        sync(c);
+    });
+}
+
+int opsec_gpu_estimate(opsec_gpu* c, int nmodes, const double* evals, const double* cov_packed, const double* y,
+                       int mixing, double* phat, double* pcov, double* F, double* W, double* M, double* q, double* f) {
+    return guard(c, [&] {
+        if (nmodes <= 0 || !evals || !cov_packed || !y) fail(OPSEC_ERR_ARG, "invalid estimate arguments");
+        if (mixing < 0 || mixing > 2) fail(OPSEC_ERR_ARG, "invalid mixing");
+        if (c->pk_k.size() < 2) fail(OPSEC_ERR_STATE, "no P(k): the prior band powers need it");
+        const int nb = c->ntab() - 1;
+        const size_t K = (size_t)nmodes * (nmodes + 1) / 2;
+        c->evals.alloc(nmodes);
+        c->y.alloc(nmodes);
+        c->Dp64.alloc(K * nb);
+        OPSEC_CUDA(cudaMemcpyAsync(c->evals.p, evals, sizeof(double) * nmodes, cudaMemcpyHostToDevice, c->stream));
+        OPSEC_CUDA(cudaMemcpyAsync(c->y.p, y, sizeof(double) * nmodes, cudaMemcpyHostToDevice, c->stream));
+        OPSEC_CUDA(cudaMemcpyAsync(c->Dp64.p, cov_packed, sizeof(double) * K * nb, cudaMemcpyHostToDevice, c->stream));
+        fisher_and_epilogue(c, nmodes, nullptr, c->Dp64.p, mixing, phat, pcov, F, W, M, q, f);
+    });
+}
+
+int opsec_gpu_fisher_build(opsec_gpu* c, int ncells, const opsec_cell* cells, const double* counts, int nmodes,
+                           int mixing, double* evals, double* phat, double* pcov, double* F, double* W, double* M,
+                           double* q, double* f) {
+    return guard(c, [&] {
+        if (!counts) fail(OPSEC_ERR_ARG, "null counts");
+        if (mixing < 0 || mixing > 2) fail(OPSEC_ERR_ARG, "invalid mixing");
+        for (int a = 0; a < ncells; a++)
+            if (!std::isfinite(counts[a])) fail(OPSEC_ERR_NUMERIC, "non-finite count");
+        // every stage is recomputed: nothing cached from an earlier call is reused
+        // (tables replaced by the caller are inputs and stay)
+        if (!c->custom_xi) c->tables_ok = false;
+        c->q_ok = c->qsq_ok = false;
+        StageTimer t(c);
+        t.mark();
+        build_tables(c);
+        t.mark();
+        build_q(c);
+        t.mark();
+        int n = eigensolve(c, ncells, cells, nmodes);
+        t.mark();
+        project_all(c, ncells, n);
+        c->counts.alloc(ncells);
+        c->y.alloc(n);
+        OPSEC_CUDA(cudaMemcpyAsync(c->counts.p, counts, sizeof(double) * ncells, cudaMemcpyHostToDevice, c->stream));
+        launch_dot(ncells, n, c->modes.p, c->counts.p, c->nbar.p, c->y.p, c->stream, &c->launches);
+        t.mark();
+        if (evals) OPSEC_CUDA(cudaMemcpyAsync(evals, c->evals.p, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+        fisher_and_epilogue(c, n, c->Dp.p, nullptr, mixing, phat, pcov, F, W, M, q, f);
+        t.mark();
+        t.finish();
+    });
+}
+
+int opsec_gpu_stage_times(const opsec_gpu* c, double* times) {
+    if (!c || !times) return OPSEC_ERR_ARG;
+    for (int i = 0; i < 5; i++) times[i] = c->stage_ms[i];
+    return OPSEC_OK;
+}
+
+long long opsec_gpu_launch_count(const opsec_gpu* c) { return c ? c->launches : 0; }
+
+const char* opsec_gpu_last_error(const opsec_gpu* c) { return c ? c->err.c_str() : "null context"; }
+
+void opsec_gpu_destroy(opsec_gpu* c) {
+    if (!c) return;
+    if (c->device >= 0) cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->solver) cusolverDnDestroy(c->solver);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+}  // extern "C"

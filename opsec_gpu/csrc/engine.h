@@ -1,0 +1,173 @@
+// engine.h -- internal declarations shared by the host code and the kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/opsec_gpu.h"
+
+#ifdef __CUDACC__
+#define OPSEC_HD __host__ __device__
+#else
+#define OPSEC_HD
+#endif
+
+namespace opsec {
+
+// Internal error carrier; the C ABI turns it into a status code + message.
+struct Error {
+    int code;
+    std::string msg;
+};
+
+[[noreturn]] void fail(int code, const std::string& msg);
+void cuda_check(cudaError_t e, const char* what);
+#define OPSEC_CUDA(x) ::opsec::cuda_check((x), #x)
+
+// Survey grid geometry: the fields of the reference Survey (Survey.h:56-72).
+struct Geometry {
+    int coordsys = 0;   // 1 Cartesian, 2 spherical (Cell.h:58-62)
+    double b[6] = {0};  // Min1, Max1, Min2, Max2, Min3, Max3
+    int n[3] = {0};     // N1, N2, N3
+    double L = 0;       // periodic box size; 0 = open box
+    bool full_sky() const;
+};
+
+// r grid of the xi tables: n1 linear points on [0, r1), n2 log points on [r1, r2]
+// (QSpline::MakeArray, QSpline.cpp:6-17).
+struct XiLayout {
+    int n1 = 512, n2 = 256;
+    double r1 = 200, r2 = 20000;
+    OPSEC_HD int n() const { return n1 + n2; }
+};
+
+// Device buffer owned by the context.
+template <class T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    void alloc(size_t count);
+    void release();
+    ~DevBuf() { release(); }
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+};
+
+// Symmetry-key space of the cached cell-pair integrals (sig.cpp:99-119,150-207).
+struct KeySpace {
+    int coordsys = 0;
+    int N1 = 0, N2 = 0, N3 = 0;
+    int H = 0;        // spherical: arcs (Nr*Nmu)
+    int nf = 0;       // spherical: phi offsets kept (Nphi, or Nphi/2+1 folded)
+    bool fold = false;
+    long long nkeys = 0;     // keys integrated by the cubature kernel
+    long long nsquare = 0;   // entries of the expanded table read by the projection
+};
+
+// ------------------------------------------------------------- kernels
+struct CubatureArgs {
+    int coordsys;
+    double L;            // periodic box (Cartesian), 0 = open
+    KeySpace ks;
+    int ng, np;          // Gauss points per axis, per cell (ng^3)
+    const double* w;     // [ng] Gauss weights on [0,1]
+    const double* node1; // [N1][ng]: x (Cartesian) or r (spherical) nodes
+    const double* node2; // [N2][ng]: y or mu nodes
+    const double* snode2;// [N2][ng]: sqrt(1-mu^2) (spherical)
+    const double* node3; // [N3][ng]: z nodes (Cartesian)
+    const double* cphi;  // [N3][ng]: cos(phi) nodes (spherical)
+    const double* sphi;  // [N3][ng]: sin(phi) nodes (spherical)
+    XiLayout xl;
+    int ntab;            // tables in the whole set
+    const float* tab32;  // [ntab][xl.n()]
+    double* Q;           // [ntab][ks.nkeys]
+};
+void launch_cubature(const CubatureArgs& a, cudaStream_t s, long long* launches);
+
+struct XiTableArgs {
+    XiLayout xl;
+    int nbands;
+    const double* band_lo;  // [nbands]
+    const double* band_hi;
+    int npk;
+    const double* pk_x;     // cubic spline of P(k): x, y, b, c, d
+    const double *pk_y, *pk_b, *pk_c, *pk_d;
+    double* r;              // [n] out
+    double* xi64;           // [1+nbands][n] out
+    float* xi32;            // [1+nbands][n] out
+    double* scratch;        // >= (32769 + nbands*8193) doubles of Simpson weights
+};
+void launch_xi_tables(const XiTableArgs& a, cudaStream_t s, long long* launches);
+
+// Expand Q[t][key] into the square table Qsq[t][(ha*H+hb)*nf + df] (spherical)
+// or copy (Cartesian), FP32, for the projection gather.
+void launch_expand_q(const KeySpace& ks, int ntab, const double* Q, float* Qsq, cudaStream_t s, long long* launches);
+
+// S_ab = sqrt(Nbar_a Nbar_b) Q[key(a,b)] for an explicit row/col block (FP64).
+struct CellKeyInfo {
+    const int* d1;
+    const int* d2;
+    const int* d3;
+    const double* nbar;
+};
+void launch_signal_block(const KeySpace& ks, const CellKeyInfo& ci, const double* Qtab, int nrows, const int* rows,
+                         int ncols, const int* cols, double* s, int lld, cudaStream_t st, long long* launches);
+
+// Azimuthal blocks of a full-sky S: Sm[m][ha][hb] = D_ha D_hb sum_df Q(ha,hb,df) cos(2 pi m df/Nphi)
+void launch_azimuthal_blocks(const KeySpace& ks, const double* Qtab, const double* nbar_arc, int nm, double* Sm,
+                             cudaStream_t st, long long* launches);
+// Modes from block eigenvectors: B[mode][h*Nphi + f] = U_m[h][idx] * trig(m f)
+void launch_assemble_modes(int H, int Nphi, int nmodes, const int* sel_m, const int* sel_idx, const int* sel_kind,
+                           const double* U, double* modes, cudaStream_t st, long long* launches);
+
+// Projection C_p = B'^T Q_p B' for all bands; B' = diag(sqrt Nbar) B.
+struct ProjectArgs {
+    KeySpace ks;
+    int ncells, nmodes, nbands;
+    const int* cell_h;     // spherical arc index h of each cell, or Cartesian dx
+    const int* cell_f;     // spherical phi index, or Cartesian dy
+    const int* cell_g;     // Cartesian dz (unused for spherical)
+    const float* Qsq;      // [ntab][nsquare], band p at table 1+p
+    const double* Bs;      // [nmodes][ncells] scaled modes B' (mode-major), FP64
+    float* Dp;             // [nbands][M(M+1)/2] packed output
+    void* work;            // scratch
+    size_t work_bytes;
+};
+size_t project_work_bytes(const ProjectArgs& a);
+void launch_project(const ProjectArgs& a, cudaStream_t s, long long* launches);
+
+// Fisher / bias / quadratic estimates from packed FP32 C_p, FP64 accumulation.
+struct FisherArgs {
+    int nmodes, nbands;
+    const float* Dp;       // [nbands][K]
+    const double* evals;   // [nmodes]
+    const double* y;       // [nmodes]
+    const double* prior;   // [nbands]
+    double* partial;       // [nblocks][nbands*(nbands+2)] scratch
+    int nblocks;
+    double* out;           // [nbands*nbands + 2*nbands]: F, f, q
+};
+int fisher_blocks(int nmodes);
+void launch_fisher(const FisherArgs& a, cudaStream_t s, long long* launches);
+
+// Nb x Nb epilogue: mixing, window, estimates, covariance; status word on error.
+void launch_epilogue(int nb, int mixing, const double* Fqf, double* out, int* status, cudaStream_t s,
+                     long long* launches);
+
+// y_i = sum_a B_ia (N_a - Nbar_a) / sqrt(Nbar_a)
+void launch_dot(int ncells, int nmodes, const double* modes, const double* counts, const double* nbar, double* y,
+                cudaStream_t s, long long* launches);
+
+// B'[i][a] = sqrt(Nbar_a) B[i][a]
+void launch_scale_modes(int ncells, int nmodes, const double* modes, const double* nbar, double* Bs, cudaStream_t s,
+                        long long* launches);
+
+// packed FP32 -> FP64
+void launch_widen(size_t n, const float* in, double* out, cudaStream_t s, long long* launches);
+
+}  // namespace opsec

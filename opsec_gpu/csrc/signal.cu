@@ -1,0 +1,209 @@
+// signal.cu -- signal-matrix assembly from the Q tables, the azimuthal block
+// decomposition of full-sky spherical surveys, and the small FP64 helpers
+// around them (mode scaling, pixel projection).
+#include <cmath>
+
+#include "engine.h"
+
+namespace opsec {
+namespace {
+
+__device__ __forceinline__ long long tri_index(int ha, int hb, int H) {
+    return (long long)ha * H - (long long)ha * (ha - 1) / 2 + (hb - ha);
+}
+
+// Compact key of a cell pair (sig.cpp:99-119 Cartesian, :150-207 spherical).
+__device__ __forceinline__ long long pair_key(const KeySpace& ks, int a1, int a2, int a3, int b1, int b2, int b3) {
+    if (ks.coordsys == 1) {
+        int kx = abs(a1 - b1), ky = abs(a2 - b2), kz = abs(a3 - b3);
+        return ((long long)kx * ks.N2 + ky) * ks.N3 + kz;
+    }
+    int h1 = a1 * ks.N2 + a2, h2 = b1 * ks.N2 + b2;
+    int ha = min(h1, h2), hb = max(h1, h2);
+    int df = abs(a3 - b3);
+    if (ks.fold && df > ks.N3 - df) df = ks.N3 - df;
+    return tri_index(ha, hb, ks.H) * ks.nf + df;
+}
+
+__global__ void expand_q_kernel(KeySpace ks, int ntab, const double* Q, float* Qsq) {
+    const long long total = (long long)ntab * ks.nsquare;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int t = (int)(e / ks.nsquare);
+        const long long s = e % ks.nsquare;
+        long long key;
+        if (ks.coordsys == 1) {
+            key = s;
+        } else {
+            const int df = (int)(s % ks.nf);
+            const long long hh = s / ks.nf;
+            const int h1 = (int)(hh / ks.H), h2 = (int)(hh % ks.H);
+            key = tri_index(min(h1, h2), max(h1, h2), ks.H) * ks.nf + df;
+        }
+        Qsq[e] = (float)Q[(size_t)t * ks.nkeys + key];
+    }
+}
+
+__global__ void signal_block_kernel(KeySpace ks, CellKeyInfo ci, const double* Qtab, int nrows, const int* rows,
+                                    int ncols, const int* cols, double* s, int lld) {
+    const long long total = (long long)nrows * ncols;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(e / ncols), j = (int)(e % ncols);
+        const int a = rows[i], b = cols[j];
+        const long long key = pair_key(ks, ci.d1[a], ci.d2[a], ci.d3[a], ci.d1[b], ci.d2[b], ci.d3[b]);
+        s[(size_t)i * lld + j] = sqrt(ci.nbar[a] * ci.nbar[b]) * Qtab[key];  // sig.cpp:120,203
+    }
+}
+
+// Sm[m][hb*H + ha] (column-major H x H) = sqrt(Nbar_ha Nbar_hb) sum_d Q(ha,hb,|d|) cos(2 pi m d / Nphi)
+__global__ void azimuthal_blocks_kernel(KeySpace ks, const double* Q, const double* nbar_arc, int nm, double* Sm) {
+    const int H = ks.H, Nphi = ks.N3;
+    const long long total = (long long)nm * H * H;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int m = (int)(e / ((long long)H * H));
+        const long long r = e % ((long long)H * H);
+        const int hb = (int)(r / H), ha = (int)(r % H);
+        const int h1 = min(ha, hb), h2 = max(ha, hb);
+        const long long base = tri_index(h1, h2, H) * ks.nf;
+        double acc = 0.0;
+        for (int d = 0; d < Nphi; d++) {
+            int df = d > Nphi - d ? Nphi - d : d;
+            // cos(2 pi m d / Nphi) with the angle reduced exactly on the integer lattice
+            int md = (int)(((long long)m * d) % Nphi);
+            acc += Q[base + df] * cospi(2.0 * md / Nphi);
+        }
+        Sm[e] = sqrt(nbar_arc[ha] * nbar_arc[hb]) * acc;
+    }
+}
+
+// modes[i][h*Nphi + f] = U_m[h][idx] * trig_kind(m f)
+__global__ void assemble_modes_kernel(int H, int Nphi, int nmodes, const int* sel_m, const int* sel_idx,
+                                      const int* sel_kind, const double* U, double* modes) {
+    const long long N = (long long)H * Nphi;
+    const long long total = (long long)nmodes * N;
+    const double c0 = 1.0 / sqrt((double)Nphi), c1 = sqrt(2.0 / Nphi);
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(e / N);
+        const long long a = e % N;
+        const int h = (int)(a / Nphi), f = (int)(a % Nphi);
+        const int m = sel_m[i];
+        const double u = U[(size_t)m * H * H + (size_t)sel_idx[i] * H + h];
+        const int mf = (int)(((long long)m * f) % Nphi);
+        double t;
+        switch (sel_kind[i]) {
+        case 0: t = c0; break;
+        case 1: t = c1 * cospi(2.0 * mf / Nphi); break;
+        case 2: t = c1 * sinpi(2.0 * mf / Nphi); break;
+        default: t = (f & 1) ? -c0 : c0; break;
+        }
+        modes[e] = u * t;
+    }
+}
+
+__global__ void scale_modes_kernel(int ncells, int nmodes, const double* modes, const double* nbar, double* Bs) {
+    const long long total = (long long)ncells * nmodes;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+         e += (long long)gridDim.x * blockDim.x) {
+        Bs[e] = sqrt(nbar[e % ncells]) * modes[e];
+    }
+}
+
+// one warp per mode: y_i = sum_a B_ia (N_a - Nbar_a)/sqrt(Nbar_a)  (dot.cpp:131-152)
+__global__ void dot_kernel(int ncells, int nmodes, const double* modes, const double* counts, const double* nbar,
+                           double* y) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (warp >= nmodes) return;
+    const double* b = modes + (size_t)warp * ncells;
+    double acc = 0.0;
+    for (int a = lane; a < ncells; a += 32) acc += b[a] * ((counts[a] - nbar[a]) / sqrt(nbar[a]));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) y[warp] = acc;
+}
+
+// modes[i][a] = A[(M-1-i)*lda + a], evals[i] = w[M-1-i]: syevdx returns ascending order
+__global__ void reverse_modes_kernel(int n, int m, int lda, const double* A, const double* w, double* modes,
+                                     double* evals) {
+    const long long total = (long long)n * m;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(e / n), a = (int)(e % n);
+        modes[e] = A[(size_t)(m - 1 - i) * lda + a];
+        if (a == 0) evals[i] = w[m - 1 - i];
+    }
+}
+
+__global__ void widen_kernel(size_t n, const float* in, double* out) {
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x)
+        out[e] = (double)in[e];
+}
+
+unsigned grid_for(long long n, int threads = 256) {
+    long long g = (n + threads - 1) / threads;
+    if (g > 152LL * 64) g = 152LL * 64;
+    if (g < 1) g = 1;
+    return (unsigned)g;
+}
+
+}  // namespace
+
+void launch_expand_q(const KeySpace& ks, int ntab, const double* Q, float* Qsq, cudaStream_t s, long long* l) {
+    expand_q_kernel<<<grid_for((long long)ntab * ks.nsquare), 256, 0, s>>>(ks, ntab, Q, Qsq);
+    OPSEC_CUDA(cudaGetLastError());
+    ++*l;
+}
+
+void launch_signal_block(const KeySpace& ks, const CellKeyInfo& ci, const double* Qtab, int nrows, const int* rows,
+                         int ncols, const int* cols, double* s, int lld, cudaStream_t st, long long* l) {
+    signal_block_kernel<<<grid_for((long long)nrows * ncols), 256, 0, st>>>(ks, ci, Qtab, nrows, rows, ncols, cols,
+                                                                           s, lld);
+    OPSEC_CUDA(cudaGetLastError());
+    ++*l;
+}
+
+void launch_azimuthal_blocks(const KeySpace& ks, const double* Q, const double* nbar_arc, int nm, double* Sm,
+                             cudaStream_t st, long long* l) {
+    azimuthal_blocks_kernel<<<grid_for((long long)nm * ks.H * ks.H), 256, 0, st>>>(ks, Q, nbar_arc, nm, Sm);
+    OPSEC_CUDA(cudaGetLastError());
+    ++*l;
+}
+
+void launch_assemble_modes(int H, int Nphi, int nmodes, const int* sel_m, const int* sel_idx, const int* sel_kind,
+                           const double* U, double* modes, cudaStream_t st, long long* l) {
+    assemble_modes_kernel<<<grid_for((long long)nmodes * H * Nphi), 256, 0, st>>>(H, Nphi, nmodes, sel_m, sel_idx,
+                                                                                 sel_kind, U, modes);
+    OPSEC_CUDA(cudaGetLastError());
+    ++*l;
+}
+
+void launch_scale_modes(int ncells, int nmodes, const double* modes, const double* nbar, double* Bs, cudaStream_t s,
+                        long long* l) {
+    scale_modes_kernel<<<grid_for((long long)ncells * nmodes), 256, 0, s>>>(ncells, nmodes, modes, nbar, Bs);
+    OPSEC_CUDA(cudaGetLastError());
+    ++*l;
+}
+
+void launch_dot(int ncells, int nmodes, const double* modes, const double* counts, const double* nbar, double* y,
+                cudaStream_t s, long long* l) {
+    dot_kernel<<<(nmodes * 32 + 255) / 256, 256, 0, s>>>(ncells, nmodes, modes, counts, nbar, y);
+    OPSEC_CUDA(cudaGetLastError());
+    ++*l;
+}
+
+void launch_reverse_modes(int n, int m, int lda, const double* A, const double* w, double* modes, double* evals,
+                          cudaStream_t s, long long* l) {
+    reverse_modes_kernel<<<grid_for((long long)n * m), 256, 0, s>>>(n, m, lda, A, w, modes, evals);
+    OPSEC_CUDA(cudaGetLastError());
+    ++*l;
+}
+
+void launch_widen(size_t n, const float* in, double* out, cudaStream_t s, long long* l) {
+    widen_kernel<<<grid_for((long long)n), 256, 0, s>>>(n, in, out);
+    OPSEC_CUDA(cudaGetLastError());
+    ++*l;
+}
+
+}  // namespace opsec

@@ -1,0 +1,130 @@
+// xi_table.cu -- xi(r) and band-derivative tables on the GPU, FP64.
+//
+// xi_l^m(r) = (1/2pi^2) int dk k^m j_l(kr) P(k) exp(-(k/kdamp)^2) by Simpson's
+// rule, l = 0, m = 2 (Model.cpp:84-123):
+//   table 0   GetXi       Nk = 32768 on [0, 10], P = cubic spline of the pkfile
+//   table 1+p GetXiDeriv  Nk = 8192 on [k_p, k_{p+1}], P = 1 on [k_p, k_{p+1})
+// (RealModel.cpp:98-127).  The spline is zero outside [x0, x_last) and the
+// constant band is zero at k = k_{p+1}, so the last Simpson node of every
+// band table contributes nothing, as in the reference.
+#include <cmath>
+
+#include "engine.h"
+
+namespace opsec {
+namespace {
+
+constexpr int kNkXi = 32768;
+constexpr int kNkBand = 8192;
+constexpr double kTwoPi2 = 2.0 * M_PI * M_PI;
+
+__device__ int lookup_index(double x, int N, const double* X) {
+    // Spline.cpp:13-35: uniform-grid guess, then bisection
+    double I = (N - 1) * (x - X[0]) / (X[N - 1] - X[0]);
+    int i = (int)I;
+    i = i < 0 ? 0 : (i > N - 2 ? N - 2 : i);
+    int ilo = 0, ihi = N - 2;
+    while (ilo < ihi) {
+        if (x < X[i]) {
+            ihi = i - 1;
+            i = (ilo + ihi) / 2;
+        } else if (x > X[i + 1]) {
+            ilo = i + 1;
+            i = (ilo + ihi) / 2;
+        } else
+            break;
+    }
+    return i;
+}
+
+__device__ double spline_eval(int N, const double* X, const double* Y, const double* b, const double* c,
+                              const double* d, double x) {
+    if (x < X[0] || x >= X[N - 1]) return 0.0;  // Spline.cpp:429-434
+    int i = lookup_index(x, N, X);
+    double u = x - X[i];
+    return Y[i] + b[i] * u + c[i] * u * u + d[i] * u * u * u;
+}
+
+__device__ __forceinline__ double sj0(double x) {
+    double x2 = x * x;
+    return (x2 < 1e-4) ? 1 - x2 * (1 / 6. + x2 * (1 / 120. - x2 * (1 / 5040.))) : sin(x) / x;
+}
+
+struct TableSpec {
+    int nk;
+    double kmin, kmax;
+    size_t off;  // offset of its weights in scratch
+};
+
+__device__ TableSpec table_spec(int t, int nbands, const double* lo, const double* hi) {
+    TableSpec s;
+    if (t == 0) {
+        s.nk = kNkXi;
+        s.kmin = 0.0;
+        s.kmax = 10.0;
+        s.off = 0;
+    } else {
+        s.nk = kNkBand;
+        s.kmin = lo[t - 1];
+        s.kmax = hi[t - 1];
+        s.off = (size_t)(kNkXi + 1) + (size_t)(t - 1) * (kNkBand + 1);
+    }
+    return s;
+}
+
+// Simpson weights times the k-dependent factors (Model.cpp:104-112).
+__global__ void simpson_weights_kernel(XiTableArgs a) {
+    const int t = blockIdx.y;
+    TableSpec s = table_spec(t, a.nbands, a.band_lo, a.band_hi);
+    const double dk = (s.kmax - s.kmin) / s.nk;
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j <= s.nk; j += gridDim.x * blockDim.x) {
+        double k = s.kmin + j * dk;
+        double P;
+        if (t == 0)
+            P = spline_eval(a.npk, a.pk_x, a.pk_y, a.pk_b, a.pk_c, a.pk_d, k);
+        else
+            P = (k >= s.kmin && k < s.kmax) ? 1.0 : 0.0;  // ConstantSpline(1, kmin, kmax)
+        double mult = 2 + 2 * (j % 2) - (j == 0) - (j == s.nk);
+        mult *= P * (k * k) * exp(-k * k / (1.0 * 1.0));
+        mult *= (dk / 3) / kTwoPi2;
+        a.scratch[s.off + j] = mult;
+    }
+}
+
+// One warp per (table, r): sum_j mult_j j0(k_j r), FP64.
+__global__ void xi_sum_kernel(XiTableArgs a) {
+    const int n = a.xl.n();
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    const int t = blockIdx.y;
+    if (warp >= n) return;
+    TableSpec s = table_spec(t, a.nbands, a.band_lo, a.band_hi);
+    const double dk = (s.kmax - s.kmin) / s.nk;
+    const double r = a.r[warp];
+    const double* mult = a.scratch + s.off;
+    double acc = 0.0;
+    for (int j = lane; j <= s.nk; j += 32) {
+        double k = s.kmin + j * dk;
+        acc += mult[j] * sj0(k * r);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) {
+        a.xi64[(size_t)t * n + warp] = acc;
+        a.xi32[(size_t)t * n + warp] = (float)acc;
+    }
+}
+
+}  // namespace
+
+void launch_xi_tables(const XiTableArgs& a, cudaStream_t s, long long* launches) {
+    const int ntab = 1 + a.nbands;
+    simpson_weights_kernel<<<dim3(64, ntab), 256, 0, s>>>(a);
+    OPSEC_CUDA(cudaGetLastError());
+    const int n = a.xl.n();
+    xi_sum_kernel<<<dim3((n * 32 + 255) / 256, ntab), 256, 0, s>>>(a);
+    OPSEC_CUDA(cudaGetLastError());
+    *launches += 2;
+}
+
+}  // namespace opsec

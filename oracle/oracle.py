@@ -370,3 +370,21 @@ def fisher_build(survey, cells, counts, pk_k, pk_P, bands, nmodes, layout=LAYOUT
     est = estimate_epilogue(F, q, f, mixing)
     return {"tables": tabs, "keys": keys, "Q": Q, "S": S, "evals": evals, "modes": modes, "cov": Dp, "y": y,
             "prior": prior, "F": F, "f": f, "q": q, "est": est}
+
+
+def gap_nmodes(evals_desc, target, rel_gap=1e-6, span=16):
+    """An Nmodes near target whose cut lies in a spectral gap (degenerate
+    clusters are not split): the smallest M in [target, target+span] with
+    lambda_{M-1} - lambda_M > rel_gap * lambda_0."""
+    lam = np.asarray(evals_desc)
+    for M in range(target, min(target + span, lam.size - 1) + 1):
+        if lam[M - 1] - lam[M] > rel_gap * abs(lam[0]):
+            return M
+    return target
+
+
+def subspace_sin(A, B):
+    """Largest principal-angle sine between the row spaces of A and B
+    (rows orthonormal)."""
+    s = np.linalg.svd(A @ B.T, compute_uv=False)
+    return float(np.sqrt(max(0.0, 1.0 - min(s) ** 2)))

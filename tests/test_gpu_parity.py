@@ -1,0 +1,187 @@
+"""GPU results against the FP64 oracle, through the C ABI.
+
+Tolerances (stated per quantity):
+  xi tables (FP64 Simpson on the GPU)            1e-12 relative to max |xi|
+  signal matrix (FP32 cubature, FP64 totals)      2e-6 relative to max |S|
+  KL eigenvalues                                  1e-6 relative to lambda_0
+  KL modes (cut at a spectral gap)                sin(largest principal angle) <= 1e-4
+  packed C_p (projection)                         1e-5 relative to max |C_p|
+  Fisher matrix and estimates, end to end         1e-6 relative (the plain-form target)
+"""
+import math
+
+import numpy as np
+import pytest
+
+import oracle as O
+from cases import cases
+from opsec_gpu import api, synth
+
+pytestmark = pytest.mark.gpu
+
+PK = synth.pk_table()
+CASES = cases()
+
+
+def engine(sv, nb=3, kmax=0.15, layout=None, nmodes=None, gauss=None, mixing=None):
+    bands = synth.band_edges(nb, 0.0, kmax)
+    e = api.Engine(api.make_config(sv, bands=bands, nmodes=nmodes, layout=layout, gauss=gauss, mixing=mixing))
+    e.set_pk(*PK)
+    return e, bands
+
+
+@pytest.mark.parametrize("layout", [O.LAYOUT_REFERENCE, O.LAYOUT_LOG4096])
+def test_xi_tables(layout):
+    sv, _ = CASES["box4"]
+    e, bands = engine(sv, nb=4, layout=layout)
+    r, xi = e.xi_tables()
+    X, _ = O.r_grid(layout)
+    np.testing.assert_array_equal(r, X)
+    ref = O.xi_tables(*PK, bands, layout)
+    for t in range(ref.shape[0]):
+        assert np.max(np.abs(xi[t] - ref[t])) <= 1e-12 * np.max(np.abs(ref[t]))
+    np.testing.assert_allclose(e.get_params(), O.band_priors(*PK, bands), rtol=1e-14)
+    e.close()
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_signal_matrix(name):
+    sv, cells = CASES[name]
+    e, bands = engine(sv)
+    tabs = O.xi_tables(*PK, bands)
+    Q = O.qtable_keys(sv, O.keys_all(sv), tabs)
+    for t in range(tabs.shape[0]):
+        ref = O.signal_matrix(sv, cells, Q[:, t])
+        got = e.signal_block(cells, table=t)
+        err = np.max(np.abs(got - ref)) / np.max(np.abs(ref))
+        assert err <= 2e-6, (name, t, err)
+    # non-contiguous rows/cols and an lld larger than ncols (sig.h:16-20)
+    rows = np.array([cells.size - 1, 0, 2], dtype=np.int32)
+    cols = np.array([1, cells.size - 2], dtype=np.int32)
+    blk = e.signal_block(cells, rows, cols, table=1, lld=5)
+    ref = O.signal_matrix(sv, cells, Q[:, 1])[np.ix_(rows, cols)]
+    assert np.max(np.abs(blk - ref)) <= 2e-6 * np.max(np.abs(ref))
+    e.close()
+
+
+def test_known_answers_on_gpu():
+    """xi = 1 gives Q = 1 (testsig.cpp:19-39); a tabulated Gaussian xi in a
+    periodic box matches the oracle's Gauss rule on the same table."""
+    sv, cells = CASES["box4"]
+    e, _ = engine(sv, nb=1)
+    n = O.r_grid(O.LAYOUT_REFERENCE)[0].size
+    e.set_xi_table(0, np.ones(n))
+    S = e.signal_block(cells, table=0)
+    ref = np.sqrt(cells["Nbar"][:, None] * cells["Nbar"][None, :])
+    assert np.max(np.abs(S / ref - 1.0)) < 2e-6
+    e.close()
+    # whole-box cell of side L = 10 on a fine table (testsig.cpp:41-66 geometry)
+    L = 10.0
+    sv = synth.Survey(synth.COORD_CARTESIAN, (0, L, 0, L, 0, L), (1, 1, 1), L=L)
+    cell = synth.make_cells(sv, lambda x, y, z: np.ones_like(x), nquad=4)
+    layout = (2000, 64, 20.0, 100.0)
+    e, _ = engine(sv, nb=1, layout=layout, gauss=6)
+    X, _ = O.r_grid(layout)
+    sigma = 1 / math.sqrt(2)
+    A, b = (2 * math.pi * sigma ** 2) ** -1.5, 1 / (2 * sigma ** 2)
+    Y = A * np.exp(-b * X ** 2)
+    e.set_xi_table(0, Y)
+    got = e.signal_block(cell, table=0)[0, 0] / cell["Nbar"][0]
+    ref = O.qtable_keys(sv, np.zeros((1, 3), np.int32), Y[None, :], layout, ng=6)[0, 0]
+    assert abs(got - ref) <= 2e-6 * abs(ref)
+    exact = math.erf(L / (2 * math.sqrt(2) * sigma)) ** 3 / L ** 3
+    assert abs(ref - exact) / exact < 0.05  # the 6-point rule's own error on this integrand
+    e.close()
+
+
+def _oracle_modes(sv, cells, bands, target):
+    tabs = O.xi_tables(*PK, bands)
+    Q = O.qtable_keys(sv, O.keys_all(sv), tabs)
+    S = O.signal_matrix(sv, cells, Q[:, 0])
+    lam = np.sort(np.linalg.eigvalsh(S))[::-1]
+    M = O.gap_nmodes(lam, target)
+    ev, modes = O.klt(S, M)
+    return tabs, Q, M, ev, modes
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_klt(name):
+    sv, cells = CASES[name]
+    e, bands = engine(sv)
+    tabs, Q, M, ev, modes = _oracle_modes(sv, cells, bands, cells.size // 2)
+    gev, gmodes = e.klt(cells, M)
+    assert np.max(np.abs(gev - ev)) <= 1e-6 * ev[0]
+    np.testing.assert_allclose(gmodes @ gmodes.T, np.eye(M), atol=1e-10)
+    assert O.subspace_sin(gmodes, modes) <= 1e-4
+    e.close()
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_comma_and_dot(name):
+    sv, cells = CASES[name]
+    e, bands = engine(sv)
+    tabs, Q, M, ev, modes = _oracle_modes(sv, cells, bands, cells.size // 2)
+    cov = e.comma(cells, modes)
+    for p in range(len(bands)):
+        ref = O.project(modes, O.signal_matrix(sv, cells, Q[:, 1 + p]))
+        assert np.max(np.abs(cov[p] - ref)) <= 1e-5 * np.max(np.abs(ref)), (name, p)
+    counts = synth.grf_counts(sv, cells)
+    y = e.dot(cells, counts, modes)
+    np.testing.assert_allclose(y, O.dot(cells, counts, modes), rtol=1e-12, atol=1e-12 * np.max(np.abs(y)))
+    e.close()
+
+
+@pytest.mark.parametrize("mixing", ["inverse", "inverse-sqrt", "identity"])
+def test_estimate(mixing):
+    rng = np.random.default_rng(7)
+    sv, cells = CASES["sph_full"]
+    e, bands = engine(sv, nb=4)
+    M = 30
+    evals = np.sort(rng.uniform(0.05, 4.0, M))[::-1]
+    Dp = np.stack([O.pack_upper((lambda A: A @ A.T / M)(rng.standard_normal((M, M)))) for _ in bands])
+    y = rng.standard_normal(M)
+    got = e.estimate(evals, Dp, y, mixing)
+    F, f, q = O.fisher(evals, Dp, y, O.band_priors(*PK, bands))
+    ref = O.estimate_epilogue(F, q, f, mixing)
+    for k in ("F", "phat", "pcov", "W", "M", "q", "f"):
+        scale = np.max(np.abs(ref[k]))
+        assert np.max(np.abs(got[k] - ref[k])) <= 1e-6 * scale, (k, mixing)
+    e.close()
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_fisher_build_end_to_end(name):
+    sv, cells = CASES[name]
+    e, bands = engine(sv)
+    tabs, Q, M, ev, modes = _oracle_modes(sv, cells, bands, cells.size // 2)
+    counts = synth.grf_counts(sv, cells)
+    got = e.fisher_build(cells, counts, M)
+    ref = O.fisher_build(sv, cells, counts, *PK, bands, M)
+    assert np.max(np.abs(got["evals"] - ref["evals"])) <= 1e-6 * ref["evals"][0]
+    for k in ("F", "phat", "pcov"):
+        r = ref["est"][k]
+        assert np.max(np.abs(got[k] - r)) <= 1e-6 * np.max(np.abs(r)), (name, k)
+    assert e.launch_count() > 0
+    e.close()
+
+
+def test_errors_are_status_codes():
+    sv, cells = CASES["box4"]
+    with pytest.raises(api.OpsecError) as ei:
+        api.Engine("survey.type = Nope\n")
+    assert ei.value.code == -1
+    e, _ = engine(sv)
+    with pytest.raises(api.OpsecError) as ei:
+        e.klt(cells, cells.size + 1)
+    assert ei.value.code == -2
+    bad = cells.copy()
+    bad["Nbar"][3] = float("nan")
+    with pytest.raises(api.OpsecError) as ei:
+        e.klt(bad, 4)
+    assert ei.value.code == -6
+    counts = np.ones(cells.size)
+    counts[0] = np.inf
+    with pytest.raises(api.OpsecError) as ei:
+        e.fisher_build(cells, counts, 4)
+    assert ei.value.code == -6
+    e.close()
