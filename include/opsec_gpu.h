@@ -119,6 +119,14 @@ int opsec_gpu_fisher_build(opsec_gpu* ctx, int ncells, const opsec_cell* cells, 
  * times must hold 5 values. */
 int opsec_gpu_stage_times(const opsec_gpu* ctx, double* times);
 
+/* Per-kernel CUDA-event timing accumulated since creation when the
+ * configuration sets profile = 1 (events on the launching stream around the
+ * cubature, projection and Fisher kernels).  name: "cubature", "project_step1",
+ * "project_step2", "fisher".  flops / bytes = algorithmic work attributed to
+ * those launches.  No counterpart in the reference, which has no timers. */
+int opsec_gpu_kernel_stats(const opsec_gpu* ctx, const char* name, long long* count, double* total_ms,
+                           double* flops, double* bytes);
+
 /* Number of kernels this context has launched since creation. */
 long long opsec_gpu_launch_count(const opsec_gpu* ctx);
 

@@ -54,6 +54,7 @@ def load():
     L.opsec_gpu_estimate.argtypes = [vp, C.c_int, dp, dp, dp, C.c_int] + [dp] * 7
     L.opsec_gpu_fisher_build.argtypes = [vp, C.c_int, vp, dp, C.c_int, C.c_int] + [dp] * 8
     L.opsec_gpu_stage_times.argtypes = [vp, dp]
+    L.opsec_gpu_kernel_stats.argtypes = [vp, C.c_char_p, C.POINTER(C.c_longlong), dp, dp, dp]
     L.opsec_gpu_launch_count.argtypes = [vp]
     L.opsec_gpu_launch_count.restype = C.c_longlong
     L.opsec_gpu_last_error.argtypes = [vp]
@@ -231,6 +232,12 @@ class Engine:
         t = np.zeros(5)
         self._check(self._L.opsec_gpu_stage_times(self._h, _d(t)))
         return dict(zip(STAGES, t))
+
+    def kernel_stats(self, name):
+        n, ms, fl, by = C.c_longlong(), C.c_double(), C.c_double(), C.c_double()
+        self._check(self._L.opsec_gpu_kernel_stats(self._h, name.encode(), C.byref(n), C.byref(ms), C.byref(fl),
+                                                   C.byref(by)))
+        return {"count": n.value, "ms": ms.value, "flops": fl.value, "bytes": by.value}
 
     def launch_count(self):
         return int(self._L.opsec_gpu_launch_count(self._h))

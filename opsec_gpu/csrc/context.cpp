@@ -30,6 +30,22 @@ void launch_reverse_modes(int n, int m, int lda, const double* A, const double* 
 
 [[noreturn]] void fail(int code, const std::string& msg) { throw Error{code, msg}; }
 
+thread_local KernelClock* g_clock = nullptr;
+
+void KernelClock::begin(const char* name, cudaStream_t s, double flops, double bytes) {
+    if (!on) return;
+    Rec r{name, nullptr, nullptr, flops, bytes};
+    OPSEC_CUDA(cudaEventCreate(&r.a));
+    OPSEC_CUDA(cudaEventCreate(&r.b));
+    OPSEC_CUDA(cudaEventRecord(r.a, s));
+    pending.push_back(r);
+}
+
+void KernelClock::end(cudaStream_t s) {
+    if (!on || pending.empty()) return;
+    OPSEC_CUDA(cudaEventRecord(pending.back().b, s));
+}
+
 void cuda_check(cudaError_t e, const char* what) {
     if (e != cudaSuccess) {
         if (e == cudaErrorMemoryAllocation) fail(OPSEC_ERR_NOMEM, std::string(what) + ": out of device memory");
@@ -262,14 +278,46 @@ struct opsec_gpu {
     DevBuf<int> status;
     int ncells_loaded = 0;
 
+    // per-kernel timing (config key profile = 1)
+    KernelClock clock;
+    struct Stat {
+        long long count = 0;
+        double ms = 0, flops = 0, bytes = 0;
+    };
+    std::map<std::string, Stat> stats;
+
     int ntab() const { return 1 + (int)band_lo.size(); }
 };
 
 namespace {
 
+void collect_clock(opsec_gpu* c) {
+    for (auto& r : c->clock.pending) {
+        float ms = 0;
+        if (cudaEventSynchronize(r.b) == cudaSuccess && cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) {
+            auto& st = c->stats[r.name];
+            st.count++;
+            st.ms += ms;
+            st.flops += r.flops;
+            st.bytes += r.bytes;
+        }
+        cudaEventDestroy(r.a);
+        cudaEventDestroy(r.b);
+    }
+    c->clock.pending.clear();
+}
+
 template <class F>
 int guard(opsec_gpu* ctx, F&& f) {
     if (!ctx) return OPSEC_ERR_ARG;
+    struct ClockScope {
+        opsec_gpu* c;
+        explicit ClockScope(opsec_gpu* cc) : c(cc) { g_clock = &cc->clock; }
+        ~ClockScope() {
+            collect_clock(c);
+            g_clock = nullptr;
+        }
+    } scope(ctx);
     try {
         ctx->err.clear();
         if (ctx->device >= 0) OPSEC_CUDA(cudaSetDevice(ctx->device));
@@ -404,6 +452,7 @@ void configure(opsec_gpu* c, const std::map<std::string, std::string>& kv) {
     if (has("sig.gauss")) c->ng = to_int("sig.gauss", get("sig.gauss"));
     if (c->ng < 1 || c->ng > 6) fail(OPSEC_ERR_CONFIG, "sig.gauss must be between 1 and 6");
     if (has("projection")) c->projection = get("projection");
+    if (has("profile")) c->clock.on = get("profile") == "1";
 }
 
 void sync(opsec_gpu* c) { OPSEC_CUDA(cudaStreamSynchronize(c->stream)); }
@@ -1075,6 +1124,17 @@ int opsec_gpu_stage_times(const opsec_gpu* c, double* times) {
 }
 
 long long opsec_gpu_launch_count(const opsec_gpu* c) { return c ? c->launches : 0; }
+
+int opsec_gpu_kernel_stats(const opsec_gpu* c, const char* name, long long* count, double* total_ms, double* flops,
+                           double* bytes) {
+    if (!c || !name) return OPSEC_ERR_ARG;
+    auto it = c->stats.find(name);
+    if (count) *count = it == c->stats.end() ? 0 : it->second.count;
+    if (total_ms) *total_ms = it == c->stats.end() ? 0 : it->second.ms;
+    if (flops) *flops = it == c->stats.end() ? 0 : it->second.flops;
+    if (bytes) *bytes = it == c->stats.end() ? 0 : it->second.bytes;
+    return OPSEC_OK;
+}
 
 const char* opsec_gpu_last_error(const opsec_gpu* c) { return c ? c->err.c_str() : "null context"; }
 

@@ -167,8 +167,10 @@ void run(const CubatureArgs& a, int tab0, int ngrp, const Lookup& lk, cudaStream
     long long want = (a.ks.nkeys + kWarps - 1) / kWarps;
     long long grid = (long long)nsm * occ;
     if (want < grid) grid = want;
+    if (g_clock) g_clock->begin("cubature", s, (double)a.ks.nkeys * NP * NP * ngrp);
     k<<<(unsigned)grid, kWarps * 32, smem, s>>>(a, tab0, ngrp, lk);
     OPSEC_CUDA(cudaGetLastError());
+    if (g_clock) g_clock->end(s);
 }
 
 template <int NG>

@@ -69,6 +69,21 @@ struct KeySpace {
     long long nsquare = 0;   // entries of the expanded table read by the projection
 };
 
+// Optional per-kernel timing: CUDA events around selected launches on the
+// launching stream, accumulated per kernel name.
+struct KernelClock {
+    bool on = false;
+    struct Rec {
+        const char* name;
+        cudaEvent_t a, b;
+        double flops, bytes;
+    };
+    std::vector<Rec> pending;
+    void begin(const char* name, cudaStream_t s, double flops = 0, double bytes = 0);
+    void end(cudaStream_t s);
+};
+extern thread_local KernelClock* g_clock;  // set by the context around its calls
+
 // ------------------------------------------------------------- kernels
 struct CubatureArgs {
     int coordsys;

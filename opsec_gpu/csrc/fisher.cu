@@ -336,8 +336,11 @@ static void run_fisher(const FisherArgs& a, const T* Dp, cudaStream_t s, long lo
     const size_t smem = sizeof(float) * (size_t)(nb + 2) * kChunk;
     auto k = fisher_kernel<T>;
     OPSEC_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const double K = (double)a.nmodes * (a.nmodes + 1) / 2;
+    if (g_clock) g_clock->begin("fisher", s, 2.0 * K * nout, K * nb * sizeof(T));
     k<<<a.nblocks, kThreads, smem, s>>>(a.nmodes, nb, Dp, a.evals, a.y, a.prior, a.partial);
     OPSEC_CUDA(cudaGetLastError());
+    if (g_clock) g_clock->end(s);
     fisher_reduce_kernel<<<(nout + 255) / 256, 256, 0, s>>>(nb, a.nblocks, a.partial, a.out);
     OPSEC_CUDA(cudaGetLastError());
     *launches += 2;

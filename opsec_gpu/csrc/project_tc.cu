@@ -1,11 +1,620 @@
-// project_tc.cu -- tensor-core form of the fused projection (placeholder until
-// the tcgen05 kernel lands): reports no supported shapes.
+// project_tc.cu -- fused projection C_p = B'^T Q_p B' on the 5th-generation
+// tensor cores (tcgen05 + TMEM + TMA), sm_103a.
+//
+// Per band (comma-scalapack.cpp:228-265; S_p = D Q_p D, B' = D B, D = diag sqrt Nbar):
+//
+//  step 1  T = Q_p B'  (N x N times N x M).  128x256 output tile per CTA,
+//          K = cells in blocks of 64.  The A operand (Q_p tile) is gathered
+//          from the symmetry-key table by eight producer warps straight into
+//          shared memory in the 128B-swizzled K-major layout, split into FP16
+//          hi + lo; S_p is never written to memory.  The B operand (B' hi/lo,
+//          mode-major) arrives by TMA.  One thread issues
+//          tcgen05.mma kind::f16 (M=128, N=256, K=16) three times per K-slice:
+//          Ah*Bh + Ah*Bl + Al*Bh accumulate into one FP32 accumulator in TMEM.
+//          The epilogue reads TMEM (tcgen05.ld) and writes T^T split into FP16
+//          hi/lo.
+//  step 2  C_p = B'^T T, both operands by TMA, only tiles touching the upper
+//          triangle; the epilogue writes the packed triangle (k = j(j+1)/2+i).
+//
+// FP16 operands are scaled by powers of two (exact) so that their largest
+// magnitude sits near 2^14; hi + lo then carry ~22 significant bits.
+// Every mbarrier wait is bounded: on timeout the kernel raises an error flag
+// that the host turns into OPSEC_ERR_CUDA, frees its TMEM and returns.
+#include <cuda.h>
+#include <cuda_fp16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
 #include "engine.h"
 
 namespace opsec {
-bool project_tc_supported(const ProjectArgs&) { return false; }
-size_t project_tc_work_bytes(const ProjectArgs&) { return 0; }
-void launch_project_tc(const ProjectArgs&, cudaStream_t, long long*) {
-    fail(OPSEC_ERR_STATE, "tensor-core projection unavailable");
+namespace {
+
+constexpr int BM = 128, BN = 256, BK = 64;
+constexpr int STAGES = 2;
+constexpr uint32_t A_BYTES = BM * BK * 2;  // one FP16 operand tile, 16 KB
+constexpr uint32_t B_BYTES = BN * BK * 2;  // 32 KB
+constexpr uint32_t STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
+constexpr int TMEM_COLS = 256;
+constexpr long long kWaitCycles = 2000000000LL;  // ~1 s at 2 GHz
+
+// instruction descriptor: D=F32, A=B=F16, both K-major, M=128, N=256
+constexpr uint32_t kIdesc = (1u << 4) | (0u << 7) | (0u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint32_t a, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(count) : "memory");
 }
+__device__ __forceinline__ void mbar_arrive(uint32_t a) {
+    asm volatile("{ .reg .b64 st; mbarrier.arrive.shared::cta.b64 st, [%0]; }" ::"r"(a) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_tx(uint32_t a, uint32_t bytes) {
+    asm volatile("{ .reg .b64 st; mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1; }" ::"r"(a), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint32_t a, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+        : "=r"(ok)
+        : "r"(a), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait.  Returns false (and raises the CTA's abort flag and the
+// global error word) when the barrier does not complete in time.
+__device__ __forceinline__ bool mbar_wait(uint32_t a, uint32_t parity, volatile int* abort_flag, int* err) {
+    if (mbar_try(a, parity)) return true;
+    const long long t0 = clock64();
+    while (true) {
+        if (mbar_try(a, parity)) return true;
+        if (*abort_flag) return false;
+        if (clock64() - t0 > kWaitCycles) {
+            *abort_flag = 1;
+            atomicExch(err, 1);
+            return false;
+        }
+    }
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, uint32_t mbar, int x, int y) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::"r"(
+            dst),
+        "l"((unsigned long long)map), "r"(mbar), "r"(x), "r"(y)
+        : "memory");
+}
+
+// UMMA shared-memory descriptor: K-major, 128-byte swizzle, 8-row atoms of 1024 B
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)1 << 16;            // leading byte offset (unused with this swizzle)
+    d |= (uint64_t)(1024 >> 4) << 32;  // stride byte offset: 8 rows x 128 B
+    d |= (uint64_t)1 << 46;            // descriptor version
+    d |= (uint64_t)2 << 61;            // SWIZZLE_128B
+    return d;
+}
+
+__device__ __forceinline__ void umma(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t accumulate) {
+    asm volatile(
+        "{ .reg .pred p; setp.ne.b32 p, %4, 0; tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p; }" ::"r"(tmem_d),
+        "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate));
+}
+__device__ __forceinline__ void umma_commit(uint32_t mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar) : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_alloc(uint32_t slot) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(slot), "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(TMEM_COLS) : "memory");
+}
+
+// 32 consecutive accumulator columns of this thread's TMEM lane
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,"
+        "%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+          "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void split_half(float x, __half& h, __half& l) {
+    h = __float2half_rn(x);
+    l = __float2half_rn(x - __half2float(h));
+}
+
+// 2^s with m * 2^s in [2^13, 2^14): exact power-of-two scaling into the FP16 range
+__host__ __device__ __forceinline__ float pow2_scale(float m) {
+    if (!(m > 0.f) || !(m < 3.0e38f)) return 1.f;
+    int e;
+    (void)frexpf(m, &e);  // m = f 2^e, f in [0.5, 1)
+    return ldexpf(1.f, 14 - e);
+}
+
+// ---------------------------------------------------------------- step 1
+struct Step1Params {
+    KeySpace ks;
+    int N, Npad, Mpad;
+    int n_at;                 // a-tiles (Npad / BM)
+    const int4* ckey;         // per padded cell: key pieces; .w = 0 for padding
+    const float* Q;           // square key table of this band
+    float qscale;             // 2^sQ
+    float out_scale;          // 2^-(sQ + sB): T in its natural units
+    float* Tf;                // [Mpad][Npad] T^T, FP32
+    int* err;
+};
+
+__device__ __forceinline__ int pair_key(const KeySpace& ks, int4 a, int4 b) {
+    if (ks.coordsys == 1) {
+        int kx = abs(a.x - b.x), ky = abs(a.y - b.y), kz = abs(a.z - b.z);
+        return (kx * ks.N2 + ky) * ks.N3 + kz;
+    }
+    int df = abs(a.y - b.y);
+    if (ks.fold) df = min(df, ks.N3 - df);
+    return a.x * ks.H + b.x + df;  // a.x = h_a nf, b.x = h_b nf
+}
+
+__global__ void __launch_bounds__(320, 1)
+    step1_kernel(const __grid_constant__ CUtensorMap mBh, const __grid_constant__ CUtensorMap mBl, Step1Params p) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    __shared__ __align__(8) unsigned long long bar_full[STAGES], bar_empty[STAGES], bar_acc;
+    __shared__ uint32_t tmem_slot;
+    __shared__ volatile int abort_flag;
+    __shared__ int4 rowkey[BM];
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int jt = blockIdx.x / p.n_at, at = blockIdx.x % p.n_at;
+    const int a0 = at * BM, j0 = jt * BN;
+    const int nk = p.Npad / BK;
+
+    if (threadIdx.x == 0) {
+        abort_flag = 0;
+        for (int s = 0; s < STAGES; s++) {
+            mbar_init(smem_u32(&bar_full[s]), 1 + 8);
+            mbar_init(smem_u32(&bar_empty[s]), 1);
+        }
+        mbar_init(smem_u32(&bar_acc), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (threadIdx.x < BM) rowkey[threadIdx.x] = p.ckey[a0 + threadIdx.x];
+    if (warp == 0) tmem_alloc(smem_u32(&tmem_slot));
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_slot;
+
+    auto A_hi = [&](int s) { return smem + s * STAGE_BYTES; };
+    auto A_lo = [&](int s) { return smem + s * STAGE_BYTES + A_BYTES; };
+    auto B_hi = [&](int s) { return smem + s * STAGE_BYTES + 2 * A_BYTES; };
+    auto B_lo = [&](int s) { return smem + s * STAGE_BYTES + 2 * A_BYTES + B_BYTES; };
+
+    if (warp == 0) {
+        // TMA producer for B' hi/lo
+        if (lane == 0) {
+            for (int k = 0; k < nk; k++) {
+                const int s = k % STAGES, n = k / STAGES;
+                if (n > 0 && !mbar_wait(smem_u32(&bar_empty[s]), (n - 1) & 1, &abort_flag, p.err)) break;
+                const uint32_t fb = smem_u32(&bar_full[s]);
+                mbar_arrive_tx(fb, 2 * B_BYTES);
+                tma_load_2d(smem_u32(B_hi(s)), &mBh, fb, k * BK, j0);
+                tma_load_2d(smem_u32(B_lo(s)), &mBl, fb, k * BK, j0);
+            }
+        }
+    } else if (warp == 1) {
+        // MMA issuer
+        for (int k = 0; k < nk; k++) {
+            const int s = k % STAGES, n = k / STAGES;
+            if (!mbar_wait(smem_u32(&bar_full[s]), n & 1, &abort_flag, p.err)) break;
+            tc_fence_after();
+            if (lane == 0) {
+                const uint64_t ah = sdesc(smem_u32(A_hi(s))), al = sdesc(smem_u32(A_lo(s)));
+                const uint64_t bh = sdesc(smem_u32(B_hi(s))), bl = sdesc(smem_u32(B_lo(s)));
+#pragma unroll
+                for (int kk = 0; kk < BK / 16; kk++) {
+                    const uint64_t adv = (uint64_t)(kk * 32) >> 4;
+                    umma(tmem, ah + adv, bh + adv, (k > 0 || kk > 0) ? 1u : 0u);
+                    umma(tmem, ah + adv, bl + adv, 1u);
+                    umma(tmem, al + adv, bh + adv, 1u);
+                }
+                umma_commit(smem_u32(&bar_empty[s]));
+            }
+            __syncwarp();
+        }
+        if (lane == 0) umma_commit(smem_u32(&bar_acc));
+        __syncwarp();
+    } else {
+        // eight gather producers: warp pw fills rows pw, pw+8, ...; lane covers columns 2 lane, 2 lane + 1
+        const int pw = warp - 2;
+        for (int k = 0; k < nk; k++) {
+            const int s = k % STAGES, n = k / STAGES;
+            if (n > 0 && !mbar_wait(smem_u32(&bar_empty[s]), (n - 1) & 1, &abort_flag, p.err)) break;
+            const int b = k * BK + 2 * lane;
+            const int4 kb0 = p.ckey[b], kb1 = p.ckey[b + 1];
+            unsigned char* ahi = A_hi(s);
+            unsigned char* alo = A_lo(s);
+#pragma unroll 4
+            for (int i = 0; i < BM / 8; i++) {
+                const int r = pw + 8 * i;
+                const int4 ka = rowkey[r];
+                float x0 = 0.f, x1 = 0.f;
+                if (ka.w && kb0.w) x0 = __ldg(p.Q + pair_key(p.ks, ka, kb0)) * p.qscale;
+                if (ka.w && kb1.w) x1 = __ldg(p.Q + pair_key(p.ks, ka, kb1)) * p.qscale;
+                __half h0, l0, h1, l1;
+                split_half(x0, h0, l0);
+                split_half(x1, h1, l1);
+                const uint32_t off = (r >> 3) * 1024 + (r & 7) * 128 + ((((uint32_t)lane >> 2) ^ (r & 7)) << 4) + (lane & 3) * 4;
+                *reinterpret_cast<__half2*>(ahi + off) = __halves2half2(h0, h1);
+                *reinterpret_cast<__half2*>(alo + off) = __halves2half2(l0, l1);
+            }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_u32(&bar_full[s]));
+        }
+        // epilogue: warps 4..7 own TMEM lane quarters 0..3
+        if (warp >= 4 && warp < 8) {
+            const int q = warp & 3;
+            if (mbar_wait(smem_u32(&bar_acc), 0, &abort_flag, p.err)) {
+                tc_fence_after();
+                const int a = a0 + 32 * q + lane;
+                for (int cc = 0; cc < BN / 32; cc++) {
+                    float v[32];
+                    tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(32 * cc), v);
+#pragma unroll
+                    for (int t = 0; t < 32; t++) p.Tf[(size_t)(j0 + 32 * cc + t) * p.Npad + a] = v[t] * p.out_scale;
+                }
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        tmem_dealloc(tmem);
+    }
+}
+
+// ---------------------------------------------------------------- step 2
+struct Step2Params {
+    int M, Npad;
+    const int2* tiles;  // (i-tile, j-tile) pairs touching the upper triangle
+    float sB;           // scale of B'
+    const unsigned* maxT;  // max |T| of this band (float bits); T was scaled by pow2_scale(maxT)
+    float* Dp;          // packed output of this band
+    int* err;
+};
+
+__global__ void __launch_bounds__(256, 1)
+    step2_kernel(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtensorMap mAl,
+                 const __grid_constant__ CUtensorMap mTh, const __grid_constant__ CUtensorMap mTl, Step2Params p) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    __shared__ __align__(8) unsigned long long bar_full[STAGES], bar_empty[STAGES], bar_acc;
+    __shared__ uint32_t tmem_slot;
+    __shared__ volatile int abort_flag;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int2 tile = p.tiles[blockIdx.x];
+    const int i0 = tile.x * BM, j0 = tile.y * BN;
+    const int nk = p.Npad / BK;
+
+    if (threadIdx.x == 0) {
+        abort_flag = 0;
+        for (int s = 0; s < STAGES; s++) {
+            mbar_init(smem_u32(&bar_full[s]), 1);
+            mbar_init(smem_u32(&bar_empty[s]), 1);
+        }
+        mbar_init(smem_u32(&bar_acc), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) tmem_alloc(smem_u32(&tmem_slot));
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_slot;
+
+    auto A_hi = [&](int s) { return smem + s * STAGE_BYTES; };
+    auto A_lo = [&](int s) { return smem + s * STAGE_BYTES + A_BYTES; };
+    auto B_hi = [&](int s) { return smem + s * STAGE_BYTES + 2 * A_BYTES; };
+    auto B_lo = [&](int s) { return smem + s * STAGE_BYTES + 2 * A_BYTES + B_BYTES; };
+
+    if (warp == 0) {
+        if (lane == 0) {
+            for (int k = 0; k < nk; k++) {
+                const int s = k % STAGES, n = k / STAGES;
+                if (n > 0 && !mbar_wait(smem_u32(&bar_empty[s]), (n - 1) & 1, &abort_flag, p.err)) break;
+                const uint32_t fb = smem_u32(&bar_full[s]);
+                mbar_arrive_tx(fb, STAGE_BYTES);
+                tma_load_2d(smem_u32(A_hi(s)), &mAh, fb, k * BK, i0);
+                tma_load_2d(smem_u32(A_lo(s)), &mAl, fb, k * BK, i0);
+                tma_load_2d(smem_u32(B_hi(s)), &mTh, fb, k * BK, j0);
+                tma_load_2d(smem_u32(B_lo(s)), &mTl, fb, k * BK, j0);
+            }
+        }
+    } else if (warp == 1) {
+        for (int k = 0; k < nk; k++) {
+            const int s = k % STAGES, n = k / STAGES;
+            if (!mbar_wait(smem_u32(&bar_full[s]), n & 1, &abort_flag, p.err)) break;
+            tc_fence_after();
+            if (lane == 0) {
+                const uint64_t ah = sdesc(smem_u32(A_hi(s))), al = sdesc(smem_u32(A_lo(s)));
+                const uint64_t bh = sdesc(smem_u32(B_hi(s))), bl = sdesc(smem_u32(B_lo(s)));
+#pragma unroll
+                for (int kk = 0; kk < BK / 16; kk++) {
+                    const uint64_t adv = (uint64_t)(kk * 32) >> 4;
+                    umma(tmem, ah + adv, bh + adv, (k > 0 || kk > 0) ? 1u : 0u);
+                    umma(tmem, ah + adv, bl + adv, 1u);
+                    umma(tmem, al + adv, bh + adv, 1u);
+                }
+                umma_commit(smem_u32(&bar_empty[s]));
+            }
+            __syncwarp();
+        }
+        if (lane == 0) umma_commit(smem_u32(&bar_acc));
+        __syncwarp();
+    } else if (warp >= 4) {
+        const int q = warp & 3;
+        if (mbar_wait(smem_u32(&bar_acc), 0, &abort_flag, p.err)) {
+            tc_fence_after();
+            const float out_scale = 1.0f / (p.sB * pow2_scale(__uint_as_float(*p.maxT)));
+            const int i = i0 + 32 * q + lane;
+            for (int cc = 0; cc < BN / 32; cc++) {
+                float v[32];
+                tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(32 * cc), v);
+#pragma unroll
+                for (int t = 0; t < 32; t++) {
+                    const int j = j0 + 32 * cc + t;
+                    if (i <= j && j < p.M) p.Dp[(size_t)j * (j + 1) / 2 + i] = v[t] * out_scale;
+                }
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        tmem_dealloc(tmem);
+    }
+}
+
+// ---------------------------------------------------------------- helpers
+__global__ void cell_keys_kernel(KeySpace ks, int N, int Npad, const int* h, const int* f, const int* g, int4* out) {
+    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < Npad; a += gridDim.x * blockDim.x) {
+        int4 k = make_int4(0, 0, 0, 0);
+        if (a < N) {
+            if (ks.coordsys == 1)
+                k = make_int4(h[a], f[a], g[a], 1);
+            else
+                k = make_int4(h[a] * ks.nf, f[a], 0, 1);
+        }
+        out[a] = k;
+    }
+}
+
+__global__ void absmax_f64_kernel(size_t n, const double* x, unsigned int* out) {
+    float m = 0.f;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x)
+        m = fmaxf(m, (float)fabs(x[e]));
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(out, __float_as_uint(m));
+}
+
+__global__ void absmax_f32_kernel(int ntab, size_t n, const float* x, unsigned int* out) {
+    const int t = blockIdx.y;
+    float m = 0.f;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x)
+        m = fmaxf(m, fabsf(x[(size_t)t * n + e]));
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(out + t, __float_as_uint(m));
+}
+
+// B'[i][a] (FP64, M x N) * scale -> hi/lo FP16 [Mpad][Npad], zero padded
+__global__ void split_modes_kernel(int M, int N, int Mpad, int Npad, const double* Bs, float scale, __half* Bh,
+                                   __half* Bl) {
+    const size_t total = (size_t)Mpad * Npad;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const int i = (int)(e / Npad), a = (int)(e % Npad);
+        float x = (i < M && a < N) ? (float)(Bs[(size_t)i * N + a] * (double)scale) : 0.f;
+        // split from the FP64 value so that lo carries the bits below the FP16 head
+        __half h = __float2half_rn(x);
+        double rem = (i < M && a < N) ? Bs[(size_t)i * N + a] * (double)scale - (double)__half2float(h) : 0.0;
+        Bh[e] = h;
+        Bl[e] = __float2half_rn((float)rem);
+    }
+}
+
+// T^T (FP32) * pow2_scale(max|T|) -> hi/lo FP16
+__global__ void split_t_kernel(size_t n, const float* Tf, const unsigned* maxT, __half* Th, __half* Tl) {
+    const float sc = pow2_scale(__uint_as_float(*maxT));
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+        __half h, l;
+        split_half(Tf[e] * sc, h, l);
+        Th[e] = h;
+        Tl[e] = l;
+    }
+}
+
+typedef CUresult (*EncodeTiled)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiled encoder() {
+    static EncodeTiled fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        OPSEC_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q));
+        if (!p || q != cudaDriverEntryPointSuccess) fail(OPSEC_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+        fn = reinterpret_cast<EncodeTiled>(p);
+    }
+    return fn;
+}
+
+// 2-D FP16 tensor [rows][cols] (cols contiguous), box = 64 cols x box_rows, 128B swizzle
+CUtensorMap make_map(const __half* base, int rows, int cols, int box_rows) {
+    CUtensorMap m;
+    std::memset(&m, 0, sizeof m);
+    cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)cols * sizeof(__half)};
+    cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = encoder()(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<__half*>(base), dims, strides, box, estr,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) fail(OPSEC_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+    return m;
+}
+
+struct Layout {
+    int Npad, Mpad;
+    size_t bh, bl, th, tl, tf, ckey, maxes, tiles, err, total;
+};
+
+Layout layout_of(const ProjectArgs& a) {
+    Layout L;
+    L.Npad = (a.ncells + BM - 1) / BM * BM;
+    L.Mpad = (a.nmodes + BN - 1) / BN * BN;
+    const size_t half_mat = (size_t)L.Mpad * L.Npad * sizeof(__half);
+    size_t o = 0;
+    auto take = [&](size_t bytes) {
+        size_t at = o;
+        o += (bytes + 1023) / 1024 * 1024;
+        return at;
+    };
+    L.bh = take(half_mat);
+    L.bl = take(half_mat);
+    L.th = take(half_mat);
+    L.tl = take(half_mat);
+    L.tf = take(2 * half_mat);
+    L.ckey = take(sizeof(int4) * L.Npad);
+    L.maxes = take(sizeof(unsigned) * (1 + 2 * a.nbands));
+    const int nti = L.Mpad / BM, ntj = L.Mpad / BN;
+    L.tiles = take(sizeof(int2) * (size_t)nti * ntj);
+    L.err = take(sizeof(int));
+    L.total = o;
+    return L;
+}
+
+}  // namespace
+
+bool project_tc_supported(const ProjectArgs& a) {
+    return a.ncells >= 1 && a.nmodes >= 1 && a.nbands >= 1 && a.ncells < (1 << 28);
+}
+
+size_t project_tc_work_bytes(const ProjectArgs& a) { return layout_of(a).total; }
+
+void launch_project_tc(const ProjectArgs& a, cudaStream_t s, long long* launches) {
+    const Layout L = layout_of(a);
+    if (a.work_bytes < L.total) fail(OPSEC_ERR_ARG, "projection workspace too small");
+    unsigned char* w = static_cast<unsigned char*>(a.work);
+    __half* Bh = reinterpret_cast<__half*>(w + L.bh);
+    __half* Bl = reinterpret_cast<__half*>(w + L.bl);
+    __half* Th = reinterpret_cast<__half*>(w + L.th);
+    __half* Tl = reinterpret_cast<__half*>(w + L.tl);
+    int4* ckey = reinterpret_cast<int4*>(w + L.ckey);
+    unsigned* maxes = reinterpret_cast<unsigned*>(w + L.maxes);
+    int2* tiles = reinterpret_cast<int2*>(w + L.tiles);
+    int* err = reinterpret_cast<int*>(w + L.err);
+    float* Tf = reinterpret_cast<float*>(w + L.tf);
+    const int N = a.ncells, M = a.nmodes, nb = a.nbands;
+    unsigned* maxT = maxes + 1 + nb;  // per band
+
+    OPSEC_CUDA(cudaMemsetAsync(maxes, 0, sizeof(unsigned) * (1 + 2 * nb), s));
+    OPSEC_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
+    cell_keys_kernel<<<(L.Npad + 255) / 256, 256, 0, s>>>(a.ks, N, L.Npad, a.cell_h, a.cell_f, a.cell_g, ckey);
+    absmax_f64_kernel<<<1024, 256, 0, s>>>((size_t)M * N, a.Bs, maxes);
+    absmax_f32_kernel<<<dim3(1024, nb), 256, 0, s>>>(nb, (size_t)a.ks.nsquare, a.Qsq + a.ks.nsquare, maxes + 1);
+    OPSEC_CUDA(cudaGetLastError());
+    *launches += 3;
+    std::vector<unsigned> hm(1 + nb);
+    OPSEC_CUDA(cudaMemcpyAsync(hm.data(), maxes, sizeof(unsigned) * (1 + nb), cudaMemcpyDeviceToHost, s));
+    OPSEC_CUDA(cudaStreamSynchronize(s));
+    auto asf = [](unsigned u) {
+        float f;
+        std::memcpy(&f, &u, sizeof f);
+        return f;
+    };
+    const float sB = pow2_scale(asf(hm[0]));
+
+    split_modes_kernel<<<2048, 256, 0, s>>>(M, N, L.Mpad, L.Npad, a.Bs, sB, Bh, Bl);
+    OPSEC_CUDA(cudaGetLastError());
+    ++*launches;
+
+    // tiles (i-tile of 128, j-tile of 256) that hold an element with i <= j
+    std::vector<int2> tl;
+    for (int tj = 0; tj < L.Mpad / BN; tj++)
+        for (int ti = 0; ti < L.Mpad / BM; ti++)
+            if (ti * BM <= tj * BN + BN - 1 && ti * BM < M && tj * BN < M) tl.push_back(make_int2(ti, tj));
+    OPSEC_CUDA(cudaMemcpyAsync(tiles, tl.data(), sizeof(int2) * tl.size(), cudaMemcpyHostToDevice, s));
+
+    const CUtensorMap mBh256 = make_map(Bh, L.Mpad, L.Npad, BN), mBl256 = make_map(Bl, L.Mpad, L.Npad, BN);
+    const CUtensorMap mBh128 = make_map(Bh, L.Mpad, L.Npad, BM), mBl128 = make_map(Bl, L.Mpad, L.Npad, BM);
+    const CUtensorMap mTh256 = make_map(Th, L.Mpad, L.Npad, BN), mTl256 = make_map(Tl, L.Mpad, L.Npad, BN);
+
+    const size_t smem = (size_t)STAGES * STAGE_BYTES + 1024;
+    OPSEC_CUDA(cudaFuncSetAttribute(step1_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    OPSEC_CUDA(cudaFuncSetAttribute(step2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+
+    const int n_at = L.Npad / BM, n_jt = L.Mpad / BN;
+    const size_t nT = (size_t)L.Mpad * L.Npad;
+    for (int p = 0; p < nb; p++) {
+        const float sQ = pow2_scale(asf(hm[1 + p]));
+        Step1Params p1;
+        p1.ks = a.ks;
+        p1.N = N;
+        p1.Npad = L.Npad;
+        p1.Mpad = L.Mpad;
+        p1.n_at = n_at;
+        p1.ckey = ckey;
+        p1.Q = a.Qsq + (size_t)(1 + p) * a.ks.nsquare;
+        p1.qscale = sQ;
+        p1.out_scale = 1.0f / (sQ * sB);
+        p1.Tf = Tf;
+        p1.err = err;
+        if (g_clock) g_clock->begin("project_step1", s, 2.0 * N * (double)N * M);
+        step1_kernel<<<n_at * n_jt, 320, smem, s>>>(mBh256, mBl256, p1);
+        OPSEC_CUDA(cudaGetLastError());
+        if (g_clock) g_clock->end(s);
+        absmax_f32_kernel<<<dim3(2048, 1), 256, 0, s>>>(1, nT, Tf, maxT + p);
+        split_t_kernel<<<4096, 256, 0, s>>>(nT, Tf, maxT + p, Th, Tl);
+        OPSEC_CUDA(cudaGetLastError());
+        Step2Params p2;
+        p2.M = M;
+        p2.Npad = L.Npad;
+        p2.tiles = tiles;
+        p2.sB = sB;
+        p2.maxT = maxT + p;
+        p2.Dp = a.Dp + (size_t)p * ((size_t)M * (M + 1) / 2);
+        p2.err = err;
+        if (g_clock) g_clock->begin("project_step2", s, (double)N * M * (double)(M + 1));
+        step2_kernel<<<(unsigned)tl.size(), 256, smem, s>>>(mBh128, mBl128, mTh256, mTl256, p2);
+        OPSEC_CUDA(cudaGetLastError());
+        if (g_clock) g_clock->end(s);
+        *launches += 4;
+    }
+    int herr = 0;
+    OPSEC_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    OPSEC_CUDA(cudaStreamSynchronize(s));
+    if (herr) fail(OPSEC_ERR_CUDA, "tensor-core projection timed out waiting on a pipeline barrier");
+}
+
 }  // namespace opsec

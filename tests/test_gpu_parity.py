@@ -185,3 +185,40 @@ def test_errors_are_status_codes():
         e.fisher_build(cells, counts, 4)
     assert ei.value.code == -6
     e.close()
+
+
+@pytest.mark.parametrize("name", ["sph_full", "box4"])
+def test_projection_tensor_core_vs_cuda_core(name):
+    """The tcgen05 FP16 3-term projection and the CUDA-core FP32 form agree
+    with each other and with the FP64 oracle."""
+    sv, cells = CASES[name]
+    bands = synth.band_edges(3, 0.0, 0.15)
+    _, Q, M, ev, modes = _oracle_modes(sv, cells, bands, cells.size // 2)
+    out = {}
+    for kind in ("tc", "simt"):
+        e = api.Engine(api.make_config(sv, bands=bands, extra=[f"projection = {kind}"]))
+        e.set_pk(*PK)
+        out[kind] = e.comma(cells, modes)
+        e.close()
+    for p in range(len(bands)):
+        ref = O.project(modes, O.signal_matrix(sv, cells, Q[:, 1 + p]))
+        scale = np.max(np.abs(ref))
+        assert np.max(np.abs(out["tc"][p] - ref)) <= 1e-5 * scale
+        assert np.max(np.abs(out["simt"][p] - ref)) <= 1e-5 * scale
+
+
+def test_projection_ragged_sizes():
+    """Cells and modes that are not multiples of the 128 x 256 tiles."""
+    sv, cells = synth.shell_survey(3, 5, 7)  # 105 cells, partial tiles everywhere
+    bands = synth.band_edges(2, 0.0, 0.1)
+    tabs = O.xi_tables(*PK, bands)
+    Q = O.qtable_keys(sv, O.keys_all(sv), tabs)
+    S = O.signal_matrix(sv, cells, Q[:, 0])
+    ev, modes = O.klt(S, 37)
+    e = api.Engine(api.make_config(sv, bands=bands, extra=["projection = tc"]))
+    e.set_pk(*PK)
+    cov = e.comma(cells, modes)
+    for p in range(2):
+        ref = O.project(modes, O.signal_matrix(sv, cells, Q[:, 1 + p]))
+        assert np.max(np.abs(cov[p] - ref)) <= 1e-5 * np.max(np.abs(ref))
+    e.close()
