@@ -91,14 +91,15 @@ def make_config(survey, bands=None, nbands=None, kmin=None, kmax=None, nmodes=No
     if pkfile:
         lines.append(f"RealModel.pkfile = {pkfile}")
     if bands is not None:
-        lines.append("RealModel.bands = " + " ".join(f"{lo!r} {hi!r}" for lo, hi in bands))
+        lines.append("RealModel.bands = " + " ".join(f"{float(lo)!r} {float(hi)!r}" for lo, hi in bands))
     else:
-        lines += [f"RealModel.Nbands = {nbands}", f"RealModel.kmin = {kmin!r}", f"RealModel.kmax = {kmax!r}"]
+        lines += [f"RealModel.Nbands = {int(nbands)}", f"RealModel.kmin = {float(kmin)!r}",
+                  f"RealModel.kmax = {float(kmax)!r}"]
     if nmodes is not None:
         lines.append(f"Nmodes = {nmodes}")
     if layout is not None:
         n1, n2, r1, r2 = layout
-        lines += [f"xi.n1 = {n1}", f"xi.n2 = {n2}", f"xi.r1 = {r1!r}", f"xi.r2 = {r2!r}"]
+        lines += [f"xi.n1 = {int(n1)}", f"xi.n2 = {int(n2)}", f"xi.r1 = {float(r1)!r}", f"xi.r2 = {float(r2)!r}"]
     if gauss is not None:
         lines.append(f"sig.gauss = {gauss}")
     if mixing is not None:

@@ -404,16 +404,14 @@ void configure(opsec_gpu* c, const std::map<std::string, std::string>& kv) {
         fail(OPSEC_ERR_CONFIG, "model must be RealModel (got '" + get("model") + "')");
     if (has("RealModel.pkfile")) load_pkfile(c, get("RealModel.pkfile"));
     if (has("RealModel.bands")) {
-        std::istringstream in(get("RealModel.bands"));
+        // whitespace- or comma-separated kmin kmax pairs (cfg_get_array_double, RealModel.cpp:44-48)
+        std::string text = get("RealModel.bands");
+        for (char& ch : text)
+            if (ch == ',') ch = ' ';
+        std::istringstream in(text);
         std::vector<double> v;
         std::string tok;
-        while (in >> tok) {
-            for (char& ch : tok)
-                if (ch == ',') ch = ' ';
-            std::istringstream t2(tok);
-            double x;
-            while (t2 >> x) v.push_back(x);
-        }
+        while (in >> tok) v.push_back(to_double("RealModel.bands", tok));
         if (v.size() % 2) v.pop_back();  // RealModel.cpp:49-52 drops an odd trailing value
         for (size_t i = 0; i + 1 < v.size(); i += 2) {
             c->band_lo.push_back(v[i]);
@@ -431,6 +429,7 @@ void configure(opsec_gpu* c, const std::map<std::string, std::string>& kv) {
     } else {
         fail(OPSEC_ERR_CONFIG, "k-bands not specified (RealModel.bands or RealModel.Nbands,kmin,kmax)");
     }
+    if (c->band_lo.empty()) fail(OPSEC_ERR_CONFIG, "at least one k-band is required");
     for (size_t i = 0; i < c->band_lo.size(); i++)
         if (!(c->band_lo[i] < c->band_hi[i]) || c->band_lo[i] < 0)
             fail(OPSEC_ERR_CONFIG, "band " + std::to_string(i) + " has kmin >= kmax or kmin < 0");

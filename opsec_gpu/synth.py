@@ -232,7 +232,7 @@ def grf_counts(survey: Survey, cells, seed_field: int = 1, seed_poisson: int = 2
     amp = np.sqrt(pk_model(kk) / box ** 3) * ngrid ** 3
     amp[0, 0, 0] = 0.0
     noise = rng.standard_normal((ngrid, ngrid, ngrid))
-    field = np.fft.irfftn(np.fft.rfftn(noise) / ngrid ** 1.5 * amp, s=(ngrid, ngrid, ngrid))
+    field = np.fft.irfftn(np.fft.rfftn(noise) / ngrid ** 1.5 * amp, s=(ngrid, ngrid, ngrid), axes=(0, 1, 2))
     idx = np.floor((xyz - lo) / h).astype(np.int64) % ngrid
     delta = field[idx[:, 0], idx[:, 1], idx[:, 2]]
     lam = np.clip(cells["Nbar"] * (1.0 + delta), 0.0, None)
