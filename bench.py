@@ -50,6 +50,10 @@ def workload(name):
         sv, cells = synth.shell_survey(32, 32, 32)
         return dict(name="c2", survey=sv, cells=cells, nbands=40, kmax=0.4, nmodes=8192,
                     layout=(256, 4096, 10.0, 20000.0), gauss=4)
+    if name == "c2-mid":  # same geometry family, 16,384 cells (profiling size)
+        sv, cells = synth.shell_survey(16, 32, 32)
+        return dict(name="c2-mid", survey=sv, cells=cells, nbands=40, kmax=0.4, nmodes=4096,
+                    layout=(256, 4096, 10.0, 20000.0), gauss=4)
     if name == "c2-small":  # same geometry family, 4,096 cells
         sv, cells = synth.shell_survey(16, 16, 16)
         return dict(name="c2-small", survey=sv, cells=cells, nbands=40, kmax=0.4, nmodes=1024,
