@@ -239,6 +239,11 @@ struct opsec_gpu {
     int device = 0;
     cudaStream_t stream = nullptr;
     cusolverDnHandle_t solver = nullptr;
+    // side streams for the independent azimuthal eigenproblems
+    static constexpr int kSide = 6;
+    cudaStream_t side[kSide] = {};
+    cusolverDnHandle_t side_solver[kSide] = {};
+    cudaEvent_t side_ev[kSide + 1] = {};
     long long launches = 0;
     double stage_ms[5] = {0, 0, 0, 0, 0};
     std::string warning;
@@ -702,12 +707,29 @@ int eigensolve(opsec_gpu* c, int ncells, const opsec_cell* cells, int M) {
         solver_check(cusolverDnDsyevd_bufferSize(c->solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, H, c->S.p,
                                                  H, c->W.p, &lwork),
                      "syevd_bufferSize");
-        c->work.alloc((size_t)lwork);
-        for (int m = 0; m < nm; m++)
-            solver_check(cusolverDnDsyevd(c->solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, H,
-                                          c->S.p + (size_t)m * H * H, H, c->W.p + (size_t)m * H, c->work.p, lwork,
-                                          c->info.p + m),
+        // the nm block eigenproblems are independent: spread them over side streams
+        const int ns = std::min(nm, (int)opsec_gpu::kSide);
+        c->work.alloc((size_t)lwork * ns);
+        for (int j = 0; j < ns; j++) {
+            if (!c->side[j]) OPSEC_CUDA(cudaStreamCreateWithFlags(&c->side[j], cudaStreamNonBlocking));
+            if (!c->side_solver[j]) solver_check(cusolverDnCreate(&c->side_solver[j]), "cusolverDnCreate");
+            solver_check(cusolverDnSetStream(c->side_solver[j], c->side[j]), "cusolverDnSetStream");
+        }
+        for (int j = 0; j <= ns; j++)
+            if (!c->side_ev[j]) OPSEC_CUDA(cudaEventCreateWithFlags(&c->side_ev[j], cudaEventDisableTiming));
+        OPSEC_CUDA(cudaEventRecord(c->side_ev[ns], c->stream));
+        for (int j = 0; j < ns; j++) OPSEC_CUDA(cudaStreamWaitEvent(c->side[j], c->side_ev[ns], 0));
+        for (int m = 0; m < nm; m++) {
+            const int j = m % ns;
+            solver_check(cusolverDnDsyevd(c->side_solver[j], CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, H,
+                                          c->S.p + (size_t)m * H * H, H, c->W.p + (size_t)m * H,
+                                          c->work.p + (size_t)j * lwork, lwork, c->info.p + m),
                          "syevd");
+        }
+        for (int j = 0; j < ns; j++) {
+            OPSEC_CUDA(cudaEventRecord(c->side_ev[j], c->side[j]));
+            OPSEC_CUDA(cudaStreamWaitEvent(c->stream, c->side_ev[j], 0));
+        }
         check_info(c, nm);
         std::vector<double> w((size_t)nm * H);
         OPSEC_CUDA(cudaMemcpyAsync(w.data(), c->W.p, sizeof(double) * w.size(), cudaMemcpyDeviceToHost, c->stream));
@@ -1142,6 +1164,13 @@ void opsec_gpu_destroy(opsec_gpu* c) {
     if (c->device >= 0) cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->solver) cusolverDnDestroy(c->solver);
+    for (int j = 0; j < opsec_gpu::kSide; j++) {
+        if (c->side[j]) cudaStreamSynchronize(c->side[j]);
+        if (c->side_solver[j]) cusolverDnDestroy(c->side_solver[j]);
+        if (c->side[j]) cudaStreamDestroy(c->side[j]);
+    }
+    for (int j = 0; j <= opsec_gpu::kSide; j++)
+        if (c->side_ev[j]) cudaEventDestroy(c->side_ev[j]);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }

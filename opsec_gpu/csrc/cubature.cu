@@ -23,7 +23,6 @@
 namespace opsec {
 namespace {
 
-constexpr int kWarps = 8;
 
 struct Lookup {
     float inv_dr;   // n1 / r1: index in the linear section
@@ -76,8 +75,8 @@ __device__ __forceinline__ void point_xyz(const CubatureArgs& a, const int* c, i
     }
 }
 
-template <int NG, int G>
-__global__ void __launch_bounds__(kWarps * 32) cubature_kernel(CubatureArgs a, int tab0, int ngrp, Lookup lk) {
+template <int NG, int G, int kWarps>
+__global__ void __launch_bounds__(kWarps * 32, 1) cubature_kernel(CubatureArgs a, int tab0, int ngrp, Lookup lk) {
     constexpr int NP = NG * NG * NG;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int nx = a.xl.n();
@@ -153,11 +152,11 @@ __global__ void __launch_bounds__(kWarps * 32) cubature_kernel(CubatureArgs a, i
     }
 }
 
-template <int NG, int G>
+template <int NG, int G, int kWarps>
 void run(const CubatureArgs& a, int tab0, int ngrp, const Lookup& lk, cudaStream_t s) {
     constexpr int NP = NG * NG * NG;
     const size_t smem = sizeof(float4) * kWarps * 2 * NP + sizeof(float) * (size_t)ngrp * a.xl.n();
-    auto k = cubature_kernel<NG, G>;
+    auto k = cubature_kernel<NG, G, kWarps>;
     OPSEC_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int dev = 0, nsm = 0, occ = 0;
     OPSEC_CUDA(cudaGetDevice(&dev));
@@ -173,10 +172,20 @@ void run(const CubatureArgs& a, int tab0, int ngrp, const Lookup& lk, cudaStream
     if (g_clock) g_clock->end(s);
 }
 
+template <int NG, int G>
+void run_w(const CubatureArgs& a, int tab0, int g, const Lookup& lk, cudaStream_t s, int warps) {
+    if (warps == 16)
+        run<NG, G, 16>(a, tab0, g, lk, s);
+    else
+        run<NG, G, 8>(a, tab0, g, lk, s);
+}
+
 template <int NG>
 void run_groups(const CubatureArgs& a, const Lookup& lk, cudaStream_t s, long long* launches) {
     constexpr int NP = NG * NG * NG;
-    const size_t budget = 220 * 1024 - sizeof(float4) * kWarps * 2 * NP;
+    // 16 warps per CTA (twice the latency hiding) while the point buffers leave room for tables
+    const int warps = (NG <= 4) ? 16 : 8;
+    const size_t budget = 224 * 1024 - sizeof(float4) * warps * 2 * NP;
     int gmax = (int)(budget / (sizeof(float) * a.xl.n()));
     if (gmax > 16) gmax = 16;
     if (gmax < 1) fail(OPSEC_ERR_CONFIG, "xi table too long for shared memory");
@@ -185,15 +194,15 @@ void run_groups(const CubatureArgs& a, const Lookup& lk, cudaStream_t s, long lo
     for (int t0 = 0; t0 < a.ntab; t0 += per) {
         const int g = (a.ntab - t0 < per) ? a.ntab - t0 : per;
         if (g <= 1)
-            run<NG, 1>(a, t0, g, lk, s);
+            run_w<NG, 1>(a, t0, g, lk, s, warps);
         else if (g <= 4)
-            run<NG, 4>(a, t0, g, lk, s);
+            run_w<NG, 4>(a, t0, g, lk, s, warps);
         else if (g <= 8)
-            run<NG, 8>(a, t0, g, lk, s);
+            run_w<NG, 8>(a, t0, g, lk, s, warps);
         else if (g <= 12)
-            run<NG, 12>(a, t0, g, lk, s);
+            run_w<NG, 12>(a, t0, g, lk, s, warps);
         else
-            run<NG, 16>(a, t0, g, lk, s);
+            run_w<NG, 16>(a, t0, g, lk, s, warps);
         ++*launches;
     }
 }

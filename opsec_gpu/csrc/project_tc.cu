@@ -243,25 +243,33 @@ __global__ void __launch_bounds__(320, 1)
         if (lane == 0) umma_commit(smem_u32(&bar_acc));
         __syncwarp();
     } else {
-        // eight gather producers: warp pw fills rows pw, pw+8, ...; lane covers columns 2 lane, 2 lane + 1
+        // eight gather producers: warp pw fills rows pw, pw+8, ...; lane covers columns 2 lane, 2 lane + 1.
+        // Software-pipelined: the 32 gathers of K-slice k+1 are in flight while the warp waits for
+        // its stage to drain and while the tensor core works on slice k.
         const int pw = warp - 2;
+        float x0[BM / 8], x1[BM / 8];
+        auto gather = [&](int k) {
+            const int b = k * BK + 2 * lane;
+            const int4 kb0 = p.ckey[b], kb1 = p.ckey[b + 1];
+#pragma unroll
+            for (int i = 0; i < BM / 8; i++) {
+                const int4 ka = rowkey[pw + 8 * i];
+                x0[i] = (ka.w && kb0.w) ? __ldg(p.Q + pair_key(p.ks, ka, kb0)) : 0.f;
+                x1[i] = (ka.w && kb1.w) ? __ldg(p.Q + pair_key(p.ks, ka, kb1)) : 0.f;
+            }
+        };
+        if (nk > 0) gather(0);
         for (int k = 0; k < nk; k++) {
             const int s = k % STAGES, n = k / STAGES;
             if (n > 0 && !mbar_wait(smem_u32(&bar_empty[s]), (n - 1) & 1, &abort_flag, p.err)) break;
-            const int b = k * BK + 2 * lane;
-            const int4 kb0 = p.ckey[b], kb1 = p.ckey[b + 1];
             unsigned char* ahi = A_hi(s);
             unsigned char* alo = A_lo(s);
-#pragma unroll 4
+#pragma unroll
             for (int i = 0; i < BM / 8; i++) {
                 const int r = pw + 8 * i;
-                const int4 ka = rowkey[r];
-                float x0 = 0.f, x1 = 0.f;
-                if (ka.w && kb0.w) x0 = __ldg(p.Q + pair_key(p.ks, ka, kb0)) * p.qscale;
-                if (ka.w && kb1.w) x1 = __ldg(p.Q + pair_key(p.ks, ka, kb1)) * p.qscale;
                 __half h0, l0, h1, l1;
-                split_half(x0, h0, l0);
-                split_half(x1, h1, l1);
+                split_half(x0[i] * p.qscale, h0, l0);
+                split_half(x1[i] * p.qscale, h1, l1);
                 const uint32_t off = (r >> 3) * 1024 + (r & 7) * 128 + ((((uint32_t)lane >> 2) ^ (r & 7)) << 4) + (lane & 3) * 4;
                 *reinterpret_cast<__half2*>(ahi + off) = __halves2half2(h0, h1);
                 *reinterpret_cast<__half2*>(alo + off) = __halves2half2(l0, l1);
@@ -269,6 +277,7 @@ __global__ void __launch_bounds__(320, 1)
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             __syncwarp();
             if (lane == 0) mbar_arrive(smem_u32(&bar_full[s]));
+            if (k + 1 < nk) gather(k + 1);
         }
         // epilogue: warps 4..7 own TMEM lane quarters 0..3
         if (warp >= 4 && warp < 8) {
