@@ -24,13 +24,24 @@ namespace opsec {
 namespace {
 
 
+// Table index of a distance r.  Linear section: t = r n1 / r1.  Log section:
+// t = n1 + (log2 r - log2 r1) (n2-1) / log2(r2/r1).  To keep the fraction of
+// t at the precision of r itself, log2 r is split into its binary exponent e
+// and log2 of the mantissa m in [1, 2) (the hardware log2 is accurate to
+// ~2^-22 absolute there), and the offset of each exponent,
+// c_e = n1 + (e - log2 r1) (n2-1)/log2(r2/r1), is precomputed in FP64 as an
+// integer part plus an FP32 fraction.
+constexpr int kMaxExp = 64;
 struct Lookup {
     float inv_dr;   // n1 / r1: index in the linear section
     float r1;
-    float l2r1;     // log2(r1)
-    float inv_du;   // (n2-1) / log2(r2/r1): index step of the log section
-    float n1;
+    float inv_du;   // (n2-1) / log2(r2/r1)
+    int n1;
     int imax;       // n - 2
+    int e0;         // smallest exponent held in the offset table
+    int ne;         // entries in the offset table
+    int ci[kMaxExp];    // integer part of c_e
+    float cf[kMaxExp];  // fraction of c_e
 };
 
 __device__ __forceinline__ void decode_key(const KeySpace& ks, long long key, int* c1, int* c2) {
@@ -84,6 +95,12 @@ __global__ void __launch_bounds__(kWarps * 32, 1) cubature_kernel(CubatureArgs a
     float* tab = reinterpret_cast<float*>(pts + kWarps * 2 * NP);  // [ngrp][nx]
 
     for (int i = threadIdx.x; i < ngrp * nx; i += blockDim.x) tab[i] = a.tab32[(size_t)tab0 * nx + i];
+    __shared__ int s_ci[kMaxExp];
+    __shared__ float s_cf[kMaxExp];
+    for (int i = threadIdx.x; i < lk.ne; i += blockDim.x) {
+        s_ci[i] = lk.ci[i];
+        s_cf[i] = lk.cf[i];
+    }
     __syncthreads();
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -125,10 +142,29 @@ __global__ void __launch_bounds__(kWarps * 32, 1) cubature_kernel(CubatureArgs a
                     dz += Lf * (float)((dz < -hL) - (dz >= hL));
                 }
                 const float r = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
-                float tf = (r < lk.r1) ? r * lk.inv_dr : fmaf(__log2f(r) - lk.l2r1, lk.inv_du, lk.n1);
-                int i = (int)tf;
-                i = i > lk.imax ? lk.imax : i;
-                const float fr = fminf(tf - (float)i, 1.0f);
+                int i;
+                float fr;
+                if (r < lk.r1) {
+                    const float t = r * lk.inv_dr;
+                    i = (int)t;
+                    fr = t - (float)i;
+                } else {
+                    const int bits = __float_as_int(r);
+                    const int e = min(max((bits >> 23) - 127 - lk.e0, 0), lk.ne - 1);
+                    const float lm = __log2f(__int_as_float((bits & 0x007FFFFF) | 0x3F800000));  // log2 of mantissa
+                    const float y = fmaf(lm, lk.inv_du, s_cf[e]);
+                    const float yi = floorf(y);
+                    i = s_ci[e] + (int)yi;
+                    fr = y - yi;
+                    if (i < lk.n1) {
+                        i = lk.n1;
+                        fr = 0.f;
+                    }
+                }
+                if (i > lk.imax) {
+                    i = lk.imax;
+                    fr = 1.0f;
+                }
 #pragma unroll
                 for (int t = 0; t < G; t++) {
                     if (t < ngrp) {
@@ -211,12 +247,24 @@ void run_groups(const CubatureArgs& a, const Lookup& lk, cudaStream_t s, long lo
 
 void launch_cubature(const CubatureArgs& a, cudaStream_t s, long long* launches) {
     Lookup lk;
+    const double inv_du = (a.xl.n2 - 1) / std::log2(a.xl.r2 / a.xl.r1);
     lk.inv_dr = (float)(a.xl.n1 / a.xl.r1);
     lk.r1 = (float)a.xl.r1;
-    lk.l2r1 = (float)std::log2(a.xl.r1);
-    lk.inv_du = (float)((a.xl.n2 - 1) / std::log2(a.xl.r2 / a.xl.r1));
-    lk.n1 = (float)a.xl.n1;
+    lk.inv_du = (float)inv_du;
+    lk.n1 = a.xl.n1;
     lk.imax = a.xl.n() - 2;
+    int e_lo = 0, e_hi = 0;
+    std::frexp(a.xl.r1, &e_lo);  // r1 = f 2^e_lo, f in [0.5,1): binary exponent of r1 is e_lo - 1
+    std::frexp(a.xl.r2, &e_hi);
+    lk.e0 = e_lo - 1;
+    lk.ne = e_hi - e_lo + 2;  // one spare exponent above r2 (clamped to the last table entry)
+    if (lk.ne > kMaxExp) fail(OPSEC_ERR_CONFIG, "xi table spans too many octaves of r");
+    for (int k = 0; k < lk.ne; k++) {
+        const double c = a.xl.n1 + ((lk.e0 + k) - std::log2(a.xl.r1)) * inv_du;
+        const double ci = std::floor(c);
+        lk.ci[k] = (int)ci;
+        lk.cf[k] = (float)(c - ci);
+    }
     switch (a.ng) {
     case 1: run_groups<1>(a, lk, s, launches); break;
     case 2: run_groups<2>(a, lk, s, launches); break;

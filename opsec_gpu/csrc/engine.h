@@ -115,7 +115,7 @@ struct XiTableArgs {
     double* r;              // [n] out
     double* xi64;           // [1+nbands][n] out
     float* xi32;            // [1+nbands][n] out
-    double* scratch;        // >= (32769 + nbands*8193) doubles of Simpson weights
+    double* scratch;        // >= 2 (32769 + nbands*8193) doubles: Simpson weights, then weights / k
 };
 void launch_xi_tables(const XiTableArgs& a, cudaStream_t s, long long* launches);
 

@@ -156,8 +156,7 @@ struct Step1Params {
     int N, Npad, Mpad;
     int n_at;                 // a-tiles (Npad / BM)
     const int4* ckey;         // per padded cell: key pieces; .w = 0 for padding
-    const float* Q;           // square key table of this band
-    float qscale;             // 2^sQ
+    const uint32_t* Qhl;      // square key table of this band, scaled by 2^sQ, FP16 hi | lo << 16
     float out_scale;          // 2^-(sQ + sB): T in its natural units
     float* Tf;                // [Mpad][Npad] T^T, FP32
     int* err;
@@ -247,15 +246,15 @@ __global__ void __launch_bounds__(320, 1)
         // Software-pipelined: the 32 gathers of K-slice k+1 are in flight while the warp waits for
         // its stage to drain and while the tensor core works on slice k.
         const int pw = warp - 2;
-        float x0[BM / 8], x1[BM / 8];
+        uint32_t x0[BM / 8], x1[BM / 8];
         auto gather = [&](int k) {
             const int b = k * BK + 2 * lane;
             const int4 kb0 = p.ckey[b], kb1 = p.ckey[b + 1];
 #pragma unroll
             for (int i = 0; i < BM / 8; i++) {
                 const int4 ka = rowkey[pw + 8 * i];
-                x0[i] = (ka.w && kb0.w) ? __ldg(p.Q + pair_key(p.ks, ka, kb0)) : 0.f;
-                x1[i] = (ka.w && kb1.w) ? __ldg(p.Q + pair_key(p.ks, ka, kb1)) : 0.f;
+                x0[i] = (ka.w && kb0.w) ? __ldg(p.Qhl + pair_key(p.ks, ka, kb0)) : 0u;
+                x1[i] = (ka.w && kb1.w) ? __ldg(p.Qhl + pair_key(p.ks, ka, kb1)) : 0u;
             }
         };
         if (nk > 0) gather(0);
@@ -267,12 +266,9 @@ __global__ void __launch_bounds__(320, 1)
 #pragma unroll
             for (int i = 0; i < BM / 8; i++) {
                 const int r = pw + 8 * i;
-                __half h0, l0, h1, l1;
-                split_half(x0[i] * p.qscale, h0, l0);
-                split_half(x1[i] * p.qscale, h1, l1);
                 const uint32_t off = (r >> 3) * 1024 + (r & 7) * 128 + ((((uint32_t)lane >> 2) ^ (r & 7)) << 4) + (lane & 3) * 4;
-                *reinterpret_cast<__half2*>(ahi + off) = __halves2half2(h0, h1);
-                *reinterpret_cast<__half2*>(alo + off) = __halves2half2(l0, l1);
+                *reinterpret_cast<uint32_t*>(ahi + off) = __byte_perm(x0[i], x1[i], 0x5410);  // (hi0, hi1)
+                *reinterpret_cast<uint32_t*>(alo + off) = __byte_perm(x0[i], x1[i], 0x7632);  // (lo0, lo1)
             }
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             __syncwarp();
@@ -451,6 +447,15 @@ __global__ void split_modes_kernel(int M, int N, int Mpad, int Npad, const doubl
     }
 }
 
+// Q table of one band * 2^sQ -> packed FP16 (hi | lo << 16)
+__global__ void split_q_kernel(size_t n, const float* Q, float scale, uint32_t* out) {
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+        __half h, l;
+        split_half(Q[e] * scale, h, l);
+        out[e] = (uint32_t)__half_as_ushort(h) | ((uint32_t)__half_as_ushort(l) << 16);
+    }
+}
+
 // T^T (FP32) * pow2_scale(max|T|) -> hi/lo FP16
 __global__ void split_t_kernel(size_t n, const float* Tf, const unsigned* maxT, __half* Th, __half* Tl) {
     const float sc = pow2_scale(__uint_as_float(*maxT));
@@ -495,7 +500,7 @@ CUtensorMap make_map(const __half* base, int rows, int cols, int box_rows) {
 
 struct Layout {
     int Npad, Mpad;
-    size_t bh, bl, th, tl, tf, ckey, maxes, tiles, err, total;
+    size_t bh, bl, th, tl, tf, qhl, ckey, maxes, tiles, err, total;
 };
 
 Layout layout_of(const ProjectArgs& a) {
@@ -514,6 +519,7 @@ Layout layout_of(const ProjectArgs& a) {
     L.th = take(half_mat);
     L.tl = take(half_mat);
     L.tf = take(2 * half_mat);
+    L.qhl = take(sizeof(uint32_t) * (size_t)a.ks.nsquare);
     L.ckey = take(sizeof(int4) * L.Npad);
     L.maxes = take(sizeof(unsigned) * (1 + 2 * a.nbands));
     const int nti = L.Mpad / BM, ntj = L.Mpad / BN;
@@ -544,6 +550,7 @@ void launch_project_tc(const ProjectArgs& a, cudaStream_t s, long long* launches
     int2* tiles = reinterpret_cast<int2*>(w + L.tiles);
     int* err = reinterpret_cast<int*>(w + L.err);
     float* Tf = reinterpret_cast<float*>(w + L.tf);
+    uint32_t* Qhl = reinterpret_cast<uint32_t*>(w + L.qhl);
     const int N = a.ncells, M = a.nmodes, nb = a.nbands;
     unsigned* maxT = maxes + 1 + nb;  // per band
 
@@ -594,8 +601,9 @@ void launch_project_tc(const ProjectArgs& a, cudaStream_t s, long long* launches
         p1.Mpad = L.Mpad;
         p1.n_at = n_at;
         p1.ckey = ckey;
-        p1.Q = a.Qsq + (size_t)(1 + p) * a.ks.nsquare;
-        p1.qscale = sQ;
+        split_q_kernel<<<2048, 256, 0, s>>>((size_t)a.ks.nsquare, a.Qsq + (size_t)(1 + p) * a.ks.nsquare, sQ, Qhl);
+        OPSEC_CUDA(cudaGetLastError());
+        p1.Qhl = Qhl;
         p1.out_scale = 1.0f / (sQ * sB);
         p1.Tf = Tf;
         p1.err = err;
@@ -618,7 +626,7 @@ void launch_project_tc(const ProjectArgs& a, cudaStream_t s, long long* launches
         step2_kernel<<<(unsigned)tl.size(), 256, smem, s>>>(mBh128, mBl128, mTh256, mTl256, p2);
         OPSEC_CUDA(cudaGetLastError());
         if (g_clock) g_clock->end(s);
-        *launches += 4;
+        *launches += 5;
     }
     int herr = 0;
     OPSEC_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, s));

@@ -50,6 +50,11 @@ __device__ __forceinline__ double sj0(double x) {
     return (x2 < 1e-4) ? 1 - x2 * (1 / 6. + x2 * (1 / 120. - x2 * (1 / 5040.))) : sin(x) / x;
 }
 
+// second half of the scratch holds mult_j / k_j
+__host__ __device__ inline size_t scratch_half(const XiTableArgs& a) {
+    return (size_t)(kNkXi + 1) + (size_t)a.nbands * (kNkBand + 1);
+}
+
 struct TableSpec {
     int nk;
     double kmin, kmax;
@@ -88,10 +93,15 @@ __global__ void simpson_weights_kernel(XiTableArgs a) {
         mult *= P * (k * k) * exp(-k * k / (1.0 * 1.0));
         mult *= (dk / 3) / kTwoPi2;
         a.scratch[s.off + j] = mult;
+        a.scratch[s.off + j + scratch_half(a)] = (k > 0.0) ? mult / k : 0.0;  // for sin(kr)/(kr) = (1/k) sin(kr) / r
     }
 }
 
-// One warp per (table, r): sum_j mult_j j0(k_j r), FP64.
+// One warp per (table, r): sum_j mult_j j0(k_j r), FP64.  Lane l takes
+// j = l, l+32, ...; sin(k_j r) advances by the angle-addition rotation
+// through 32 dk r and is re-anchored with an exact sincos every 32 steps, so
+// each term costs a few FMAs instead of a sine and a division.  Terms with
+// (k_j r)^2 < 1e-4 use the series of sj0 (Model.cpp:56-59).
 __global__ void xi_sum_kernel(XiTableArgs a) {
     const int n = a.xl.n();
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -102,11 +112,30 @@ __global__ void xi_sum_kernel(XiTableArgs a) {
     const double dk = (s.kmax - s.kmin) / s.nk;
     const double r = a.r[warp];
     const double* mult = a.scratch + s.off;
-    double acc = 0.0;
-    for (int j = lane; j <= s.nk; j += 32) {
-        double k = s.kmin + j * dk;
-        acc += mult[j] * sj0(k * r);
+    const double* minv = a.scratch + s.off + scratch_half(a);
+    double acc_series = 0.0, acc_sin = 0.0;
+    if (r == 0.0) {
+        for (int j = lane; j <= s.nk; j += 32) acc_series += mult[j];
+    } else {
+        double sd, cd;
+        sincos(32.0 * dk * r, &sd, &cd);
+        constexpr int kAnchor = 32;
+        for (int j0 = lane; j0 <= s.nk; j0 += 32 * kAnchor) {
+            double sn, cs;
+            sincos((s.kmin + j0 * dk) * r, &sn, &cs);
+            for (int m = 0, j = j0; m < kAnchor && j <= s.nk; m++, j += 32) {
+                const double x = (s.kmin + j * dk) * r;
+                if (x * x < 1e-4)
+                    acc_series += mult[j] * sj0(x);
+                else
+                    acc_sin += minv[j] * sn;
+                const double sn2 = sn * cd + cs * sd;
+                cs = cs * cd - sn * sd;
+                sn = sn2;
+            }
+        }
     }
+    double acc = acc_series + acc_sin / r;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     if (lane == 0) {
