@@ -135,7 +135,7 @@ __global__ void xi_sum_kernel(XiTableArgs a) {
             }
         }
     }
-    double acc = acc_series + acc_sin / r;
+    double acc = (r > 0.0) ? acc_series + acc_sin / r : acc_series;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     if (lane == 0) {
