@@ -51,6 +51,34 @@ def _compile(src, verbose=False, ptxas_info=False):
     return obj, out
 
 
+PROGRAMS = ("klt", "comma", "dot", "estimate")
+PROG_DIR = os.path.join(HERE, "programs")
+BIN = os.path.join(HERE, "bin")
+
+
+def build_programs():
+    """The drop-in programs klt / comma / dot / estimate, linked against the library."""
+    os.makedirs(BIN, exist_ok=True)
+    common = os.path.join(PROG_DIR, "progs.cpp")
+    hdrs = [os.path.join(PROG_DIR, "progs.h"), os.path.join(os.path.dirname(HERE), "include", "opsec_gpu.h")]
+    cxx = shutil.which("g++") or "g++"
+    out = []
+    for name in PROGRAMS:
+        exe = os.path.join(BIN, name)
+        src = os.path.join(PROG_DIR, name + ".cpp")
+        deps = [src, common, LIB] + hdrs
+        if os.path.exists(exe) and all(os.path.getmtime(exe) >= os.path.getmtime(d) for d in deps):
+            out.append(exe)
+            continue
+        cmd = [cxx, "-O2", "-std=c++17", "-o", exe, src, common, f"-L{HERE}", "-lopsec_gpu",
+               "-Wl,-rpath,$ORIGIN/.."]
+        res = subprocess.run(cmd, capture_output=True, text=True)
+        if res.returncode != 0:
+            raise RuntimeError(f"building {name} failed:\n{res.stdout}\n{res.stderr}")
+        out.append(exe)
+    return out
+
+
 def build(verbose=False, ptxas_info=False, jobs=None):
     os.makedirs(BUILD, exist_ok=True)
     srcs = sources()
@@ -65,6 +93,7 @@ def build(verbose=False, ptxas_info=False, jobs=None):
         if res.returncode != 0:
             raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
         os.replace(LIB + ".tmp", LIB)
+    build_programs()
     return LIB, "".join(r[1] for r in results)
 
 

@@ -255,6 +255,7 @@ struct opsec_gpu {
     int nmodes_cfg = 0;
     int mixing = OPSEC_MIXING_INVERSE;
     std::string projection = "auto";
+    int proj_chunk = 2;
     std::vector<double> pk_k, pk_P;
     std::vector<double> band_lo, band_hi;
 
@@ -456,6 +457,8 @@ void configure(opsec_gpu* c, const std::map<std::string, std::string>& kv) {
     if (has("sig.gauss")) c->ng = to_int("sig.gauss", get("sig.gauss"));
     if (c->ng < 1 || c->ng > 6) fail(OPSEC_ERR_CONFIG, "sig.gauss must be between 1 and 6");
     if (has("projection")) c->projection = get("projection");
+    if (has("projection.chunk")) c->proj_chunk = to_int("projection.chunk", get("projection.chunk"));
+    if (c->proj_chunk < 1) fail(OPSEC_ERR_CONFIG, "projection.chunk must be >= 1");
     if (has("profile")) c->clock.on = get("profile") == "1";
 }
 
@@ -821,6 +824,7 @@ void project_all(opsec_gpu* c, int ncells, int M) {
     a.Qsq = c->Qsq.p;
     a.Bs = c->Bs.p;
     a.Dp = c->Dp.p;
+    a.chunk = c->proj_chunk;
     bool tc = (c->projection != "simt") && project_tc_supported(a);
     if (c->projection == "tc" && !tc) fail(OPSEC_ERR_CONFIG, "projection=tc requested but the shape is not supported");
     size_t wb = tc ? project_tc_work_bytes(a) : sizeof(float) * (size_t)M * ncells;

@@ -152,6 +152,7 @@ struct ProjectArgs {
     float* Dp;             // [nbands][M(M+1)/2] packed output
     void* work;            // scratch
     size_t work_bytes;
+    int chunk = 2;         // tensor-core path: K-slices of 64 per FP32 accumulator chunk
 };
 size_t project_work_bytes(const ProjectArgs& a);
 void launch_project(const ProjectArgs& a, cudaStream_t s, long long* launches);

@@ -38,7 +38,7 @@ constexpr int STAGES = 2;
 constexpr uint32_t A_BYTES = BM * BK * 2;  // one FP16 operand tile, 16 KB
 constexpr uint32_t B_BYTES = BN * BK * 2;  // 32 KB
 constexpr uint32_t STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
-constexpr int TMEM_COLS = 256;
+constexpr int TMEM_COLS = 512;  // [0,256) accumulator D, [256,512) running sum R
 constexpr long long kWaitCycles = 2000000000LL;  // ~1 s at 2 GHz
 
 // instruction descriptor: D=F32, A=B=F16, both K-major, M=128, N=256
@@ -137,6 +137,76 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
     for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
 }
 
+__device__ __forceinline__ void tmem_st32(uint32_t taddr, const float* v) {
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,"
+        "%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32};" ::"r"(taddr),
+        "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])), "r"(__float_as_uint(v[3])),
+        "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])), "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7])),
+        "r"(__float_as_uint(v[8])), "r"(__float_as_uint(v[9])), "r"(__float_as_uint(v[10])), "r"(__float_as_uint(v[11])),
+        "r"(__float_as_uint(v[12])), "r"(__float_as_uint(v[13])), "r"(__float_as_uint(v[14])), "r"(__float_as_uint(v[15])),
+        "r"(__float_as_uint(v[16])), "r"(__float_as_uint(v[17])), "r"(__float_as_uint(v[18])), "r"(__float_as_uint(v[19])),
+        "r"(__float_as_uint(v[20])), "r"(__float_as_uint(v[21])), "r"(__float_as_uint(v[22])), "r"(__float_as_uint(v[23])),
+        "r"(__float_as_uint(v[24])), "r"(__float_as_uint(v[25])), "r"(__float_as_uint(v[26])), "r"(__float_as_uint(v[27])),
+        "r"(__float_as_uint(v[28])), "r"(__float_as_uint(v[29])), "r"(__float_as_uint(v[30])), "r"(__float_as_uint(v[31]))
+        : "memory");
+}
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+
+// The tensor core accumulates FP32 with truncation, so a long K loop biases
+// every sum toward zero by ~1 ulp per MMA.  The K loop is therefore cut into
+// chunks of `chunk` K-slices: the MMA restarts the accumulator D at each
+// chunk, and four drain warps (one per TMEM lane quarter) add D into an FP32
+// running sum R (round to nearest) in the other half of TMEM while the MMA
+// waits.  The last drain hands the final sums to `store(col_block, v[32])`.
+struct ChunkBars {
+    uint32_t chunk_done;  // MMA -> drain warps (tcgen05.commit)
+    uint32_t drained;     // drain warps -> MMA (4 arrivals)
+};
+
+template <class Store>
+__device__ __forceinline__ void drain_loop(uint32_t tmem, int q, int lane, int nchunks, ChunkBars b,
+                                           volatile int* abort_flag, int* err, Store store) {
+    const uint32_t lane_base = (uint32_t)(32 * q) << 16;
+    for (int c = 0; c < nchunks; c++) {
+        if (!mbar_wait(b.chunk_done, c & 1, abort_flag, err)) return;
+        tc_fence_after();
+        const bool last = (c == nchunks - 1);
+        for (int cc = 0; cc < 8; cc++) {
+            float v[32];
+            tmem_ld32(tmem + lane_base + (uint32_t)(32 * cc), v);
+            if (c > 0) {
+                float r[32];
+                tmem_ld32(tmem + lane_base + 256u + (uint32_t)(32 * cc), r);
+#pragma unroll
+                for (int t = 0; t < 32; t++) v[t] += r[t];
+            }
+            if (last)
+                store(cc, v);
+            else
+                tmem_st32(tmem + lane_base + 256u + (uint32_t)(32 * cc), v);
+        }
+        if (!last) {
+            tmem_wait_st();
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(b.drained);
+        }
+    }
+}
+
+// MMA issue for one K-slice of 64 (3-term split), restarting D at chunk starts
+__device__ __forceinline__ void issue_slice(uint32_t tmem, uint64_t ah, uint64_t al, uint64_t bh, uint64_t bl,
+                                            bool first_in_chunk) {
+#pragma unroll
+    for (int kk = 0; kk < BK / 16; kk++) {
+        const uint64_t adv = (uint64_t)(kk * 32) >> 4;
+        umma(tmem, ah + adv, bh + adv, (!first_in_chunk || kk > 0) ? 1u : 0u);
+        umma(tmem, ah + adv, bl + adv, 1u);
+        umma(tmem, al + adv, bh + adv, 1u);
+    }
+}
+
 __device__ __forceinline__ void split_half(float x, __half& h, __half& l) {
     h = __float2half_rn(x);
     l = __float2half_rn(x - __half2float(h));
@@ -159,6 +229,7 @@ struct Step1Params {
     const uint32_t* Qhl;      // square key table of this band, scaled by 2^sQ, FP16 hi | lo << 16
     float out_scale;          // 2^-(sQ + sB): T in its natural units
     float* Tf;                // [Mpad][Npad] T^T, FP32
+    int chunk;                // K-slices per accumulator chunk
     int* err;
 };
 
@@ -172,11 +243,12 @@ __device__ __forceinline__ int pair_key(const KeySpace& ks, int4 a, int4 b) {
     return a.x * ks.H + b.x + df;  // a.x = h_a nf, b.x = h_b nf
 }
 
-__global__ void __launch_bounds__(320, 1)
+// warps: 0 TMA, 1 MMA, 2-9 gather producers, 10-11 idle, 12-15 drain + epilogue (lane quarters 0-3)
+__global__ void __launch_bounds__(512, 1)
     step1_kernel(const __grid_constant__ CUtensorMap mBh, const __grid_constant__ CUtensorMap mBl, Step1Params p) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    __shared__ __align__(8) unsigned long long bar_full[STAGES], bar_empty[STAGES], bar_acc;
+    __shared__ __align__(8) unsigned long long bar_full[STAGES], bar_empty[STAGES], bar_chunk, bar_drained;
     __shared__ uint32_t tmem_slot;
     __shared__ volatile int abort_flag;
     __shared__ int4 rowkey[BM];
@@ -185,6 +257,8 @@ __global__ void __launch_bounds__(320, 1)
     const int jt = blockIdx.x / p.n_at, at = blockIdx.x % p.n_at;
     const int a0 = at * BM, j0 = jt * BN;
     const int nk = p.Npad / BK;
+    const int chunk = p.chunk > 0 ? p.chunk : 1;
+    const int nchunks = (nk + chunk - 1) / chunk;
 
     if (threadIdx.x == 0) {
         abort_flag = 0;
@@ -192,7 +266,8 @@ __global__ void __launch_bounds__(320, 1)
             mbar_init(smem_u32(&bar_full[s]), 1 + 8);
             mbar_init(smem_u32(&bar_empty[s]), 1);
         }
-        mbar_init(smem_u32(&bar_acc), 1);
+        mbar_init(smem_u32(&bar_chunk), 1);
+        mbar_init(smem_u32(&bar_drained), 4);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (threadIdx.x < BM) rowkey[threadIdx.x] = p.ckey[a0 + threadIdx.x];
@@ -223,25 +298,30 @@ __global__ void __launch_bounds__(320, 1)
         // MMA issuer
         for (int k = 0; k < nk; k++) {
             const int s = k % STAGES, n = k / STAGES;
+            const bool first = (k % chunk) == 0;
+            if (first && k > 0) {  // the previous chunk's accumulator must be drained first
+                if (!mbar_wait(smem_u32(&bar_drained), ((k / chunk) - 1) & 1, &abort_flag, p.err)) break;
+            }
             if (!mbar_wait(smem_u32(&bar_full[s]), n & 1, &abort_flag, p.err)) break;
             tc_fence_after();
             if (lane == 0) {
-                const uint64_t ah = sdesc(smem_u32(A_hi(s))), al = sdesc(smem_u32(A_lo(s)));
-                const uint64_t bh = sdesc(smem_u32(B_hi(s))), bl = sdesc(smem_u32(B_lo(s)));
-#pragma unroll
-                for (int kk = 0; kk < BK / 16; kk++) {
-                    const uint64_t adv = (uint64_t)(kk * 32) >> 4;
-                    umma(tmem, ah + adv, bh + adv, (k > 0 || kk > 0) ? 1u : 0u);
-                    umma(tmem, ah + adv, bl + adv, 1u);
-                    umma(tmem, al + adv, bh + adv, 1u);
-                }
+                issue_slice(tmem, sdesc(smem_u32(A_hi(s))), sdesc(smem_u32(A_lo(s))), sdesc(smem_u32(B_hi(s))),
+                            sdesc(smem_u32(B_lo(s))), first);
                 umma_commit(smem_u32(&bar_empty[s]));
+                if ((k % chunk) == chunk - 1 || k == nk - 1) umma_commit(smem_u32(&bar_chunk));
             }
             __syncwarp();
         }
-        if (lane == 0) umma_commit(smem_u32(&bar_acc));
-        __syncwarp();
-    } else {
+    } else if (warp >= 12) {
+        // drain warps + epilogue: T^T[j][a] in natural units
+        const int q = warp & 3;
+        const int a = a0 + 32 * q + lane;
+        drain_loop(tmem, q, lane, nchunks, ChunkBars{smem_u32(&bar_chunk), smem_u32(&bar_drained)}, &abort_flag,
+                   p.err, [&](int cc, const float* v) {
+#pragma unroll
+                       for (int t = 0; t < 32; t++) p.Tf[(size_t)(j0 + 32 * cc + t) * p.Npad + a] = v[t] * p.out_scale;
+                   });
+    } else if (warp < 10) {
         // eight gather producers: warp pw fills rows pw, pw+8, ...; lane covers columns 2 lane, 2 lane + 1.
         // Software-pipelined: the 32 gathers of K-slice k+1 are in flight while the warp waits for
         // its stage to drain and while the tensor core works on slice k.
@@ -275,20 +355,6 @@ __global__ void __launch_bounds__(320, 1)
             if (lane == 0) mbar_arrive(smem_u32(&bar_full[s]));
             if (k + 1 < nk) gather(k + 1);
         }
-        // epilogue: warps 4..7 own TMEM lane quarters 0..3
-        if (warp >= 4 && warp < 8) {
-            const int q = warp & 3;
-            if (mbar_wait(smem_u32(&bar_acc), 0, &abort_flag, p.err)) {
-                tc_fence_after();
-                const int a = a0 + 32 * q + lane;
-                for (int cc = 0; cc < BN / 32; cc++) {
-                    float v[32];
-                    tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(32 * cc), v);
-#pragma unroll
-                    for (int t = 0; t < 32; t++) p.Tf[(size_t)(j0 + 32 * cc + t) * p.Npad + a] = v[t] * p.out_scale;
-                }
-            }
-        }
     }
     tc_fence_before();
     __syncthreads();
@@ -305,6 +371,7 @@ struct Step2Params {
     float sB;           // scale of B'
     const unsigned* maxT;  // max |T| of this band (float bits); T was scaled by pow2_scale(maxT)
     float* Dp;          // packed output of this band
+    int chunk;          // K-slices per accumulator chunk
     int* err;
 };
 
@@ -313,7 +380,7 @@ __global__ void __launch_bounds__(256, 1)
                  const __grid_constant__ CUtensorMap mTh, const __grid_constant__ CUtensorMap mTl, Step2Params p) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    __shared__ __align__(8) unsigned long long bar_full[STAGES], bar_empty[STAGES], bar_acc;
+    __shared__ __align__(8) unsigned long long bar_full[STAGES], bar_empty[STAGES], bar_chunk, bar_drained;
     __shared__ uint32_t tmem_slot;
     __shared__ volatile int abort_flag;
 
@@ -321,6 +388,8 @@ __global__ void __launch_bounds__(256, 1)
     const int2 tile = p.tiles[blockIdx.x];
     const int i0 = tile.x * BM, j0 = tile.y * BN;
     const int nk = p.Npad / BK;
+    const int chunk = p.chunk > 0 ? p.chunk : 1;
+    const int nchunks = (nk + chunk - 1) / chunk;
 
     if (threadIdx.x == 0) {
         abort_flag = 0;
@@ -328,7 +397,8 @@ __global__ void __launch_bounds__(256, 1)
             mbar_init(smem_u32(&bar_full[s]), 1);
             mbar_init(smem_u32(&bar_empty[s]), 1);
         }
-        mbar_init(smem_u32(&bar_acc), 1);
+        mbar_init(smem_u32(&bar_chunk), 1);
+        mbar_init(smem_u32(&bar_drained), 4);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) tmem_alloc(smem_u32(&tmem_slot));
@@ -358,40 +428,32 @@ __global__ void __launch_bounds__(256, 1)
     } else if (warp == 1) {
         for (int k = 0; k < nk; k++) {
             const int s = k % STAGES, n = k / STAGES;
+            const bool first = (k % chunk) == 0;
+            if (first && k > 0) {
+                if (!mbar_wait(smem_u32(&bar_drained), ((k / chunk) - 1) & 1, &abort_flag, p.err)) break;
+            }
             if (!mbar_wait(smem_u32(&bar_full[s]), n & 1, &abort_flag, p.err)) break;
             tc_fence_after();
             if (lane == 0) {
-                const uint64_t ah = sdesc(smem_u32(A_hi(s))), al = sdesc(smem_u32(A_lo(s)));
-                const uint64_t bh = sdesc(smem_u32(B_hi(s))), bl = sdesc(smem_u32(B_lo(s)));
-#pragma unroll
-                for (int kk = 0; kk < BK / 16; kk++) {
-                    const uint64_t adv = (uint64_t)(kk * 32) >> 4;
-                    umma(tmem, ah + adv, bh + adv, (k > 0 || kk > 0) ? 1u : 0u);
-                    umma(tmem, ah + adv, bl + adv, 1u);
-                    umma(tmem, al + adv, bh + adv, 1u);
-                }
+                issue_slice(tmem, sdesc(smem_u32(A_hi(s))), sdesc(smem_u32(A_lo(s))), sdesc(smem_u32(B_hi(s))),
+                            sdesc(smem_u32(B_lo(s))), first);
                 umma_commit(smem_u32(&bar_empty[s]));
+                if ((k % chunk) == chunk - 1 || k == nk - 1) umma_commit(smem_u32(&bar_chunk));
             }
             __syncwarp();
         }
-        if (lane == 0) umma_commit(smem_u32(&bar_acc));
-        __syncwarp();
     } else if (warp >= 4) {
         const int q = warp & 3;
-        if (mbar_wait(smem_u32(&bar_acc), 0, &abort_flag, p.err)) {
-            tc_fence_after();
-            const float out_scale = 1.0f / (p.sB * pow2_scale(__uint_as_float(*p.maxT)));
-            const int i = i0 + 32 * q + lane;
-            for (int cc = 0; cc < BN / 32; cc++) {
-                float v[32];
-                tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(32 * cc), v);
+        const float out_scale = 1.0f / (p.sB * pow2_scale(__uint_as_float(*p.maxT)));
+        const int i = i0 + 32 * q + lane;
+        drain_loop(tmem, q, lane, nchunks, ChunkBars{smem_u32(&bar_chunk), smem_u32(&bar_drained)}, &abort_flag,
+                   p.err, [&](int cc, const float* v) {
 #pragma unroll
-                for (int t = 0; t < 32; t++) {
-                    const int j = j0 + 32 * cc + t;
-                    if (i <= j && j < p.M) p.Dp[(size_t)j * (j + 1) / 2 + i] = v[t] * out_scale;
-                }
-            }
-        }
+                       for (int t = 0; t < 32; t++) {
+                           const int j = j0 + 32 * cc + t;
+                           if (i <= j && j < p.M) p.Dp[(size_t)j * (j + 1) / 2 + i] = v[t] * out_scale;
+                       }
+                   });
     }
     tc_fence_before();
     __syncthreads();
@@ -606,9 +668,10 @@ void launch_project_tc(const ProjectArgs& a, cudaStream_t s, long long* launches
         p1.Qhl = Qhl;
         p1.out_scale = 1.0f / (sQ * sB);
         p1.Tf = Tf;
+        p1.chunk = a.chunk;
         p1.err = err;
         if (g_clock) g_clock->begin("project_step1", s, 2.0 * N * (double)N * M);
-        step1_kernel<<<n_at * n_jt, 320, smem, s>>>(mBh256, mBl256, p1);
+        step1_kernel<<<n_at * n_jt, 512, smem, s>>>(mBh256, mBl256, p1);
         OPSEC_CUDA(cudaGetLastError());
         if (g_clock) g_clock->end(s);
         absmax_f32_kernel<<<dim3(2048, 1), 256, 0, s>>>(1, nT, Tf, maxT + p);
@@ -620,6 +683,7 @@ void launch_project_tc(const ProjectArgs& a, cudaStream_t s, long long* launches
         p2.tiles = tiles;
         p2.sB = sB;
         p2.maxT = maxT + p;
+        p2.chunk = a.chunk;
         p2.Dp = a.Dp + (size_t)p * ((size_t)M * (M + 1) / 2);
         p2.err = err;
         if (g_clock) g_clock->begin("project_step2", s, (double)N * M * (double)(M + 1));

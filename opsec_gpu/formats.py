@@ -1,0 +1,106 @@
+"""Annotated binary (ABN) files and key = value configuration, in Python.
+
+The layout is the reference's (code/opsec/src/abn.h:13-60, abn.c:150-330):
+free text and ``key = value`` lines, then the line
+``#!Begin data block: n = N, size = S, endian = E, format = F`` followed by
+N*S raw bytes; several blocks may follow each other (the estfile holds seven).
+Used by the tests and by callers that want to read or write the programs'
+files from Python.
+"""
+from __future__ import annotations
+
+import re
+import sys
+
+import numpy as np
+
+from .synth import CELL_DTYPE
+
+_BEGIN = re.compile(rb"#!Begin data block: n = (\d+), size = (\d+), endian = (\S), format = (\S+)")
+_DTYPES = {"d": "f8", "f": "f4", "i": "i4", "q": "i8", "4i8d": None}
+
+
+def parse_config(text: str) -> dict:
+    """cfg_read_line semantics: '#' comments, key = value, quotes stripped."""
+    out = {}
+    for line in text.splitlines():
+        s = line.strip()
+        if not s or s.startswith("#") or "=" not in s:
+            continue
+        k, v = s.split("=", 1)
+        k, v = k.strip(), v.strip()
+        if len(v) >= 2 and v[0] == v[-1] and v[0] in "\"'":
+            v = v[1:-1]
+        if k:
+            out[k] = v
+    return out
+
+
+def _dtype(fmt: str, size: int, endian: str):
+    e = "<" if endian == "L" else ">"
+    if fmt == "4i8d":
+        dt = CELL_DTYPE if e == "<" else CELL_DTYPE.newbyteorder(">")
+        return dt
+    code = _DTYPES.get(fmt)
+    if code is None:
+        return np.dtype(f"V{size}")
+    return np.dtype(e + code)
+
+
+def read_blocks(path: str):
+    """All data blocks of an ABN file: list of (opts, array)."""
+    data = open(path, "rb").read()
+    pos = 0
+    blocks = []
+    while True:
+        m = _BEGIN.search(data, pos)
+        if not m:
+            break
+        header = data[pos:m.start()].decode("ascii", "replace")
+        n, size, endian, fmt = int(m.group(1)), int(m.group(2)), m.group(3).decode(), m.group(4).decode()
+        start = data.index(b"\n", m.end()) + 1
+        dt = _dtype(fmt, size, endian)
+        arr = np.frombuffer(data[start:start + n * size], dtype=dt, count=n).copy()
+        blocks.append((parse_config(header), arr))
+        pos = start + n * size
+    return blocks
+
+
+def read(path: str):
+    """The first data block: (opts, array)."""
+    b = read_blocks(path)
+    if not b:
+        raise ValueError(f"{path}: no ABN data block")
+    return b[0]
+
+
+def write(f, array, fmt: str, opts: dict | None = None, comment: str = ""):
+    """Append one block to an open binary file (abn_write, abn.c:247-270)."""
+    a = np.ascontiguousarray(array)
+    size = a.dtype.itemsize
+    endian = "L" if sys.byteorder == "little" else "B"
+    head = comment + "\n"
+    for k, v in (opts or {}).items():
+        head += f"{k} = {v}\n"
+    head += f"#!Begin data block: n = {a.size}, size = {size}, endian = {endian}, format = {fmt}\n"
+    f.write(head.encode())
+    f.write(a.tobytes())
+
+
+def write_cells(path: str, cells, survey_lines=()):
+    """A cellfile as basis writes it (basis.cpp:197-201): survey options, Ncells, 4i8d records."""
+    opts = parse_config("\n".join(survey_lines))
+    opts["Ncells"] = str(len(cells))
+    with open(path, "wb") as f:
+        write(f, np.asarray(cells, dtype=CELL_DTYPE), "4i8d", opts)
+
+
+def read_estfile(path: str):
+    """The seven records of an estfile (estimate-mpi.cpp:635-641)."""
+    b = read_blocks(path)
+    nb = int(b[0][0]["Nparams"])
+    names = ["phat", "pcov", "F", "W", "M", "q", "f"]
+    out = {}
+    for name, (_, arr) in zip(names, b):
+        out[name] = arr.reshape(nb, nb) if arr.size == nb * nb and name in ("pcov", "F", "W", "M") else arr
+    return out

@@ -1,0 +1,286 @@
+// progs.cpp -- configuration, ABN and cell-file handling for the programs.
+#include "progs.h"
+
+#include <unistd.h>
+
+#include <cctype>
+#include <cerrno>
+#include <cstdint>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+
+namespace progs {
+
+const std::string& Config::get(const std::string& k) const {
+    static const std::string empty;
+    auto it = kv.find(k);
+    return it == kv.end() ? empty : it->second;
+}
+
+int Config::get_int(const std::string& k) const { return std::atoi(get(k).c_str()); }
+
+void Config::set(const std::string& k, const std::string& v) {
+    if (!kv.count(k)) order.push_back(k);
+    kv[k] = v;
+}
+
+// cfg_read_line (cfg.c:238-295): blank and '#' lines ignored, key = value,
+// whitespace trimmed, one pair of surrounding quotes stripped
+void Config::read_line(const std::string& line) {
+    size_t p = line.find_first_not_of(" \t\r\n");
+    if (p == std::string::npos || line[p] == '#') return;
+    size_t eq = line.find('=', p);
+    if (eq == std::string::npos || eq == p) {
+        std::fprintf(stderr, "cfg_read_line: '%s' is not a valid configuration line\n", line.c_str());
+        return;
+    }
+    std::string key = line.substr(p, eq - p);
+    key.erase(key.find_last_not_of(" \t") + 1);
+    std::string val = line.substr(eq + 1);
+    size_t vb = val.find_first_not_of(" \t\r\n");
+    val = vb == std::string::npos ? std::string() : val.substr(vb);
+    val.erase(val.find_last_not_of(" \t\r\n") + 1);
+    if (val.size() >= 2 && ((val.front() == '"' && val.back() == '"') || (val.front() == '\'' && val.back() == '\'')))
+        val = val.substr(1, val.size() - 2);
+    set(key, val);
+}
+
+bool Config::read_file(const std::string& path) {
+    std::ifstream in(path);
+    if (!in) return false;
+    std::string line;
+    while (std::getline(in, line)) read_line(line);
+    return true;
+}
+
+std::string Config::missing(const std::string& keys) const {
+    std::string out;
+    std::stringstream ss(keys);
+    std::string k;
+    while (std::getline(ss, k, ','))
+        if (!has(k)) out += (out.empty() ? "" : ",") + k;
+    return out;
+}
+
+std::string Config::text() const {
+    std::string t;
+    for (const auto& k : order) t += k + " = " + kv.at(k) + "\n";
+    return t;
+}
+
+Config init(int argc, char** argv, const char* usage) {
+    Config cfg;
+    int opt;
+    opterr = 0;
+    while ((opt = getopt(argc, argv, "hc:")) != -1) {
+        switch (opt) {
+        case 'h':
+            std::fputs(usage, stdout);
+            std::exit(0);
+        case 'c':
+            if (!cfg.read_file(optarg)) {
+                std::fprintf(stderr, "cfg_read_file: could not read file '%s'\n", optarg);
+                std::exit(1);
+            }
+            break;
+        default:
+            std::fputs(usage, stdout);
+            std::exit(1);
+        }
+    }
+    for (int i = optind; i < argc; i++) cfg.read_line(argv[i]);
+    return cfg;
+}
+
+void die(const char* prog, const std::string& msg) {
+    std::fprintf(stderr, "%s: %s\n", prog, msg.c_str());
+    std::exit(1);
+}
+
+char host_endian() {
+    const uint16_t one = 1;
+    return *reinterpret_cast<const unsigned char*>(&one) ? 'L' : 'B';
+}
+
+// abn_calcsize (abn.c:16-82): struct-module codes with repeat counts
+int abn_calcsize(const std::string& fmt) {
+    int size = 0;
+    size_t i = 0;
+    while (i < fmt.size()) {
+        while (i < fmt.size() && std::isspace((unsigned char)fmt[i])) i++;
+        if (i >= fmt.size()) break;
+        int num = 0;
+        bool have = false;
+        while (i < fmt.size() && std::isdigit((unsigned char)fmt[i])) {
+            num = num * 10 + (fmt[i] - '0');
+            i++;
+            have = true;
+        }
+        if (!have) num = 1;
+        if (i >= fmt.size()) return -1;
+        switch (fmt[i]) {
+        case 'x': case 'c': case 'b': case 'B': size += num; break;
+        case 'h': case 'H': size += num * 2; break;
+        case 'i': case 'I': size += num * 4; break;
+        case 'l': case 'L': size += num * (int)sizeof(long); break;
+        case 'q': case 'Q': size += num * 8; break;
+        case 'f': size += num * 4; break;
+        case 'd': size += num * 8; break;
+        default: return -1;
+        }
+        i++;
+    }
+    return size;
+}
+
+static std::vector<int> field_sizes(const std::string& fmt) {
+    std::vector<int> f;
+    size_t i = 0;
+    while (i < fmt.size()) {
+        int num = 0;
+        bool have = false;
+        while (i < fmt.size() && std::isdigit((unsigned char)fmt[i])) {
+            num = num * 10 + (fmt[i] - '0');
+            i++;
+            have = true;
+        }
+        if (!have) num = 1;
+        if (i >= fmt.size()) break;
+        int len = abn_calcsize(std::string(1, fmt[i]));
+        for (int k = 0; k < num; k++) f.push_back(len);
+        i++;
+    }
+    return f;
+}
+
+bool abn_read_header(FILE* f, AbnHeader& h) {
+    char line[4096];
+    while (std::fgets(line, sizeof line, f)) {
+        unsigned long long n = 0, size = 0;
+        char endian = 0;
+        char fmt[256] = {0};
+        if (std::sscanf(line, "#!Begin data block: n = %llu, size = %llu, endian = %c, format = %255s", &n, &size,
+                        &endian, fmt) == 4) {
+            h.n = (size_t)n;
+            h.size = (size_t)size;
+            h.endian = endian;
+            h.format = fmt;
+            return true;
+        }
+        h.opts.read_line(line);
+    }
+    return false;
+}
+
+bool abn_read(FILE* f, AbnHeader& h, std::vector<char>& data) {
+    if (!abn_read_header(f, h)) return false;
+    data.resize(h.n * h.size);
+    if (h.n && std::fread(data.data(), h.size, h.n, f) != h.n) return false;
+    if (h.endian != host_endian()) {
+        std::vector<int> fs = field_sizes(h.format);
+        char* p = data.data();
+        for (size_t e = 0; e < h.n; e++)
+            for (int len : fs) {
+                for (int k = 0; k < len / 2; k++) std::swap(p[k], p[len - 1 - k]);
+                p += len;
+            }
+    }
+    return true;
+}
+
+void abn_write_header(FILE* f, size_t n, const char* fmt, const Config* opts) {
+    std::fprintf(f, "\n");
+    if (opts)
+        for (const auto& k : opts->order) {
+            const std::string& v = opts->kv.at(k);
+            bool quote = !v.empty() && (std::isspace((unsigned char)v.front()) || std::isspace((unsigned char)v.back()));
+            std::fprintf(f, quote ? "%s = \"%s\"\n" : "%s = %s\n", k.c_str(), v.c_str());
+        }
+    std::fprintf(f, "#!Begin data block: n = %zu, size = %i, endian = %c, format = %s\n", n, abn_calcsize(fmt),
+                 host_endian(), fmt);
+}
+
+void abn_write(FILE* f, const void* data, size_t n, const char* fmt, const Config* opts) {
+    abn_write_header(f, n, fmt, opts);
+    std::fwrite(data, abn_calcsize(fmt), n, f);
+}
+
+std::vector<opsec_cell> read_cells(const std::string& path, std::string& err) {
+    std::vector<opsec_cell> cells;
+    FILE* f = std::fopen(path.c_str(), "rb");
+    if (!f) {
+        err = "could not open '" + path + "'";
+        return cells;
+    }
+    AbnHeader h;
+    std::vector<char> data;
+    bool ok = abn_read(f, h, data);
+    std::fclose(f);
+    if (!ok) {
+        err = "error reading cells from '" + path + "'";
+        return cells;
+    }
+    if (h.size != sizeof(opsec_cell) || abn_calcsize(h.format) != (int)sizeof(opsec_cell)) {
+        err = "cell size mismatch in '" + path + "' (format " + h.format + ")";
+        return cells;
+    }
+    if (h.opts.has("Ncells") && (size_t)h.opts.get_int("Ncells") != h.n) {
+        err = "consistency check fail for Ncells in '" + path + "'";
+        return cells;
+    }
+    cells.resize(h.n);
+    std::memcpy(cells.data(), data.data(), data.size());
+    return cells;
+}
+
+bool read_modes(const std::string& path, int& nmodes, int& ncells, std::vector<double>& modes, std::string& err) {
+    FILE* f = std::fopen(path.c_str(), "rb");
+    if (!f) {
+        err = "could not open '" + path + "'";
+        return false;
+    }
+    AbnHeader h;
+    std::vector<char> data;
+    bool ok = abn_read(f, h, data);
+    std::fclose(f);
+    nmodes = h.opts.get_int("Nmodes");
+    ncells = h.opts.get_int("Ncells");
+    if (!ok || nmodes <= 0 || ncells <= 0 || h.n != (size_t)nmodes * ncells || h.size != sizeof(double)) {
+        err = "error reading '" + path + "'";  // ReadModesHeader (sig.cpp:617-641)
+        return false;
+    }
+    modes.resize(h.n);
+    std::memcpy(modes.data(), data.data(), data.size());
+    return true;
+}
+
+bool read_doubles(const std::string& path, std::vector<double>& v, Config* opts, std::string& err) {
+    FILE* f = std::fopen(path.c_str(), "rb");
+    if (!f) {
+        err = "could not open '" + path + "'";
+        return false;
+    }
+    AbnHeader h;
+    std::vector<char> data;
+    bool ok = abn_read(f, h, data);
+    std::fclose(f);
+    if (!ok || h.size != sizeof(double)) {
+        err = "error reading '" + path + "'";
+        return false;
+    }
+    v.resize(h.n);
+    std::memcpy(v.data(), data.data(), data.size());
+    if (opts) *opts = h.opts;
+    return true;
+}
+
+opsec_gpu* make_context(const char* prog, const Config& cfg) {
+    opsec_gpu* g = nullptr;
+    int rc = opsec_gpu_create(&g, cfg.text().c_str());
+    if (rc != OPSEC_OK) die(prog, std::string("configuration: ") + opsec_gpu_last_error(g));
+    return g;
+}
+
+}  // namespace progs

@@ -24,6 +24,7 @@
 #include "Spline.h"
 #include "TestModel.h"
 #include "XiFunc.h"
+#include "abn.h"
 #include "cfg.h"
 #include "sig.h"
 
@@ -160,5 +161,21 @@ void ref_signal_block(int coordsys, const double* grid, const int* n, double L, 
 }
 
 int ref_sizeof_cell() { return (int)sizeof(Cell); }
+
+// A cellfile written by the reference's own ABN writer with the header basis
+// puts in it (basis.cpp:195-201): survey options, then Ncells.
+int ref_write_cells(const char* path, int coordsys, const double* grid, const int* n, double L, int ncells,
+                    const void* cells) {
+    Survey* sv = make_survey(coordsys, grid, n, L);
+    Config opts = sv->GetConfigurationOptions();
+    cfg_set_int(opts, "Ncells", ncells);
+    FILE* f = fopen(path, "w");
+    if (!f) return 1;
+    abn_write(f, cells, ncells, CELL_FMT_STRING, opts);
+    fclose(f);
+    cfg_destroy(opts);
+    delete sv;
+    return 0;
+}
 
 }  // extern "C"

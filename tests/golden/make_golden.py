@@ -52,6 +52,7 @@ def load_ref():
     R.ref_signal_block.argtypes = [C.c_int, dp, ip, C.c_double, C.c_int, C.c_void_p, C.c_int, ip, C.c_int, ip, dp,
                                    C.c_int, C.c_int, C.c_int, dp, dp, C.c_double, C.c_double]
     R.ref_sizeof_cell.restype = C.c_int
+    R.ref_write_cells.argtypes = [C.c_char_p, C.c_int, dp, ip, C.c_double, C.c_int, C.c_void_p]
     assert R.ref_sizeof_cell() == 80
     return R
 
@@ -136,6 +137,13 @@ def main():
         out[f"block_{name}_n"] = np.array(sv.n, dtype=np.int32)
         out[f"block_{name}_L"] = sv.L
         out[f"block_{name}_S"] = S
+
+    # a cellfile written by the reference's ABN writer (basis.cpp:195-201 header)
+    sv, cells = synth.shell_survey(3, 4, 6)
+    path = os.path.join(HERE, "cells_ref.abn")
+    assert R.ref_write_cells(path.encode(), sv.coordsys, np.array(sv.bounds, dtype=np.float64),
+                             np.array(sv.n, dtype=np.int32), sv.L, cells.size, cells.ctypes.data) == 0
+    out["cells_ref"] = cells
 
     np.savez_compressed(os.path.join(HERE, "reference_vectors.npz"), **out)
     print("wrote", os.path.join(HERE, "reference_vectors.npz"))
