@@ -223,6 +223,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="c2")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--set", action="append", default=[], metavar="KEY=VALUE",
+                    help="extra configuration line for the engine, e.g. cubature.precision=fast")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -273,7 +275,7 @@ def main():
     bands = synth.band_edges(w["nbands"], 0.0, w["kmax"])
     counts = synth.grf_counts(sv, cells, seed_field=1 + rank, seed_poisson=2 + rank)
     cfg = api.make_config(sv, bands=bands, nmodes=w["nmodes"], layout=w["layout"], gauss=w["gauss"],
-                          extra=["profile = 1"])
+                          extra=["profile = 1"] + [kv.replace("=", " = ", 1) for kv in args.set])
     eng = api.Engine(cfg)
     eng.set_pk(k, P)
 
@@ -341,7 +343,8 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f16x3+f32+f64", "data": "synthetic",
             "config": {"workload": w["name"], "cells": int(cells.size), "bands": nb, "modes": w["nmodes"],
                        "xi_table": "256 linear + 4096 log r", "gauss_points": f"{w['gauss']}^3 x {w['gauss']}^3",
-                       "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (Q tables 2.9 GB)"},
+                       "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (Q tables 2.9 GB)",
+                       **({"engine_options": args.set} if args.set else {})},
             "e2e": {"value": per_build_wall / world, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},
             "stages_ms": {n: v / args.steps for n, v in stage_tot.items()},

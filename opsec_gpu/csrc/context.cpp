@@ -255,7 +255,8 @@ struct opsec_gpu {
     int nmodes_cfg = 0;
     int mixing = OPSEC_MIXING_INVERSE;
     std::string projection = "auto";
-    int proj_chunk = 2;
+    int proj_chunk = 1;
+    int cub_exact = 1;
     std::vector<double> pk_k, pk_P;
     std::vector<double> band_lo, band_hi;
 
@@ -268,6 +269,7 @@ struct opsec_gpu {
     DevBuf<double> Q;      // [ntab][nkeys]
     DevBuf<float> Qsq;     // [ntab][nsquare]
     DevBuf<double> nodes;  // node tables for the cubature kernel
+    DevBuf<float> cubpts;  // cubature point table, 8 floats per Gauss point of every cell
     DevBuf<int> cell_i;    // d1,d2,d3 then h,f,g per cell
     DevBuf<double> nbar;
     DevBuf<int> rc;        // rows/cols for signal blocks
@@ -459,6 +461,15 @@ void configure(opsec_gpu* c, const std::map<std::string, std::string>& kv) {
     if (has("projection")) c->projection = get("projection");
     if (has("projection.chunk")) c->proj_chunk = to_int("projection.chunk", get("projection.chunk"));
     if (c->proj_chunk < 1) fail(OPSEC_ERR_CONFIG, "projection.chunk must be >= 1");
+    if (has("cubature.precision")) {
+        const std::string& v = get("cubature.precision");
+        if (v == "exact")
+            c->cub_exact = 1;
+        else if (v == "fast")
+            c->cub_exact = 0;
+        else
+            fail(OPSEC_ERR_CONFIG, "cubature.precision must be exact or fast");
+    }
     if (has("profile")) c->clock.on = get("profile") == "1";
 }
 
@@ -599,6 +610,9 @@ void build_q(opsec_gpu* c) {
     a.ntab = c->ntab();
     a.tab32 = c->xi32.p;
     a.Q = c->Q.p;
+    c->cubpts.alloc(8 * cubature_point_count(c->ks, ng));
+    a.pts = reinterpret_cast<float4*>(c->cubpts.p);
+    a.exact = c->cub_exact;
     launch_cubature(a, c->stream, &c->launches);
     sync(c);
     c->q_ok = true;

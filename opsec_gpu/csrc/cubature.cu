@@ -6,42 +6,70 @@
 // that the map is volume-uniform (sig.cpp:453-458).
 //
 // Layout and precision:
+//  * a point table holds every Gauss point of every grid cell once, as an
+//    FP32 pair (hi, lo) with hi + lo = the FP64 position to ~1e-14, and its
+//    FP32 weight: [cell][point][hi, lo] float4s, built by one kernel per
+//    build, so the per-key setup is FP32 arithmetic (FP64 runs at 1/64 of
+//    the FP32 rate on this part);
 //  * one warp integrates one key; a CTA holds G xi tables in shared memory
-//    (FP32) and loops its warps over keys;
-//  * the 2 ng^3 Gauss points of the pair are built in FP64 from per-axis node
-//    tables, shifted to the first cell (pair-relative coordinates) and stored
-//    in FP32 in the warp's slice of shared memory, so FP32 differences keep
-//    ~1e-7 relative accuracy at every separation;
-//  * per lane: FP32 distance, log2 index into the table, linear interpolation
-//    (the QSpline rule, QSpline.cpp:61-70) and FP32 sums over the ng^3 points
-//    of the second cell; FP64 for the outer sum and the warp reduction.
+//    (FP32) and loops its warps over keys.  The second cell's points are
+//    shifted to the first cell's middle point (pair-relative coordinates) and
+//    staged in the warp's slice of shared memory; each lane keeps its own
+//    first-cell point in registers;
+//  * exact mode (the default): the separation of a point pair is formed as
+//    an FP32 pair by Knuth's two-sum, r^2 as an FP32 pair by FMA two-product
+//    and two-sum, and the table index from log2(r^2) = E + log2(T_k) +
+//    log2(1 + delta), with E the binary exponent of r^2, T_k = 1 + k/128 from
+//    its top 7 mantissa bits and delta < 1/128 from the FP32 pair; in the
+//    linear section t = r n1/r1 takes r and n1/r1 as FP32 pairs and the
+//    fraction from the FMA residual of the rounded product.  The fraction of
+//    the index is then good to ~3e-7 of a grid step at every r, and the error
+//    left is that of the FP32 tables (~1e-7 of max|Q| per band);
+//  * fast mode: one FP32 separation, sqrt and hardware log2 of the mantissa;
+//    the fraction of the index then carries the ~6e-8 relative rounding of r,
+//    i.e. a phase error k r 6e-8 in an oscillating band table;
+//  * FP32 sums over the ng^3 points of the second cell; FP64 for the outer
+//    sum and the warp reduction.
 // Periodic boxes wrap each pair difference into [-L/2, L/2) (BoxSurvey.cpp:26-30).
 #include <cmath>
+#include <cstring>
 
 #include "engine.h"
 
 namespace opsec {
 namespace {
 
-
 // Table index of a distance r.  Linear section: t = r n1 / r1.  Log section:
-// t = n1 + (log2 r - log2 r1) (n2-1) / log2(r2/r1).  To keep the fraction of
-// t at the precision of r itself, log2 r is split into its binary exponent e
-// and log2 of the mantissa m in [1, 2) (the hardware log2 is accurate to
-// ~2^-22 absolute there), and the offset of each exponent,
-// c_e = n1 + (e - log2 r1) (n2-1)/log2(r2/r1), is precomputed in FP64 as an
-// integer part plus an FP32 fraction.
+// t = n1 + (log2 r - log2 r1) (n2-1) / log2(r2/r1).  log2 is split into the
+// binary exponent e of the argument and the log2 of its mantissa, and the
+// offset of each exponent, c_e, is precomputed in FP64 as an integer part
+// plus an FP32 fraction.  Fast mode takes the exponent of r, exact mode the
+// exponent of r^2 (c_e = n1 + (e/2 - log2 r1) (n2-1)/log2(r2/r1)).
 constexpr int kMaxExp = 64;
+constexpr int kLogBits = 7;
+constexpr int kLogN = 1 << kLogBits;
 struct Lookup {
     float inv_dr;   // n1 / r1: index in the linear section
-    float r1;
+    float inv_dr_lo;  // n1 / r1 - inv_dr
+    float r1, r1sq;
     float inv_du;   // (n2-1) / log2(r2/r1)
+    float cp;       // exact mode: (n2-1) / log2(r2/r1) / (2 ln 2), index per unit of ln(1 + delta)
     int n1;
     int imax;       // n - 2
     int e0;         // smallest exponent held in the offset table
     int ne;         // entries in the offset table
     int ci[kMaxExp];    // integer part of c_e
     float cf[kMaxExp];  // fraction of c_e
+    // exact mode, per k < 128: (1/T_k, fraction of z_k, integer part of z_k, 0),
+    // z_k = log2(T_k) (n2-1) / log2(r2/r1) / 2
+    float4 kt[kLogN];
+};
+
+template <int NG>
+struct Shape {
+    static constexpr int NP = NG * NG * NG;
+    // 16 warps per CTA (twice the latency hiding) while the point buffers leave room for tables
+    static constexpr int kWarps = NG <= 4 ? 16 : 8;
 };
 
 __device__ __forceinline__ void decode_key(const KeySpace& ks, long long key, int* c1, int* c2) {
@@ -67,60 +95,110 @@ __device__ __forceinline__ void decode_key(const KeySpace& ks, long long key, in
     c2[0] = hb / ks.N2; c2[1] = hb % ks.N2; c2[2] = df;
 }
 
-template <int NG>
-__device__ __forceinline__ void point_xyz(const CubatureArgs& a, const int* c, int p, double* x, double* w) {
-    const int i = p / (NG * NG), j = (p / NG) % NG, l = p % NG;
-    *w = a.w[i] * a.w[j] * a.w[l];
-    if (a.coordsys == 1) {
-        x[0] = a.node1[c[0] * NG + i];
-        x[1] = a.node2[c[1] * NG + j];
-        x[2] = a.node3[c[2] * NG + l];
-    } else {
-        const double r = a.node1[c[0] * NG + i];
-        const double mu = a.node2[c[1] * NG + j];
-        const double s = a.snode2[c[1] * NG + j];
-        const double rs = r * s;
-        x[0] = rs * a.cphi[c[2] * NG + l];
-        x[1] = rs * a.sphi[c[2] * NG + l];
-        x[2] = r * mu;
+// Knuth's two-sum: s + e == a + b exactly.  The _rn intrinsics keep the
+// compiler from contracting a product that feeds these sums into an FMA.
+__device__ __forceinline__ float two_sum(float a, float b, float* e) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    *e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return s;
+}
+
+// (hi, lo) of b - a for FP32 pairs
+__device__ __forceinline__ float diff2(float bh, float bl, float ah, float al, float* lo) {
+    float e;
+    const float s = two_sum(bh, -ah, &e);
+    *lo = e + (bl - al);
+    return s;
+}
+
+// Gauss points of every cell: [cell][p] -> hi (x, y, z, w), lo (x, y, z, 0).
+__global__ void point_table_kernel(CubatureArgs a, int ng, long long ncell) {
+    const int np = ng * ng * ng;
+    const long long n = ncell * np;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        const long long cell = t / np;
+        const int p = (int)(t % np);
+        const int c2 = (int)(cell % a.ks.N3);
+        const int c1 = (int)((cell / a.ks.N3) % a.ks.N2);
+        const int c0 = (int)(cell / ((long long)a.ks.N3 * a.ks.N2));
+        const int i = p / (ng * ng), j = (p / ng) % ng, l = p % ng;
+        const double w = a.w[i] * a.w[j] * a.w[l];
+        double x[3];
+        if (a.coordsys == 1) {
+            x[0] = a.node1[c0 * ng + i];
+            x[1] = a.node2[c1 * ng + j];
+            x[2] = a.node3[c2 * ng + l];
+        } else {
+            const double r = a.node1[c0 * ng + i];
+            const double mu = a.node2[c1 * ng + j];
+            const double rs = r * a.snode2[c1 * ng + j];
+            x[0] = rs * a.cphi[c2 * ng + l];
+            x[1] = rs * a.sphi[c2 * ng + l];
+            x[2] = r * mu;
+        }
+        float h[3], lo[3];
+        for (int d = 0; d < 3; d++) {
+            h[d] = (float)x[d];
+            lo[d] = (float)(x[d] - (double)h[d]);
+        }
+        a.pts[2 * t] = make_float4(h[0], h[1], h[2], (float)w);
+        a.pts[2 * t + 1] = make_float4(lo[0], lo[1], lo[2], 0.f);
     }
 }
 
-template <int NG, int G, int kWarps>
-__global__ void __launch_bounds__(kWarps * 32, 1) cubature_kernel(CubatureArgs a, int tab0, int ngrp, Lookup lk) {
-    constexpr int NP = NG * NG * NG;
+__device__ __forceinline__ long long cell_id(const KeySpace& ks, const int* c) {
+    return ((long long)c[0] * ks.N2 + c[1]) * ks.N3 + c[2];
+}
+
+template <int NG, int G, bool EXACT>
+__global__ void __launch_bounds__(Shape<NG>::kWarps * 32, 1)
+    cubature_kernel(CubatureArgs a, int tab0, int ngrp, Lookup lk) {
+    constexpr int NP = Shape<NG>::NP;
+    constexpr int kWarps = Shape<NG>::kWarps;
+    constexpr int NB = EXACT ? 2 : 1;  // staged float4s per second-cell point
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int nx = a.xl.n();
-    float4* pts = reinterpret_cast<float4*>(smem_raw);           // [kWarps][2][NP]
-    float* tab = reinterpret_cast<float*>(pts + kWarps * 2 * NP);  // [ngrp][nx]
+    float4* pts = reinterpret_cast<float4*>(smem_raw);           // [kWarps][NB][NP]
+    float* tab = reinterpret_cast<float*>(pts + kWarps * NB * NP);  // [ngrp][nx]
 
     for (int i = threadIdx.x; i < ngrp * nx; i += blockDim.x) tab[i] = a.tab32[(size_t)tab0 * nx + i];
     __shared__ int s_ci[kMaxExp];
     __shared__ float s_cf[kMaxExp];
+    __shared__ float4 s_kt[EXACT ? kLogN : 1];
     for (int i = threadIdx.x; i < lk.ne; i += blockDim.x) {
         s_ci[i] = lk.ci[i];
         s_cf[i] = lk.cf[i];
     }
+    if (EXACT)
+        for (int i = threadIdx.x; i < kLogN; i += blockDim.x) s_kt[i] = lk.kt[i];
     __syncthreads();
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    float4* P1 = pts + warp * 2 * NP;
-    float4* P2 = P1 + NP;
+    float4* P2 = pts + warp * NB * NP;   // hi (x, y, z, w)
+    float4* P2l = P2 + (NB - 1) * NP;    // lo (x, y, z, 0), exact mode
     const bool periodic = (a.coordsys == 1 && a.L > 0);
-    const float Lf = (float)a.L, hL = (float)(0.5 * a.L);
+    const float Lh = (float)a.L, Ll = (float)(a.L - (double)Lh), hL = 0.5f * Lh;
 
     for (long long key = (long long)blockIdx.x * kWarps + warp; key < a.ks.nkeys;
          key += (long long)gridDim.x * kWarps) {
         int c1[3], c2[3];
         decode_key(a.ks, key, c1, c2);
-        double org[3], wo;
-        point_xyz<NG>(a, c1, NP / 2, org, &wo);
-        for (int p = lane; p < NP; p += 32) {
-            double x[3], w;
-            point_xyz<NG>(a, c1, p, x, &w);
-            P1[p] = make_float4((float)(x[0] - org[0]), (float)(x[1] - org[1]), (float)(x[2] - org[2]), (float)w);
-            point_xyz<NG>(a, c2, p, x, &w);
-            P2[p] = make_float4((float)(x[0] - org[0]), (float)(x[1] - org[1]), (float)(x[2] - org[2]), (float)w);
+        const float4* G1 = a.pts + 2 * NP * cell_id(a.ks, c1);
+        const float4* G2 = a.pts + 2 * NP * cell_id(a.ks, c2);
+        const float4 Oh = G1[2 * (NP / 2)], Ol = G1[2 * (NP / 2) + 1];  // origin: middle point of cell 1
+        for (int q = lane; q < NP; q += 32) {
+            const float4 Bh = G2[2 * q], Bl = G2[2 * q + 1];
+            float lx, ly, lz;
+            const float sx = diff2(Bh.x, Bl.x, Oh.x, Ol.x, &lx);
+            const float sy = diff2(Bh.y, Bl.y, Oh.y, Ol.y, &ly);
+            const float sz = diff2(Bh.z, Bl.z, Oh.z, Ol.z, &lz);
+            if (EXACT) {
+                P2[q] = make_float4(sx, sy, sz, Bh.w);
+                P2l[q] = make_float4(lx, ly, lz, 0.f);
+            } else {
+                P2[q] = make_float4(sx + lx, sy + ly, sz + lz, Bh.w);
+            }
         }
         __syncwarp();
 
@@ -128,37 +206,94 @@ __global__ void __launch_bounds__(kWarps * 32, 1) cubature_kernel(CubatureArgs a
 #pragma unroll
         for (int t = 0; t < G; t++) tot[t] = 0.0;
         for (int p = lane; p < NP; p += 32) {
-            const float4 A = P1[p];
+            const float4 Ah = G1[2 * p], Al = G1[2 * p + 1];
+            float alx, aly, alz;
+            const float ax = diff2(Ah.x, Al.x, Oh.x, Ol.x, &alx);
+            const float ay = diff2(Ah.y, Al.y, Oh.y, Ol.y, &aly);
+            const float az = diff2(Ah.z, Al.z, Oh.z, Ol.z, &alz);
             float acc[G];
 #pragma unroll
             for (int t = 0; t < G; t++) acc[t] = 0.f;
 #pragma unroll 4
             for (int q = 0; q < NP; q++) {
                 const float4 B = P2[q];
-                float dx = B.x - A.x, dy = B.y - A.y, dz = B.z - A.z;
-                if (periodic) {
-                    dx += Lf * (float)((dx < -hL) - (dx >= hL));
-                    dy += Lf * (float)((dy < -hL) - (dy >= hL));
-                    dz += Lf * (float)((dz < -hL) - (dz >= hL));
-                }
-                const float r = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
                 int i;
                 float fr;
-                if (r < lk.r1) {
-                    const float t = r * lk.inv_dr;
-                    i = (int)t;
-                    fr = t - (float)i;
+                if (EXACT) {
+                    const float4 Bl = P2l[q];
+                    float lx, ly, lz;
+                    float dx = diff2(B.x, Bl.x, ax, alx, &lx);
+                    float dy = diff2(B.y, Bl.y, ay, aly, &ly);
+                    float dz = diff2(B.z, Bl.z, az, alz, &lz);
+                    if (periodic) {
+                        // |d| in [L/2, L]: d -+ L is exact in FP32 (Sterbenz)
+                        const float wx = (float)((dx < -hL) - (dx >= hL));
+                        const float wy = (float)((dy < -hL) - (dy >= hL));
+                        const float wz = (float)((dz < -hL) - (dz >= hL));
+                        dx = fmaf(wx, Lh, dx); lx = fmaf(wx, Ll, lx);
+                        dy = fmaf(wy, Lh, dy); ly = fmaf(wy, Ll, ly);
+                        dz = fmaf(wz, Lh, dz); lz = fmaf(wz, Ll, lz);
+                    }
+                    // r^2 = hi + lo: exact squares by FMA, exact sums by two-sum
+                    const float px = __fmul_rn(dx, dx), py = __fmul_rn(dy, dy), pz = __fmul_rn(dz, dz);
+                    float e1, e2;
+                    const float h1 = two_sum(px, py, &e1);
+                    const float r2 = two_sum(h1, pz, &e2);
+                    float r2l = fmaf(dx, dx, -px) + fmaf(dy, dy, -py) + fmaf(dz, dz, -pz) + (e1 + e2);
+                    r2l = fmaf(2.f * dx, lx, fmaf(2.f * dy, ly, fmaf(2.f * dz, lz, r2l)));
+                    if (r2 < lk.r1sq) {
+                        // t = r n1 / r1 with r = rh + rl and n1 / r1 = inv_dr + inv_dr_lo; the
+                        // fraction is formed from the exact residual of the rounded product
+                        const float rh = sqrtf(r2);
+                        const float rl = rh > 0.f ? __fdividef(fmaf(-rh, rh, r2) + r2l, 2.f * rh) : 0.f;
+                        const float t = rh * lk.inv_dr;
+                        i = (int)t;
+                        fr = fmaf(rh, lk.inv_dr, -(float)i) + fmaf(rh, lk.inv_dr_lo, rl * lk.inv_dr);
+                    } else {
+                        const int bits = __float_as_int(r2);
+                        const int eb = bits >> 23;  // biased exponent; r2 > 0 here
+                        const int e = min(max(eb - 127 - lk.e0, 0), lk.ne - 1);
+                        const int k = (bits >> (23 - kLogBits)) & (kLogN - 1);
+                        const float Rk = __int_as_float(bits & ~((1 << (23 - kLogBits)) - 1));
+                        const float4 kt = s_kt[k];
+                        const float inv_pow = __int_as_float((254 - eb) << 23);  // 2^-(eb-127)
+                        const float delta = ((r2 - Rk) + r2l) * (kt.x * inv_pow);
+                        // ln(1 + delta), |delta| < 1/128: the series to delta^4 is good to 3e-12
+                        const float ln1p =
+                            delta * fmaf(-delta, fmaf(-delta, fmaf(-delta, 0.25f, 1.f / 3.f), 0.5f), 1.f);
+                        const float y = fmaf(ln1p, lk.cp, s_cf[e] + kt.y);
+                        const float yi = floorf(y);
+                        i = s_ci[e] + __float_as_int(kt.z) + (int)yi;
+                        fr = y - yi;
+                        if (i < lk.n1) {
+                            i = lk.n1;
+                            fr = 0.f;
+                        }
+                    }
                 } else {
-                    const int bits = __float_as_int(r);
-                    const int e = min(max((bits >> 23) - 127 - lk.e0, 0), lk.ne - 1);
-                    const float lm = __log2f(__int_as_float((bits & 0x007FFFFF) | 0x3F800000));  // log2 of mantissa
-                    const float y = fmaf(lm, lk.inv_du, s_cf[e]);
-                    const float yi = floorf(y);
-                    i = s_ci[e] + (int)yi;
-                    fr = y - yi;
-                    if (i < lk.n1) {
-                        i = lk.n1;
-                        fr = 0.f;
+                    float dx = B.x - ax, dy = B.y - ay, dz = B.z - az;
+                    if (periodic) {
+                        dx += Lh * (float)((dx < -hL) - (dx >= hL));
+                        dy += Lh * (float)((dy < -hL) - (dy >= hL));
+                        dz += Lh * (float)((dz < -hL) - (dz >= hL));
+                    }
+                    const float r = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
+                    if (r < lk.r1) {
+                        const float t = r * lk.inv_dr;
+                        i = (int)t;
+                        fr = t - (float)i;
+                    } else {
+                        const int bits = __float_as_int(r);
+                        const int e = min(max((bits >> 23) - 127 - lk.e0, 0), lk.ne - 1);
+                        const float lm = __log2f(__int_as_float((bits & 0x007FFFFF) | 0x3F800000));  // log2 of mantissa
+                        const float y = fmaf(lm, lk.inv_du, s_cf[e]);
+                        const float yi = floorf(y);
+                        i = s_ci[e] + (int)yi;
+                        fr = y - yi;
+                        if (i < lk.n1) {
+                            i = lk.n1;
+                            fr = 0.f;
+                        }
                     }
                 }
                 if (i > lk.imax) {
@@ -175,7 +310,7 @@ __global__ void __launch_bounds__(kWarps * 32, 1) cubature_kernel(CubatureArgs a
                 }
             }
 #pragma unroll
-            for (int t = 0; t < G; t++) tot[t] += (double)A.w * (double)acc[t];
+            for (int t = 0; t < G; t++) tot[t] += (double)Ah.w * (double)acc[t];
         }
 #pragma unroll
         for (int t = 0; t < G; t++) {
@@ -188,11 +323,17 @@ __global__ void __launch_bounds__(kWarps * 32, 1) cubature_kernel(CubatureArgs a
     }
 }
 
-template <int NG, int G, int kWarps>
+template <int NG, bool EXACT>
+size_t smem_points() {
+    return sizeof(float4) * Shape<NG>::kWarps * (EXACT ? 2 : 1) * Shape<NG>::NP;
+}
+
+template <int NG, int G, bool EXACT>
 void run(const CubatureArgs& a, int tab0, int ngrp, const Lookup& lk, cudaStream_t s) {
-    constexpr int NP = NG * NG * NG;
-    const size_t smem = sizeof(float4) * kWarps * 2 * NP + sizeof(float) * (size_t)ngrp * a.xl.n();
-    auto k = cubature_kernel<NG, G, kWarps>;
+    constexpr int kWarps = Shape<NG>::kWarps;
+    constexpr int NP = Shape<NG>::NP;
+    const size_t smem = smem_points<NG, EXACT>() + sizeof(float) * (size_t)ngrp * a.xl.n();
+    auto k = cubature_kernel<NG, G, EXACT>;
     OPSEC_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int dev = 0, nsm = 0, occ = 0;
     OPSEC_CUDA(cudaGetDevice(&dev));
@@ -208,20 +349,9 @@ void run(const CubatureArgs& a, int tab0, int ngrp, const Lookup& lk, cudaStream
     if (g_clock) g_clock->end(s);
 }
 
-template <int NG, int G>
-void run_w(const CubatureArgs& a, int tab0, int g, const Lookup& lk, cudaStream_t s, int warps) {
-    if (warps == 16)
-        run<NG, G, 16>(a, tab0, g, lk, s);
-    else
-        run<NG, G, 8>(a, tab0, g, lk, s);
-}
-
-template <int NG>
+template <int NG, bool EXACT>
 void run_groups(const CubatureArgs& a, const Lookup& lk, cudaStream_t s, long long* launches) {
-    constexpr int NP = NG * NG * NG;
-    // 16 warps per CTA (twice the latency hiding) while the point buffers leave room for tables
-    const int warps = (NG <= 4) ? 16 : 8;
-    const size_t budget = 224 * 1024 - sizeof(float4) * warps * 2 * NP;
+    const size_t budget = 222 * 1024 - smem_points<NG, EXACT>();
     int gmax = (int)(budget / (sizeof(float) * a.xl.n()));
     if (gmax > 16) gmax = 16;
     if (gmax < 1) fail(OPSEC_ERR_CONFIG, "xi table too long for shared memory");
@@ -230,48 +360,87 @@ void run_groups(const CubatureArgs& a, const Lookup& lk, cudaStream_t s, long lo
     for (int t0 = 0; t0 < a.ntab; t0 += per) {
         const int g = (a.ntab - t0 < per) ? a.ntab - t0 : per;
         if (g <= 1)
-            run_w<NG, 1>(a, t0, g, lk, s, warps);
+            run<NG, 1, EXACT>(a, t0, g, lk, s);
         else if (g <= 4)
-            run_w<NG, 4>(a, t0, g, lk, s, warps);
+            run<NG, 4, EXACT>(a, t0, g, lk, s);
         else if (g <= 8)
-            run_w<NG, 8>(a, t0, g, lk, s, warps);
+            run<NG, 8, EXACT>(a, t0, g, lk, s);
         else if (g <= 12)
-            run_w<NG, 12>(a, t0, g, lk, s, warps);
+            run<NG, 12, EXACT>(a, t0, g, lk, s);
         else
-            run_w<NG, 16>(a, t0, g, lk, s, warps);
+            run<NG, 16, EXACT>(a, t0, g, lk, s);
         ++*launches;
     }
 }
 
+template <int NG>
+void run_mode(const CubatureArgs& a, const Lookup& lk, cudaStream_t s, long long* launches) {
+    if (a.exact)
+        run_groups<NG, true>(a, lk, s, launches);
+    else
+        run_groups<NG, false>(a, lk, s, launches);
+}
+
 }  // namespace
 
+size_t cubature_point_count(const KeySpace& ks, int ng) {
+    return (size_t)ks.N1 * ks.N2 * ks.N3 * ng * ng * ng;
+}
+
 void launch_cubature(const CubatureArgs& a, cudaStream_t s, long long* launches) {
-    Lookup lk;
+    // point table: every Gauss point of every cell, once
+    {
+        const long long ncell = (long long)a.ks.N1 * a.ks.N2 * a.ks.N3;
+        const long long n = ncell * a.np;
+        const int threads = 256;
+        long long blocks = (n + threads - 1) / threads;
+        if (blocks > 65536) blocks = 65536;
+        point_table_kernel<<<(unsigned)blocks, threads, 0, s>>>(a, a.ng, ncell);
+        OPSEC_CUDA(cudaGetLastError());
+        ++*launches;
+    }
+    Lookup lk{};
     const double inv_du = (a.xl.n2 - 1) / std::log2(a.xl.r2 / a.xl.r1);
     lk.inv_dr = (float)(a.xl.n1 / a.xl.r1);
+    lk.inv_dr_lo = (float)(a.xl.n1 / a.xl.r1 - (double)lk.inv_dr);
     lk.r1 = (float)a.xl.r1;
+    lk.r1sq = (float)(a.xl.r1 * a.xl.r1);
     lk.inv_du = (float)inv_du;
+    lk.cp = (float)(0.5 * inv_du / std::log(2.0));
     lk.n1 = a.xl.n1;
     lk.imax = a.xl.n() - 2;
+    // exponents of r (fast) or r^2 (exact) over [r1, r2], one spare below and above
+    const double lo = a.exact ? a.xl.r1 * a.xl.r1 : a.xl.r1;
+    const double hi = a.exact ? a.xl.r2 * a.xl.r2 : a.xl.r2;
+    const double scale = a.exact ? 0.5 : 1.0;  // log2 r = scale * log2(argument)
     int e_lo = 0, e_hi = 0;
-    std::frexp(a.xl.r1, &e_lo);  // r1 = f 2^e_lo, f in [0.5,1): binary exponent of r1 is e_lo - 1
-    std::frexp(a.xl.r2, &e_hi);
-    lk.e0 = e_lo - 1;
-    lk.ne = e_hi - e_lo + 2;  // one spare exponent above r2 (clamped to the last table entry)
+    std::frexp(lo, &e_lo);  // lo = f 2^e_lo, f in [0.5,1): binary exponent of lo is e_lo - 1
+    std::frexp(hi, &e_hi);
+    lk.e0 = e_lo - 2;
+    lk.ne = e_hi - e_lo + 3;
     if (lk.ne > kMaxExp) fail(OPSEC_ERR_CONFIG, "xi table spans too many octaves of r");
     for (int k = 0; k < lk.ne; k++) {
-        const double c = a.xl.n1 + ((lk.e0 + k) - std::log2(a.xl.r1)) * inv_du;
+        const double c = a.xl.n1 + (scale * (lk.e0 + k) - std::log2(a.xl.r1)) * inv_du;
         const double ci = std::floor(c);
         lk.ci[k] = (int)ci;
         lk.cf[k] = (float)(c - ci);
     }
+    for (int k = 0; k < kLogN; k++) {
+        const double T = 1.0 + (double)k / kLogN;
+        const double z = 0.5 * std::log2(T) * inv_du;
+        const double zi = std::floor(z);
+        int zi_bits = (int)zi;
+        float zi_f;
+        std::memcpy(&zi_f, &zi_bits, sizeof zi_f);
+        lk.kt[k] = make_float4((float)(1.0 / T), (float)(z - zi), zi_f, 0.f);
+    }
     switch (a.ng) {
-    case 1: run_groups<1>(a, lk, s, launches); break;
-    case 2: run_groups<2>(a, lk, s, launches); break;
-    case 3: run_groups<3>(a, lk, s, launches); break;
-    case 4: run_groups<4>(a, lk, s, launches); break;
-    case 5: run_groups<5>(a, lk, s, launches); break;
-    case 6: run_groups<6>(a, lk, s, launches); break;
+    case 1: run_mode<1>(a, lk, s, launches); break;
+    case 2: run_mode<2>(a, lk, s, launches); break;
+    case 3: run_mode<3>(a, lk, s, launches); break;
+    case 4: run_mode<4>(a, lk, s, launches); break;
+    case 5: run_mode<5>(a, lk, s, launches); break;
+    case 6: run_mode<6>(a, lk, s, launches); break;
     default: fail(OPSEC_ERR_CONFIG, "sig.gauss must be between 1 and 6");
     }
 }

@@ -101,7 +101,11 @@ struct CubatureArgs {
     int ntab;            // tables in the whole set
     const float* tab32;  // [ntab][xl.n()]
     double* Q;           // [ntab][ks.nkeys]
+    float4* pts;         // [N1 N2 N3][np][2]: point table (hi: x y z w, lo: x y z 0), filled here
+    int exact = 1;       // FP32-pair separations and table index (1) or plain FP32 (0)
 };
+// float4s of the point table for a key space and ng
+size_t cubature_point_count(const KeySpace& ks, int ng);
 void launch_cubature(const CubatureArgs& a, cudaStream_t s, long long* launches);
 
 struct XiTableArgs {
@@ -152,7 +156,7 @@ struct ProjectArgs {
     float* Dp;             // [nbands][M(M+1)/2] packed output
     void* work;            // scratch
     size_t work_bytes;
-    int chunk = 2;         // tensor-core path: K-slices of 64 per FP32 accumulator chunk
+    int chunk = 1;         // tensor-core path: K-slices of 64 per FP32 accumulator chunk
 };
 size_t project_work_bytes(const ProjectArgs& a);
 void launch_project(const ProjectArgs& a, cudaStream_t s, long long* launches);

@@ -195,15 +195,23 @@ __device__ __forceinline__ void drain_loop(uint32_t tmem, int q, int lane, int n
     }
 }
 
-// MMA issue for one K-slice of 64 (3-term split), restarting D at chunk starts
+// MMA issue for one K-slice of 64 (3-term split), restarting D at chunk starts.
+// The tensor core rounds each accumulation toward zero, a bias of about half
+// an FP32 ulp of |D| per MMA.  The two cross terms (2^-11 of the main term)
+// are issued first, while D is small, so only the four main-term MMAs of a
+// slice add bias at the scale of the result.
 __device__ __forceinline__ void issue_slice(uint32_t tmem, uint64_t ah, uint64_t al, uint64_t bh, uint64_t bl,
                                             bool first_in_chunk) {
 #pragma unroll
     for (int kk = 0; kk < BK / 16; kk++) {
         const uint64_t adv = (uint64_t)(kk * 32) >> 4;
-        umma(tmem, ah + adv, bh + adv, (!first_in_chunk || kk > 0) ? 1u : 0u);
-        umma(tmem, ah + adv, bl + adv, 1u);
+        umma(tmem, ah + adv, bl + adv, (!first_in_chunk || kk > 0) ? 1u : 0u);
         umma(tmem, al + adv, bh + adv, 1u);
+    }
+#pragma unroll
+    for (int kk = 0; kk < BK / 16; kk++) {
+        const uint64_t adv = (uint64_t)(kk * 32) >> 4;
+        umma(tmem, ah + adv, bh + adv, 1u);
     }
 }
 
