@@ -1,0 +1,83 @@
+"""The drop-in programs klt -> comma -> dot -> estimate, run as the reference
+pipeline is (code/opsec/python/opsec-submit.in:196-201), on files, against the
+library called directly on the same inputs."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+from opsec_gpu import api, formats, synth
+
+pytestmark = pytest.mark.gpu
+BIN = os.path.join(ROOT, "opsec_gpu", "bin")
+
+
+def run(prog, cfgfile, *args):
+    res = subprocess.run([os.path.join(BIN, prog), "-c", str(cfgfile), *args], capture_output=True, text=True)
+    assert res.returncode == 0, res.stderr
+    return res
+
+
+def test_pipeline_programs(tmp_path):
+    from opsec_gpu import build
+
+    build.build()
+    sv, cells = synth.shell_survey(3, 4, 8)
+    k, P = synth.pk_table()
+    pk = tmp_path / "pk.dat"
+    synth.write_pkfile(str(pk), k, P)
+    bands = synth.band_edges(3, 0.0, 0.15)
+    nmodes = 40
+    cfg = api.make_config(sv, bands=bands, nmodes=nmodes, pkfile=str(pk))
+    files = {n: tmp_path / f"{n}.abn" for n in ("cells", "modes", "evals", "cov", "counts", "pix", "est")}
+    cfg += "".join(f"{n}file = {p}\n" for n, p in [("cell", files["cells"]), ("mode", files["modes"]),
+                                                    ("eval", files["evals"]), ("cov", files["cov"]),
+                                                    ("count", files["counts"]), ("pix", files["pix"]),
+                                                    ("est", files["est"])])
+    cfgfile = tmp_path / "opsec.cfg"
+    cfgfile.write_text(cfg)
+    formats.write_cells(str(files["cells"]), cells, sv.config_lines())
+    counts = synth.grf_counts(sv, cells)
+    with open(files["counts"], "wb") as f:
+        formats.write(f, counts, "d")
+    run("klt", cfgfile)
+    run("comma", cfgfile)
+    run("dot", cfgfile)
+    out = run("estimate", cfgfile)
+    assert "p_n" in out.stdout
+
+    mopts, modes = formats.read(str(files["modes"]))
+    assert int(mopts["Nmodes"]) == nmodes and int(mopts["Ncells"]) == cells.size and int(mopts["nconv"]) == nmodes
+    modes = modes.reshape(nmodes, cells.size)
+    _, evals = formats.read(str(files["evals"]))
+    copts, cov = formats.read(str(files["cov"]))
+    assert copts["packed"] == "1" and int(copts["Nparams"]) == len(bands)
+    _, y = formats.read(str(files["pix"]))
+    est = formats.read_estfile(str(files["est"]))
+
+    e = api.Engine(api.make_config(sv, bands=bands, nmodes=nmodes))
+    e.set_pk(k, P)
+    ev2, modes2 = e.klt(cells, nmodes)
+    np.testing.assert_array_equal(evals, ev2)
+    np.testing.assert_array_equal(modes, modes2)
+    cov2 = e.comma(cells, modes)
+    np.testing.assert_array_equal(cov.reshape(cov2.shape), cov2)
+    np.testing.assert_array_equal(y, e.dot(cells, counts, modes))
+    r = e.estimate(evals, cov2, y)
+    for name in ("phat", "pcov", "F", "W", "M", "q", "f"):
+        np.testing.assert_array_equal(est[name], r[name])
+    e.close()
+
+
+def test_programs_reject_missing_options(tmp_path):
+    from opsec_gpu import build
+
+    build.build()
+    cfgfile = tmp_path / "empty.cfg"
+    cfgfile.write_text("# nothing\n")
+    res = subprocess.run([os.path.join(BIN, "klt"), "-c", str(cfgfile)], capture_output=True, text=True)
+    assert res.returncode == 1 and "missing configuration options" in res.stderr
+    res = subprocess.run([os.path.join(BIN, "klt"), "-h"], capture_output=True, text=True)
+    assert res.returncode == 0 and "Usage: klt" in res.stdout
