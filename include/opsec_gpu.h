@@ -130,6 +130,35 @@ int opsec_gpu_kernel_stats(const opsec_gpu* ctx, const char* name, long long* co
 /* Number of kernels this context has launched since creation. */
 long long opsec_gpu_launch_count(const opsec_gpu* ctx);
 
+/* Largest band count opsec_gpu_fisher_noalloc accepts. */
+#define OPSEC_NOALLOC_MAX_BANDS 64
+
+/* Fisher matrix, bias and quadratic estimates from device-resident inputs,
+ * with no memory allocation -- for callers that cannot call cudaMalloc: code
+ * whose device memory is all handed out by its own pool allocator, or a
+ * latency-critical loop where an allocation or free could synchronize the
+ * device.  No counterpart in the reference (its estimate allocates freely).
+ *
+ * All pointers are device memory owned by the caller: cov_packed = FP32
+ * packed upper triangles, band after band (nbands x nmodes(nmodes+1)/2),
+ * evals (nmodes), y (nmodes), prior band powers (nbands); out receives
+ * F (nbands x nbands, row-major), then f (nbands), then q (nbands, the raw
+ * quadratic estimate).  Kernels are queued on `stream` (a cudaStream_t, NULL
+ * for the legacy stream) and the call returns without waiting.
+ *
+ * Scratch: one file-scope device array of 2.7 MB (152 x 2208 doubles) that
+ * every GPU which loads this library holds until the process exits.  The
+ * first call on a device, with that device current, looks up the array's
+ * device address; make that first call before any stream capture.  Every call
+ * shares the array and overwrites all of it that it reads, so no clearing is
+ * needed -- but calls that overlap on the GPU (different streams, or
+ * different host threads, running at once) race on it.
+ *
+ * Returns OPSEC_ERR_ARG for nbands > OPSEC_NOALLOC_MAX_BANDS (64), non-positive
+ * sizes or null pointers, OPSEC_ERR_CUDA if a launch fails. */
+int opsec_gpu_fisher_noalloc(int nmodes, int nbands, const float* cov_packed, const double* evals, const double* y,
+                             const double* prior, double* out, void* stream);
+
 const char* opsec_gpu_last_error(const opsec_gpu* ctx);
 void opsec_gpu_destroy(opsec_gpu* ctx);
 

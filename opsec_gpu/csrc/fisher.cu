@@ -362,3 +362,60 @@ void launch_epilogue(int nb, int mixing, const double* Fqf, double* out, int* st
 }
 
 }  // namespace opsec
+
+// ---------------------------------------------------------------- no-allocation entry point
+// Some callers cannot call cudaMalloc: applications whose device memory is all
+// owned by their own pool allocator (a pipeline framework that hands out
+// buffers and forbids raw allocations), and latency-critical loops where an
+// allocation or free could synchronize the device between kernels on the
+// caller's stream.  For them the Fisher reduction below allocates nothing:
+// inputs and outputs are caller-owned device buffers, and the only scratch --
+// the per-CTA partial sums -- lives in one file-scope device array that every
+// GPU loading this library keeps until the process exits.
+namespace opsec {
+namespace {
+
+constexpr int kNoallocBlocks = 152;
+constexpr int kNoallocMaxBands = OPSEC_NOALLOC_MAX_BANDS;
+constexpr int kNoallocMaxOut = kNoallocMaxBands * (kNoallocMaxBands + 1) / 2 + 2 * kNoallocMaxBands;
+
+// 152 x 2208 doubles = 2.7 MB
+static __device__ __align__(256) double g_noalloc_partial[kNoallocBlocks * kNoallocMaxOut];
+
+constexpr int kMaxDevices = 64;
+double* g_partial_addr[kMaxDevices] = {nullptr};
+bool g_attr_done[kMaxDevices] = {false};
+
+}  // namespace
+
+}  // namespace opsec
+
+extern "C" int opsec_gpu_fisher_noalloc(int nmodes, int nbands, const float* cov_packed, const double* evals,
+                                        const double* y, const double* prior, double* out, void* stream) {
+    using namespace opsec;
+    if (nmodes <= 0 || nbands <= 0 || !cov_packed || !evals || !y || !prior || !out) return OPSEC_ERR_ARG;
+    if (nbands > kNoallocMaxBands) return OPSEC_ERR_ARG;  // scratch holds at most 64 bands
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return OPSEC_ERR_CUDA;
+    // once per device, with that device current: the device address of the scratch array
+    if (!g_partial_addr[dev]) {
+        void* p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_noalloc_partial) != cudaSuccess || !p) return OPSEC_ERR_CUDA;
+        g_partial_addr[dev] = static_cast<double*>(p);
+    }
+    const int nb = nbands;
+    const int nout = nb * (nb + 1) / 2 + 2 * nb;
+    const size_t smem = sizeof(float) * (size_t)(nb + 2) * kChunk;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (!g_attr_done[dev]) {
+        if (cudaFuncSetAttribute(fisher_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(sizeof(float) * (size_t)(kNoallocMaxBands + 2) * kChunk)) != cudaSuccess)
+            return OPSEC_ERR_CUDA;
+        g_attr_done[dev] = true;
+    }
+    // every CTA writes all nout partials of its slot, so nothing needs clearing
+    fisher_kernel<float><<<kNoallocBlocks, kThreads, smem, s>>>(nmodes, nb, cov_packed, evals, y, prior,
+                                                                g_partial_addr[dev]);
+    fisher_reduce_kernel<<<(nout + 255) / 256, 256, 0, s>>>(nb, kNoallocBlocks, g_partial_addr[dev], out);
+    return cudaGetLastError() == cudaSuccess ? OPSEC_OK : OPSEC_ERR_CUDA;
+}
