@@ -77,6 +77,45 @@ def peaks():
     return 6800.0, 1900.0, "fallback"
 
 
+def tensor_roofline(s1, bf16, peak_kind):
+    """Step-1 projection (tensor cores): algorithmic work 2 N^2 M per band counted once; the
+    3-term FP16 split issues 3x that on the tensor pipe."""
+    if not (s1["count"] > 0 and s1["ms"] > 0):
+        return None
+    avg_s = s1["ms"] / 1000.0 / s1["count"]
+    alg = s1["flops"] / s1["count"]
+    achieved = 3.0 * alg / avg_s / 1e12
+    return {"kernel": "project_step1 (tcgen05 FP16 3-term)", "bound": "tensor", "achieved": achieved,
+            "peak": bf16, "unit": "TFLOP/s", "frac": achieved / bf16, "traffic": None,
+            "peak_kind": f"{peak_kind} bf16 dense burst", "algorithmic_tflops_per_s": alg / avg_s / 1e12,
+            "avg_launch_ms": avg_s * 1000, "launches": int(s1["count"])}
+
+
+def roofline(stats, clk, bf16, peak_kind):
+    """Roofline of the kernel with the most device time in the timed builds."""
+    dom = max(stats, key=lambda n: stats[n]["ms"])
+    s = stats[dom]
+    if s["count"] == 0 or s["ms"] <= 0:
+        return None
+    if dom == "cubature":
+        # bound by shared-memory table lookups: two 4-byte loads per lookup, 32 banks x 4 B per clock
+        # per SM -> 16 lookups / clock / SM.  No measured figure exists for it: derived from the
+        # SM count and the SM clock sampled under load.
+        nsm = 152
+        mhz = clk.get("sm_mhz") or 2070.0
+        peak = 16.0 * nsm * mhz * 1e6 / 1e9
+        avg_s = s["ms"] / 1000.0 / s["count"]
+        achieved = s["flops"] / s["count"] / avg_s / 1e9
+        return {"kernel": "cubature_kernel (exact mode)", "bound": "smem", "achieved": achieved, "peak": peak,
+                "unit": "Glookups/s", "frac": achieved / peak, "traffic": None,
+                "peak_kind": f"derived: 16 lookups/clk/SM x {nsm} SMs x {mhz:.0f} MHz (sampled median)",
+                "algorithmic_unit": "one Gauss-point pair x one xi table", "avg_launch_ms": avg_s * 1000,
+                "launches": int(s["count"])}
+    if dom == "project_step1":
+        return tensor_roofline(s, bf16, peak_kind)
+    return {"kernel": dom, "bound": None, "avg_launch_ms": s["ms"] / max(s["count"], 1)}
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons during the timed region."""
 
@@ -223,6 +262,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="c2")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-tc-roofline", action="store_true",
+                    help="skip the one-band dense tensor-core projection run after the timed builds")
     ap.add_argument("--set", action="append", default=[], metavar="KEY=VALUE",
                     help="extra configuration line for the engine, e.g. cubature.precision=fast")
     args = ap.parse_args()
@@ -286,7 +327,8 @@ def main():
 
     for _ in range(args.warmup):
         res = eng.fisher_build(cells, counts, w["nmodes"])
-    base = {n: eng.kernel_stats(n) for n in ("project_step1", "project_step2", "cubature", "fisher")}
+    names = ("cubature", "azimuthal_transform", "azimuthal_gemm", "project_step1", "project_step2", "fisher")
+    base = {n: eng.kernel_stats(n) for n in names}
     launches0 = eng.launch_count()
     clocks = ClockSampler(local)
     clocks.start()
@@ -318,20 +360,20 @@ def main():
         return
 
     hbm, bf16, peak_kind = peaks()
-    s1 = stats["project_step1"]
-    s2 = stats["project_step2"]
-    # dominant kernel: the step-1 projection (tensor cores).  Algorithmic work 2 N^2 M per band
-    # counted once; the 3-term FP16 split issues 3x that on the tensor pipe.
-    if s1["count"] > 0 and s1["ms"] > 0:
-        avg_s = s1["ms"] / 1000.0 / s1["count"]
-        alg = s1["flops"] / s1["count"]
-        achieved = 3.0 * alg / avg_s / 1e12
-        roof = {"kernel": "project_step1 (tcgen05 FP16 3-term)", "bound": "tensor", "achieved": achieved,
-                "peak": bf16, "unit": "TFLOP/s", "frac": achieved / bf16, "traffic": None,
-                "peak_kind": f"{peak_kind} bf16 dense burst",
-                "algorithmic_tflops_per_s": alg / avg_s / 1e12, "avg_launch_ms": avg_s * 1000}
-    else:
-        roof = None
+    roof = roofline(stats, clk, bf16, peak_kind)
+    # the fused tensor-core projection is the path for every non-azimuthal geometry and for the
+    # comma drop-in; its roofline is taken on a one-band build of the same cells and modes
+    roof_tc = None
+    if not args.no_tc_roofline:
+        e2 = api.Engine(api.make_config(sv, bands=bands[:1], nmodes=w["nmodes"], layout=w["layout"],
+                                        gauss=w["gauss"], extra=["profile = 1", "projection = tc"]))
+        e2.set_pk(k, P)
+        e2.fisher_build(cells, counts, w["nmodes"])
+        b2 = e2.kernel_stats("project_step1")
+        e2.fisher_build(cells, counts, w["nmodes"])
+        s1 = {kk: e2.kernel_stats("project_step1")[kk] - b2[kk] for kk in b2}
+        e2.close()
+        roof_tc = tensor_roofline(s1, bf16, peak_kind)
     cpu = None
     if not args.no_cpu_baseline:
         cpu = cpu_baseline_obj(w, cores)
@@ -349,7 +391,8 @@ def main():
                     "d2h_bytes_per_step": int(d2h)},
             "stages_ms": {n: v / args.steps for n, v in stage_tot.items()},
             "kernels": {n: {"launches": v["count"], "ms": v["ms"]} for n, v in stats.items()},
-            "roofline": roof, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches)}
+            "roofline": roof, "roofline_projection_tc": roof_tc, "cpu_baseline": cpu, "clocks": clk,
+            "gpu_launches": int(launches)}
     print(json.dumps(line), flush=True)
     eng.close()
     if dist is not None:

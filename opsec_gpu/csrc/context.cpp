@@ -1,6 +1,7 @@
 // context.cpp -- host side of the engine: configuration, model and survey
 // setup, device-resident pipeline, and the C ABI of include/opsec_gpu.h.
 #include <cuda_runtime.h>
+#include <cublas_v2.h>
 #include <cusolverDn.h>
 
 #include <algorithm>
@@ -53,6 +54,10 @@ void cuda_check(cudaError_t e, const char* what) {
     }
 }
 
+static void blas_check(cublasStatus_t st, const char* what) {
+    if (st != CUBLAS_STATUS_SUCCESS) fail(OPSEC_ERR_CUDA, std::string(what) + " failed (cuBLAS status " + std::to_string((int)st) + ")");
+}
+
 static void solver_check(cusolverStatus_t st, const char* what) {
     if (st != CUSOLVER_STATUS_SUCCESS) fail(OPSEC_ERR_CUDA, std::string(what) + ": cuSOLVER status " + std::to_string((int)st));
 }
@@ -83,6 +88,7 @@ template struct DevBuf<double>;
 template struct DevBuf<float>;
 template struct DevBuf<int>;
 template struct DevBuf<unsigned char>;
+template struct DevBuf<long long>;
 
 bool Geometry::full_sky() const { return coordsys == 2 && std::fabs(b[5] - b[4] - 2 * M_PI) < 1e-12; }
 
@@ -239,6 +245,7 @@ struct opsec_gpu {
     int device = 0;
     cudaStream_t stream = nullptr;
     cusolverDnHandle_t solver = nullptr;
+    cublasHandle_t blas = nullptr;
     // side streams for the independent azimuthal eigenproblems
     static constexpr int kSide = 6;
     cudaStream_t side[kSide] = {};
@@ -279,6 +286,13 @@ struct opsec_gpu {
     DevBuf<double> work;   // solver workspace
     DevBuf<int> info;
     DevBuf<int> sel;
+    // modes of the last azimuthal eigensolve: per mode its order m, block eigenvector idx, kind
+    bool az_valid = false;
+    std::vector<int> az_m, az_idx, az_kind;
+    std::vector<double> nbar_arc;
+    DevBuf<double> Ucat, Tm, Cm;
+    DevBuf<int> az_i;
+    DevBuf<long long> az_off;
     DevBuf<double> evals, modes, Bs, y, counts, prior, fout, partial, est;
     DevBuf<float> Dp;
     DevBuf<double> Dp64;
@@ -708,11 +722,13 @@ int eigensolve(opsec_gpu* c, int ncells, const opsec_cell* cells, int M) {
     c->evals.alloc(M);
     c->modes.alloc((size_t)M * ncells);
     c->warning.clear();
+    c->az_valid = false;
     if (azimuthal_ok(c, ncells, cells)) {
         const KeySpace& ks = c->ks;
         const int H = ks.H, Nphi = ks.N3, nm = Nphi / 2 + 1;
         std::vector<double> nba(H);
         for (int h = 0; h < H; h++) nba[h] = cells[(size_t)h * Nphi].Nbar;
+        c->nbar_arc = nba;
         DevBuf<double> d_nba;
         d_nba.alloc(H);
         OPSEC_CUDA(cudaMemcpyAsync(d_nba.p, nba.data(), sizeof(double) * H, cudaMemcpyHostToDevice, c->stream));
@@ -792,6 +808,10 @@ int eigensolve(opsec_gpu* c, int ncells, const opsec_cell* cells, int M) {
         launch_assemble_modes(H, Nphi, M, c->sel.p, c->sel.p + M, c->sel.p + 2 * M, c->S.p, c->modes.p, c->stream,
                               &c->launches);
         sync(c);
+        c->az_m.assign(sel.begin(), sel.begin() + M);
+        c->az_idx.assign(sel.begin() + M, sel.begin() + 2 * M);
+        c->az_kind.assign(sel.begin() + 2 * M, sel.end());
+        c->az_valid = true;
         return M;
     }
     // dense path: S in FP64, top-M by syevdx (klt.cpp:173-248 via PARPACK there)
@@ -820,7 +840,116 @@ int eigensolve(opsec_gpu* c, int ncells, const opsec_cell* cells, int M) {
     return M;
 }
 
-void project_all(opsec_gpu* c, int ncells, int M) {
+// Projection of a full-sky spherical build onto its own azimuthal modes.
+// S_p is block circulant in phi (Q depends on |phi_a - phi_b| only and Nbar
+// does not depend on phi), and every mode is U_m[:, idx] (x) a cos or sin of
+// order m.  So C_p[i][j] = U_m[:, idx_i]^T S_p(m) U_m[:, idx_j] when modes i
+// and j have the same order m and the same trig class, and 0 otherwise, with
+// S_p(m) the H x H cosine transform of the band table (as for the eigensolve).
+// Per band: the transform (FP64), then for each m two FP64 GEMMs
+// T = S_p(m) U_m and C_m = U_m^T T, then one scatter into the packed triangle.
+// Work per band sum_m 2 H^2 K_m + 2 H K_m^2 (K_m distinct block vectors of
+// order m), against 2 N^2 M + N M^2 for the dense projection.
+void project_azimuthal(opsec_gpu* c, int ncells, int M) {
+    const KeySpace& ks = c->ks;
+    const int H = ks.H, Nphi = ks.N3, nm = Nphi / 2 + 1;
+    const int nb = c->ntab() - 1;
+    // distinct (m, idx) columns, grouped by m
+    std::vector<std::vector<int>> cols(nm);
+    for (int i = 0; i < M; i++) cols[c->az_m[i]].push_back(c->az_idx[i]);
+    std::vector<int> col_m, col_idx, Km(nm), base(nm);
+    std::vector<long long> off(nm);
+    long long csize = 0;
+    int Kmax = 0;
+    for (int m = 0; m < nm; m++) {
+        auto& v = cols[m];
+        std::sort(v.begin(), v.end());
+        v.erase(std::unique(v.begin(), v.end()), v.end());
+        Km[m] = (int)v.size();
+        base[m] = (int)col_m.size();
+        off[m] = csize;
+        csize += (long long)Km[m] * Km[m];
+        Kmax = std::max(Kmax, Km[m]);
+        for (int idx : v) {
+            col_m.push_back(m);
+            col_idx.push_back(idx);
+        }
+    }
+    const int ncol = (int)col_m.size();
+    std::vector<int> mode_cls(M), mode_col(M);
+    for (int i = 0; i < M; i++) {
+        const int m = c->az_m[i];
+        mode_cls[i] = c->az_kind[i] == 2 ? 1 : 0;
+        mode_col[i] = (int)(std::lower_bound(cols[m].begin(), cols[m].end(), c->az_idx[i]) - cols[m].begin());
+    }
+    // device tables: col_m, col_idx, mode_m, mode_cls, mode_col, Km; offsets
+    std::vector<int> ti;
+    ti.insert(ti.end(), col_m.begin(), col_m.end());
+    ti.insert(ti.end(), col_idx.begin(), col_idx.end());
+    ti.insert(ti.end(), c->az_m.begin(), c->az_m.end());
+    ti.insert(ti.end(), mode_cls.begin(), mode_cls.end());
+    ti.insert(ti.end(), mode_col.begin(), mode_col.end());
+    ti.insert(ti.end(), Km.begin(), Km.end());
+    c->az_i.alloc(ti.size());
+    OPSEC_CUDA(cudaMemcpyAsync(c->az_i.p, ti.data(), sizeof(int) * ti.size(), cudaMemcpyHostToDevice, c->stream));
+    c->az_off.alloc(nm);
+    OPSEC_CUDA(cudaMemcpyAsync(c->az_off.p, off.data(), sizeof(long long) * nm, cudaMemcpyHostToDevice, c->stream));
+    const int* d_col_m = c->az_i.p;
+    const int* d_col_idx = d_col_m + ncol;
+    const int* d_mode_m = d_col_idx + ncol;
+    const int* d_mode_cls = d_mode_m + M;
+    const int* d_mode_col = d_mode_cls + M;
+    const int* d_Km = d_mode_col + M;
+    // the block eigenvectors the modes use, before the blocks are overwritten
+    c->Ucat.alloc((size_t)ncol * H);
+    launch_gather_block_vectors(H, ncol, d_col_m, d_col_idx, c->S.p, c->Ucat.p, c->stream, &c->launches);
+    std::vector<double> nba(H);
+    for (int h = 0; h < H; h++) nba[h] = c->nbar_arc[h];
+    DevBuf<double> d_nba;
+    d_nba.alloc(H);
+    OPSEC_CUDA(cudaMemcpyAsync(d_nba.p, nba.data(), sizeof(double) * H, cudaMemcpyHostToDevice, c->stream));
+    c->S.alloc((size_t)nm * H * H);
+    c->Tm.alloc((size_t)H * std::max(Kmax, 1));
+    c->Cm.alloc((size_t)std::max(csize, 1LL) * nb);
+    if (!c->blas) blas_check(cublasCreate(&c->blas), "cublasCreate");
+    blas_check(cublasSetStream(c->blas, c->stream), "cublasSetStream");
+    const double one = 1.0, zero = 0.0;
+    for (int p = 0; p < nb; p++) {
+        if (g_clock) g_clock->begin("azimuthal_transform", c->stream, 2.0 * nm * (double)H * H * ks.nf);
+        launch_azimuthal_blocks(ks, c->Q.p + (size_t)(1 + p) * ks.nkeys, d_nba.p, nm, c->S.p, c->stream,
+                                &c->launches);
+        if (g_clock) g_clock->end(c->stream);
+        double fl = 0;
+        for (int m = 0; m < nm; m++) fl += 2.0 * H * H * Km[m] + 2.0 * H * (double)Km[m] * Km[m];
+        if (g_clock) g_clock->begin("azimuthal_gemm", c->stream, fl);
+        for (int m = 0; m < nm; m++) {
+            const int K = Km[m];
+            if (K == 0) continue;
+            const double* Sm = c->S.p + (size_t)m * H * H;
+            const double* U = c->Ucat.p + (size_t)base[m] * H;
+            blas_check(cublasDgemm(c->blas, CUBLAS_OP_N, CUBLAS_OP_N, H, K, H, &one, Sm, H, U, H, &zero, c->Tm.p, H),
+                       "cublasDgemm");
+            blas_check(cublasDgemm(c->blas, CUBLAS_OP_T, CUBLAS_OP_N, K, K, H, &one, U, H, c->Tm.p, H, &zero,
+                                   c->Cm.p + (size_t)p * csize + off[m], K),
+                       "cublasDgemm");
+            c->launches += 2;
+        }
+        if (g_clock) g_clock->end(c->stream);
+    }
+    const size_t Kp = (size_t)M * (M + 1) / 2;
+    c->Dp.alloc(Kp * nb);
+    launch_azimuthal_scatter(M, nb, d_mode_m, d_mode_cls, d_mode_col, c->az_off.p, d_Km, csize, c->Cm.p, c->Dp.p,
+                             c->stream, &c->launches);
+    (void)ncells;
+}
+
+void project_all(opsec_gpu* c, int ncells, int M, bool own_modes) {
+    if (own_modes && c->az_valid && (c->projection == "auto" || c->projection == "azimuthal")) {
+        project_azimuthal(c, ncells, M);
+        return;
+    }
+    if (c->projection == "azimuthal")
+        fail(OPSEC_ERR_CONFIG, "projection=azimuthal needs a full-sky spherical build on its own modes");
     build_qsq(c);
     const int nb = c->ntab() - 1;
     c->Bs.alloc((size_t)M * ncells);
@@ -1079,7 +1208,7 @@ int opsec_gpu_comma(opsec_gpu* c, int ncells, const opsec_cell* cells, int nmode
         c->modes.alloc((size_t)nmodes * ncells);
         OPSEC_CUDA(cudaMemcpyAsync(c->modes.p, modes, sizeof(double) * (size_t)nmodes * ncells, cudaMemcpyHostToDevice,
                                    c->stream));
-        project_all(c, ncells, nmodes);
+        project_all(c, ncells, nmodes, false);
         const size_t K = (size_t)nmodes * (nmodes + 1) / 2, tot = K * (c->ntab() - 1);
         c->Dp64.alloc(tot);
         launch_widen(tot, c->Dp.p, c->Dp64.p, c->stream, &c->launches);
@@ -1143,7 +1272,7 @@ int opsec_gpu_fisher_build(opsec_gpu* c, int ncells, const opsec_cell* cells, co
         t.mark();
         int n = eigensolve(c, ncells, cells, nmodes);
         t.mark();
-        project_all(c, ncells, n);
+        project_all(c, ncells, n, true);
         c->counts.alloc(ncells);
         c->y.alloc(n);
         OPSEC_CUDA(cudaMemcpyAsync(c->counts.p, counts, sizeof(double) * ncells, cudaMemcpyHostToDevice, c->stream));

@@ -220,6 +220,34 @@ def test_fisher_build_end_to_end(name):
     e.close()
 
 
+def test_fisher_build_azimuthal_projection():
+    """Full-sky shell, 8 x 8 x 16 = 1024 cells, 10 bands: the build projects
+    onto its own azimuthal modes block by block (FP64 GEMMs on the H x H
+    cosine transforms of each band).  Against the dense tensor-core projection
+    of the same modes (projection = tc) and against the oracle end to end."""
+    sv, cells = synth.shell_survey(8, 8, 16)
+    bands = synth.band_edges(10, 0.0, 0.2)
+    counts = synth.grf_counts(sv, cells)
+    tabs = O.xi_tables(*PK, bands)
+    Q = O.qtable_keys(sv, O.keys_all(sv), tabs)
+    S = O.signal_matrix(sv, cells, Q[:, 0])
+    lam = np.sort(np.linalg.eigvalsh(S))[::-1]
+    M = O.gap_nmodes(lam, 256, rel_gap=1e-4, span=64)
+    out = {}
+    for proj in ("auto", "tc", "simt"):
+        e = api.Engine(api.make_config(sv, bands=bands, extra=[f"projection = {proj}"]))
+        e.set_pk(*PK)
+        out[proj] = e.fisher_build(cells, counts, M)
+        e.close()
+    scale = np.max(np.abs(out["simt"]["F"]))
+    d_tc = np.max(np.abs(out["auto"]["F"] - out["tc"]["F"])) / scale
+    d_simt = np.max(np.abs(out["auto"]["F"] - out["simt"]["F"])) / scale
+    print(f"azimuthal vs tc {d_tc:.2e}, vs simt {d_simt:.2e}")
+    assert d_tc <= 1e-6 and d_simt <= 1e-6, (d_tc, d_simt)
+    ref = O.fisher_build(sv, cells, counts, *PK, bands, M)
+    check_estimates(out["auto"], ref, "shell1024/end-to-end", tol=1e-5)
+
+
 def check_estimates(got, ref, name, tol=1e-6):
     """F, f and q within tol of their scale; p-hat and Cov within tol of the
     scale their own inputs propagate (p-hat = M (q - f) cancels q against f,
