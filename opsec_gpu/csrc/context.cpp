@@ -264,6 +264,7 @@ struct opsec_gpu {
     std::string projection = "auto";
     int proj_chunk = 1;
     int cub_exact = 1;
+    int az_gemm64 = 0;
     std::vector<double> pk_k, pk_P;
     std::vector<double> band_lo, band_hi;
 
@@ -290,7 +291,7 @@ struct opsec_gpu {
     bool az_valid = false;
     std::vector<int> az_m, az_idx, az_kind;
     std::vector<double> nbar_arc;
-    DevBuf<double> Ucat, Tm, Cm;
+    DevBuf<unsigned char> azws;  // azimuthal projection workspace
     DevBuf<int> az_i;
     DevBuf<long long> az_off;
     DevBuf<double> evals, modes, Bs, y, counts, prior, fout, partial, est;
@@ -475,6 +476,15 @@ void configure(opsec_gpu* c, const std::map<std::string, std::string>& kv) {
     if (has("projection")) c->projection = get("projection");
     if (has("projection.chunk")) c->proj_chunk = to_int("projection.chunk", get("projection.chunk"));
     if (c->proj_chunk < 1) fail(OPSEC_ERR_CONFIG, "projection.chunk must be >= 1");
+    if (has("azimuthal.gemm")) {
+        const std::string& v = get("azimuthal.gemm");
+        if (v == "f64")
+            c->az_gemm64 = 1;
+        else if (v == "f32")
+            c->az_gemm64 = 0;
+        else
+            fail(OPSEC_ERR_CONFIG, "azimuthal.gemm must be f64 or f32");
+    }
     if (has("cubature.precision")) {
         const std::string& v = get("cubature.precision");
         if (v == "exact")
@@ -840,6 +850,72 @@ int eigensolve(opsec_gpu* c, int ncells, const opsec_cell* cells, int M) {
     return M;
 }
 
+struct AzPlan {
+    int H, nm, nb, ncol;
+    long long csize;
+    int Kmax;
+    double flops;
+    const int *col_m, *col_idx, *mode_m, *mode_cls, *mode_col, *Km_dev;
+    const std::vector<int>* Km;
+    const std::vector<int>* base;
+    const std::vector<long long>* off;
+    const double* nbar_arc;
+};
+
+template <typename T>
+cublasStatus_t gemm(cublasHandle_t h, cublasOperation_t ta, cublasOperation_t tb, int m, int n, int k, const T* A,
+                    int lda, const T* B, int ldb, T* C, int ldc);
+template <>
+cublasStatus_t gemm<double>(cublasHandle_t h, cublasOperation_t ta, cublasOperation_t tb, int m, int n, int k,
+                            const double* A, int lda, const double* B, int ldb, double* C, int ldc) {
+    const double one = 1.0, zero = 0.0;
+    return cublasDgemm(h, ta, tb, m, n, k, &one, A, lda, B, ldb, &zero, C, ldc);
+}
+template <>
+cublasStatus_t gemm<float>(cublasHandle_t h, cublasOperation_t ta, cublasOperation_t tb, int m, int n, int k,
+                           const float* A, int lda, const float* B, int ldb, float* C, int ldc) {
+    const float one = 1.f, zero = 0.f;
+    return cublasSgemm(h, ta, tb, m, n, k, &one, A, lda, B, ldb, &zero, C, ldc);
+}
+
+// Band blocks, block GEMMs and the scatter, in FP64 or FP32 (the transform
+// itself always sums in FP64).
+template <typename T>
+void az_blocks(opsec_gpu* c, const AzPlan& a, int M) {
+    const int H = a.H;
+    DevBuf<unsigned char>& ws = c->azws;
+    const size_t nU = (size_t)a.ncol * H, nS = (size_t)a.nm * H * H, nT = (size_t)H * std::max(a.Kmax, 1),
+                 nC = (size_t)std::max(a.csize, 1LL) * a.nb;
+    ws.alloc(sizeof(T) * (nU + nS + nT + nC));
+    T* U = reinterpret_cast<T*>(ws.p);
+    T* Sb = U + nU;
+    T* Tm = Sb + nS;
+    T* Cm = Tm + nT;
+    // the block eigenvectors the modes use
+    launch_gather_block_vectors(H, a.ncol, a.col_m, a.col_idx, c->S.p, U, c->stream, &c->launches);
+    for (int p = 0; p < a.nb; p++) {
+        if (g_clock) g_clock->begin("azimuthal_transform", c->stream, 2.0 * a.nm * (double)H * H * c->ks.nf);
+        launch_azimuthal_blocks(c->ks, c->Q.p + (size_t)(1 + p) * c->ks.nkeys, a.nbar_arc, a.nm, Sb, c->stream,
+                                &c->launches);
+        if (g_clock) g_clock->end(c->stream);
+        if (g_clock) g_clock->begin("azimuthal_gemm", c->stream, a.flops);
+        for (int m = 0; m < a.nm; m++) {
+            const int K = (*a.Km)[m];
+            if (K == 0) continue;
+            const T* Sm = Sb + (size_t)m * H * H;
+            const T* Um = U + (size_t)(*a.base)[m] * H;
+            blas_check(gemm<T>(c->blas, CUBLAS_OP_N, CUBLAS_OP_N, H, K, H, Sm, H, Um, H, Tm, H), "gemm");
+            blas_check(gemm<T>(c->blas, CUBLAS_OP_T, CUBLAS_OP_N, K, K, H, Um, H, Tm, H,
+                               Cm + (size_t)p * a.csize + (*a.off)[m], K),
+                       "gemm");
+            c->launches += 2;
+        }
+        if (g_clock) g_clock->end(c->stream);
+    }
+    launch_azimuthal_scatter(M, a.nb, a.mode_m, a.mode_cls, a.mode_col, c->az_off.p, a.Km_dev, a.csize, Cm, c->Dp.p,
+                             c->stream, &c->launches);
+}
+
 // Projection of a full-sky spherical build onto its own azimuthal modes.
 // S_p is block circulant in phi (Q depends on |phi_a - phi_b| only and Nbar
 // does not depend on phi), and every mode is U_m[:, idx] (x) a cos or sin of
@@ -900,46 +976,22 @@ void project_azimuthal(opsec_gpu* c, int ncells, int M) {
     const int* d_mode_cls = d_mode_m + M;
     const int* d_mode_col = d_mode_cls + M;
     const int* d_Km = d_mode_col + M;
-    // the block eigenvectors the modes use, before the blocks are overwritten
-    c->Ucat.alloc((size_t)ncol * H);
-    launch_gather_block_vectors(H, ncol, d_col_m, d_col_idx, c->S.p, c->Ucat.p, c->stream, &c->launches);
-    std::vector<double> nba(H);
-    for (int h = 0; h < H; h++) nba[h] = c->nbar_arc[h];
+    if (!c->blas) blas_check(cublasCreate(&c->blas), "cublasCreate");
+    blas_check(cublasSetStream(c->blas, c->stream), "cublasSetStream");
+    std::vector<double> nba(c->nbar_arc);
     DevBuf<double> d_nba;
     d_nba.alloc(H);
     OPSEC_CUDA(cudaMemcpyAsync(d_nba.p, nba.data(), sizeof(double) * H, cudaMemcpyHostToDevice, c->stream));
-    c->S.alloc((size_t)nm * H * H);
-    c->Tm.alloc((size_t)H * std::max(Kmax, 1));
-    c->Cm.alloc((size_t)std::max(csize, 1LL) * nb);
-    if (!c->blas) blas_check(cublasCreate(&c->blas), "cublasCreate");
-    blas_check(cublasSetStream(c->blas, c->stream), "cublasSetStream");
-    const double one = 1.0, zero = 0.0;
-    for (int p = 0; p < nb; p++) {
-        if (g_clock) g_clock->begin("azimuthal_transform", c->stream, 2.0 * nm * (double)H * H * ks.nf);
-        launch_azimuthal_blocks(ks, c->Q.p + (size_t)(1 + p) * ks.nkeys, d_nba.p, nm, c->S.p, c->stream,
-                                &c->launches);
-        if (g_clock) g_clock->end(c->stream);
-        double fl = 0;
-        for (int m = 0; m < nm; m++) fl += 2.0 * H * H * Km[m] + 2.0 * H * (double)Km[m] * Km[m];
-        if (g_clock) g_clock->begin("azimuthal_gemm", c->stream, fl);
-        for (int m = 0; m < nm; m++) {
-            const int K = Km[m];
-            if (K == 0) continue;
-            const double* Sm = c->S.p + (size_t)m * H * H;
-            const double* U = c->Ucat.p + (size_t)base[m] * H;
-            blas_check(cublasDgemm(c->blas, CUBLAS_OP_N, CUBLAS_OP_N, H, K, H, &one, Sm, H, U, H, &zero, c->Tm.p, H),
-                       "cublasDgemm");
-            blas_check(cublasDgemm(c->blas, CUBLAS_OP_T, CUBLAS_OP_N, K, K, H, &one, U, H, c->Tm.p, H, &zero,
-                                   c->Cm.p + (size_t)p * csize + off[m], K),
-                       "cublasDgemm");
-            c->launches += 2;
-        }
-        if (g_clock) g_clock->end(c->stream);
-    }
     const size_t Kp = (size_t)M * (M + 1) / 2;
     c->Dp.alloc(Kp * nb);
-    launch_azimuthal_scatter(M, nb, d_mode_m, d_mode_cls, d_mode_col, c->az_off.p, d_Km, csize, c->Cm.p, c->Dp.p,
-                             c->stream, &c->launches);
+    double fl = 0;
+    for (int m = 0; m < nm; m++) fl += 2.0 * H * H * Km[m] + 2.0 * H * (double)Km[m] * Km[m];
+    AzPlan plan{H, nm, nb, ncol, csize, Kmax, fl, d_col_m, d_col_idx, d_mode_m, d_mode_cls, d_mode_col, d_Km, &Km,
+                &base, &off, d_nba.p};
+    if (c->az_gemm64)
+        az_blocks<double>(c, plan, M);
+    else
+        az_blocks<float>(c, plan, M);
     (void)ncells;
 }
 
@@ -1311,6 +1363,7 @@ void opsec_gpu_destroy(opsec_gpu* c) {
     if (c->device >= 0) cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->solver) cusolverDnDestroy(c->solver);
+    if (c->blas) cublasDestroy(c->blas);
     for (int j = 0; j < opsec_gpu::kSide; j++) {
         if (c->side[j]) cudaStreamSynchronize(c->side[j]);
         if (c->side_solver[j]) cusolverDnDestroy(c->side_solver[j]);

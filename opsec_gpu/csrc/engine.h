@@ -140,12 +140,19 @@ void launch_signal_block(const KeySpace& ks, const CellKeyInfo& ci, const double
 // Azimuthal blocks of a full-sky S: Sm[m][ha][hb] = D_ha D_hb sum_df Q(ha,hb,df) cos(2 pi m df/Nphi)
 void launch_azimuthal_blocks(const KeySpace& ks, const double* Qtab, const double* nbar_arc, int nm, double* Sm,
                              cudaStream_t st, long long* launches);
+void launch_azimuthal_blocks(const KeySpace& ks, const double* Qtab, const double* nbar_arc, int nm, float* Sm,
+                             cudaStream_t st, long long* launches);
 // Block eigenvector columns (m, idx) gathered into Ucat[col][h]
 void launch_gather_block_vectors(int H, int ncol, const int* col_m, const int* col_idx, const double* U, double* Ucat,
+                                 cudaStream_t st, long long* launches);
+void launch_gather_block_vectors(int H, int ncol, const int* col_m, const int* col_idx, const double* U, float* Ucat,
                                  cudaStream_t st, long long* launches);
 // Packed FP32 C_p of every band from per-block products C[p][blk_off[m] + col_i + col_j K_m]
 void launch_azimuthal_scatter(int M, int nbands, const int* mode_m, const int* mode_cls, const int* mode_col,
                               const long long* blk_off, const int* blk_K, long long csize, const double* C, float* Dp,
+                              cudaStream_t st, long long* launches);
+void launch_azimuthal_scatter(int M, int nbands, const int* mode_m, const int* mode_cls, const int* mode_col,
+                              const long long* blk_off, const int* blk_K, long long csize, const float* C, float* Dp,
                               cudaStream_t st, long long* launches);
 // Modes from block eigenvectors: B[mode][h*Nphi + f] = U_m[h][idx] * trig(m f)
 void launch_assemble_modes(int H, int Nphi, int nmodes, const int* sel_m, const int* sel_idx, const int* sel_kind,

@@ -61,7 +61,8 @@ __global__ void signal_block_kernel(KeySpace ks, CellKeyInfo ci, const double* Q
 // (cos(2 pi m (Nphi - df)/Nphi) = cos(2 pi m df/Nphi)).  The weighted cosines of the block
 // (m0 .. m0+nmb-1) x (df = 0..nf-1) sit in shared memory, computed with the angle reduced
 // exactly on the integer lattice; blockIdx.y picks the m of the output.
-__global__ void azimuthal_blocks_kernel(KeySpace ks, const double* Q, const double* nbar_arc, int nm, double* Sm) {
+template <typename T>
+__global__ void azimuthal_blocks_kernel(KeySpace ks, const double* Q, const double* nbar_arc, int nm, T* Sm) {
     extern __shared__ double cw[];  // [nm][nf]
     const int H = ks.H, Nphi = ks.N3, nf = ks.nf;
     for (int t = threadIdx.x; t < nm * nf; t += blockDim.x) {
@@ -81,20 +82,21 @@ __global__ void azimuthal_blocks_kernel(KeySpace ks, const double* Q, const doub
             const double* c = cw + m * nf;
             double acc = 0.0;
             for (int df = 0; df < nf; df++) acc = fma(q[df], c[df], acc);
-            Sm[(size_t)m * HH + r] = d * acc;
+            Sm[(size_t)m * HH + r] = (T)(d * acc);
         }
     }
 }
 
 // Ucat[col][h] = U_m[h][idx] for the listed (m, idx) columns: the block
 // eigenvectors the selected modes are built from, one copy per (m, idx).
+template <typename T>
 __global__ void gather_block_vectors_kernel(int H, int ncol, const int* col_m, const int* col_idx, const double* U,
-                                            double* Ucat) {
+                                            T* Ucat) {
     const long long total = (long long)ncol * H;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
          e += (long long)gridDim.x * blockDim.x) {
         const int c = (int)(e / H), h = (int)(e % H);
-        Ucat[e] = U[(size_t)col_m[c] * H * H + (size_t)col_idx[c] * H + h];
+        Ucat[e] = (T)U[(size_t)col_m[c] * H * H + (size_t)col_idx[c] * H + h];
     }
 }
 
@@ -102,16 +104,17 @@ __global__ void gather_block_vectors_kernel(int H, int ncol, const int* col_m, c
 // order and the same trig class (cos-type or sin-type) take C_m[col_i][col_j];
 // every other pair is zero by the orthogonality of the azimuthal factors.
 // blockIdx.z = band, blockIdx.y strides over j, threads over i <= j.
+template <typename T>
 __global__ void azimuthal_scatter_kernel(int M, const int* mode_m, const int* mode_cls, const int* mode_col,
-                                         const long long* blk_off, const int* blk_K, long long csize, const double* C,
+                                         const long long* blk_off, const int* blk_K, long long csize, const T* C,
                                          float* Dp) {
     const int p = blockIdx.z;
     const size_t K = (size_t)M * (M + 1) / 2;
-    const double* Cp = C + (size_t)p * csize;
+    const T* Cp = C + (size_t)p * csize;
     float* out = Dp + (size_t)p * K;
     for (int j = blockIdx.y; j < M; j += gridDim.y) {
         const int mj = mode_m[j], cj = mode_cls[j], colj = mode_col[j];
-        const double* Cj = Cp + blk_off[mj] + (size_t)colj * blk_K[mj];
+        const T* Cj = Cp + blk_off[mj] + (size_t)colj * blk_K[mj];
         const size_t row = (size_t)j * (j + 1) / 2;
         for (int i = blockIdx.x * blockDim.x + threadIdx.x; i <= j; i += gridDim.x * blockDim.x) {
             float v = 0.f;
@@ -207,24 +210,58 @@ void launch_signal_block(const KeySpace& ks, const CellKeyInfo& ci, const double
     ++*l;
 }
 
-void launch_azimuthal_blocks(const KeySpace& ks, const double* Q, const double* nbar_arc, int nm, double* Sm,
-                             cudaStream_t st, long long* l) {
+template <typename T>
+void launch_azimuthal_blocks_t(const KeySpace& ks, const double* Q, const double* nbar_arc, int nm, T* Sm,
+                               cudaStream_t st, long long* l) {
     if (!ks.fold) fail(OPSEC_ERR_CONFIG, "azimuthal blocks need a full-sky grid");
     const size_t smem = sizeof(double) * (size_t)nm * ks.nf;
     if (smem > 200 * 1024) fail(OPSEC_ERR_CONFIG, "too many phi cells for the azimuthal block transform");
-    OPSEC_CUDA(cudaFuncSetAttribute(azimuthal_blocks_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    OPSEC_CUDA(cudaFuncSetAttribute(azimuthal_blocks_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const long long HH = (long long)ks.H * ks.H;
     const int gy = nm < 8 ? nm : 8;
     long long gx = (HH + 255) / 256;
     if (gx > 4096) gx = 4096;
-    azimuthal_blocks_kernel<<<dim3((unsigned)gx, gy), 256, smem, st>>>(ks, Q, nbar_arc, nm, Sm);
+    azimuthal_blocks_kernel<T><<<dim3((unsigned)gx, gy), 256, smem, st>>>(ks, Q, nbar_arc, nm, Sm);
+    OPSEC_CUDA(cudaGetLastError());
+    ++*l;
+}
+
+void launch_azimuthal_blocks(const KeySpace& ks, const double* Q, const double* nbar_arc, int nm, double* Sm,
+                             cudaStream_t st, long long* l) {
+    launch_azimuthal_blocks_t(ks, Q, nbar_arc, nm, Sm, st, l);
+}
+
+void launch_azimuthal_blocks(const KeySpace& ks, const double* Q, const double* nbar_arc, int nm, float* Sm,
+                             cudaStream_t st, long long* l) {
+    launch_azimuthal_blocks_t(ks, Q, nbar_arc, nm, Sm, st, l);
+}
+
+template <typename T>
+void launch_gather_t(int H, int ncol, const int* col_m, const int* col_idx, const double* U, T* Ucat, cudaStream_t st,
+                     long long* l) {
+    gather_block_vectors_kernel<T><<<grid_for((long long)ncol * H), 256, 0, st>>>(H, ncol, col_m, col_idx, U, Ucat);
     OPSEC_CUDA(cudaGetLastError());
     ++*l;
 }
 
 void launch_gather_block_vectors(int H, int ncol, const int* col_m, const int* col_idx, const double* U, double* Ucat,
                                  cudaStream_t st, long long* l) {
-    gather_block_vectors_kernel<<<grid_for((long long)ncol * H), 256, 0, st>>>(H, ncol, col_m, col_idx, U, Ucat);
+    launch_gather_t(H, ncol, col_m, col_idx, U, Ucat, st, l);
+}
+
+void launch_gather_block_vectors(int H, int ncol, const int* col_m, const int* col_idx, const double* U, float* Ucat,
+                                 cudaStream_t st, long long* l) {
+    launch_gather_t(H, ncol, col_m, col_idx, U, Ucat, st, l);
+}
+
+template <typename T>
+void launch_scatter_t(int M, int nbands, const int* mode_m, const int* mode_cls, const int* mode_col,
+                      const long long* blk_off, const int* blk_K, long long csize, const T* C, float* Dp,
+                      cudaStream_t st, long long* l) {
+    const int gy = M < 8192 ? M : 8192;
+    const int gx = (M + 255) / 256 < 8 ? (M + 255) / 256 : 8;
+    azimuthal_scatter_kernel<T><<<dim3(gx, gy, nbands), 256, 0, st>>>(M, mode_m, mode_cls, mode_col, blk_off, blk_K,
+                                                                      csize, C, Dp);
     OPSEC_CUDA(cudaGetLastError());
     ++*l;
 }
@@ -232,12 +269,13 @@ void launch_gather_block_vectors(int H, int ncol, const int* col_m, const int* c
 void launch_azimuthal_scatter(int M, int nbands, const int* mode_m, const int* mode_cls, const int* mode_col,
                               const long long* blk_off, const int* blk_K, long long csize, const double* C, float* Dp,
                               cudaStream_t st, long long* l) {
-    const int gy = M < 8192 ? M : 8192;
-    const int gx = (M + 255) / 256 < 8 ? (M + 255) / 256 : 8;
-    azimuthal_scatter_kernel<<<dim3(gx, gy, nbands), 256, 0, st>>>(M, mode_m, mode_cls, mode_col, blk_off, blk_K,
-                                                                   csize, C, Dp);
-    OPSEC_CUDA(cudaGetLastError());
-    ++*l;
+    launch_scatter_t(M, nbands, mode_m, mode_cls, mode_col, blk_off, blk_K, csize, C, Dp, st, l);
+}
+
+void launch_azimuthal_scatter(int M, int nbands, const int* mode_m, const int* mode_cls, const int* mode_col,
+                              const long long* blk_off, const int* blk_K, long long csize, const float* C, float* Dp,
+                              cudaStream_t st, long long* l) {
+    launch_scatter_t(M, nbands, mode_m, mode_cls, mode_col, blk_off, blk_K, csize, C, Dp, st, l);
 }
 
 void launch_assemble_modes(int H, int Nphi, int nmodes, const int* sel_m, const int* sel_idx, const int* sel_kind,

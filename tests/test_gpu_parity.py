@@ -234,18 +234,21 @@ def test_fisher_build_azimuthal_projection():
     lam = np.sort(np.linalg.eigvalsh(S))[::-1]
     M = O.gap_nmodes(lam, 256, rel_gap=1e-4, span=64)
     out = {}
-    for proj in ("auto", "tc", "simt"):
-        e = api.Engine(api.make_config(sv, bands=bands, extra=[f"projection = {proj}"]))
+    for name, extra in (("az32", ["azimuthal.gemm = f32"]), ("az64", ["azimuthal.gemm = f64"]),
+                        ("tc", ["projection = tc"]), ("simt", ["projection = simt"])):
+        e = api.Engine(api.make_config(sv, bands=bands, extra=extra))
         e.set_pk(*PK)
-        out[proj] = e.fisher_build(cells, counts, M)
+        out[name] = e.fisher_build(cells, counts, M)
         e.close()
     scale = np.max(np.abs(out["simt"]["F"]))
-    d_tc = np.max(np.abs(out["auto"]["F"] - out["tc"]["F"])) / scale
-    d_simt = np.max(np.abs(out["auto"]["F"] - out["simt"]["F"])) / scale
-    print(f"azimuthal vs tc {d_tc:.2e}, vs simt {d_simt:.2e}")
-    assert d_tc <= 1e-6 and d_simt <= 1e-6, (d_tc, d_simt)
+    d = {k: np.max(np.abs(out[k]["F"] - out["az64"]["F"])) / scale for k in ("az32", "tc", "simt")}
+    print("F against the FP64 azimuthal projection: " + ", ".join(f"{k} {v:.2e}" for k, v in d.items()))
+    assert max(d.values()) <= 1e-6, d
     ref = O.fisher_build(sv, cells, counts, *PK, bands, M)
-    check_estimates(out["auto"], ref, "shell1024/end-to-end", tol=1e-5)
+    for k in ("az32", "az64"):
+        rel = np.max(np.abs(out[k]["F"] - ref["est"]["F"])) / np.max(np.abs(ref["est"]["F"]))
+        print(f"{k}: end-to-end Fisher rel err {rel:.2e}")
+        check_estimates(out[k], ref, f"shell1024/{k}/end-to-end", tol=1e-5)
 
 
 def check_estimates(got, ref, name, tol=1e-6):
