@@ -90,6 +90,10 @@ template struct DevBuf<int>;
 template struct DevBuf<unsigned char>;
 template struct DevBuf<long long>;
 
+bool Geometry::mu_symmetric() const {
+    return coordsys == 2 && std::fabs(b[2] + b[3]) <= 1e-12 * std::fabs(b[3] - b[2]);
+}
+
 bool Geometry::full_sky() const { return coordsys == 2 && std::fabs(b[5] - b[4] - 2 * M_PI) < 1e-12; }
 
 // ---------------------------------------------------------------- config
@@ -247,7 +251,7 @@ struct opsec_gpu {
     cusolverDnHandle_t solver = nullptr;
     cublasHandle_t blas = nullptr;
     // side streams for the independent azimuthal eigenproblems
-    static constexpr int kSide = 6;
+    static constexpr int kSide = 16;
     cudaStream_t side[kSide] = {};
     cusolverDnHandle_t side_solver[kSide] = {};
     cudaEvent_t side_ev[kSide + 1] = {};
@@ -265,6 +269,11 @@ struct opsec_gpu {
     int proj_chunk = 1;
     int cub_exact = 1;
     int az_gemm64 = 0;
+    bool cub_reflect = true;
+    bool az_parity = true;
+    bool az_batched = true;
+    int az_streams = 6;
+    int az_npar = 1;
     std::vector<double> pk_k, pk_P;
     std::vector<double> band_lo, band_hi;
 
@@ -485,6 +494,25 @@ void configure(opsec_gpu* c, const std::map<std::string, std::string>& kv) {
         else
             fail(OPSEC_ERR_CONFIG, "azimuthal.gemm must be f64 or f32");
     }
+    if (has("azimuthal.parity")) c->az_parity = get("azimuthal.parity") != "0";
+    if (has("azimuthal.eig")) {
+        const std::string& v = get("azimuthal.eig");
+        if (v != "streams" && v != "batched") fail(OPSEC_ERR_CONFIG, "azimuthal.eig must be streams or batched");
+        c->az_batched = v == "batched";
+    }
+    if (has("azimuthal.streams")) {
+        c->az_streams = to_int("azimuthal.streams", get("azimuthal.streams"));
+        if (c->az_streams < 1 || c->az_streams > opsec_gpu::kSide) fail(OPSEC_ERR_CONFIG, "azimuthal.streams must be in [1, 16]");
+    }
+    if (has("cubature.symmetry")) {
+        const std::string& v = get("cubature.symmetry");
+        if (v == "reflect")
+            c->cub_reflect = true;
+        else if (v == "none")
+            c->cub_reflect = false;
+        else
+            fail(OPSEC_ERR_CONFIG, "cubature.symmetry must be reflect or none");
+    }
     if (has("cubature.precision")) {
         const std::string& v = get("cubature.precision");
         if (v == "exact")
@@ -558,6 +586,8 @@ void setup_keys(opsec_gpu* c) {
     } else {
         ks.H = ks.N1 * ks.N2;
         ks.fold = c->geo.full_sky();
+        // reflection z -> -z maps mu cell j to N_mu-1-j when the mu range is symmetric about 0
+        ks.mu_reflect = c->cub_reflect && c->geo.mu_symmetric();
         ks.nf = ks.fold ? ks.N3 / 2 + 1 : ks.N3;
         ks.nkeys = (long long)ks.H * (ks.H + 1) / 2 * ks.nf;
         ks.nsquare = (long long)ks.H * ks.H * ks.nf;
@@ -735,24 +765,55 @@ int eigensolve(opsec_gpu* c, int ncells, const opsec_cell* cells, int M) {
     c->az_valid = false;
     if (azimuthal_ok(c, ncells, cells)) {
         const KeySpace& ks = c->ks;
-        const int H = ks.H, Nphi = ks.N3, nm = Nphi / 2 + 1;
+        const int H = ks.H, Nphi = ks.N3, Nmu = ks.N2, nm = Nphi / 2 + 1;
         std::vector<double> nba(H);
         for (int h = 0; h < H; h++) nba[h] = cells[(size_t)h * Nphi].Nbar;
         c->nbar_arc = nba;
+        // mu parity split: reflection-symmetric mu grid, even N_mu, Nbar symmetric under j -> N_mu-1-j
+        bool par = c->az_parity && c->geo.mu_symmetric() && Nmu % 2 == 0;
+        for (int h = 0; par && h < H; h++) {
+            const int ph = (h / Nmu) * Nmu + (Nmu - 1 - h % Nmu);
+            if (std::fabs(nba[h] - nba[ph]) > 1e-12 * nba[h]) par = false;
+        }
+        const int npar = par ? 2 : 1, Hb = H / npar, nblk = nm * npar;
+        c->az_npar = npar;
         DevBuf<double> d_nba;
         d_nba.alloc(H);
         OPSEC_CUDA(cudaMemcpyAsync(d_nba.p, nba.data(), sizeof(double) * H, cudaMemcpyHostToDevice, c->stream));
-        c->S.alloc((size_t)nm * H * H);
-        launch_azimuthal_blocks(ks, c->Q.p, d_nba.p, nm, c->S.p, c->stream, &c->launches);
-        c->W.alloc((size_t)nm * H);
-        c->info.alloc(nm);
+        c->S.alloc((size_t)nblk * Hb * Hb);
+        launch_azimuthal_blocks(ks, c->Q.p, d_nba.p, nm, npar, c->S.p, c->stream, &c->launches);
+        c->W.alloc((size_t)nblk * Hb);
+        c->info.alloc(nblk);
         int lwork = 0;
-        solver_check(cusolverDnDsyevd_bufferSize(c->solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, H, c->S.p,
-                                                 H, c->W.p, &lwork),
+        solver_check(cusolverDnDsyevd_bufferSize(c->solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, Hb,
+                                                 c->S.p, Hb, c->W.p, &lwork),
                      "syevd_bufferSize");
-        // the nm block eigenproblems are independent: spread them over side streams
-        const int ns = std::min(nm, (int)opsec_gpu::kSide);
-        c->work.alloc((size_t)lwork * ns);
+        bool batched_done = false;
+        if (c->az_batched) {
+            // one batched call over the equal-size blocks; streams of single solves if it is refused
+            cusolverDnParams_t prm = nullptr;
+            solver_check(cusolverDnCreateParams(&prm), "cusolverDnCreateParams");
+            size_t dbytes = 0, hbytes = 0;
+            cusolverStatus_t st = cusolverDnXsyevBatched_bufferSize(
+                c->solver, prm, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, Hb, CUDA_R_64F, c->S.p, Hb,
+                CUDA_R_64F, c->W.p, CUDA_R_64F, &dbytes, &hbytes, nblk);
+            if (st == CUSOLVER_STATUS_SUCCESS) {
+                DevBuf<unsigned char> dw;
+                dw.alloc(std::max<size_t>(dbytes, 1));
+                std::vector<unsigned char> hw(std::max<size_t>(hbytes, 1));
+                st = cusolverDnXsyevBatched(c->solver, prm, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, Hb,
+                                            CUDA_R_64F, c->S.p, Hb, CUDA_R_64F, c->W.p, CUDA_R_64F, dw.p, dbytes,
+                                            hw.data(), hbytes, c->info.p, nblk);
+                sync(c);
+            }
+            cusolverDnDestroyParams(prm);
+            batched_done = st == CUSOLVER_STATUS_SUCCESS;
+            if (!batched_done)  // the blocks may have been partly overwritten: rebuild them
+                launch_azimuthal_blocks(ks, c->Q.p, d_nba.p, nm, npar, c->S.p, c->stream, &c->launches);
+        }
+        // the block eigenproblems are independent: spread them over side streams
+        const int ns = batched_done ? 0 : std::min(nblk, c->az_streams);
+        c->work.alloc((size_t)lwork * std::max(ns, 1));
         for (int j = 0; j < ns; j++) {
             if (!c->side[j]) OPSEC_CUDA(cudaStreamCreateWithFlags(&c->side[j], cudaStreamNonBlocking));
             if (!c->side_solver[j]) solver_check(cusolverDnCreate(&c->side_solver[j]), "cusolverDnCreate");
@@ -762,52 +823,55 @@ int eigensolve(opsec_gpu* c, int ncells, const opsec_cell* cells, int M) {
             if (!c->side_ev[j]) OPSEC_CUDA(cudaEventCreateWithFlags(&c->side_ev[j], cudaEventDisableTiming));
         OPSEC_CUDA(cudaEventRecord(c->side_ev[ns], c->stream));
         for (int j = 0; j < ns; j++) OPSEC_CUDA(cudaStreamWaitEvent(c->side[j], c->side_ev[ns], 0));
-        for (int m = 0; m < nm; m++) {
-            const int j = m % ns;
-            solver_check(cusolverDnDsyevd(c->side_solver[j], CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, H,
-                                          c->S.p + (size_t)m * H * H, H, c->W.p + (size_t)m * H,
-                                          c->work.p + (size_t)j * lwork, lwork, c->info.p + m),
+        for (int b = 0; b < nblk && ns > 0; b++) {
+            const int j = b % ns;
+            solver_check(cusolverDnDsyevd(c->side_solver[j], CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, Hb,
+                                          c->S.p + (size_t)b * Hb * Hb, Hb, c->W.p + (size_t)b * Hb,
+                                          c->work.p + (size_t)j * lwork, lwork, c->info.p + b),
                          "syevd");
         }
         for (int j = 0; j < ns; j++) {
             OPSEC_CUDA(cudaEventRecord(c->side_ev[j], c->side[j]));
             OPSEC_CUDA(cudaStreamWaitEvent(c->stream, c->side_ev[j], 0));
         }
-        check_info(c, nm);
-        std::vector<double> w((size_t)nm * H);
+        check_info(c, nblk);
+        std::vector<double> w((size_t)nblk * Hb);
         OPSEC_CUDA(cudaMemcpyAsync(w.data(), c->W.p, sizeof(double) * w.size(), cudaMemcpyDeviceToHost, c->stream));
         sync(c);
         struct Ent {
             double lam;
-            int m, idx, kind;
+            int b, idx, kind;
         };
         std::vector<Ent> ent;
         ent.reserve((size_t)H * Nphi);
-        for (int m = 0; m < nm; m++)
-            for (int i = 0; i < H; i++) {
-                double lam = w[(size_t)m * H + i];
+        for (int b = 0; b < nblk; b++) {
+            const int m = b / npar;
+            for (int i = 0; i < Hb; i++) {
+                double lam = w[(size_t)b * Hb + i];
                 if (m == 0)
-                    ent.push_back({lam, m, i, 0});
+                    ent.push_back({lam, b, i, 0});
                 else if (2 * m == Nphi)
-                    ent.push_back({lam, m, i, 3});
+                    ent.push_back({lam, b, i, 3});
                 else {
-                    ent.push_back({lam, m, i, 1});
-                    ent.push_back({lam, m, i, 2});
+                    ent.push_back({lam, b, i, 1});
+                    ent.push_back({lam, b, i, 2});
                 }
             }
+        }
         std::stable_sort(ent.begin(), ent.end(), [](const Ent& x, const Ent& y) {
             if (x.lam != y.lam) return x.lam > y.lam;
-            if (x.m != y.m) return x.m < y.m;
+            if (x.b != y.b) return x.b < y.b;
             if (x.idx != y.idx) return x.idx < y.idx;
             return x.kind < y.kind;
         });
-        if (M < (int)ent.size() && ent[M - 1].kind == 1 && ent[M].kind == 2 && ent[M].m == ent[M - 1].m &&
+        if (M < (int)ent.size() && ent[M - 1].kind == 1 && ent[M].kind == 2 && ent[M].b == ent[M - 1].b &&
             ent[M].idx == ent[M - 1].idx)
-            c->warning = "Nmodes splits a degenerate (cos, sin) pair of azimuthal order m=" + std::to_string(ent[M].m);
+            c->warning = "Nmodes splits a degenerate (cos, sin) pair of azimuthal order m=" +
+                         std::to_string(ent[M].b / npar);
         std::vector<int> sel((size_t)3 * M);
         std::vector<double> ev(M);
         for (int i = 0; i < M; i++) {
-            sel[i] = ent[i].m;
+            sel[i] = ent[i].b;
             sel[M + i] = ent[i].idx;
             sel[2 * M + i] = ent[i].kind;
             ev[i] = ent[i].lam;
@@ -815,8 +879,8 @@ int eigensolve(opsec_gpu* c, int ncells, const opsec_cell* cells, int M) {
         c->sel.alloc(sel.size());
         OPSEC_CUDA(cudaMemcpyAsync(c->sel.p, sel.data(), sizeof(int) * sel.size(), cudaMemcpyHostToDevice, c->stream));
         OPSEC_CUDA(cudaMemcpyAsync(c->evals.p, ev.data(), sizeof(double) * M, cudaMemcpyHostToDevice, c->stream));
-        launch_assemble_modes(H, Nphi, M, c->sel.p, c->sel.p + M, c->sel.p + 2 * M, c->S.p, c->modes.p, c->stream,
-                              &c->launches);
+        launch_assemble_modes(H, Nphi, Nmu, npar, M, c->sel.p, c->sel.p + M, c->sel.p + 2 * M, c->S.p, c->modes.p,
+                              c->stream, &c->launches);
         sync(c);
         c->az_m.assign(sel.begin(), sel.begin() + M);
         c->az_idx.assign(sel.begin() + M, sel.begin() + 2 * M);
@@ -851,7 +915,7 @@ int eigensolve(opsec_gpu* c, int ncells, const opsec_cell* cells, int M) {
 }
 
 struct AzPlan {
-    int H, nm, nb, ncol;
+    int H, nm, npar, nb, ncol;  // H: block size (arcs / npar)
     long long csize;
     int Kmax;
     double flops;
@@ -884,7 +948,8 @@ template <typename T>
 void az_blocks(opsec_gpu* c, const AzPlan& a, int M) {
     const int H = a.H;
     DevBuf<unsigned char>& ws = c->azws;
-    const size_t nU = (size_t)a.ncol * H, nS = (size_t)a.nm * H * H, nT = (size_t)H * std::max(a.Kmax, 1),
+    const int nblk = a.nm * a.npar;
+    const size_t nU = (size_t)a.ncol * H, nS = (size_t)nblk * H * H, nT = (size_t)H * std::max(a.Kmax, 1),
                  nC = (size_t)std::max(a.csize, 1LL) * a.nb;
     ws.alloc(sizeof(T) * (nU + nS + nT + nC));
     T* U = reinterpret_cast<T*>(ws.p);
@@ -894,12 +959,12 @@ void az_blocks(opsec_gpu* c, const AzPlan& a, int M) {
     // the block eigenvectors the modes use
     launch_gather_block_vectors(H, a.ncol, a.col_m, a.col_idx, c->S.p, U, c->stream, &c->launches);
     for (int p = 0; p < a.nb; p++) {
-        if (g_clock) g_clock->begin("azimuthal_transform", c->stream, 2.0 * a.nm * (double)H * H * c->ks.nf);
-        launch_azimuthal_blocks(c->ks, c->Q.p + (size_t)(1 + p) * c->ks.nkeys, a.nbar_arc, a.nm, Sb, c->stream,
-                                &c->launches);
+        if (g_clock) g_clock->begin("azimuthal_transform", c->stream, 2.0 * nblk * (double)H * H * c->ks.nf);
+        launch_azimuthal_blocks(c->ks, c->Q.p + (size_t)(1 + p) * c->ks.nkeys, a.nbar_arc, a.nm, a.npar, Sb,
+                                c->stream, &c->launches);
         if (g_clock) g_clock->end(c->stream);
         if (g_clock) g_clock->begin("azimuthal_gemm", c->stream, a.flops);
-        for (int m = 0; m < a.nm; m++) {
+        for (int m = 0; m < nblk; m++) {
             const int K = (*a.Km)[m];
             if (K == 0) continue;
             const T* Sm = Sb + (size_t)m * H * H;
@@ -928,16 +993,16 @@ void az_blocks(opsec_gpu* c, const AzPlan& a, int M) {
 // order m), against 2 N^2 M + N M^2 for the dense projection.
 void project_azimuthal(opsec_gpu* c, int ncells, int M) {
     const KeySpace& ks = c->ks;
-    const int H = ks.H, Nphi = ks.N3, nm = Nphi / 2 + 1;
+    const int Nphi = ks.N3, nm = Nphi / 2 + 1, npar = c->az_npar, nblk = nm * npar, H = ks.H / npar;
     const int nb = c->ntab() - 1;
-    // distinct (m, idx) columns, grouped by m
-    std::vector<std::vector<int>> cols(nm);
+    // distinct (block, idx) columns, grouped by block (block = m npar + mu parity)
+    std::vector<std::vector<int>> cols(nblk);
     for (int i = 0; i < M; i++) cols[c->az_m[i]].push_back(c->az_idx[i]);
-    std::vector<int> col_m, col_idx, Km(nm), base(nm);
-    std::vector<long long> off(nm);
+    std::vector<int> col_m, col_idx, Km(nblk), base(nblk);
+    std::vector<long long> off(nblk);
     long long csize = 0;
     int Kmax = 0;
-    for (int m = 0; m < nm; m++) {
+    for (int m = 0; m < nblk; m++) {
         auto& v = cols[m];
         std::sort(v.begin(), v.end());
         v.erase(std::unique(v.begin(), v.end()), v.end());
@@ -968,8 +1033,8 @@ void project_azimuthal(opsec_gpu* c, int ncells, int M) {
     ti.insert(ti.end(), Km.begin(), Km.end());
     c->az_i.alloc(ti.size());
     OPSEC_CUDA(cudaMemcpyAsync(c->az_i.p, ti.data(), sizeof(int) * ti.size(), cudaMemcpyHostToDevice, c->stream));
-    c->az_off.alloc(nm);
-    OPSEC_CUDA(cudaMemcpyAsync(c->az_off.p, off.data(), sizeof(long long) * nm, cudaMemcpyHostToDevice, c->stream));
+    c->az_off.alloc(nblk);
+    OPSEC_CUDA(cudaMemcpyAsync(c->az_off.p, off.data(), sizeof(long long) * nblk, cudaMemcpyHostToDevice, c->stream));
     const int* d_col_m = c->az_i.p;
     const int* d_col_idx = d_col_m + ncol;
     const int* d_mode_m = d_col_idx + ncol;
@@ -980,13 +1045,13 @@ void project_azimuthal(opsec_gpu* c, int ncells, int M) {
     blas_check(cublasSetStream(c->blas, c->stream), "cublasSetStream");
     std::vector<double> nba(c->nbar_arc);
     DevBuf<double> d_nba;
-    d_nba.alloc(H);
-    OPSEC_CUDA(cudaMemcpyAsync(d_nba.p, nba.data(), sizeof(double) * H, cudaMemcpyHostToDevice, c->stream));
+    d_nba.alloc(nba.size());
+    OPSEC_CUDA(cudaMemcpyAsync(d_nba.p, nba.data(), sizeof(double) * nba.size(), cudaMemcpyHostToDevice, c->stream));
     const size_t Kp = (size_t)M * (M + 1) / 2;
     c->Dp.alloc(Kp * nb);
     double fl = 0;
-    for (int m = 0; m < nm; m++) fl += 2.0 * H * H * Km[m] + 2.0 * H * (double)Km[m] * Km[m];
-    AzPlan plan{H, nm, nb, ncol, csize, Kmax, fl, d_col_m, d_col_idx, d_mode_m, d_mode_cls, d_mode_col, d_Km, &Km,
+    for (int m = 0; m < nblk; m++) fl += 2.0 * H * H * Km[m] + 2.0 * H * (double)Km[m] * Km[m];
+    AzPlan plan{H, nm, npar, nb, ncol, csize, Kmax, fl, d_col_m, d_col_idx, d_mode_m, d_mode_cls, d_mode_col, d_Km, &Km,
                 &base, &off, d_nba.p};
     if (c->az_gemm64)
         az_blocks<double>(c, plan, M);

@@ -95,6 +95,27 @@ __device__ __forceinline__ void decode_key(const KeySpace& ks, long long key, in
     c2[0] = hb / ks.N2; c2[1] = hb % ks.N2; c2[2] = df;
 }
 
+// Spherical grids whose mu range is symmetric about 0: the reflection
+// z -> -z maps arc h = (i, j) to P h = (i, N_mu-1-j) and leaves phi alone, so
+// Q(h_a, h_b, df) = Q(P h_a, P h_b, df).  Of the two keys of such an orbit the
+// one with the smaller (h_a, h_b) triangle index is integrated; the other is
+// copied after the cubature.  Returns the partner key (= key on self-orbits).
+__device__ __forceinline__ long long reflect_partner(const KeySpace& ks, long long key) {
+    const int df = (int)(key % ks.nf);
+    const long long tri = key / ks.nf;
+    const double H2 = 2.0 * ks.H + 1.0;
+    int ha = (int)floor((H2 - sqrt(H2 * H2 - 8.0 * (double)tri)) * 0.5);
+    if (ha < 0) ha = 0;
+    while (ha > 0 && (long long)ha * ks.H - (long long)ha * (ha - 1) / 2 > tri) --ha;
+    while ((long long)(ha + 1) * ks.H - (long long)(ha + 1) * ha / 2 <= tri) ++ha;
+    const int hb = ha + (int)(tri - ((long long)ha * ks.H - (long long)ha * (ha - 1) / 2));
+    const int pa = (ha / ks.N2) * ks.N2 + (ks.N2 - 1 - ha % ks.N2);
+    const int pb = (hb / ks.N2) * ks.N2 + (ks.N2 - 1 - hb % ks.N2);
+    const int p1 = min(pa, pb), p2 = max(pa, pb);
+    const long long ptri = (long long)p1 * ks.H - (long long)p1 * (p1 - 1) / 2 + (p2 - p1);
+    return ptri * ks.nf + df;
+}
+
 // Knuth's two-sum: s + e == a + b exactly.  The _rn intrinsics keep the
 // compiler from contracting a product that feeds these sums into an FMA.
 __device__ __forceinline__ float two_sum(float a, float b, float* e) {
@@ -147,6 +168,16 @@ __global__ void point_table_kernel(CubatureArgs a, int ng, long long ncell) {
     }
 }
 
+// Q of the keys skipped by the reflection symmetry, from their partners.
+__global__ void reflect_fill_kernel(KeySpace ks, int ntab, double* Q) {
+    for (long long key = blockIdx.x * (long long)blockDim.x + threadIdx.x; key < ks.nkeys;
+         key += (long long)gridDim.x * blockDim.x) {
+        const long long p = reflect_partner(ks, key);
+        if (p < key)
+            for (int t = 0; t < ntab; t++) Q[(size_t)t * ks.nkeys + key] = Q[(size_t)t * ks.nkeys + p];
+    }
+}
+
 __device__ __forceinline__ long long cell_id(const KeySpace& ks, const int* c) {
     return ((long long)c[0] * ks.N2 + c[1]) * ks.N3 + c[2];
 }
@@ -182,6 +213,7 @@ __global__ void __launch_bounds__(Shape<NG>::kWarps * 32, 1)
 
     for (long long key = (long long)blockIdx.x * kWarps + warp; key < a.ks.nkeys;
          key += (long long)gridDim.x * kWarps) {
+        if (a.ks.coordsys == 2 && a.ks.mu_reflect && reflect_partner(a.ks, key) < key) continue;  // copied later
         int c1[3], c2[3];
         decode_key(a.ks, key, c1, c2);
         const float4* G1 = a.pts + 2 * NP * cell_id(a.ks, c1);
@@ -442,6 +474,13 @@ void launch_cubature(const CubatureArgs& a, cudaStream_t s, long long* launches)
     case 5: run_mode<5>(a, lk, s, launches); break;
     case 6: run_mode<6>(a, lk, s, launches); break;
     default: fail(OPSEC_ERR_CONFIG, "sig.gauss must be between 1 and 6");
+    }
+    if (a.ks.coordsys == 2 && a.ks.mu_reflect) {
+        long long blocks = (a.ks.nkeys + 255) / 256;
+        if (blocks > 65536) blocks = 65536;
+        reflect_fill_kernel<<<(unsigned)blocks, 256, 0, s>>>(a.ks, a.ntab, a.Q);
+        OPSEC_CUDA(cudaGetLastError());
+        ++*launches;
     }
 }
 

@@ -35,6 +35,7 @@ struct Geometry {
     int n[3] = {0};     // N1, N2, N3
     double L = 0;       // periodic box size; 0 = open box
     bool full_sky() const;
+    bool mu_symmetric() const;  // spherical mu range symmetric about 0 (reflection z -> -z maps the grid to itself)
 };
 
 // r grid of the xi tables: n1 linear points on [0, r1), n2 log points on [r1, r2]
@@ -65,6 +66,7 @@ struct KeySpace {
     int H = 0;        // spherical: arcs (Nr*Nmu)
     int nf = 0;       // spherical: phi offsets kept (Nphi, or Nphi/2+1 folded)
     bool fold = false;
+    bool mu_reflect = false;  // spherical: mu grid symmetric about 0, Q(h_a,h_b,df) = Q(P h_a,P h_b,df)
     long long nkeys = 0;     // keys integrated by the cubature kernel
     long long nsquare = 0;   // entries of the expanded table read by the projection
 };
@@ -138,10 +140,11 @@ void launch_signal_block(const KeySpace& ks, const CellKeyInfo& ci, const double
                          int ncols, const int* cols, double* s, int lld, cudaStream_t st, long long* launches);
 
 // Azimuthal blocks of a full-sky S: Sm[m][ha][hb] = D_ha D_hb sum_df Q(ha,hb,df) cos(2 pi m df/Nphi)
-void launch_azimuthal_blocks(const KeySpace& ks, const double* Qtab, const double* nbar_arc, int nm, double* Sm,
-                             cudaStream_t st, long long* launches);
-void launch_azimuthal_blocks(const KeySpace& ks, const double* Qtab, const double* nbar_arc, int nm, float* Sm,
-                             cudaStream_t st, long long* launches);
+// npar = 2 splits each order into its mu-even and mu-odd blocks (half size); block b = m npar + parity
+void launch_azimuthal_blocks(const KeySpace& ks, const double* Qtab, const double* nbar_arc, int nm, int npar,
+                             double* Sm, cudaStream_t st, long long* launches);
+void launch_azimuthal_blocks(const KeySpace& ks, const double* Qtab, const double* nbar_arc, int nm, int npar,
+                             float* Sm, cudaStream_t st, long long* launches);
 // Block eigenvector columns (m, idx) gathered into Ucat[col][h]
 void launch_gather_block_vectors(int H, int ncol, const int* col_m, const int* col_idx, const double* U, double* Ucat,
                                  cudaStream_t st, long long* launches);
@@ -155,8 +158,8 @@ void launch_azimuthal_scatter(int M, int nbands, const int* mode_m, const int* m
                               const long long* blk_off, const int* blk_K, long long csize, const float* C, float* Dp,
                               cudaStream_t st, long long* launches);
 // Modes from block eigenvectors: B[mode][h*Nphi + f] = U_m[h][idx] * trig(m f)
-void launch_assemble_modes(int H, int Nphi, int nmodes, const int* sel_m, const int* sel_idx, const int* sel_kind,
-                           const double* U, double* modes, cudaStream_t st, long long* launches);
+void launch_assemble_modes(int H, int Nphi, int Nmu, int npar, int nmodes, const int* sel_b, const int* sel_idx,
+                           const int* sel_kind, const double* U, double* modes, cudaStream_t st, long long* launches);
 
 // Projection C_p = B'^T Q_p B' for all bands; B' = diag(sqrt Nbar) B.
 struct ProjectArgs {

@@ -56,15 +56,19 @@ __global__ void signal_block_kernel(KeySpace ks, CellKeyInfo ci, const double* Q
     }
 }
 
-// Sm[m][hb*H + ha] (column-major H x H) = sqrt(Nbar_ha Nbar_hb) sum_d Q(ha,hb,|d|) cos(2 pi m d / Nphi).
+// Azimuthal blocks of a full-sky S (or S_p): S(m)[h][h'] = D_h D_h' sum_d Q(h,h',|d|) cos(2 pi m d/Nphi).
 // Folded form: sum over df = 0..Nphi/2 with weight 1 at df = 0 and df = Nphi/2, 2 between
-// (cos(2 pi m (Nphi - df)/Nphi) = cos(2 pi m df/Nphi)).  The weighted cosines of the block
-// (m0 .. m0+nmb-1) x (df = 0..nf-1) sit in shared memory, computed with the angle reduced
-// exactly on the integer lattice; blockIdx.y picks the m of the output.
+// (cos(2 pi m (Nphi - df)/Nphi) = cos(2 pi m df/Nphi)); the weighted cosines sit in shared
+// memory, computed with the angle reduced exactly on the integer lattice.
+//
+// npar = 2 (mu grid symmetric about 0, N_mu even, Nbar symmetric): the reflection
+// P(i, j) = (i, N_mu-1-j) commutes with S(m), which splits into an even and an odd block
+// over the half grid x = (i, j < N_mu/2):  S_+-(m)[x][y] = S(m)[h_x][h_y] +- S(m)[h_x][P h_y].
+// Output block b = m npar + parity, Hb = H / npar, column-major [b][y][x].
 template <typename T>
-__global__ void azimuthal_blocks_kernel(KeySpace ks, const double* Q, const double* nbar_arc, int nm, T* Sm) {
+__global__ void azimuthal_blocks_kernel(KeySpace ks, const double* Q, const double* nbar_arc, int nm, int npar, T* Sm) {
     extern __shared__ double cw[];  // [nm][nf]
-    const int H = ks.H, Nphi = ks.N3, nf = ks.nf;
+    const int H = ks.H, Nphi = ks.N3, nf = ks.nf, Nmu = ks.N2;
     for (int t = threadIdx.x; t < nm * nf; t += blockDim.x) {
         const int m = t / nf, df = t % nf;
         const int md = (int)(((long long)m * df) % Nphi);
@@ -72,17 +76,27 @@ __global__ void azimuthal_blocks_kernel(KeySpace ks, const double* Q, const doub
         cw[t] = w * cospi(2.0 * md / Nphi);
     }
     __syncthreads();
-    const long long HH = (long long)H * H;
+    const int Hb = H / npar, half = Nmu / npar;
+    const long long HH = (long long)Hb * Hb;
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < HH; r += (long long)gridDim.x * blockDim.x) {
-        const int hb = (int)(r / H), ha = (int)(r % H);
-        const int h1 = min(ha, hb), h2 = max(ha, hb);
-        const double* q = Q + tri_index(h1, h2, H) * nf;
+        const int y = (int)(r / Hb), x = (int)(r % Hb);
+        const int ha = (x / half) * Nmu + x % half, hb = (y / half) * Nmu + y % half;
+        const double* q1 = Q + tri_index(min(ha, hb), max(ha, hb), H) * nf;
+        const int pb = (hb / Nmu) * Nmu + (Nmu - 1 - hb % Nmu);
+        const double* q2 = Q + tri_index(min(ha, pb), max(ha, pb), H) * nf;
         const double d = sqrt(nbar_arc[ha] * nbar_arc[hb]);
         for (int m = blockIdx.y; m < nm; m += gridDim.y) {
             const double* c = cw + m * nf;
-            double acc = 0.0;
-            for (int df = 0; df < nf; df++) acc = fma(q[df], c[df], acc);
-            Sm[(size_t)m * HH + r] = (T)(d * acc);
+            double a1 = 0.0;
+            for (int df = 0; df < nf; df++) a1 = fma(q1[df], c[df], a1);
+            if (npar == 1) {
+                Sm[(size_t)m * HH + r] = (T)(d * a1);
+            } else {
+                double a2 = 0.0;
+                for (int df = 0; df < nf; df++) a2 = fma(q2[df], c[df], a2);
+                Sm[(size_t)(2 * m) * HH + r] = (T)(d * (a1 + a2));
+                Sm[(size_t)(2 * m + 1) * HH + r] = (T)(d * (a1 - a2));
+            }
         }
     }
 }
@@ -124,19 +138,28 @@ __global__ void azimuthal_scatter_kernel(int M, const int* mode_m, const int* mo
     }
 }
 
-// modes[i][h*Nphi + f] = U_m[h][idx] * trig_kind(m f)
-__global__ void assemble_modes_kernel(int H, int Nphi, int nmodes, const int* sel_m, const int* sel_idx,
-                                      const int* sel_kind, const double* U, double* modes) {
+// modes[i][h*Nphi + f] = u_i(h) * trig_kind(m f), u_i the block eigenvector idx of block b = m npar + parity
+// expanded to the full arc grid: u(h_x) = U_b[x][idx] / sqrt(npar), u(P h_x) = +-u(h_x) (even / odd)
+__global__ void assemble_modes_kernel(int H, int Nphi, int Nmu, int npar, int nmodes, const int* sel_b,
+                                      const int* sel_idx, const int* sel_kind, const double* U, double* modes) {
     const long long N = (long long)H * Nphi;
     const long long total = (long long)nmodes * N;
-    const double c0 = 1.0 / sqrt((double)Nphi), c1 = sqrt(2.0 / Nphi);
+    const int Hb = H / npar, half = Nmu / npar;
+    const double c0 = 1.0 / sqrt((double)Nphi), c1 = sqrt(2.0 / Nphi), cp = npar == 2 ? sqrt(0.5) : 1.0;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
          e += (long long)gridDim.x * blockDim.x) {
         const int i = (int)(e / N);
         const long long a = e % N;
         const int h = (int)(a / Nphi), f = (int)(a % Nphi);
-        const int m = sel_m[i];
-        const double u = U[(size_t)m * H * H + (size_t)sel_idx[i] * H + h];
+        const int b = sel_b[i], m = b / npar;
+        int j = h % Nmu;
+        double sgn = cp;
+        if (j >= half) {  // reflected half (npar = 2 only)
+            j = Nmu - 1 - j;
+            if (b % 2 == 1) sgn = -cp;
+        }
+        const int x = (h / Nmu) * half + j;
+        const double u = sgn * U[(size_t)b * Hb * Hb + (size_t)sel_idx[i] * Hb + x];
         const int mf = (int)(((long long)m * f) % Nphi);
         double t;
         switch (sel_kind[i]) {
@@ -211,29 +234,30 @@ void launch_signal_block(const KeySpace& ks, const CellKeyInfo& ci, const double
 }
 
 template <typename T>
-void launch_azimuthal_blocks_t(const KeySpace& ks, const double* Q, const double* nbar_arc, int nm, T* Sm,
+void launch_azimuthal_blocks_t(const KeySpace& ks, const double* Q, const double* nbar_arc, int nm, int npar, T* Sm,
                                cudaStream_t st, long long* l) {
+    if (npar != 1 && !(npar == 2 && ks.N2 % 2 == 0)) fail(OPSEC_ERR_ARG, "parity split needs an even mu grid");
     if (!ks.fold) fail(OPSEC_ERR_CONFIG, "azimuthal blocks need a full-sky grid");
     const size_t smem = sizeof(double) * (size_t)nm * ks.nf;
     if (smem > 200 * 1024) fail(OPSEC_ERR_CONFIG, "too many phi cells for the azimuthal block transform");
     OPSEC_CUDA(cudaFuncSetAttribute(azimuthal_blocks_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const long long HH = (long long)ks.H * ks.H;
+    const long long HH = (long long)(ks.H / npar) * (ks.H / npar);
     const int gy = nm < 8 ? nm : 8;
     long long gx = (HH + 255) / 256;
     if (gx > 4096) gx = 4096;
-    azimuthal_blocks_kernel<T><<<dim3((unsigned)gx, gy), 256, smem, st>>>(ks, Q, nbar_arc, nm, Sm);
+    azimuthal_blocks_kernel<T><<<dim3((unsigned)gx, gy), 256, smem, st>>>(ks, Q, nbar_arc, nm, npar, Sm);
     OPSEC_CUDA(cudaGetLastError());
     ++*l;
 }
 
-void launch_azimuthal_blocks(const KeySpace& ks, const double* Q, const double* nbar_arc, int nm, double* Sm,
+void launch_azimuthal_blocks(const KeySpace& ks, const double* Q, const double* nbar_arc, int nm, int npar, double* Sm,
                              cudaStream_t st, long long* l) {
-    launch_azimuthal_blocks_t(ks, Q, nbar_arc, nm, Sm, st, l);
+    launch_azimuthal_blocks_t(ks, Q, nbar_arc, nm, npar, Sm, st, l);
 }
 
-void launch_azimuthal_blocks(const KeySpace& ks, const double* Q, const double* nbar_arc, int nm, float* Sm,
+void launch_azimuthal_blocks(const KeySpace& ks, const double* Q, const double* nbar_arc, int nm, int npar, float* Sm,
                              cudaStream_t st, long long* l) {
-    launch_azimuthal_blocks_t(ks, Q, nbar_arc, nm, Sm, st, l);
+    launch_azimuthal_blocks_t(ks, Q, nbar_arc, nm, npar, Sm, st, l);
 }
 
 template <typename T>
@@ -278,10 +302,10 @@ void launch_azimuthal_scatter(int M, int nbands, const int* mode_m, const int* m
     launch_scatter_t(M, nbands, mode_m, mode_cls, mode_col, blk_off, blk_K, csize, C, Dp, st, l);
 }
 
-void launch_assemble_modes(int H, int Nphi, int nmodes, const int* sel_m, const int* sel_idx, const int* sel_kind,
-                           const double* U, double* modes, cudaStream_t st, long long* l) {
-    assemble_modes_kernel<<<grid_for((long long)nmodes * H * Nphi), 256, 0, st>>>(H, Nphi, nmodes, sel_m, sel_idx,
-                                                                                 sel_kind, U, modes);
+void launch_assemble_modes(int H, int Nphi, int Nmu, int npar, int nmodes, const int* sel_b, const int* sel_idx,
+                           const int* sel_kind, const double* U, double* modes, cudaStream_t st, long long* l) {
+    assemble_modes_kernel<<<grid_for((long long)nmodes * H * Nphi), 256, 0, st>>>(H, Nphi, Nmu, npar, nmodes, sel_b,
+                                                                                 sel_idx, sel_kind, U, modes);
     OPSEC_CUDA(cudaGetLastError());
     ++*l;
 }
