@@ -98,17 +98,21 @@ def roofline(stats, clk, bf16, peak_kind):
     if s["count"] == 0 or s["ms"] <= 0:
         return None
     if dom == "cubature":
-        # bound by shared-memory table lookups: two 4-byte loads per lookup, 32 banks x 4 B per clock
-        # per SM -> 16 lookups / clock / SM.  No measured figure exists for it: derived from the
-        # SM count and the SM clock sampled under load.
+        # Unit: one Gauss-point pair x one xi table (an interpolated table value, weighted and summed).
+        # Reference roofline: evaluating each unit by two 4-byte shared-memory table loads, 32 banks x
+        # 4 B per clock per SM -> 16 units / clock / SM.  The window path does not load per unit (one
+        # pass over the pairs scatters interpolation weights into a per-key bin histogram, then one
+        # dot product per table), so it is measured against what direct lookups could reach.  No
+        # measured figure exists for shared memory: derived from the SM count and the sampled clock.
         nsm = 152
         mhz = clk.get("sm_mhz") or 2070.0
         peak = 16.0 * nsm * mhz * 1e6 / 1e9
         avg_s = s["ms"] / 1000.0 / s["count"]
         achieved = s["flops"] / s["count"] / avg_s / 1e9
-        return {"kernel": "cubature_kernel (exact mode)", "bound": "smem", "achieved": achieved, "peak": peak,
-                "unit": "Glookups/s", "frac": achieved / peak, "traffic": None,
-                "peak_kind": f"derived: 16 lookups/clk/SM x {nsm} SMs x {mhz:.0f} MHz (sampled median)",
+        return {"kernel": "cubature (window-histogram kernel for far keys, table-group kernel for near keys)",
+                "bound": "smem", "achieved": achieved, "peak": peak, "unit": "G pair-table units/s",
+                "frac": achieved / peak, "traffic": None,
+                "peak_kind": f"derived: 16 table lookups/clk/SM x {nsm} SMs x {mhz:.0f} MHz (sampled median)",
                 "algorithmic_unit": "one Gauss-point pair x one xi table", "avg_launch_ms": avg_s * 1000,
                 "launches": int(s["count"])}
     if dom == "project_step1":

@@ -270,6 +270,8 @@ struct opsec_gpu {
     int cub_exact = 1;
     int az_gemm64 = 0;
     bool cub_reflect = true;
+    int cub_window = 1;
+    int win_key = 384, win_flush = 8, win_dot64 = 0;
     bool az_parity = true;
     bool az_batched = true;
     int az_streams = 6;
@@ -287,6 +289,7 @@ struct opsec_gpu {
     DevBuf<float> Qsq;     // [ntab][nsquare]
     DevBuf<double> nodes;  // node tables for the cubature kernel
     DevBuf<float> cubpts;  // cubature point table, 8 floats per Gauss point of every cell
+    DevBuf<unsigned char> cubwork;  // cubature window-path scratch
     DevBuf<int> cell_i;    // d1,d2,d3 then h,f,g per cell
     DevBuf<double> nbar;
     DevBuf<int> rc;        // rows/cols for signal blocks
@@ -504,6 +507,12 @@ void configure(opsec_gpu* c, const std::map<std::string, std::string>& kv) {
         c->az_streams = to_int("azimuthal.streams", get("azimuthal.streams"));
         if (c->az_streams < 1 || c->az_streams > opsec_gpu::kSide) fail(OPSEC_ERR_CONFIG, "azimuthal.streams must be in [1, 16]");
     }
+    if (has("cubature.window")) c->cub_window = get("cubature.window") != "0";
+    if (has("cubature.window_bins")) c->win_key = to_int("cubature.window_bins", get("cubature.window_bins"));
+    if (c->win_key < 16 || c->win_key > 4096) fail(OPSEC_ERR_CONFIG, "cubature.window_bins must be in [16, 4096]");
+    if (has("cubature.flush")) c->win_flush = to_int("cubature.flush", get("cubature.flush"));
+    if (c->win_flush < 0) fail(OPSEC_ERR_CONFIG, "cubature.flush must be >= 0");
+    if (has("cubature.dot")) c->win_dot64 = get("cubature.dot") != "f32";
     if (has("cubature.symmetry")) {
         const std::string& v = get("cubature.symmetry");
         if (v == "reflect")
@@ -667,6 +676,15 @@ void build_q(opsec_gpu* c) {
     c->cubpts.alloc(8 * cubature_point_count(c->ks, ng));
     a.pts = reinterpret_cast<float4*>(c->cubpts.p);
     a.exact = c->cub_exact;
+    a.window = c->cub_window;
+    a.win_key = c->win_key;
+    a.win_flush = c->win_flush;
+    a.win_dot64 = c->win_dot64;
+    if (a.exact && a.window) {
+        a.work_bytes = cubature_work_bytes(c->ks, c->xl.n());
+        c->cubwork.alloc(a.work_bytes);
+        a.work = c->cubwork.p;
+    }
     launch_cubature(a, c->stream, &c->launches);
     sync(c);
     c->q_ok = true;

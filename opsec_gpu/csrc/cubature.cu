@@ -32,7 +32,9 @@
 //    sum and the warp reduction.
 // Periodic boxes wrap each pair difference into [-L/2, L/2) (BoxSurvey.cpp:26-30).
 #include <cmath>
+#include <algorithm>
 #include <cstring>
+#include <string>
 
 #include "engine.h"
 
@@ -133,6 +135,66 @@ __device__ __forceinline__ float diff2(float bh, float bl, float ah, float al, f
     return s;
 }
 
+// Table index (i, fr) of one point pair in exact mode: separation and r^2
+// as FP32 pairs, log2(r^2) split as E + log2(T_k) + log2(1 + delta).
+__device__ __forceinline__ void exact_index(const Lookup& lk, const int* s_ci, const float* s_cf, const float4* s_kt,
+                                            float4 B, float4 Bl, float ax, float alx, float ay, float aly, float az,
+                                            float alz, bool periodic, float Lh, float Ll, float hL, int& i,
+                                            float& fr) {
+    float lx, ly, lz;
+    float dx = diff2(B.x, Bl.x, ax, alx, &lx);
+    float dy = diff2(B.y, Bl.y, ay, aly, &ly);
+    float dz = diff2(B.z, Bl.z, az, alz, &lz);
+    if (periodic) {
+        // |d| in [L/2, L]: d -+ L is exact in FP32 (Sterbenz)
+        const float wx = (float)((dx < -hL) - (dx >= hL));
+        const float wy = (float)((dy < -hL) - (dy >= hL));
+        const float wz = (float)((dz < -hL) - (dz >= hL));
+        dx = fmaf(wx, Lh, dx); lx = fmaf(wx, Ll, lx);
+        dy = fmaf(wy, Lh, dy); ly = fmaf(wy, Ll, ly);
+        dz = fmaf(wz, Lh, dz); lz = fmaf(wz, Ll, lz);
+    }
+    // r^2 = hi + lo: exact squares by FMA, exact sums by two-sum
+    const float px = __fmul_rn(dx, dx), py = __fmul_rn(dy, dy), pz = __fmul_rn(dz, dz);
+    float e1, e2;
+    const float h1 = two_sum(px, py, &e1);
+    const float r2 = two_sum(h1, pz, &e2);
+    float r2l = fmaf(dx, dx, -px) + fmaf(dy, dy, -py) + fmaf(dz, dz, -pz) + (e1 + e2);
+    r2l = fmaf(2.f * dx, lx, fmaf(2.f * dy, ly, fmaf(2.f * dz, lz, r2l)));
+    if (r2 < lk.r1sq) {
+        // t = r n1 / r1 with r = rh + rl and n1 / r1 = inv_dr + inv_dr_lo; the
+        // fraction is formed from the exact residual of the rounded product
+        const float rh = sqrtf(r2);
+        const float rl = rh > 0.f ? __fdividef(fmaf(-rh, rh, r2) + r2l, 2.f * rh) : 0.f;
+        const float t = rh * lk.inv_dr;
+        i = (int)t;
+        fr = fmaf(rh, lk.inv_dr, -(float)i) + fmaf(rh, lk.inv_dr_lo, rl * lk.inv_dr);
+    } else {
+        const int bits = __float_as_int(r2);
+        const int eb = bits >> 23;  // biased exponent; r2 > 0 here
+        const int e = min(max(eb - 127 - lk.e0, 0), lk.ne - 1);
+        const int k = (bits >> (23 - kLogBits)) & (kLogN - 1);
+        const float Rk = __int_as_float(bits & ~((1 << (23 - kLogBits)) - 1));
+        const float4 kt = s_kt[k];
+        const float inv_pow = __int_as_float((254 - eb) << 23);  // 2^-(eb-127)
+        const float delta = ((r2 - Rk) + r2l) * (kt.x * inv_pow);
+        // ln(1 + delta), |delta| < 1/128: the series to delta^4 is good to 3e-12
+        const float ln1p = delta * fmaf(-delta, fmaf(-delta, fmaf(-delta, 0.25f, 1.f / 3.f), 0.5f), 1.f);
+        const float y = fmaf(ln1p, lk.cp, s_cf[e] + kt.y);
+        const float yi = floorf(y);
+        i = s_ci[e] + __float_as_int(kt.z) + (int)yi;
+        fr = y - yi;
+        if (i < lk.n1) {
+            i = lk.n1;
+            fr = 0.f;
+        }
+    }
+    if (i > lk.imax) {
+        i = lk.imax;
+        fr = 1.0f;
+    }
+}
+
 // Gauss points of every cell: [cell][p] -> hi (x, y, z, w), lo (x, y, z, 0).
 __global__ void point_table_kernel(CubatureArgs a, int ng, long long ncell) {
     const int np = ng * ng * ng;
@@ -211,9 +273,10 @@ __global__ void __launch_bounds__(Shape<NG>::kWarps * 32, 1)
     const bool periodic = (a.coordsys == 1 && a.L > 0);
     const float Lh = (float)a.L, Ll = (float)(a.L - (double)Lh), hL = 0.5f * Lh;
 
-    for (long long key = (long long)blockIdx.x * kWarps + warp; key < a.ks.nkeys;
-         key += (long long)gridDim.x * kWarps) {
-        if (a.ks.coordsys == 2 && a.ks.mu_reflect && reflect_partner(a.ks, key) < key) continue;  // copied later
+    const long long nwork = a.list ? (long long)*a.list_count : a.ks.nkeys;
+    for (long long j = (long long)blockIdx.x * kWarps + warp; j < nwork; j += (long long)gridDim.x * kWarps) {
+        const long long key = a.list ? (long long)a.list[j] : j;
+        if (!a.list && a.ks.coordsys == 2 && a.ks.mu_reflect && reflect_partner(a.ks, key) < key) continue;
         int c1[3], c2[3];
         decode_key(a.ks, key, c1, c2);
         const float4* G1 = a.pts + 2 * NP * cell_id(a.ks, c1);
@@ -252,56 +315,8 @@ __global__ void __launch_bounds__(Shape<NG>::kWarps * 32, 1)
                 int i;
                 float fr;
                 if (EXACT) {
-                    const float4 Bl = P2l[q];
-                    float lx, ly, lz;
-                    float dx = diff2(B.x, Bl.x, ax, alx, &lx);
-                    float dy = diff2(B.y, Bl.y, ay, aly, &ly);
-                    float dz = diff2(B.z, Bl.z, az, alz, &lz);
-                    if (periodic) {
-                        // |d| in [L/2, L]: d -+ L is exact in FP32 (Sterbenz)
-                        const float wx = (float)((dx < -hL) - (dx >= hL));
-                        const float wy = (float)((dy < -hL) - (dy >= hL));
-                        const float wz = (float)((dz < -hL) - (dz >= hL));
-                        dx = fmaf(wx, Lh, dx); lx = fmaf(wx, Ll, lx);
-                        dy = fmaf(wy, Lh, dy); ly = fmaf(wy, Ll, ly);
-                        dz = fmaf(wz, Lh, dz); lz = fmaf(wz, Ll, lz);
-                    }
-                    // r^2 = hi + lo: exact squares by FMA, exact sums by two-sum
-                    const float px = __fmul_rn(dx, dx), py = __fmul_rn(dy, dy), pz = __fmul_rn(dz, dz);
-                    float e1, e2;
-                    const float h1 = two_sum(px, py, &e1);
-                    const float r2 = two_sum(h1, pz, &e2);
-                    float r2l = fmaf(dx, dx, -px) + fmaf(dy, dy, -py) + fmaf(dz, dz, -pz) + (e1 + e2);
-                    r2l = fmaf(2.f * dx, lx, fmaf(2.f * dy, ly, fmaf(2.f * dz, lz, r2l)));
-                    if (r2 < lk.r1sq) {
-                        // t = r n1 / r1 with r = rh + rl and n1 / r1 = inv_dr + inv_dr_lo; the
-                        // fraction is formed from the exact residual of the rounded product
-                        const float rh = sqrtf(r2);
-                        const float rl = rh > 0.f ? __fdividef(fmaf(-rh, rh, r2) + r2l, 2.f * rh) : 0.f;
-                        const float t = rh * lk.inv_dr;
-                        i = (int)t;
-                        fr = fmaf(rh, lk.inv_dr, -(float)i) + fmaf(rh, lk.inv_dr_lo, rl * lk.inv_dr);
-                    } else {
-                        const int bits = __float_as_int(r2);
-                        const int eb = bits >> 23;  // biased exponent; r2 > 0 here
-                        const int e = min(max(eb - 127 - lk.e0, 0), lk.ne - 1);
-                        const int k = (bits >> (23 - kLogBits)) & (kLogN - 1);
-                        const float Rk = __int_as_float(bits & ~((1 << (23 - kLogBits)) - 1));
-                        const float4 kt = s_kt[k];
-                        const float inv_pow = __int_as_float((254 - eb) << 23);  // 2^-(eb-127)
-                        const float delta = ((r2 - Rk) + r2l) * (kt.x * inv_pow);
-                        // ln(1 + delta), |delta| < 1/128: the series to delta^4 is good to 3e-12
-                        const float ln1p =
-                            delta * fmaf(-delta, fmaf(-delta, fmaf(-delta, 0.25f, 1.f / 3.f), 0.5f), 1.f);
-                        const float y = fmaf(ln1p, lk.cp, s_cf[e] + kt.y);
-                        const float yi = floorf(y);
-                        i = s_ci[e] + __float_as_int(kt.z) + (int)yi;
-                        fr = y - yi;
-                        if (i < lk.n1) {
-                            i = lk.n1;
-                            fr = 0.f;
-                        }
-                    }
+                    exact_index(lk, s_ci, s_cf, s_kt, B, P2l[q], ax, alx, ay, aly, az, alz, periodic, Lh, Ll, hL, i,
+                                fr);
                 } else {
                     float dx = B.x - ax, dy = B.y - ay, dz = B.z - az;
                     if (periodic) {
@@ -355,6 +370,303 @@ __global__ void __launch_bounds__(Shape<NG>::kWarps * 32, 1)
     }
 }
 
+// ---------------------------------------------------------------- window path (exact mode)
+// Q_t(key) = sum_pairs w_p w_q [(1-fr) T_t[i] + fr T_t[i+1]] = sum_bins T_t[bin] h_key[bin]:
+// one pass over the point pairs of a key scatters the interpolation weights
+// into a histogram h over the key's window of table bins, then one dot product
+// per table.  The pair geometry is computed once for all tables.  A key's
+// window follows from the bounding spheres of its two cells; keys are
+// bucketed by window start so a CTA's batch of keys shares one shared-memory
+// tile of every table.  Keys with windows wider than a tile allows (near and
+// self pairs) go to the table-group kernel in list mode.
+struct WinPlan {
+    int W;        // tile width in bins
+    int stride;   // tile row stride in floats (= 1 mod 32: conflict-free across tables)
+    int Wkey;     // widest key window on the window path
+    int KB;       // keys per batch
+    int flush;    // second-cell points per FP32 partial histogram before the FP64 flush (0: no flush)
+    int dot64;    // dot products in FP64 (1) or in FP32 chunks of 8 bins (0)
+    int nbucket;  // nx + 1: bucket nx holds the near keys
+    int2* win;        // [nkeys]: (bucket, width); bucket -1 = key copied by the reflection fill
+    int* order;       // [2 nkeys]: far keys by bucket, then near keys, then overflows
+    int* count;       // [nbucket + 1]
+    int* cursor;      // [nbucket + 1]
+    int* nfar;        // far keys
+    int* nnear;       // near keys incl. overflows (list length from order + nfar)
+    int* violations;  // pairs that fell outside their key's window (must stay 0)
+    float4* cen;      // per cell: bounding-sphere centre and radius
+};
+
+// bounding sphere of each cell from its Gauss points (FP64), radius inflated by a margin
+__global__ void cell_sphere_kernel(const float4* pts, int np, long long ncell, float4* cen) {
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < ncell;
+         c += (long long)gridDim.x * blockDim.x) {
+        const float4* P = pts + 2 * np * c;
+        double m[3] = {0, 0, 0};
+        for (int p = 0; p < np; p++) {
+            m[0] += (double)P[2 * p].x + P[2 * p + 1].x;
+            m[1] += (double)P[2 * p].y + P[2 * p + 1].y;
+            m[2] += (double)P[2 * p].z + P[2 * p + 1].z;
+        }
+        for (int d = 0; d < 3; d++) m[d] /= np;
+        double r = 0;
+        for (int p = 0; p < np; p++) {
+            const double dx = (double)P[2 * p].x + P[2 * p + 1].x - m[0];
+            const double dy = (double)P[2 * p].y + P[2 * p + 1].y - m[1];
+            const double dz = (double)P[2 * p].z + P[2 * p + 1].z - m[2];
+            r = fmax(r, sqrt(dx * dx + dy * dy + dz * dz));
+        }
+        cen[c] = make_float4((float)m[0], (float)m[1], (float)m[2], (float)(r * (1.0 + 1e-5) + 1e-3));
+    }
+}
+
+// table bin of a distance (the QSpline grid), FP64: the index the pair kernels compute, up to rounding
+__device__ __forceinline__ int bin_floor(const XiLayout& xl, double r) {
+    if (r < xl.r1) return (int)floor(r * xl.n1 / xl.r1);
+    if (r >= xl.r2) return xl.n() - 1;
+    return xl.n1 + (int)floor(log(r / xl.r1) * (xl.n2 - 1) / log(xl.r2 / xl.r1));
+}
+
+__global__ void key_window_kernel(CubatureArgs a, WinPlan w) {
+    const bool periodic = (a.coordsys == 1 && a.L > 0);
+    const int nx = a.xl.n();
+    for (long long key = blockIdx.x * (long long)blockDim.x + threadIdx.x; key < a.ks.nkeys;
+         key += (long long)gridDim.x * blockDim.x) {
+        if (a.ks.coordsys == 2 && a.ks.mu_reflect && reflect_partner(a.ks, key) < key) {
+            w.win[key] = make_int2(-1, 0);
+            continue;
+        }
+        int c1[3], c2[3];
+        decode_key(a.ks, key, c1, c2);
+        const float4 A = w.cen[cell_id(a.ks, c1)], B = w.cen[cell_id(a.ks, c2)];
+        double d[3] = {(double)B.x - A.x, (double)B.y - A.y, (double)B.z - A.z};
+        const double R = (double)A.w + B.w;
+        bool near = false;
+        if (periodic) {
+            for (int k = 0; k < 3; k++) {
+                d[k] -= a.L * floor(d[k] / a.L + 0.5);
+                if (fabs(d[k]) + R >= 0.5 * a.L) near = true;  // pair differences may wrap differently
+            }
+        }
+        const double dist = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+        const int blo = max(bin_floor(a.xl, fmax(dist - R, 0.0)) - 1, 0);
+        const int bhi = min(bin_floor(a.xl, dist + R) + 3, nx);
+        const int width = bhi - blo;
+        const int bucket = (near || width > w.Wkey) ? nx : blo;
+        w.win[key] = make_int2(bucket, width);
+        atomicAdd(&w.count[bucket], 1);
+    }
+}
+
+// exclusive scan of the bucket counts (one block)
+__global__ void bucket_scan_kernel(WinPlan w) {
+    __shared__ int part[1024];
+    const int n = w.nbucket;
+    const int per = (n + blockDim.x - 1) / blockDim.x;
+    const int b0 = threadIdx.x * per, b1 = min(n, b0 + per);
+    int s = 0;
+    for (int b = b0; b < b1; b++) s += w.count[b];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int run = 0;
+        for (int t = 0; t < (int)blockDim.x; t++) {
+            const int v = part[t];
+            part[t] = run;
+            run += v;
+        }
+    }
+    __syncthreads();
+    int run = part[threadIdx.x];
+    for (int b = b0; b < b1; b++) {
+        w.cursor[b] = run;
+        run += w.count[b];
+    }
+    if (threadIdx.x == 0) {
+        *w.nfar = 0;
+        for (int b = 0; b < n - 1; b++) *w.nfar += w.count[b];
+        *w.nnear = w.count[n - 1];
+    }
+}
+
+__global__ void bucket_scatter_kernel(long long nkeys, WinPlan w) {
+    for (long long key = blockIdx.x * (long long)blockDim.x + threadIdx.x; key < nkeys;
+         key += (long long)gridDim.x * blockDim.x) {
+        const int b = w.win[key].x;
+        if (b < 0) continue;
+        w.order[atomicAdd(&w.cursor[b], 1)] = (int)key;
+    }
+}
+
+// Histogram bins hold sum w_p w_q (1-fr) and sum w_p w_q fr.  They are summed
+// by FP32 shared-memory atomics over `flush` (8) second-cell points at a time
+// and then moved into an FP64 histogram, so every FP32 partial sum stays small.
+// A bin summed in FP32 over all 4096 pairs of a key carries a rounding error
+// relative to its whole (positive) sum into the strongly cancelling dot
+// product with an oscillating band table.  Measured on the 4x4x4 box, band
+// k in [0.1, 0.15], max|dS|/max|S|: no flush 2.2e-6, flush every 32 points
+// 1.8e-6, every 16 7.9e-7, every 8 9e-8 (the table-group kernel: 2.8e-7);
+// cubature time at 32k cells 199, 259, 267, 245 ms.  The dot products run in
+// FP32 over chunks of 8 bins added in FP64 (`dot64` = FP64 throughout: same
+// error, +38 ms on the FP64 pipe).  64-bit integer (fixed-point) histogram
+// atomics would sum exactly but cost +177 ms in shared-memory atomics.
+
+template <int NG>
+struct FarShape {
+    static constexpr int NP = NG * NG * NG;
+    static constexpr int kWarps = 16;
+};
+
+template <int NG>
+__global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 1)
+    cubature_far_kernel(CubatureArgs a, Lookup lk, WinPlan w) {
+    constexpr int NP = FarShape<NG>::NP;
+    constexpr int kWarps = FarShape<NG>::kWarps;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int nx = a.xl.n(), ntab = a.ntab;
+    float4* pts = reinterpret_cast<float4*>(smem_raw);                       // [kWarps][2][NP]
+    double* master = reinterpret_cast<double*>(pts + kWarps * 2 * NP);         // [kWarps][Wkey]
+    float* part = reinterpret_cast<float*>(master + kWarps * w.Wkey);          // [kWarps][Wkey]
+    float* tile = part + kWarps * w.Wkey;                                      // [ntab][stride]
+    __shared__ int s_ci[kMaxExp];
+    __shared__ float s_cf[kMaxExp];
+    __shared__ float4 s_kt[kLogN];
+    for (int i = threadIdx.x; i < lk.ne; i += blockDim.x) {
+        s_ci[i] = lk.ci[i];
+        s_cf[i] = lk.cf[i];
+    }
+    for (int i = threadIdx.x; i < kLogN; i += blockDim.x) s_kt[i] = lk.kt[i];
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float4* P2 = pts + warp * 2 * NP;
+    float4* P2l = P2 + NP;
+    double* hm = master + warp * w.Wkey;
+    float* hp = part + warp * w.Wkey;
+    const bool periodic = (a.coordsys == 1 && a.L > 0);
+    const float Lh = (float)a.L, Ll = (float)(a.L - (double)Lh), hL = 0.5f * Lh;
+    const int nfar = *w.nfar;
+    const int nbatch = (nfar + w.KB - 1) / w.KB;
+    for (int bt = blockIdx.x; bt < nbatch; bt += gridDim.x) {
+        const int k0 = bt * w.KB, k1 = min(nfar, k0 + w.KB);
+        const int tlo = w.win[w.order[k0]].x;
+        __syncthreads();  // the previous batch is done with the tile
+        for (int e = threadIdx.x; e < ntab * w.W; e += blockDim.x) {
+            const int t = e / w.W, b = e % w.W, g = tlo + b;
+            tile[t * w.stride + b] = g < nx ? a.tab32[(size_t)t * nx + g] : 0.f;
+        }
+        __syncthreads();
+        for (int kk = k0 + warp; kk < k1; kk += kWarps) {
+            const int key = w.order[kk];
+            const int2 wn = w.win[key];
+            const int off = wn.x - tlo, wl = wn.y;
+            if (off + wl > w.W) {  // does not fit this batch's tile: table-group kernel
+                if (lane == 0) w.order[(size_t)nfar + atomicAdd(w.nnear, 1)] = key;
+                continue;
+            }
+            for (int j = lane; j < wl; j += 32) {
+                hm[j] = 0.0;
+                hp[j] = 0.f;
+            }
+            int c1[3], c2[3];
+            decode_key(a.ks, key, c1, c2);
+            const float4* G1 = a.pts + 2 * NP * cell_id(a.ks, c1);
+            const float4* G2 = a.pts + 2 * NP * cell_id(a.ks, c2);
+            const float4 Oh = G1[2 * (NP / 2)], Ol = G1[2 * (NP / 2) + 1];
+            for (int q = lane; q < NP; q += 32) {
+                const float4 Bh = G2[2 * q], Bl = G2[2 * q + 1];
+                float lx, ly, lz;
+                const float sx = diff2(Bh.x, Bl.x, Oh.x, Ol.x, &lx);
+                const float sy = diff2(Bh.y, Bl.y, Oh.y, Ol.y, &ly);
+                const float sz = diff2(Bh.z, Bl.z, Oh.z, Ol.z, &lz);
+                P2[q] = make_float4(sx, sy, sz, Bh.w);
+                P2l[q] = make_float4(lx, ly, lz, 0.f);
+            }
+            __syncwarp();
+            int bad = 0;
+            // every lane runs the same trip counts: the flushes below are warp-wide
+            for (int p0 = 0; p0 < NP; p0 += 32) {
+                const int p = p0 + lane;
+                const bool act = p < NP;
+                const float4 Ah = act ? G1[2 * p] : make_float4(0.f, 0.f, 0.f, 0.f);
+                const float4 Al = act ? G1[2 * p + 1] : make_float4(0.f, 0.f, 0.f, 0.f);
+                float alx, aly, alz;
+                const float ax = diff2(Ah.x, Al.x, Oh.x, Ol.x, &alx);
+                const float ay = diff2(Ah.y, Al.y, Oh.y, Ol.y, &aly);
+                const float az = diff2(Ah.z, Al.z, Oh.z, Ol.z, &alz);
+                const int nfl = w.flush > 0 ? w.flush : NP;
+                for (int q0 = 0; q0 < NP; q0 += nfl) {
+                    if (act) {
+#pragma unroll 4
+                        for (int q = q0; q < q0 + nfl && q < NP; q++) {
+                            const float4 B = P2[q];
+                            int i;
+                            float fr;
+                            exact_index(lk, s_ci, s_cf, s_kt, B, P2l[q], ax, alx, ay, aly, az, alz, periodic, Lh, Ll,
+                                        hL, i, fr);
+                            int bi = i - wn.x;
+                            if (bi < 0 || bi > wl - 2) {  // outside the window: cannot happen for a sound window
+                                bad++;
+                                bi = min(max(bi, 0), wl - 2);
+                            }
+                            const float ww = Ah.w * B.w;
+                            atomicAdd(&hp[bi], fmaf(-ww, fr, ww));
+                            atomicAdd(&hp[bi + 1], ww * fr);
+                        }
+                    }
+                    if (w.flush) {
+                        // the FP32 partial sums stay small: move them into the FP64 histogram
+                        __syncwarp();
+                        for (int b = lane; b < wl; b += 32) {
+                            hm[b] += (double)hp[b];
+                            hp[b] = 0.f;
+                        }
+                        __syncwarp();
+                    }
+                }
+            }
+            if (bad) atomicAdd(w.violations, bad);
+            __syncwarp();
+            for (int t = lane; t < ntab; t += 32) {
+                const float* tr = tile + t * w.stride + off;
+                double acc = 0.0;
+                if (w.flush && w.dot64) {
+                    for (int b = 0; b < wl; b++) acc = fma((double)tr[b], hm[b], acc);
+                } else if (w.flush) {
+                    for (int b0 = 0; b0 < wl; b0 += 8) {
+                        float pt = 0.f;
+                        for (int b = b0; b < min(b0 + 8, wl); b++) pt = fmaf(tr[b], (float)hm[b], pt);
+                        acc += (double)pt;
+                    }
+                } else {
+                    for (int b0 = 0; b0 < wl; b0 += 8) {
+                        float pt = 0.f;
+                        for (int b = b0; b < min(b0 + 8, wl); b++) pt = fmaf(tr[b], hp[b], pt);
+                        acc += (double)pt;
+                    }
+                }
+                a.Q[(size_t)t * a.ks.nkeys + key] = acc;
+            }
+            __syncwarp();
+        }
+    }
+}
+
+// keys the cubature integrates (the others are copied by the reflection fill)
+double canonical_keys(const KeySpace& ks) {
+    if (!(ks.coordsys == 2 && ks.mu_reflect)) return (double)ks.nkeys;
+    long long n = 0;
+    for (int ha = 0; ha < ks.H; ha++)
+        for (int hb = ha; hb < ks.H; hb++) {
+            const int pa = (ha / ks.N2) * ks.N2 + (ks.N2 - 1 - ha % ks.N2);
+            const int pb = (hb / ks.N2) * ks.N2 + (ks.N2 - 1 - hb % ks.N2);
+            const int p1 = std::min(pa, pb), p2 = std::max(pa, pb);
+            if (p1 > ha || (p1 == ha && p2 >= hb)) ++n;
+        }
+    return (double)n * ks.nf;
+}
+
+double cubature_lookups(const CubatureArgs& a) { return canonical_keys(a.ks) * a.np * a.np * a.ntab; }
+
 template <int NG, bool EXACT>
 size_t smem_points() {
     return sizeof(float4) * Shape<NG>::kWarps * (EXACT ? 2 : 1) * Shape<NG>::NP;
@@ -372,13 +684,13 @@ void run(const CubatureArgs& a, int tab0, int ngrp, const Lookup& lk, cudaStream
     OPSEC_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     OPSEC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, kWarps * 32, smem));
     if (occ < 1) fail(OPSEC_ERR_CUDA, "cubature kernel does not fit on an SM");
-    long long want = (a.ks.nkeys + kWarps - 1) / kWarps;
+    long long want = a.list ? (long long)nsm * occ : (a.ks.nkeys + kWarps - 1) / kWarps;
     long long grid = (long long)nsm * occ;
     if (want < grid) grid = want;
-    if (g_clock) g_clock->begin("cubature", s, (double)a.ks.nkeys * NP * NP * ngrp);
+    if (g_clock && !a.list) g_clock->begin("cubature", s, canonical_keys(a.ks) * NP * NP * ngrp);
     k<<<(unsigned)grid, kWarps * 32, smem, s>>>(a, tab0, ngrp, lk);
     OPSEC_CUDA(cudaGetLastError());
-    if (g_clock) g_clock->end(s);
+    if (g_clock && !a.list) g_clock->end(s);
 }
 
 template <int NG, bool EXACT>
@@ -418,6 +730,112 @@ void run_mode(const CubatureArgs& a, const Lookup& lk, cudaStream_t s, long long
 size_t cubature_point_count(const KeySpace& ks, int ng) {
     return (size_t)ks.N1 * ks.N2 * ks.N3 * ng * ng * ng;
 }
+
+namespace {
+// scratch layout of the window path
+struct WinLayout {
+    size_t win, order, count, cursor, scal, cen, total;
+};
+WinLayout win_layout(const KeySpace& ks, int nx) {
+    auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+    const size_t ncell = (size_t)ks.N1 * ks.N2 * ks.N3;
+    WinLayout L;
+    L.win = 0;
+    L.order = L.win + al(sizeof(int2) * ks.nkeys);
+    L.count = L.order + al(sizeof(int) * 2 * ks.nkeys);
+    L.cursor = L.count + al(sizeof(int) * (nx + 2));
+    L.scal = L.cursor + al(sizeof(int) * (nx + 2));
+    L.cen = L.scal + 256;
+    L.total = L.cen + al(sizeof(float4) * ncell);
+    return L;
+}
+
+template <int NG>
+size_t far_smem(const WinPlan& w, int ntab) {
+    return sizeof(float4) * FarShape<NG>::kWarps * 2 * FarShape<NG>::NP +
+           (sizeof(double) + sizeof(float)) * FarShape<NG>::kWarps * w.Wkey + sizeof(float) * (size_t)ntab * w.stride;
+}
+
+// Far keys by windows, near keys by table groups in list mode.  Returns false (nothing
+// launched) when the tables are too many for a useful tile.
+template <int NG>
+bool run_window(const CubatureArgs& a, const Lookup& lk, cudaStream_t s, long long* launches) {
+    constexpr int NP = FarShape<NG>::NP;
+    constexpr int kWarps = FarShape<NG>::kWarps;
+    const int nx = a.xl.n();
+    WinPlan w{};
+    w.Wkey = a.win_key;
+    w.flush = a.win_flush;
+    w.dot64 = a.win_dot64;
+    const size_t fixed = sizeof(float4) * kWarps * 2 * NP + (sizeof(double) + sizeof(float)) * kWarps * w.Wkey;
+    const size_t budget = 222 * 1024;
+    if (fixed >= budget) return false;
+    long long stride = (long long)((budget - fixed) / (sizeof(float) * a.ntab));
+    stride = ((stride - 1) / 32) * 32 + 1;
+    w.W = (int)std::min<long long>(stride - 1, nx);
+    w.stride = ((w.W + 31) / 32) * 32 + 1;
+    if (w.W < 2 * 128) return false;
+    w.Wkey = std::min(w.Wkey, w.W / 2);
+    w.KB = 256;
+    w.nbucket = nx + 1;
+    const WinLayout L = win_layout(a.ks, nx);
+    if (!a.work || a.work_bytes < L.total) fail(OPSEC_ERR_ARG, "cubature scratch too small");
+    unsigned char* base = static_cast<unsigned char*>(a.work);
+    w.win = reinterpret_cast<int2*>(base + L.win);
+    w.order = reinterpret_cast<int*>(base + L.order);
+    w.count = reinterpret_cast<int*>(base + L.count);
+    w.cursor = reinterpret_cast<int*>(base + L.cursor);
+    int* scal = reinterpret_cast<int*>(base + L.scal);
+    w.nfar = scal;
+    w.nnear = scal + 1;
+    w.violations = scal + 2;
+    w.cen = reinterpret_cast<float4*>(base + L.cen);
+    OPSEC_CUDA(cudaMemsetAsync(w.count, 0, sizeof(int) * (nx + 2), s));
+    OPSEC_CUDA(cudaMemsetAsync(scal, 0, 256, s));
+    const long long ncell = (long long)a.ks.N1 * a.ks.N2 * a.ks.N3;
+    auto blocks = [](long long n) { return (unsigned)std::min<long long>((n + 255) / 256, 65536); };
+    cell_sphere_kernel<<<blocks(ncell), 256, 0, s>>>(a.pts, a.np, ncell, w.cen);
+    OPSEC_CUDA(cudaGetLastError());
+    key_window_kernel<<<blocks(a.ks.nkeys), 256, 0, s>>>(a, w);
+    OPSEC_CUDA(cudaGetLastError());
+    bucket_scan_kernel<<<1, 1024, 0, s>>>(w);
+    OPSEC_CUDA(cudaGetLastError());
+    bucket_scatter_kernel<<<blocks(a.ks.nkeys), 256, 0, s>>>(a.ks.nkeys, w);
+    OPSEC_CUDA(cudaGetLastError());
+    *launches += 4;
+    int h_nfar = 0;
+    OPSEC_CUDA(cudaMemcpyAsync(&h_nfar, w.nfar, sizeof(int), cudaMemcpyDeviceToHost, s));
+    OPSEC_CUDA(cudaStreamSynchronize(s));
+    // far keys
+    const size_t smem = far_smem<NG>(w, a.ntab);
+    auto k = cubature_far_kernel<NG>;
+    OPSEC_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int dev = 0, nsm = 0, occ = 0;
+    OPSEC_CUDA(cudaGetDevice(&dev));
+    OPSEC_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    OPSEC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, kWarps * 32, smem));
+    if (occ < 1) fail(OPSEC_ERR_CUDA, "cubature window kernel does not fit on an SM");
+    const long long nbatch = ((long long)h_nfar + w.KB - 1) / w.KB;
+    const long long grid = std::max<long long>(1, std::min<long long>((long long)nsm * occ, nbatch));
+    if (h_nfar > 0) {
+        k<<<(unsigned)grid, kWarps * 32, smem, s>>>(a, lk, w);
+        OPSEC_CUDA(cudaGetLastError());
+        ++*launches;
+    }
+    // near keys and tile overflows: the table-group kernel over the list
+    CubatureArgs an = a;
+    an.list = w.order + h_nfar;
+    an.list_count = w.nnear;
+    run_groups<NG, true>(an, lk, s, launches);
+    int viol = 0;
+    OPSEC_CUDA(cudaMemcpyAsync(&viol, w.violations, sizeof(int), cudaMemcpyDeviceToHost, s));
+    OPSEC_CUDA(cudaStreamSynchronize(s));
+    if (viol != 0) fail(OPSEC_ERR_NUMERIC, "cubature: " + std::to_string(viol) + " point pairs outside their key window");
+    return true;
+}
+}  // namespace
+
+size_t cubature_work_bytes(const KeySpace& ks, int nx) { return win_layout(ks, nx).total; }
 
 void launch_cubature(const CubatureArgs& a, cudaStream_t s, long long* launches) {
     // point table: every Gauss point of every cell, once
@@ -466,7 +884,22 @@ void launch_cubature(const CubatureArgs& a, cudaStream_t s, long long* launches)
         std::memcpy(&zi_f, &zi_bits, sizeof zi_f);
         lk.kt[k] = make_float4((float)(1.0 / T), (float)(z - zi), zi_f, 0.f);
     }
-    switch (a.ng) {
+    // exact mode: far keys through the window path when it applies
+    bool done = false;
+    if (a.exact && a.window && a.work) {
+        if (g_clock) g_clock->begin("cubature", s, cubature_lookups(a));
+        switch (a.ng) {
+        case 1: done = run_window<1>(a, lk, s, launches); break;
+        case 2: done = run_window<2>(a, lk, s, launches); break;
+        case 3: done = run_window<3>(a, lk, s, launches); break;
+        case 4: done = run_window<4>(a, lk, s, launches); break;
+        case 5: done = run_window<5>(a, lk, s, launches); break;
+        case 6: done = run_window<6>(a, lk, s, launches); break;
+        default: fail(OPSEC_ERR_CONFIG, "sig.gauss must be between 1 and 6");
+        }
+        if (g_clock) g_clock->end(s);
+    }
+    if (!done) switch (a.ng) {
     case 1: run_mode<1>(a, lk, s, launches); break;
     case 2: run_mode<2>(a, lk, s, launches); break;
     case 3: run_mode<3>(a, lk, s, launches); break;

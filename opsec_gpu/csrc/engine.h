@@ -105,9 +105,20 @@ struct CubatureArgs {
     double* Q;           // [ntab][ks.nkeys]
     float4* pts;         // [N1 N2 N3][np][2]: point table (hi: x y z w, lo: x y z 0), filled here
     int exact = 1;       // FP32-pair separations and table index (1) or plain FP32 (0)
+    int window = 1;      // exact mode: per-key bin-window histograms for the far keys (1) or table groups only (0)
+    int win_key = 384;   // widest key window (bins) on the window path
+    int win_flush = 8;   // window histograms: second-cell points per FP32 partial sum before the FP64 flush (0: none)
+    int win_dot64 = 0;   // window dot products in FP64 (1) or FP32 chunks of 8 bins added in FP64 (0)
+    void* work = nullptr;  // cubature_work_bytes() of scratch for the window path
+    size_t work_bytes = 0;
+    // list mode (set internally): integrate the keys list[0 .. *list_count) only
+    const int* list = nullptr;
+    const int* list_count = nullptr;
 };
 // float4s of the point table for a key space and ng
 size_t cubature_point_count(const KeySpace& ks, int ng);
+// scratch bytes for the window path
+size_t cubature_work_bytes(const KeySpace& ks, int nx);
 void launch_cubature(const CubatureArgs& a, cudaStream_t s, long long* launches);
 
 struct XiTableArgs {

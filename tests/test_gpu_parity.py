@@ -99,6 +99,35 @@ def test_signal_matrix_high_k(name, precision, tol):
     e.close()
 
 
+@pytest.mark.parametrize("name", ["shell768", "box12"])
+def test_cubature_window_path(name):
+    """Exact-mode far keys go through per-key bin-window histograms (one pass
+    over the point pairs for all tables); near keys through the table-group
+    kernel.  Both paths against the oracle and against each other."""
+    if name == "shell768":
+        sv, cells = synth.shell_survey(6, 8, 16)
+        bands = synth.band_edges(20, 0.0, 0.4)
+    else:
+        sv, cells = synth.box_survey(12)
+        bands = synth.band_edges(20, 0.0, 0.2)
+    layout = O.LAYOUT_LOG4096
+    got = {}
+    for win in ("1", "0"):
+        e = api.Engine(api.make_config(sv, bands=bands, layout=layout, extra=[f"cubature.window = {win}"]))
+        e.set_pk(*PK)
+        got[win] = [e.signal_block(cells, table=t) for t in (0, 10, 20)]
+        e.close()
+    tabs = O.xi_tables(*PK, bands, layout)
+    Q = O.qtable_keys(sv, O.keys_all(sv), tabs[[0, 10, 20]], layout)
+    for j, t in enumerate((0, 10, 20)):
+        ref = O.signal_matrix(sv, cells, Q[:, j])
+        sc = np.max(np.abs(ref))
+        e_win = np.max(np.abs(got["1"][j] - ref)) / sc
+        e_grp = np.max(np.abs(got["0"][j] - ref)) / sc
+        print(f"{name} table {t}: window {e_win:.2e}, groups {e_grp:.2e}")
+        assert e_win <= 3e-7 and e_grp <= 3e-7, (name, t, e_win, e_grp)
+
+
 def test_cubature_precision_key_is_checked():
     sv, _ = CASES["box4"]
     with pytest.raises(api.OpsecError):
