@@ -50,6 +50,10 @@ def workload(name):
         sv, cells = synth.shell_survey(32, 32, 32)
         return dict(name="c2", survey=sv, cells=cells, nbands=40, kmax=0.4, nmodes=8192,
                     layout=(256, 4096, 10.0, 20000.0), gauss=4)
+    if name == "c3":  # 65,536 cells: 64 (r) x 32 (mu) x 32 (phi) on the same shell, 64 bands on [0, 0.4]
+        sv, cells = synth.shell_survey(64, 32, 32)
+        return dict(name="c3", survey=sv, cells=cells, nbands=64, kmax=0.4, nmodes=16384,
+                    layout=(256, 4096, 10.0, 20000.0), gauss=4)
     if name == "c2-mid":  # same geometry family, 16,384 cells (profiling size)
         sv, cells = synth.shell_survey(16, 32, 32)
         return dict(name="c2-mid", survey=sv, cells=cells, nbands=40, kmax=0.4, nmodes=4096,
@@ -67,6 +71,18 @@ def workload(name):
         return dict(name="c1", survey=sv, cells=cells, nbands=20, kmax=0.2, nmodes=500,
                     layout=(256, 4096, 10.0, 20000.0), gauss=4)
     raise SystemExit(f"unknown workload {name}")
+
+
+def q_table_gb(w):
+    """FP64 Q table bytes of a workload: tables x symmetry keys."""
+    sv = w["survey"]
+    n1, n2, n3 = sv.n
+    if sv.coordsys == 1:
+        keys = n1 * n2 * n3
+    else:
+        h = n1 * n2
+        keys = h * (h + 1) // 2 * (n3 // 2 + 1)
+    return (1 + w["nbands"]) * keys * 8 / 1e9
 
 
 def peaks():
@@ -389,7 +405,7 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f16x3+f32+f64", "data": "synthetic",
             "config": {"workload": w["name"], "cells": int(cells.size), "bands": nb, "modes": w["nmodes"],
                        "xi_table": "256 linear + 4096 log r", "gauss_points": f"{w['gauss']}^3 x {w['gauss']}^3",
-                       "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (Q tables 2.9 GB)",
+                       "parallelism": f"replicas x{world}", "l2": f"inputs larger than L2 (Q tables {q_table_gb(w):.1f} GB)",
                        **({"engine_options": args.set} if args.set else {})},
             "e2e": {"value": per_build_wall / world, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},
