@@ -130,6 +130,32 @@ int opsec_gpu_kernel_stats(const opsec_gpu* ctx, const char* name, long long* co
 /* Number of kernels this context has launched since creation. */
 long long opsec_gpu_launch_count(const opsec_gpu* ctx);
 
+/* ---- learned far-field surrogate (no counterpart in the reference, whose
+ * cell-pair integrals are all adaptive cubature).  A 4-member ensemble of MLPs
+ * (12 geometry/band inputs -> 3 x 128 GELU -> 1, BF16 products, FP32
+ * accumulation) predicts the integrals of key pairs at least `surrogate.far`
+ * (default 2) cell widths apart on spherical grids; a key whose members
+ * disagree by more than `surrogate.tol` (default 1e-3, in units of the table
+ * at r = 0) and every nearer key are integrated by the cubature.  Enabled by
+ * the configuration key `surrogate = 1` once weights are present. */
+
+/* Train the ensemble on this context's own survey: every key integrated by
+ * the cubature, then up to max_samples (far key, table) samples, 2% held out,
+ * `epochs` passes of Adam.  stats (4, may be NULL): samples, validation rms of
+ * the residual (units of the table at r = 0), training seconds, output scale. */
+int opsec_gpu_surrogate_train(opsec_gpu* ctx, long long max_samples, int epochs, unsigned seed, double* stats);
+/* Floats in a weight buffer: 4 networks x 35336 FP32 parameters, then the output scale. */
+int opsec_gpu_surrogate_size(void);
+/* Copy the ensemble out (get = 1) or in (get = 0, e.g. weights trained on another survey). */
+int opsec_gpu_surrogate_weights(opsec_gpu* ctx, float* buf, int get);
+/* After a build with the surrogate: keys predicted, keys sent back to the cubature, far keys. */
+int opsec_gpu_surrogate_stats(const opsec_gpu* ctx, long long* counts);
+/* One network on explicit inputs (n x 16 floats, BF16-rounded on entry): out_tc from the
+ * fused tensor-core inference kernel, out_simt from the training forward pass; with y
+ * (n targets) also the mean squared error and its gradient (35336 floats). */
+int opsec_gpu_surrogate_eval(opsec_gpu* ctx, const float* params, int n, const float* feats, const float* y,
+                             float* out_tc, float* out_simt, double* loss, float* grad);
+
 /* Largest band count opsec_gpu_fisher_noalloc accepts. */
 #define OPSEC_NOALLOC_MAX_BANDS 64
 

@@ -60,6 +60,12 @@ def load():
     L.opsec_gpu_last_error.argtypes = [vp]
     L.opsec_gpu_last_error.restype = C.c_char_p
     L.opsec_gpu_destroy.argtypes = [vp]
+    fp = C.POINTER(C.c_float)
+    L.opsec_gpu_surrogate_train.argtypes = [vp, C.c_longlong, C.c_int, C.c_uint, dp]
+    L.opsec_gpu_surrogate_size.argtypes = []
+    L.opsec_gpu_surrogate_weights.argtypes = [vp, fp, C.c_int]
+    L.opsec_gpu_surrogate_stats.argtypes = [vp, C.POINTER(C.c_longlong)]
+    L.opsec_gpu_surrogate_eval.argtypes = [vp, fp, C.c_int, fp, fp, fp, fp, dp, fp]
     _lib = L
     return L
 
@@ -70,6 +76,10 @@ def _d(a):
 
 def _i(a):
     return None if a is None else a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+def _fp(a):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_float))
 
 
 def _f64(a):
@@ -217,6 +227,47 @@ class Engine:
                                                _d(r["phat"]), _d(r["pcov"]), _d(r["F"]), _d(r["W"]), _d(r["M"]),
                                                _d(r["q"]), _d(r["f"])))
         return r
+
+    # ---- learned far-field surrogate
+    def surrogate_train(self, max_samples=20_000_000, epochs=4, seed=1):
+        """Train the 4-network ensemble on this engine's survey; returns
+        samples, validation rms of the residual, seconds and the output scale."""
+        st = np.zeros(4)
+        self._check(self._L.opsec_gpu_surrogate_train(self._h, int(max_samples), int(epochs), int(seed), _d(st)))
+        return {"samples": int(st[0]), "val_rms": st[1], "seconds": st[2], "ysc": st[3]}
+
+    def surrogate_weights(self, weights=None):
+        """Without an argument: the ensemble's weights (float32, scale last); with one: load them."""
+        n = self._L.opsec_gpu_surrogate_size()
+        if weights is None:
+            buf = np.zeros(n, dtype=np.float32)
+            self._check(self._L.opsec_gpu_surrogate_weights(self._h, _fp(buf), 1))
+            return buf
+        buf = np.ascontiguousarray(weights, dtype=np.float32)
+        if buf.size != n:
+            raise ValueError(f"surrogate weights need {n} floats")
+        self._check(self._L.opsec_gpu_surrogate_weights(self._h, _fp(buf), 0))
+
+    def surrogate_stats(self):
+        out = (C.c_longlong * 3)()
+        self._check(self._L.opsec_gpu_surrogate_stats(self._h, out))
+        return {"predicted": out[0], "fallback": out[1], "far": out[2]}
+
+    def surrogate_eval(self, params, feats, y=None):
+        params = np.ascontiguousarray(params, dtype=np.float32)
+        feats = np.ascontiguousarray(feats, dtype=np.float32)
+        n = feats.shape[0]
+        if feats.shape != (n, 16) or params.size != 35336:
+            raise ValueError("params: 35336 floats; feats: n x 16")
+        out_tc = np.zeros(n, dtype=np.float32)
+        out_simt = np.zeros(n, dtype=np.float32)
+        loss = np.zeros(1)
+        grad = np.zeros(35336, dtype=np.float32)
+        yy = None if y is None else np.ascontiguousarray(y, dtype=np.float32)
+        self._check(self._L.opsec_gpu_surrogate_eval(self._h, _fp(params), n, _fp(feats), _fp(yy), _fp(out_tc),
+                                                     _fp(out_simt), _d(loss), _fp(grad)))
+        return {"out_tc": out_tc, "out_simt": out_simt, "loss": loss[0] if y is not None else None,
+                "grad": grad if y is not None else None}
 
     def fisher_build(self, cells, counts, nmodes, mixing="inverse", want_evals=True):
         cells = _cells(cells)

@@ -5,6 +5,7 @@
 #include <cusolverDn.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cerrno>
 #include <cmath>
 #include <cstdio>
@@ -304,6 +305,17 @@ struct opsec_gpu {
     std::vector<int> az_m, az_idx, az_kind;
     std::vector<double> nbar_arc;
     DevBuf<unsigned char> azws;  // azimuthal projection workspace
+    // learned far-field surrogate: 4 networks (FP32 master weights) and the target scale
+    static constexpr int kMembers = 4;
+    bool surr_on = false;
+    float surr_tol = 1e-3f, surr_far = 2.0f;
+    std::vector<float> surr_w;  // kMembers * kSurrParams, empty until trained or loaded
+    float surr_ysc = 0.f;
+    long long surr_counts[3] = {0, 0, 0};  // keys predicted, sent back to the cubature, far keys
+    DevBuf<float> surr_kg, surr_wdev, surr_pred, surr_tinfo;
+    DevBuf<long long> surr_list;
+    DevBuf<unsigned char> surr_done;
+    DevBuf<int> surr_cnt;
     DevBuf<int> az_i;
     DevBuf<long long> az_off;
     DevBuf<double> evals, modes, Bs, y, counts, prior, fout, partial, est;
@@ -507,6 +519,10 @@ void configure(opsec_gpu* c, const std::map<std::string, std::string>& kv) {
         c->az_streams = to_int("azimuthal.streams", get("azimuthal.streams"));
         if (c->az_streams < 1 || c->az_streams > opsec_gpu::kSide) fail(OPSEC_ERR_CONFIG, "azimuthal.streams must be in [1, 16]");
     }
+    if (has("surrogate")) c->surr_on = get("surrogate") == "1";
+    if (has("surrogate.tol")) c->surr_tol = (float)to_double("surrogate.tol", get("surrogate.tol"));
+    if (has("surrogate.far")) c->surr_far = (float)to_double("surrogate.far", get("surrogate.far"));
+    if (!(c->surr_tol > 0) || !(c->surr_far >= 1)) fail(OPSEC_ERR_CONFIG, "surrogate.tol must be > 0 and surrogate.far >= 1");
     if (has("cubature.window")) c->cub_window = get("cubature.window") != "0";
     if (has("cubature.window_bins")) c->win_key = to_int("cubature.window_bins", get("cubature.window_bins"));
     if (c->win_key < 16 || c->win_key > 4096) fail(OPSEC_ERR_CONFIG, "cubature.window_bins must be in [16, 4096]");
@@ -603,6 +619,242 @@ void setup_keys(opsec_gpu* c) {
     }
 }
 
+// ---------------------------------------------------------------- learned surrogate
+void build_q(opsec_gpu* c);
+
+SurrGrid surr_grid(const opsec_gpu* c) {
+    const Geometry& g = c->geo;
+    SurrGrid sg;
+    for (int k = 0; k < 6; k++) sg.b[k] = g.b[k];
+    for (int k = 0; k < 3; k++) sg.d[k] = (g.b[2 * k + 1] - g.b[2 * k]) / g.n[k];
+    return sg;
+}
+
+// per table: (k_lo 5, k_hi 5, band centre k, 0); the full xi table is (0, 0, 0, 0)
+void surr_tables(opsec_gpu* c) {
+    std::vector<float4> ti(c->ntab());
+    ti[0] = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (size_t p = 0; p < c->band_lo.size(); p++)
+        ti[p + 1] = make_float4((float)(5 * c->band_lo[p]), (float)(5 * c->band_hi[p]),
+                                (float)(0.5 * (c->band_lo[p] + c->band_hi[p])), 0.f);
+    c->surr_tinfo.alloc(4 * ti.size());
+    OPSEC_CUDA(cudaMemcpyAsync(c->surr_tinfo.p, ti.data(), sizeof(float4) * ti.size(), cudaMemcpyHostToDevice,
+                               c->stream));
+}
+
+// key geometry and the canonical far keys; returns their number
+long long surr_far_keys(opsec_gpu* c) {
+    if (c->geo.coordsys != 2) fail(OPSEC_ERR_CONFIG, "the surrogate covers spherical grids only");
+    const KeySpace& ks = c->ks;
+    c->surr_kg.alloc((size_t)ks.nkeys * kSurrKeyStride);
+    launch_surr_key_geometry(ks, surr_grid(c), c->surr_far, c->surr_kg.p, c->stream, &c->launches);
+    c->surr_list.alloc((size_t)ks.nkeys);
+    c->surr_cnt.alloc(4);
+    OPSEC_CUDA(cudaMemsetAsync(c->surr_cnt.p, 0, sizeof(int) * 4, c->stream));
+    launch_surr_far_list(ks, c->surr_kg.p, c->surr_list.p, c->surr_cnt.p, c->stream, &c->launches);
+    int n = 0;
+    OPSEC_CUDA(cudaMemcpyAsync(&n, c->surr_cnt.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    sync(c);
+    return n;
+}
+
+// Predict Q of the canonical far keys with the ensemble; keys it accepts are
+// marked in surr_done and skipped by the cubature.
+void surrogate_stage(opsec_gpu* c) {
+    if (c->surr_w.size() != (size_t)opsec_gpu::kMembers * kSurrParams)
+        fail(OPSEC_ERR_STATE, "surrogate = 1 but no trained weights: call opsec_gpu_surrogate_train or _weights");
+    const KeySpace& ks = c->ks;
+    const int ntab = c->ntab();
+    surr_tables(c);
+    const long long nfar = surr_far_keys(c);
+    c->surr_done.alloc((size_t)ks.nkeys);
+    OPSEC_CUDA(cudaMemsetAsync(c->surr_done.p, 0, (size_t)ks.nkeys, c->stream));
+    c->surr_counts[0] = c->surr_counts[1] = 0;
+    c->surr_counts[2] = nfar;
+    if (nfar == 0) return;
+    const int nm = opsec_gpu::kMembers;
+    c->surr_wdev.alloc(c->surr_w.size());
+    OPSEC_CUDA(cudaMemcpyAsync(c->surr_wdev.p, c->surr_w.data(), sizeof(float) * c->surr_w.size(),
+                               cudaMemcpyHostToDevice, c->stream));
+    const long long nsamp = nfar * ntab;
+    c->surr_pred.alloc((size_t)nm * nsamp);
+    const float4* ti = reinterpret_cast<const float4*>(c->surr_tinfo.p);
+    if (g_clock) g_clock->begin("surrogate", c->stream, 2.0 * nm * nsamp * (16.0 * 128 + 2 * 128.0 * 128 + 128));
+    for (int m = 0; m < nm; m++)
+        launch_surr_infer(nsamp, c->surr_list.p, ntab, c->surr_kg.p, ti, nullptr,
+                          c->surr_wdev.p + (size_t)m * kSurrParams, c->surr_pred.p + (size_t)m * nsamp, c->stream,
+                          &c->launches);
+    launch_surr_combine(nfar, c->surr_list.p, ntab, nm, c->surr_pred.p, c->surr_kg.p, c->xl, c->xi64.p, c->surr_ysc,
+                        c->surr_tol, ks.nkeys, c->Q.p, c->surr_done.p, c->surr_cnt.p + 1, c->stream, &c->launches);
+    if (g_clock) g_clock->end(c->stream);
+    int cnt[2] = {0, 0};
+    OPSEC_CUDA(cudaMemcpyAsync(cnt, c->surr_cnt.p + 1, sizeof(int) * 2, cudaMemcpyDeviceToHost, c->stream));
+    sync(c);
+    c->surr_counts[0] = cnt[0];
+    c->surr_counts[1] = cnt[1];
+}
+
+// Glorot-uniform weights (the first layer over its 12 used inputs), zero biases
+void surr_init(std::vector<float>& w, unsigned seed) {
+    w.assign(kSurrParams, 0.f);
+    uint64_t st = 0x9E3779B97F4A7C15ull ^ ((uint64_t)seed * 0xBF58476D1CE4E5B9ull);
+    auto uni = [&]() {  // splitmix64 -> [0, 1)
+        st += 0x9E3779B97F4A7C15ull;
+        uint64_t z = st;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        return (double)(z >> 11) / 9007199254740992.0;
+    };
+    auto fill = [&](int off, int nout, int nin, int nin_used) {
+        const double a = std::sqrt(6.0 / (nin_used + nout));
+        for (int o = 0; o < nout; o++)
+            for (int i = 0; i < nin; i++) w[off + o * nin + i] = i < nin_used ? (float)((2 * uni() - 1) * a) : 0.f;
+    };
+    fill(kSurrOffW1, kSurrHid, kSurrIn, 12);
+    fill(kSurrOffW2, kSurrHid, kSurrHid, kSurrHid);
+    fill(kSurrOffW3, kSurrHid, kSurrHid, kSurrHid);
+    fill(kSurrOffW4, 1, kSurrHid, kSurrHid);
+}
+
+float bf16_round_host(float x) {
+    uint32_t u;
+    std::memcpy(&u, &x, 4);
+    if ((u & 0x7f800000u) == 0x7f800000u) return x;
+    u += 0x7fffu + ((u >> 16) & 1u);
+    u &= 0xffff0000u;
+    float r;
+    std::memcpy(&r, &u, 4);
+    return r;
+}
+
+long long gcd_ll(long long a, long long b) {
+    while (b) {
+        const long long t = a % b;
+        a = b;
+        b = t;
+    }
+    return a;
+}
+
+// Train the ensemble on this context's own survey: plain cubature Q of every key,
+// then up to max_samples (canonical far key, table) samples, 2 % held out.
+// stats: samples, validation rms error of y (mean over members), training seconds, ysc.
+void surrogate_train(opsec_gpu* c, long long max_samples, int epochs, unsigned seed, double* stats) {
+    const bool was_on = c->surr_on;
+    c->surr_on = false;
+    c->q_ok = c->qsq_ok = false;
+    build_q(c);
+    c->surr_on = was_on;
+    c->q_ok = c->qsq_ok = false;  // the next build recomputes Q, with the surrogate when it is on
+    const KeySpace& ks = c->ks;
+    const int ntab = c->ntab();
+    surr_tables(c);
+    const long long nfar = surr_far_keys(c);
+    if (nfar < 16) fail(OPSEC_ERR_ARG, "too few far keys to train the surrogate");
+    std::vector<long long> keys(nfar);
+    OPSEC_CUDA(cudaMemcpyAsync(keys.data(), c->surr_list.p, sizeof(long long) * nfar, cudaMemcpyDeviceToHost,
+                               c->stream));
+    sync(c);
+    std::sort(keys.begin(), keys.end());
+    uint64_t st = 0x243F6A8885A308D3ull ^ seed;
+    auto rnd = [&]() {  // xorshift64
+        st ^= st << 13;
+        st ^= st >> 7;
+        st ^= st << 17;
+        return st;
+    };
+    for (long long i = nfar - 1; i > 0; i--) std::swap(keys[i], keys[rnd() % (uint64_t)(i + 1)]);
+    const long long nk = std::max<long long>(1, std::min<long long>(nfar, max_samples / ntab));
+    keys.resize(nk);
+    DevBuf<long long> dkeys;
+    dkeys.alloc(nk);
+    OPSEC_CUDA(cudaMemcpyAsync(dkeys.p, keys.data(), sizeof(long long) * nk, cudaMemcpyHostToDevice, c->stream));
+    const long long S = nk * ntab;
+    DevBuf<float> feat, y;
+    feat.alloc((size_t)S * kSurrIn);
+    y.alloc(S);
+    launch_surr_samples(S, dkeys.p, ntab, c->surr_kg.p, reinterpret_cast<const float4*>(c->surr_tinfo.p), c->xl,
+                        c->xi64.p, c->Q.p, ks.nkeys, feat.p, y.p, c->stream, &c->launches);
+    std::vector<float> hy(S);
+    OPSEC_CUDA(cudaMemcpyAsync(hy.data(), y.p, sizeof(float) * S, cudaMemcpyDeviceToHost, c->stream));
+    sync(c);
+    float ysc = 0.f;
+    for (float v : hy) ysc = std::max(ysc, std::fabs(v));
+    if (!(ysc > 0)) ysc = 1.f;
+    for (float& v : hy) v /= ysc;
+    OPSEC_CUDA(cudaMemcpyAsync(y.p, hy.data(), sizeof(float) * S, cudaMemcpyHostToDevice, c->stream));
+    const long long Sval = std::max<long long>(1, S / 50), Str = S - Sval;
+    const int Bn = (int)std::min<long long>(2048, Str);
+    DevBuf<float> xb, yb, w, wb, g, m1, v1, scratch, out;
+    xb.alloc((size_t)Bn * kSurrIn);
+    yb.alloc(Bn);
+    w.alloc(kSurrParams);
+    wb.alloc(kSurrParams);
+    g.alloc(kSurrParams);
+    m1.alloc(kSurrParams);
+    v1.alloc(kSurrParams);
+    scratch.alloc((size_t)7 * Bn * kSurrHid);
+    out.alloc(Bn);
+    DevBuf<double> loss;
+    loss.alloc(1);
+    std::vector<float> all((size_t)opsec_gpu::kMembers * kSurrParams);
+    auto t0 = std::chrono::steady_clock::now();
+    double val_sum = 0;
+    for (int mem = 0; mem < opsec_gpu::kMembers; mem++) {
+        std::vector<float> hw;
+        surr_init(hw, seed * 7919u + 101u * (unsigned)mem + 1u);
+        std::vector<float> hwb(hw.size());
+        for (size_t i = 0; i < hw.size(); i++) hwb[i] = bf16_round_host(hw[i]);
+        OPSEC_CUDA(cudaMemcpyAsync(w.p, hw.data(), sizeof(float) * kSurrParams, cudaMemcpyHostToDevice, c->stream));
+        OPSEC_CUDA(cudaMemcpyAsync(wb.p, hwb.data(), sizeof(float) * kSurrParams, cudaMemcpyHostToDevice, c->stream));
+        OPSEC_CUDA(cudaMemsetAsync(g.p, 0, sizeof(float) * kSurrParams, c->stream));
+        OPSEC_CUDA(cudaMemsetAsync(m1.p, 0, sizeof(float) * kSurrParams, c->stream));
+        OPSEC_CUDA(cudaMemsetAsync(v1.p, 0, sizeof(float) * kSurrParams, c->stream));
+        const long long steps_per_epoch = std::max<long long>(1, Str / Bn);
+        int step = 0;
+        for (int ep = 0; ep < epochs; ep++) {
+            long long stride = (long long)(rnd() % (uint64_t)Str) | 1;
+            while (gcd_ll(stride, Str) != 1) stride += 2;
+            const long long off = (long long)(rnd() % (uint64_t)Str);
+            const float lr = 2e-3f * std::pow(0.05f, (float)ep / (float)std::max(1, epochs - 1));
+            for (long long k = 0; k < steps_per_epoch; k++) {
+                launch_surr_gather(Bn, Str, (off + (k * Bn % Str) * (stride % Str)) % Str, stride, feat.p, y.p, xb.p,
+                                   yb.p, c->stream, &c->launches);
+                surr_forward_backward(Bn, xb.p, yb.p, wb.p, g.p, nullptr, out.p, scratch.p, c->stream, &c->launches);
+                launch_surr_adam(w.p, wb.p, g.p, m1.p, v1.p, lr, ++step, c->stream, &c->launches);
+            }
+        }
+        // validation rms of y over the held-out tail
+        double se = 0;
+        long long nv = 0;
+        for (long long i0 = Str; i0 < S; i0 += Bn) {
+            const int nb = (int)std::min<long long>(Bn, S - i0);
+            OPSEC_CUDA(cudaMemsetAsync(loss.p, 0, sizeof(double), c->stream));
+            surr_forward_backward(nb, feat.p + (size_t)i0 * kSurrIn, y.p + i0, wb.p, g.p, loss.p, out.p, scratch.p,
+                                  c->stream, &c->launches);
+            double l = 0;
+            OPSEC_CUDA(cudaMemcpyAsync(&l, loss.p, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+            sync(c);
+            se += l * nb;
+            nv += nb;
+        }
+        val_sum += std::sqrt(se / std::max<long long>(nv, 1)) * ysc;
+        OPSEC_CUDA(cudaMemcpyAsync(all.data() + (size_t)mem * kSurrParams, w.p, sizeof(float) * kSurrParams,
+                                   cudaMemcpyDeviceToHost, c->stream));
+        sync(c);
+    }
+    const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    c->surr_w = all;
+    c->surr_ysc = ysc;
+    if (stats) {
+        stats[0] = (double)S;
+        stats[1] = val_sum / opsec_gpu::kMembers;
+        stats[2] = secs;
+        stats[3] = ysc;
+    }
+}
+
 void build_q(opsec_gpu* c) {
     if (c->q_ok) return;
     build_tables(c);
@@ -684,6 +936,10 @@ void build_q(opsec_gpu* c) {
         a.work_bytes = cubature_work_bytes(c->ks, c->xl.n());
         c->cubwork.alloc(a.work_bytes);
         a.work = c->cubwork.p;
+    }
+    if (c->surr_on) {
+        surrogate_stage(c);
+        a.skip = c->surr_done.p;
     }
     launch_cubature(a, c->stream, &c->launches);
     sync(c);
@@ -1417,6 +1673,76 @@ int opsec_gpu_fisher_build(opsec_gpu* c, int ncells, const opsec_cell* cells, co
         fisher_and_epilogue(c, n, c->Dp.p, nullptr, mixing, phat, pcov, F, W, M, q, f);
         t.mark();
         t.finish();
+    });
+}
+
+int opsec_gpu_surrogate_train(opsec_gpu* c, long long max_samples, int epochs, unsigned seed, double* stats) {
+    return guard(c, [&] {
+        if (max_samples < 64 || epochs < 1) fail(OPSEC_ERR_ARG, "max_samples must be >= 64 and epochs >= 1");
+        surrogate_train(c, max_samples, epochs, seed, stats);
+    });
+}
+
+int opsec_gpu_surrogate_size(void) { return opsec_gpu::kMembers * kSurrParams + 1; }
+
+int opsec_gpu_surrogate_weights(opsec_gpu* c, float* buf, int get) {
+    return guard(c, [&] {
+        if (!buf) fail(OPSEC_ERR_ARG, "null buffer");
+        const size_t n = (size_t)opsec_gpu::kMembers * kSurrParams;
+        if (get) {
+            if (c->surr_w.size() != n) fail(OPSEC_ERR_STATE, "no surrogate weights");
+            std::memcpy(buf, c->surr_w.data(), sizeof(float) * n);
+            buf[n] = c->surr_ysc;
+        } else {
+            if (!(buf[n] > 0) || !std::isfinite(buf[n])) fail(OPSEC_ERR_ARG, "invalid surrogate scale");
+            c->surr_w.assign(buf, buf + n);
+            c->surr_ysc = buf[n];
+            c->q_ok = c->qsq_ok = false;
+        }
+    });
+}
+
+int opsec_gpu_surrogate_stats(const opsec_gpu* c, long long* counts) {
+    if (!c || !counts) return OPSEC_ERR_ARG;
+    for (int i = 0; i < 3; i++) counts[i] = c->surr_counts[i];
+    return OPSEC_OK;
+}
+
+int opsec_gpu_surrogate_eval(opsec_gpu* c, const float* params, int n, const float* feats, const float* y,
+                             float* out_tc, float* out_simt, double* loss, float* grad) {
+    return guard(c, [&] {
+        if (!params || !feats || n <= 0 || n > (1 << 20)) fail(OPSEC_ERR_ARG, "invalid surrogate evaluation arguments");
+        DevBuf<float> w, wb, f, yy, g, scratch, out, o2;
+        DevBuf<double> l;
+        std::vector<float> hwb(params, params + kSurrParams);
+        for (float& v : hwb) v = bf16_round_host(v);
+        std::vector<float> hf(feats, feats + (size_t)n * kSurrIn);
+        for (float& v : hf) v = bf16_round_host(v);
+        w.alloc(kSurrParams);
+        wb.alloc(kSurrParams);
+        f.alloc((size_t)n * kSurrIn);
+        g.alloc(kSurrParams);
+        scratch.alloc((size_t)7 * n * kSurrHid);
+        out.alloc(n);
+        o2.alloc(n);
+        l.alloc(1);
+        OPSEC_CUDA(cudaMemcpyAsync(w.p, params, sizeof(float) * kSurrParams, cudaMemcpyHostToDevice, c->stream));
+        OPSEC_CUDA(cudaMemcpyAsync(wb.p, hwb.data(), sizeof(float) * kSurrParams, cudaMemcpyHostToDevice, c->stream));
+        OPSEC_CUDA(cudaMemcpyAsync(f.p, hf.data(), sizeof(float) * hf.size(), cudaMemcpyHostToDevice, c->stream));
+        OPSEC_CUDA(cudaMemsetAsync(g.p, 0, sizeof(float) * kSurrParams, c->stream));
+        OPSEC_CUDA(cudaMemsetAsync(l.p, 0, sizeof(double), c->stream));
+        if (y) {
+            yy.alloc(n);
+            OPSEC_CUDA(cudaMemcpyAsync(yy.p, y, sizeof(float) * n, cudaMemcpyHostToDevice, c->stream));
+        }
+        surr_forward_backward(n, f.p, y ? yy.p : nullptr, wb.p, g.p, l.p, out.p, scratch.p, c->stream, &c->launches);
+        launch_surr_infer(n, nullptr, 1, nullptr, nullptr, f.p, w.p, o2.p, c->stream, &c->launches);
+        if (out_simt) OPSEC_CUDA(cudaMemcpyAsync(out_simt, out.p, sizeof(float) * n, cudaMemcpyDeviceToHost, c->stream));
+        if (out_tc) OPSEC_CUDA(cudaMemcpyAsync(out_tc, o2.p, sizeof(float) * n, cudaMemcpyDeviceToHost, c->stream));
+        if (y && grad)
+            OPSEC_CUDA(cudaMemcpyAsync(grad, g.p, sizeof(float) * kSurrParams, cudaMemcpyDeviceToHost, c->stream));
+        if (y && loss) OPSEC_CUDA(cudaMemcpyAsync(loss, l.p, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+        sync(c);
     });
 }
 

@@ -277,6 +277,7 @@ __global__ void __launch_bounds__(Shape<NG>::kWarps * 32, 1)
     for (long long j = (long long)blockIdx.x * kWarps + warp; j < nwork; j += (long long)gridDim.x * kWarps) {
         const long long key = a.list ? (long long)a.list[j] : j;
         if (!a.list && a.ks.coordsys == 2 && a.ks.mu_reflect && reflect_partner(a.ks, key) < key) continue;
+        if (!a.list && a.skip && a.skip[key]) continue;
         int c1[3], c2[3];
         decode_key(a.ks, key, c1, c2);
         const float4* G1 = a.pts + 2 * NP * cell_id(a.ks, c1);
@@ -432,7 +433,7 @@ __global__ void key_window_kernel(CubatureArgs a, WinPlan w) {
     const int nx = a.xl.n();
     for (long long key = blockIdx.x * (long long)blockDim.x + threadIdx.x; key < a.ks.nkeys;
          key += (long long)gridDim.x * blockDim.x) {
-        if (a.ks.coordsys == 2 && a.ks.mu_reflect && reflect_partner(a.ks, key) < key) {
+        if ((a.ks.coordsys == 2 && a.ks.mu_reflect && reflect_partner(a.ks, key) < key) || (a.skip && a.skip[key])) {
             w.win[key] = make_int2(-1, 0);
             continue;
         }

@@ -114,6 +114,7 @@ struct CubatureArgs {
     // list mode (set internally): integrate the keys list[0 .. *list_count) only
     const int* list = nullptr;
     const int* list_count = nullptr;
+    const unsigned char* skip = nullptr;  // keys already filled (by the surrogate): not integrated
 };
 // float4s of the point table for a key space and ng
 size_t cubature_point_count(const KeySpace& ks, int ng);
@@ -188,6 +189,39 @@ struct ProjectArgs {
 };
 size_t project_work_bytes(const ProjectArgs& a);
 void launch_project(const ProjectArgs& a, cudaStream_t s, long long* launches);
+
+// ------------------------------------------------------------- learned far-field surrogate
+constexpr int kSurrIn = 16;      // 12 features, zero-padded to one 16-wide MMA step
+constexpr int kSurrHid = 128;
+constexpr int kSurrKeyStride = 10;  // per key: 8 geometry features, d, far flag
+// FP32 layout of one network: W1[128][16] b1 W2[128][128] b2 W3[128][128] b3 w4[128] b4 (padded)
+constexpr int kSurrOffW1 = 0, kSurrOffB1 = 2048, kSurrOffW2 = 2176, kSurrOffB2 = 18560, kSurrOffW3 = 18688,
+              kSurrOffB3 = 35072, kSurrOffW4 = 35200, kSurrOffB4 = 35328, kSurrParams = 35336;
+struct SurrGrid {
+    double b[6];  // survey bounds
+    double d[3];  // cell spacing per axis
+};
+void launch_surr_key_geometry(const KeySpace& ks, const SurrGrid& g, float far_widths, float* kg, cudaStream_t s,
+                              long long* launches);
+void launch_surr_far_list(const KeySpace& ks, const float* kg, long long* list, int* count, cudaStream_t s,
+                          long long* launches);
+void launch_surr_samples(long long nsamp, const long long* keys, int ntab, const float* kg, const float4* tinfo,
+                         const XiLayout& xl, const double* xi64, const double* Q, long long nkeys, float* feat,
+                         float* y, cudaStream_t s, long long* launches);
+// fused BF16 tensor-core forward of one member over samples (keys x tables, or explicit features)
+void launch_surr_infer(long long nsamp, const long long* keys, int ntab, const float* kg, const float4* tinfo,
+                       const float* feat, const float* w, float* out, cudaStream_t s, long long* launches);
+void launch_surr_combine(long long nlist, const long long* keys, int ntab, int nmem, const float* pred,
+                         const float* kg, const XiLayout& xl, const double* xi64, float ysc, float tol,
+                         long long nkeys, double* Q, unsigned char* done, int* counts, cudaStream_t s,
+                         long long* launches);
+// training: forward (+ backward when y != null) over one batch; scratch 7 Bn 128 floats
+void surr_forward_backward(int Bn, const float* x, const float* y, const float* wb, float* grad, double* loss,
+                           float* out, float* scratch, cudaStream_t s, long long* launches);
+void launch_surr_gather(int Bn, long long S, long long off, long long stride, const float* feat, const float* y,
+                        float* xb, float* yb, cudaStream_t s, long long* launches);
+void launch_surr_adam(float* w, float* wb, const float* g, float* m, float* v, float lr, int step, cudaStream_t s,
+                      long long* launches);
 
 // Fisher / bias / quadratic estimates from packed FP32 C_p, FP64 accumulation.
 struct FisherArgs {

@@ -1,0 +1,123 @@
+"""The learned far-field surrogate.
+
+CPU: the numpy restatement (oracle/surrogate_net.py) against finite differences.
+GPU, through the C ABI:
+  * the fused tensor-core forward kernel and the training forward pass against
+    the restatement (BF16 inputs, parameters and hidden activations on both
+    sides): 2e-3 of the largest output;
+  * the training gradient against the restatement's: 1e-3 of its norm;
+  * an ensemble trained on one full-sky shell, applied to another: its Fisher
+    matrix against the plain cubature's, and against the method without the
+    network (zero networks: every far key set to the point value xi_t(d)).
+"""
+import numpy as np
+import pytest
+
+import surrogate_net as SO
+from opsec_gpu import api, synth
+
+PK = synth.pk_table()
+
+
+def features(n, rng):
+    """Inputs in the ranges the surrogate sees: d/1000, mu, 6 extents/100, k edges x 5, sin, cos."""
+    f = np.zeros((n, 16))
+    d = rng.uniform(50, 2000, n)
+    f[:, 0] = d / 1000
+    f[:, 1] = rng.uniform(0, 1, n)
+    f[:, 2:8] = rng.uniform(0.05, 2.0, (n, 6))
+    k = rng.uniform(0, 0.4, n)
+    f[:, 8] = 5 * k
+    f[:, 9] = 5 * (k + 0.01)
+    f[:, 10] = np.sin((k + 0.005) * d)
+    f[:, 11] = np.cos((k + 0.005) * d)
+    return f
+
+
+def test_oracle_gradient_matches_finite_differences():
+    rng = np.random.default_rng(1)
+    p = SO.init(3).astype(np.float64)
+    p[SO.OFF["b1"]:SO.OFF["b1"] + 128] = rng.normal(0, 0.1, 128)
+    x = features(40, rng)
+    y = rng.normal(0, 0.3, 40)
+    _, g = SO.loss_and_grad(p, x, y, rounded=False)
+    idx = [rng.choice(np.arange(o, o + 128), 5, replace=False) for n, o in SO.OFF.items() if n != "b4"]
+    for i in np.concatenate(idx + [[SO.OFF["b4"]]]):
+        h = 1e-6
+        pp, pm = p.copy(), p.copy()
+        pp[i] += h
+        pm[i] -= h
+        fd = (SO.loss(pp, x, y, rounded=False) - SO.loss(pm, x, y, rounded=False)) / (2 * h)
+        assert abs(fd - g[i]) <= 1e-6 * max(1.0, abs(g[i])) + 1e-9, (i, fd, g[i])
+
+
+@pytest.mark.gpu
+def test_surrogate_forward_and_gradient_against_restatement():
+    rng = np.random.default_rng(2)
+    sv, _ = synth.shell_survey(3, 4, 8)
+    e = api.Engine(api.make_config(sv, bands=synth.band_edges(2, 0.0, 0.1)))
+    p = SO.init(5)
+    p[SO.OFF["b1"]:SO.OFF["b1"] + 128] = rng.normal(0, 0.1, 128)
+    p[SO.OFF["b2"]:SO.OFF["b2"] + 128] = rng.normal(0, 0.1, 128)
+    n = 300
+    x = features(n, rng)
+    y = rng.normal(0, 0.3, n)
+    r = e.surrogate_eval(p, x, y)
+    ref_out, _ = SO.forward(p.astype(np.float64), x)
+    scale = np.max(np.abs(ref_out))
+    print("max |out - ref| / max|ref|: simt", np.max(np.abs(r["out_simt"] - ref_out)) / scale,
+          "tc", np.max(np.abs(r["out_tc"] - ref_out)) / scale)
+    assert np.max(np.abs(r["out_simt"] - ref_out)) <= 2e-3 * scale
+    assert np.max(np.abs(r["out_tc"] - ref_out)) <= 2e-3 * scale
+    assert np.max(np.abs(r["out_tc"] - r["out_simt"])) <= 2e-3 * scale
+    ref_loss, ref_g = SO.loss_and_grad(p.astype(np.float64), x, y.astype(np.float32).astype(np.float64))
+    print("loss", r["loss"], ref_loss, "grad rel", np.linalg.norm(r["grad"] - ref_g) / np.linalg.norm(ref_g))
+    assert abs(r["loss"] - ref_loss) <= 1e-3 * ref_loss
+    assert np.linalg.norm(r["grad"] - ref_g) <= 1e-3 * np.linalg.norm(ref_g)
+    sizes = {"W1": 2048, "b1": 128, "W2": 16384, "b2": 128, "W3": 16384, "b3": 128, "w4": 128, "b4": 1}
+    for name, off in SO.OFF.items():  # every parameter block, not only the norm
+        blk = slice(off, off + sizes[name])
+        assert np.linalg.norm(r["grad"][blk] - ref_g[blk]) <= 5e-3 * np.linalg.norm(ref_g[blk]) + 1e-12, name
+    e.close()
+
+
+def fisher(sv, cells, counts, bands, M, extra, weights=None):
+    e = api.Engine(api.make_config(sv, bands=bands, extra=extra))
+    e.set_pk(*PK)
+    if weights is not None:
+        e.surrogate_weights(weights)
+    r = e.fisher_build(cells, counts, M)
+    stats = e.surrogate_stats() if weights is not None else None
+    e.close()
+    return r, stats
+
+
+@pytest.mark.gpu
+def test_surrogate_trained_on_one_shell_applied_to_another():
+    bands = synth.band_edges(20, 0.0, 0.2)
+    # train on a 10 x 10 x 20 shell
+    sv_t, _ = synth.shell_survey(10, 10, 20)
+    et = api.Engine(api.make_config(sv_t, bands=bands))
+    et.set_pk(*PK)
+    info = et.surrogate_train(max_samples=1_500_000, epochs=30, seed=1)
+    w = et.surrogate_weights()
+    et.close()
+    print("training:", info)
+    # apply to an 8 x 12 x 24 shell (other cell sizes and shapes)
+    sv, cells = synth.shell_survey(8, 12, 24)
+    counts = synth.grf_counts(sv, cells)
+    M = 400
+    plain, _ = fisher(sv, cells, counts, bands, M, [])
+    surr, st = fisher(sv, cells, counts, bands, M, ["surrogate = 1"], w)
+    zero = np.zeros_like(w)
+    zero[-1] = w[-1]
+    point, st0 = fisher(sv, cells, counts, bands, M, ["surrogate = 1"], zero)
+    sc = np.max(np.abs(plain["F"]))
+    err_s = np.max(np.abs(surr["F"] - plain["F"])) / sc
+    err_p = np.max(np.abs(point["F"] - plain["F"])) / sc
+    print(f"far keys {st['far']}, predicted {st['predicted']}, sent back {st['fallback']}; "
+          f"Fisher rel err: surrogate {err_s:.2e}, point value {err_p:.2e}")
+    assert st["predicted"] > 0
+    assert st0["predicted"] == st0["far"]  # identical zero networks always agree
+    assert err_s < 0.2 * err_p, (err_s, err_p)
+    assert err_s < 2e-2, err_s
