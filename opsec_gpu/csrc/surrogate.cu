@@ -173,17 +173,20 @@ __global__ void __launch_bounds__(256) surr_gemm_kernel(int M, int N, int K, con
     __shared__ float Bs[kTK][kTN + 4];
     const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
     const int m0 = blockIdx.y * kTM, n0 = blockIdx.x * kTN;
+    // split K over blockIdx.z (then the partial products are added into C, which starts at zero)
+    const int kc = (K + gridDim.z - 1) / gridDim.z;
+    const int kbeg = blockIdx.z * kc, kend = min(K, kbeg + kc);
     float acc[4][4] = {};
-    for (int k0 = 0; k0 < K; k0 += kTK) {
+    for (int k0 = kbeg; k0 < kend; k0 += kTK) {
         for (int e = threadIdx.x; e < kTK * kTM; e += 256) {
             const int kk = e / kTM, mm = e % kTM;
             const int m = m0 + mm, k = k0 + kk;
-            As[kk][mm] = (m < M && k < K) ? A[m * sam + k * sak] : 0.f;
+            As[kk][mm] = (m < M && k < kend) ? A[m * sam + k * sak] : 0.f;
         }
         for (int e = threadIdx.x; e < kTK * kTN; e += 256) {
             const int kk = e / kTN, nn = e % kTN;
             const int n = n0 + nn, k = k0 + kk;
-            Bs[kk][nn] = (n < N && k < K) ? B[k * sbk + n * sbn] : 0.f;
+            Bs[kk][nn] = (n < N && k < kend) ? B[k * sbk + n * sbn] : 0.f;
         }
         __syncthreads();
 #pragma unroll
@@ -215,7 +218,10 @@ __global__ void __launch_bounds__(256) surr_gemm_kernel(int M, int N, int K, con
             } else if (epi == 2) {
                 v *= gelu_grad(zprev[(size_t)m * ldc + n]);
             }
-            C[(size_t)m * ldc + n] = v;
+            if (gridDim.z > 1)
+                atomicAdd(&C[(size_t)m * ldc + n], v);
+            else
+                C[(size_t)m * ldc + n] = v;
         }
 }
 
@@ -539,6 +545,9 @@ void surr_forward_backward(int Bn, const float* x, const float* y, const float* 
     float* dz = a3 + (size_t)Bn * H;
     const dim3 blk(256);
     auto grid = [&](int M, int N) { return dim3((N + kTN - 1) / kTN, (M + kTM - 1) / kTM); };
+    // weight gradients sum over the batch: split it over 256-row slices, added atomically
+    const int ks = std::max(1, std::min(32, Bn / 256));
+    auto gridk = [&](int M, int N) { return dim3((N + kTN - 1) / kTN, (M + kTM - 1) / kTM, ks); };
     // forward: Z = X W^T + b, A = gelu(Z) (a1, a2 BF16-valued; a3 FP32 into the output layer)
     surr_gemm_kernel<<<grid(Bn, H), blk, 0, s>>>(Bn, H, kSurrIn, x, kSurrIn, 1, wb + kSurrOffW1, 1, kSurrIn, z1, H, 1,
                                                  wb + kSurrOffB1, a1, 1, nullptr);
@@ -553,22 +562,23 @@ void surr_forward_backward(int Bn, const float* x, const float* y, const float* 
         ++*l;
         return;
     }
+    OPSEC_CUDA(cudaMemsetAsync(grad, 0, sizeof(float) * kSurrParams, s));
     surr_out_kernel<<<(Bn + 7) / 8, dim3(32, 8), 0, s>>>(Bn, a3, z3, wb, y, out, dz, loss);
     surr_outgrad_kernel<<<1, kSurrHid + 32, 0, s>>>(Bn, a3, out, y, grad);
     // layer 3: dW3 = dZ3^T A2, db3, dZ2 = (dZ3 W3) * gelu'(Z2) (into a3)
-    surr_gemm_kernel<<<grid(H, H), blk, 0, s>>>(H, H, Bn, dz, 1, H, a2, H, 1, grad + kSurrOffW3, H, 0, nullptr,
+    surr_gemm_kernel<<<gridk(H, H), blk, 0, s>>>(H, H, Bn, dz, 1, H, a2, H, 1, grad + kSurrOffW3, H, 0, nullptr,
                                                 nullptr, 0, nullptr);
     surr_colsum_kernel<<<1, H, 0, s>>>(Bn, H, dz, grad + kSurrOffB3);
     surr_gemm_kernel<<<grid(Bn, H), blk, 0, s>>>(Bn, H, H, dz, H, 1, wb + kSurrOffW3, H, 1, a3, H, 2, nullptr,
                                                  nullptr, 0, z2);
     // layer 2: dW2 = dZ2^T A1, db2, dZ1 = (dZ2 W2) * gelu'(Z1) (into dz)
-    surr_gemm_kernel<<<grid(H, H), blk, 0, s>>>(H, H, Bn, a3, 1, H, a1, H, 1, grad + kSurrOffW2, H, 0, nullptr,
+    surr_gemm_kernel<<<gridk(H, H), blk, 0, s>>>(H, H, Bn, a3, 1, H, a1, H, 1, grad + kSurrOffW2, H, 0, nullptr,
                                                 nullptr, 0, nullptr);
     surr_colsum_kernel<<<1, H, 0, s>>>(Bn, H, a3, grad + kSurrOffB2);
     surr_gemm_kernel<<<grid(Bn, H), blk, 0, s>>>(Bn, H, H, a3, H, 1, wb + kSurrOffW2, H, 1, dz, H, 2, nullptr,
                                                  nullptr, 0, z1);
     // layer 1: dW1 = dZ1^T X, db1
-    surr_gemm_kernel<<<grid(H, kSurrIn), blk, 0, s>>>(H, kSurrIn, Bn, dz, 1, H, x, kSurrIn, 1, grad + kSurrOffW1,
+    surr_gemm_kernel<<<gridk(H, kSurrIn), blk, 0, s>>>(H, kSurrIn, Bn, dz, 1, H, x, kSurrIn, 1, grad + kSurrOffW1,
                                                       kSurrIn, 0, nullptr, nullptr, 0, nullptr);
     surr_colsum_kernel<<<1, H, 0, s>>>(Bn, H, dz, grad + kSurrOffB1);
     OPSEC_CUDA(cudaGetLastError());
