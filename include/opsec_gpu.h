@@ -135,14 +135,15 @@ long long opsec_gpu_launch_count(const opsec_gpu* ctx);
  * (12 geometry/band inputs -> 3 x 128 GELU -> 1, BF16 products, FP32
  * accumulation) predicts the integrals of key pairs at least `surrogate.far`
  * (default 2) cell widths apart on spherical grids; a key whose members
- * disagree by more than `surrogate.tol` (default 1e-3, in units of the table
- * at r = 0) and every nearer key are integrated by the cubature.  Enabled by
+ * disagree by more than `surrogate.tol` (default 1e-3, in units of the
+ * table's largest magnitude within 25 % of the pair's centre separation)
+ * and every nearer key are integrated by the cubature.  Enabled by
  * the configuration key `surrogate = 1` once weights are present. */
 
 /* Train the ensemble on this context's own survey: every key integrated by
  * the cubature, then up to max_samples (far key, table) samples, 2% held out,
  * `epochs` passes of Adam.  stats (4, may be NULL): samples, validation rms of
- * the residual (units of the table at r = 0), training seconds, output scale. */
+ * the residual (units of the local table envelope), training seconds, output scale. */
 int opsec_gpu_surrogate_train(opsec_gpu* ctx, long long max_samples, int epochs, unsigned seed, double* stats);
 /* Floats in a weight buffer: 4 networks x 35336 FP32 parameters, then the output scale. */
 int opsec_gpu_surrogate_size(void);

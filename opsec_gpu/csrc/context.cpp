@@ -313,6 +313,7 @@ struct opsec_gpu {
     float surr_ysc = 0.f;
     long long surr_counts[3] = {0, 0, 0};  // keys predicted, sent back to the cubature, far keys
     DevBuf<float> surr_kg, surr_wdev, surr_pred, surr_tinfo;
+    DevBuf<double> surr_env;  // [ntab][n]: local envelope of every table
     DevBuf<long long> surr_list;
     DevBuf<unsigned char> surr_done;
     DevBuf<int> surr_cnt;
@@ -642,6 +643,33 @@ void surr_tables(opsec_gpu* c) {
                                c->stream));
 }
 
+// env_t(r_i) = max |xi_t(r_j)| over r_j in [r_i / 1.25, 1.25 r_i]: the scale of
+// the surrogate's target, so that its error follows the local size of a table
+void surr_envelope(opsec_gpu* c) {
+    const int n = c->xl.n(), ntab = c->ntab();
+    std::vector<double> tab((size_t)ntab * n), env((size_t)ntab * n);
+    OPSEC_CUDA(cudaMemcpyAsync(tab.data(), c->xi64.p, sizeof(double) * tab.size(), cudaMemcpyDeviceToHost, c->stream));
+    std::vector<double> r(n);
+    OPSEC_CUDA(cudaMemcpyAsync(r.data(), c->r_grid.p, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+    sync(c);
+    for (int t = 0; t < ntab; t++) {
+        const double* T = tab.data() + (size_t)t * n;
+        int lo = 0, hi = 0;  // window [lo, hi) of r_j in [r_i / 1.25, 1.25 r_i]
+        for (int i = 0; i < n; i++) {
+            while (lo < i && r[lo] < r[i] / 1.25) lo++;
+            if (hi < i + 1) hi = i + 1;
+            while (hi < n && r[hi] <= 1.25 * r[i]) hi++;
+            double m = 0;
+            for (int j = lo; j < hi; j++) m = std::max(m, std::fabs(T[j]));
+            env[(size_t)t * n + i] = m > 0 ? m : 1e-300;
+        }
+    }
+    c->surr_env.alloc(env.size());
+    OPSEC_CUDA(cudaMemcpyAsync(c->surr_env.p, env.data(), sizeof(double) * env.size(), cudaMemcpyHostToDevice,
+                               c->stream));
+    sync(c);
+}
+
 // key geometry and the canonical far keys; returns their number
 long long surr_far_keys(opsec_gpu* c) {
     if (c->geo.coordsys != 2) fail(OPSEC_ERR_CONFIG, "the surrogate covers spherical grids only");
@@ -666,6 +694,7 @@ void surrogate_stage(opsec_gpu* c) {
     const KeySpace& ks = c->ks;
     const int ntab = c->ntab();
     surr_tables(c);
+    surr_envelope(c);
     const long long nfar = surr_far_keys(c);
     c->surr_done.alloc((size_t)ks.nkeys);
     OPSEC_CUDA(cudaMemsetAsync(c->surr_done.p, 0, (size_t)ks.nkeys, c->stream));
@@ -684,8 +713,9 @@ void surrogate_stage(opsec_gpu* c) {
         launch_surr_infer(nsamp, c->surr_list.p, ntab, c->surr_kg.p, ti, nullptr,
                           c->surr_wdev.p + (size_t)m * kSurrParams, c->surr_pred.p + (size_t)m * nsamp, c->stream,
                           &c->launches);
-    launch_surr_combine(nfar, c->surr_list.p, ntab, nm, c->surr_pred.p, c->surr_kg.p, c->xl, c->xi64.p, c->surr_ysc,
-                        c->surr_tol, ks.nkeys, c->Q.p, c->surr_done.p, c->surr_cnt.p + 1, c->stream, &c->launches);
+    launch_surr_combine(nfar, c->surr_list.p, ntab, nm, c->surr_pred.p, c->surr_kg.p, c->xl, c->xi64.p,
+                        c->surr_env.p, c->surr_ysc, c->surr_tol, ks.nkeys, c->Q.p, c->surr_done.p, c->surr_cnt.p + 1,
+                        c->stream, &c->launches);
     if (g_clock) g_clock->end(c->stream);
     int cnt[2] = {0, 0};
     OPSEC_CUDA(cudaMemcpyAsync(cnt, c->surr_cnt.p + 1, sizeof(int) * 2, cudaMemcpyDeviceToHost, c->stream));
@@ -750,6 +780,7 @@ void surrogate_train(opsec_gpu* c, long long max_samples, int epochs, unsigned s
     const KeySpace& ks = c->ks;
     const int ntab = c->ntab();
     surr_tables(c);
+    surr_envelope(c);
     const long long nfar = surr_far_keys(c);
     if (nfar < 16) fail(OPSEC_ERR_ARG, "too few far keys to train the surrogate");
     std::vector<long long> keys(nfar);
@@ -775,7 +806,7 @@ void surrogate_train(opsec_gpu* c, long long max_samples, int epochs, unsigned s
     feat.alloc((size_t)S * kSurrIn);
     y.alloc(S);
     launch_surr_samples(S, dkeys.p, ntab, c->surr_kg.p, reinterpret_cast<const float4*>(c->surr_tinfo.p), c->xl,
-                        c->xi64.p, c->Q.p, ks.nkeys, feat.p, y.p, c->stream, &c->launches);
+                        c->xi64.p, c->surr_env.p, c->Q.p, ks.nkeys, feat.p, y.p, c->stream, &c->launches);
     std::vector<float> hy(S);
     OPSEC_CUDA(cudaMemcpyAsync(hy.data(), y.p, sizeof(float) * S, cudaMemcpyDeviceToHost, c->stream));
     sync(c);

@@ -206,14 +206,14 @@ void launch_surr_key_geometry(const KeySpace& ks, const SurrGrid& g, float far_w
 void launch_surr_far_list(const KeySpace& ks, const float* kg, long long* list, int* count, cudaStream_t s,
                           long long* launches);
 void launch_surr_samples(long long nsamp, const long long* keys, int ntab, const float* kg, const float4* tinfo,
-                         const XiLayout& xl, const double* xi64, const double* Q, long long nkeys, float* feat,
-                         float* y, cudaStream_t s, long long* launches);
+                         const XiLayout& xl, const double* xi64, const double* env, const double* Q, long long nkeys,
+                         float* feat, float* y, cudaStream_t s, long long* launches);
 // fused BF16 tensor-core forward of one member over samples (keys x tables, or explicit features)
 void launch_surr_infer(long long nsamp, const long long* keys, int ntab, const float* kg, const float4* tinfo,
                        const float* feat, const float* w, float* out, cudaStream_t s, long long* launches);
 void launch_surr_combine(long long nlist, const long long* keys, int ntab, int nmem, const float* pred,
-                         const float* kg, const XiLayout& xl, const double* xi64, float ysc, float tol,
-                         long long nkeys, double* Q, unsigned char* done, int* counts, cudaStream_t s,
+                         const float* kg, const XiLayout& xl, const double* xi64, const double* env, float ysc,
+                         float tol, long long nkeys, double* Q, unsigned char* done, int* counts, cudaStream_t s,
                          long long* launches);
 // training: forward (+ backward when y != null) over one batch; scratch 7 Bn 128 floats
 void surr_forward_backward(int Bn, const float* x, const float* y, const float* wb, float* grad, double* loss,

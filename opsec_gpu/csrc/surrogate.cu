@@ -2,9 +2,10 @@
 //
 // For a key whose two cells are at least `far` cell widths apart, a small MLP
 // predicts the residual of Q_t(key) from the point value xi_t(d) at the
-// centre separation d, in units of the table's value at r = 0:
+// centre separation d, in units of the table's local envelope env_t(d) =
+// max |xi_t(r)| over r in [d / 1.25, 1.25 d]:
 //
-//   y_t(key) = (Q_t(key) - xi_t(d)) / xi_t(0),   Q_t = xi_t(d) + xi_t(0) ysc net(f)
+//   y_t(key) = (Q_t(key) - xi_t(d)) / env_t(d),   Q_t = xi_t(d) + env_t(d) ysc net(f)
 //
 // Inputs (12): d / 1000, mu (|cos| of the separation against the line of
 // sight through the pair's midpoint), the extents of both cells
@@ -143,10 +144,10 @@ __device__ __forceinline__ float surr_feature(const float* kg, float4 ti, int c)
 }
 
 // Training samples: sample s = (key list[s / ntab], table s % ntab): BF16-valued
-// features [s][16] and target y = (Q - xi_t(d)) / xi_t(0).
+// features [s][16] and target y = (Q - xi_t(d)) / env_t(d).
 __global__ void surr_samples_kernel(long long nsamp, const long long* keys, int ntab, const float* kg,
-                                    const float4* tinfo, XiLayout xl, const double* xi64, const double* Q,
-                                    long long nkeys, float* feat, float* y) {
+                                    const float4* tinfo, XiLayout xl, const double* xi64, const double* env,
+                                    const double* Q, long long nkeys, float* feat, float* y) {
     const int n = xl.n();
     for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < nsamp;
          s += (long long)gridDim.x * blockDim.x) {
@@ -156,7 +157,7 @@ __global__ void surr_samples_kernel(long long nsamp, const long long* keys, int 
         const float4 ti = tinfo[t];
         for (int c = 0; c < kSurrIn; c++) feat[(size_t)s * kSurrIn + c] = bf16r(surr_feature(g, ti, c));
         const double* tab = xi64 + (size_t)t * n;
-        y[s] = (float)((Q[(size_t)t * nkeys + key] - xi_at(xl, tab, g[8])) / tab[0]);
+        y[s] = (float)((Q[(size_t)t * nkeys + key] - xi_at(xl, tab, g[8])) / xi_at(xl, env + (size_t)t * n, g[8]));
     }
 }
 
@@ -420,11 +421,11 @@ __global__ void __launch_bounds__(256) surr_infer_kernel(long long nsamp, const 
 }
 
 // Ensemble: per key of the list, every table's member mean and spread; a key
-// whose spreads all stay within tol gets Q_t = xi_t(d) + xi_t(0) ysc mean and
+// whose spreads all stay within tol gets Q_t = xi_t(d) + env_t(d) ysc mean and
 // is marked done; the others are left to the cubature.
 __global__ void surr_combine_kernel(long long nlist, const long long* keys, int ntab, int nmem, const float* pred,
-                                    const float* kg, XiLayout xl, const double* xi64, float ysc, float tol,
-                                    long long nkeys, double* Q, unsigned char* done, int* counts) {
+                                    const float* kg, XiLayout xl, const double* xi64, const double* env, float ysc,
+                                    float tol, long long nkeys, double* Q, unsigned char* done, int* counts) {
     const int n = xl.n();
     const long long nsamp = nlist * ntab;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nlist;
@@ -448,8 +449,8 @@ __global__ void surr_combine_kernel(long long nlist, const long long* keys, int 
         for (int t = 0; t < ntab; t++) {
             double s = 0;
             for (int m = 0; m < nmem; m++) s += pred[(size_t)m * nsamp + i * ntab + t];
-            const double* tab = xi64 + (size_t)t * n;
-            Q[(size_t)t * nkeys + key] = xi_at(xl, tab, d) + tab[0] * ysc * (s / nmem);
+            Q[(size_t)t * nkeys + key] =
+                xi_at(xl, xi64 + (size_t)t * n, d) + xi_at(xl, env + (size_t)t * n, d) * ysc * (s / nmem);
         }
         done[key] = 1;
         atomicAdd(&counts[0], 1);
@@ -499,9 +500,10 @@ void launch_surr_far_list(const KeySpace& ks, const float* kg, long long* list, 
 }
 
 void launch_surr_samples(long long nsamp, const long long* keys, int ntab, const float* kg, const float4* tinfo,
-                         const XiLayout& xl, const double* xi64, const double* Q, long long nkeys, float* feat,
-                         float* y, cudaStream_t s, long long* l) {
-    surr_samples_kernel<<<blocks_for(nsamp), 256, 0, s>>>(nsamp, keys, ntab, kg, tinfo, xl, xi64, Q, nkeys, feat, y);
+                         const XiLayout& xl, const double* xi64, const double* env, const double* Q, long long nkeys,
+                         float* feat, float* y, cudaStream_t s, long long* l) {
+    surr_samples_kernel<<<blocks_for(nsamp), 256, 0, s>>>(nsamp, keys, ntab, kg, tinfo, xl, xi64, env, Q, nkeys, feat,
+                                                          y);
     OPSEC_CUDA(cudaGetLastError());
     ++*l;
 }
@@ -522,9 +524,10 @@ void launch_surr_infer(long long nsamp, const long long* keys, int ntab, const f
 }
 
 void launch_surr_combine(long long nlist, const long long* keys, int ntab, int nmem, const float* pred,
-                         const float* kg, const XiLayout& xl, const double* xi64, float ysc, float tol,
-                         long long nkeys, double* Q, unsigned char* done, int* counts, cudaStream_t s, long long* l) {
-    surr_combine_kernel<<<blocks_for(nlist), 256, 0, s>>>(nlist, keys, ntab, nmem, pred, kg, xl, xi64, ysc, tol,
+                         const float* kg, const XiLayout& xl, const double* xi64, const double* env, float ysc,
+                         float tol, long long nkeys, double* Q, unsigned char* done, int* counts, cudaStream_t s,
+                         long long* l) {
+    surr_combine_kernel<<<blocks_for(nlist), 256, 0, s>>>(nlist, keys, ntab, nmem, pred, kg, xl, xi64, env, ysc, tol,
                                                          nkeys, Q, done, counts);
     OPSEC_CUDA(cudaGetLastError());
     ++*l;
