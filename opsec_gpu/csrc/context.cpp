@@ -631,10 +631,10 @@ SurrGrid surr_grid(const opsec_gpu* c) {
     return sg;
 }
 
-// per table: (k_lo 5, k_hi 5, band centre k, 0); the full xi table is (0, 0, 0, 0)
+// per table: (k_lo 5, k_hi 5, band centre k, 0); the full xi table is (0, 0, 0.02, 0)
 void surr_tables(opsec_gpu* c) {
     std::vector<float4> ti(c->ntab());
-    ti[0] = make_float4(0.f, 0.f, 0.f, 0.f);
+    ti[0] = make_float4(0.f, 0.f, 0.02f, 0.f);  // the full xi table: scale of the peak of k^2 P(k)
     for (size_t p = 0; p < c->band_lo.size(); p++)
         ti[p + 1] = make_float4((float)(5 * c->band_lo[p]), (float)(5 * c->band_hi[p]),
                                 (float)(0.5 * (c->band_lo[p] + c->band_hi[p])), 0.f);

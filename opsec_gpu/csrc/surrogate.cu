@@ -7,12 +7,13 @@
 //
 //   y_t(key) = (Q_t(key) - xi_t(d)) / env_t(d),   Q_t = xi_t(d) + env_t(d) ysc net(f)
 //
-// Inputs (12): d / 1000, mu (|cos| of the separation against the line of
-// sight through the pair's midpoint), the extents of both cells
-// (dr, r dtheta, r sin(theta) dphi) / 100, the band's k edges x 5 (both 0 for
-// the full xi table), sin(k d) and cos(k d) at the band centre k.  The phase
-// features carry the oscillation of a band table across the pair, so the
-// network only learns its smooth modulation by the cell geometry.
+// Inputs (12): d / 1000; k times the mean transverse path difference
+// <|e_perp|^2> / 24 d; k times the six cell edges (dr, r dtheta, r sin(theta)
+// dphi of both cells) projected on the separation, / 10; the band's k edges
+// x 5 (both 0 for the full xi table); sin(k d) and cos(k d), with k the band
+// centre (0.02 for the full xi table).  The phase features carry the
+// oscillation of a table across the pair and the k-scaled extents its
+// averaging over the cells, so the network learns a smooth map.
 // Network: 12 (padded to 16) -> 128 -> 128 -> 128 -> 1, tanh-form GELU,
 // BF16 weights and activations into every product, FP32 accumulation, FP32
 // master weights trained by Adam.  Four members with different initial
@@ -108,33 +109,44 @@ __global__ void surr_key_geometry_kernel(KeySpace ks, SurrGrid g, float far_widt
             e[s][1] = r * (acos(fmax(fmin(m0, 1.0), -1.0)) - acos(fmax(fmin(m1, 1.0), -1.0)));
             e[s][2] = r * st * g.d[2];
         }
-        double dv[3], mid[3];
-        for (int k = 0; k < 3; k++) {
-            dv[k] = c[1][k] - c[0][k];
-            mid[k] = 0.5 * (c[1][k] + c[0][k]);
-        }
+        double dv[3];
+        for (int k = 0; k < 3; k++) dv[k] = c[1][k] - c[0][k];
         const double d = sqrt(dv[0] * dv[0] + dv[1] * dv[1] + dv[2] * dv[2]);
-        const double rm = sqrt(mid[0] * mid[0] + mid[1] * mid[1] + mid[2] * mid[2]);
-        const double mu = d > 0 && rm > 0 ? fabs(dv[0] * mid[0] + dv[1] * mid[1] + dv[2] * mid[2]) / (d * rm) : 0.0;
-        double w = 0;
-        for (int s = 0; s < 2; s++)
-            for (int k = 0; k < 3; k++) w = fmax(w, e[s][k]);
+        double nh[3] = {0, 0, 1};
+        if (d > 0)
+            for (int k = 0; k < 3; k++) nh[k] = dv[k] / d;
+        // edges of each cell along its local (r, theta, phi) frame, projected on the separation:
+        // a = |e . n| (longitudinal spread), and the transverse spread sum |e|^2 - a^2
+        double a[6], trans = 0, w = 0;
+        for (int s = 0; s < 2; s++) {
+            const double r = sqrt(c[s][0] * c[s][0] + c[s][1] * c[s][1] + c[s][2] * c[s][2]);
+            const double ct = c[s][2] / r, st = sqrt(fmax(1.0 - ct * ct, 0.0));
+            const double ph = atan2(c[s][1], c[s][0]);
+            const double cp = cos(ph), sp = sin(ph);
+            const double fr[3][3] = {{st * cp, st * sp, ct}, {ct * cp, ct * sp, -st}, {-sp, cp, 0.0}};
+            for (int k = 0; k < 3; k++) {
+                const double proj = e[s][k] * fabs(fr[k][0] * nh[0] + fr[k][1] * nh[1] + fr[k][2] * nh[2]);
+                a[3 * s + k] = proj;
+                trans += e[s][k] * e[s][k] - proj * proj;
+                w = fmax(w, e[s][k]);
+            }
+        }
         float* o = kg + (size_t)key * kSurrKeyStride;
         o[0] = (float)(d / 1000);
-        o[1] = (float)mu;
-        for (int k = 0; k < 3; k++) {
-            o[2 + k] = (float)(e[0][k] / 100);
-            o[5 + k] = (float)(e[1][k] / 100);
-        }
+        o[1] = (float)(d > 0 ? trans / (24.0 * d) : 0.0);  // mean transverse path difference, Mpc
+        for (int k = 0; k < 6; k++) o[2 + k] = (float)a[k];
         o[8] = (float)d;
         o[9] = d >= far_widths * w ? 1.f : 0.f;
     }
 }
 
-// feature c of sample (key geometry kg, table info ti = (k_lo 5, k_hi 5, k mid, 0))
+// feature c of sample (key geometry kg, table info ti = (k_lo 5, k_hi 5, k mid, 0)):
+// d / 1000, k <t^2> / 2d, k a_i / 10 for the six projected cell edges, the k edges, sin(k d), cos(k d)
 __device__ __forceinline__ float surr_feature(const float* kg, float4 ti, int c) {
     switch (c) {
-    case 0: case 1: case 2: case 3: case 4: case 5: case 6: case 7: return kg[c];
+    case 0: return kg[0];
+    case 1: return ti.z * kg[1];  // phase of the mean transverse path difference
+    case 2: case 3: case 4: case 5: case 6: case 7: return 0.1f * ti.z * kg[c];  // k x projected extents
     case 8: return ti.x;
     case 9: return ti.y;
     case 10: return sinf(ti.z * kg[8]);
