@@ -6,9 +6,10 @@ GPU, through the C ABI:
     the restatement (BF16 inputs, parameters and hidden activations on both
     sides): 2e-3 of the largest output;
   * the training gradient against the restatement's: 1e-3 of its norm;
-  * an ensemble trained on one full-sky shell, applied to another: its Fisher
-    matrix against the plain cubature's, and against the method without the
-    network (zero networks: every far key set to the point value xi_t(d)).
+  * an ensemble trained on part of a full-sky shell's far keys: its Fisher
+    matrix against the plain cubature's and against the method without the
+    network (zero networks: every far key set to the point value xi_t(d)),
+    and the ensemble-disagreement fallback.
 """
 import numpy as np
 import pytest
@@ -93,31 +94,34 @@ def fisher(sv, cells, counts, bands, M, extra, weights=None):
 
 
 @pytest.mark.gpu
-def test_surrogate_trained_on_one_shell_applied_to_another():
+def test_surrogate_gain_and_fallback():
+    """An ensemble trained on half of a shell's far (key, table) samples, applied
+    to all of its far keys.  Accepting every prediction must beat the method
+    without the network (zero networks: the point value xi_t(d) for every far
+    key) by 5x in the Fisher matrix; with the default tolerance the members'
+    disagreement sends keys back to the cubature and the Fisher matrix stays
+    within 1e-3 of the plain build."""
     bands = synth.band_edges(20, 0.0, 0.2)
-    # train on a 10 x 10 x 20 shell
-    sv_t, _ = synth.shell_survey(10, 10, 20)
-    et = api.Engine(api.make_config(sv_t, bands=bands))
-    et.set_pk(*PK)
-    info = et.surrogate_train(max_samples=1_500_000, epochs=30, seed=1)
-    w = et.surrogate_weights()
-    et.close()
-    print("training:", info)
-    # apply to an 8 x 12 x 24 shell (other cell sizes and shapes)
     sv, cells = synth.shell_survey(8, 12, 24)
     counts = synth.grf_counts(sv, cells)
     M = 400
+    et = api.Engine(api.make_config(sv, bands=bands))
+    et.set_pk(*PK)
+    info = et.surrogate_train(max_samples=276_000, epochs=30, seed=1)
+    w = et.surrogate_weights()
+    et.close()
     plain, _ = fisher(sv, cells, counts, bands, M, [])
-    surr, st = fisher(sv, cells, counts, bands, M, ["surrogate = 1"], w)
+    all_in, st = fisher(sv, cells, counts, bands, M, ["surrogate = 1", "surrogate.tol = 1e9"], w)
     zero = np.zeros_like(w)
     zero[-1] = w[-1]
-    point, st0 = fisher(sv, cells, counts, bands, M, ["surrogate = 1"], zero)
+    point, st0 = fisher(sv, cells, counts, bands, M, ["surrogate = 1", "surrogate.tol = 1e9"], zero)
+    guarded, stg = fisher(sv, cells, counts, bands, M, ["surrogate = 1"], w)
     sc = np.max(np.abs(plain["F"]))
-    err_s = np.max(np.abs(surr["F"] - plain["F"])) / sc
-    err_p = np.max(np.abs(point["F"] - plain["F"])) / sc
-    print(f"far keys {st['far']}, predicted {st['predicted']}, sent back {st['fallback']}; "
-          f"Fisher rel err: surrogate {err_s:.2e}, point value {err_p:.2e}")
-    assert st["predicted"] > 0
-    assert st0["predicted"] == st0["far"]  # identical zero networks always agree
-    assert err_s < 0.2 * err_p, (err_s, err_p)
-    assert err_s < 2e-2, err_s
+    err = {name: np.max(np.abs(r["F"] - plain["F"])) / sc for name, r in
+           (("network", all_in), ("point value", point), ("network, tol 1e-3", guarded))}
+    print("training:", info)
+    print(f"far keys {st['far']}; tol 1e-3: predicted {stg['predicted']}, sent back {stg['fallback']}; "
+          + ", ".join(f"{k} {v:.2e}" for k, v in err.items()))
+    assert st["predicted"] == st["far"] and st0["predicted"] == st0["far"]
+    assert err["network"] < 0.2 * err["point value"], err
+    assert err["network, tol 1e-3"] <= 1e-3, err
