@@ -157,6 +157,31 @@ int opsec_gpu_surrogate_stats(const opsec_gpu* ctx, long long* counts);
 int opsec_gpu_surrogate_eval(opsec_gpu* ctx, const float* params, int n, const float* feats, const float* y,
                              float* out_tc, float* out_simt, double* loss, float* grad);
 
+/* ---- batched mocks (no counterpart in the reference, which runs one survey per
+ * program invocation).  One full-sky spherical survey per mock: the shell
+ * r in [rmin, rmax] on an nr x nmu x nphi grid (mu in [-1, 1], phi in
+ * [0, 2 pi)), its cells in grid order and its counts, built to nmodes modes. */
+typedef struct {
+    double rmin, rmax;
+    int nr, nmu, nphi;
+    int ncells; /* nr * nmu * nphi */
+    const opsec_cell* cells;
+    const double* counts;
+    int nmodes;
+} opsec_mock;
+
+/* Fisher builds of many mocks with the bands, xi layout, Gauss rule and P(k) of
+ * `ctx`: worker contexts (each with its own stream, solver handles and xi
+ * tables, computed once) take mocks in turn from host threads, so that the
+ * builds of small surveys overlap on the GPU.  workers = 1 runs them one after
+ * the other; workers <= 0 autotunes the count on the first mocks (1, 2, 4 and 8
+ * workers, two mocks each) and runs the rest with the fastest.  Outputs per
+ * mock i (mixing = inverse): F + i nb^2, phat + i nb, pcov + i nb^2 (any may be
+ * NULL).  stats (6, may be NULL): seconds, workers used, then the mocks per
+ * second measured for 1, 2, 4 and 8 workers while autotuning. */
+int opsec_gpu_batch_fisher(opsec_gpu* ctx, int nmocks, const opsec_mock* mocks, int workers, double* F,
+                           double* phat, double* pcov, double* stats);
+
 /* Largest band count opsec_gpu_fisher_noalloc accepts. */
 #define OPSEC_NOALLOC_MAX_BANDS 64
 

@@ -66,6 +66,7 @@ def load():
     L.opsec_gpu_surrogate_weights.argtypes = [vp, fp, C.c_int]
     L.opsec_gpu_surrogate_stats.argtypes = [vp, C.POINTER(C.c_longlong)]
     L.opsec_gpu_surrogate_eval.argtypes = [vp, fp, C.c_int, fp, fp, fp, fp, dp, fp]
+    L.opsec_gpu_batch_fisher.argtypes = [vp, C.c_int, vp, C.c_int, dp, dp, dp, dp]
     _lib = L
     return L
 
@@ -76,6 +77,12 @@ def _d(a):
 
 def _i(a):
     return None if a is None else a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+class Mock(C.Structure):
+    """opsec_mock: one full-sky spherical survey of a batch."""
+    _fields_ = [("rmin", C.c_double), ("rmax", C.c_double), ("nr", C.c_int), ("nmu", C.c_int), ("nphi", C.c_int),
+                ("ncells", C.c_int), ("cells", C.c_void_p), ("counts", C.c_void_p), ("nmodes", C.c_int)]
 
 
 def _fp(a):
@@ -268,6 +275,27 @@ class Engine:
                                                      _fp(out_simt), _d(loss), _fp(grad)))
         return {"out_tc": out_tc, "out_simt": out_simt, "loss": loss[0] if y is not None else None,
                 "grad": grad if y is not None else None}
+
+    def batch_fisher(self, mocks, workers=0):
+        """mocks: list of dicts (rmin, rmax, nr, nmu, nphi, cells, counts, nmodes).  Returns
+        F [n][nb][nb], phat [n][nb], pcov [n][nb][nb] and stats (seconds, workers, autotune rates)."""
+        keep = []
+        arr = (Mock * len(mocks))()
+        for i, m in enumerate(mocks):
+            cells = _cells(m["cells"])
+            counts = _f64(m["counts"])
+            keep += [cells, counts]
+            arr[i] = Mock(m["rmin"], m["rmax"], m["nr"], m["nmu"], m["nphi"], cells.size, cells.ctypes.data,
+                          counts.ctypes.data, m["nmodes"])
+        nb = self.num_params()
+        F = np.zeros((len(mocks), nb, nb))
+        phat = np.zeros((len(mocks), nb))
+        pcov = np.zeros((len(mocks), nb, nb))
+        st = np.zeros(6)
+        self._check(self._L.opsec_gpu_batch_fisher(self._h, len(mocks), C.cast(arr, C.c_void_p), int(workers), _d(F),
+                                                   _d(phat), _d(pcov), _d(st)))
+        return {"F": F, "phat": phat, "pcov": pcov, "seconds": st[0], "workers": int(st[1]),
+                "autotune_mocks_per_s": {k: st[2 + i] for i, k in enumerate((1, 2, 4, 8))}}
 
     def fisher_build(self, cells, counts, nmodes, mixing="inverse", want_evals=True):
         cells = _cells(cells)

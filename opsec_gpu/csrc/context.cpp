@@ -5,6 +5,7 @@
 #include <cusolverDn.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cerrno>
 #include <cmath>
@@ -12,10 +13,12 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <memory>
 #include <new>
 #include <sstream>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "engine.h"
@@ -305,6 +308,9 @@ struct opsec_gpu {
     std::vector<int> az_m, az_idx, az_kind;
     std::vector<double> nbar_arc;
     DevBuf<unsigned char> azws;  // azimuthal projection workspace
+    DevBuf<double> nba_dev;      // Nbar per arc
+    DevBuf<unsigned char> syev_ws;  // batched eigensolver workspace
+    std::string cfg_text;        // the configuration the context was created with
     // learned far-field surrogate: 4 networks (FP32 master weights) and the target scale
     static constexpr int kMembers = 4;
     bool surr_on = false;
@@ -1082,7 +1088,7 @@ int eigensolve(opsec_gpu* c, int ncells, const opsec_cell* cells, int M) {
         }
         const int npar = par ? 2 : 1, Hb = H / npar, nblk = nm * npar;
         c->az_npar = npar;
-        DevBuf<double> d_nba;
+        DevBuf<double>& d_nba = c->nba_dev;
         d_nba.alloc(H);
         OPSEC_CUDA(cudaMemcpyAsync(d_nba.p, nba.data(), sizeof(double) * H, cudaMemcpyHostToDevice, c->stream));
         c->S.alloc((size_t)nblk * Hb * Hb);
@@ -1103,7 +1109,7 @@ int eigensolve(opsec_gpu* c, int ncells, const opsec_cell* cells, int M) {
                 c->solver, prm, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, Hb, CUDA_R_64F, c->S.p, Hb,
                 CUDA_R_64F, c->W.p, CUDA_R_64F, &dbytes, &hbytes, nblk);
             if (st == CUSOLVER_STATUS_SUCCESS) {
-                DevBuf<unsigned char> dw;
+                DevBuf<unsigned char>& dw = c->syev_ws;
                 dw.alloc(std::max<size_t>(dbytes, 1));
                 std::vector<unsigned char> hw(std::max<size_t>(hbytes, 1));
                 st = cusolverDnXsyevBatched(c->solver, prm, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, Hb,
@@ -1349,7 +1355,7 @@ void project_azimuthal(opsec_gpu* c, int ncells, int M) {
     if (!c->blas) blas_check(cublasCreate(&c->blas), "cublasCreate");
     blas_check(cublasSetStream(c->blas, c->stream), "cublasSetStream");
     std::vector<double> nba(c->nbar_arc);
-    DevBuf<double> d_nba;
+    DevBuf<double>& d_nba = c->nba_dev;
     d_nba.alloc(nba.size());
     OPSEC_CUDA(cudaMemcpyAsync(d_nba.p, nba.data(), sizeof(double) * nba.size(), cudaMemcpyHostToDevice, c->stream));
     const size_t Kp = (size_t)M * (M + 1) / 2;
@@ -1514,6 +1520,7 @@ int opsec_gpu_create(opsec_gpu** out, const char* cfg_text) {
         OPSEC_CUDA(cudaGetDevice(&dev));
         c->device = dev;
         configure(c, parse_config(cfg_text));
+        c->cfg_text = cfg_text ? cfg_text : "";
         OPSEC_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     });
     *out = c;  // returned even on error so that opsec_gpu_last_error can report it
@@ -1704,6 +1711,117 @@ int opsec_gpu_fisher_build(opsec_gpu* c, int ncells, const opsec_cell* cells, co
         fisher_and_epilogue(c, n, c->Dp.p, nullptr, mixing, phat, pcov, F, W, M, q, f);
         t.mark();
         t.finish();
+    });
+}
+
+// ---------------------------------------------------------------- batched mocks
+namespace {
+// One mock on a worker context whose xi tables are already built: the survey
+// grid is replaced, every geometry-dependent stage is recomputed.
+void run_mock(opsec_gpu* w, const opsec_mock& m, size_t i, int nb, double* F, double* phat, double* pcov) {
+    if (m.nr <= 0 || m.nmu <= 0 || m.nphi <= 0 || (long long)m.nr * m.nmu * m.nphi != m.ncells || !m.cells ||
+        !m.counts || !(m.rmin >= 0) || !(m.rmax > m.rmin))
+        fail(OPSEC_ERR_ARG, "mock " + std::to_string(i) + ": invalid grid, cells or counts");
+    Geometry& g = w->geo;
+    g.coordsys = 2;
+    g.b[0] = m.rmin;
+    g.b[1] = m.rmax;
+    g.b[2] = -1.0;
+    g.b[3] = 1.0;
+    g.b[4] = 0.0;
+    g.b[5] = 2 * M_PI;
+    g.n[0] = m.nr;
+    g.n[1] = m.nmu;
+    g.n[2] = m.nphi;
+    g.L = 0.0;
+    w->q_ok = w->qsq_ok = false;
+    build_tables(w);  // no-op: the tables do not depend on the grid
+    build_q(w);
+    const int n = eigensolve(w, m.ncells, m.cells, m.nmodes);
+    project_all(w, m.ncells, n, true);
+    w->counts.alloc(m.ncells);
+    w->y.alloc(n);
+    OPSEC_CUDA(cudaMemcpyAsync(w->counts.p, m.counts, sizeof(double) * m.ncells, cudaMemcpyHostToDevice, w->stream));
+    launch_dot(m.ncells, n, w->modes.p, w->counts.p, w->nbar.p, w->y.p, w->stream, &w->launches);
+    const size_t n2 = (size_t)nb * nb;
+    fisher_and_epilogue(w, n, w->Dp.p, nullptr, OPSEC_MIXING_INVERSE, phat ? phat + i * nb : nullptr,
+                        pcov ? pcov + i * n2 : nullptr, F ? F + i * n2 : nullptr, nullptr, nullptr, nullptr, nullptr);
+}
+}  // namespace
+
+int opsec_gpu_batch_fisher(opsec_gpu* c, int nmocks, const opsec_mock* mocks, int workers, double* F, double* phat,
+                           double* pcov, double* stats) {
+    return guard(c, [&] {
+        if (nmocks <= 0 || !mocks) fail(OPSEC_ERR_ARG, "no mocks");
+        if (workers > 16) fail(OPSEC_ERR_ARG, "at most 16 workers");
+        const int nb = c->ntab() - 1;
+        const int maxw = workers > 0 ? workers : 8;
+        // worker contexts: the template's configuration and P(k), tables built once each
+        std::vector<opsec_gpu*> ctx(maxw, nullptr);
+        struct Cleanup {
+            std::vector<opsec_gpu*>& v;
+            ~Cleanup() {
+                for (auto* w : v) opsec_gpu_destroy(w);
+            }
+        } cleanup{ctx};
+        for (int k = 0; k < maxw; k++) {
+            if (opsec_gpu_create(&ctx[k], c->cfg_text.c_str()) != OPSEC_OK)
+                fail(OPSEC_ERR_CONFIG, std::string("worker context: ") + opsec_gpu_last_error(ctx[k]));
+            ctx[k]->pk_k = c->pk_k;
+            ctx[k]->pk_P = c->pk_P;
+            ctx[k]->surr_on = false;
+            build_tables(ctx[k]);
+        }
+        std::atomic<int> next{0};
+        std::atomic<int> err_code{OPSEC_OK};
+        std::string err_msg;
+        std::mutex err_mu;
+        auto run_range = [&](int nw, int end) {
+            std::vector<std::thread> th;
+            for (int k = 0; k < nw; k++)
+                th.emplace_back([&, k] {
+                    cudaSetDevice(c->device);
+                    int i;
+                    while (err_code.load() == OPSEC_OK && (i = next.fetch_add(1)) < end) {
+                        try {
+                            run_mock(ctx[k], mocks[i], (size_t)i, nb, F, phat, pcov);
+                        } catch (const Error& e) {
+                            std::lock_guard<std::mutex> lk(err_mu);
+                            if (err_code.load() == OPSEC_OK) {
+                                err_msg = e.msg;
+                                err_code = e.code;
+                            }
+                        }
+                    }
+                });
+            for (auto& t : th) t.join();
+            if (next.load() > end) next = end;
+        };
+        auto now = [] { return std::chrono::steady_clock::now(); };
+        const auto t0 = now();
+        int best = maxw;
+        if (workers <= 0) {
+            // autotune the concurrency on the first mocks: 1, 2, 4, 8 workers, 2 per worker each
+            const int cand[4] = {1, 2, 4, 8};
+            double best_rate = 0;
+            for (int ci = 0; ci < 4 && next.load() < nmocks; ci++) {
+                const int start = next.load(), end = std::min(nmocks, start + 2 * cand[ci]);
+                const auto ta = now();
+                run_range(cand[ci], end);
+                const double rate = (end - start) / std::chrono::duration<double>(now() - ta).count();
+                if (stats) stats[2 + ci] = rate;
+                if (rate > best_rate) {
+                    best_rate = rate;
+                    best = cand[ci];
+                }
+            }
+        }
+        run_range(best, nmocks);
+        if (err_code.load() != OPSEC_OK) fail(err_code.load(), err_msg);
+        if (stats) {
+            stats[0] = std::chrono::duration<double>(now() - t0).count();
+            stats[1] = best;
+        }
     });
 }
 

@@ -237,3 +237,24 @@ def grf_counts(survey: Survey, cells, seed_field: int = 1, seed_poisson: int = 2
     delta = field[idx[:, 0], idx[:, 1], idx[:, 2]]
     lam = np.clip(cells["Nbar"] * (1.0 + delta), 0.0, None)
     return np.random.default_rng(seed_poisson).poisson(lam).astype(np.float64)
+
+
+def mock_batch(n: int, seed: int = 5, nmu: int = 16, nphi: int = 16, ncells_range=(2000, 20000)):
+    """Independent full-sky shells with their own Gaussian radial selections:
+    N_s ~ U[ncells_range], centre ~ U[300, 900], width ~ U[100, 300] (Mpc/h);
+    grid nr x nmu x nphi with nr = N_s / (nmu nphi) (at least 8), r in
+    [max(20, centre - 2 width), centre + 2 width]; counts are Poisson draws of
+    Nbar; nmodes = Ncells / 4.  Returns a list of dicts for Engine.batch_fisher."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        ns = rng.uniform(*ncells_range)
+        rc = rng.uniform(300.0, 900.0)
+        width = rng.uniform(100.0, 300.0)
+        nr = max(8, int(round(ns / (nmu * nphi))))
+        rmin, rmax = max(20.0, rc - 2 * width), rc + 2 * width
+        sv, cells = shell_survey(nr, nmu, nphi, rmin=rmin, rmax=rmax, rc=rc, width=width, nquad=8)
+        counts = rng.poisson(cells["Nbar"]).astype(np.float64)
+        out.append({"survey": sv, "rmin": rmin, "rmax": rmax, "nr": nr, "nmu": nmu, "nphi": nphi, "cells": cells,
+                    "counts": counts, "nmodes": cells.size // 4, "centre": rc, "width": width})
+    return out
