@@ -73,6 +73,38 @@ def workload(name):
     raise SystemExit(f"unknown workload {name}")
 
 
+def bench_mocks(args):
+    """256 independent full-sky surveys (2,000-20,000 cells, own Gaussian shells, 20 bands):
+    mocks per second one after the other (workers = 1) and with the autotuned worker count."""
+    from opsec_gpu import api, synth
+
+    t0 = time.perf_counter()
+    mocks = synth.mock_batch(256, seed=5)
+    gen_s = time.perf_counter() - t0
+    bands = synth.band_edges(20, 0.0, 0.2)
+    k, P = synth.pk_table()
+    e = api.Engine(api.make_config(mocks[0]["survey"], bands=bands))
+    e.set_pk(k, P)
+    e.batch_fisher(mocks[:8], workers=4)  # warm-up: libraries, kernels, allocator
+    seq = e.batch_fisher(mocks, workers=1)
+    auto = e.batch_fisher(mocks, workers=0)
+    e.close()
+    dF = max(float(np.max(np.abs(auto["F"][i] - seq["F"][i]) / np.max(np.abs(seq["F"][i])))) for i in range(256))
+    rate = 256 / auto["seconds"]
+    line = {"metric": "batched mocks: Fisher builds per second", "value": rate, "unit": "mocks/s", "n_gpus": 1,
+            "steps": 1, "warmup": 1, "ms_per_step": auto["seconds"] * 1000, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+            "config": {"workload": "c5", "mocks": 256, "cells": "U[2000, 20000]", "bands": 20,
+                       "modes": "Ncells / 4", "grid": "nr x 16 x 16 full-sky shells",
+                       "selection": "Gaussian shell, centre U[300, 900], width U[100, 300]"},
+            "sequential_mocks_per_s": 256 / seq["seconds"], "workers": auto["workers"],
+            "autotune_mocks_per_s": auto["autotune_mocks_per_s"], "max_fisher_diff_batched_vs_sequential": dF,
+            "mock_generation_s": gen_s,
+            "e2e": {"value": rate, "unit": "mocks/s", "h2d_bytes_per_step": int(sum(m["cells"].nbytes + m["counts"].nbytes for m in mocks)),
+                    "d2h_bytes_per_step": int(256 * 8 * (2 * 20 * 20 + 20))}}
+    print(json.dumps(line), flush=True)
+
+
 def q_table_gb(w):
     """FP64 Q table bytes of a workload: tables x symmetry keys."""
     sv = w["survey"]
@@ -299,6 +331,11 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
 
+    if args.workload == "c5":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the batched-mock workload has no reference CPU arm"}))
+            return
+        return bench_mocks(args)
     w = workload(args.workload)
     if args.impl == "reference":
         if rank != 0:
