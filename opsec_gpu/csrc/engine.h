@@ -242,7 +242,8 @@ void launch_epilogue(int nb, int mixing, const double* Fqf, double* out, int* st
                      long long* launches);
 
 // y_i = sum_a B_ia (N_a - Nbar_a) / sqrt(Nbar_a)
-void launch_dot(int ncells, int nmodes, const double* modes, const double* counts, const double* nbar, double* y,
+// y = B^T x with x = (N - Nbar) / sqrt(Nbar) formed in place of `counts`
+void launch_dot(int ncells, int nmodes, const double* modes, double* counts, const double* nbar, double* y,
                 cudaStream_t s, long long* launches);
 
 // B'[i][a] = sqrt(Nbar_a) B[i][a]

@@ -142,6 +142,12 @@ __global__ void azimuthal_scatter_kernel(int M, const int* mode_m, const int* mo
 // expanded to the full arc grid: u(h_x) = U_b[x][idx] / sqrt(npar), u(P h_x) = +-u(h_x) (even / odd)
 __global__ void assemble_modes_kernel(int H, int Nphi, int Nmu, int npar, int nmodes, const int* sel_b,
                                       const int* sel_idx, const int* sel_kind, const double* U, double* modes) {
+    extern __shared__ double trig[];  // cos, sin of 2 pi j / Nphi, j < Nphi
+    for (int j = threadIdx.x; j < Nphi; j += blockDim.x) {
+        trig[2 * j] = cospi(2.0 * j / Nphi);
+        trig[2 * j + 1] = sinpi(2.0 * j / Nphi);
+    }
+    __syncthreads();
     const long long N = (long long)H * Nphi;
     const long long total = (long long)nmodes * N;
     const int Hb = H / npar, half = Nmu / npar;
@@ -164,8 +170,8 @@ __global__ void assemble_modes_kernel(int H, int Nphi, int Nmu, int npar, int nm
         double t;
         switch (sel_kind[i]) {
         case 0: t = c0; break;
-        case 1: t = c1 * cospi(2.0 * mf / Nphi); break;
-        case 2: t = c1 * sinpi(2.0 * mf / Nphi); break;
+        case 1: t = c1 * trig[2 * mf]; break;
+        case 2: t = c1 * trig[2 * mf + 1]; break;
         default: t = (f & 1) ? -c0 : c0; break;
         }
         modes[e] = u * t;
@@ -181,13 +187,18 @@ __global__ void scale_modes_kernel(int ncells, int nmodes, const double* modes, 
 }
 
 // one warp per mode: y_i = sum_a B_ia (N_a - Nbar_a)/sqrt(Nbar_a)  (dot.cpp:131-152)
-__global__ void dot_kernel(int ncells, int nmodes, const double* modes, const double* counts, const double* nbar,
-                           double* y) {
+// x_a = (N_a - Nbar_a) / sqrt(Nbar_a), in place of the counts (dot.cpp:120-152)
+__global__ void pixel_values_kernel(int ncells, double* counts, const double* nbar) {
+    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < ncells; a += gridDim.x * blockDim.x)
+        counts[a] = (counts[a] - nbar[a]) / sqrt(nbar[a]);
+}
+
+__global__ void dot_kernel(int ncells, int nmodes, const double* modes, const double* x, double* y) {
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (warp >= nmodes) return;
     const double* b = modes + (size_t)warp * ncells;
     double acc = 0.0;
-    for (int a = lane; a < ncells; a += 32) acc += b[a] * ((counts[a] - nbar[a]) / sqrt(nbar[a]));
+    for (int a = lane; a < ncells; a += 32) acc = fma(b[a], x[a], acc);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     if (lane == 0) y[warp] = acc;
@@ -304,8 +315,10 @@ void launch_azimuthal_scatter(int M, int nbands, const int* mode_m, const int* m
 
 void launch_assemble_modes(int H, int Nphi, int Nmu, int npar, int nmodes, const int* sel_b, const int* sel_idx,
                            const int* sel_kind, const double* U, double* modes, cudaStream_t st, long long* l) {
-    assemble_modes_kernel<<<grid_for((long long)nmodes * H * Nphi), 256, 0, st>>>(H, Nphi, Nmu, npar, nmodes, sel_b,
-                                                                                 sel_idx, sel_kind, U, modes);
+    const size_t smem = sizeof(double) * 2 * Nphi;
+    if (smem > 48 * 1024) fail(OPSEC_ERR_CONFIG, "too many phi cells for the mode assembly");
+    assemble_modes_kernel<<<grid_for((long long)nmodes * H * Nphi), 256, smem, st>>>(H, Nphi, Nmu, npar, nmodes,
+                                                                                    sel_b, sel_idx, sel_kind, U, modes);
     OPSEC_CUDA(cudaGetLastError());
     ++*l;
 }
@@ -317,11 +330,12 @@ void launch_scale_modes(int ncells, int nmodes, const double* modes, const doubl
     ++*l;
 }
 
-void launch_dot(int ncells, int nmodes, const double* modes, const double* counts, const double* nbar, double* y,
+void launch_dot(int ncells, int nmodes, const double* modes, double* counts, const double* nbar, double* y,
                 cudaStream_t s, long long* l) {
-    dot_kernel<<<(nmodes * 32 + 255) / 256, 256, 0, s>>>(ncells, nmodes, modes, counts, nbar, y);
+    pixel_values_kernel<<<grid_for(ncells), 256, 0, s>>>(ncells, counts, nbar);
+    dot_kernel<<<(nmodes * 32 + 255) / 256, 256, 0, s>>>(ncells, nmodes, modes, counts, y);
     OPSEC_CUDA(cudaGetLastError());
-    ++*l;
+    *l += 2;
 }
 
 void launch_reverse_modes(int n, int m, int lda, const double* A, const double* w, double* modes, double* evals,
