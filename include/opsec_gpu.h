@@ -135,7 +135,7 @@ long long opsec_gpu_launch_count(const opsec_gpu* ctx);
  * (12 geometry/band inputs -> 3 x 128 GELU -> 1, BF16 products, FP32
  * accumulation) predicts the integrals of key pairs at least `surrogate.far`
  * (default 2) cell widths apart on spherical grids; a key whose members
- * disagree by more than `surrogate.tol` (default 1e-3, in units of the
+ * disagree by more than `surrogate.tol` (default 0.02, in units of the
  * table's largest magnitude within 25 % of the pair's centre separation)
  * and every nearer key are integrated by the cubature.  Enabled by
  * the configuration key `surrogate = 1` once weights are present. */

@@ -314,7 +314,7 @@ struct opsec_gpu {
     // learned far-field surrogate: 4 networks (FP32 master weights) and the target scale
     static constexpr int kMembers = 4;
     bool surr_on = false;
-    float surr_tol = 1e-3f, surr_far = 2.0f;
+    float surr_tol = 0.02f, surr_far = 2.0f;
     std::vector<float> surr_w;  // kMembers * kSurrParams, empty until trained or loaded
     float surr_ysc = 0.f;
     long long surr_counts[3] = {0, 0, 0};  // keys predicted, sent back to the cubature, far keys

@@ -98,7 +98,7 @@ def test_surrogate_gain_and_fallback():
     """An ensemble trained on half of a shell's far (key, table) samples, applied
     to all of its far keys.  Accepting every prediction must beat the method
     without the network (zero networks: the point value xi_t(d) for every far
-    key) by 5x in the Fisher matrix; with the default tolerance the members'
+    key) by 5x in the Fisher matrix; with a tolerance of 1e-3 the members'
     disagreement sends keys back to the cubature and the Fisher matrix stays
     within 1e-3 of the plain build."""
     bands = synth.band_edges(20, 0.0, 0.2)
@@ -115,7 +115,7 @@ def test_surrogate_gain_and_fallback():
     zero = np.zeros_like(w)
     zero[-1] = w[-1]
     point, st0 = fisher(sv, cells, counts, bands, M, ["surrogate = 1", "surrogate.tol = 1e9"], zero)
-    guarded, stg = fisher(sv, cells, counts, bands, M, ["surrogate = 1"], w)
+    guarded, stg = fisher(sv, cells, counts, bands, M, ["surrogate = 1", "surrogate.tol = 1e-3"], w)
     sc = np.max(np.abs(plain["F"]))
     err = {name: np.max(np.abs(r["F"] - plain["F"])) / sc for name, r in
            (("network", all_in), ("point value", point), ("network, tol 1e-3", guarded))}
