@@ -51,6 +51,20 @@ void KernelClock::end(cudaStream_t s) {
     OPSEC_CUDA(cudaEventRecord(pending.back().b, s));
 }
 
+int max_dynamic_smem() {
+    static std::atomic<int> cache[64];
+    int dev = 0;
+    cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+    if (dev < 0 || dev >= 64) fail(OPSEC_ERR_CUDA, "device index out of range");
+    int v = cache[dev].load();
+    if (v <= 0) {
+        cuda_check(cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev),
+                   "cudaDeviceGetAttribute(MaxSharedMemoryPerBlockOptin)");
+        cache[dev] = v;
+    }
+    return v;
+}
+
 void cuda_check(cudaError_t e, const char* what) {
     if (e != cudaSuccess) {
         if (e == cudaErrorMemoryAllocation) fail(OPSEC_ERR_NOMEM, std::string(what) + ": out of device memory");
