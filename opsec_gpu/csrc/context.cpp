@@ -51,7 +51,7 @@ void KernelClock::end(cudaStream_t s) {
     OPSEC_CUDA(cudaEventRecord(pending.back().b, s));
 }
 
-int max_dynamic_smem() {
+int max_dynamic_smem(const void* func) {
     static std::atomic<int> cache[64];
     int dev = 0;
     cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
@@ -62,7 +62,10 @@ int max_dynamic_smem() {
                    "cudaDeviceGetAttribute(MaxSharedMemoryPerBlockOptin)");
         cache[dev] = v;
     }
-    return v;
+    // The opt-in ceiling covers static plus dynamic shared memory of one block.
+    cudaFuncAttributes fa;
+    cuda_check(cudaFuncGetAttributes(&fa, func), "cudaFuncGetAttributes");
+    return v - (int)fa.sharedSizeBytes;
 }
 
 void cuda_check(cudaError_t e, const char* what) {

@@ -679,7 +679,7 @@ void run(const CubatureArgs& a, int tab0, int ngrp, const Lookup& lk, cudaStream
     constexpr int NP = Shape<NG>::NP;
     const size_t smem = smem_points<NG, EXACT>() + sizeof(float) * (size_t)ngrp * a.xl.n();
     auto k = cubature_kernel<NG, G, EXACT>;
-    OPSEC_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem()));
+    OPSEC_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem((const void*)k)));
     int dev = 0, nsm = 0, occ = 0;
     OPSEC_CUDA(cudaGetDevice(&dev));
     OPSEC_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
@@ -810,7 +810,7 @@ bool run_window(const CubatureArgs& a, const Lookup& lk, cudaStream_t s, long lo
     // far keys
     const size_t smem = far_smem<NG>(w, a.ntab);
     auto k = cubature_far_kernel<NG>;
-    OPSEC_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem()));
+    OPSEC_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem((const void*)k)));
     int dev = 0, nsm = 0, occ = 0;
     OPSEC_CUDA(cudaGetDevice(&dev));
     OPSEC_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));

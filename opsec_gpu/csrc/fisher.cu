@@ -335,7 +335,7 @@ static void run_fisher(const FisherArgs& a, const T* Dp, cudaStream_t s, long lo
     if (nout > kThreads * kMaxOut) fail(OPSEC_ERR_ARG, "too many bands for the Fisher kernel (max 88)");
     const size_t smem = sizeof(float) * (size_t)(nb + 2) * kChunk;
     auto k = fisher_kernel<T>;
-    OPSEC_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem()));
+    OPSEC_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem((const void*)k)));
     const double K = (double)a.nmodes * (a.nmodes + 1) / 2;
     if (g_clock) g_clock->begin("fisher", s, 2.0 * K * nout, K * nb * sizeof(T));
     k<<<a.nblocks, kThreads, smem, s>>>(a.nmodes, nb, Dp, a.evals, a.y, a.prior, a.partial);
@@ -355,7 +355,7 @@ void launch_fisher64(const FisherArgs& a, const double* Dp64, cudaStream_t s, lo
 void launch_epilogue(int nb, int mixing, const double* Fqf, double* out, int* status, cudaStream_t s,
                      long long* launches) {
     const size_t smem = sizeof(double) * (5 * (size_t)nb * nb + nb);
-    OPSEC_CUDA(cudaFuncSetAttribute(epilogue_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem()));
+    OPSEC_CUDA(cudaFuncSetAttribute(epilogue_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem((const void*)epilogue_kernel)));
     epilogue_kernel<<<1, 256, smem, s>>>(nb, mixing, Fqf, out, status);
     OPSEC_CUDA(cudaGetLastError());
     ++*launches;

@@ -251,7 +251,7 @@ void launch_azimuthal_blocks_t(const KeySpace& ks, const double* Q, const double
     if (!ks.fold) fail(OPSEC_ERR_CONFIG, "azimuthal blocks need a full-sky grid");
     const size_t smem = sizeof(double) * (size_t)nm * ks.nf;
     if (smem > 200 * 1024) fail(OPSEC_ERR_CONFIG, "too many phi cells for the azimuthal block transform");
-    OPSEC_CUDA(cudaFuncSetAttribute(azimuthal_blocks_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem()));
+    OPSEC_CUDA(cudaFuncSetAttribute(azimuthal_blocks_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem((const void*)azimuthal_blocks_kernel<T>)));
     const long long HH = (long long)(ks.H / npar) * (ks.H / npar);
     const int gy = nm < 8 ? nm : 8;
     long long gx = (HH + 255) / 256;

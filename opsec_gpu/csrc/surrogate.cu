@@ -529,7 +529,7 @@ void launch_surr_infer(long long nsamp, const long long* keys, int ntab, const f
     long long grid = std::min<long long>((tiles + 7) / 8, (long long)nsm * 4);
     if (grid < 1) grid = 1;
     const size_t smem = sizeof(__nv_bfloat16) * kSurrHid * (kW1S + 2 * kW23S) + sizeof(float) * (4 * kSurrHid + 1);
-    OPSEC_CUDA(cudaFuncSetAttribute(surr_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem()));
+    OPSEC_CUDA(cudaFuncSetAttribute(surr_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem((const void*)surr_infer_kernel)));
     surr_infer_kernel<<<(unsigned)grid, 256, smem, s>>>(nsamp, keys, ntab, kg, tinfo, feat, w, out);
     OPSEC_CUDA(cudaGetLastError());
     ++*l;
