@@ -8,8 +8,11 @@
 //   q_p  = sum_k m w_i w_j D_p[k] y_i y_j
 // One pass over the packed triangle reads every D_p[k] once: a CTA stages a
 // chunk of k for all bands in shared memory as h_p[k] = sqrt(m w_i w_j) D_p[k]
-// (plus the rows R and y_i y_j), each thread owns a few (p,q) outputs, FP32
-// products summed over the chunk and FP64 across chunks.  Per-CTA partials
+// (plus the rows R and y_i y_j); the outputs are the upper triangle of the
+// Gram matrix of those rows, and each thread owns a 4 x 4 tile of it over a
+// slice of the chunk (8 shared loads per 16 FMAs, rows padded to 129 floats so
+// that the rows read by one warp sit in different banks).  FP32 products are
+// summed over the slice and FP64 across chunks; slices and per-CTA partials
 // are reduced in a fixed order, so reruns are bit-identical.
 #include <cmath>
 
@@ -18,12 +21,37 @@
 namespace opsec {
 namespace {
 
-constexpr int kThreads = 512;
 constexpr int kChunk = 128;
-constexpr int kMaxOut = 8;  // outputs per thread: nb(nb+1)/2 + 2nb <= 4096
+constexpr int kStride = kChunk + 1;  // padded row: rows a multiple of 32 floats apart fall in different banks
+constexpr int kTile = 4;             // each thread owns a 4 x 4 tile of the Gram matrix of the staged rows
+constexpr int kMaxThreads = 512;
+constexpr int kMaxBands = 88;
+
+// Staged rows: h_0..h_{nb-1}, then R sc and y_i y_j sc, zero rows up to a
+// multiple of 4.  Tiles (I <= J) of 4 rows x 4 rows; the chunk's k range is cut
+// into `slices` parts so that ntiles x slices threads share the work.
+struct FisherTiling {
+    int rows, nt, ntiles, slices, threads;
+    size_t smem;
+};
+
+__host__ __device__ inline FisherTiling fisher_tiling(int nb) {
+    FisherTiling t;
+    t.nt = (nb + 2 + kTile - 1) / kTile;
+    t.rows = t.nt * kTile;
+    t.ntiles = t.nt * (t.nt + 1) / 2;
+    t.slices = 1;
+    while (t.slices < 32 && t.ntiles * t.slices * 2 <= kMaxThreads) t.slices *= 2;
+    t.threads = (t.ntiles * t.slices + 31) / 32 * 32;
+    if (t.threads < kChunk) t.threads = kChunk;
+    const size_t stage = sizeof(float) * (size_t)t.rows * kStride;
+    const size_t red = sizeof(double) * (size_t)t.ntiles * t.slices * kTile * kTile;
+    t.smem = stage > red ? stage : red;
+    return t;
+}
 
 __device__ __forceinline__ void unpack(long long k, int* i, int* j) {
-    long long jj = (long long)((sqrt(8.0 * (double)k + 1.0) - 1.0) * 0.5);
+    long long jj = (long long)((sqrtf((float)(8 * k + 1)) - 1.0f) * 0.5f);
     while (jj * (jj + 1) / 2 > k) --jj;
     while ((jj + 1) * (jj + 2) / 2 <= k) ++jj;
     *j = (int)jj;
@@ -50,65 +78,118 @@ __device__ __forceinline__ void out_pair(int o, int nb, int* p, int* q) {
     }
 }
 
+// (row, col) of the staged Gram matrix -> output index, or -1
+__device__ __forceinline__ int out_index(int row, int col, int nb) {
+    if (row > col || row >= nb) return -1;
+    const int nF = nb * (nb + 1) / 2;
+    if (col < nb) return row * nb - row * (row - 1) / 2 + (col - row);
+    if (col == nb) return nF + row;
+    if (col == nb + 1) return nF + nb + row;
+    return -1;
+}
+
 template <class T>
-__global__ void __launch_bounds__(kThreads) fisher_kernel(int M, int nb, const T* Dp, const double* evals,
-                                                          const double* y, const double* prior, double* partial) {
-    extern __shared__ float hs[];  // [nb+2][kChunk]
+__global__ void __launch_bounds__(kMaxThreads) fisher_kernel(int M, int nb, const T* Dp, const double* evals,
+                                                             const double* y, const double* prior, double* partial) {
+    extern __shared__ __align__(16) unsigned char fisher_smem[];
+    float* hs = reinterpret_cast<float*>(fisher_smem);  // [rows][kStride]
+    const FisherTiling tl = fisher_tiling(nb);
     const long long K = (long long)M * (M + 1) / 2;
     const int nout = nb * (nb + 1) / 2 + 2 * nb;
-    int op[kMaxOut], oq[kMaxOut];
-    double acc[kMaxOut];
-#pragma unroll
-    for (int s = 0; s < kMaxOut; s++) {
-        int o = threadIdx.x + s * kThreads;
-        op[s] = oq[s] = -1;
-        acc[s] = 0.0;
-        if (o < nout) out_pair(o, nb, &op[s], &oq[s]);
+
+    // this thread's tile (I <= J) and k slice
+    const int me = threadIdx.x;
+    const bool worker = me < tl.ntiles * tl.slices;
+    const int tile = worker ? me % tl.ntiles : 0;
+    const int slice = worker ? me / tl.ntiles : 0;
+    int I = 0, rem = tile;
+    while (rem >= tl.nt - I) {
+        rem -= tl.nt - I;
+        ++I;
     }
+    const int J = I + rem;
+    const int per = kChunk / tl.slices;
+    const float* ra = hs + (size_t)(I * kTile) * kStride + slice * per;
+    const float* rb = hs + (size_t)(J * kTile) * kStride + slice * per;
+    double acc[kTile][kTile];
+#pragma unroll
+    for (int a = 0; a < kTile; a++)
+#pragma unroll
+        for (int b = 0; b < kTile; b++) acc[a][b] = 0.0;
+
+    for (int e = me; e < (tl.rows - nb - 2) * kStride; e += blockDim.x) hs[(size_t)(nb + 2) * kStride + e] = 0.f;
+
     for (long long k0 = (long long)blockIdx.x * kChunk; k0 < K; k0 += (long long)gridDim.x * kChunk) {
         // stage raw D_p[k]
-        for (int e = threadIdx.x; e < nb * kChunk; e += kThreads) {
-            int p = e / kChunk, kk = e % kChunk;
-            long long k = k0 + kk;
-            hs[p * kChunk + kk] = (k < K) ? (float)Dp[(size_t)p * K + k] : 0.f;
+        for (int e = me; e < nb * kChunk; e += blockDim.x) {
+            const int p = e / kChunk, kk = e % kChunk;
+            const long long k = k0 + kk;
+            hs[p * kStride + kk] = (k < K) ? (float)Dp[(size_t)p * K + k] : 0.f;
         }
         __syncthreads();
-        // per-k weights, residual row, data row
-        for (int kk = threadIdx.x; kk < kChunk; kk += kThreads) {
-            long long k = k0 + kk;
+        // per-k weights sqrt(m w_i w_j), residual row R (FP64: its diagonal is 1 + lambda_i
+        // less a sum close to lambda_i), data row y_i y_j
+        for (int kk = me; kk < kChunk; kk += blockDim.x) {
+            const long long k = k0 + kk;
             float sc = 0.f, R = 0.f, yy = 0.f;
             if (k < K) {
                 int i, j;
                 unpack(k, &i, &j);
-                double wi = 1.0 / (1.0 + evals[i]), wj = 1.0 / (1.0 + evals[j]);
-                double c = (i == j ? 0.5 : 1.0) * wi * wj;
-                sc = (float)sqrt(c);
+                const float wi = 1.0f / (1.0f + (float)evals[i]), wj = 1.0f / (1.0f + (float)evals[j]);
+                sc = sqrtf((i == j ? 0.5f : 1.0f) * wi * wj);
                 double r = (i == j) ? 1.0 + evals[i] : 0.0;
-                for (int n = 0; n < nb; n++) r -= prior[n] * (double)hs[n * kChunk + kk];
+                for (int n = 0; n < nb; n++) r -= prior[n] * (double)hs[n * kStride + kk];
                 R = (float)r;
                 yy = (float)(y[i] * y[j]);
             }
-            for (int p = 0; p < nb; p++) hs[p * kChunk + kk] *= sc;
-            hs[nb * kChunk + kk] = R * sc;
-            hs[(nb + 1) * kChunk + kk] = yy * sc;
+            for (int p = 0; p < nb; p++) hs[p * kStride + kk] *= sc;
+            hs[nb * kStride + kk] = R * sc;
+            hs[(nb + 1) * kStride + kk] = yy * sc;
         }
         __syncthreads();
+        if (worker) {
+            float part[kTile][kTile];
 #pragma unroll
-        for (int s = 0; s < kMaxOut; s++) {
-            if (op[s] < 0) continue;
-            const float* a = hs + op[s] * kChunk;
-            const float* b = hs + oq[s] * kChunk;
-            float part = 0.f;
-#pragma unroll 8
-            for (int kk = 0; kk < kChunk; kk++) part = fmaf(a[kk], b[kk], part);
-            acc[s] += (double)part;
+            for (int a = 0; a < kTile; a++)
+#pragma unroll
+                for (int b = 0; b < kTile; b++) part[a][b] = 0.f;
+#pragma unroll 4
+            for (int kk = 0; kk < per; kk++) {
+                float va[kTile], vb[kTile];
+#pragma unroll
+                for (int a = 0; a < kTile; a++) {
+                    va[a] = ra[a * kStride + kk];
+                    vb[a] = rb[a * kStride + kk];
+                }
+#pragma unroll
+                for (int a = 0; a < kTile; a++)
+#pragma unroll
+                    for (int b = 0; b < kTile; b++) part[a][b] = fmaf(va[a], vb[b], part[a][b]);
+            }
+#pragma unroll
+            for (int a = 0; a < kTile; a++)
+#pragma unroll
+                for (int b = 0; b < kTile; b++) acc[a][b] += (double)part[a][b];
         }
         __syncthreads();
     }
+
+    // slices of one tile summed in a fixed order, then one write per output
+    double* red = reinterpret_cast<double*>(fisher_smem);  // [ntiles * slices][16]
+    if (worker)
 #pragma unroll
-    for (int s = 0; s < kMaxOut; s++) {
-        int o = threadIdx.x + s * kThreads;
-        if (o < nout) partial[(size_t)blockIdx.x * nout + o] = acc[s];
+        for (int a = 0; a < kTile; a++)
+#pragma unroll
+            for (int b = 0; b < kTile; b++) red[(size_t)me * kTile * kTile + a * kTile + b] = acc[a][b];
+    __syncthreads();
+    if (me < tl.ntiles) {
+        for (int e = 0; e < kTile * kTile; e++) {
+            const int o = out_index(I * kTile + e / kTile, J * kTile + e % kTile, nb);
+            if (o < 0) continue;
+            double sum = 0.0;
+            for (int sl = 0; sl < tl.slices; sl++) sum += red[(size_t)(sl * tl.ntiles + me) * kTile * kTile + e];
+            partial[(size_t)blockIdx.x * nout + o] = sum;
+        }
     }
 }
 
@@ -332,13 +413,13 @@ template <class T>
 static void run_fisher(const FisherArgs& a, const T* Dp, cudaStream_t s, long long* launches) {
     const int nb = a.nbands;
     const int nout = nb * (nb + 1) / 2 + 2 * nb;
-    if (nout > kThreads * kMaxOut) fail(OPSEC_ERR_ARG, "too many bands for the Fisher kernel (max 88)");
-    const size_t smem = sizeof(float) * (size_t)(nb + 2) * kChunk;
+    if (nb > kMaxBands) fail(OPSEC_ERR_ARG, "too many bands for the Fisher kernel (max 88)");
+    const FisherTiling tl = fisher_tiling(nb);
     auto k = fisher_kernel<T>;
     OPSEC_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem((const void*)k)));
     const double K = (double)a.nmodes * (a.nmodes + 1) / 2;
     if (g_clock) g_clock->begin("fisher", s, 2.0 * K * nout, K * nb * sizeof(T));
-    k<<<a.nblocks, kThreads, smem, s>>>(a.nmodes, nb, Dp, a.evals, a.y, a.prior, a.partial);
+    k<<<a.nblocks, tl.threads, tl.smem, s>>>(a.nmodes, nb, Dp, a.evals, a.y, a.prior, a.partial);
     OPSEC_CUDA(cudaGetLastError());
     if (g_clock) g_clock->end(s);
     fisher_reduce_kernel<<<(nout + 255) / 256, 256, 0, s>>>(nb, a.nblocks, a.partial, a.out);
@@ -405,17 +486,19 @@ extern "C" int opsec_gpu_fisher_noalloc(int nmodes, int nbands, const float* cov
     }
     const int nb = nbands;
     const int nout = nb * (nb + 1) / 2 + 2 * nb;
-    const size_t smem = sizeof(float) * (size_t)(nb + 2) * kChunk;
+    const FisherTiling tl = fisher_tiling(nb);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     if (!g_attr_done[dev]) {
-        if (cudaFuncSetAttribute(fisher_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)(sizeof(float) * (size_t)(kNoallocMaxBands + 2) * kChunk)) != cudaSuccess)
+        size_t most = 0;  // the largest request of any band count this entry point accepts
+        for (int n = 1; n <= kNoallocMaxBands; n++) most = fisher_tiling(n).smem > most ? fisher_tiling(n).smem : most;
+        if (cudaFuncSetAttribute(fisher_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)most) !=
+            cudaSuccess)
             return OPSEC_ERR_CUDA;
         g_attr_done[dev] = true;
     }
     // every CTA writes all nout partials of its slot, so nothing needs clearing
-    fisher_kernel<float><<<kNoallocBlocks, kThreads, smem, s>>>(nmodes, nb, cov_packed, evals, y, prior,
-                                                                g_partial_addr[dev]);
+    fisher_kernel<float><<<kNoallocBlocks, tl.threads, tl.smem, s>>>(nmodes, nb, cov_packed, evals, y, prior,
+                                                                     g_partial_addr[dev]);
     fisher_reduce_kernel<<<(nout + 255) / 256, 256, 0, s>>>(nb, kNoallocBlocks, g_partial_addr[dev], out);
     return cudaGetLastError() == cudaSuccess ? OPSEC_OK : OPSEC_ERR_CUDA;
 }

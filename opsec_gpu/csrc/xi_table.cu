@@ -97,50 +97,114 @@ __global__ void simpson_weights_kernel(XiTableArgs a) {
     }
 }
 
-// One warp per (table, r): sum_j mult_j j0(k_j r), FP64.  Lane l takes
-// j = l, l+32, ...; sin(k_j r) advances by the angle-addition rotation
-// through 32 dk r and is re-anchored with an exact sincos every 32 steps, so
-// each term costs a few FMAs instead of a sine and a division.  Terms with
-// (k_j r)^2 < 1e-4 use the series of sj0 (Model.cpp:56-59).
+constexpr int kRPerWarp = 4;   // r values per warp; each weight load feeds all of them
+constexpr int kAnchor = 32;    // Chebyshev steps per lane between rotation anchors
+
+// One warp per (table, 4 consecutive r): sum_j mult_j j0(k_j r), FP64.
+//
+// Terms with (k_j r)^2 < 1e-4 use the series of sj0 (Model.cpp:56-59); k_j
+// grows with j, so they form a prefix j < jc of the sum, evaluated term by
+// term (series, or sin(x)/x for the few prefix terms past the threshold when
+// the four r values have different jc).  The rest is (1/r) sum_j (mult_j/k_j)
+// sin(k_j r) with lane l taking j = jc + l + 32 m: along one lane the angle
+// advances by theta = 32 dk r and sin(x + (m+1) theta) = 2 cos(theta) sin(x + m
+// theta) - sin(x + (m-1) theta), two FMAs per term with the accumulation.  The
+// recurrence restarts every 32 steps from anchor values (sin, cos) advanced by
+// the angle-addition rotation through 1024 dk r from one sincos per lane, so
+// the error stays within a few hundred ulps of the largest term (the error of
+// the three-term recurrence grows at most quadratically in its length).
 __global__ void xi_sum_kernel(XiTableArgs a) {
     const int n = a.xl.n();
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     const int t = blockIdx.y;
-    if (warp >= n) return;
+    const int i0 = warp * kRPerWarp;
+    if (i0 >= n) return;
     TableSpec s = table_spec(t, a.nbands, a.band_lo, a.band_hi);
     const double dk = (s.kmax - s.kmin) / s.nk;
-    const double r = a.r[warp];
     const double* mult = a.scratch + s.off;
     const double* minv = a.scratch + s.off + scratch_half(a);
-    double acc_series = 0.0, acc_sin = 0.0;
-    if (r == 0.0) {
-        for (int j = lane; j <= s.nk; j += 32) acc_series += mult[j];
-    } else {
-        double sd, cd;
-        sincos(32.0 * dk * r, &sd, &cd);
-        constexpr int kAnchor = 32;
-        for (int j0 = lane; j0 <= s.nk; j0 += 32 * kAnchor) {
-            double sn, cs;
-            sincos((s.kmin + j0 * dk) * r, &sn, &cs);
-            for (int m = 0, j = j0; m < kAnchor && j <= s.nk; m++, j += 32) {
-                const double x = (s.kmin + j * dk) * r;
-                if (x * x < 1e-4)
-                    acc_series += mult[j] * sj0(x);
-                else
-                    acc_sin += minv[j] * sn;
-                const double sn2 = sn * cd + cs * sd;
-                cs = cs * cd - sn * sd;
-                sn = sn2;
+    const int nk = s.nk;
+
+    double r[kRPerWarp], acc_series[kRPerWarp], acc_sin[kRPerWarp];
+    int jc = 0;
+#pragma unroll
+    for (int q = 0; q < kRPerWarp; q++) {
+        r[q] = a.r[min(i0 + q, n - 1)];  // past the end: a copy of the last r, not stored
+        acc_series[q] = 0.0;
+        acc_sin[q] = 0.0;
+        // first j with (kmin + j dk) r >= 0.01, from below; the prefix loop tests each term exactly
+        if (r[q] > 0.0) {
+            const double jf = (0.01 / r[q] - s.kmin) / dk;
+            jc = max(jc, jf < 0.0 ? 0 : (jf > (double)nk ? nk + 1 : (int)jf + 2));
+        } else {
+            // r = 0: every term is mult_j j0(0) = mult_j; sin(k_j r) = 0 below
+            for (int j = lane; j <= nk; j += 32) acc_series[q] += mult[j];
+        }
+    }
+    jc = min(jc, nk + 1);
+
+    // prefix, term by term
+    for (int j = lane; j < jc; j += 32) {
+        const double k = s.kmin + j * dk;
+#pragma unroll
+        for (int q = 0; q < kRPerWarp; q++) {
+            const double x = k * r[q];
+            if (r[q] == 0.0) continue;  // summed above
+            if (x * x < 1e-4)
+                acc_series[q] += mult[j] * sj0(x);
+            else
+                acc_sin[q] += minv[j] * sin(x);
+        }
+    }
+
+    // the rest, by the three-term recurrence
+    if (jc <= nk) {
+        double c2[kRPerWarp], cth[kRPerWarp], sth[kRPerWarp], cT[kRPerWarp], sT[kRPerWarp];
+        double sn[kRPerWarp], cs[kRPerWarp];
+#pragma unroll
+        for (int q = 0; q < kRPerWarp; q++) {
+            sincos(32.0 * dk * r[q], &sth[q], &cth[q]);
+            sincos((32.0 * kAnchor) * dk * r[q], &sT[q], &cT[q]);
+            c2[q] = 2.0 * cth[q];
+            sincos((s.kmin + (jc + lane) * dk) * r[q], &sn[q], &cs[q]);
+        }
+        for (int j0 = jc + lane; j0 <= nk; j0 += 32 * kAnchor) {
+            double cur[kRPerWarp], prev[kRPerWarp];
+#pragma unroll
+            for (int q = 0; q < kRPerWarp; q++) {
+                cur[q] = sn[q];
+                prev[q] = sn[q] * cth[q] - cs[q] * sth[q];  // sin(x - theta)
+            }
+            const int steps = min(kAnchor, (nk - j0) / 32 + 1);
+            for (int m = 0; m < steps; m++) {
+                const double w = minv[j0 + 32 * m];
+#pragma unroll
+                for (int q = 0; q < kRPerWarp; q++) {
+                    acc_sin[q] = fma(w, cur[q], acc_sin[q]);
+                    const double nxt = fma(c2[q], cur[q], -prev[q]);
+                    prev[q] = cur[q];
+                    cur[q] = nxt;
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < kRPerWarp; q++) {
+                const double sn2 = sn[q] * cT[q] + cs[q] * sT[q];
+                cs[q] = cs[q] * cT[q] - sn[q] * sT[q];
+                sn[q] = sn2;
             }
         }
     }
-    double acc = (r > 0.0) ? acc_series + acc_sin / r : acc_series;
+
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (lane == 0) {
-        a.xi64[(size_t)t * n + warp] = acc;
-        a.xi32[(size_t)t * n + warp] = (float)acc;
+    for (int q = 0; q < kRPerWarp; q++) {
+        double acc = (r[q] > 0.0) ? acc_series[q] + acc_sin[q] / r[q] : acc_series[q];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0 && i0 + q < n) {
+            a.xi64[(size_t)t * n + i0 + q] = acc;
+            a.xi32[(size_t)t * n + i0 + q] = (float)acc;
+        }
     }
 }
 
@@ -151,7 +215,8 @@ void launch_xi_tables(const XiTableArgs& a, cudaStream_t s, long long* launches)
     simpson_weights_kernel<<<dim3(64, ntab), 256, 0, s>>>(a);
     OPSEC_CUDA(cudaGetLastError());
     const int n = a.xl.n();
-    xi_sum_kernel<<<dim3((n * 32 + 255) / 256, ntab), 256, 0, s>>>(a);
+    const int warps = (n + kRPerWarp - 1) / kRPerWarp;
+    xi_sum_kernel<<<dim3((warps * 32 + 255) / 256, ntab), 256, 0, s>>>(a);
     OPSEC_CUDA(cudaGetLastError());
     *launches += 2;
 }
