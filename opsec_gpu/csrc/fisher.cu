@@ -26,6 +26,7 @@ constexpr int kStride = kChunk + 1;  // padded row: rows a multiple of 32 floats
 constexpr int kTile = 4;             // each thread owns a 4 x 4 tile of the Gram matrix of the staged rows
 constexpr int kMaxThreads = 512;
 constexpr int kMaxBands = 88;
+constexpr int kFlush = 4;  // chunks summed in FP32 per FP64 update (128 products per slice of 32)
 
 // Staged rows: h_0..h_{nb-1}, then R sc and y_i y_j sc, zero rows up to a
 // multiple of 4.  Tiles (I <= J) of 4 rows x 4 rows; the chunk's k range is cut
@@ -93,7 +94,12 @@ __global__ void __launch_bounds__(kMaxThreads) fisher_kernel(int M, int nb, cons
                                                              const double* y, const double* prior, double* partial) {
     extern __shared__ __align__(16) unsigned char fisher_smem[];
     float* hs = reinterpret_cast<float*>(fisher_smem);  // [rows][kStride]
+    __shared__ float p_hi[kMaxBands], p_lo[kMaxBands];   // prior p_n = p_hi + p_lo
     const FisherTiling tl = fisher_tiling(nb);
+    for (int n = threadIdx.x; n < nb; n += blockDim.x) {
+        p_hi[n] = (float)prior[n];
+        p_lo[n] = (float)(prior[n] - (double)p_hi[n]);
+    }
     const long long K = (long long)M * (M + 1) / 2;
     const int nout = nb * (nb + 1) / 2 + 2 * nb;
 
@@ -112,10 +118,15 @@ __global__ void __launch_bounds__(kMaxThreads) fisher_kernel(int M, int nb, cons
     const float* ra = hs + (size_t)(I * kTile) * kStride + slice * per;
     const float* rb = hs + (size_t)(J * kTile) * kStride + slice * per;
     double acc[kTile][kTile];
+    float part[kTile][kTile];  // FP32 over kFlush chunks of this thread's slice, then into acc
+    int nsum = 0;
 #pragma unroll
     for (int a = 0; a < kTile; a++)
 #pragma unroll
-        for (int b = 0; b < kTile; b++) acc[a][b] = 0.0;
+        for (int b = 0; b < kTile; b++) {
+            acc[a][b] = 0.0;
+            part[a][b] = 0.f;
+        }
 
     for (int e = me; e < (tl.rows - nb - 2) * kStride; e += blockDim.x) hs[(size_t)(nb + 2) * kStride + e] = 0.f;
 
@@ -127,8 +138,10 @@ __global__ void __launch_bounds__(kMaxThreads) fisher_kernel(int M, int nb, cons
             hs[p * kStride + kk] = (k < K) ? (float)Dp[(size_t)p * K + k] : 0.f;
         }
         __syncthreads();
-        // per-k weights sqrt(m w_i w_j), residual row R (FP64: its diagonal is 1 + lambda_i
-        // less a sum close to lambda_i), data row y_i y_j
+        // per-k weights sqrt(m w_i w_j), residual row R, data row y_i y_j.  R's
+        // diagonal is 1 + lambda_i less a sum close to lambda_i, so the sum runs
+        // in compensated FP32 (a two-sum per term plus the exact rounding error
+        // of each product, about FP64 accuracy) instead of on the FP64 pipe.
         for (int kk = me; kk < kChunk; kk += blockDim.x) {
             const long long k = k0 + kk;
             float sc = 0.f, R = 0.f, yy = 0.f;
@@ -137,9 +150,23 @@ __global__ void __launch_bounds__(kMaxThreads) fisher_kernel(int M, int nb, cons
                 unpack(k, &i, &j);
                 const float wi = 1.0f / (1.0f + (float)evals[i]), wj = 1.0f / (1.0f + (float)evals[j]);
                 sc = sqrtf((i == j ? 0.5f : 1.0f) * wi * wj);
-                double r = (i == j) ? 1.0 + evals[i] : 0.0;
-                for (int n = 0; n < nb; n++) r -= prior[n] * (double)hs[n * kStride + kk];
-                R = (float)r;
+                float rs = 0.f, rc = 0.f;
+                if (i == j) {
+                    const double d = 1.0 + evals[i];
+                    rs = (float)d;
+                    rc = (float)(d - (double)rs);
+                }
+                for (int n = 0; n < nb; n++) {
+                    const float dn = hs[n * kStride + kk];
+                    const float t = -p_hi[n] * dn;
+                    const float te = fmaf(-p_hi[n], dn, -t);  // exact: -p_hi dn = t + te
+                    const float u = rs + t;                    // two-sum: rs + t = u + ue
+                    const float bb = u - rs;
+                    const float ue = (rs - (u - bb)) + (t - bb);
+                    rs = u;
+                    rc += ue + te - p_lo[n] * dn;
+                }
+                R = rs + rc;
                 yy = (float)(y[i] * y[j]);
             }
             for (int p = 0; p < nb; p++) hs[p * kStride + kk] *= sc;
@@ -148,11 +175,6 @@ __global__ void __launch_bounds__(kMaxThreads) fisher_kernel(int M, int nb, cons
         }
         __syncthreads();
         if (worker) {
-            float part[kTile][kTile];
-#pragma unroll
-            for (int a = 0; a < kTile; a++)
-#pragma unroll
-                for (int b = 0; b < kTile; b++) part[a][b] = 0.f;
 #pragma unroll 4
             for (int kk = 0; kk < per; kk++) {
                 float va[kTile], vb[kTile];
@@ -166,13 +188,23 @@ __global__ void __launch_bounds__(kMaxThreads) fisher_kernel(int M, int nb, cons
 #pragma unroll
                     for (int b = 0; b < kTile; b++) part[a][b] = fmaf(va[a], vb[b], part[a][b]);
             }
+            if (++nsum == kFlush) {
 #pragma unroll
-            for (int a = 0; a < kTile; a++)
+                for (int a = 0; a < kTile; a++)
 #pragma unroll
-                for (int b = 0; b < kTile; b++) acc[a][b] += (double)part[a][b];
+                    for (int b = 0; b < kTile; b++) {
+                        acc[a][b] += (double)part[a][b];
+                        part[a][b] = 0.f;
+                    }
+                nsum = 0;
+            }
         }
         __syncthreads();
     }
+#pragma unroll
+    for (int a = 0; a < kTile; a++)
+#pragma unroll
+        for (int b = 0; b < kTile; b++) acc[a][b] += (double)part[a][b];
 
     // slices of one tile summed in a fixed order, then one write per output
     double* red = reinterpret_cast<double*>(fisher_smem);  // [ntiles * slices][16]
