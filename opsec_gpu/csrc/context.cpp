@@ -987,7 +987,7 @@ void build_q(opsec_gpu* c) {
     a.win_flush = c->win_flush;
     a.win_dot64 = c->win_dot64;
     if (a.exact && a.window) {
-        a.work_bytes = cubature_work_bytes(c->ks, c->xl.n());
+        a.work_bytes = cubature_work_bytes(c->ks, c->xl.n(), a.ntab);
         c->cubwork.alloc(a.work_bytes);
         a.work = c->cubwork.p;
     }

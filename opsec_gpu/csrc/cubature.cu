@@ -381,10 +381,7 @@ __global__ void __launch_bounds__(Shape<NG>::kWarps * 32, 1)
 // tile of every table.  Keys with windows wider than a tile allows (near and
 // self pairs) go to the table-group kernel in list mode.
 struct WinPlan {
-    int W;        // tile width in bins
-    int stride;   // tile row stride in floats (= 1 mod 32: conflict-free across tables)
     int Wkey;     // widest key window on the window path
-    int KB;       // keys per batch
     int flush;    // second-cell points per FP32 partial histogram before the FP64 flush (0: no flush)
     int dot64;    // dot products in FP64 (1) or in FP32 chunks of 8 bins (0)
     int nbucket;  // nx + 1: bucket nx holds the near keys
@@ -396,7 +393,18 @@ struct WinPlan {
     int* nnear;       // near keys incl. overflows (list length from order + nfar)
     int* violations;  // pairs that fell outside their key's window (must stay 0)
     float4* cen;      // per cell: bounding-sphere centre and radius
+    float* tabT;      // [nx][ntab]: the FP32 tables transposed, bin-major
 };
+
+// The tables bin-major, so that the lanes of a warp (one table each) read one
+// bin of every table with one coalesced load.
+__global__ void transpose_tables_kernel(const float* tab32, int ntab, int nx, float* tabT) {
+    const long long n = (long long)ntab * nx;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        const int b = (int)(e / ntab), t = (int)(e % ntab);
+        tabT[e] = tab32[(size_t)t * nx + b];
+    }
+}
 
 // bounding sphere of each cell from its Gauss points (FP64), radius inflated by a margin
 __global__ void cell_sphere_kernel(const float4* pts, int np, long long ncell, float4* cen) {
@@ -501,16 +509,19 @@ __global__ void bucket_scatter_kernel(long long nkeys, WinPlan w) {
 
 // Histogram bins hold sum w_p w_q (1-fr) and sum w_p w_q fr.  They are summed
 // by FP32 shared-memory atomics over `flush` (8) second-cell points at a time
-// and then moved into an FP64 histogram, so every FP32 partial sum stays small.
-// A bin summed in FP32 over all 4096 pairs of a key carries a rounding error
-// relative to its whole (positive) sum into the strongly cancelling dot
-// product with an oscillating band table.  Measured on the 4x4x4 box, band
-// k in [0.1, 0.15], max|dS|/max|S|: no flush 2.2e-6, flush every 32 points
-// 1.8e-6, every 16 7.9e-7, every 8 9e-8 (the table-group kernel: 2.8e-7);
-// cubature time at 32k cells 199, 259, 267, 245 ms.  The dot products run in
-// FP32 over chunks of 8 bins added in FP64 (`dot64` = FP64 throughout: same
-// error, +38 ms on the FP64 pipe).  64-bit integer (fixed-point) histogram
-// atomics would sum exactly but cost +177 ms in shared-memory atomics.
+// and then moved into a compensated FP32 histogram (high part + low part by
+// two-sum, about 48 bits; on the FP32 pipe, not the slow FP64 one), so every
+// FP32 partial sum stays small.  A bin summed in FP32 over all 4096 pairs of a
+// key carries a rounding error relative to its whole (positive) sum into the
+// strongly cancelling dot product with an oscillating band table.  Measured on
+// the 4x4x4 box, band k in [0.1, 0.15], max|dS|/max|S|: no flush 2.2e-6, flush
+// every 32 points 1.8e-6, every 16 7.9e-7, every 8 9e-8 (the table-group
+// kernel: 2.8e-7).  The dot products run in FP32 over chunks of 8 bins added
+// in FP64 (`dot64` = FP64 throughout: same error, more FP64 work); lane t
+// takes table t and reads the bin-major tables from L1/L2, so the tables take
+// no shared memory and two 16-warp CTAs fit on an SM.  64-bit integer
+// (fixed-point) histogram atomics would sum exactly but cost +177 ms at 32k
+// cells in shared-memory atomics.
 
 template <int NG>
 struct FarShape {
@@ -519,16 +530,16 @@ struct FarShape {
 };
 
 template <int NG>
-__global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 1)
+__global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
     cubature_far_kernel(CubatureArgs a, Lookup lk, WinPlan w) {
     constexpr int NP = FarShape<NG>::NP;
     constexpr int kWarps = FarShape<NG>::kWarps;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int nx = a.xl.n(), ntab = a.ntab;
-    float4* pts = reinterpret_cast<float4*>(smem_raw);                       // [kWarps][2][NP]
-    double* master = reinterpret_cast<double*>(pts + kWarps * 2 * NP);         // [kWarps][Wkey]
-    float* part = reinterpret_cast<float*>(master + kWarps * w.Wkey);          // [kWarps][Wkey]
-    float* tile = part + kWarps * w.Wkey;                                      // [ntab][stride]
+    const int ntab = a.ntab;
+    float4* pts = reinterpret_cast<float4*>(smem_raw);                  // [kWarps][2][NP]
+    float* mhi = reinterpret_cast<float*>(pts + kWarps * 2 * NP);       // [kWarps][Wkey]: histogram, high part
+    float* mlo = mhi + kWarps * w.Wkey;                                 // [kWarps][Wkey]: low part
+    float* part = mlo + kWarps * w.Wkey;                                // [kWarps][Wkey]: FP32 sums between flushes
     __shared__ int s_ci[kMaxExp];
     __shared__ float s_cf[kMaxExp];
     __shared__ float4 s_kt[kLogN];
@@ -537,118 +548,110 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 1)
         s_cf[i] = lk.cf[i];
     }
     for (int i = threadIdx.x; i < kLogN; i += blockDim.x) s_kt[i] = lk.kt[i];
+    __syncthreads();
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     float4* P2 = pts + warp * 2 * NP;
     float4* P2l = P2 + NP;
-    double* hm = master + warp * w.Wkey;
+    float* hh = mhi + warp * w.Wkey;
+    float* hl = mlo + warp * w.Wkey;
     float* hp = part + warp * w.Wkey;
     const bool periodic = (a.coordsys == 1 && a.L > 0);
     const float Lh = (float)a.L, Ll = (float)(a.L - (double)Lh), hL = 0.5f * Lh;
     const int nfar = *w.nfar;
-    const int nbatch = (nfar + w.KB - 1) / w.KB;
-    for (int bt = blockIdx.x; bt < nbatch; bt += gridDim.x) {
-        const int k0 = bt * w.KB, k1 = min(nfar, k0 + w.KB);
-        const int tlo = w.win[w.order[k0]].x;
-        __syncthreads();  // the previous batch is done with the tile
-        for (int e = threadIdx.x; e < ntab * w.W; e += blockDim.x) {
-            const int t = e / w.W, b = e % w.W, g = tlo + b;
-            tile[t * w.stride + b] = g < nx ? a.tab32[(size_t)t * nx + g] : 0.f;
+    // consecutive warps take consecutive keys of the window-start order: the
+    // keys in flight at any time read neighbouring rows of the tables
+    for (int kk = blockIdx.x * kWarps + warp; kk < nfar; kk += gridDim.x * kWarps) {
+        const int key = w.order[kk];
+        const int2 wn = w.win[key];
+        const int wl = wn.y;
+        for (int j = lane; j < wl; j += 32) {
+            hh[j] = 0.f;
+            hl[j] = 0.f;
+            hp[j] = 0.f;
         }
-        __syncthreads();
-        for (int kk = k0 + warp; kk < k1; kk += kWarps) {
-            const int key = w.order[kk];
-            const int2 wn = w.win[key];
-            const int off = wn.x - tlo, wl = wn.y;
-            if (off + wl > w.W) {  // does not fit this batch's tile: table-group kernel
-                if (lane == 0) w.order[(size_t)nfar + atomicAdd(w.nnear, 1)] = key;
-                continue;
-            }
-            for (int j = lane; j < wl; j += 32) {
-                hm[j] = 0.0;
-                hp[j] = 0.f;
-            }
-            int c1[3], c2[3];
-            decode_key(a.ks, key, c1, c2);
-            const float4* G1 = a.pts + 2 * NP * cell_id(a.ks, c1);
-            const float4* G2 = a.pts + 2 * NP * cell_id(a.ks, c2);
-            const float4 Oh = G1[2 * (NP / 2)], Ol = G1[2 * (NP / 2) + 1];
-            for (int q = lane; q < NP; q += 32) {
-                const float4 Bh = G2[2 * q], Bl = G2[2 * q + 1];
-                float lx, ly, lz;
-                const float sx = diff2(Bh.x, Bl.x, Oh.x, Ol.x, &lx);
-                const float sy = diff2(Bh.y, Bl.y, Oh.y, Ol.y, &ly);
-                const float sz = diff2(Bh.z, Bl.z, Oh.z, Ol.z, &lz);
-                P2[q] = make_float4(sx, sy, sz, Bh.w);
-                P2l[q] = make_float4(lx, ly, lz, 0.f);
-            }
-            __syncwarp();
-            int bad = 0;
-            // every lane runs the same trip counts: the flushes below are warp-wide
-            for (int p0 = 0; p0 < NP; p0 += 32) {
-                const int p = p0 + lane;
-                const bool act = p < NP;
-                const float4 Ah = act ? G1[2 * p] : make_float4(0.f, 0.f, 0.f, 0.f);
-                const float4 Al = act ? G1[2 * p + 1] : make_float4(0.f, 0.f, 0.f, 0.f);
-                float alx, aly, alz;
-                const float ax = diff2(Ah.x, Al.x, Oh.x, Ol.x, &alx);
-                const float ay = diff2(Ah.y, Al.y, Oh.y, Ol.y, &aly);
-                const float az = diff2(Ah.z, Al.z, Oh.z, Ol.z, &alz);
-                const int nfl = w.flush > 0 ? w.flush : NP;
-                for (int q0 = 0; q0 < NP; q0 += nfl) {
-                    if (act) {
+        int c1[3], c2[3];
+        decode_key(a.ks, key, c1, c2);
+        const float4* G1 = a.pts + 2 * NP * cell_id(a.ks, c1);
+        const float4* G2 = a.pts + 2 * NP * cell_id(a.ks, c2);
+        const float4 Oh = G1[2 * (NP / 2)], Ol = G1[2 * (NP / 2) + 1];
+        for (int q = lane; q < NP; q += 32) {
+            const float4 Bh = G2[2 * q], Bl = G2[2 * q + 1];
+            float lx, ly, lz;
+            const float sx = diff2(Bh.x, Bl.x, Oh.x, Ol.x, &lx);
+            const float sy = diff2(Bh.y, Bl.y, Oh.y, Ol.y, &ly);
+            const float sz = diff2(Bh.z, Bl.z, Oh.z, Ol.z, &lz);
+            P2[q] = make_float4(sx, sy, sz, Bh.w);
+            P2l[q] = make_float4(lx, ly, lz, 0.f);
+        }
+        __syncwarp();
+        int bad = 0;
+        // every lane runs the same trip counts: the flushes below are warp-wide
+        for (int p0 = 0; p0 < NP; p0 += 32) {
+            const int p = p0 + lane;
+            const bool act = p < NP;
+            const float4 Ah = act ? G1[2 * p] : make_float4(0.f, 0.f, 0.f, 0.f);
+            const float4 Al = act ? G1[2 * p + 1] : make_float4(0.f, 0.f, 0.f, 0.f);
+            float alx, aly, alz;
+            const float ax = diff2(Ah.x, Al.x, Oh.x, Ol.x, &alx);
+            const float ay = diff2(Ah.y, Al.y, Oh.y, Ol.y, &aly);
+            const float az = diff2(Ah.z, Al.z, Oh.z, Ol.z, &alz);
+            const int nfl = w.flush > 0 ? w.flush : NP;
+            for (int q0 = 0; q0 < NP; q0 += nfl) {
+                if (act) {
 #pragma unroll 4
-                        for (int q = q0; q < q0 + nfl && q < NP; q++) {
-                            const float4 B = P2[q];
-                            int i;
-                            float fr;
-                            exact_index(lk, s_ci, s_cf, s_kt, B, P2l[q], ax, alx, ay, aly, az, alz, periodic, Lh, Ll,
-                                        hL, i, fr);
-                            int bi = i - wn.x;
-                            if (bi < 0 || bi > wl - 2) {  // outside the window: cannot happen for a sound window
-                                bad++;
-                                bi = min(max(bi, 0), wl - 2);
-                            }
-                            const float ww = Ah.w * B.w;
-                            atomicAdd(&hp[bi], fmaf(-ww, fr, ww));
-                            atomicAdd(&hp[bi + 1], ww * fr);
+                    for (int q = q0; q < q0 + nfl && q < NP; q++) {
+                        const float4 B = P2[q];
+                        int i;
+                        float fr;
+                        exact_index(lk, s_ci, s_cf, s_kt, B, P2l[q], ax, alx, ay, aly, az, alz, periodic, Lh, Ll, hL,
+                                    i, fr);
+                        int bi = i - wn.x;
+                        if (bi < 0 || bi > wl - 2) {  // outside the window: cannot happen for a sound window
+                            bad++;
+                            bi = min(max(bi, 0), wl - 2);
                         }
-                    }
-                    if (w.flush) {
-                        // the FP32 partial sums stay small: move them into the FP64 histogram
-                        __syncwarp();
-                        for (int b = lane; b < wl; b += 32) {
-                            hm[b] += (double)hp[b];
-                            hp[b] = 0.f;
-                        }
-                        __syncwarp();
+                        const float ww = Ah.w * B.w;
+                        atomicAdd(&hp[bi], fmaf(-ww, fr, ww));
+                        atomicAdd(&hp[bi + 1], ww * fr);
                     }
                 }
-            }
-            if (bad) atomicAdd(w.violations, bad);
-            __syncwarp();
-            for (int t = lane; t < ntab; t += 32) {
-                const float* tr = tile + t * w.stride + off;
-                double acc = 0.0;
-                if (w.flush && w.dot64) {
-                    for (int b = 0; b < wl; b++) acc = fma((double)tr[b], hm[b], acc);
-                } else if (w.flush) {
-                    for (int b0 = 0; b0 < wl; b0 += 8) {
-                        float pt = 0.f;
-                        for (int b = b0; b < min(b0 + 8, wl); b++) pt = fmaf(tr[b], (float)hm[b], pt);
-                        acc += (double)pt;
+                if (w.flush) {
+                    // the FP32 partial sums stay small: move them into the compensated histogram
+                    __syncwarp();
+                    for (int b = lane; b < wl; b += 32) {
+                        float e;
+                        hh[b] = two_sum(hh[b], hp[b], &e);
+                        hl[b] += e;
+                        hp[b] = 0.f;
                     }
-                } else {
-                    for (int b0 = 0; b0 < wl; b0 += 8) {
-                        float pt = 0.f;
-                        for (int b = b0; b < min(b0 + 8, wl); b++) pt = fmaf(tr[b], hp[b], pt);
-                        acc += (double)pt;
-                    }
+                    __syncwarp();
                 }
-                a.Q[(size_t)t * a.ks.nkeys + key] = acc;
             }
-            __syncwarp();
         }
+        if (bad) atomicAdd(w.violations, bad);
+        __syncwarp();
+        for (int t = lane; t < ntab; t += 32) {
+            const float* tr = w.tabT + (size_t)wn.x * ntab + t;
+            double acc = 0.0;
+            if (w.flush && w.dot64) {
+                for (int b = 0; b < wl; b++) acc = fma((double)tr[(size_t)b * ntab], (double)hh[b] + hl[b], acc);
+            } else if (w.flush) {
+                for (int b0 = 0; b0 < wl; b0 += 8) {
+                    float pt = 0.f;
+                    for (int b = b0; b < min(b0 + 8, wl); b++) pt = fmaf(tr[(size_t)b * ntab], hh[b] + hl[b], pt);
+                    acc += (double)pt;
+                }
+            } else {
+                for (int b0 = 0; b0 < wl; b0 += 8) {
+                    float pt = 0.f;
+                    for (int b = b0; b < min(b0 + 8, wl); b++) pt = fmaf(tr[(size_t)b * ntab], hp[b], pt);
+                    acc += (double)pt;
+                }
+            }
+            a.Q[(size_t)t * a.ks.nkeys + key] = acc;
+        }
+        __syncwarp();
     }
 }
 
@@ -735,9 +738,9 @@ size_t cubature_point_count(const KeySpace& ks, int ng) {
 namespace {
 // scratch layout of the window path
 struct WinLayout {
-    size_t win, order, count, cursor, scal, cen, total;
+    size_t win, order, count, cursor, scal, cen, tabT, total;
 };
-WinLayout win_layout(const KeySpace& ks, int nx) {
+WinLayout win_layout(const KeySpace& ks, int nx, int ntab) {
     auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
     const size_t ncell = (size_t)ks.N1 * ks.N2 * ks.N3;
     WinLayout L;
@@ -747,39 +750,30 @@ WinLayout win_layout(const KeySpace& ks, int nx) {
     L.cursor = L.count + al(sizeof(int) * (nx + 2));
     L.scal = L.cursor + al(sizeof(int) * (nx + 2));
     L.cen = L.scal + 256;
-    L.total = L.cen + al(sizeof(float4) * ncell);
+    L.tabT = L.cen + al(sizeof(float4) * ncell);
+    L.total = L.tabT + al(sizeof(float) * (size_t)nx * ntab);
     return L;
 }
 
 template <int NG>
-size_t far_smem(const WinPlan& w, int ntab) {
+size_t far_smem(const WinPlan& w) {
     return sizeof(float4) * FarShape<NG>::kWarps * 2 * FarShape<NG>::NP +
-           (sizeof(double) + sizeof(float)) * FarShape<NG>::kWarps * w.Wkey + sizeof(float) * (size_t)ntab * w.stride;
+           3 * sizeof(float) * FarShape<NG>::kWarps * w.Wkey;
 }
 
 // Far keys by windows, near keys by table groups in list mode.  Returns false (nothing
-// launched) when the tables are too many for a useful tile.
+// launched) when the per-warp histograms of the widest window do not fit in shared memory.
 template <int NG>
 bool run_window(const CubatureArgs& a, const Lookup& lk, cudaStream_t s, long long* launches) {
-    constexpr int NP = FarShape<NG>::NP;
     constexpr int kWarps = FarShape<NG>::kWarps;
     const int nx = a.xl.n();
     WinPlan w{};
-    w.Wkey = a.win_key;
+    w.Wkey = std::min(a.win_key, nx);
     w.flush = a.win_flush;
     w.dot64 = a.win_dot64;
-    const size_t fixed = sizeof(float4) * kWarps * 2 * NP + (sizeof(double) + sizeof(float)) * kWarps * w.Wkey;
-    const size_t budget = 222 * 1024;
-    if (fixed >= budget) return false;
-    long long stride = (long long)((budget - fixed) / (sizeof(float) * a.ntab));
-    stride = ((stride - 1) / 32) * 32 + 1;
-    w.W = (int)std::min<long long>(stride - 1, nx);
-    w.stride = ((w.W + 31) / 32) * 32 + 1;
-    if (w.W < 2 * 128) return false;
-    w.Wkey = std::min(w.Wkey, w.W / 2);
-    w.KB = 256;
+    if (w.Wkey < 8 || far_smem<NG>(w) > (size_t)max_dynamic_smem((const void*)cubature_far_kernel<NG>)) return false;
     w.nbucket = nx + 1;
-    const WinLayout L = win_layout(a.ks, nx);
+    const WinLayout L = win_layout(a.ks, nx, a.ntab);
     if (!a.work || a.work_bytes < L.total) fail(OPSEC_ERR_ARG, "cubature scratch too small");
     unsigned char* base = static_cast<unsigned char*>(a.work);
     w.win = reinterpret_cast<int2*>(base + L.win);
@@ -791,6 +785,7 @@ bool run_window(const CubatureArgs& a, const Lookup& lk, cudaStream_t s, long lo
     w.nnear = scal + 1;
     w.violations = scal + 2;
     w.cen = reinterpret_cast<float4*>(base + L.cen);
+    w.tabT = reinterpret_cast<float*>(base + L.tabT);
     OPSEC_CUDA(cudaMemsetAsync(w.count, 0, sizeof(int) * (nx + 2), s));
     OPSEC_CUDA(cudaMemsetAsync(scal, 0, 256, s));
     const long long ncell = (long long)a.ks.N1 * a.ks.N2 * a.ks.N3;
@@ -803,12 +798,14 @@ bool run_window(const CubatureArgs& a, const Lookup& lk, cudaStream_t s, long lo
     OPSEC_CUDA(cudaGetLastError());
     bucket_scatter_kernel<<<blocks(a.ks.nkeys), 256, 0, s>>>(a.ks.nkeys, w);
     OPSEC_CUDA(cudaGetLastError());
-    *launches += 4;
+    transpose_tables_kernel<<<blocks((long long)a.ntab * nx), 256, 0, s>>>(a.tab32, a.ntab, nx, w.tabT);
+    OPSEC_CUDA(cudaGetLastError());
+    *launches += 5;
     int h_nfar = 0;
     OPSEC_CUDA(cudaMemcpyAsync(&h_nfar, w.nfar, sizeof(int), cudaMemcpyDeviceToHost, s));
     OPSEC_CUDA(cudaStreamSynchronize(s));
     // far keys
-    const size_t smem = far_smem<NG>(w, a.ntab);
+    const size_t smem = far_smem<NG>(w);
     auto k = cubature_far_kernel<NG>;
     OPSEC_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem((const void*)k)));
     int dev = 0, nsm = 0, occ = 0;
@@ -816,14 +813,14 @@ bool run_window(const CubatureArgs& a, const Lookup& lk, cudaStream_t s, long lo
     OPSEC_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     OPSEC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, kWarps * 32, smem));
     if (occ < 1) fail(OPSEC_ERR_CUDA, "cubature window kernel does not fit on an SM");
-    const long long nbatch = ((long long)h_nfar + w.KB - 1) / w.KB;
-    const long long grid = std::max<long long>(1, std::min<long long>((long long)nsm * occ, nbatch));
+    const long long grid =
+        std::max<long long>(1, std::min<long long>((long long)nsm * occ, ((long long)h_nfar + kWarps - 1) / kWarps));
     if (h_nfar > 0) {
         k<<<(unsigned)grid, kWarps * 32, smem, s>>>(a, lk, w);
         OPSEC_CUDA(cudaGetLastError());
         ++*launches;
     }
-    // near keys and tile overflows: the table-group kernel over the list
+    // near keys: the table-group kernel over the list
     CubatureArgs an = a;
     an.list = w.order + h_nfar;
     an.list_count = w.nnear;
@@ -836,7 +833,7 @@ bool run_window(const CubatureArgs& a, const Lookup& lk, cudaStream_t s, long lo
 }
 }  // namespace
 
-size_t cubature_work_bytes(const KeySpace& ks, int nx) { return win_layout(ks, nx).total; }
+size_t cubature_work_bytes(const KeySpace& ks, int nx, int ntab) { return win_layout(ks, nx, ntab).total; }
 
 void launch_cubature(const CubatureArgs& a, cudaStream_t s, long long* launches) {
     // point table: every Gauss point of every cell, once
