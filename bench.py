@@ -139,30 +139,42 @@ def tensor_roofline(s1, bf16, peak_kind):
             "avg_launch_ms": avg_s * 1000, "launches": int(s1["count"])}
 
 
+# Instructions one point pair costs in the far-key window kernel's inner loop, counted from
+# the source (opsec_gpu/csrc/cubature.cu, exact_index and the histogram update): two shared
+# loads of the second point, three FP32-pair differences (24), r^2 as an FP32 pair (27), the
+# log2(r^2) split into exponent, table slot and series (about 30 with three shared loads and
+# the clamps), the window offset and its check (4), the two weights and two shared atomics (7),
+# loop control (about 2).
+FAR_OPS_PER_PAIR = 100
+
+
 def roofline(stats, clk, bf16, peak_kind):
     """Roofline of the kernel with the most device time in the timed builds."""
     dom = max(stats, key=lambda n: stats[n]["ms"])
     s = stats[dom]
     if s["count"] == 0 or s["ms"] <= 0:
         return None
-    if dom == "cubature":
-        # Unit: one Gauss-point pair x one xi table (an interpolated table value, weighted and summed).
-        # Reference roofline: evaluating each unit by two 4-byte shared-memory table loads, 32 banks x
-        # 4 B per clock per SM -> 16 units / clock / SM.  The window path does not load per unit (one
-        # pass over the pairs scatters interpolation weights into a per-key bin histogram, then one
-        # dot product per table), so it is measured against what direct lookups could reach.  No
-        # measured figure exists for shared memory: derived from the SM count and the sampled clock.
+    if dom in ("cubature", "cubature_far") and stats.get("cubature_far", {}).get("count", 0) > 0:
+        # The cubature stage's dominant kernel is the far-key window kernel: per key one pass over
+        # the 4096 Gauss-point pairs scatters interpolation weights into a bin histogram, then one
+        # dot product per table, so its work is point pairs, each FAR_OPS_PER_PAIR instructions,
+        # against the instruction issue rate: 4 schedulers x 32 lanes per clock per SM.  No
+        # measured figure exists for issue: derived from the SM count and the sampled clock.
+        f = stats["cubature_far"]
         nsm = 152
         mhz = clk.get("sm_mhz") or 2070.0
-        peak = 16.0 * nsm * mhz * 1e6 / 1e9
-        avg_s = s["ms"] / 1000.0 / s["count"]
-        achieved = s["flops"] / s["count"] / avg_s / 1e9
-        return {"kernel": "cubature (window-histogram kernel for far keys, table-group kernel for near keys)",
-                "bound": "smem", "achieved": achieved, "peak": peak, "unit": "G pair-table units/s",
-                "frac": achieved / peak, "traffic": None,
-                "peak_kind": f"derived: 16 table lookups/clk/SM x {nsm} SMs x {mhz:.0f} MHz (sampled median)",
-                "algorithmic_unit": "one Gauss-point pair x one xi table", "avg_launch_ms": avg_s * 1000,
-                "launches": int(s["count"])}
+        peak = 128.0 * nsm * mhz * 1e6 / FAR_OPS_PER_PAIR / 1e9
+        avg_s = f["ms"] / 1000.0 / f["count"]
+        achieved = f["flops"] / f["count"] / avg_s / 1e9
+        st = stats["cubature"]
+        return {"kernel": "cubature_far_kernel (window histograms, far keys)", "bound": "issue",
+                "achieved": achieved, "peak": peak, "unit": "G point pairs/s", "frac": achieved / peak,
+                "traffic": None,
+                "peak_kind": f"derived: 128 lane instructions/clk/SM x {nsm} SMs x {mhz:.0f} MHz (sampled median)"
+                             f" / {FAR_OPS_PER_PAIR} instructions per point pair",
+                "algorithmic_unit": "one Gauss-point pair (all xi tables at once)", "avg_launch_ms": avg_s * 1000,
+                "launches": int(f["count"]),
+                "stage_xi_evaluations_per_s": st["flops"] / (st["ms"] / 1000.0) if st["ms"] > 0 else None}
     if dom == "project_step1":
         return tensor_roofline(s, bf16, peak_kind)
     return {"kernel": dom, "bound": None, "avg_launch_ms": s["ms"] / max(s["count"], 1)}
@@ -393,7 +405,7 @@ def main():
 
     for _ in range(args.warmup):
         res = eng.fisher_build(cells, counts, w["nmodes"])
-    names = ("cubature", "surrogate", "azimuthal_transform", "azimuthal_gemm", "project_step1", "project_step2",
+    names = ("cubature", "cubature_far", "surrogate", "azimuthal_transform", "azimuthal_gemm", "project_step1", "project_step2",
              "fisher")
     base = {n: eng.kernel_stats(n) for n in names}
     launches0 = eng.launch_count()

@@ -43,12 +43,14 @@ void KernelClock::begin(const char* name, cudaStream_t s, double flops, double b
     OPSEC_CUDA(cudaEventCreate(&r.a));
     OPSEC_CUDA(cudaEventCreate(&r.b));
     OPSEC_CUDA(cudaEventRecord(r.a, s));
+    open.push_back(pending.size());
     pending.push_back(r);
 }
 
 void KernelClock::end(cudaStream_t s) {
-    if (!on || pending.empty()) return;
-    OPSEC_CUDA(cudaEventRecord(pending.back().b, s));
+    if (!on || open.empty()) return;
+    OPSEC_CUDA(cudaEventRecord(pending[open.back()].b, s));
+    open.pop_back();
 }
 
 int max_dynamic_smem(const void* func) {
@@ -376,6 +378,7 @@ void collect_clock(opsec_gpu* c) {
         cudaEventDestroy(r.b);
     }
     c->clock.pending.clear();
+    c->clock.open.clear();
 }
 
 template <class F>

@@ -381,7 +381,8 @@ __global__ void __launch_bounds__(Shape<NG>::kWarps * 32, 1)
 // tile of every table.  Keys with windows wider than a tile allows (near and
 // self pairs) go to the table-group kernel in list mode.
 struct WinPlan {
-    int Wkey;     // widest key window on the window path
+    int Wkey;     // histogram bins per warp: one pass covers Wkey - 1 bins of a key's window
+    int Wmax;     // widest key window on the window path (npass_max passes)
     int flush;    // second-cell points per FP32 partial histogram before the FP64 flush (0: no flush)
     int dot64;    // dot products in FP64 (1) or in FP32 chunks of 8 bins (0)
     int nbucket;  // nx + 1: bucket nx holds the near keys
@@ -461,7 +462,7 @@ __global__ void key_window_kernel(CubatureArgs a, WinPlan w) {
         const int blo = max(bin_floor(a.xl, fmax(dist - R, 0.0)) - 1, 0);
         const int bhi = min(bin_floor(a.xl, dist + R) + 3, nx);
         const int width = bhi - blo;
-        const int bucket = (near || width > w.Wkey) ? nx : blo;
+        const int bucket = (near || width > w.Wmax) ? nx : blo;
         w.win[key] = make_int2(bucket, width);
         atomicAdd(&w.count[bucket], 1);
     }
@@ -523,6 +524,8 @@ __global__ void bucket_scatter_kernel(long long nkeys, WinPlan w) {
 // (fixed-point) histogram atomics would sum exactly but cost +177 ms at 32k
 // cells in shared-memory atomics.
 
+constexpr int kMaxPasses = 8;  // passes over the point pairs for windows wider than one histogram
+
 template <int NG>
 struct FarShape {
     static constexpr int NP = NG * NG * NG;
@@ -565,11 +568,6 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
         const int key = w.order[kk];
         const int2 wn = w.win[key];
         const int wl = wn.y;
-        for (int j = lane; j < wl; j += 32) {
-            hh[j] = 0.f;
-            hl[j] = 0.f;
-            hp[j] = 0.f;
-        }
         int c1[3], c2[3];
         decode_key(a.ks, key, c1, c2);
         const float4* G1 = a.pts + 2 * NP * cell_id(a.ks, c1);
@@ -586,72 +584,91 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
         }
         __syncwarp();
         int bad = 0;
-        // every lane runs the same trip counts: the flushes below are warp-wide
-        for (int p0 = 0; p0 < NP; p0 += 32) {
-            const int p = p0 + lane;
-            const bool act = p < NP;
-            const float4 Ah = act ? G1[2 * p] : make_float4(0.f, 0.f, 0.f, 0.f);
-            const float4 Al = act ? G1[2 * p + 1] : make_float4(0.f, 0.f, 0.f, 0.f);
-            float alx, aly, alz;
-            const float ax = diff2(Ah.x, Al.x, Oh.x, Ol.x, &alx);
-            const float ay = diff2(Ah.y, Al.y, Oh.y, Ol.y, &aly);
-            const float az = diff2(Ah.z, Al.z, Oh.z, Ol.z, &alz);
-            const int nfl = w.flush > 0 ? w.flush : NP;
-            for (int q0 = 0; q0 < NP; q0 += nfl) {
-                if (act) {
-#pragma unroll 4
-                    for (int q = q0; q < q0 + nfl && q < NP; q++) {
-                        const float4 B = P2[q];
-                        int i;
-                        float fr;
-                        exact_index(lk, s_ci, s_cf, s_kt, B, P2l[q], ax, alx, ay, aly, az, alz, periodic, Lh, Ll, hL,
-                                    i, fr);
-                        int bi = i - wn.x;
-                        if (bi < 0 || bi > wl - 2) {  // outside the window: cannot happen for a sound window
-                            bad++;
-                            bi = min(max(bi, 0), wl - 2);
+        // A window wider than the histogram takes several passes over the point pairs, pass s
+        // keeping the pairs whose lower bin lies in [s S, s S + S), S = Wkey - 1 (the upper
+        // bin of such a pair is at most s S + S); the dot products of the passes are summed.
+        const int S = w.Wkey - 1;
+        const int npass = (wl - 1 + S - 1) / S;
+        for (int pass = 0; pass < npass; pass++) {
+            const int s0 = pass * S;
+            const int segw = min(S, wl - 1 - s0) + 1;  // bins s0 .. s0 + segw - 1 of the window
+            for (int j = lane; j < segw; j += 32) {
+                hh[j] = 0.f;
+                hl[j] = 0.f;
+                hp[j] = 0.f;
+            }
+            __syncwarp();
+            // every lane runs the same trip counts: the flushes below are warp-wide
+            for (int p0 = 0; p0 < NP; p0 += 32) {
+                const int p = p0 + lane;
+                const bool act = p < NP;
+                const float4 Ah = act ? G1[2 * p] : make_float4(0.f, 0.f, 0.f, 0.f);
+                const float4 Al = act ? G1[2 * p + 1] : make_float4(0.f, 0.f, 0.f, 0.f);
+                float alx, aly, alz;
+                const float ax = diff2(Ah.x, Al.x, Oh.x, Ol.x, &alx);
+                const float ay = diff2(Ah.y, Al.y, Oh.y, Ol.y, &aly);
+                const float az = diff2(Ah.z, Al.z, Oh.z, Ol.z, &alz);
+                const int nfl = w.flush > 0 ? w.flush : NP;
+                for (int q0 = 0; q0 < NP; q0 += nfl) {
+                    if (act) {
+    #pragma unroll 4
+                        for (int q = q0; q < q0 + nfl && q < NP; q++) {
+                            const float4 B = P2[q];
+                            int i;
+                            float fr;
+                            exact_index(lk, s_ci, s_cf, s_kt, B, P2l[q], ax, alx, ay, aly, az, alz, periodic, Lh, Ll, hL,
+                                        i, fr);
+                            int bi = i - wn.x;
+                            if (bi < 0 || bi > wl - 2) {  // outside the window: cannot happen for a sound window
+                                bad += pass == 0;
+                                bi = min(max(bi, 0), wl - 2);
+                            }
+                            bi -= s0;
+                            if (bi >= 0 && bi < S) {
+                                const float ww = Ah.w * B.w;
+                                atomicAdd(&hp[bi], fmaf(-ww, fr, ww));
+                                atomicAdd(&hp[bi + 1], ww * fr);
+                            }
                         }
-                        const float ww = Ah.w * B.w;
-                        atomicAdd(&hp[bi], fmaf(-ww, fr, ww));
-                        atomicAdd(&hp[bi + 1], ww * fr);
                     }
-                }
-                if (w.flush) {
-                    // the FP32 partial sums stay small: move them into the compensated histogram
-                    __syncwarp();
-                    for (int b = lane; b < wl; b += 32) {
-                        float e;
-                        hh[b] = two_sum(hh[b], hp[b], &e);
-                        hl[b] += e;
-                        hp[b] = 0.f;
+                    if (w.flush) {
+                        // the FP32 partial sums stay small: move them into the compensated histogram
+                        __syncwarp();
+                        for (int b = lane; b < segw; b += 32) {
+                            float e;
+                            hh[b] = two_sum(hh[b], hp[b], &e);
+                            hl[b] += e;
+                            hp[b] = 0.f;
+                        }
+                        __syncwarp();
                     }
-                    __syncwarp();
                 }
             }
+            __syncwarp();
+            for (int t = lane; t < ntab; t += 32) {
+                const float* tr = w.tabT + (size_t)(wn.x + s0) * ntab + t;
+                double acc = 0.0;
+                if (w.flush && w.dot64) {
+                    for (int b = 0; b < segw; b++) acc = fma((double)tr[(size_t)b * ntab], (double)hh[b] + hl[b], acc);
+                } else if (w.flush) {
+                    for (int b0 = 0; b0 < segw; b0 += 8) {
+                        float pt = 0.f;
+                        for (int b = b0; b < min(b0 + 8, segw); b++) pt = fmaf(tr[(size_t)b * ntab], hh[b] + hl[b], pt);
+                        acc += (double)pt;
+                    }
+                } else {
+                    for (int b0 = 0; b0 < segw; b0 += 8) {
+                        float pt = 0.f;
+                        for (int b = b0; b < min(b0 + 8, segw); b++) pt = fmaf(tr[(size_t)b * ntab], hp[b], pt);
+                        acc += (double)pt;
+                    }
+                }
+                double* q = a.Q + (size_t)t * a.ks.nkeys + key;
+                *q = pass == 0 ? acc : *q + acc;
+            }
+            __syncwarp();
         }
         if (bad) atomicAdd(w.violations, bad);
-        __syncwarp();
-        for (int t = lane; t < ntab; t += 32) {
-            const float* tr = w.tabT + (size_t)wn.x * ntab + t;
-            double acc = 0.0;
-            if (w.flush && w.dot64) {
-                for (int b = 0; b < wl; b++) acc = fma((double)tr[(size_t)b * ntab], (double)hh[b] + hl[b], acc);
-            } else if (w.flush) {
-                for (int b0 = 0; b0 < wl; b0 += 8) {
-                    float pt = 0.f;
-                    for (int b = b0; b < min(b0 + 8, wl); b++) pt = fmaf(tr[(size_t)b * ntab], hh[b] + hl[b], pt);
-                    acc += (double)pt;
-                }
-            } else {
-                for (int b0 = 0; b0 < wl; b0 += 8) {
-                    float pt = 0.f;
-                    for (int b = b0; b < min(b0 + 8, wl); b++) pt = fmaf(tr[(size_t)b * ntab], hp[b], pt);
-                    acc += (double)pt;
-                }
-            }
-            a.Q[(size_t)t * a.ks.nkeys + key] = acc;
-        }
-        __syncwarp();
     }
 }
 
@@ -769,6 +786,7 @@ bool run_window(const CubatureArgs& a, const Lookup& lk, cudaStream_t s, long lo
     const int nx = a.xl.n();
     WinPlan w{};
     w.Wkey = std::min(a.win_key, nx);
+    w.Wmax = std::min(kMaxPasses * (w.Wkey - 1) + 1, nx);
     w.flush = a.win_flush;
     w.dot64 = a.win_dot64;
     if (w.Wkey < 8 || far_smem<NG>(w) > (size_t)max_dynamic_smem((const void*)cubature_far_kernel<NG>)) return false;
@@ -816,8 +834,11 @@ bool run_window(const CubatureArgs& a, const Lookup& lk, cudaStream_t s, long lo
     const long long grid =
         std::max<long long>(1, std::min<long long>((long long)nsm * occ, ((long long)h_nfar + kWarps - 1) / kWarps));
     if (h_nfar > 0) {
+        constexpr int NP = FarShape<NG>::NP;
+        if (g_clock) g_clock->begin("cubature_far", s, (double)h_nfar * NP * NP);  // point pairs
         k<<<(unsigned)grid, kWarps * 32, smem, s>>>(a, lk, w);
         OPSEC_CUDA(cudaGetLastError());
+        if (g_clock) g_clock->end(s);
         ++*launches;
     }
     // near keys: the table-group kernel over the list

@@ -87,6 +87,7 @@ struct KernelClock {
         double flops, bytes;
     };
     std::vector<Rec> pending;
+    std::vector<size_t> open;  // begun, not yet ended (brackets nest)
     void begin(const char* name, cudaStream_t s, double flops = 0, double bytes = 0);
     void end(cudaStream_t s);
 };
