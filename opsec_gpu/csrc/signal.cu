@@ -3,6 +3,8 @@
 // around them (mode scaling, pixel projection).
 #include <cmath>
 
+#include <type_traits>
+
 #include "engine.h"
 
 namespace opsec {
@@ -244,11 +246,86 @@ void launch_signal_block(const KeySpace& ks, const CellKeyInfo& ci, const double
     ++*l;
 }
 
+// FP32 blocks for the band projection: the same transform with the 17 (for
+// N_phi = 32) products per output in FP32 (the blocks are rounded to FP32
+// anyway and feed FP32 GEMMs), each thread holding its two key rows in
+// registers and producing every azimuthal order, so FP64 work (slow on this
+// part) is only the conversion of the loaded Q values.
+template <int NFM>
+__global__ void azimuthal_blocks_f32_kernel(KeySpace ks, const double* Q, const double* nbar_arc, int nm, int npar,
+                                            float* Sm) {
+    extern __shared__ float cwf[];  // [nm][NFM], zero past nf
+    const int H = ks.H, Nphi = ks.N3, nf = ks.nf, Nmu = ks.N2;
+    for (int t = threadIdx.x; t < nm * NFM; t += blockDim.x) {
+        const int m = t / NFM, df = t % NFM;
+        const int md = (int)(((long long)m * df) % Nphi);
+        const double w = (df == 0 || 2 * df == Nphi) ? 1.0 : 2.0;
+        cwf[t] = df < nf ? (float)(w * cospi(2.0 * md / Nphi)) : 0.f;
+    }
+    __syncthreads();
+    const int Hb = H / npar, half = Nmu / npar;
+    const long long HH = (long long)Hb * Hb;
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < HH; r += (long long)gridDim.x * blockDim.x) {
+        const int y = (int)(r / Hb), x = (int)(r % Hb);
+        const int ha = (x / half) * Nmu + x % half, hb = (y / half) * Nmu + y % half;
+        const double* p1 = Q + tri_index(min(ha, hb), max(ha, hb), H) * nf;
+        const int pb = (hb / Nmu) * Nmu + (Nmu - 1 - hb % Nmu);
+        const double* p2 = Q + tri_index(min(ha, pb), max(ha, pb), H) * nf;
+        float q1[NFM], q2[NFM];
+#pragma unroll
+        for (int df = 0; df < NFM; df++) {
+            q1[df] = df < nf ? (float)p1[df] : 0.f;
+            q2[df] = (npar == 2 && df < nf) ? (float)p2[df] : 0.f;
+        }
+        const float d = sqrtf((float)nbar_arc[ha]) * sqrtf((float)nbar_arc[hb]);
+        for (int m = 0; m < nm; m++) {
+            const float* c = cwf + m * NFM;
+            float a1 = 0.f, a2 = 0.f;
+#pragma unroll
+            for (int df = 0; df < NFM; df++) {
+                a1 = fmaf(q1[df], c[df], a1);
+                a2 = fmaf(q2[df], c[df], a2);
+            }
+            if (npar == 1) {
+                Sm[(size_t)m * HH + r] = d * a1;
+            } else {
+                Sm[(size_t)(2 * m) * HH + r] = d * (a1 + a2);
+                Sm[(size_t)(2 * m + 1) * HH + r] = d * (a1 - a2);
+            }
+        }
+    }
+}
+
+template <int NFM>
+void launch_azimuthal_f32(const KeySpace& ks, const double* Q, const double* nbar_arc, int nm, int npar, float* Sm,
+                          cudaStream_t st) {
+    const size_t smem = sizeof(float) * (size_t)nm * NFM;
+    OPSEC_CUDA(cudaFuncSetAttribute(azimuthal_blocks_f32_kernel<NFM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    max_dynamic_smem((const void*)azimuthal_blocks_f32_kernel<NFM>)));
+    const long long HH = (long long)(ks.H / npar) * (ks.H / npar);
+    long long gx = (HH + 255) / 256;
+    if (gx > 65535) gx = 65535;
+    azimuthal_blocks_f32_kernel<NFM><<<(unsigned)gx, 256, smem, st>>>(ks, Q, nbar_arc, nm, npar, Sm);
+}
+
 template <typename T>
 void launch_azimuthal_blocks_t(const KeySpace& ks, const double* Q, const double* nbar_arc, int nm, int npar, T* Sm,
                                cudaStream_t st, long long* l) {
     if (npar != 1 && !(npar == 2 && ks.N2 % 2 == 0)) fail(OPSEC_ERR_ARG, "parity split needs an even mu grid");
     if (!ks.fold) fail(OPSEC_ERR_CONFIG, "azimuthal blocks need a full-sky grid");
+    if constexpr (std::is_same<T, float>::value) {
+        if (ks.nf <= 33) {
+            if (ks.nf <= 9)
+                launch_azimuthal_f32<9>(ks, Q, nbar_arc, nm, npar, Sm, st);
+            else if (ks.nf <= 17)
+                launch_azimuthal_f32<17>(ks, Q, nbar_arc, nm, npar, Sm, st);
+            else
+                launch_azimuthal_f32<33>(ks, Q, nbar_arc, nm, npar, Sm, st);
+            OPSEC_CUDA(cudaGetLastError());
+            ++*l;
+            return;
+        }
+    }
     const size_t smem = sizeof(double) * (size_t)nm * ks.nf;
     if (smem > 200 * 1024) fail(OPSEC_ERR_CONFIG, "too many phi cells for the azimuthal block transform");
     OPSEC_CUDA(cudaFuncSetAttribute(azimuthal_blocks_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem((const void*)azimuthal_blocks_kernel<T>)));
