@@ -344,6 +344,12 @@ struct opsec_gpu {
     DevBuf<int> surr_cnt;
     DevBuf<int> az_i;
     DevBuf<long long> az_off;
+    // block Fisher of the last azimuthal projection (Fisher build without the packed triangle)
+    bool az_blockF = false;
+    BlockFisherArgs bf{};
+    long long bf_entries = 0;
+    DevBuf<int> bf_i;
+    DevBuf<long long> bf_l;
     DevBuf<double> evals, modes, Bs, y, counts, prior, fout, partial, est;
     DevBuf<float> Dp;
     DevBuf<double> Dp64;
@@ -1257,59 +1263,72 @@ struct AzPlan {
     const double* nbar_arc;
 };
 
+// C_b = A_b op B_b over `batch` equal-shape problems at fixed strides (a stride may be 0: one
+// operand shared by every problem).
 template <typename T>
-cublasStatus_t gemm(cublasHandle_t h, cublasOperation_t ta, cublasOperation_t tb, int m, int n, int k, const T* A,
-                    int lda, const T* B, int ldb, T* C, int ldc);
+cublasStatus_t gemm_sb(cublasHandle_t h, cublasOperation_t ta, cublasOperation_t tb, int m, int n, int k, const T* A,
+                       int lda, long long sa, const T* B, int ldb, long long sb, T* C, int ldc, long long sc, int batch);
 template <>
-cublasStatus_t gemm<double>(cublasHandle_t h, cublasOperation_t ta, cublasOperation_t tb, int m, int n, int k,
-                            const double* A, int lda, const double* B, int ldb, double* C, int ldc) {
+cublasStatus_t gemm_sb<double>(cublasHandle_t h, cublasOperation_t ta, cublasOperation_t tb, int m, int n, int k,
+                               const double* A, int lda, long long sa, const double* B, int ldb, long long sb,
+                               double* C, int ldc, long long sc, int batch) {
     const double one = 1.0, zero = 0.0;
-    return cublasDgemm(h, ta, tb, m, n, k, &one, A, lda, B, ldb, &zero, C, ldc);
+    return cublasDgemmStridedBatched(h, ta, tb, m, n, k, &one, A, lda, sa, B, ldb, sb, &zero, C, ldc, sc, batch);
 }
 template <>
-cublasStatus_t gemm<float>(cublasHandle_t h, cublasOperation_t ta, cublasOperation_t tb, int m, int n, int k,
-                           const float* A, int lda, const float* B, int ldb, float* C, int ldc) {
+cublasStatus_t gemm_sb<float>(cublasHandle_t h, cublasOperation_t ta, cublasOperation_t tb, int m, int n, int k,
+                              const float* A, int lda, long long sa, const float* B, int ldb, long long sb, float* C,
+                              int ldc, long long sc, int batch) {
     const float one = 1.f, zero = 0.f;
-    return cublasSgemm(h, ta, tb, m, n, k, &one, A, lda, B, ldb, &zero, C, ldc);
+    return cublasSgemmStridedBatched(h, ta, tb, m, n, k, &one, A, lda, sa, B, ldb, sb, &zero, C, ldc, sc, batch);
 }
 
-// Band blocks, block GEMMs and the scatter, in FP64 or FP32 (the transform
-// itself always sums in FP64).
+// Band blocks and block GEMMs, in FP64 or FP32, for every band: the blocks of
+// up to ~2 GB of bands at a time are transformed, then for each block one
+// batched GEMM over those bands forms T = S_p(b) U_b and one more
+// C_b = U_b^T T.  The C_b of all bands stay in the workspace (`Cm`, csize
+// floats per band) for the scatter into the packed triangle or for the block
+// Fisher sums.
 template <typename T>
-void az_blocks(opsec_gpu* c, const AzPlan& a, int M) {
+T* az_blocks(opsec_gpu* c, const AzPlan& a) {
     const int H = a.H;
     DevBuf<unsigned char>& ws = c->azws;
     const int nblk = a.nm * a.npar;
     const size_t nU = (size_t)a.ncol * H, nS = (size_t)nblk * H * H, nT = (size_t)H * std::max(a.Kmax, 1),
                  nC = (size_t)std::max(a.csize, 1LL) * a.nb;
-    ws.alloc(sizeof(T) * (nU + nS + nT + nC));
+    const int bpp = (int)std::max<size_t>(1, std::min<size_t>(a.nb, (size_t(2) << 30) / (sizeof(T) * nS)));
+    ws.alloc(sizeof(T) * (nU + nS * bpp + nT * bpp + nC));
     T* U = reinterpret_cast<T*>(ws.p);
     T* Sb = U + nU;
-    T* Tm = Sb + nS;
-    T* Cm = Tm + nT;
+    T* Tm = Sb + nS * bpp;
+    T* Cm = Tm + nT * bpp;
     // the block eigenvectors the modes use
     launch_gather_block_vectors(H, a.ncol, a.col_m, a.col_idx, c->S.p, U, c->stream, &c->launches);
-    for (int p = 0; p < a.nb; p++) {
-        if (g_clock) g_clock->begin("azimuthal_transform", c->stream, 2.0 * nblk * (double)H * H * c->ks.nf);
-        launch_azimuthal_blocks(c->ks, c->Q.p + (size_t)(1 + p) * c->ks.nkeys, a.nbar_arc, a.nm, a.npar, Sb,
-                                c->stream, &c->launches);
-        if (g_clock) g_clock->end(c->stream);
-        if (g_clock) g_clock->begin("azimuthal_gemm", c->stream, a.flops);
+    for (int p0 = 0; p0 < a.nb; p0 += bpp) {
+        const int np = std::min(bpp, a.nb - p0);
+        for (int p = p0; p < p0 + np; p++) {
+            if (g_clock) g_clock->begin("azimuthal_transform", c->stream, 2.0 * nblk * (double)H * H * c->ks.nf);
+            launch_azimuthal_blocks(c->ks, c->Q.p + (size_t)(1 + p) * c->ks.nkeys, a.nbar_arc, a.nm, a.npar,
+                                    Sb + (size_t)(p - p0) * nS, c->stream, &c->launches);
+            if (g_clock) g_clock->end(c->stream);
+        }
+        if (g_clock) g_clock->begin("azimuthal_gemm", c->stream, a.flops * np);
         for (int m = 0; m < nblk; m++) {
             const int K = (*a.Km)[m];
             if (K == 0) continue;
             const T* Sm = Sb + (size_t)m * H * H;
             const T* Um = U + (size_t)(*a.base)[m] * H;
-            blas_check(gemm<T>(c->blas, CUBLAS_OP_N, CUBLAS_OP_N, H, K, H, Sm, H, Um, H, Tm, H), "gemm");
-            blas_check(gemm<T>(c->blas, CUBLAS_OP_T, CUBLAS_OP_N, K, K, H, Um, H, Tm, H,
-                               Cm + (size_t)p * a.csize + (*a.off)[m], K),
+            blas_check(gemm_sb<T>(c->blas, CUBLAS_OP_N, CUBLAS_OP_N, H, K, H, Sm, H, (long long)nS, Um, H, 0, Tm, H,
+                                  (long long)nT, np),
+                       "gemm");
+            blas_check(gemm_sb<T>(c->blas, CUBLAS_OP_T, CUBLAS_OP_N, K, K, H, Um, H, 0, Tm, H, (long long)nT,
+                                  Cm + (size_t)p0 * a.csize + (*a.off)[m], K, a.csize, np),
                        "gemm");
             c->launches += 2;
         }
         if (g_clock) g_clock->end(c->stream);
     }
-    launch_azimuthal_scatter(M, a.nb, a.mode_m, a.mode_cls, a.mode_col, c->az_off.p, a.Km_dev, a.csize, Cm, c->Dp.p,
-                             c->stream, &c->launches);
+    return Cm;
 }
 
 // Projection of a full-sky spherical build onto its own azimuthal modes.
@@ -1318,11 +1337,12 @@ void az_blocks(opsec_gpu* c, const AzPlan& a, int M) {
 // order m.  So C_p[i][j] = U_m[:, idx_i]^T S_p(m) U_m[:, idx_j] when modes i
 // and j have the same order m and the same trig class, and 0 otherwise, with
 // S_p(m) the H x H cosine transform of the band table (as for the eigensolve).
-// Per band: the transform (FP64), then for each m two FP64 GEMMs
-// T = S_p(m) U_m and C_m = U_m^T T, then one scatter into the packed triangle.
+// Per band the transform, then per block two GEMMs T = S_p(m) U_m and
+// C_m = U_m^T T (batched over the bands), then one scatter into the packed
+// triangle (or, for the Fisher build, block sums that skip the triangle).
 // Work per band sum_m 2 H^2 K_m + 2 H K_m^2 (K_m distinct block vectors of
 // order m), against 2 N^2 M + N M^2 for the dense projection.
-void project_azimuthal(opsec_gpu* c, int ncells, int M) {
+void project_azimuthal(opsec_gpu* c, int ncells, int M, bool packed) {
     const KeySpace& ks = c->ks;
     const int Nphi = ks.N3, nm = Nphi / 2 + 1, npar = c->az_npar, nblk = nm * npar, H = ks.H / npar;
     const int nb = c->ntab() - 1;
@@ -1378,22 +1398,71 @@ void project_azimuthal(opsec_gpu* c, int ncells, int M) {
     DevBuf<double>& d_nba = c->nba_dev;
     d_nba.alloc(nba.size());
     OPSEC_CUDA(cudaMemcpyAsync(d_nba.p, nba.data(), sizeof(double) * nba.size(), cudaMemcpyHostToDevice, c->stream));
-    const size_t Kp = (size_t)M * (M + 1) / 2;
-    c->Dp.alloc(Kp * nb);
     double fl = 0;
     for (int m = 0; m < nblk; m++) fl += 2.0 * H * H * Km[m] + 2.0 * H * (double)Km[m] * Km[m];
     AzPlan plan{H, nm, npar, nb, ncol, csize, Kmax, fl, d_col_m, d_col_idx, d_mode_m, d_mode_cls, d_mode_col, d_Km, &Km,
                 &base, &off, d_nba.p};
-    if (c->az_gemm64)
-        az_blocks<double>(c, plan, M);
-    else
-        az_blocks<float>(c, plan, M);
+    c->az_blockF = false;
+    if (!packed && !c->az_gemm64) {
+        // the Fisher sums read the block matrices directly: groups (block, trig class)
+        // of ascending modes and their pair counts
+        std::vector<std::vector<int>> gm((size_t)nblk * 2);
+        for (int i = 0; i < M; i++) gm[(size_t)c->az_m[i] * 2 + mode_cls[i]].push_back(i);
+        std::vector<int> g_mode{0}, g_blk, modes;
+        std::vector<long long> g_entry{0};
+        for (size_t g = 0; g < gm.size(); g++) {
+            if (gm[g].empty()) continue;
+            const long long n = (long long)gm[g].size();
+            g_entry.push_back(g_entry.back() + n * (n + 1) / 2);
+            g_blk.push_back((int)(g / 2));
+            modes.insert(modes.end(), gm[g].begin(), gm[g].end());
+            g_mode.push_back((int)modes.size());
+        }
+        const int G = (int)g_blk.size();
+        std::vector<int> bi;
+        bi.insert(bi.end(), g_mode.begin(), g_mode.end());
+        bi.insert(bi.end(), g_blk.begin(), g_blk.end());
+        bi.insert(bi.end(), modes.begin(), modes.end());
+        c->bf_i.alloc(bi.size());
+        OPSEC_CUDA(cudaMemcpyAsync(c->bf_i.p, bi.data(), sizeof(int) * bi.size(), cudaMemcpyHostToDevice, c->stream));
+        c->bf_l.alloc(g_entry.size());
+        OPSEC_CUDA(cudaMemcpyAsync(c->bf_l.p, g_entry.data(), sizeof(long long) * g_entry.size(),
+                                   cudaMemcpyHostToDevice, c->stream));
+        BlockFisherArgs& b = c->bf;
+        b.ngroups = G;
+        b.g_entry = c->bf_l.p;
+        b.g_mode = c->bf_i.p;
+        b.g_blk = c->bf_i.p + (G + 1);
+        b.modes = c->bf_i.p + (G + 1) + G;
+        b.mode_col = d_mode_col;
+        b.Km = d_Km;
+        b.off = c->az_off.p;
+        b.csize = csize;
+        b.C = az_blocks<float>(c, plan);
+        c->bf_entries = g_entry.back();
+        c->az_blockF = true;
+        return;
+    }
+    const size_t Kp = (size_t)M * (M + 1) / 2;
+    c->Dp.alloc(Kp * nb);
+    if (c->az_gemm64) {
+        const double* Cm = az_blocks<double>(c, plan);
+        launch_azimuthal_scatter(M, nb, d_mode_m, d_mode_cls, d_mode_col, c->az_off.p, d_Km, csize, Cm, c->Dp.p,
+                                 c->stream, &c->launches);
+    } else {
+        const float* Cm = az_blocks<float>(c, plan);
+        launch_azimuthal_scatter(M, nb, d_mode_m, d_mode_cls, d_mode_col, c->az_off.p, d_Km, csize, Cm, c->Dp.p,
+                                 c->stream, &c->launches);
+    }
     (void)ncells;
 }
 
-void project_all(opsec_gpu* c, int ncells, int M, bool own_modes) {
+// packed = false: the caller needs only the Fisher sums, which on the azimuthal
+// path then read the block matrices (az_blockF) instead of the packed triangle.
+void project_all(opsec_gpu* c, int ncells, int M, bool own_modes, bool packed = true) {
+    c->az_blockF = false;
     if (own_modes && c->az_valid && (c->projection == "auto" || c->projection == "azimuthal")) {
-        project_azimuthal(c, ncells, M);
+        project_azimuthal(c, ncells, M, packed);
         return;
     }
     if (c->projection == "azimuthal")
@@ -1472,10 +1541,17 @@ void fisher_and_epilogue(opsec_gpu* c, int M, const float* Dp32, const double* D
     a.partial = c->partial.p;
     c->fout.alloc((size_t)nb * nb + 2 * nb);
     a.out = c->fout.p;
-    if (Dp64)
+    if (Dp64) {
         launch_fisher64(a, Dp64, c->stream, &c->launches);
-    else
+    } else if (Dp32) {
         launch_fisher(a, c->stream, &c->launches);
+    } else {
+        if (!c->az_blockF) fail(OPSEC_ERR_ARG, "no derivative matrices for the Fisher sums");
+        a.nblocks = fisher_blocks_for(c->bf_entries);
+        c->partial.alloc((size_t)a.nblocks * nout);
+        a.partial = c->partial.p;
+        launch_fisher_blocks(a, c->bf, c->bf_entries, c->stream, &c->launches);
+    }
     const size_t nrec = (size_t)nb + 4 * (size_t)nb * nb + 2 * nb;
     c->est.alloc(nrec);
     c->status.alloc(1);
@@ -1721,14 +1797,14 @@ int opsec_gpu_fisher_build(opsec_gpu* c, int ncells, const opsec_cell* cells, co
         t.mark();
         int n = eigensolve(c, ncells, cells, nmodes);
         t.mark();
-        project_all(c, ncells, n, true);
+        project_all(c, ncells, n, true, false);
         c->counts.alloc(ncells);
         c->y.alloc(n);
         OPSEC_CUDA(cudaMemcpyAsync(c->counts.p, counts, sizeof(double) * ncells, cudaMemcpyHostToDevice, c->stream));
         launch_dot(ncells, n, c->modes.p, c->counts.p, c->nbar.p, c->y.p, c->stream, &c->launches);
         t.mark();
         if (evals) OPSEC_CUDA(cudaMemcpyAsync(evals, c->evals.p, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
-        fisher_and_epilogue(c, n, c->Dp.p, nullptr, mixing, phat, pcov, F, W, M, q, f);
+        fisher_and_epilogue(c, n, c->az_blockF ? nullptr : c->Dp.p, nullptr, mixing, phat, pcov, F, W, M, q, f);
         t.mark();
         t.finish();
     });
@@ -1758,13 +1834,13 @@ void run_mock(opsec_gpu* w, const opsec_mock& m, size_t i, int nb, double* F, do
     build_tables(w);  // no-op: the tables do not depend on the grid
     build_q(w);
     const int n = eigensolve(w, m.ncells, m.cells, m.nmodes);
-    project_all(w, m.ncells, n, true);
+    project_all(w, m.ncells, n, true, false);
     w->counts.alloc(m.ncells);
     w->y.alloc(n);
     OPSEC_CUDA(cudaMemcpyAsync(w->counts.p, m.counts, sizeof(double) * m.ncells, cudaMemcpyHostToDevice, w->stream));
     launch_dot(m.ncells, n, w->modes.p, w->counts.p, w->nbar.p, w->y.p, w->stream, &w->launches);
     const size_t n2 = (size_t)nb * nb;
-    fisher_and_epilogue(w, n, w->Dp.p, nullptr, OPSEC_MIXING_INVERSE, phat ? phat + i * nb : nullptr,
+    fisher_and_epilogue(w, n, w->az_blockF ? nullptr : w->Dp.p, nullptr, OPSEC_MIXING_INVERSE, phat ? phat + i * nb : nullptr,
                         pcov ? pcov + i * n2 : nullptr, F ? F + i * n2 : nullptr, nullptr, nullptr, nullptr, nullptr);
 }
 }  // namespace

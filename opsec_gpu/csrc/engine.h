@@ -242,7 +242,28 @@ struct FisherArgs {
     double* out;           // [nbands*nbands + 2*nbands]: F, f, q
 };
 int fisher_blocks(int nmodes);
+int fisher_blocks_for(long long entries);
 void launch_fisher(const FisherArgs& a, cudaStream_t s, long long* launches);
+
+// The Fisher sums over the same-group mode pairs of the azimuthal block
+// structure, values read from the per-block matrices C_b of every band (the
+// packed triangle is never formed).  Groups are (block, trig class); their
+// modes ascending; entries of group g are its pairs u <= v, numbered as a
+// packed triangle from g_entry[g].
+struct BlockFisherArgs {
+    int ngroups;
+    const long long* g_entry;  // [ngroups + 1] entry prefix
+    const int* g_mode;         // [ngroups + 1] prefix into modes
+    const int* g_blk;          // [ngroups] block of the group
+    const int* modes;          // [nmodes] mode indices, grouped
+    const int* mode_col;       // [nmodes] column of mode i in its block's C_b
+    const int* Km;             // [nblk] C_b is Km x Km
+    const long long* off;      // [nblk] offset of C_b in one band's array
+    long long csize;           // floats per band
+    const float* C;            // [nbands][csize]
+};
+void launch_fisher_blocks(const FisherArgs& a, const BlockFisherArgs& b, long long entries, cudaStream_t s,
+                          long long* launches);
 
 // Nb x Nb epilogue: mixing, window, estimates, covariance; status word on error.
 void launch_epilogue(int nb, int mixing, const double* Fqf, double* out, int* status, cudaStream_t s,

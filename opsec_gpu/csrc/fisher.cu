@@ -89,18 +89,61 @@ __device__ __forceinline__ int out_index(int row, int col, int nb) {
     return -1;
 }
 
+// Where the entries come from.  An entry is one (i <= j) mode pair: its
+// indices and the position of its value in each band's array.
+//
+// Packed: every pair of the packed upper triangle, D_p at p K + k.
 template <class T>
-__global__ void __launch_bounds__(kMaxThreads) fisher_kernel(int M, int nb, const T* Dp, const double* evals,
-                                                             const double* y, const double* prior, double* partial) {
+struct PackedSource {
+    const T* Dp;
+    long long K;
+    __device__ long long count() const { return K; }
+    __device__ void entry(long long k, int* i, int* j, long long* off) const {
+        unpack(k, i, j);
+        *off = k;
+    }
+    __device__ float value(int p, long long off) const { return (float)Dp[(size_t)p * K + off]; }
+};
+
+// Block: only the pairs whose packed value can be nonzero on the azimuthal
+// path -- both modes in the same (block, trig class) group -- with the value
+// read from the group block's K x K matrix C_b of band p (column j, row i, as
+// the scatter into the packed triangle reads it).
+struct BlockSource {
+    BlockFisherArgs b;
+    __device__ long long count() const { return b.g_entry[b.ngroups]; }
+    __device__ void entry(long long k, int* i, int* j, long long* off) const {
+        int lo = 0, hi = b.ngroups - 1;  // the group holding entry k
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (b.g_entry[mid] <= k) lo = mid;
+            else hi = mid - 1;
+        }
+        int u, v;
+        unpack(k - b.g_entry[lo], &u, &v);
+        const int* md = b.modes + b.g_mode[lo];
+        *i = md[u];
+        *j = md[v];
+        const int blk = b.g_blk[lo];
+        *off = b.off[blk] + (long long)b.mode_col[*j] * b.Km[blk] + b.mode_col[*i];
+    }
+    __device__ float value(int p, long long off) const { return b.C[(size_t)p * b.csize + off]; }
+};
+
+template <class Src>
+__global__ void __launch_bounds__(kMaxThreads) fisher_kernel(Src src, int nb, const double* evals, const double* y,
+                                                             const double* prior, double* partial) {
     extern __shared__ __align__(16) unsigned char fisher_smem[];
     float* hs = reinterpret_cast<float*>(fisher_smem);  // [rows][kStride]
     __shared__ float p_hi[kMaxBands], p_lo[kMaxBands];   // prior p_n = p_hi + p_lo
+    __shared__ int s_i[kChunk], s_j[kChunk];            // the chunk's entries
+    __shared__ long long s_off[kChunk];
     const FisherTiling tl = fisher_tiling(nb);
     for (int n = threadIdx.x; n < nb; n += blockDim.x) {
         p_hi[n] = (float)prior[n];
         p_lo[n] = (float)(prior[n] - (double)p_hi[n]);
     }
-    const long long K = (long long)M * (M + 1) / 2;
+    const long long K = src.count();
     const int nout = nb * (nb + 1) / 2 + 2 * nb;
 
     // this thread's tile (I <= J) and k slice
@@ -131,11 +174,21 @@ __global__ void __launch_bounds__(kMaxThreads) fisher_kernel(int M, int nb, cons
     for (int e = me; e < (tl.rows - nb - 2) * kStride; e += blockDim.x) hs[(size_t)(nb + 2) * kStride + e] = 0.f;
 
     for (long long k0 = (long long)blockIdx.x * kChunk; k0 < K; k0 += (long long)gridDim.x * kChunk) {
+        for (int kk = me; kk < kChunk; kk += blockDim.x) {
+            const long long k = k0 + kk;
+            int i = 0, j = 0;
+            long long off = 0;
+            if (k < K) src.entry(k, &i, &j, &off);
+            s_i[kk] = i;
+            s_j[kk] = j;
+            s_off[kk] = off;
+        }
+        __syncthreads();
         // stage raw D_p[k]
         for (int e = me; e < nb * kChunk; e += blockDim.x) {
             const int p = e / kChunk, kk = e % kChunk;
             const long long k = k0 + kk;
-            hs[p * kStride + kk] = (k < K) ? (float)Dp[(size_t)p * K + k] : 0.f;
+            hs[p * kStride + kk] = (k < K) ? src.value(p, s_off[kk]) : 0.f;
         }
         __syncthreads();
         // per-k weights sqrt(m w_i w_j), residual row R, data row y_i y_j.  R's
@@ -146,8 +199,7 @@ __global__ void __launch_bounds__(kMaxThreads) fisher_kernel(int M, int nb, cons
             const long long k = k0 + kk;
             float sc = 0.f, R = 0.f, yy = 0.f;
             if (k < K) {
-                int i, j;
-                unpack(k, &i, &j);
+                const int i = s_i[kk], j = s_j[kk];
                 const float wi = 1.0f / (1.0f + (float)evals[i]), wj = 1.0f / (1.0f + (float)evals[j]);
                 sc = sqrtf((i == j ? 0.5f : 1.0f) * wi * wj);
                 float rs = 0.f, rc = 0.f;
@@ -433,25 +485,26 @@ __global__ void epilogue_kernel(int nb, int mixing, const double* Fqf, double* o
 
 }  // namespace
 
-int fisher_blocks(int nmodes) {
-    const long long K = (long long)nmodes * (nmodes + 1) / 2;
+int fisher_blocks(int nmodes) { return fisher_blocks_for((long long)nmodes * (nmodes + 1) / 2); }
+
+int fisher_blocks_for(long long K) {
     long long chunks = (K + kChunk - 1) / kChunk;
     long long b = 152LL * 2;
     if (chunks < b) b = chunks;
     return (int)(b < 1 ? 1 : b);
 }
 
-template <class T>
-static void run_fisher(const FisherArgs& a, const T* Dp, cudaStream_t s, long long* launches) {
+template <class Src>
+static void run_fisher(const FisherArgs& a, const Src& src, double K, double elem_bytes, cudaStream_t s,
+                       long long* launches) {
     const int nb = a.nbands;
     const int nout = nb * (nb + 1) / 2 + 2 * nb;
     if (nb > kMaxBands) fail(OPSEC_ERR_ARG, "too many bands for the Fisher kernel (max 88)");
     const FisherTiling tl = fisher_tiling(nb);
-    auto k = fisher_kernel<T>;
+    auto k = fisher_kernel<Src>;
     OPSEC_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem((const void*)k)));
-    const double K = (double)a.nmodes * (a.nmodes + 1) / 2;
-    if (g_clock) g_clock->begin("fisher", s, 2.0 * K * nout, K * nb * sizeof(T));
-    k<<<a.nblocks, tl.threads, tl.smem, s>>>(a.nmodes, nb, Dp, a.evals, a.y, a.prior, a.partial);
+    if (g_clock) g_clock->begin("fisher", s, 2.0 * K * nout, K * nb * elem_bytes);
+    k<<<a.nblocks, tl.threads, tl.smem, s>>>(src, nb, a.evals, a.y, a.prior, a.partial);
     OPSEC_CUDA(cudaGetLastError());
     if (g_clock) g_clock->end(s);
     fisher_reduce_kernel<<<(nout + 255) / 256, 256, 0, s>>>(nb, a.nblocks, a.partial, a.out);
@@ -459,10 +512,19 @@ static void run_fisher(const FisherArgs& a, const T* Dp, cudaStream_t s, long lo
     *launches += 2;
 }
 
-void launch_fisher(const FisherArgs& a, cudaStream_t s, long long* launches) { run_fisher(a, a.Dp, s, launches); }
+void launch_fisher(const FisherArgs& a, cudaStream_t s, long long* launches) {
+    const long long K = (long long)a.nmodes * (a.nmodes + 1) / 2;
+    run_fisher(a, PackedSource<float>{a.Dp, K}, (double)K, sizeof(float), s, launches);
+}
 
 void launch_fisher64(const FisherArgs& a, const double* Dp64, cudaStream_t s, long long* launches) {
-    run_fisher(a, Dp64, s, launches);
+    const long long K = (long long)a.nmodes * (a.nmodes + 1) / 2;
+    run_fisher(a, PackedSource<double>{Dp64, K}, (double)K, sizeof(double), s, launches);
+}
+
+void launch_fisher_blocks(const FisherArgs& a, const BlockFisherArgs& b, long long entries, cudaStream_t s,
+                          long long* launches) {
+    run_fisher(a, BlockSource{b}, (double)entries, sizeof(float), s, launches);
 }
 
 void launch_epilogue(int nb, int mixing, const double* Fqf, double* out, int* status, cudaStream_t s,
@@ -523,14 +585,15 @@ extern "C" int opsec_gpu_fisher_noalloc(int nmodes, int nbands, const float* cov
     if (!g_attr_done[dev]) {
         size_t most = 0;  // the largest request of any band count this entry point accepts
         for (int n = 1; n <= kNoallocMaxBands; n++) most = fisher_tiling(n).smem > most ? fisher_tiling(n).smem : most;
-        if (cudaFuncSetAttribute(fisher_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)most) !=
-            cudaSuccess)
+        if (cudaFuncSetAttribute(fisher_kernel<PackedSource<float>>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)most) != cudaSuccess)
             return OPSEC_ERR_CUDA;
         g_attr_done[dev] = true;
     }
     // every CTA writes all nout partials of its slot, so nothing needs clearing
-    fisher_kernel<float><<<kNoallocBlocks, tl.threads, tl.smem, s>>>(nmodes, nb, cov_packed, evals, y, prior,
-                                                                     g_partial_addr[dev]);
+    const PackedSource<float> src{cov_packed, (long long)nmodes * (nmodes + 1) / 2};
+    fisher_kernel<PackedSource<float>><<<kNoallocBlocks, tl.threads, tl.smem, s>>>(src, nb, evals, y, prior,
+                                                                                   g_partial_addr[dev]);
     fisher_reduce_kernel<<<(nout + 255) / 256, 256, 0, s>>>(nb, kNoallocBlocks, g_partial_addr[dev], out);
     return cudaGetLastError() == cudaSuccess ? OPSEC_OK : OPSEC_ERR_CUDA;
 }
