@@ -67,6 +67,11 @@ struct Lookup {
     float4 kt[kLogN];
 };
 
+// Smallest separation whose table index is b (the QSpline grid: linear below r1, log above).
+__device__ __forceinline__ float bin_edge(const Lookup& lk, int b) {
+    return b <= lk.n1 ? (float)b / lk.inv_dr : lk.r1 * exp2f((float)(b - lk.n1) / lk.inv_du);
+}
+
 template <int NG>
 struct Shape {
     static constexpr int NP = NG * NG * NG;
@@ -592,6 +597,23 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
         for (int pass = 0; pass < npass; pass++) {
             const int s0 = pass * S;
             const int segw = min(S, wl - 1 - s0) + 1;  // bins s0 .. s0 + segw - 1 of the window
+            // With several passes a pair whose plain FP32 r^2 lies well outside the
+            // separations of this pass's bins skips the exact arithmetic: margins of 1e-4
+            // relative plus 0.01 in r cover the rounding of the plain r^2 and of the bin
+            // edges.  The first pass has no lower bound and the last no upper bound, so
+            // pairs outside the whole window still reach the clamp and the violation count.
+            const bool filt = npass > 1 && !periodic;
+            float f_lo = 0.f, f_hi = INFINITY;
+            if (filt) {
+                if (pass > 0) {
+                    const float r = bin_edge(lk, wn.x + s0) * (1.f - 1e-4f) - 0.01f;
+                    f_lo = r > 0.f ? r * r : 0.f;
+                }
+                if (pass < npass - 1) {
+                    const float r = bin_edge(lk, wn.x + s0 + S) * (1.f + 1e-4f) + 0.01f;
+                    f_hi = r * r;
+                }
+            }
             for (int j = lane; j < segw; j += 32) {
                 hh[j] = 0.f;
                 hl[j] = 0.f;
@@ -614,17 +636,20 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
     #pragma unroll 4
                         for (int q = q0; q < q0 + nfl && q < NP; q++) {
                             const float4 B = P2[q];
+                            if (filt) {
+                                const float dx = B.x - ax, dy = B.y - ay, dz = B.z - az;
+                                const float r2a = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                                if (r2a < f_lo || r2a >= f_hi) continue;
+                            }
                             int i;
                             float fr;
                             exact_index(lk, s_ci, s_cf, s_kt, B, P2l[q], ax, alx, ay, aly, az, alz, periodic, Lh, Ll, hL,
                                         i, fr);
                             int bi = i - wn.x;
-                            if (bi < 0 || bi > wl - 2) {  // outside the window: cannot happen for a sound window
-                                bad += pass == 0;
-                                bi = min(max(bi, 0), wl - 2);
-                            }
-                            bi -= s0;
+                            const bool out = bi < 0 || bi > wl - 2;  // outside the window: cannot happen for a sound window
+                            bi = min(max(bi, 0), wl - 2) - s0;
                             if (bi >= 0 && bi < S) {
+                                bad += out;
                                 const float ww = Ah.w * B.w;
                                 atomicAdd(&hp[bi], fmaf(-ww, fr, ww));
                                 atomicAdd(&hp[bi + 1], ww * fr);
