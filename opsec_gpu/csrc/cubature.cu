@@ -541,6 +541,7 @@ template <int NG>
 __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
     cubature_far_kernel(CubatureArgs a, Lookup lk, WinPlan w) {
     constexpr int NP = FarShape<NG>::NP;
+    constexpr int NG2 = NG * NG;
     constexpr int kWarps = FarShape<NG>::kWarps;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int ntab = a.ntab;
@@ -578,14 +579,16 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
         const float4* G1 = a.pts + 2 * NP * cell_id(a.ks, c1);
         const float4* G2 = a.pts + 2 * NP * cell_id(a.ks, c2);
         const float4 Oh = G1[2 * (NP / 2)], Ol = G1[2 * (NP / 2) + 1];
-        for (int q = lane; q < NP; q += 32) {
+        // second-cell points in the order (innermost node l, other nodes): P2[l NG^2 + ij]
+        for (int qq = lane; qq < NP; qq += 32) {
+            const int q = (qq % NG2) * NG + qq / NG2;
             const float4 Bh = G2[2 * q], Bl = G2[2 * q + 1];
             float lx, ly, lz;
             const float sx = diff2(Bh.x, Bl.x, Oh.x, Ol.x, &lx);
             const float sy = diff2(Bh.y, Bl.y, Oh.y, Ol.y, &ly);
             const float sz = diff2(Bh.z, Bl.z, Oh.z, Ol.z, &lz);
-            P2[q] = make_float4(sx, sy, sz, Bh.w);
-            P2l[q] = make_float4(lx, ly, lz, 0.f);
+            P2[qq] = make_float4(sx, sy, sz, Bh.w);
+            P2l[qq] = make_float4(lx, ly, lz, 0.f);
         }
         __syncwarp();
         int bad = 0;
@@ -620,21 +623,34 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
                 hp[j] = 0.f;
             }
             __syncwarp();
-            // every lane runs the same trip counts: the flushes below are warp-wide
+            // Mirror symmetry of the innermost axis (phi on spherical grids, z on Cartesian
+            // ones): the Gauss nodes are symmetric about each cell's centre, so the pair of
+            // innermost nodes (l_p, l_q) and (NG-1-l_q, NG-1-l_p) have the same separation
+            // along it, the same other coordinates and the same weight.  Only pairs with
+            // l_p + l_q <= NG-1 are evaluated, those with l_p + l_q < NG-1 at twice the
+            // weight: 10 of every 16 node pairs for NG = 4.  The lanes take the first-cell
+            // points in the order (l, other nodes), so the lanes of one iteration share
+            // their smallest l_p and the second-cell loop stops at l_q = NG-1-l_p(min).
+            // Every lane runs the same trip counts: the flushes below are warp-wide.
             for (int p0 = 0; p0 < NP; p0 += 32) {
-                const int p = p0 + lane;
-                const bool act = p < NP;
+                const int pp = p0 + lane;
+                const bool act = pp < NP;
+                const int lp = pp / NG2;
+                const int p = (pp % NG2) * NG + lp;
                 const float4 Ah = act ? G1[2 * p] : make_float4(0.f, 0.f, 0.f, 0.f);
                 const float4 Al = act ? G1[2 * p + 1] : make_float4(0.f, 0.f, 0.f, 0.f);
                 float alx, aly, alz;
                 const float ax = diff2(Ah.x, Al.x, Oh.x, Ol.x, &alx);
                 const float ay = diff2(Ah.y, Al.y, Oh.y, Ol.y, &aly);
                 const float az = diff2(Ah.z, Al.z, Oh.z, Ol.z, &alz);
+                const int qend = (NG - p0 / NG2) * NG2;  // second-cell points with l_q <= NG-1-l_p(min)
                 const int nfl = w.flush > 0 ? w.flush : NP;
-                for (int q0 = 0; q0 < NP; q0 += nfl) {
+                for (int q0 = 0; q0 < qend; q0 += nfl) {
                     if (act) {
-    #pragma unroll 4
-                        for (int q = q0; q < q0 + nfl && q < NP; q++) {
+#pragma unroll 4
+                        for (int q = q0; q < q0 + nfl && q < qend; q++) {
+                            const int lsum = lp + q / NG2;
+                            if (lsum > NG - 1) continue;  // the mirror image of an evaluated pair
                             const float4 B = P2[q];
                             if (filt) {
                                 const float dx = B.x - ax, dy = B.y - ay, dz = B.z - az;
@@ -650,7 +666,7 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
                             bi = min(max(bi, 0), wl - 2) - s0;
                             if (bi >= 0 && bi < S) {
                                 bad += out;
-                                const float ww = Ah.w * B.w;
+                                const float ww = (lsum < NG - 1 ? 2.f : 1.f) * Ah.w * B.w;
                                 atomicAdd(&hp[bi], fmaf(-ww, fr, ww));
                                 atomicAdd(&hp[bi + 1], ww * fr);
                             }
