@@ -686,26 +686,35 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
                 }
             }
             __syncwarp();
-            for (int t = lane; t < ntab; t += 32) {
-                const float* tr = w.tabT + (size_t)(wn.x + s0) * ntab + t;
+            // the histogram as FP32 values once (hp is zero after the last flush)
+            if (w.flush && !w.dot64)
+                for (int b = lane; b < segw; b += 32) hp[b] = hh[b] + hl[b];
+            __syncwarp();
+            // Dot products: two work items per table, alternate chunks of 8 bins, spread
+            // over the lanes (table t: items 2t and 2t+1 on neighbouring lanes, combined by
+            // one shuffle); FP32 within a chunk, FP64 across chunks.
+            for (int base = 0; base < 2 * ntab; base += 32) {
+                const int it = base + lane;
+                const int t = it >> 1, h = it & 1;
                 double acc = 0.0;
-                if (w.flush && w.dot64) {
-                    for (int b = 0; b < segw; b++) acc = fma((double)tr[(size_t)b * ntab], (double)hh[b] + hl[b], acc);
-                } else if (w.flush) {
-                    for (int b0 = 0; b0 < segw; b0 += 8) {
-                        float pt = 0.f;
-                        for (int b = b0; b < min(b0 + 8, segw); b++) pt = fmaf(tr[(size_t)b * ntab], hh[b] + hl[b], pt);
-                        acc += (double)pt;
-                    }
-                } else {
-                    for (int b0 = 0; b0 < segw; b0 += 8) {
-                        float pt = 0.f;
-                        for (int b = b0; b < min(b0 + 8, segw); b++) pt = fmaf(tr[(size_t)b * ntab], hp[b], pt);
-                        acc += (double)pt;
+                if (it < 2 * ntab) {
+                    const float* tr = w.tabT + (size_t)(wn.x + s0) * ntab + t;
+                    for (int b0 = 8 * h; b0 < segw; b0 += 16) {
+                        const int b1 = min(b0 + 8, segw);
+                        if (w.flush && w.dot64) {
+                            for (int b = b0; b < b1; b++) acc = fma((double)tr[(size_t)b * ntab], (double)hh[b] + hl[b], acc);
+                        } else {
+                            float pt = 0.f;
+                            for (int b = b0; b < b1; b++) pt = fmaf(tr[(size_t)b * ntab], hp[b], pt);
+                            acc += (double)pt;
+                        }
                     }
                 }
-                double* q = a.Q + (size_t)t * a.ks.nkeys + key;
-                *q = pass == 0 ? acc : *q + acc;
+                acc += __shfl_xor_sync(0xffffffffu, acc, 1);
+                if (it < 2 * ntab && h == 0) {
+                    double* q = a.Q + (size_t)t * a.ks.nkeys + key;
+                    *q = pass == 0 ? acc : *q + acc;
+                }
             }
             __syncwarp();
         }
