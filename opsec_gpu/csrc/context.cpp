@@ -298,6 +298,7 @@ struct opsec_gpu {
     bool az_parity = true;
     bool az_batched = true;
     int az_streams = 6;
+    int az_split = 1;  // batched eigensolve calls in flight at once
     int az_npar = 1;
     std::vector<double> pk_k, pk_P;
     std::vector<double> band_lo, band_hi;
@@ -547,6 +548,10 @@ void configure(opsec_gpu* c, const std::map<std::string, std::string>& kv) {
         const std::string& v = get("azimuthal.eig");
         if (v != "streams" && v != "batched") fail(OPSEC_ERR_CONFIG, "azimuthal.eig must be streams or batched");
         c->az_batched = v == "batched";
+    }
+    if (has("azimuthal.split")) {
+        c->az_split = to_int("azimuthal.split", get("azimuthal.split"));
+        if (c->az_split < 1 || c->az_split > opsec_gpu::kSide) fail(OPSEC_ERR_CONFIG, "azimuthal.split must be in [1, 16]");
     }
     if (has("azimuthal.streams")) {
         c->az_streams = to_int("azimuthal.streams", get("azimuthal.streams"));
@@ -1127,20 +1132,54 @@ int eigensolve(opsec_gpu* c, int ncells, const opsec_cell* cells, int M) {
                      "syevd_bufferSize");
         bool batched_done = false;
         if (c->az_batched) {
-            // one batched call over the equal-size blocks; streams of single solves if it is refused
+            // Batched calls over the equal-size blocks, `azimuthal.split` of them on side
+            // streams at once (each is a chain of small launches, mostly latency); streams of
+            // single solves if a batched call is refused.
+            const int nsplit = std::max(1, std::min(c->az_split, nblk));
             cusolverDnParams_t prm = nullptr;
             solver_check(cusolverDnCreateParams(&prm), "cusolverDnCreateParams");
-            size_t dbytes = 0, hbytes = 0;
-            cusolverStatus_t st = cusolverDnXsyevBatched_bufferSize(
-                c->solver, prm, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, Hb, CUDA_R_64F, c->S.p, Hb,
-                CUDA_R_64F, c->W.p, CUDA_R_64F, &dbytes, &hbytes, nblk);
+            std::vector<cusolverDnHandle_t> hs(nsplit, c->solver);
+            if (nsplit > 1) {
+                for (int j = 0; j < nsplit; j++) {
+                    if (!c->side[j]) OPSEC_CUDA(cudaStreamCreateWithFlags(&c->side[j], cudaStreamNonBlocking));
+                    if (!c->side_solver[j]) solver_check(cusolverDnCreate(&c->side_solver[j]), "cusolverDnCreate");
+                    solver_check(cusolverDnSetStream(c->side_solver[j], c->side[j]), "cusolverDnSetStream");
+                    hs[j] = c->side_solver[j];
+                }
+                for (int j = 0; j <= nsplit; j++)
+                    if (!c->side_ev[j]) OPSEC_CUDA(cudaEventCreateWithFlags(&c->side_ev[j], cudaEventDisableTiming));
+            }
+            std::vector<int> b0(nsplit + 1);
+            for (int j = 0; j <= nsplit; j++) b0[j] = (int)((long long)j * nblk / nsplit);
+            std::vector<size_t> dbytes(nsplit, 0), hbytes(nsplit, 0), doff(nsplit + 1, 0);
+            cusolverStatus_t st = CUSOLVER_STATUS_SUCCESS;
+            for (int j = 0; j < nsplit && st == CUSOLVER_STATUS_SUCCESS; j++) {
+                st = cusolverDnXsyevBatched_bufferSize(hs[j], prm, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER,
+                                                       Hb, CUDA_R_64F, c->S.p + (size_t)b0[j] * Hb * Hb, Hb,
+                                                       CUDA_R_64F, c->W.p + (size_t)b0[j] * Hb, CUDA_R_64F,
+                                                       &dbytes[j], &hbytes[j], b0[j + 1] - b0[j]);
+                doff[j + 1] = doff[j] + ((std::max<size_t>(dbytes[j], 1) + 255) & ~size_t(255));
+            }
             if (st == CUSOLVER_STATUS_SUCCESS) {
                 DevBuf<unsigned char>& dw = c->syev_ws;
-                dw.alloc(std::max<size_t>(dbytes, 1));
-                std::vector<unsigned char> hw(std::max<size_t>(hbytes, 1));
-                st = cusolverDnXsyevBatched(c->solver, prm, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, Hb,
-                                            CUDA_R_64F, c->S.p, Hb, CUDA_R_64F, c->W.p, CUDA_R_64F, dw.p, dbytes,
-                                            hw.data(), hbytes, c->info.p, nblk);
+                dw.alloc(doff[nsplit]);
+                std::vector<std::vector<unsigned char>> hw(nsplit);
+                if (nsplit > 1) {
+                    OPSEC_CUDA(cudaEventRecord(c->side_ev[nsplit], c->stream));
+                    for (int j = 0; j < nsplit; j++) OPSEC_CUDA(cudaStreamWaitEvent(c->side[j], c->side_ev[nsplit], 0));
+                }
+                for (int j = 0; j < nsplit && st == CUSOLVER_STATUS_SUCCESS; j++) {
+                    hw[j].resize(std::max<size_t>(hbytes[j], 1));
+                    st = cusolverDnXsyevBatched(hs[j], prm, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, Hb,
+                                                CUDA_R_64F, c->S.p + (size_t)b0[j] * Hb * Hb, Hb, CUDA_R_64F,
+                                                c->W.p + (size_t)b0[j] * Hb, CUDA_R_64F, dw.p + doff[j], dbytes[j],
+                                                hw[j].data(), hbytes[j], c->info.p + b0[j], b0[j + 1] - b0[j]);
+                }
+                if (nsplit > 1)
+                    for (int j = 0; j < nsplit; j++) {
+                        OPSEC_CUDA(cudaEventRecord(c->side_ev[j], c->side[j]));
+                        OPSEC_CUDA(cudaStreamWaitEvent(c->stream, c->side_ev[j], 0));
+                    }
                 sync(c);
             }
             cusolverDnDestroyParams(prm);
