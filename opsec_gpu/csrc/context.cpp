@@ -5,6 +5,7 @@
 #include <cusolverDn.h>
 
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <chrono>
 #include <cerrno>
@@ -299,6 +300,11 @@ struct opsec_gpu {
     bool az_batched = true;
     int az_streams = 6;
     int az_split = 1;  // batched eigensolve calls in flight at once
+    // the batched eigensolve as a CUDA graph, for builds that repeat the shapes and buffers
+    bool eig_graph_ok = true;
+    std::array<size_t, 6> eig_key{};
+    cudaGraphExec_t eig_exec = nullptr;
+    std::vector<unsigned char> eig_hw;  // the captured call's host workspace
     int az_npar = 1;
     std::vector<double> pk_k, pk_P;
     std::vector<double> band_lo, band_hi;
@@ -1096,6 +1102,14 @@ void check_info(opsec_gpu* c, int count) {
 }
 
 // Top-M eigenpairs of S into c->evals / c->modes (mode-major).  Returns nconv.
+// Forget the captured batched eigensolve: called before any other solver call on the
+// context, which may move the library's internal buffers the graph refers to.
+void drop_eig_graph(opsec_gpu* c) {
+    if (c->eig_exec) cudaGraphExecDestroy(c->eig_exec);
+    c->eig_exec = nullptr;
+    c->eig_key = {};
+}
+
 int eigensolve(opsec_gpu* c, int ncells, const opsec_cell* cells, int M) {
     build_q(c);
     load_cells(c, ncells, cells);
@@ -1168,12 +1182,47 @@ int eigensolve(opsec_gpu* c, int ncells, const opsec_cell* cells, int M) {
                     OPSEC_CUDA(cudaEventRecord(c->side_ev[nsplit], c->stream));
                     for (int j = 0; j < nsplit; j++) OPSEC_CUDA(cudaStreamWaitEvent(c->side[j], c->side_ev[nsplit], 0));
                 }
-                for (int j = 0; j < nsplit && st == CUSOLVER_STATUS_SUCCESS; j++) {
-                    hw[j].resize(std::max<size_t>(hbytes[j], 1));
-                    st = cusolverDnXsyevBatched(hs[j], prm, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, Hb,
-                                                CUDA_R_64F, c->S.p + (size_t)b0[j] * Hb * Hb, Hb, CUDA_R_64F,
-                                                c->W.p + (size_t)b0[j] * Hb, CUDA_R_64F, dw.p + doff[j], dbytes[j],
-                                                hw[j].data(), hbytes[j], c->info.p + b0[j], b0[j + 1] - b0[j]);
+                auto solve = [&](int j, std::vector<unsigned char>& host) {
+                    host.resize(std::max<size_t>(hbytes[j], 1));
+                    return cusolverDnXsyevBatched(hs[j], prm, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, Hb,
+                                                  CUDA_R_64F, c->S.p + (size_t)b0[j] * Hb * Hb, Hb, CUDA_R_64F,
+                                                  c->W.p + (size_t)b0[j] * Hb, CUDA_R_64F, dw.p + doff[j], dbytes[j],
+                                                  host.data(), hbytes[j], c->info.p + b0[j], b0[j + 1] - b0[j]);
+                };
+                // One call is a chain of thousands of small launches, bound by their host-side
+                // cost.  When a build repeats the previous one's shapes and buffers, the call is
+                // captured once into a CUDA graph and replayed; a capture the library refuses
+                // (a host synchronisation inside) falls back to the direct call for good.
+                const std::array<size_t, 6> key{(size_t)Hb, (size_t)nblk, (size_t)c->S.p, (size_t)c->W.p,
+                                                (size_t)c->info.p, (size_t)dw.p};
+                bool done = false;
+                if (nsplit == 1 && c->eig_graph_ok && key == c->eig_key) {
+                    if (!c->eig_exec) {
+                        cudaGraph_t g = nullptr;
+                        cudaError_t ce = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
+                        cusolverStatus_t cst = CUSOLVER_STATUS_INTERNAL_ERROR;
+                        if (ce == cudaSuccess) {
+                            cst = solve(0, c->eig_hw);  // kept while the graph lives: it may read it
+                            ce = cudaStreamEndCapture(c->stream, &g);
+                        }
+                        if (ce == cudaSuccess && cst == CUSOLVER_STATUS_SUCCESS && g)
+                            ce = cudaGraphInstantiate(&c->eig_exec, g, 0);
+                        if (g) cudaGraphDestroy(g);
+                        if (ce != cudaSuccess || cst != CUSOLVER_STATUS_SUCCESS) {
+                            (void)cudaGetLastError();
+                            c->eig_exec = nullptr;
+                            c->eig_graph_ok = false;
+                        }
+                    }
+                    if (c->eig_exec) {
+                        OPSEC_CUDA(cudaGraphLaunch(c->eig_exec, c->stream));
+                        done = true;
+                    }
+                }
+                if (!done) {
+                    if (key != c->eig_key) drop_eig_graph(c);
+                    for (int j = 0; j < nsplit && st == CUSOLVER_STATUS_SUCCESS; j++) st = solve(j, hw[j]);
+                    c->eig_key = key;
                 }
                 if (nsplit > 1)
                     for (int j = 0; j < nsplit; j++) {
@@ -1189,6 +1238,7 @@ int eigensolve(opsec_gpu* c, int ncells, const opsec_cell* cells, int M) {
         }
         // the block eigenproblems are independent: spread them over side streams
         const int ns = batched_done ? 0 : std::min(nblk, c->az_streams);
+        if (ns > 0) drop_eig_graph(c);
         c->work.alloc((size_t)lwork * std::max(ns, 1));
         for (int j = 0; j < ns; j++) {
             if (!c->side[j]) OPSEC_CUDA(cudaStreamCreateWithFlags(&c->side[j], cudaStreamNonBlocking));
@@ -1264,6 +1314,7 @@ int eigensolve(opsec_gpu* c, int ncells, const opsec_cell* cells, int M) {
         c->az_valid = true;
         return M;
     }
+    drop_eig_graph(c);
     // dense path: S in FP64, top-M by syevdx (klt.cpp:173-248 via PARPACK there)
     const int N = ncells;
     c->S.alloc((size_t)N * N);
@@ -2055,6 +2106,7 @@ void opsec_gpu_destroy(opsec_gpu* c) {
     if (!c) return;
     if (c->device >= 0) cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->eig_exec) cudaGraphExecDestroy(c->eig_exec);
     if (c->solver) cusolverDnDestroy(c->solver);
     if (c->blas) cublasDestroy(c->blas);
     for (int j = 0; j < opsec_gpu::kSide; j++) {
