@@ -140,6 +140,9 @@ __device__ __forceinline__ float diff2(float bh, float bl, float ah, float al, f
     return s;
 }
 
+__device__ __forceinline__ void index_r2(const Lookup& lk, const int* s_ci, const float* s_cf, const float4* s_kt,
+                                         float r2, float r2l, int& i, float& fr);
+
 // Table index (i, fr) of one point pair in exact mode: separation and r^2
 // as FP32 pairs, log2(r^2) split as E + log2(T_k) + log2(1 + delta).
 __device__ __forceinline__ void exact_index(const Lookup& lk, const int* s_ci, const float* s_cf, const float4* s_kt,
@@ -166,6 +169,12 @@ __device__ __forceinline__ void exact_index(const Lookup& lk, const int* s_ci, c
     const float r2 = two_sum(h1, pz, &e2);
     float r2l = fmaf(dx, dx, -px) + fmaf(dy, dy, -py) + fmaf(dz, dz, -pz) + (e1 + e2);
     r2l = fmaf(2.f * dx, lx, fmaf(2.f * dy, ly, fmaf(2.f * dz, lz, r2l)));
+    index_r2(lk, s_ci, s_cf, s_kt, r2, r2l, i, fr);
+}
+
+// Table index (i, fr) of a separation given as r^2 = r2 + r2l (an FP32 pair).
+__device__ __forceinline__ void index_r2(const Lookup& lk, const int* s_ci, const float* s_cf, const float4* s_kt,
+                                         float r2, float r2l, int& i, float& fr) {
     if (r2 < lk.r1sq) {
         // t = r n1 / r1 with r = rh + rl and n1 / r1 = inv_dr + inv_dr_lo; the
         // fraction is formed from the exact residual of the rounded product
@@ -400,7 +409,49 @@ struct WinPlan {
     int* violations;  // pairs that fell outside their key's window (must stay 0)
     float4* cen;      // per cell: bounding-sphere centre and radius
     float* tabT;      // [nx][ntab]: the FP32 tables transposed, bin-major
+    // spherical grids (see cubature_far_sph_kernel)
+    float4* arc;      // [H][ng^2]: rho hi, rho lo, z hi, z lo of node pair P = i_r ng + i_mu
+    float* wrm;       // [ng^2]: w_r w_mu of node pair P
+    float4* sph;      // [nf][ng(ng+1)/2]: sin^2(theta/2) hi, lo, phi-node weight (x2 off the diagonal), 0
 };
+
+// Tables of the spherical window kernel, from the cubature nodes (FP64 products,
+// split into FP32 pairs).  Canonical phi-node pairs (l_p, l_q), l_p + l_q <= ng-1,
+// in the order l_p, then l_q.
+__global__ void sph_tables_kernel(CubatureArgs a, WinPlan w) {
+    const int ng = a.ng, ng2 = ng * ng, nc = ng * (ng + 1) / 2;
+    const long long narc = (long long)a.ks.H * ng2;
+    const long long nsph = (long long)a.ks.nf * nc;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < narc + ng2 + nsph;
+         e += (long long)gridDim.x * blockDim.x) {
+        if (e < narc) {
+            const int h = (int)(e / ng2), P = (int)(e % ng2);
+            const int d1 = h / a.ks.N2, d2 = h % a.ks.N2, ir = P / ng, im = P % ng;
+            const double r = a.node1[d1 * ng + ir];
+            const double rho = r * a.snode2[d2 * ng + im], z = r * a.node2[d2 * ng + im];
+            const float rh = (float)rho, zh = (float)z;
+            w.arc[e] = make_float4(rh, (float)(rho - (double)rh), zh, (float)(z - (double)zh));
+        } else if (e < narc + ng2) {
+            const int P = (int)(e - narc);
+            w.wrm[P] = (float)(a.w[P / ng] * a.w[P % ng]);
+        } else {
+            const long long t = e - narc - ng2;
+            const int df = (int)(t / nc);
+            int c = (int)(t % nc), lp = 0;
+            while (c >= ng - lp) {
+                c -= ng - lp;
+                ++lp;
+            }
+            const int lq = c;
+            // chord of the two phi nodes' unit vectors: |e_q - e_p| = 2 sin(theta / 2)
+            const double dc = a.cphi[df * ng + lq] - a.cphi[lp], ds = a.sphi[df * ng + lq] - a.sphi[lp];
+            const double s2 = 0.25 * (dc * dc + ds * ds);
+            const float sh = (float)s2;
+            const double wphi = a.w[lp] * a.w[lq] * (lp + lq < ng - 1 ? 2.0 : 1.0);
+            w.sph[t] = make_float4(sh, (float)(s2 - (double)sh), (float)wphi, 0.f);
+        }
+    }
+}
 
 // The tables bin-major, so that the lanes of a warp (one table each) read one
 // bin of every table with one coalesced load.
@@ -722,6 +773,170 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
     }
 }
 
+// Spherical grids.  A point of node pair P = (i_r, i_mu) and phi node l sits at
+// rho = r sqrt(1 - mu^2), z = r mu, angle phi_l, so for the pair (P of arc h_a,
+// l_p) and (Q of arc h_b, l_q)
+//   r^2 = (rho_P - rho_Q)^2 + (z_P - z_Q)^2 + 4 rho_P rho_Q sin^2(theta / 2),
+// theta the angle between the two phi nodes (cells df apart): three
+// non-negative terms, no cancellation.  The first two and 4 rho_P rho_Q are FP32
+// pairs formed once per (P, Q) -- one lane each -- and every canonical
+// phi-node pair then costs one FP32-pair product and a two-sum; the mirror
+// symmetry of the phi nodes is in the table of sin^2(theta / 2) (10 canonical
+// pairs of 16 for ng = 4, weighted 2 below the diagonal).  Histograms, flushes,
+// passes and dot products as in cubature_far_kernel.
+template <int NG>
+__global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
+    cubature_far_sph_kernel(CubatureArgs a, Lookup lk, WinPlan w) {
+    constexpr int NG2 = NG * NG;
+    constexpr int NC = NG * (NG + 1) / 2;
+    constexpr int kWarps = FarShape<NG>::kWarps;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int ntab = a.ntab;
+    float4* sphw = reinterpret_cast<float4*>(smem_raw);        // [kWarps][NC]: the key's phi-node pairs
+    float* mhi = reinterpret_cast<float*>(sphw + kWarps * NC);  // [kWarps][Wkey]: histogram, high part
+    float* mlo = mhi + kWarps * w.Wkey;                         // [kWarps][Wkey]: low part
+    float* part = mlo + kWarps * w.Wkey;                        // [kWarps][Wkey]: FP32 sums between flushes
+    __shared__ int s_ci[kMaxExp];
+    __shared__ float s_cf[kMaxExp];
+    __shared__ float4 s_kt[kLogN];
+    __shared__ float s_wrm[NG2];
+    for (int i = threadIdx.x; i < lk.ne; i += blockDim.x) {
+        s_ci[i] = lk.ci[i];
+        s_cf[i] = lk.cf[i];
+    }
+    for (int i = threadIdx.x; i < kLogN; i += blockDim.x) s_kt[i] = lk.kt[i];
+    for (int i = threadIdx.x; i < NG2; i += blockDim.x) s_wrm[i] = w.wrm[i];
+    __syncthreads();
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float4* SP = sphw + warp * NC;
+    float* hh = mhi + warp * w.Wkey;
+    float* hl = mlo + warp * w.Wkey;
+    float* hp = part + warp * w.Wkey;
+    const int nfar = *w.nfar;
+    for (int kk = blockIdx.x * kWarps + warp; kk < nfar; kk += gridDim.x * kWarps) {
+        const int key = w.order[kk];
+        const int2 wn = w.win[key];
+        const int wl = wn.y;
+        int c1[3], c2[3];
+        decode_key(a.ks, key, c1, c2);
+        const int ha = c1[0] * a.ks.N2 + c1[1], hb = c2[0] * a.ks.N2 + c2[1], df = c2[2];
+        for (int c = lane; c < NC; c += 32) SP[c] = w.sph[(size_t)df * NC + c];
+        const float4* AA = w.arc + (size_t)ha * NG2;
+        const float4* AB = w.arc + (size_t)hb * NG2;
+        __syncwarp();
+        int bad = 0;
+        const int S = w.Wkey - 1;
+        const int npass = (wl - 1 + S - 1) / S;
+        for (int pass = 0; pass < npass; pass++) {
+            const int s0 = pass * S;
+            const int segw = min(S, wl - 1 - s0) + 1;
+            const bool filt = npass > 1;
+            float f_lo = 0.f, f_hi = INFINITY;
+            if (filt) {
+                if (pass > 0) {
+                    const float r = bin_edge(lk, wn.x + s0) * (1.f - 1e-4f) - 0.01f;
+                    f_lo = r > 0.f ? r * r : 0.f;
+                }
+                if (pass < npass - 1) {
+                    const float r = bin_edge(lk, wn.x + s0 + S) * (1.f + 1e-4f) + 0.01f;
+                    f_hi = r * r;
+                }
+            }
+            for (int j = lane; j < segw; j += 32) {
+                hh[j] = 0.f;
+                hl[j] = 0.f;
+                hp[j] = 0.f;
+            }
+            __syncwarp();
+            // lanes take the (P, Q) node pairs; every lane runs the same trip counts
+            for (int c0 = 0; c0 < NG2 * NG2; c0 += 32) {
+                const int c = c0 + lane;
+                if (c < NG2 * NG2) {
+                    const int P = c / NG2, Q = c % NG2;
+                    const float4 A = AA[P], B = AB[Q];
+                    float rl, zl;
+                    const float dr = diff2(B.x, B.y, A.x, A.y, &rl);
+                    const float dz = diff2(B.z, B.w, A.z, A.w, &zl);
+                    // D = dr^2 + dz^2 and B4 = 4 rho_P rho_Q as FP32 pairs
+                    const float pr = __fmul_rn(dr, dr), pz = __fmul_rn(dz, dz);
+                    float e1;
+                    const float Dh = two_sum(pr, pz, &e1);
+                    const float Dl = fmaf(dr, dr, -pr) + fmaf(dz, dz, -pz) + e1 + fmaf(2.f * dr, rl, 2.f * dz * zl);
+                    const float t0 = __fmul_rn(A.x, B.x);
+                    const float B4h = 4.f * t0;
+                    const float B4l = 4.f * (fmaf(A.x, B.x, -t0) + fmaf(A.x, B.y, A.y * B.x));
+                    const float wpq = s_wrm[P] * s_wrm[Q];
+#pragma unroll
+                    for (int j = 0; j < NC; j++) {
+                        const float4 sp = SP[j];
+                        if (filt) {
+                            const float r2a = fmaf(B4h, sp.x, Dh);
+                            if (r2a < f_lo || r2a >= f_hi) continue;
+                        }
+                        const float t = __fmul_rn(B4h, sp.x);
+                        const float tl = fmaf(B4h, sp.x, -t) + fmaf(B4h, sp.y, B4l * sp.x);
+                        float e;
+                        const float r2 = two_sum(Dh, t, &e);
+                        const float r2l = e + Dl + tl;
+                        int i;
+                        float fr;
+                        index_r2(lk, s_ci, s_cf, s_kt, r2, r2l, i, fr);
+                        int bi = i - wn.x;
+                        const bool out = bi < 0 || bi > wl - 2;  // outside the window: cannot happen for a sound window
+                        bi = min(max(bi, 0), wl - 2) - s0;
+                        if (bi >= 0 && bi < S) {
+                            bad += out;
+                            const float ww = wpq * sp.z;
+                            atomicAdd(&hp[bi], fmaf(-ww, fr, ww));
+                            atomicAdd(&hp[bi + 1], ww * fr);
+                        }
+                    }
+                }
+                if (w.flush) {
+                    __syncwarp();
+                    for (int b = lane; b < segw; b += 32) {
+                        float e;
+                        hh[b] = two_sum(hh[b], hp[b], &e);
+                        hl[b] += e;
+                        hp[b] = 0.f;
+                    }
+                    __syncwarp();
+                }
+            }
+            __syncwarp();
+            if (w.flush && !w.dot64)
+                for (int b = lane; b < segw; b += 32) hp[b] = hh[b] + hl[b];
+            __syncwarp();
+            for (int base = 0; base < 2 * ntab; base += 32) {
+                const int it = base + lane;
+                const int t = it >> 1, h = it & 1;
+                double acc = 0.0;
+                if (it < 2 * ntab) {
+                    const float* tr = w.tabT + (size_t)(wn.x + s0) * ntab + t;
+                    for (int b0 = 8 * h; b0 < segw; b0 += 16) {
+                        const int b1 = min(b0 + 8, segw);
+                        if (w.flush && w.dot64) {
+                            for (int b = b0; b < b1; b++) acc = fma((double)tr[(size_t)b * ntab], (double)hh[b] + hl[b], acc);
+                        } else {
+                            float pt = 0.f;
+                            for (int b = b0; b < b1; b++) pt = fmaf(tr[(size_t)b * ntab], hp[b], pt);
+                            acc += (double)pt;
+                        }
+                    }
+                }
+                acc += __shfl_xor_sync(0xffffffffu, acc, 1);
+                if (it < 2 * ntab && h == 0) {
+                    double* q = a.Q + (size_t)t * a.ks.nkeys + key;
+                    *q = pass == 0 ? acc : *q + acc;
+                }
+            }
+            __syncwarp();
+        }
+        if (bad) atomicAdd(w.violations, bad);
+    }
+}
+
 // keys the cubature integrates (the others are copied by the reflection fill)
 double canonical_keys(const KeySpace& ks) {
     if (!(ks.coordsys == 2 && ks.mu_reflect)) return (double)ks.nkeys;
@@ -805,9 +1020,9 @@ size_t cubature_point_count(const KeySpace& ks, int ng) {
 namespace {
 // scratch layout of the window path
 struct WinLayout {
-    size_t win, order, count, cursor, scal, cen, tabT, total;
+    size_t win, order, count, cursor, scal, cen, tabT, arc, wrm, sph, total;
 };
-WinLayout win_layout(const KeySpace& ks, int nx, int ntab) {
+WinLayout win_layout(const KeySpace& ks, int nx, int ntab, int ng) {
     auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
     const size_t ncell = (size_t)ks.N1 * ks.N2 * ks.N3;
     WinLayout L;
@@ -818,14 +1033,18 @@ WinLayout win_layout(const KeySpace& ks, int nx, int ntab) {
     L.scal = L.cursor + al(sizeof(int) * (nx + 2));
     L.cen = L.scal + 256;
     L.tabT = L.cen + al(sizeof(float4) * ncell);
-    L.total = L.tabT + al(sizeof(float) * (size_t)nx * ntab);
+    L.arc = L.tabT + al(sizeof(float) * (size_t)nx * ntab);
+    const bool sph = ks.coordsys == 2;
+    L.wrm = L.arc + (sph ? al(sizeof(float4) * (size_t)ks.H * ng * ng) : 0);
+    L.sph = L.wrm + (sph ? al(sizeof(float) * (size_t)ng * ng) : 0);
+    L.total = L.sph + (sph ? al(sizeof(float4) * (size_t)ks.nf * (ng * (ng + 1) / 2)) : 0);
     return L;
 }
 
 template <int NG>
-size_t far_smem(const WinPlan& w) {
-    return sizeof(float4) * FarShape<NG>::kWarps * 2 * FarShape<NG>::NP +
-           3 * sizeof(float) * FarShape<NG>::kWarps * w.Wkey;
+size_t far_smem(const WinPlan& w, bool sph) {
+    const size_t pts = sph ? sizeof(float4) * (NG * (NG + 1) / 2) : sizeof(float4) * 2 * FarShape<NG>::NP;
+    return FarShape<NG>::kWarps * (pts + 3 * sizeof(float) * w.Wkey);
 }
 
 // Far keys by windows, near keys by table groups in list mode.  Returns false (nothing
@@ -839,9 +1058,11 @@ bool run_window(const CubatureArgs& a, const Lookup& lk, cudaStream_t s, long lo
     w.Wmax = std::min(kMaxPasses * (w.Wkey - 1) + 1, nx);
     w.flush = a.win_flush;
     w.dot64 = a.win_dot64;
-    if (w.Wkey < 8 || far_smem<NG>(w) > (size_t)max_dynamic_smem((const void*)cubature_far_kernel<NG>)) return false;
+    const bool sph = a.coordsys == 2;
+    const void* kfn = sph ? (const void*)cubature_far_sph_kernel<NG> : (const void*)cubature_far_kernel<NG>;
+    if (w.Wkey < 8 || far_smem<NG>(w, sph) > (size_t)max_dynamic_smem(kfn)) return false;
     w.nbucket = nx + 1;
-    const WinLayout L = win_layout(a.ks, nx, a.ntab);
+    const WinLayout L = win_layout(a.ks, nx, a.ntab, a.ng);
     if (!a.work || a.work_bytes < L.total) fail(OPSEC_ERR_ARG, "cubature scratch too small");
     unsigned char* base = static_cast<unsigned char*>(a.work);
     w.win = reinterpret_cast<int2*>(base + L.win);
@@ -854,6 +1075,11 @@ bool run_window(const CubatureArgs& a, const Lookup& lk, cudaStream_t s, long lo
     w.violations = scal + 2;
     w.cen = reinterpret_cast<float4*>(base + L.cen);
     w.tabT = reinterpret_cast<float*>(base + L.tabT);
+    if (sph) {
+        w.arc = reinterpret_cast<float4*>(base + L.arc);
+        w.wrm = reinterpret_cast<float*>(base + L.wrm);
+        w.sph = reinterpret_cast<float4*>(base + L.sph);
+    }
     OPSEC_CUDA(cudaMemsetAsync(w.count, 0, sizeof(int) * (nx + 2), s));
     OPSEC_CUDA(cudaMemsetAsync(scal, 0, 256, s));
     const long long ncell = (long long)a.ks.N1 * a.ks.N2 * a.ks.N3;
@@ -869,12 +1095,18 @@ bool run_window(const CubatureArgs& a, const Lookup& lk, cudaStream_t s, long lo
     transpose_tables_kernel<<<blocks((long long)a.ntab * nx), 256, 0, s>>>(a.tab32, a.ntab, nx, w.tabT);
     OPSEC_CUDA(cudaGetLastError());
     *launches += 5;
+    if (sph) {
+        const long long n = (long long)a.ks.H * a.ng * a.ng + a.ng * a.ng + (long long)a.ks.nf * (a.ng * (a.ng + 1) / 2);
+        sph_tables_kernel<<<blocks(n), 256, 0, s>>>(a, w);
+        OPSEC_CUDA(cudaGetLastError());
+        ++*launches;
+    }
     int h_nfar = 0;
     OPSEC_CUDA(cudaMemcpyAsync(&h_nfar, w.nfar, sizeof(int), cudaMemcpyDeviceToHost, s));
     OPSEC_CUDA(cudaStreamSynchronize(s));
     // far keys
-    const size_t smem = far_smem<NG>(w);
-    auto k = cubature_far_kernel<NG>;
+    const size_t smem = far_smem<NG>(w, sph);
+    auto k = sph ? cubature_far_sph_kernel<NG> : cubature_far_kernel<NG>;
     OPSEC_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem((const void*)k)));
     int dev = 0, nsm = 0, occ = 0;
     OPSEC_CUDA(cudaGetDevice(&dev));
@@ -904,7 +1136,7 @@ bool run_window(const CubatureArgs& a, const Lookup& lk, cudaStream_t s, long lo
 }
 }  // namespace
 
-size_t cubature_work_bytes(const KeySpace& ks, int nx, int ntab) { return win_layout(ks, nx, ntab).total; }
+size_t cubature_work_bytes(const KeySpace& ks, int nx, int ntab, int ng) { return win_layout(ks, nx, ntab, ng).total; }
 
 void launch_cubature(const CubatureArgs& a, cudaStream_t s, long long* launches) {
     // point table: every Gauss point of every cell, once

@@ -126,7 +126,7 @@ struct CubatureArgs {
 // float4s of the point table for a key space and ng
 size_t cubature_point_count(const KeySpace& ks, int ng);
 // scratch bytes for the window path
-size_t cubature_work_bytes(const KeySpace& ks, int nx, int ntab);
+size_t cubature_work_bytes(const KeySpace& ks, int nx, int ntab, int ng);
 void launch_cubature(const CubatureArgs& a, cudaStream_t s, long long* launches);
 
 struct XiTableArgs {
