@@ -62,6 +62,10 @@ def workload(name):
         sv, cells = synth.shell_survey(16, 16, 32)
         return dict(name="c2-prof", survey=sv, cells=cells, nbands=40, kmax=0.4, nmodes=2048,
                     layout=(256, 4096, 10.0, 20000.0), gauss=4)
+    if name == "c2-inner":  # the 32k-cell shell's cell sizes on its inner half (r in [200, 600]), 16,384 cells
+        sv, cells = synth.shell_survey(16, 32, 32, rmin=200.0, rmax=600.0)
+        return dict(name="c2-inner", survey=sv, cells=cells, nbands=40, kmax=0.4, nmodes=4096,
+                    layout=(256, 4096, 10.0, 20000.0), gauss=4)
     if name == "c2-small":  # same geometry family, 4,096 cells
         sv, cells = synth.shell_survey(16, 16, 16)
         return dict(name="c2-small", survey=sv, cells=cells, nbands=40, kmax=0.4, nmodes=1024,

@@ -398,7 +398,7 @@ struct WinPlan {
     int Wkey;     // histogram bins per warp: one pass covers Wkey - 1 bins of a key's window
     int Wmax;     // widest key window on the window path (npass_max passes)
     int flush;    // second-cell points per FP32 partial histogram before the FP64 flush (0: no flush)
-    int dot64;    // dot products in FP64 (1) or in FP32 chunks of 8 bins (0)
+    int dot64;    // dot products in FP64 (1) or in FP32 chunks of kDotChunk bins (0)
     int nbucket;  // nx + 1: bucket nx holds the near keys
     int2* win;        // [nkeys]: (bucket, width); bucket -1 = key copied by the reflection fill
     int* order;       // [2 nkeys]: far keys by bucket, then near keys, then overflows
@@ -573,14 +573,15 @@ __global__ void bucket_scatter_kernel(long long nkeys, WinPlan w) {
 // strongly cancelling dot product with an oscillating band table.  Measured on
 // the 4x4x4 box, band k in [0.1, 0.15], max|dS|/max|S|: no flush 2.2e-6, flush
 // every 32 points 1.8e-6, every 16 7.9e-7, every 8 9e-8 (the table-group
-// kernel: 2.8e-7).  The dot products run in FP32 over chunks of 8 bins added
-// in FP64 (`dot64` = FP64 throughout: same error, more FP64 work); lane t
+// kernel: 2.8e-7).  The dot products run in FP32 over chunks of kDotChunk bins
+// added in FP64 (`dot64` = FP64 throughout: same error, more FP64 work); lane t
 // takes table t and reads the bin-major tables from L1/L2, so the tables take
 // no shared memory and two 16-warp CTAs fit on an SM.  64-bit integer
 // (fixed-point) histogram atomics would sum exactly but cost +177 ms at 32k
 // cells in shared-memory atomics.
 
 constexpr int kMaxPasses = 8;  // passes over the point pairs for windows wider than one histogram
+constexpr int kDotChunk = 16;  // bins summed in FP32 per FP64 addition in the window dot products
 
 template <int NG>
 struct FarShape {
@@ -741,7 +742,7 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
             if (w.flush && !w.dot64)
                 for (int b = lane; b < segw; b += 32) hp[b] = hh[b] + hl[b];
             __syncwarp();
-            // Dot products: two work items per table, alternate chunks of 8 bins, spread
+            // Dot products: two work items per table, alternate chunks of kDotChunk bins, spread
             // over the lanes (table t: items 2t and 2t+1 on neighbouring lanes, combined by
             // one shuffle); FP32 within a chunk, FP64 across chunks.
             for (int base = 0; base < 2 * ntab; base += 32) {
@@ -750,8 +751,8 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
                 double acc = 0.0;
                 if (it < 2 * ntab) {
                     const float* tr = w.tabT + (size_t)(wn.x + s0) * ntab + t;
-                    for (int b0 = 8 * h; b0 < segw; b0 += 16) {
-                        const int b1 = min(b0 + 8, segw);
+                    for (int b0 = kDotChunk * h; b0 < segw; b0 += 2 * kDotChunk) {
+                        const int b1 = min(b0 + kDotChunk, segw);
                         if (w.flush && w.dot64) {
                             for (int b = b0; b < b1; b++) acc = fma((double)tr[(size_t)b * ntab], (double)hh[b] + hl[b], acc);
                         } else {
@@ -914,8 +915,8 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
                 double acc = 0.0;
                 if (it < 2 * ntab) {
                     const float* tr = w.tabT + (size_t)(wn.x + s0) * ntab + t;
-                    for (int b0 = 8 * h; b0 < segw; b0 += 16) {
-                        const int b1 = min(b0 + 8, segw);
+                    for (int b0 = kDotChunk * h; b0 < segw; b0 += 2 * kDotChunk) {
+                        const int b1 = min(b0 + kDotChunk, segw);
                         if (w.flush && w.dot64) {
                             for (int b = b0; b < b1; b++) acc = fma((double)tr[(size_t)b * ntab], (double)hh[b] + hl[b], acc);
                         } else {
