@@ -989,6 +989,7 @@ void build_q(opsec_gpu* c) {
     a.ng = ng;
     a.np = ng * ng * ng;
     a.w = c->nodes.p + off_w;
+    a.wmax = *std::max_element(w.begin(), w.end());
     a.node1 = c->nodes.p + off1;
     a.node2 = c->nodes.p + off2;
     a.snode2 = c->nodes.p + offs;

@@ -399,6 +399,8 @@ struct WinPlan {
     int Wmax;     // widest key window on the window path (npass_max passes)
     int flush;    // second-cell points per FP32 partial histogram before the FP64 flush (0: no flush)
     int dot64;    // dot products in FP64 (1) or in FP32 chunks of kDotChunk bins (0)
+    float qinv;   // fixed-point units per unit of pair weight (2^k / largest pair weight)
+    float qscale; // 1 / qinv
     int nbucket;  // nx + 1: bucket nx holds the near keys
     int2* win;        // [nkeys]: (bucket, width); bucket -1 = key copied by the reflection fill
     int* order;       // [2 nkeys]: far keys by bucket, then near keys, then overflows
@@ -580,6 +582,22 @@ __global__ void bucket_scatter_kernel(long long nkeys, WinPlan w) {
 // (fixed-point) histogram atomics would sum exactly but cost +177 ms at 32k
 // cells in shared-memory atomics.
 
+// round-to-nearest integer of 0 <= v < 2^22 by the FP32 magic-number addition (FMA/ALU pipes)
+__device__ __forceinline__ int fix_round(float v) { return __float_as_int(v + 12582912.f) - 0x4B400000; }
+
+// Move the fixed-point partial sums into the compensated FP32 histogram (high + low by
+// two-sum) and clear them.  Warp-wide.
+__device__ __forceinline__ void flush_fixed(int* hq, float* hh, float* hl, int n, int lane, float qscale) {
+    __syncwarp();
+    for (int b = lane; b < n; b += 32) {
+        float e;
+        hh[b] = two_sum(hh[b], (float)hq[b] * qscale, &e);
+        hl[b] += e;
+        hq[b] = 0;
+    }
+    __syncwarp();
+}
+
 constexpr int kMaxPasses = 8;  // passes over the point pairs for windows wider than one histogram
 constexpr int kDotChunk = 16;  // bins summed in FP32 per FP64 addition in the window dot products
 
@@ -600,7 +618,7 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
     float4* pts = reinterpret_cast<float4*>(smem_raw);                  // [kWarps][2][NP]
     float* mhi = reinterpret_cast<float*>(pts + kWarps * 2 * NP);       // [kWarps][Wkey]: histogram, high part
     float* mlo = mhi + kWarps * w.Wkey;                                 // [kWarps][Wkey]: low part
-    float* part = mlo + kWarps * w.Wkey;                                // [kWarps][Wkey]: FP32 sums between flushes
+    float* part = mlo + kWarps * w.Wkey;                                // [kWarps][Wkey]: fixed-point sums between flushes
     __shared__ int s_ci[kMaxExp];
     __shared__ float s_cf[kMaxExp];
     __shared__ float4 s_kt[kLogN];
@@ -617,6 +635,7 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
     float* hh = mhi + warp * w.Wkey;
     float* hl = mlo + warp * w.Wkey;
     float* hp = part + warp * w.Wkey;
+    int* hq = reinterpret_cast<int*>(hp);  // the same words: fixed-point partial sums, then FP32 values
     const bool periodic = (a.coordsys == 1 && a.L > 0);
     const float Lh = (float)a.L, Ll = (float)(a.L - (double)Lh), hL = 0.5f * Lh;
     const int nfar = *w.nfar;
@@ -672,7 +691,7 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
             for (int j = lane; j < segw; j += 32) {
                 hh[j] = 0.f;
                 hl[j] = 0.f;
-                hp[j] = 0.f;
+                hq[j] = 0;
             }
             __syncwarp();
             // Mirror symmetry of the innermost axis (phi on spherical grids, z on Cartesian
@@ -719,27 +738,19 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
                             if (bi >= 0 && bi < S) {
                                 bad += out;
                                 const float ww = (lsum < NG - 1 ? 2.f : 1.f) * Ah.w * B.w;
-                                atomicAdd(&hp[bi], fmaf(-ww, fr, ww));
-                                atomicAdd(&hp[bi + 1], ww * fr);
+                                const float wq = ww * w.qinv;  // fixed point: ww_max -> 2^k units
+                                atomicAdd(&hq[bi], fix_round(fmaf(-wq, fr, wq)));
+                                atomicAdd(&hq[bi + 1], fix_round(wq * fr));
                             }
                         }
                     }
-                    if (w.flush) {
-                        // the FP32 partial sums stay small: move them into the compensated histogram
-                        __syncwarp();
-                        for (int b = lane; b < segw; b += 32) {
-                            float e;
-                            hh[b] = two_sum(hh[b], hp[b], &e);
-                            hl[b] += e;
-                            hp[b] = 0.f;
-                        }
-                        __syncwarp();
-                    }
+                    if (w.flush) flush_fixed(hq, hh, hl, segw, lane, w.qscale);
                 }
             }
+            if (!w.flush) flush_fixed(hq, hh, hl, segw, lane, w.qscale);
             __syncwarp();
-            // the histogram as FP32 values once (hp is zero after the last flush)
-            if (w.flush && !w.dot64)
+            // the histogram as FP32 values once (the fixed-point buffer is zero after the last flush)
+            if (!w.dot64)
                 for (int b = lane; b < segw; b += 32) hp[b] = hh[b] + hl[b];
             __syncwarp();
             // Dot products: two work items per table, alternate chunks of kDotChunk bins, spread
@@ -753,7 +764,7 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
                     const float* tr = w.tabT + (size_t)(wn.x + s0) * ntab + t;
                     for (int b0 = kDotChunk * h; b0 < segw; b0 += 2 * kDotChunk) {
                         const int b1 = min(b0 + kDotChunk, segw);
-                        if (w.flush && w.dot64) {
+                        if (w.dot64) {
                             for (int b = b0; b < b1; b++) acc = fma((double)tr[(size_t)b * ntab], (double)hh[b] + hl[b], acc);
                         } else {
                             float pt = 0.f;
@@ -796,7 +807,7 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
     float4* sphw = reinterpret_cast<float4*>(smem_raw);        // [kWarps][NC]: the key's phi-node pairs
     float* mhi = reinterpret_cast<float*>(sphw + kWarps * NC);  // [kWarps][Wkey]: histogram, high part
     float* mlo = mhi + kWarps * w.Wkey;                         // [kWarps][Wkey]: low part
-    float* part = mlo + kWarps * w.Wkey;                        // [kWarps][Wkey]: FP32 sums between flushes
+    float* part = mlo + kWarps * w.Wkey;                        // [kWarps][Wkey]: fixed-point sums between flushes
     __shared__ int s_ci[kMaxExp];
     __shared__ float s_cf[kMaxExp];
     __shared__ float4 s_kt[kLogN];
@@ -814,6 +825,7 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
     float* hh = mhi + warp * w.Wkey;
     float* hl = mlo + warp * w.Wkey;
     float* hp = part + warp * w.Wkey;
+    int* hq = reinterpret_cast<int*>(hp);  // the same words: fixed-point partial sums, then FP32 values
     const int nfar = *w.nfar;
     for (int kk = blockIdx.x * kWarps + warp; kk < nfar; kk += gridDim.x * kWarps) {
         const int key = w.order[kk];
@@ -847,7 +859,7 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
             for (int j = lane; j < segw; j += 32) {
                 hh[j] = 0.f;
                 hl[j] = 0.f;
-                hp[j] = 0.f;
+                hq[j] = 0;
             }
             __syncwarp();
             // lanes take the (P, Q) node pairs; every lane runs the same trip counts
@@ -889,24 +901,18 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
                         if (bi >= 0 && bi < S) {
                             bad += out;
                             const float ww = wpq * sp.z;
-                            atomicAdd(&hp[bi], fmaf(-ww, fr, ww));
-                            atomicAdd(&hp[bi + 1], ww * fr);
+                            const float wq = ww * w.qinv;  // fixed point: ww_max -> 2^k units
+                            atomicAdd(&hq[bi], fix_round(fmaf(-wq, fr, wq)));
+                            atomicAdd(&hq[bi + 1], fix_round(wq * fr));
                         }
                     }
                 }
-                if (w.flush) {
-                    __syncwarp();
-                    for (int b = lane; b < segw; b += 32) {
-                        float e;
-                        hh[b] = two_sum(hh[b], hp[b], &e);
-                        hl[b] += e;
-                        hp[b] = 0.f;
-                    }
-                    __syncwarp();
-                }
+                if (w.flush) flush_fixed(hq, hh, hl, segw, lane, w.qscale);
             }
+            if (!w.flush) flush_fixed(hq, hh, hl, segw, lane, w.qscale);
             __syncwarp();
-            if (w.flush && !w.dot64)
+            // the histogram as FP32 values once (the fixed-point buffer is zero after the last flush)
+            if (!w.dot64)
                 for (int b = lane; b < segw; b += 32) hp[b] = hh[b] + hl[b];
             __syncwarp();
             for (int base = 0; base < 2 * ntab; base += 32) {
@@ -917,7 +923,7 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
                     const float* tr = w.tabT + (size_t)(wn.x + s0) * ntab + t;
                     for (int b0 = kDotChunk * h; b0 < segw; b0 += 2 * kDotChunk) {
                         const int b1 = min(b0 + kDotChunk, segw);
-                        if (w.flush && w.dot64) {
+                        if (w.dot64) {
                             for (int b = b0; b < b1; b++) acc = fma((double)tr[(size_t)b * ntab], (double)hh[b] + hl[b], acc);
                         } else {
                             float pt = 0.f;
@@ -1060,6 +1066,18 @@ bool run_window(const CubatureArgs& a, const Lookup& lk, cudaStream_t s, long lo
     w.flush = a.win_flush;
     w.dot64 = a.win_dot64;
     const bool sph = a.coordsys == 2;
+    {
+        // Fixed-point partial histograms: at most `pairs` contributions reach one bin between
+        // flushes, each at most the largest pair weight (mirror factor 2 included), so with
+        // that weight at 2^k units the sums stay below 2^30.
+        constexpr int NP = FarShape<NG>::NP, NC = NG * (NG + 1) / 2;
+        const double pairs = sph ? (w.flush ? 32.0 * NC : (double)NG * NG * NG * NG * NC)
+                                 : (w.flush ? 32.0 * w.flush : (double)NP * NP);
+        const int k = std::min(21, 30 - (int)std::ceil(std::log2(pairs)));
+        const double wwmax = 2.0 * std::pow(a.wmax, 6) * (1.0 + 1e-6);
+        w.qinv = (float)(std::ldexp(1.0, k) / wwmax);
+        w.qscale = (float)(wwmax / std::ldexp(1.0, k));
+    }
     const void* kfn = sph ? (const void*)cubature_far_sph_kernel<NG> : (const void*)cubature_far_kernel<NG>;
     if (w.Wkey < 8 || far_smem<NG>(w, sph) > (size_t)max_dynamic_smem(kfn)) return false;
     w.nbucket = nx + 1;

@@ -100,6 +100,7 @@ struct CubatureArgs {
     KeySpace ks;
     int ng, np;          // Gauss points per axis, per cell (ng^3)
     const double* w;     // [ng] Gauss weights on [0,1]
+    double wmax = 1.0;   // the largest of them (host copy)
     const double* node1; // [N1][ng]: x (Cartesian) or r (spherical) nodes
     const double* node2; // [N2][ng]: y or mu nodes
     const double* snode2;// [N2][ng]: sqrt(1-mu^2) (spherical)
