@@ -399,8 +399,8 @@ struct WinPlan {
     int Wmax;     // widest key window on the window path (npass_max passes)
     int flush;    // second-cell points per FP32 partial histogram before the FP64 flush (0: no flush)
     int dot64;    // dot products in FP64 (1) or in FP32 chunks of kDotChunk bins (0)
-    float qinv;   // fixed-point units per unit of pair weight (2^k / largest pair weight)
-    float qscale; // 1 / qinv
+    float qinv;   // coarse fixed-point units per unit of pair weight (2^k / largest pair weight)
+    float qfine;  // pair weight per unit of the 64-bit histogram (2^-20 / qinv)
     int nbucket;  // nx + 1: bucket nx holds the near keys
     int2* win;        // [nkeys]: (bucket, width); bucket -1 = key copied by the reflection fill
     int* order;       // [2 nkeys]: far keys by bucket, then near keys, then overflows
@@ -566,34 +566,43 @@ __global__ void bucket_scatter_kernel(long long nkeys, WinPlan w) {
     }
 }
 
-// Histogram bins hold sum w_p w_q (1-fr) and sum w_p w_q fr.  They are summed
-// by FP32 shared-memory atomics over `flush` (8) second-cell points at a time
-// and then moved into a compensated FP32 histogram (high part + low part by
-// two-sum, about 48 bits; on the FP32 pipe, not the slow FP64 one), so every
-// FP32 partial sum stays small.  A bin summed in FP32 over all 4096 pairs of a
-// key carries a rounding error relative to its whole (positive) sum into the
-// strongly cancelling dot product with an oscillating band table.  Measured on
-// the 4x4x4 box, band k in [0.1, 0.15], max|dS|/max|S|: no flush 2.2e-6, flush
-// every 32 points 1.8e-6, every 16 7.9e-7, every 8 9e-8 (the table-group
-// kernel: 2.8e-7).  The dot products run in FP32 over chunks of kDotChunk bins
-// added in FP64 (`dot64` = FP64 throughout: same error, more FP64 work); lane t
-// takes table t and reads the bin-major tables from L1/L2, so the tables take
-// no shared memory and two 16-warp CTAs fit on an SM.  64-bit integer
-// (fixed-point) histogram atomics would sum exactly but cost +177 ms at 32k
-// cells in shared-memory atomics.
+// Histogram bins hold sum w_p w_q (1-fr) and sum w_p w_q fr, in fixed point:
+// each contribution is scaled so that the largest pair weight is 2^21 coarse
+// units, rounded once in FP32 (the product), split into its integer part and
+// its fraction in 2^-20 units, and added with two native 32-bit integer
+// shared-memory atomics; every `flush` second-cell points (Cartesian) or every
+// 32 node pairs (spherical) the two partial sums move into a 64-bit integer
+// histogram.  The sums are exact and independent of the order of the atomics.
+// (FP32 shared-memory atomics were slower -- the counters showed them retried
+// -- and their rounding grows with the partial sum: a bin summed in FP32 over
+// a whole key carries rounding relative to its positive sum into the strongly
+// cancelling dot product with an oscillating band table, 2.2e-6 of max|S| on
+// the 4x4x4 box without flushes.  21 bits without the fraction gave 1.5e-6 on
+// the same box.)  The dot products run in FP32 over chunks of kDotChunk bins
+// added in FP64 (`dot64` = FP64 throughout); lane pairs take the tables and
+// read the bin-major tables from L1/L2, so the tables take no shared memory
+// and two 16-warp CTAs fit on an SM.
 
-// round-to-nearest integer of 0 <= v < 2^22 by the FP32 magic-number addition (FMA/ALU pipes)
+// round-to-nearest integer of |v| < 2^22 by the FP32 magic-number addition (FMA/ALU pipes)
 __device__ __forceinline__ int fix_round(float v) { return __float_as_int(v + 12582912.f) - 0x4B400000; }
 
-// Move the fixed-point partial sums into the compensated FP32 histogram (high + low by
-// two-sum) and clear them.  Warp-wide.
-__device__ __forceinline__ void flush_fixed(int* hq, float* hh, float* hl, int n, int lane, float qscale) {
+// Add x (in units of the coarse quantum) to bin b of the fixed-point partial histogram:
+// the integer part into hqa, the fraction in units of 2^-20 into hqb (both native integer
+// shared atomics, exact and order-independent).  x - floor(x) is exact in FP32.
+__device__ __forceinline__ void add_fixed(int* hqa, int* hqb, int b, float x) {
+    const float a = floorf(x);
+    atomicAdd(&hqa[b], fix_round(a));
+    atomicAdd(&hqb[b], fix_round((x - a) * 1048576.f));
+}
+
+// Move the partial sums into the 64-bit histogram (units of 2^-20 of the coarse quantum:
+// exact) and clear them.  Warp-wide.
+__device__ __forceinline__ void flush_fixed(int* hqa, int* hqb, long long* hm, int n, int lane) {
     __syncwarp();
     for (int b = lane; b < n; b += 32) {
-        float e;
-        hh[b] = two_sum(hh[b], (float)hq[b] * qscale, &e);
-        hl[b] += e;
-        hq[b] = 0;
+        hm[b] += ((long long)hqa[b] << 20) + hqb[b];
+        hqa[b] = 0;
+        hqb[b] = 0;
     }
     __syncwarp();
 }
@@ -616,9 +625,9 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int ntab = a.ntab;
     float4* pts = reinterpret_cast<float4*>(smem_raw);                  // [kWarps][2][NP]
-    float* mhi = reinterpret_cast<float*>(pts + kWarps * 2 * NP);       // [kWarps][Wkey]: histogram, high part
-    float* mlo = mhi + kWarps * w.Wkey;                                 // [kWarps][Wkey]: low part
-    float* part = mlo + kWarps * w.Wkey;                                // [kWarps][Wkey]: fixed-point sums between flushes
+    long long* mas = reinterpret_cast<long long*>(pts + kWarps * 2 * NP);  // [kWarps][Wkey]: 64-bit histogram
+    int* pa = reinterpret_cast<int*>(mas + kWarps * w.Wkey);               // [kWarps][Wkey]: partial sums, integer part
+    int* pb = pa + kWarps * w.Wkey;                                        // [kWarps][Wkey]: partial sums, fraction
     __shared__ int s_ci[kMaxExp];
     __shared__ float s_cf[kMaxExp];
     __shared__ float4 s_kt[kLogN];
@@ -632,10 +641,10 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     float4* P2 = pts + warp * 2 * NP;
     float4* P2l = P2 + NP;
-    float* hh = mhi + warp * w.Wkey;
-    float* hl = mlo + warp * w.Wkey;
-    float* hp = part + warp * w.Wkey;
-    int* hq = reinterpret_cast<int*>(hp);  // the same words: fixed-point partial sums, then FP32 values
+    long long* hm = mas + warp * w.Wkey;
+    int* hqa = pa + warp * w.Wkey;
+    int* hqb = pb + warp * w.Wkey;
+    float* hp = reinterpret_cast<float*>(hqa);  // the same words: FP32 histogram values for the dot products
     const bool periodic = (a.coordsys == 1 && a.L > 0);
     const float Lh = (float)a.L, Ll = (float)(a.L - (double)Lh), hL = 0.5f * Lh;
     const int nfar = *w.nfar;
@@ -689,9 +698,9 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
                 }
             }
             for (int j = lane; j < segw; j += 32) {
-                hh[j] = 0.f;
-                hl[j] = 0.f;
-                hq[j] = 0;
+                hm[j] = 0;
+                hqa[j] = 0;
+                hqb[j] = 0;
             }
             __syncwarp();
             // Mirror symmetry of the innermost axis (phi on spherical grids, z on Cartesian
@@ -738,20 +747,19 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
                             if (bi >= 0 && bi < S) {
                                 bad += out;
                                 const float ww = (lsum < NG - 1 ? 2.f : 1.f) * Ah.w * B.w;
-                                const float wq = ww * w.qinv;  // fixed point: ww_max -> 2^k units
-                                atomicAdd(&hq[bi], fix_round(fmaf(-wq, fr, wq)));
-                                atomicAdd(&hq[bi + 1], fix_round(wq * fr));
+                                const float wq = ww * w.qinv;  // fixed point: the largest pair weight -> 2^k units
+                                add_fixed(hqa, hqb, bi, fmaf(-wq, fr, wq));
+                                add_fixed(hqa, hqb, bi + 1, wq * fr);
                             }
                         }
                     }
-                    if (w.flush) flush_fixed(hq, hh, hl, segw, lane, w.qscale);
+                    if (w.flush) flush_fixed(hqa, hqb, hm, segw, lane);
                 }
             }
-            if (!w.flush) flush_fixed(hq, hh, hl, segw, lane, w.qscale);
-            __syncwarp();
-            // the histogram as FP32 values once (the fixed-point buffer is zero after the last flush)
+            if (!w.flush) flush_fixed(hqa, hqb, hm, segw, lane);
+            // the histogram as FP32 values once (over the partial sums, which are zero now)
             if (!w.dot64)
-                for (int b = lane; b < segw; b += 32) hp[b] = hh[b] + hl[b];
+                for (int b = lane; b < segw; b += 32) hp[b] = (float)hm[b] * w.qfine;
             __syncwarp();
             // Dot products: two work items per table, alternate chunks of kDotChunk bins, spread
             // over the lanes (table t: items 2t and 2t+1 on neighbouring lanes, combined by
@@ -765,7 +773,7 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
                     for (int b0 = kDotChunk * h; b0 < segw; b0 += 2 * kDotChunk) {
                         const int b1 = min(b0 + kDotChunk, segw);
                         if (w.dot64) {
-                            for (int b = b0; b < b1; b++) acc = fma((double)tr[(size_t)b * ntab], (double)hh[b] + hl[b], acc);
+                            for (int b = b0; b < b1; b++) acc = fma((double)tr[(size_t)b * ntab], (double)hm[b] * w.qfine, acc);
                         } else {
                             float pt = 0.f;
                             for (int b = b0; b < b1; b++) pt = fmaf(tr[(size_t)b * ntab], hp[b], pt);
@@ -805,9 +813,9 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int ntab = a.ntab;
     float4* sphw = reinterpret_cast<float4*>(smem_raw);        // [kWarps][NC]: the key's phi-node pairs
-    float* mhi = reinterpret_cast<float*>(sphw + kWarps * NC);  // [kWarps][Wkey]: histogram, high part
-    float* mlo = mhi + kWarps * w.Wkey;                         // [kWarps][Wkey]: low part
-    float* part = mlo + kWarps * w.Wkey;                        // [kWarps][Wkey]: fixed-point sums between flushes
+    long long* mas = reinterpret_cast<long long*>(sphw + kWarps * NC);  // [kWarps][Wkey]: 64-bit histogram
+    int* pa = reinterpret_cast<int*>(mas + kWarps * w.Wkey);            // [kWarps][Wkey]: partial sums, integer part
+    int* pb = pa + kWarps * w.Wkey;                                     // [kWarps][Wkey]: partial sums, fraction
     __shared__ int s_ci[kMaxExp];
     __shared__ float s_cf[kMaxExp];
     __shared__ float4 s_kt[kLogN];
@@ -822,10 +830,10 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     float4* SP = sphw + warp * NC;
-    float* hh = mhi + warp * w.Wkey;
-    float* hl = mlo + warp * w.Wkey;
-    float* hp = part + warp * w.Wkey;
-    int* hq = reinterpret_cast<int*>(hp);  // the same words: fixed-point partial sums, then FP32 values
+    long long* hm = mas + warp * w.Wkey;
+    int* hqa = pa + warp * w.Wkey;
+    int* hqb = pb + warp * w.Wkey;
+    float* hp = reinterpret_cast<float*>(hqa);  // the same words: FP32 histogram values for the dot products
     const int nfar = *w.nfar;
     for (int kk = blockIdx.x * kWarps + warp; kk < nfar; kk += gridDim.x * kWarps) {
         const int key = w.order[kk];
@@ -857,9 +865,9 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
                 }
             }
             for (int j = lane; j < segw; j += 32) {
-                hh[j] = 0.f;
-                hl[j] = 0.f;
-                hq[j] = 0;
+                hm[j] = 0;
+                hqa[j] = 0;
+                hqb[j] = 0;
             }
             __syncwarp();
             // lanes take the (P, Q) node pairs; every lane runs the same trip counts
@@ -901,19 +909,18 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
                         if (bi >= 0 && bi < S) {
                             bad += out;
                             const float ww = wpq * sp.z;
-                            const float wq = ww * w.qinv;  // fixed point: ww_max -> 2^k units
-                            atomicAdd(&hq[bi], fix_round(fmaf(-wq, fr, wq)));
-                            atomicAdd(&hq[bi + 1], fix_round(wq * fr));
+                            const float wq = ww * w.qinv;  // fixed point: the largest pair weight -> 2^k units
+                            add_fixed(hqa, hqb, bi, fmaf(-wq, fr, wq));
+                            add_fixed(hqa, hqb, bi + 1, wq * fr);
                         }
                     }
                 }
-                if (w.flush) flush_fixed(hq, hh, hl, segw, lane, w.qscale);
+                if (w.flush) flush_fixed(hqa, hqb, hm, segw, lane);
             }
-            if (!w.flush) flush_fixed(hq, hh, hl, segw, lane, w.qscale);
-            __syncwarp();
-            // the histogram as FP32 values once (the fixed-point buffer is zero after the last flush)
+            if (!w.flush) flush_fixed(hqa, hqb, hm, segw, lane);
+            // the histogram as FP32 values once (over the partial sums, which are zero now)
             if (!w.dot64)
-                for (int b = lane; b < segw; b += 32) hp[b] = hh[b] + hl[b];
+                for (int b = lane; b < segw; b += 32) hp[b] = (float)hm[b] * w.qfine;
             __syncwarp();
             for (int base = 0; base < 2 * ntab; base += 32) {
                 const int it = base + lane;
@@ -924,7 +931,7 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
                     for (int b0 = kDotChunk * h; b0 < segw; b0 += 2 * kDotChunk) {
                         const int b1 = min(b0 + kDotChunk, segw);
                         if (w.dot64) {
-                            for (int b = b0; b < b1; b++) acc = fma((double)tr[(size_t)b * ntab], (double)hh[b] + hl[b], acc);
+                            for (int b = b0; b < b1; b++) acc = fma((double)tr[(size_t)b * ntab], (double)hm[b] * w.qfine, acc);
                         } else {
                             float pt = 0.f;
                             for (int b = b0; b < b1; b++) pt = fmaf(tr[(size_t)b * ntab], hp[b], pt);
@@ -1051,7 +1058,7 @@ WinLayout win_layout(const KeySpace& ks, int nx, int ntab, int ng) {
 template <int NG>
 size_t far_smem(const WinPlan& w, bool sph) {
     const size_t pts = sph ? sizeof(float4) * (NG * (NG + 1) / 2) : sizeof(float4) * 2 * FarShape<NG>::NP;
-    return FarShape<NG>::kWarps * (pts + 3 * sizeof(float) * w.Wkey);
+    return FarShape<NG>::kWarps * (pts + (sizeof(long long) + 2 * sizeof(int)) * w.Wkey);
 }
 
 // Far keys by windows, near keys by table groups in list mode.  Returns false (nothing
@@ -1061,7 +1068,9 @@ bool run_window(const CubatureArgs& a, const Lookup& lk, cudaStream_t s, long lo
     constexpr int kWarps = FarShape<NG>::kWarps;
     const int nx = a.xl.n();
     WinPlan w{};
-    w.Wkey = std::min(a.win_key, nx);
+    // Cartesian grids also keep the second cell's points per warp: narrower histograms so
+    // that two CTAs still fit on an SM
+    w.Wkey = std::min(a.coordsys == 2 ? a.win_key : std::min(a.win_key, 256), nx);
     w.Wmax = std::min(kMaxPasses * (w.Wkey - 1) + 1, nx);
     w.flush = a.win_flush;
     w.dot64 = a.win_dot64;
@@ -1069,14 +1078,15 @@ bool run_window(const CubatureArgs& a, const Lookup& lk, cudaStream_t s, long lo
     {
         // Fixed-point partial histograms: at most `pairs` contributions reach one bin between
         // flushes, each at most the largest pair weight (mirror factor 2 included), so with
-        // that weight at 2^k units the sums stay below 2^30.
+        // that weight at 2^k coarse units (and fractions in 2^-20 of a unit) both partial
+        // sums stay below 2^30; a key's 64-bit total stays below 2^(k + 20 + 13).
         constexpr int NP = FarShape<NG>::NP, NC = NG * (NG + 1) / 2;
         const double pairs = sph ? (w.flush ? 32.0 * NC : (double)NG * NG * NG * NG * NC)
                                  : (w.flush ? 32.0 * w.flush : (double)NP * NP);
         const int k = std::min(21, 30 - (int)std::ceil(std::log2(pairs)));
         const double wwmax = 2.0 * std::pow(a.wmax, 6) * (1.0 + 1e-6);
         w.qinv = (float)(std::ldexp(1.0, k) / wwmax);
-        w.qscale = (float)(wwmax / std::ldexp(1.0, k));
+        w.qfine = (float)(wwmax / std::ldexp(1.0, k + 20));
     }
     const void* kfn = sph ? (const void*)cubature_far_sph_kernel<NG> : (const void*)cubature_far_kernel<NG>;
     if (w.Wkey < 8 || far_smem<NG>(w, sph) > (size_t)max_dynamic_smem(kfn)) return false;
