@@ -171,11 +171,11 @@ def roofline(stats, clk, bf16, peak_kind):
         avg_s = f["ms"] / 1000.0 / f["count"]
         achieved = f["flops"] / f["count"] / avg_s / 1e9
         st = stats["cubature"]
-        return {"kernel": "cubature_far_kernel (window histograms, far keys)", "bound": "issue",
+        return {"kernel": "cubature_far_sph_kernel / cubature_far_kernel (window histograms)", "bound": "issue",
                 "achieved": achieved, "peak": peak, "unit": "G point pairs/s", "frac": achieved / peak,
                 "traffic": None,
                 "peak_kind": f"derived: 128 lane instructions/clk/SM x {nsm} SMs x {mhz:.0f} MHz (sampled median)"
-                             f" / {FAR_OPS_PER_PAIR} instructions per point pair",
+                             f" / {FAR_OPS_PER_PAIR} instructions per point pair of the direct exact method",
                 "algorithmic_unit": "one Gauss-point pair (all xi tables at once)", "avg_launch_ms": avg_s * 1000,
                 "launches": int(f["count"]),
                 "stage_xi_evaluations_per_s": st["flops"] / (st["ms"] / 1000.0) if st["ms"] > 0 else None}
