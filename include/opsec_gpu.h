@@ -182,6 +182,16 @@ typedef struct {
 int opsec_gpu_batch_fisher(opsec_gpu* ctx, int nmocks, const opsec_mock* mocks, int workers, double* F,
                            double* phat, double* pcov, double* stats);
 
+/* Mock counts for the context's P(k) (replaces the mock generator of
+ * code/opsec/utils/gmock.cpp:1-40 and the counting of dot.cpp:123-129 for
+ * Gaussian-random-field mocks): a Gaussian random field of P(k) on a periodic
+ * ngrid^3 mesh enclosing the cell centres (side 1.25 x their span), sampled at
+ * each centre's mesh point, then counts[a] ~ Poisson(Nbar_a max(0, 1 + bias
+ * delta_a)).  Deterministic in seed (Philox4x64-10 streams; see the engine
+ * sources).  delta (may be NULL) receives delta_a.  ngrid even, 4..1024. */
+int opsec_gpu_mock_counts(opsec_gpu* ctx, int ncells, const opsec_cell* cells, int ngrid, unsigned long long seed,
+                          double bias, double* counts, double* delta);
+
 /* Largest band count opsec_gpu_fisher_noalloc accepts. */
 #define OPSEC_NOALLOC_MAX_BANDS 64
 

@@ -67,6 +67,7 @@ def load():
     L.opsec_gpu_surrogate_stats.argtypes = [vp, C.POINTER(C.c_longlong)]
     L.opsec_gpu_surrogate_eval.argtypes = [vp, fp, C.c_int, fp, fp, fp, fp, dp, fp]
     L.opsec_gpu_batch_fisher.argtypes = [vp, C.c_int, vp, C.c_int, dp, dp, dp, dp]
+    L.opsec_gpu_mock_counts.argtypes = [vp, C.c_int, vp, C.c_int, C.c_ulonglong, C.c_double, dp, dp]
     _lib = L
     return L
 
@@ -221,6 +222,16 @@ class Engine:
         self._check(self._L.opsec_gpu_dot(self._h, cells.size, cells.ctypes.data, _d(counts), modes.shape[0],
                                           _d(modes), _d(y)))
         return y
+
+    def mock_counts(self, cells, ngrid=64, seed=1, bias=1.0, want_delta=False):
+        """Poisson counts of a Gaussian random field of this context's P(k) at the cell centres."""
+        cells = _cells(cells)
+        counts = np.zeros(cells.size)
+        delta = np.zeros(cells.size) if want_delta else None
+        self._check(self._L.opsec_gpu_mock_counts(self._h, cells.size, cells.ctypes.data, int(ngrid),
+                                                  C.c_ulonglong(int(seed)), C.c_double(float(bias)), _d(counts),
+                                                  _d(delta)))
+        return (counts, delta) if want_delta else counts
 
     def _records(self):
         nb = self.num_params()

@@ -1,7 +1,7 @@
 """Build opsec_gpu/libopsec_gpu.so in-tree with nvcc for sm_103a.
 
 Every translation unit in opsec_gpu/csrc is compiled in parallel into
-opsec_gpu/_build/ and linked with cuSOLVER (the FP64 eigensolve).  Host code
+opsec_gpu/_build/ and linked with cuSOLVER (the FP64 eigensolve), cuBLAS and cuFFT (mock fields).  Host code
 carries no architecture-specific flags, so the same recipe builds on x86_64
 and aarch64 hosts.
 
@@ -88,7 +88,7 @@ def build(verbose=False, ptxas_info=False, jobs=None):
     if not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):
         cuda_lib = os.path.join(os.path.dirname(os.path.dirname(nvcc_path())), "lib64")
         cmd = [nvcc_path(), *ARCH, "-shared", "-o", LIB + ".tmp", *objs, f"-L{cuda_lib}", "-lcusolver", "-lcublas",
-               "-lcudart", f"-Xlinker=-rpath={cuda_lib}"]
+               "-lcufft", "-lcudart", f"-Xlinker=-rpath={cuda_lib}"]
         res = subprocess.run(cmd, capture_output=True, text=True)
         if res.returncode != 0:
             raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")

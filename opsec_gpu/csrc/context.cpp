@@ -351,6 +351,10 @@ struct opsec_gpu {
     DevBuf<int> surr_cnt;
     DevBuf<int> az_i;
     DevBuf<long long> az_off;
+    // mock counts: cuFFT plans for the last mesh size, mesh and per-cell buffers
+    MockPlans mock_plans;
+    DevBuf<double> mock_grid, mock_spec, mock_nbar, mock_out;
+    DevBuf<long long> mock_idx;
     // block Fisher of the last azimuthal projection (Fisher build without the packed triangle)
     bool az_blockF = false;
     BlockFisherArgs bf{};
@@ -1107,6 +1111,7 @@ void check_info(opsec_gpu* c, int count) {
 // context, which may move the library's internal buffers the graph refers to.
 void drop_eig_graph(opsec_gpu* c) {
     if (c->eig_exec) cudaGraphExecDestroy(c->eig_exec);
+    destroy_mock_plans(c->mock_plans);
     c->eig_exec = nullptr;
     c->eig_key = {};
 }
@@ -1850,6 +1855,81 @@ int opsec_gpu_dot(opsec_gpu* c, int ncells, const opsec_cell* cells, const doubl
     });
 }
 
+int opsec_gpu_mock_counts(opsec_gpu* c, int ncells, const opsec_cell* cells, int ngrid, unsigned long long seed,
+                          double bias, double* counts, double* delta) {
+    return guard(c, [&] {
+        if (ncells <= 0 || !cells || !counts) fail(OPSEC_ERR_ARG, "invalid mock arguments");
+        if (ngrid < 4 || ngrid > 1024 || ngrid % 2) fail(OPSEC_ERR_ARG, "ngrid must be even, in [4, 1024]");
+        if (!std::isfinite(bias)) fail(OPSEC_ERR_ARG, "bias must be finite");
+        build_tables(c);  // uploads the P(k) spline
+        // cell centres (Cartesian, or (r, mu, phi) mapped to x, y, z), the enclosing periodic
+        // mesh (side 1.25 x the span of the centres plus a margin of 1) and each centre's mesh point
+        std::vector<double> xyz((size_t)3 * ncells), nb(ncells);
+        double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+        for (int a = 0; a < ncells; a++) {
+            const opsec_cell& e = cells[a];
+            const double c1 = 0.5 * (e.min1 + e.max1), c2 = 0.5 * (e.min2 + e.max2), c3 = 0.5 * (e.min3 + e.max3);
+            double x[3] = {c1, c2, c3};
+            if (c->geo.coordsys == 2) {
+                const double st = std::sqrt(std::fmax(1.0 - c2 * c2, 0.0));
+                x[0] = c1 * st * std::cos(c3);
+                x[1] = c1 * st * std::sin(c3);
+                x[2] = c1 * c2;
+            }
+            for (int d = 0; d < 3; d++) {
+                xyz[(size_t)3 * a + d] = x[d];
+                lo[d] = std::fmin(lo[d], x[d]);
+                hi[d] = std::fmax(hi[d], x[d]);
+            }
+            if (!std::isfinite(e.Nbar) || e.Nbar < 0) fail(OPSEC_ERR_NUMERIC, "Nbar must be finite and >= 0");
+            nb[a] = e.Nbar;
+        }
+        double span = 0.0;
+        for (int d = 0; d < 3; d++) {
+            lo[d] -= 1.0;
+            span = std::fmax(span, hi[d] - lo[d]);
+        }
+        const double box = (span + 1.0) * 1.25, h = box / ngrid;
+        std::vector<long long> idx(ncells);
+        for (int a = 0; a < ncells; a++) {
+            long long m[3];
+            for (int d = 0; d < 3; d++) {
+                long long v = (long long)std::floor((xyz[(size_t)3 * a + d] - lo[d]) / h) % ngrid;
+                m[d] = v < 0 ? v + ngrid : v;
+            }
+            idx[a] = (m[0] * ngrid + m[1]) * ngrid + m[2];
+        }
+        const long long npts = (long long)ngrid * ngrid * ngrid;
+        c->mock_grid.alloc(npts);
+        c->mock_spec.alloc((size_t)2 * ngrid * ngrid * (ngrid / 2 + 1));
+        c->mock_idx.alloc(ncells);
+        c->mock_nbar.alloc(ncells);
+        c->mock_out.alloc((size_t)2 * ncells);
+        OPSEC_CUDA(cudaMemcpyAsync(c->mock_idx.p, idx.data(), sizeof(long long) * ncells, cudaMemcpyHostToDevice,
+                                   c->stream));
+        OPSEC_CUDA(cudaMemcpyAsync(c->mock_nbar.p, nb.data(), sizeof(double) * ncells, cudaMemcpyHostToDevice,
+                                   c->stream));
+        MockArgs m;
+        m.ngrid = ngrid;
+        m.box = box;
+        m.seed = seed;
+        m.bias = bias;
+        m.npk = (int)c->pk_k.size();
+        m.pk = c->pk_dev.p;
+        m.grid = c->mock_grid.p;
+        m.spec = reinterpret_cast<double2*>(c->mock_spec.p);
+        m.ncells = ncells;
+        m.idx = c->mock_idx.p;
+        m.nbar = c->mock_nbar.p;
+        m.counts = c->mock_out.p;
+        m.delta = c->mock_out.p + ncells;
+        launch_mock_counts(m, c->mock_plans, c->stream, &c->launches);
+        OPSEC_CUDA(cudaMemcpyAsync(counts, m.counts, sizeof(double) * ncells, cudaMemcpyDeviceToHost, c->stream));
+        if (delta) OPSEC_CUDA(cudaMemcpyAsync(delta, m.delta, sizeof(double) * ncells, cudaMemcpyDeviceToHost, c->stream));
+        sync(c);
+    });
+}
+
 int opsec_gpu_estimate(opsec_gpu* c, int nmodes, const double* evals, const double* cov_packed, const double* y,
                        int mixing, double* phat, double* pcov, double* F, double* W, double* M, double* q, double* f) {
     return guard(c, [&] {
@@ -2108,6 +2188,7 @@ void opsec_gpu_destroy(opsec_gpu* c) {
     if (c->device >= 0) cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->eig_exec) cudaGraphExecDestroy(c->eig_exec);
+    destroy_mock_plans(c->mock_plans);
     if (c->solver) cusolverDnDestroy(c->solver);
     if (c->blas) cublasDestroy(c->blas);
     for (int j = 0; j < opsec_gpu::kSide; j++) {

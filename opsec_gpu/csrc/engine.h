@@ -282,4 +282,60 @@ void launch_scale_modes(int ncells, int nmodes, const double* modes, const doubl
 // packed FP32 -> FP64
 void launch_widen(size_t n, const float* in, double* out, cudaStream_t s, long long* launches);
 
+// Mock counts (mock.cu): white noise, FFT, P(k) shaping, inverse FFT, cell counts.
+constexpr unsigned long long kMockNoiseStream = 0x6E6F697365ULL;    // Philox key word 1 of the noise
+constexpr unsigned long long kMockPoissonStream = 0x706F6973ULL;    // Philox key word 1 of the counts
+constexpr int kMockMaxAttempts = 64;                               // PTRS attempts per draw
+struct MockArgs {
+    int ngrid;             // mesh points per axis (even)
+    double box;            // mesh side
+    unsigned long long seed;
+    double bias;
+    int npk;
+    const double* pk;      // cubic spline of P(k): x, y, b, c, d (npk each)
+    double* grid;          // [ngrid^3] noise, then the field
+    double2* spec;         // [ngrid][ngrid][ngrid/2+1]
+    int ncells;
+    const long long* idx;  // [ncells] mesh point of each cell centre
+    const double* nbar;    // [ncells]
+    double* counts;        // [ncells] out
+    double* delta;         // [ncells] out: the field at the cell centres
+};
+struct MockPlans {
+    int n = 0;
+    int fwd = 0, inv = 0;  // cuFFT handles
+};
+void launch_mock_counts(const MockArgs& m, MockPlans& plans, cudaStream_t s, long long* launches);
+void destroy_mock_plans(MockPlans& plans);
+
+#ifdef __CUDACC__
+// Cubic spline of a tabulated function (Spline.cpp:13-35 lookup, :429-434 zero outside
+// [x0, x_last)); shared by the xi tables and the mock spectrum.
+__device__ inline int lookup_index(double x, int N, const double* X) {
+    double I = (N - 1) * (x - X[0]) / (X[N - 1] - X[0]);
+    int i = (int)I;
+    i = i < 0 ? 0 : (i > N - 2 ? N - 2 : i);
+    int ilo = 0, ihi = N - 2;
+    while (ilo < ihi) {
+        if (x < X[i]) {
+            ihi = i - 1;
+            i = (ilo + ihi) / 2;
+        } else if (x > X[i + 1]) {
+            ilo = i + 1;
+            i = (ilo + ihi) / 2;
+        } else
+            break;
+    }
+    return i;
+}
+
+__device__ inline double spline_eval(int N, const double* X, const double* Y, const double* b, const double* c,
+                                     const double* d, double x) {
+    if (x < X[0] || x >= X[N - 1]) return 0.0;
+    int i = lookup_index(x, N, X);
+    double u = x - X[i];
+    return Y[i] + b[i] * u + c[i] * u * u + d[i] * u * u * u;
+}
+#endif
+
 }  // namespace opsec

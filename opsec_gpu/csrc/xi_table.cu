@@ -18,33 +18,6 @@ constexpr int kNkXi = 32768;
 constexpr int kNkBand = 8192;
 constexpr double kTwoPi2 = 2.0 * M_PI * M_PI;
 
-__device__ int lookup_index(double x, int N, const double* X) {
-    // Spline.cpp:13-35: uniform-grid guess, then bisection
-    double I = (N - 1) * (x - X[0]) / (X[N - 1] - X[0]);
-    int i = (int)I;
-    i = i < 0 ? 0 : (i > N - 2 ? N - 2 : i);
-    int ilo = 0, ihi = N - 2;
-    while (ilo < ihi) {
-        if (x < X[i]) {
-            ihi = i - 1;
-            i = (ilo + ihi) / 2;
-        } else if (x > X[i + 1]) {
-            ilo = i + 1;
-            i = (ilo + ihi) / 2;
-        } else
-            break;
-    }
-    return i;
-}
-
-__device__ double spline_eval(int N, const double* X, const double* Y, const double* b, const double* c,
-                              const double* d, double x) {
-    if (x < X[0] || x >= X[N - 1]) return 0.0;  // Spline.cpp:429-434
-    int i = lookup_index(x, N, X);
-    double u = x - X[i];
-    return Y[i] + b[i] * u + c[i] * u * u + d[i] * u * u * u;
-}
-
 __device__ __forceinline__ double sj0(double x) {
     double x2 = x * x;
     return (x2 < 1e-4) ? 1 - x2 * (1 / 6. + x2 * (1 / 120. - x2 * (1 / 5040.))) : sin(x) / x;
