@@ -60,12 +60,13 @@ __global__ void mock_noise_kernel(long long npts, unsigned long long seed, doubl
     }
 }
 
-// F(k) *= sqrt(P(|k|) / V) / n^1.5 / n^3 (the last factor normalises the unnormalised inverse)
+// F(k) *= sqrt(P(|k|) / V) n^1.5 / n^3 (the last factor normalises the unnormalised inverse):
+// unit white noise has |F|^2 = n^3 per mode, so the field's variance is sum_k P(k) / V
 __global__ void mock_spectrum_kernel(int n, double box, int npk, const double* pk, double2* F) {
     const int nz = n / 2 + 1;
     const long long total = (long long)n * n * nz;
     const double kf = 2.0 * M_PI / box;
-    const double scale = 1.0 / (pow((double)n, 1.5) * (double)n * n * n);
+    const double scale = 1.0 / pow((double)n, 1.5);
     const double* X = pk;
     const double* Y = pk + npk;
     const double* B = pk + 2 * npk;

@@ -7,7 +7,7 @@ same random streams, what opsec_gpu_mock_counts does on the GPU:
                        easy as 1, 2, 3" (SC 2011); pinned against numpy's own
                        numpy.random.Philox in tests/test_mock.py
   Box-Muller           two normals per pair of uniforms
-  field                white noise -> rfftn -> x sqrt(P(|k|) / V) / n^1.5 -> irfftn
+  field                white noise -> rfftn -> x sqrt(P(|k|) / V) n^1.5 -> irfftn
                        (the Gaussian random field of the mock generator,
                        code/opsec/utils/gmock.cpp:1-40, drawn from white noise)
   counts               Poisson(Nbar (1 + b delta)^+): CDF inversion below 10,
@@ -77,7 +77,7 @@ def field(n, box, seed, pk):
     FX, FY, FZ = np.meshgrid(fx, fx, fz, indexing="ij")
     kk = kf * np.sqrt(FX ** 2 + FY ** 2 + FZ ** 2)
     P = np.asarray(pk(kk.ravel())).reshape(kk.shape)
-    amp = np.sqrt(P / box ** 3) / n ** 1.5
+    amp = np.sqrt(P / box ** 3) * n ** 1.5
     amp[0, 0, 0] = 0.0
     return np.fft.irfftn(np.fft.rfftn(white_noise(n, seed)) * amp, s=(n, n, n), axes=(0, 1, 2))
 

@@ -62,7 +62,13 @@ def test_mock_counts_match_oracle(geom):
     assert np.array_equal(counts, ref_counts)
     assert np.array_equal(again, counts)          # deterministic in the seed
     assert not np.array_equal(other, counts)      # and a different seed differs
-    # the field's variance at the cells and the counts' mean follow the inputs
-    assert np.std(delta) > 0.05
+    # the field's variance follows the spectrum: sum over the mesh modes of P(k) / V
+    idx, box = M.mesh_index(coordsys, cells, n)
+    kf = 2 * math.pi / box
+    f = np.fft.fftfreq(n, d=1.0 / n)
+    kk = kf * np.sqrt(f[:, None, None] ** 2 + f[None, :, None] ** 2 + f[None, None, :] ** 2).ravel()
+    var = np.sum(np.asarray(spl(kk[1:]))) / box ** 3
+    fld = M.field(n, box, 17, spl)
+    assert abs(fld.var() / var - 1.0) < 0.1
     lam = np.fmax(cells["Nbar"] * (1 + 1.3 * delta), 0)
     assert abs(counts.sum() - lam.sum()) < 6 * math.sqrt(lam.sum())
