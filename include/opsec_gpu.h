@@ -182,6 +182,30 @@ typedef struct {
 int opsec_gpu_batch_fisher(opsec_gpu* ctx, int nmocks, const opsec_mock* mocks, int workers, double* F,
                            double* phat, double* pcov, double* stats);
 
+/* The cell builder (replaces basis.cpp:89-128, 160-201 with FinalizeCell's
+ * adaptive cubature): every cell of the configured grid whose expected count
+ * Nbar is positive, numbered in grid order (d1, d2, d3), with its bounds
+ * (Survey::CreateEmptyCell, Survey.cpp:80-97), Veff and Nbar.  Cartesian
+ * grids: the constant selection survey.nbar (BoxSurvey.cpp:61-75), Nbar =
+ * nbar Veff.  Spherical grids: the radial linear spline of
+ * opsec_gpu_set_radial times the HEALPix map of opsec_gpu_set_mask
+ * (SphericalSurvey.cpp:51-80); the radial integral is exact (closed form per
+ * spline segment), the map's by basis.samples^2 points per cell (default
+ * 16^2).  The reference's spherical Nbar is 3x the expected count (it
+ * integrates over r^3 without the 1/3); configuration basis.quirk3 = 1
+ * reproduces that.  With capacity 0 only *ncells is set. */
+int opsec_gpu_basis(opsec_gpu* ctx, int capacity, opsec_cell* cells, int* ncells);
+/* The radial selection nbar(r) (the `radial` file of SphericalSurvey.cpp:126-131):
+ * linear between the n points, zero outside [r_0, r_{n-1}). */
+int opsec_gpu_set_radial(opsec_gpu* ctx, int n, const double* r, const double* nbar);
+/* The angular completeness map (the FITS `maskfile` of SphericalSurvey.cpp:100-118,
+ * as 12 nside^2 floats; nest = 1 for NESTED ordering, 0 for RING).  nside 0
+ * removes it (completeness 1). */
+int opsec_gpu_set_mask(opsec_gpu* ctx, long long nside, int nest, const float* mask);
+/* HEALPix pixel of each (theta, phi) (chealpix.c ang2pix_ring / ang2pix_nest). */
+int opsec_gpu_ang2pix(opsec_gpu* ctx, long long nside, int nest, int n, const double* theta, const double* phi,
+                      long long* pix);
+
 /* Mock counts for the context's P(k) (replaces the mock generator of
  * code/opsec/utils/gmock.cpp:1-40 and the counting of dot.cpp:123-129 for
  * Gaussian-random-field mocks): a Gaussian random field of P(k) on a periodic

@@ -68,6 +68,10 @@ def load():
     L.opsec_gpu_surrogate_eval.argtypes = [vp, fp, C.c_int, fp, fp, fp, fp, dp, fp]
     L.opsec_gpu_batch_fisher.argtypes = [vp, C.c_int, vp, C.c_int, dp, dp, dp, dp]
     L.opsec_gpu_mock_counts.argtypes = [vp, C.c_int, vp, C.c_int, C.c_ulonglong, C.c_double, dp, dp]
+    L.opsec_gpu_set_radial.argtypes = [vp, C.c_int, dp, dp]
+    L.opsec_gpu_set_mask.argtypes = [vp, C.c_longlong, C.c_int, C.POINTER(C.c_float)]
+    L.opsec_gpu_basis.argtypes = [vp, C.c_int, vp, ip]
+    L.opsec_gpu_ang2pix.argtypes = [vp, C.c_longlong, C.c_int, C.c_int, dp, dp, C.POINTER(C.c_longlong)]
     _lib = L
     return L
 
@@ -222,6 +226,31 @@ class Engine:
         self._check(self._L.opsec_gpu_dot(self._h, cells.size, cells.ctypes.data, _d(counts), modes.shape[0],
                                           _d(modes), _d(y)))
         return y
+
+    def set_radial(self, r, nbar):
+        r, nbar = _f64(r), _f64(nbar)
+        self._check(self._L.opsec_gpu_set_radial(self._h, r.size, _d(r), _d(nbar)))
+
+    def set_mask(self, nside, nest=False, mask=None):
+        m = None if mask is None else np.ascontiguousarray(mask, dtype=np.float32)
+        self._check(self._L.opsec_gpu_set_mask(self._h, int(nside), 1 if nest else 0, _fp(m)))
+
+    def basis(self):
+        """Every grid cell with positive Nbar (CELL_DTYPE records, grid order)."""
+        from .synth import CELL_DTYPE
+        n = C.c_int(0)
+        self._check(self._L.opsec_gpu_basis(self._h, 0, None, C.byref(n)))
+        cells = np.zeros(n.value, dtype=CELL_DTYPE)
+        if n.value:
+            self._check(self._L.opsec_gpu_basis(self._h, n.value, cells.ctypes.data, C.byref(n)))
+        return cells
+
+    def ang2pix(self, nside, nest, theta, phi):
+        theta, phi = _f64(theta), _f64(phi)
+        pix = np.zeros(theta.size, dtype=np.int64)
+        self._check(self._L.opsec_gpu_ang2pix(self._h, int(nside), 1 if nest else 0, theta.size, _d(theta), _d(phi),
+                                              pix.ctypes.data_as(C.POINTER(C.c_longlong))))
+        return pix
 
     def mock_counts(self, cells, ngrid=64, seed=1, bias=1.0, want_delta=False):
         """Poisson counts of a Gaussian random field of this context's P(k) at the cell centres."""

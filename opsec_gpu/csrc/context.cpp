@@ -351,6 +351,13 @@ struct opsec_gpu {
     DevBuf<int> surr_cnt;
     DevBuf<int> az_i;
     DevBuf<long long> az_off;
+    // cell builder: the selection function (Cartesian constant, spherical radial spline x map)
+    double sel_nbar = 0.0;
+    std::vector<double> rad_r, rad_n;
+    long long mask_nside = 0;
+    int mask_nest = 0;
+    DevBuf<float> mask_dev;
+    int basis_quirk3 = 0, basis_samples = 16;
     // mock counts: cuFFT plans for the last mesh size, mesh and per-cell buffers
     MockPlans mock_plans;
     DevBuf<double> mock_grid, mock_spec, mock_nbar, mock_out;
@@ -558,6 +565,12 @@ void configure(opsec_gpu* c, const std::map<std::string, std::string>& kv) {
         const std::string& v = get("azimuthal.eig");
         if (v != "streams" && v != "batched") fail(OPSEC_ERR_CONFIG, "azimuthal.eig must be streams or batched");
         c->az_batched = v == "batched";
+    }
+    if (has("survey.nbar")) c->sel_nbar = to_double("survey.nbar", get("survey.nbar"));
+    if (has("basis.quirk3")) c->basis_quirk3 = to_int("basis.quirk3", get("basis.quirk3")) != 0;
+    if (has("basis.samples")) {
+        c->basis_samples = to_int("basis.samples", get("basis.samples"));
+        if (c->basis_samples < 1 || c->basis_samples > 1024) fail(OPSEC_ERR_CONFIG, "basis.samples must be in [1, 1024]");
     }
     if (has("azimuthal.split")) {
         c->az_split = to_int("azimuthal.split", get("azimuthal.split"));
@@ -1852,6 +1865,136 @@ int opsec_gpu_dot(opsec_gpu* c, int ncells, const opsec_cell* cells, const doubl
         launch_dot(ncells, nmodes, c->modes.p, c->counts.p, c->nbar.p, c->y.p, c->stream, &c->launches);
         OPSEC_CUDA(cudaMemcpyAsync(y, c->y.p, sizeof(double) * nmodes, cudaMemcpyDeviceToHost, c->stream));
         sync(c);
+    });
+}
+
+int opsec_gpu_set_radial(opsec_gpu* c, int n, const double* r, const double* nbar) {
+    return guard(c, [&] {
+        if (n < 2 || !r || !nbar) fail(OPSEC_ERR_ARG, "the radial selection needs at least two points");
+        for (int i = 0; i < n; i++) {
+            if (!std::isfinite(r[i]) || !std::isfinite(nbar[i])) fail(OPSEC_ERR_NUMERIC, "non-finite radial selection");
+            if (i && !(r[i] > r[i - 1])) fail(OPSEC_ERR_ARG, "radial selection abscissae must increase");
+        }
+        c->rad_r.assign(r, r + n);
+        c->rad_n.assign(nbar, nbar + n);
+    });
+}
+
+int opsec_gpu_set_mask(opsec_gpu* c, long long nside, int nest, const float* mask) {
+    return guard(c, [&] {
+        if (nside == 0) {
+            c->mask_nside = 0;
+            return;
+        }
+        if (nside < 1 || nside > 8192 || (nest && (nside & (nside - 1)))) fail(OPSEC_ERR_ARG, "invalid HEALPix nside");
+        if (!mask) fail(OPSEC_ERR_ARG, "no map");
+        const size_t npix = (size_t)12 * nside * nside;
+        for (size_t i = 0; i < npix; i++)
+            if (!std::isfinite(mask[i])) fail(OPSEC_ERR_NUMERIC, "non-finite map value");
+        c->mask_dev.alloc(npix);
+        OPSEC_CUDA(cudaMemcpyAsync(c->mask_dev.p, mask, sizeof(float) * npix, cudaMemcpyHostToDevice, c->stream));
+        sync(c);
+        c->mask_nside = nside;
+        c->mask_nest = nest ? 1 : 0;
+    });
+}
+
+int opsec_gpu_ang2pix(opsec_gpu* c, long long nside, int nest, int n, const double* theta, const double* phi,
+                      long long* pix) {
+    return guard(c, [&] {
+        if (nside < 1 || nside > 8192 || (nest && (nside & (nside - 1))) || n < 0 || (n && (!theta || !phi || !pix)))
+            fail(OPSEC_ERR_ARG, "invalid ang2pix arguments");
+        if (n == 0) return;
+        DevBuf<double> in;
+        DevBuf<long long> out;
+        in.alloc((size_t)2 * n);
+        out.alloc(n);
+        OPSEC_CUDA(cudaMemcpyAsync(in.p, theta, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+        OPSEC_CUDA(cudaMemcpyAsync(in.p + n, phi, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+        launch_ang2pix(nside, nest, n, in.p, in.p + n, out.p, c->stream, &c->launches);
+        OPSEC_CUDA(cudaMemcpyAsync(pix, out.p, sizeof(long long) * n, cudaMemcpyDeviceToHost, c->stream));
+        sync(c);
+    });
+}
+
+int opsec_gpu_basis(opsec_gpu* c, int capacity, opsec_cell* cells, int* ncells) {
+    return guard(c, [&] {
+        const Geometry& g = c->geo;
+        const long long total = (long long)g.n[0] * g.n[1] * g.n[2];
+        if (!ncells || (capacity > 0 && !cells) || total <= 0 || total > (1LL << 31) - 1)
+            fail(OPSEC_ERR_ARG, "invalid basis arguments");
+        if (g.coordsys == 1 && !(c->sel_nbar > 0)) fail(OPSEC_ERR_CONFIG, "survey.nbar must be > 0 (constant selection)");
+        if (g.coordsys == 2 && c->rad_r.size() < 2) fail(OPSEC_ERR_STATE, "no radial selection: call opsec_gpu_set_radial");
+        // cell bounds as Survey::CreateEmptyCell (Survey.cpp:80-97), grid order d1, d2, d3
+        std::vector<double> bounds((size_t)6 * total);
+        long long k = 0;
+        for (int d1 = 0; d1 < g.n[0]; d1++)
+            for (int d2 = 0; d2 < g.n[1]; d2++)
+                for (int d3 = 0; d3 < g.n[2]; d3++, k++) {
+                    const int dd[3] = {d1, d2, d3};
+                    for (int ax = 0; ax < 3; ax++) {
+                        const double lo = g.b[2 * ax], hi = g.b[2 * ax + 1];
+                        bounds[6 * k + 2 * ax] = lo + dd[ax] * (hi - lo) / g.n[ax];
+                        bounds[6 * k + 2 * ax + 1] = lo + (dd[ax] + 1) * (hi - lo) / g.n[ax];
+                    }
+                }
+        DevBuf<double> dev;
+        dev.alloc((size_t)6 * total + 2 * total + 2 * c->rad_r.size());
+        double* d_bounds = dev.p;
+        double* d_out = dev.p + 6 * total;
+        double* d_rad = d_out + 2 * total;
+        OPSEC_CUDA(cudaMemcpyAsync(d_bounds, bounds.data(), sizeof(double) * bounds.size(), cudaMemcpyHostToDevice,
+                                   c->stream));
+        const int nr = (int)c->rad_r.size();
+        if (nr) {
+            OPSEC_CUDA(cudaMemcpyAsync(d_rad, c->rad_r.data(), sizeof(double) * nr, cudaMemcpyHostToDevice, c->stream));
+            OPSEC_CUDA(cudaMemcpyAsync(d_rad + nr, c->rad_n.data(), sizeof(double) * nr, cudaMemcpyHostToDevice,
+                                       c->stream));
+        }
+        BasisArgs b;
+        b.coordsys = g.coordsys;
+        for (int ax = 0; ax < 3; ax++) b.n[ax] = g.n[ax];
+        b.bounds = d_bounds;
+        b.nbar = c->sel_nbar;
+        b.nrad = nr;
+        b.rad_r = d_rad;
+        b.rad_n = d_rad + nr;
+        b.nside = c->mask_nside;
+        b.nest = c->mask_nest;
+        b.mask = c->mask_dev.p;
+        b.samples = c->basis_samples;
+        b.quirk3 = c->basis_quirk3;
+        b.out = d_out;
+        launch_basis(b, c->stream, &c->launches);
+        std::vector<double> out((size_t)2 * total);
+        OPSEC_CUDA(cudaMemcpyAsync(out.data(), d_out, sizeof(double) * out.size(), cudaMemcpyDeviceToHost, c->stream));
+        sync(c);
+        // keep the cells whose Nbar is positive (basis.cpp:118-127), numbered in grid order
+        int kept = 0;
+        k = 0;
+        for (int d1 = 0; d1 < g.n[0]; d1++)
+            for (int d2 = 0; d2 < g.n[1]; d2++)
+                for (int d3 = 0; d3 < g.n[2]; d3++, k++) {
+                    if (!(out[2 * k + 1] > 0)) continue;
+                    if (kept < capacity) {
+                        opsec_cell& e = cells[kept];
+                        e.a = kept;
+                        e.d1 = d1;
+                        e.d2 = d2;
+                        e.d3 = d3;
+                        e.min1 = bounds[6 * k];
+                        e.max1 = bounds[6 * k + 1];
+                        e.min2 = bounds[6 * k + 2];
+                        e.max2 = bounds[6 * k + 3];
+                        e.min3 = bounds[6 * k + 4];
+                        e.max3 = bounds[6 * k + 5];
+                        e.Veff = out[2 * k];
+                        e.Nbar = out[2 * k + 1];
+                    }
+                    ++kept;
+                }
+        *ncells = kept;
+        if (kept > capacity && capacity > 0) fail(OPSEC_ERR_ARG, "cell array too small: " + std::to_string(kept) + " cells");
     });
 }
 

@@ -282,6 +282,26 @@ void launch_scale_modes(int ncells, int nmodes, const double* modes, const doubl
 // packed FP32 -> FP64
 void launch_widen(size_t n, const float* in, double* out, cudaStream_t s, long long* launches);
 
+// Cell builder (basis.cu): Veff and Nbar of every grid cell.
+struct BasisArgs {
+    int coordsys;           // 1 Cartesian (constant nbar), 2 spherical (radial spline x map)
+    int n[3];
+    const double* bounds;   // [cells][6]: min1 max1 min2 max2 min3 max3, grid order
+    double nbar;            // Cartesian: the constant selection
+    int nrad;
+    const double* rad_r;    // spherical: radial linear spline knots
+    const double* rad_n;
+    long long nside;        // HEALPix map (0: none)
+    int nest;
+    const float* mask;
+    int samples;            // map points per cell axis
+    int quirk3;             // 1: the reference's 3x spherical Nbar
+    double* out;            // [cells][2]: Veff, Nbar
+};
+void launch_basis(const BasisArgs& b, cudaStream_t s, long long* launches);
+void launch_ang2pix(long long nside, int nest, int n, const double* theta, const double* phi, long long* pix,
+                    cudaStream_t s, long long* launches);
+
 // Mock counts (mock.cu): white noise, FFT, P(k) shaping, inverse FFT, cell counts.
 constexpr unsigned long long kMockNoiseStream = 0x6E6F697365ULL;    // Philox key word 1 of the noise
 constexpr unsigned long long kMockPoissonStream = 0x706F6973ULL;    // Philox key word 1 of the counts

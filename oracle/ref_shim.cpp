@@ -6,9 +6,9 @@
 // is used to pin the oracle restatement and to generate golden vectors; the
 // GPU library never links it.
 //
-// The reference spherical survey links against HEALPix map readers
-// (chealpix.c needs cfitsio, which is absent); the three symbols it names are
-// stubbed below because the separation function never calls them.
+// chealpix.c (HEALPix pixelisation) is compiled from the reference too,
+// against a stub fitsio.h whose map readers fail (cfitsio is absent); and
+// basis.cpp, whose FinalizeCell integrates a selection function over a cell.
 
 #include <cmath>
 #include <cstdio>
@@ -28,11 +28,10 @@
 #include "cfg.h"
 #include "sig.h"
 
-extern "C" {
-float* read_healpix_map(const char*, long*, char*, char*) { return NULL; }
-void ang2pix_nest(long, double, double, long* ip) { *ip = 0; }
-void ang2pix_ring(long, double, double, long* ip) { *ip = 0; }
-}
+#include "SelectionFunc.h"
+#include "chealpix.h"
+
+bool FinalizeCell(int coordsys, Cell& c, SelectionFunc& nbar, double epsrel, double epsabs);  // basis.cpp:89
 
 namespace {
 
@@ -73,6 +72,32 @@ Survey* make_survey(int coordsys, const double* grid, const int* n, double L) {
     s->MuMin = grid[2];
     return s;
 }
+
+// The spherical selection of SphericalSurvey.cpp:51-80 -- radial linear spline
+// times a HEALPix completeness map -- built from arrays instead of its files
+// (the map reader needs cfitsio); evaluate() as SphericalSurvey.cpp:70-80.
+struct ArraySphericalSelection : public SelectionFuncImpl {
+    long nside;
+    int nest;
+    std::vector<float> mask;
+    Spline radial;
+    double evaluate(double r, double mu, double phi) {
+        double rad = radial(r);
+        if (nside <= 0) return rad;
+        double theta = acos(mu);
+        long ip;
+        if (nest)
+            ang2pix_nest(nside, theta, phi, &ip);
+        else
+            ang2pix_ring(nside, theta, phi, &ip);
+        return mask[ip] * rad;
+    }
+};
+
+struct ConstantSelection : public SelectionFuncImpl {  // BoxSurvey.cpp:61-75
+    double v;
+    double evaluate(double, double, double) { return v; }
+};
 
 void to_cell(const double* c, Cell& cell) {
     memset(&cell, 0, sizeof(Cell));
@@ -176,6 +201,57 @@ int ref_write_cells(const char* path, int coordsys, const double* grid, const in
     cfg_destroy(opts);
     delete sv;
     return 0;
+}
+
+}  // extern "C"
+
+extern "C" {
+
+// HEALPix pixel of each (theta, phi) by the reference's ang2pix_ring / ang2pix_nest (chealpix.c:100-246).
+void ref_ang2pix(long nside, int nest, int n, const double* theta, const double* phi, long* pix) {
+    for (int i = 0; i < n; i++) {
+        if (nest)
+            ang2pix_nest(nside, theta[i], phi[i], &pix[i]);
+        else
+            ang2pix_ring(nside, theta[i], phi[i], &pix[i]);
+    }
+}
+
+// The reference cell builder (basis.cpp:160-190): every grid cell by Survey::CreateEmptyCell,
+// Veff and Nbar by FinalizeCell (adaptive cubature, epsrel 1e-5) of the constant selection
+// (coordsys 1) or the radial-spline x HEALPix-map selection (coordsys 2; nside 0 = no map).
+// out[c] = (Veff, Nbar, kept) per cell in grid order.
+void ref_basis(int coordsys, const double* grid, const int* n, double nbar_const, int nrad, const double* rad_r,
+               const double* rad_n, long nside, int nest, const float* mask, double* out) {
+    Survey* s = make_survey(coordsys, grid, n, 0.0);
+    // the bounds exactly (the configuration text above keeps 6 significant digits)
+    s->Min1 = grid[0]; s->Max1 = grid[1];
+    s->Min2 = grid[2]; s->Max2 = grid[3];
+    s->Min3 = grid[4]; s->Max3 = grid[5];
+    SelectionFunc sel;
+    if (coordsys == CoordSysCartesian) {
+        ConstantSelection* c = new ConstantSelection;
+        c->v = nbar_const;
+        sel = SelectionFunc(c);
+    } else {
+        ArraySphericalSelection* a = new ArraySphericalSelection;
+        a->nside = nside;
+        a->nest = nest;
+        if (nside > 0) a->mask.assign(mask, mask + 12 * nside * nside);
+        a->radial = LinearSpline(nrad, rad_r, rad_n);
+        sel = SelectionFunc(a);
+    }
+    long k = 0;
+    for (int d1 = 0; d1 < n[0]; d1++)
+        for (int d2 = 0; d2 < n[1]; d2++)
+            for (int d3 = 0; d3 < n[2]; d3++, k++) {
+                Cell c = s->CreateEmptyCell(d1, d2, d3);
+                bool kept = FinalizeCell(coordsys, c, sel, 1e-5, 1e-10);
+                out[3 * k] = kept ? c.Veff : 0.0;
+                out[3 * k + 1] = kept ? c.Nbar : 0.0;
+                out[3 * k + 2] = kept ? 1.0 : 0.0;
+            }
+    delete s;
 }
 
 }  // extern "C"
