@@ -51,7 +51,7 @@ def _compile(src, verbose=False, ptxas_info=False):
     return obj, out
 
 
-PROGRAMS = ("klt", "comma", "dot", "estimate")
+PROGRAMS = ("basis", "klt", "comma", "dot", "estimate", "mockcounts")
 PROG_DIR = os.path.join(HERE, "programs")
 BIN = os.path.join(HERE, "bin")
 

@@ -81,3 +81,41 @@ def test_programs_reject_missing_options(tmp_path):
     assert res.returncode == 1 and "missing configuration options" in res.stderr
     res = subprocess.run([os.path.join(BIN, "klt"), "-h"], capture_output=True, text=True)
     assert res.returncode == 0 and "Usage: klt" in res.stdout
+
+
+def test_basis_and_mockcounts_programs(tmp_path):
+    """basis writes the cell list (radial selection, quirk off and on), mockcounts the counts per
+    cell; both equal the library's own calls."""
+    from opsec_gpu import build
+
+    build.build()
+    sv = synth.Survey(2, (200.0, 1000.0, -1.0, 1.0, 0.0, 2 * np.pi), (4, 4, 8))
+    rr = np.linspace(150.0, 1100.0, 12)
+    rn = 3e-4 * np.exp(-((rr - 600.0) / 250.0) ** 2)
+    rad = tmp_path / "radial.dat"
+    rad.write_text("".join(f"{a!r} {b!r}\n" for a, b in zip(rr, rn)))
+    k, P = synth.pk_table()
+    pk = tmp_path / "pk.dat"
+    synth.write_pkfile(str(pk), k, P)
+    bands = synth.band_edges(2, 0.0, 0.1)
+    for quirk in (0, 1):
+        cells_f, counts_f = tmp_path / f"cells{quirk}.abn", tmp_path / f"counts{quirk}.abn"
+        cfg = api.make_config(sv, bands=bands, pkfile=str(pk), extra=(
+            f"survey.radial = {rad}", f"basis.quirk3 = {quirk}", f"cellfile = {cells_f}", f"countfile = {counts_f}",
+            "mock.seed = 7", "mock.ngrid = 32"))
+        cfgfile = tmp_path / f"opsec{quirk}.cfg"
+        cfgfile.write_text(cfg)
+        run("basis", cfgfile)
+        run("mockcounts", cfgfile)
+        opts, data = formats.read(str(cells_f))
+        cells = np.frombuffer(data.tobytes(), dtype=synth.CELL_DTYPE)
+        assert int(opts["Ncells"]) == cells.size == 128
+        _, counts = formats.read(str(counts_f))
+        e = api.Engine(api.make_config(sv, bands=bands, extra=(f"basis.quirk3 = {quirk}",)))
+        e.set_pk(k, P)
+        e.set_radial(rr, rn)
+        ref = e.basis()
+        ref_counts = e.mock_counts(ref, ngrid=32, seed=7)
+        e.close()
+        assert np.array_equal(cells.view(np.uint8), ref.view(np.uint8))
+        assert np.array_equal(counts, ref_counts)
