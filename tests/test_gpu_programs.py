@@ -93,7 +93,7 @@ def test_basis_and_mockcounts_programs(tmp_path):
     rr = np.linspace(150.0, 1100.0, 12)
     rn = 3e-4 * np.exp(-((rr - 600.0) / 250.0) ** 2)
     rad = tmp_path / "radial.dat"
-    rad.write_text("".join(f"{a!r} {b!r}\n" for a, b in zip(rr, rn)))
+    rad.write_text("".join(f"{float(a)!r} {float(b)!r}\n" for a, b in zip(rr, rn)))
     k, P = synth.pk_table()
     pk = tmp_path / "pk.dat"
     synth.write_pkfile(str(pk), k, P)
