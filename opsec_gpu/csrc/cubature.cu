@@ -400,7 +400,9 @@ struct WinPlan {
     int flush;    // second-cell points per FP32 partial histogram before the FP64 flush (0: no flush)
     int dot64;    // dot products in FP64 (1) or in FP32 chunks of kDotChunk bins (0)
     float qinv;   // coarse fixed-point units per unit of pair weight (2^k / largest pair weight)
-    float qfine;  // pair weight per unit of the 64-bit histogram (2^-20 / qinv)
+    float qfrac;  // fraction units per coarse unit (2^fbits)
+    int fbits;
+    float qfine;  // pair weight per unit of the 64-bit histogram (2^-fbits / qinv)
     int nbucket;  // nx + 1: bucket nx holds the near keys
     int2* win;        // [nkeys]: (bucket, width); bucket -1 = key copied by the reflection fill
     int* order;       // [2 nkeys]: far keys by bucket, then near keys, then overflows
@@ -567,12 +569,14 @@ __global__ void bucket_scatter_kernel(long long nkeys, WinPlan w) {
 }
 
 // Histogram bins hold sum w_p w_q (1-fr) and sum w_p w_q fr, in fixed point:
-// each contribution is scaled so that the largest pair weight is 2^21 coarse
-// units, rounded once in FP32 (the product), split into its integer part and
-// its fraction in 2^-20 units, and added with two native 32-bit integer
-// shared-memory atomics; every `flush` second-cell points (Cartesian) or every
-// 32 node pairs (spherical) the two partial sums move into a 64-bit integer
+// each contribution is scaled so that the largest pair weight is 2^k coarse
+// units (k = 18 for 4^3 x 4^3 points), rounded once in FP32 (the product),
+// split into its integer part and its fraction in 2^-k units, and added with
+// two native 32-bit integer shared-memory atomics; neither partial sum can
+// overflow within a pass, at whose end they move into a 64-bit integer
 // histogram.  The sums are exact and independent of the order of the atomics.
+// (64-bit integer shared atomics instead: cubature 90 ms against 66 ms at 32k
+// cells.)
 // (FP32 shared-memory atomics were slower -- the counters showed them retried
 // -- and their rounding grows with the partial sum: a bin summed in FP32 over
 // a whole key carries rounding relative to its positive sum into the strongly
@@ -587,20 +591,21 @@ __global__ void bucket_scatter_kernel(long long nkeys, WinPlan w) {
 __device__ __forceinline__ int fix_round(float v) { return __float_as_int(v + 12582912.f) - 0x4B400000; }
 
 // Add x (in units of the coarse quantum) to bin b of the fixed-point partial histogram:
-// the integer part into hqa, the fraction in units of 2^-20 into hqb (both native integer
-// shared atomics, exact and order-independent).  x - floor(x) is exact in FP32.
-__device__ __forceinline__ void add_fixed(int* hqa, int* hqb, int b, float x) {
+// the integer part into hqa, the fraction in units of 1/frac (a power of two) into hqb
+// (both native integer shared atomics, exact and order-independent).  x - floor(x) is
+// exact in FP32.
+__device__ __forceinline__ void add_fixed(int* hqa, int* hqb, int b, float x, float frac) {
     const float a = floorf(x);
     atomicAdd(&hqa[b], fix_round(a));
-    atomicAdd(&hqb[b], fix_round((x - a) * 1048576.f));
+    atomicAdd(&hqb[b], fix_round((x - a) * frac));
 }
 
-// Move the partial sums into the 64-bit histogram (units of 2^-20 of the coarse quantum:
+// Move the partial sums into the 64-bit histogram (units of 2^-fbits of the coarse quantum:
 // exact) and clear them.  Warp-wide.
-__device__ __forceinline__ void flush_fixed(int* hqa, int* hqb, long long* hm, int n, int lane) {
+__device__ __forceinline__ void flush_fixed(int* hqa, int* hqb, long long* hm, int n, int lane, int fbits) {
     __syncwarp();
     for (int b = lane; b < n; b += 32) {
-        hm[b] += ((long long)hqa[b] << 20) + hqb[b];
+        hm[b] += ((long long)hqa[b] << fbits) + hqb[b];
         hqa[b] = 0;
         hqb[b] = 0;
     }
@@ -748,15 +753,14 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
                                 bad += out;
                                 const float ww = (lsum < NG - 1 ? 2.f : 1.f) * Ah.w * B.w;
                                 const float wq = ww * w.qinv;  // fixed point: the largest pair weight -> 2^k units
-                                add_fixed(hqa, hqb, bi, fmaf(-wq, fr, wq));
-                                add_fixed(hqa, hqb, bi + 1, wq * fr);
+                                add_fixed(hqa, hqb, bi, fmaf(-wq, fr, wq), w.qfrac);
+                                add_fixed(hqa, hqb, bi + 1, wq * fr, w.qfrac);
                             }
                         }
                     }
-                    if (w.flush) flush_fixed(hqa, hqb, hm, segw, lane);
                 }
             }
-            if (!w.flush) flush_fixed(hqa, hqb, hm, segw, lane);
+            flush_fixed(hqa, hqb, hm, segw, lane, w.fbits);
             // the histogram as FP32 values once (over the partial sums, which are zero now)
             if (!w.dot64)
                 for (int b = lane; b < segw; b += 32) hp[b] = (float)hm[b] * w.qfine;
@@ -910,14 +914,13 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
                             bad += out;
                             const float ww = wpq * sp.z;
                             const float wq = ww * w.qinv;  // fixed point: the largest pair weight -> 2^k units
-                            add_fixed(hqa, hqb, bi, fmaf(-wq, fr, wq));
-                            add_fixed(hqa, hqb, bi + 1, wq * fr);
+                            add_fixed(hqa, hqb, bi, fmaf(-wq, fr, wq), w.qfrac);
+                            add_fixed(hqa, hqb, bi + 1, wq * fr, w.qfrac);
                         }
                     }
                 }
-                if (w.flush) flush_fixed(hqa, hqb, hm, segw, lane);
             }
-            if (!w.flush) flush_fixed(hqa, hqb, hm, segw, lane);
+            flush_fixed(hqa, hqb, hm, segw, lane, w.fbits);
             // the histogram as FP32 values once (over the partial sums, which are zero now)
             if (!w.dot64)
                 for (int b = lane; b < segw; b += 32) hp[b] = (float)hm[b] * w.qfine;
@@ -1076,17 +1079,19 @@ bool run_window(const CubatureArgs& a, const Lookup& lk, cudaStream_t s, long lo
     w.dot64 = a.win_dot64;
     const bool sph = a.coordsys == 2;
     {
-        // Fixed-point partial histograms: at most `pairs` contributions reach one bin between
-        // flushes, each at most the largest pair weight (mirror factor 2 included), so with
-        // that weight at 2^k coarse units (and fractions in 2^-20 of a unit) both partial
-        // sums stay below 2^30; a key's 64-bit total stays below 2^(k + 20 + 13).
+        // Fixed-point partial histograms, summed over a whole pass: at most `pairs`
+        // contributions reach one bin (every evaluated pair of a key), each at most the
+        // largest pair weight (mirror factor 2 included).  With that weight at 2^k coarse
+        // units and fractions in 2^-k of a unit, both partial sums stay below 2^30; the
+        // quantum is 2^-2k of the largest weight (2^-36 for 4^3 x 4^3 points).
         constexpr int NP = FarShape<NG>::NP, NC = NG * (NG + 1) / 2;
-        const double pairs = sph ? (w.flush ? 32.0 * NC : (double)NG * NG * NG * NG * NC)
-                                 : (w.flush ? 32.0 * w.flush : (double)NP * NP);
+        const double pairs = sph ? (double)NG * NG * NG * NG * NC : (double)NP * NP;
         const int k = std::min(21, 30 - (int)std::ceil(std::log2(pairs)));
         const double wwmax = 2.0 * std::pow(a.wmax, 6) * (1.0 + 1e-6);
         w.qinv = (float)(std::ldexp(1.0, k) / wwmax);
-        w.qfine = (float)(wwmax / std::ldexp(1.0, k + 20));
+        w.fbits = k;
+        w.qfrac = (float)std::ldexp(1.0, k);
+        w.qfine = (float)(wwmax / std::ldexp(1.0, 2 * k));
     }
     const void* kfn = sph ? (const void*)cubature_far_sph_kernel<NG> : (const void*)cubature_far_kernel<NG>;
     if (w.Wkey < 8 || far_smem<NG>(w, sph) > (size_t)max_dynamic_smem(kfn)) return false;
