@@ -128,6 +128,30 @@ def test_cubature_window_path(name):
         assert e_win <= 3e-7 and e_grp <= 3e-7, (name, t, e_win, e_grp)
 
 
+@pytest.mark.parametrize("gauss", [2, 3, 5])
+@pytest.mark.parametrize("name", ["shell", "box"])
+def test_cubature_window_gauss_orders(name, gauss):
+    """The window kernels at Gauss orders other than 4: their lane maps (node pairs per lane,
+    canonical mirror pairs, 2^k fixed-point scale) change with the order."""
+    if name == "shell":
+        sv, cells = synth.shell_survey(4, 4, 8)
+        bands = synth.band_edges(10, 0.0, 0.4)
+    else:
+        sv, cells = synth.box_survey(4)
+        bands = synth.band_edges(10, 0.0, 0.2)
+    layout = O.LAYOUT_LOG4096
+    e = api.Engine(api.make_config(sv, bands=bands, layout=layout, gauss=gauss))
+    e.set_pk(*PK)
+    got = [e.signal_block(cells, table=t) for t in (0, 5, 10)]
+    e.close()
+    tabs = O.xi_tables(*PK, bands, layout)
+    Q = O.qtable_keys(sv, O.keys_all(sv), tabs[[0, 5, 10]], layout, ng=gauss)
+    for j, t in enumerate((0, 5, 10)):
+        ref = O.signal_matrix(sv, cells, Q[:, j])
+        err = np.max(np.abs(got[j] - ref)) / np.max(np.abs(ref))
+        assert err <= 3e-7, (name, gauss, t, err)
+
+
 def test_cubature_precision_key_is_checked():
     sv, _ = CASES["box4"]
     with pytest.raises(api.OpsecError):
