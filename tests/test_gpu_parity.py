@@ -132,7 +132,10 @@ def test_cubature_window_path(name):
 @pytest.mark.parametrize("name", ["shell", "box"])
 def test_cubature_window_gauss_orders(name, gauss):
     """The window kernels at Gauss orders other than 4: their lane maps (node pairs per lane,
-    canonical mirror pairs, 2^k fixed-point scale) change with the order."""
+    canonical mirror pairs, 2^k fixed-point scale) change with the order.  A wrong pair or
+    weight would show at 1e-3 or more.  The 4^3 box has cells of 150 Mpc/h: a self pair spans
+    separations 0-260 across several periods of the band tables, whose strong cancellation lifts
+    the FP32-table floor to ~1e-6 of max|S| (the table-group kernel: 8e-7 at order 5)."""
     if name == "shell":
         sv, cells = synth.shell_survey(4, 4, 8)
         bands = synth.band_edges(10, 0.0, 0.4)
@@ -149,7 +152,7 @@ def test_cubature_window_gauss_orders(name, gauss):
     for j, t in enumerate((0, 5, 10)):
         ref = O.signal_matrix(sv, cells, Q[:, j])
         err = np.max(np.abs(got[j] - ref)) / np.max(np.abs(ref))
-        assert err <= 3e-7, (name, gauss, t, err)
+        assert err <= (3e-7 if name == "shell" else 2.5e-6), (name, gauss, t, err)
 
 
 def test_cubature_precision_key_is_checked():
