@@ -398,7 +398,7 @@ struct WinPlan {
     int Wkey;     // histogram bins per warp: one pass covers Wkey - 1 bins of a key's window
     int Wmax;     // widest key window on the window path (npass_max passes)
     int flush;    // second-cell points per FP32 partial histogram before the FP64 flush (0: no flush)
-    int dot64;    // dot products in FP64 (1) or in FP32 chunks of kDotChunk bins (0)
+    int dot64;    // compensated dot products for every key (1) or only where windows cancel strongly (0)
     float qinv;   // coarse fixed-point units per unit of pair weight (2^k / largest pair weight)
     float qfrac;  // fraction units per coarse unit (2^fbits)
     int fbits;
@@ -582,10 +582,9 @@ __global__ void bucket_scatter_kernel(long long nkeys, WinPlan w) {
 // a whole key carries rounding relative to its positive sum into the strongly
 // cancelling dot product with an oscillating band table, 2.2e-6 of max|S| on
 // the 4x4x4 box without flushes.  21 bits without the fraction gave 1.5e-6 on
-// the same box.)  The dot products run in FP32 over chunks of kDotChunk bins
-// added in FP64 (`dot64` = FP64 throughout); lane pairs take the tables and
-// read the bin-major tables from L1/L2, so the tables take no shared memory
-// and two 16-warp CTAs fit on an SM.
+// the same box.)  The dot products (window_dots) read the bin-major tables
+// from L1/L2, so the tables take no shared memory and two 16-warp CTAs fit on
+// an SM.
 
 // round-to-nearest integer of |v| < 2^22 by the FP32 magic-number addition (FMA/ALU pipes)
 __device__ __forceinline__ int fix_round(float v) { return __float_as_int(v + 12582912.f) - 0x4B400000; }
@@ -614,6 +613,65 @@ __device__ __forceinline__ void flush_fixed(int* hqa, int* hqb, long long* hm, i
 
 constexpr int kMaxPasses = 8;  // passes over the point pairs for windows wider than one histogram
 constexpr int kDotChunk = 16;  // bins summed in FP32 per FP64 addition in the window dot products
+
+// Dot products of one pass's histogram (64-bit, bins s0 .. s0 + segw - 1 of the key's window)
+// with every table, added into Q.  Two work items per table, alternate chunks of kDotChunk
+// bins, spread over the lanes (table t: items 2t and 2t+1 on neighbouring lanes, combined by
+// one shuffle).  Far keys: FP32 within a chunk, FP64 across chunks.  Keys whose window
+// reaches the linear section of the table or needs several passes (self and adjacent
+// cells, whose integrals cancel strongly over several periods of a band table) and every
+// key with `dot64`: compensated FP32 -- exact products by FMA, two-sum accumulation, the bin
+// values as FP32 high + low parts -- about FP64 accuracy.  hp and hl are the words of the
+// (now zero) partial sums.  Warp-wide.
+__device__ __forceinline__ void window_dots(const CubatureArgs& a, const WinPlan& w, const long long* hm, float* hp,
+                                            float* hl, int key, int wx, int s0, int segw, int pass, bool precise,
+                                            int lane) {
+    const int ntab = a.ntab;
+    for (int b = lane; b < segw; b += 32) {
+        if (precise) {
+            const double v = (double)hm[b] * (double)w.qfine;
+            const float hi = (float)v;
+            hp[b] = hi;
+            hl[b] = (float)(v - (double)hi);
+        } else {
+            hp[b] = (float)hm[b] * w.qfine;
+        }
+    }
+    __syncwarp();
+    for (int base = 0; base < 2 * ntab; base += 32) {
+        const int it = base + lane;
+        const int t = it >> 1, h = it & 1;
+        double acc = 0.0;
+        if (it < 2 * ntab) {
+            const float* tr = w.tabT + (size_t)(wx + s0) * ntab + t;
+            if (precise) {
+                float sh = 0.f, sl = 0.f;
+                for (int b0 = kDotChunk * h; b0 < segw; b0 += 2 * kDotChunk)
+                    for (int b = b0; b < min(b0 + kDotChunk, segw); b++) {
+                        const float tv = tr[(size_t)b * ntab], v = hp[b];
+                        const float p = tv * v;
+                        float e;
+                        sh = two_sum(sh, p, &e);
+                        sl += e + fmaf(tv, v, -p) + tv * hl[b];
+                    }
+                acc = (double)sh + (double)sl;
+            } else {
+                for (int b0 = kDotChunk * h; b0 < segw; b0 += 2 * kDotChunk) {
+                    float pt = 0.f;
+                    for (int b = b0; b < min(b0 + kDotChunk, segw); b++) pt = fmaf(tr[(size_t)b * ntab], hp[b], pt);
+                    acc += (double)pt;
+                }
+            }
+        }
+        acc += __shfl_xor_sync(0xffffffffu, acc, 1);
+        if (it < 2 * ntab && h == 0) {
+            double* q = a.Q + (size_t)t * a.ks.nkeys + key;
+            *q = pass == 0 ? acc : *q + acc;
+        }
+    }
+    __syncwarp();
+}
+
 
 template <int NG>
 struct FarShape {
@@ -761,37 +819,8 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
                 }
             }
             flush_fixed(hqa, hqb, hm, segw, lane, w.fbits);
-            // the histogram as FP32 values once (over the partial sums, which are zero now)
-            if (!w.dot64)
-                for (int b = lane; b < segw; b += 32) hp[b] = (float)hm[b] * w.qfine;
-            __syncwarp();
-            // Dot products: two work items per table, alternate chunks of kDotChunk bins, spread
-            // over the lanes (table t: items 2t and 2t+1 on neighbouring lanes, combined by
-            // one shuffle); FP32 within a chunk, FP64 across chunks.
-            for (int base = 0; base < 2 * ntab; base += 32) {
-                const int it = base + lane;
-                const int t = it >> 1, h = it & 1;
-                double acc = 0.0;
-                if (it < 2 * ntab) {
-                    const float* tr = w.tabT + (size_t)(wn.x + s0) * ntab + t;
-                    for (int b0 = kDotChunk * h; b0 < segw; b0 += 2 * kDotChunk) {
-                        const int b1 = min(b0 + kDotChunk, segw);
-                        if (w.dot64) {
-                            for (int b = b0; b < b1; b++) acc = fma((double)tr[(size_t)b * ntab], (double)hm[b] * w.qfine, acc);
-                        } else {
-                            float pt = 0.f;
-                            for (int b = b0; b < b1; b++) pt = fmaf(tr[(size_t)b * ntab], hp[b], pt);
-                            acc += (double)pt;
-                        }
-                    }
-                }
-                acc += __shfl_xor_sync(0xffffffffu, acc, 1);
-                if (it < 2 * ntab && h == 0) {
-                    double* q = a.Q + (size_t)t * a.ks.nkeys + key;
-                    *q = pass == 0 ? acc : *q + acc;
-                }
-            }
-            __syncwarp();
+            window_dots(a, w, hm, hp, reinterpret_cast<float*>(hqb), key, wn.x, s0, segw, pass,
+                        w.dot64 || npass > 1 || wn.x < lk.n1, lane);
         }
         if (bad) atomicAdd(w.violations, bad);
     }
@@ -921,34 +950,8 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
                 }
             }
             flush_fixed(hqa, hqb, hm, segw, lane, w.fbits);
-            // the histogram as FP32 values once (over the partial sums, which are zero now)
-            if (!w.dot64)
-                for (int b = lane; b < segw; b += 32) hp[b] = (float)hm[b] * w.qfine;
-            __syncwarp();
-            for (int base = 0; base < 2 * ntab; base += 32) {
-                const int it = base + lane;
-                const int t = it >> 1, h = it & 1;
-                double acc = 0.0;
-                if (it < 2 * ntab) {
-                    const float* tr = w.tabT + (size_t)(wn.x + s0) * ntab + t;
-                    for (int b0 = kDotChunk * h; b0 < segw; b0 += 2 * kDotChunk) {
-                        const int b1 = min(b0 + kDotChunk, segw);
-                        if (w.dot64) {
-                            for (int b = b0; b < b1; b++) acc = fma((double)tr[(size_t)b * ntab], (double)hm[b] * w.qfine, acc);
-                        } else {
-                            float pt = 0.f;
-                            for (int b = b0; b < b1; b++) pt = fmaf(tr[(size_t)b * ntab], hp[b], pt);
-                            acc += (double)pt;
-                        }
-                    }
-                }
-                acc += __shfl_xor_sync(0xffffffffu, acc, 1);
-                if (it < 2 * ntab && h == 0) {
-                    double* q = a.Q + (size_t)t * a.ks.nkeys + key;
-                    *q = pass == 0 ? acc : *q + acc;
-                }
-            }
-            __syncwarp();
+            window_dots(a, w, hm, hp, reinterpret_cast<float*>(hqb), key, wn.x, s0, segw, pass,
+                        w.dot64 || npass > 1 || wn.x < lk.n1, lane);
         }
         if (bad) atomicAdd(w.violations, bad);
     }
