@@ -151,6 +151,12 @@ def tensor_roofline(s1, bf16, peak_kind):
 # loop control (about 2).
 FAR_OPS_PER_PAIR = 100
 
+# DRAM bytes (read + written) per canonical key of the spherical window kernel, from one ncu
+# capture on the inner half of the 32k-cell shell (profiles/cubature_far_sph_c2inner.md:
+# 1.114 GB + 1.239 GB over 1,118,464 keys); the kernel's traffic grows with the keys it
+# integrates (Q written per key and table), so a launch's traffic is this x its keys.
+FAR_TRAFFIC_PER_KEY = (1.114271e9 + 1.239336e9) / 1118464
+
 
 def roofline(stats, clk, bf16, peak_kind):
     """Roofline of the kernel with the most device time in the timed builds."""
@@ -171,9 +177,11 @@ def roofline(stats, clk, bf16, peak_kind):
         avg_s = f["ms"] / 1000.0 / f["count"]
         achieved = f["flops"] / f["count"] / avg_s / 1e9
         st = stats["cubature"]
+        keys = f["flops"] / f["count"] / 4096.0  # algorithmic pairs per launch / pairs per key (4^3 x 4^3 rule)
         return {"kernel": "cubature_far_sph_kernel / cubature_far_kernel (window histograms)", "bound": "issue",
                 "achieved": achieved, "peak": peak, "unit": "G point pairs/s", "frac": achieved / peak,
-                "traffic": None,
+                "traffic": FAR_TRAFFIC_PER_KEY * keys,
+                "traffic_note": "DRAM bytes per launch: ncu bytes per key on the 16x32x32 shell x this launch's keys",
                 "peak_kind": f"derived: 128 lane instructions/clk/SM x {nsm} SMs x {mhz:.0f} MHz (sampled median)"
                              f" / {FAR_OPS_PER_PAIR} instructions per point pair of the direct exact method",
                 "algorithmic_unit": "one Gauss-point pair (all xi tables at once)", "avg_launch_ms": avg_s * 1000,
