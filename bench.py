@@ -329,6 +329,26 @@ def cpu_baseline_obj(w, cores):
             "stages_s": {k: v for k, v in s.items() if k.endswith("_s")}}
 
 
+# ---------------------------------------------------------------- ranks
+def max_over_ranks(values, dist=None):
+    """Each value's maximum over the ranks of the process group (the slowest replica's
+    times); the values themselves with one rank.  CUDA tensors under NCCL, CPU under gloo."""
+    if dist is None:
+        return [float(v) for v in values]
+    import torch
+
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t.cpu()]
+
+
+def whole_job_seconds_per_build(per_build_max, world):
+    """N replicas each build their own survey in the slowest replica's time: the job
+    completes a build every per_build_max / N seconds."""
+    return per_build_max / world
+
+
 # ---------------------------------------------------------------- main
 def main():
     ap = argparse.ArgumentParser()
@@ -441,10 +461,7 @@ def main():
 
     per_build_dev = dev_ms / 1000.0 / args.steps
     per_build_wall = wall / args.steps
-    if dist is not None:
-        t = torch.tensor([per_build_dev, per_build_wall], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        per_build_dev, per_build_wall = float(t[0]), float(t[1])
+    per_build_dev, per_build_wall = max_over_ranks([per_build_dev, per_build_wall], dist)
     if rank != 0:
         eng.close()
         dist.destroy_process_group() if dist is not None else None
@@ -483,7 +500,7 @@ def main():
     metric = METRIC if args.form == "plain" else METRIC.replace("plain GPU form", "surrogate form")
     if w["name"] != "c2":  # other workloads name their own size
         metric = metric.replace("at 32k cells", f"at {int(w['cells'].size) // 1024}k cells ({w['name']})")
-    line = {"metric": metric, "value": per_build_dev / world, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+    line = {"metric": metric, "value": whole_job_seconds_per_build(per_build_dev, world), "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": per_build_wall * 1000, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f16x3+f32+f64", "data": "synthetic",
             "config": {"workload": w["name"], "cells": int(cells.size), "bands": nb, "modes": w["nmodes"],
