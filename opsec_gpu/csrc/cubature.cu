@@ -921,7 +921,7 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
                     const float B4h = 4.f * t0;
                     const float B4l = 4.f * (fmaf(A.x, B.x, -t0) + fmaf(A.x, B.y, A.y * B.x));
                     const float wpq = s_wrm[P] * s_wrm[Q];
-#pragma unroll
+#pragma unroll 2
                     for (int j = 0; j < NC; j++) {
                         const float4 sp = SP[j];
                         if (filt) {
