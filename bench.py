@@ -158,7 +158,7 @@ FAR_OPS_PER_PAIR = 100
 FAR_TRAFFIC_PER_KEY = (1.114271e9 + 1.239336e9) / 1118464
 
 
-def roofline(stats, clk, bf16, peak_kind):
+def roofline(stats, clk, hbm, bf16, peak_kind, ntab):
     """Roofline of the kernel with the most device time in the timed builds."""
     dom = max(stats, key=lambda n: stats[n]["ms"])
     s = stats[dom]
@@ -167,25 +167,36 @@ def roofline(stats, clk, bf16, peak_kind):
     if dom in ("cubature", "cubature_far") and stats.get("cubature_far", {}).get("count", 0) > 0:
         # The cubature stage's dominant kernel is the far-key window kernel: per key one pass over
         # the 4096 Gauss-point pairs scatters interpolation weights into a bin histogram, then one
-        # dot product per table, so its work is point pairs, each FAR_OPS_PER_PAIR instructions,
-        # against the instruction issue rate: 4 schedulers x 32 lanes per clock per SM.  No
-        # measured figure exists for issue: derived from the SM count and the sampled clock.
+        # dot product per table.  Against HBM (the roofline bound reported): its algorithmic bytes
+        # are the Q values it must write, 8 bytes per key and table (its inputs -- per-arc node
+        # tables, the bin-major xi tables -- are a few MB and stay in L2); it is far from that
+        # bound.  What bounds it is instruction issue (roofline_issue below): point pairs, each
+        # FAR_OPS_PER_PAIR instructions of the direct exact method, against 4 schedulers x 32
+        # lanes per clock per SM (no measured figure exists for issue: derived from the SM count
+        # and the sampled clock).
         f = stats["cubature_far"]
+        avg_s = f["ms"] / 1000.0 / f["count"]
+        keys = f["flops"] / f["count"] / 4096.0  # algorithmic pairs per launch / pairs per key (4^3 x 4^3 rule)
+        alg_bytes = 8.0 * ntab * keys
+        achieved_gbs = alg_bytes / avg_s / 1e9
         nsm = 152
         mhz = clk.get("sm_mhz") or 2070.0
-        peak = 128.0 * nsm * mhz * 1e6 / FAR_OPS_PER_PAIR / 1e9
-        avg_s = f["ms"] / 1000.0 / f["count"]
-        achieved = f["flops"] / f["count"] / avg_s / 1e9
+        ipeak = 128.0 * nsm * mhz * 1e6 / FAR_OPS_PER_PAIR / 1e9
+        iach = f["flops"] / f["count"] / avg_s / 1e9
         st = stats["cubature"]
-        keys = f["flops"] / f["count"] / 4096.0  # algorithmic pairs per launch / pairs per key (4^3 x 4^3 rule)
-        return {"kernel": "cubature_far_sph_kernel / cubature_far_kernel (window histograms)", "bound": "issue",
-                "achieved": achieved, "peak": peak, "unit": "G point pairs/s", "frac": achieved / peak,
+        return {"kernel": "cubature_far_sph_kernel / cubature_far_kernel (window histograms)", "bound": "hbm",
+                "achieved": achieved_gbs, "peak": hbm, "unit": "GB/s", "frac": achieved_gbs / hbm,
                 "traffic": FAR_TRAFFIC_PER_KEY * keys,
+                "peak_kind": f"{peak_kind} HBM copy bandwidth",
+                "algorithmic_bytes_per_launch": alg_bytes,
                 "traffic_note": "DRAM bytes per launch: ncu bytes per key on the 16x32x32 shell x this launch's keys",
-                "peak_kind": f"derived: 128 lane instructions/clk/SM x {nsm} SMs x {mhz:.0f} MHz (sampled median)"
-                             f" / {FAR_OPS_PER_PAIR} instructions per point pair of the direct exact method",
-                "algorithmic_unit": "one Gauss-point pair (all xi tables at once)", "avg_launch_ms": avg_s * 1000,
-                "launches": int(f["count"]),
+                "binding": "instruction issue, not HBM: see roofline_issue",
+                "avg_launch_ms": avg_s * 1000, "launches": int(f["count"]),
+                "roofline_issue": {"achieved": iach, "peak": ipeak, "unit": "G point pairs/s", "frac": iach / ipeak,
+                                   "peak_kind": f"derived: 128 lane instructions/clk/SM x {nsm} SMs x {mhz:.0f} MHz "
+                                                f"(sampled median) / {FAR_OPS_PER_PAIR} instructions per point pair "
+                                                f"of the direct exact method",
+                                   "algorithmic_unit": "one Gauss-point pair (all xi tables at once)"},
                 "stage_xi_evaluations_per_s": st["flops"] / (st["ms"] / 1000.0) if st["ms"] > 0 else None}
     if dom == "project_step1":
         return tensor_roofline(s, bf16, peak_kind)
@@ -477,7 +488,7 @@ def main():
         surr = {"training": surr_info, **eng.surrogate_stats(),
                 "fisher_rel_err_vs_plain": float(np.max(np.abs(res["F"] - ref["F"])) / np.max(np.abs(ref["F"])))}
     hbm, bf16, peak_kind = peaks()
-    roof = roofline(stats, clk, bf16, peak_kind)
+    roof = roofline(stats, clk, hbm, bf16, peak_kind, w["nbands"] + 1)
     # the fused tensor-core projection is the path for every non-azimuthal geometry and for the
     # comma drop-in; its roofline is taken on a one-band build of the same cells and modes
     roof_tc = None
