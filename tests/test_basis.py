@@ -105,3 +105,31 @@ def test_gpu_basis_matches_reference_and_oracle():
         keep = mine[:, 1] > 0
         assert cells.size == int(np.sum(keep))
         assert np.allclose(cells["Nbar"], mine[keep, 1], rtol=1e-12)
+
+
+@pytest.mark.gpu
+def test_new_entry_points_reject_bad_arguments():
+    """Invalid sizes and states return errors (no fault, no partial output)."""
+    sv = synth.Survey(2, G["sph_grid"], G["sph_n"])
+    e = _engine(sv)
+    with pytest.raises(api.OpsecError):
+        e.basis()                      # no radial selection yet
+    with pytest.raises(api.OpsecError):
+        e.set_radial([1.0], [2.0])     # one point
+    with pytest.raises(api.OpsecError):
+        e.set_radial([2.0, 1.0], [1.0, 1.0])  # decreasing abscissae
+    with pytest.raises(api.OpsecError):
+        e.set_mask(3, True, np.ones(12 * 9, dtype=np.float32))  # NESTED needs a power of two
+    with pytest.raises(api.OpsecError):
+        e.ang2pix(0, 0, [0.1], [0.2])
+    e.set_radial(*(G["rad_r"], G["rad_n"]))
+    cells = e.basis()
+    assert cells.size == int(np.prod(G["sph_n"]))
+    with pytest.raises(api.OpsecError):
+        e.mock_counts(cells, ngrid=33)  # odd mesh
+    with pytest.raises(api.OpsecError):
+        e.mock_counts(cells, ngrid=2)
+    # a negative bias beyond -1/delta clips lambda at zero: counts stay non-negative integers
+    c = e.mock_counts(cells, ngrid=16, seed=3, bias=-50.0)
+    assert np.all(c >= 0) and np.all(c == np.floor(c))
+    e.close()
