@@ -397,7 +397,7 @@ __global__ void __launch_bounds__(Shape<NG>::kWarps * 32, 1)
 struct WinPlan {
     int Wkey;     // histogram bins per warp: one pass covers Wkey - 1 bins of a key's window
     int Wmax;     // widest key window on the window path (npass_max passes)
-    int flush;    // second-cell points per FP32 partial histogram before the FP64 flush (0: no flush)
+    int flush;    // Cartesian window kernel: second-cell points per loop chunk (0: all)
     int dot64;    // compensated dot products for every key (1) or only where windows cancel strongly (0)
     float qinv;   // coarse fixed-point units per unit of pair weight (2^k / largest pair weight)
     float qfrac;  // fraction units per coarse unit (2^fbits)

@@ -115,7 +115,7 @@ struct CubatureArgs {
     int exact = 1;       // FP32-pair separations and table index (1) or plain FP32 (0)
     int window = 1;      // exact mode: per-key bin-window histograms for the far keys (1) or table groups only (0)
     int win_key = 384;   // widest key window (bins) on the window path
-    int win_flush = 8;   // window histograms: second-cell points per FP32 partial sum before the FP64 flush (0: none)
+    int win_flush = 8;   // Cartesian window kernel: second-cell points per loop chunk (0: all)
     int win_dot64 = 0;   // window dot products in FP64 (1) or FP32 chunks of 8 bins added in FP64 (0)
     void* work = nullptr;  // cubature_work_bytes() of scratch for the window path
     size_t work_bytes = 0;
