@@ -182,6 +182,17 @@ typedef struct {
 int opsec_gpu_batch_fisher(opsec_gpu* ctx, int nmocks, const opsec_mock* mocks, int workers, double* F,
                            double* phat, double* pcov, double* stats);
 
+/* Weighted galaxy counts per cell (dot.cpp:95-130): gals holds ngal records
+ * (x1, x2, x3, w) as float32 -- the survey's galaxy file, ABN format "4f"
+ * (Survey.h:14-19) -- in the survey's coordinates (x, y, z or r, mu, phi);
+ * each goes to its grid cell (Survey::GetGridIndex, Survey.cpp:93-101).
+ * counts[a] (ncells) receives the weight in cell a; *outside (may be NULL) the
+ * weight of galaxies outside the grid or in grid cells without a listed cell.
+ * Unlike the reference, galaxies in the cell at grid index 0 are counted there
+ * (dot.cpp:127 tests e > 0). */
+int opsec_gpu_count_galaxies(opsec_gpu* ctx, int ncells, const opsec_cell* cells, long long ngal, const float* gals,
+                             double* counts, double* outside);
+
 /* The cell builder (replaces basis.cpp:89-128, 160-201 with FinalizeCell's
  * adaptive cubature): every cell of the configured grid whose expected count
  * Nbar is positive, numbered in grid order (d1, d2, d3), with its bounds

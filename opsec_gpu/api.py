@@ -69,6 +69,7 @@ def load():
     L.opsec_gpu_batch_fisher.argtypes = [vp, C.c_int, vp, C.c_int, dp, dp, dp, dp]
     L.opsec_gpu_mock_counts.argtypes = [vp, C.c_int, vp, C.c_int, C.c_ulonglong, C.c_double, dp, dp]
     L.opsec_gpu_set_radial.argtypes = [vp, C.c_int, dp, dp]
+    L.opsec_gpu_count_galaxies.argtypes = [vp, C.c_int, vp, C.c_longlong, C.POINTER(C.c_float), dp, dp]
     L.opsec_gpu_set_mask.argtypes = [vp, C.c_longlong, C.c_int, C.POINTER(C.c_float)]
     L.opsec_gpu_basis.argtypes = [vp, C.c_int, vp, ip]
     L.opsec_gpu_ang2pix.argtypes = [vp, C.c_longlong, C.c_int, C.c_int, dp, dp, C.POINTER(C.c_longlong)]
@@ -226,6 +227,16 @@ class Engine:
         self._check(self._L.opsec_gpu_dot(self._h, cells.size, cells.ctypes.data, _d(counts), modes.shape[0],
                                           _d(modes), _d(y)))
         return y
+
+    def count_galaxies(self, cells, gals):
+        """Weighted counts per cell of galaxies (n x 4 float32: x1, x2, x3, w); returns (counts, outside)."""
+        cells = _cells(cells)
+        g = np.ascontiguousarray(gals, dtype=np.float32).reshape(-1, 4)
+        counts = np.zeros(cells.size)
+        out = np.zeros(1)
+        self._check(self._L.opsec_gpu_count_galaxies(self._h, cells.size, cells.ctypes.data, g.shape[0], _fp(g),
+                                                     _d(counts), _d(out)))
+        return counts, float(out[0])
 
     def set_radial(self, r, nbar):
         r, nbar = _f64(r), _f64(nbar)

@@ -1868,6 +1868,47 @@ int opsec_gpu_dot(opsec_gpu* c, int ncells, const opsec_cell* cells, const doubl
     });
 }
 
+int opsec_gpu_count_galaxies(opsec_gpu* c, int ncells, const opsec_cell* cells, long long ngal, const float* gals,
+                             double* counts, double* outside) {
+    return guard(c, [&] {
+        const Geometry& g = c->geo;
+        const long long grid = (long long)g.n[0] * g.n[1] * g.n[2];
+        if (ncells <= 0 || !cells || !counts || ngal < 0 || (ngal > 0 && !gals) || grid <= 0)
+            fail(OPSEC_ERR_ARG, "invalid galaxy-count arguments");
+        // grid index -> cell (dot.cpp:105-117)
+        std::vector<int> map((size_t)grid, -1);
+        for (int a = 0; a < ncells; a++) {
+            const opsec_cell& e = cells[a];
+            if (e.d1 < 0 || e.d1 >= g.n[0] || e.d2 < 0 || e.d2 >= g.n[1] || e.d3 < 0 || e.d3 >= g.n[2])
+                fail(OPSEC_ERR_ARG, "cell " + std::to_string(a) + " lies outside the survey grid");
+            map[((size_t)e.d1 * g.n[1] + e.d2) * g.n[2] + e.d3] = a;
+        }
+        DevBuf<int> d_map;
+        DevBuf<double> d_counts;
+        DevBuf<float> d_gal;
+        d_map.alloc((size_t)grid);
+        d_counts.alloc((size_t)ncells + 1);
+        d_gal.alloc((size_t)4 * std::max<long long>(ngal, 1));
+        OPSEC_CUDA(cudaMemcpyAsync(d_map.p, map.data(), sizeof(int) * map.size(), cudaMemcpyHostToDevice, c->stream));
+        if (ngal > 0)
+            OPSEC_CUDA(cudaMemcpyAsync(d_gal.p, gals, sizeof(float) * 4 * (size_t)ngal, cudaMemcpyHostToDevice,
+                                       c->stream));
+        GridBox box;
+        for (int ax = 0; ax < 3; ax++) {
+            box.lo[ax] = g.b[2 * ax];
+            box.hi[ax] = g.b[2 * ax + 1];
+            box.n[ax] = g.n[ax];
+        }
+        launch_galaxy_counts(ngal, reinterpret_cast<const float4*>(d_gal.p), box, d_map.p, ncells, d_counts.p,
+                             c->stream, &c->launches);
+        OPSEC_CUDA(cudaMemcpyAsync(counts, d_counts.p, sizeof(double) * ncells, cudaMemcpyDeviceToHost, c->stream));
+        double out = 0.0;
+        OPSEC_CUDA(cudaMemcpyAsync(&out, d_counts.p + ncells, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+        sync(c);
+        if (outside) *outside = out;
+    });
+}
+
 int opsec_gpu_set_radial(opsec_gpu* c, int n, const double* r, const double* nbar) {
     return guard(c, [&] {
         if (n < 2 || !r || !nbar) fail(OPSEC_ERR_ARG, "the radial selection needs at least two points");

@@ -282,6 +282,15 @@ void launch_scale_modes(int ncells, int nmodes, const double* modes, const doubl
 // packed FP32 -> FP64
 void launch_widen(size_t n, const float* in, double* out, cudaStream_t s, long long* launches);
 
+// Weighted galaxy counts per cell (signal.cu); counts has ncells + 1 entries, the last
+// for galaxies outside every cell.
+struct GridBox {
+    double lo[3], hi[3];
+    int n[3];
+};
+void launch_galaxy_counts(long long ngal, const float4* gal, const GridBox& g, const int* cellmap, int ncells,
+                          double* counts, cudaStream_t st, long long* l);
+
 // Cell builder (basis.cu): Veff and Nbar of every grid cell.
 struct BasisArgs {
     int coordsys;           // 1 Cartesian (constant nbar), 2 spherical (radial spline x map)

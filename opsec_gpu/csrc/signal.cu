@@ -140,6 +140,30 @@ __global__ void azimuthal_scatter_kernel(int M, const int* mode_m, const int* mo
     }
 }
 
+// Weighted galaxy counts per cell (dot.cpp:105-130): each galaxy (x1, x2, x3, w) in the
+// survey's coordinates goes to the grid cell of Survey::GetGridIndex (Survey.cpp:93-101,
+// floor per axis in FP64), then through the map grid index -> cell.  Galaxies outside the
+// grid or in a grid cell without a cell are summed into counts[ncells].  The reference
+// sends the galaxies of grid index 0 there too (`e > 0`, dot.cpp:127) and indexes the
+// counts with -1 for a galaxy in an empty cell; both are not reproduced.  FP64 atomics:
+// integer weights sum exactly, others to the order of the additions.
+__global__ void galaxy_counts_kernel(long long ngal, const float4* gal, GridBox g, const int* cellmap, int ncells,
+                                     double* counts) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ngal; i += (long long)gridDim.x * blockDim.x) {
+        const float4 v = gal[i];
+        // range tests on the FP64 floor before any conversion: NaN and far-away coordinates fail them
+        const double t1 = floor(g.n[0] * ((double)v.x - g.lo[0]) / (g.hi[0] - g.lo[0]));
+        const double t2 = floor(g.n[1] * ((double)v.y - g.lo[1]) / (g.hi[1] - g.lo[1]));
+        const double t3 = floor(g.n[2] * ((double)v.z - g.lo[2]) / (g.hi[2] - g.lo[2]));
+        int a = ncells;
+        if (t1 >= 0.0 && t1 < g.n[0] && t2 >= 0.0 && t2 < g.n[1] && t3 >= 0.0 && t3 < g.n[2]) {
+            const int m = cellmap[((long long)t1 * g.n[1] + (long long)t2) * g.n[2] + (long long)t3];
+            if (m >= 0) a = m;
+        }
+        atomicAdd(&counts[a], (double)v.w);
+    }
+}
+
 // modes[i][h*Nphi + f] = u_i(h) * trig_kind(m f), u_i the block eigenvector idx of block b = m npar + parity
 // expanded to the full arc grid: u(h_x) = U_b[x][idx] / sqrt(npar), u(P h_x) = +-u(h_x) (even / odd)
 __global__ void assemble_modes_kernel(int H, int Nphi, int Nmu, int npar, int nmodes, const int* sel_b,
@@ -426,6 +450,16 @@ void launch_widen(size_t n, const float* in, double* out, cudaStream_t s, long l
     widen_kernel<<<grid_for((long long)n), 256, 0, s>>>(n, in, out);
     OPSEC_CUDA(cudaGetLastError());
     ++*l;
+}
+
+void launch_galaxy_counts(long long ngal, const float4* gal, const GridBox& g, const int* cellmap, int ncells,
+                          double* counts, cudaStream_t st, long long* l) {
+    OPSEC_CUDA(cudaMemsetAsync(counts, 0, sizeof(double) * (ncells + 1), st));
+    if (ngal > 0) {
+        galaxy_counts_kernel<<<grid_for(ngal), 256, 0, st>>>(ngal, gal, g, cellmap, ncells, counts);
+        OPSEC_CUDA(cudaGetLastError());
+        ++*l;
+    }
 }
 
 }  // namespace opsec

@@ -11,6 +11,9 @@ this restatement in tests/test_basis.py through tests/golden/basis_ref.npz):
                segment) x the mean of the map over S x S points of the cell
                x dmu dphi (SphericalSurvey.cpp:51-80); the reference's 3x
                (basis.cpp:72-84, 103-108) with quirk3
+  galaxies     grid index per galaxy (Survey::GetGridIndex, Survey.cpp:93-101)
+               and weighted counts per cell (dot.cpp:105-129); pinned against
+               the reference through tests/golden/galaxy_ref.npz
 """
 from __future__ import annotations
 
@@ -117,3 +120,34 @@ def basis(coordsys, grid, n, nbar=0.0, rad=None, nside=0, nest=0, mask=None, sam
                     A *= float(np.mean(np.asarray(mask, dtype=np.float64)[ang2pix(nside, nest, TH, PH)]))
                 out.append((V, R * A * (3.0 if quirk3 else 1.0)))
     return np.array(out)
+
+
+def grid_index(grid, n, gals):
+    """Grid index (d1 N2 + d2) N3 + d3 of each galaxy, -1 outside: floor(N (x - min) / (max - min))
+    per axis in FP64 from the float32 coordinate, the reference's order of operations."""
+    g = np.asarray(gals, dtype=np.float32)
+    d = []
+    for ax in range(3):
+        lo, hi = float(grid[2 * ax]), float(grid[2 * ax + 1])
+        with np.errstate(invalid="ignore"):
+            d.append(np.floor(int(n[ax]) * (g[:, ax].astype(np.float64) - lo) / (hi - lo)))
+    ok = np.ones(g.shape[0], dtype=bool)
+    for ax in range(3):
+        ok &= (d[ax] >= 0) & (d[ax] < int(n[ax]))
+    di = [np.where(ok, x, 0).astype(np.int64) for x in d]
+    return np.where(ok, (di[0] * int(n[1]) + di[1]) * int(n[2]) + di[2], -1)
+
+
+def count_galaxies(grid, n, cellidx, gals, ref_zero=False):
+    """Weighted counts per cell (len(cellidx) + 1 values; the last: galaxies in no cell), summed in
+    galaxy order.  ref_zero: as the reference, send the galaxies of grid index 0 to the last entry
+    (dot.cpp:127 tests e > 0)."""
+    g = np.asarray(gals, dtype=np.float32)
+    e = grid_index(grid, n, g)
+    cellmap = np.full(int(np.prod(n)), -1, dtype=np.int64)
+    cellmap[np.asarray(cellidx)] = np.arange(len(cellidx))
+    a = np.where(e >= (1 if ref_zero else 0), cellmap[np.maximum(e, 0)], -1)
+    a = np.where(a < 0, len(cellidx), a)
+    counts = np.zeros(len(cellidx) + 1)
+    np.add.at(counts, a, g[:, 3].astype(np.float64))
+    return counts

@@ -254,4 +254,27 @@ void ref_basis(int coordsys, const double* grid, const int* n, double nbar_const
     delete s;
 }
 
+// The reference's galaxy binning (dot.cpp:124-129): grid index of each galaxy by
+// Survey::GetGridIndex (Survey.cpp:93-101), and the weighted counts per cell as dot
+// accumulates them -- a galaxy goes to cellmap[e] when e > 0, else to counts[ncells].
+// gals: ngal records (x1, x2, x3, w) float32; cellidx: grid index of each cell.
+void ref_count_galaxies(int coordsys, const double* grid, const int* n, long ngal, const float* gals, int ncells,
+                        const int* cellidx, int* index, double* counts) {
+    Survey* s = make_survey(coordsys, grid, n, 0.0);
+    s->Min1 = grid[0]; s->Max1 = grid[1];
+    s->Min2 = grid[2]; s->Max2 = grid[3];
+    s->Min3 = grid[4]; s->Max3 = grid[5];
+    std::vector<int> cellmap((size_t)n[0] * n[1] * n[2], -1);
+    for (int a = 0; a < ncells; a++) cellmap[cellidx[a]] = a;
+    for (int a = 0; a <= ncells; a++) counts[a] = 0.0;
+    for (long i = 0; i < ngal; i++) {
+        const float* g = gals + 4 * i;
+        const int e = s->GetGridIndex(g[0], g[1], g[2]);
+        index[i] = e;
+        const int a = (e > 0) ? cellmap[e] : ncells;
+        if (a >= 0) counts[a] += g[3];  // a = -1 (an empty grid cell) indexes before the array there
+    }
+    delete s;
+}
+
 }  // extern "C"
