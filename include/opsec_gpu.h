@@ -119,10 +119,20 @@ int opsec_gpu_fisher_build(opsec_gpu* ctx, int ncells, const opsec_cell* cells, 
  * times must hold 5 values. */
 int opsec_gpu_stage_times(const opsec_gpu* ctx, double* times);
 
+/* How the last eigensolve ran: stats[0] the solver (0 dense FP64 syevdx, 1 azimuthal
+ * blocks, 2 Chebyshev-filtered subspace iteration -- klt.solver), then for the last:
+ * [1] filter iterations, [2] final Chebyshev degree, [3] N x N x B GEMMs, [4] block
+ * size B, [5] [6] the spectrum bounds used, [7] the largest relative residual
+ * |S x - lambda x| / lambda of the returned modes (FP64), [8] FP64 Rayleigh-Ritz
+ * rounds, [9] CG steps of the refinement.  stats must hold 10 values.  It replaces
+ * ARPACK's iteration report (ParpackSolver.cpp:140-190). */
+int opsec_gpu_eig_stats(const opsec_gpu* ctx, double* stats);
+
 /* Per-kernel CUDA-event timing accumulated since creation when the
  * configuration sets profile = 1 (events on the launching stream around the
  * cubature, projection and Fisher kernels).  name: "cubature", "project_step1",
- * "project_step2", "fisher".  flops / bytes = algorithmic work attributed to
+ * "project_step2", "fisher", and for the subspace-iteration eigensolver
+ * "chfsi_filter", "chfsi_rayleigh_ritz", "chfsi_refine".  flops / bytes = algorithmic work attributed to
  * those launches.  No counterpart in the reference, which has no timers. */
 int opsec_gpu_kernel_stats(const opsec_gpu* ctx, const char* name, long long* count, double* total_ms,
                            double* flops, double* bytes);

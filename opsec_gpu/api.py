@@ -55,6 +55,7 @@ def load():
     L.opsec_gpu_fisher_build.argtypes = [vp, C.c_int, vp, dp, C.c_int, C.c_int] + [dp] * 8
     L.opsec_gpu_stage_times.argtypes = [vp, dp]
     L.opsec_gpu_kernel_stats.argtypes = [vp, C.c_char_p, C.POINTER(C.c_longlong), dp, dp, dp]
+    L.opsec_gpu_eig_stats.argtypes = [vp, dp]
     L.opsec_gpu_launch_count.argtypes = [vp]
     L.opsec_gpu_launch_count.restype = C.c_longlong
     L.opsec_gpu_last_error.argtypes = [vp]
@@ -363,6 +364,14 @@ class Engine:
         t = np.zeros(5)
         self._check(self._L.opsec_gpu_stage_times(self._h, _d(t)))
         return dict(zip(STAGES, t))
+
+    def eig_stats(self):
+        """How the last eigensolve ran (opsec_gpu_eig_stats)."""
+        t = np.zeros(10)
+        self._check(self._L.opsec_gpu_eig_stats(self._h, _d(t)))
+        return {"solver": ("dense", "azimuthal", "chfsi")[int(t[0])], "iterations": int(t[1]), "degree": int(t[2]),
+                "gemms": int(t[3]), "block": int(t[4]), "lo": t[5], "hi": t[6], "resid": t[7],
+                "refine_rounds": int(t[8]), "cg_steps": int(t[9])}
 
     def kernel_stats(self, name):
         n, ms, fl, by = C.c_longlong(), C.c_double(), C.c_double(), C.c_double()

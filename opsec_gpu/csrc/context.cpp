@@ -78,6 +78,10 @@ void cuda_check(cudaError_t e, const char* what) {
     }
 }
 
+// klt.solver = auto: the subspace iteration from this many cells on (and a block of at most
+// a quarter of them); the dense FP64 syevdx below
+constexpr int kChfsiMinCells = 16384;
+
 static void blas_check(cublasStatus_t st, const char* what) {
     if (st != CUBLAS_STATUS_SUCCESS) fail(OPSEC_ERR_CUDA, std::string(what) + " failed (cuBLAS status " + std::to_string((int)st) + ")");
 }
@@ -358,6 +362,11 @@ struct opsec_gpu {
     int mask_nest = 0;
     DevBuf<float> mask_dev;
     int basis_quirk3 = 0, basis_samples = 16;
+    // dense-grid eigensolver: dense FP64 syevdx, Chebyshev-filtered subspace iteration, or by size
+    std::string eig_solver = "auto";
+    ChfsiArgs chfsi;  // its options (sizes and buffers set per call)
+    bool chfsi_guard_set = false;
+    double eig_stats[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     // mock counts: cuFFT plans for the last mesh size, mesh and per-cell buffers
     MockPlans mock_plans;
     DevBuf<double> mock_grid, mock_spec, mock_nbar, mock_out;
@@ -566,6 +575,29 @@ void configure(opsec_gpu* c, const std::map<std::string, std::string>& kv) {
         if (v != "streams" && v != "batched") fail(OPSEC_ERR_CONFIG, "azimuthal.eig must be streams or batched");
         c->az_batched = v == "batched";
     }
+    if (has("klt.solver")) {
+        c->eig_solver = get("klt.solver");
+        if (c->eig_solver != "auto" && c->eig_solver != "dense" && c->eig_solver != "chfsi")
+            fail(OPSEC_ERR_CONFIG, "klt.solver must be auto, dense or chfsi");
+    }
+    if (has("klt.tol")) c->chfsi.tol = to_double("klt.tol", get("klt.tol"));
+    if (has("klt.degree")) c->chfsi.degree = to_int("klt.degree", get("klt.degree"));
+    if (has("klt.maxit")) c->chfsi.maxit = to_int("klt.maxit", get("klt.maxit"));
+    if (has("klt.guard")) {
+        c->chfsi.guard = to_int("klt.guard", get("klt.guard"));
+        c->chfsi_guard_set = true;
+    }
+    if (has("klt.refine")) c->chfsi.refine = to_int("klt.refine", get("klt.refine"));
+    if (has("klt.cg")) c->chfsi.cg_steps = to_int("klt.cg", get("klt.cg"));
+    if (c->chfsi.refine < 0 || c->chfsi.cg_steps < 1) fail(OPSEC_ERR_CONFIG, "klt.refine must be >= 0, klt.cg >= 1");
+    if (has("klt.seed")) c->chfsi.seed = (unsigned long long)to_int("klt.seed", get("klt.seed"));
+    if (has("klt.gemm")) {
+        const std::string& v = get("klt.gemm");
+        if (v != "bf16x9" && v != "f32") fail(OPSEC_ERR_CONFIG, "klt.gemm must be bf16x9 or f32");
+        c->chfsi.emulate = v == "bf16x9";
+    }
+    if (!(c->chfsi.tol > 0) || c->chfsi.degree < 1 || c->chfsi.degree > 64 || c->chfsi.maxit < 1 || c->chfsi.guard < 0)
+        fail(OPSEC_ERR_CONFIG, "klt.tol must be > 0, klt.degree in [1, 64], klt.maxit >= 1, klt.guard >= 0");
     if (has("survey.nbar")) c->sel_nbar = to_double("survey.nbar", get("survey.nbar"));
     if (has("basis.quirk3")) c->basis_quirk3 = to_int("basis.quirk3", get("basis.quirk3")) != 0;
     if (has("basis.samples")) {
@@ -1139,6 +1171,8 @@ int eigensolve(opsec_gpu* c, int ncells, const opsec_cell* cells, int M) {
     c->warning.clear();
     c->az_valid = false;
     if (azimuthal_ok(c, ncells, cells)) {
+        std::fill(c->eig_stats, c->eig_stats + 10, 0.0);
+        c->eig_stats[0] = 1.0;
         const KeySpace& ks = c->ks;
         const int H = ks.H, Nphi = ks.N3, Nmu = ks.N2, nm = Nphi / 2 + 1;
         std::vector<double> nba(H);
@@ -1334,7 +1368,7 @@ int eigensolve(opsec_gpu* c, int ncells, const opsec_cell* cells, int M) {
         return M;
     }
     drop_eig_graph(c);
-    // dense path: S in FP64, top-M by syevdx (klt.cpp:173-248 via PARPACK there)
+    // dense path: S in FP64, top-M by syevdx or by subspace iteration (klt.cpp:173-248 via PARPACK there)
     const int N = ncells;
     c->S.alloc((size_t)N * N);
     std::vector<int> all(N);
@@ -1342,17 +1376,45 @@ int eigensolve(opsec_gpu* c, int ncells, const opsec_cell* cells, int M) {
     c->rc.alloc(N);
     OPSEC_CUDA(cudaMemcpyAsync(c->rc.p, all.data(), sizeof(int) * N, cudaMemcpyHostToDevice, c->stream));
     launch_signal_block(c->ks, cell_info(c), c->Q.p, N, c->rc.p, N, c->rc.p, c->S.p, N, c->stream, &c->launches);
+    ChfsiArgs ca = c->chfsi;
+    if (!c->chfsi_guard_set) ca.guard = std::max(32, M / 4);
+    const long long blk = std::min<long long>(N, ((long long)M + ca.guard + 31) / 32 * 32);
+    if (c->eig_solver == "chfsi" || (c->eig_solver == "auto" && N >= kChfsiMinCells && 4 * blk <= N)) {
+        if (!c->blas) blas_check(cublasCreate(&c->blas), "cublasCreate");
+        ca.N = N;
+        ca.M = M;
+        ca.S = c->S.p;
+        ca.modes = c->modes.p;
+        ca.evals = c->evals.p;
+        ChfsiStats st;
+        chfsi_eigensolve(ca, c->blas, c->solver, c->stream, &c->launches, &st);
+        const double v[10] = {2.0,   (double)st.iterations, (double)st.degree, (double)st.gemms, (double)st.block,
+                              st.lo, st.hi, st.resid, (double)st.refine_gemms, (double)st.cg_steps};
+        std::copy(v, v + 10, c->eig_stats);
+        return M;
+    }
+    std::fill(c->eig_stats, c->eig_stats + 10, 0.0);
     c->W.alloc(N);
     c->info.alloc(1);
-    int lwork = 0, meig = 0;
-    solver_check(cusolverDnDsyevdx_bufferSize(c->solver, CUSOLVER_EIG_MODE_VECTOR, CUSOLVER_EIG_RANGE_I,
-                                              CUBLAS_FILL_MODE_LOWER, N, c->S.p, N, 0.0, 0.0, N - M + 1, N, &meig,
-                                              c->W.p, &lwork),
-                 "syevdx_bufferSize");
-    c->work.alloc((size_t)lwork);
-    solver_check(cusolverDnDsyevdx(c->solver, CUSOLVER_EIG_MODE_VECTOR, CUSOLVER_EIG_RANGE_I, CUBLAS_FILL_MODE_LOWER,
-                                   N, c->S.p, N, 0.0, 0.0, N - M + 1, N, &meig, c->W.p, c->work.p, lwork, c->info.p),
-                 "syevdx");
+    // the 64-bit interface: the 32-bit one's workspace count overflows from N ~ 23,000 on
+    int64_t meig = 0;
+    size_t wdev = 0, whost = 0;
+    double vl = 0.0, vu = 0.0;
+    cusolverDnParams_t prm = nullptr;
+    solver_check(cusolverDnCreateParams(&prm), "cusolverDnCreateParams");
+    cusolverStatus_t sst = cusolverDnXsyevdx_bufferSize(
+        c->solver, prm, CUSOLVER_EIG_MODE_VECTOR, CUSOLVER_EIG_RANGE_I, CUBLAS_FILL_MODE_LOWER, N, CUDA_R_64F, c->S.p, N,
+        &vl, &vu, N - M + 1, N, &meig, CUDA_R_64F, c->W.p, CUDA_R_64F, &wdev, &whost);
+    if (sst == CUSOLVER_STATUS_SUCCESS) {
+        c->work.alloc((wdev + sizeof(double) - 1) / sizeof(double) + 1);
+        std::vector<unsigned char> hw(whost + 1);
+        sst = cusolverDnXsyevdx(c->solver, prm, CUSOLVER_EIG_MODE_VECTOR, CUSOLVER_EIG_RANGE_I, CUBLAS_FILL_MODE_LOWER,
+                                N, CUDA_R_64F, c->S.p, N, &vl, &vu, N - M + 1, N, &meig, CUDA_R_64F, c->W.p,
+                                CUDA_R_64F, c->work.p, wdev, hw.data(), whost, c->info.p);
+        if (sst == CUSOLVER_STATUS_SUCCESS) OPSEC_CUDA(cudaStreamSynchronize(c->stream));  // host workspace in use
+    }
+    cusolverDnDestroyParams(prm);
+    solver_check(sst, "syevdx");
     check_info(c, 1);
     if (meig < M) fail(OPSEC_ERR_NUMERIC, "eigensolver returned fewer modes than requested");
     launch_reverse_modes(N, M, N, c->S.p, c->W.p, c->modes.p, c->evals.p, c->stream, &c->launches);
@@ -2353,6 +2415,12 @@ int opsec_gpu_stage_times(const opsec_gpu* c, double* times) {
 }
 
 long long opsec_gpu_launch_count(const opsec_gpu* c) { return c ? c->launches : 0; }
+
+int opsec_gpu_eig_stats(const opsec_gpu* c, double* stats) {
+    if (!c || !stats) return OPSEC_ERR_ARG;
+    std::copy(c->eig_stats, c->eig_stats + 10, stats);
+    return OPSEC_OK;
+}
 
 int opsec_gpu_kernel_stats(const opsec_gpu* c, const char* name, long long* count, double* total_ms, double* flops,
                            double* bytes) {

@@ -1,7 +1,9 @@
 // engine.h -- internal declarations shared by the host code and the kernels.
 #pragma once
 
+#include <cublas_v2.h>
 #include <cuda_runtime.h>
+#include <cusolverDn.h>
 
 #include <cstddef>
 #include <cstdint>
@@ -281,6 +283,29 @@ void launch_scale_modes(int ncells, int nmodes, const double* modes, const doubl
 
 // packed FP32 -> FP64
 void launch_widen(size_t n, const float* in, double* out, cudaStream_t s, long long* launches);
+
+// Top-M eigenpairs of a dense symmetric FP64 matrix by Chebyshev-filtered subspace
+// iteration (chfsi.cu).
+struct ChfsiArgs {
+    int N = 0, M = 0;
+    const double* S = nullptr;  // N x N, symmetric, both triangles
+    int guard = 32;             // block B = M + guard, rounded up to a multiple of 32
+    int degree = 12;            // largest Chebyshev degree
+    int maxit = 100;            // filter iterations at most
+    double tol = 1e-5;          // |S x - theta x| <= tol |theta| for the top M
+    int emulate = 1;            // FP32 GEMMs as BF16x9 on the tensor cores (1) or FP32 SIMT (0)
+    int refine = 2;             // FP64 refinement rounds (correction solves) at most
+    int cg_steps = 20;          // CG steps per correction solve at most
+    unsigned long long seed = 1;
+    double* modes = nullptr;    // out: M x N, mode-major
+    double* evals = nullptr;    // out: M, descending
+};
+struct ChfsiStats {
+    int iterations = 0, degree = 0, gemms = 0, block = 0, refine_gemms = 0, cg_steps = 0;
+    double lo = 0, hi = 0, resid = 0;  // spectrum bounds; largest relative FP64 residual of the top M
+};
+void chfsi_eigensolve(const ChfsiArgs& a, cublasHandle_t blas, cusolverDnHandle_t solver, cudaStream_t s,
+                      long long* launches, ChfsiStats* stats);
 
 // Weighted galaxy counts per cell (signal.cu); counts has ncells + 1 entries, the last
 // for galaxies outside every cell.
