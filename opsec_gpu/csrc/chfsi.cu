@@ -163,17 +163,19 @@ __global__ void reverse_kernel(int n, int m, const double* U, const double* w, d
     }
 }
 
-// r_j <- AX_j - theta_j X_j in place of AX, norms[j] = |r_j|; one block per column (FP64)
-__global__ void residual_vectors_kernel(int n, double* AX, const double* X, const double* theta, double* norms) {
+// R_j = AX_j - theta_j X_j, norms[j] = |R_j|; one block per column (FP64)
+__global__ void residual_vectors_kernel(int n, const double* AX, const double* X, const double* theta, double* R,
+                                        double* norms) {
     __shared__ double sh[32];
     const int j = blockIdx.x;
-    double* a = AX + (size_t)j * n;
+    const double* a = AX + (size_t)j * n;
     const double* x = X + (size_t)j * n;
+    double* r = R + (size_t)j * n;
     const double th = theta[j];
     double s = 0.0;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         const double d = a[i] - th * x[i];
-        a[i] = d;
+        r[i] = d;
         s += d * d;
     }
     s = block_sum(s, sh);
@@ -504,13 +506,24 @@ void chfsi_eigensolve(const ChfsiArgs& g, cublasHandle_t blas, cusolverDnHandle_
     const double one = 1.0, zero = 0.0;
     const double target = 0.1 * g.tol;  // refine until the residuals are a tenth of the tolerance
     for (int round = 0;; round++) {
-        // orthonormal basis of the current vectors, then Rayleigh-Ritz with the FP64 S
+        // orthonormal basis Q of the current vectors and Z = S Q.  Round 0: Z by a DGEMM with the
+        // FP64 S.  Later rounds: X = U + D and Z = S U + S D are carried in (S U from the last
+        // round in FP64, S D by an FP32 GEMM: D is small, so FP32 costs it nothing), and X = Q R
+        // turns Z into Z R^-1 = S Q by a triangular solve before R is overwritten
         solver_ok(cusolverDnDgeqrf(solver, N, Mr, X64.p, N, tau64.p, wsd.p, lmax, info.p), "Dgeqrf");
+        if (round > 0)
+            blas_ok(cublasDtrsm(blas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, N, Mr,
+                                &one, X64.p, N, Z64.p, N),
+                    "Dtrsm");
         solver_ok(cusolverDnDorgqr(solver, N, Mr, Mr, X64.p, N, tau64.p, wsd.p, lmax, info.p), "Dorgqr");
         check_info("Dgeqrf/Dorgqr");
-        if (g_clock) g_clock->begin("chfsi_refine", st, 2.0 * NN * Mr + 6.0 * NR * Mr);
-        blas_ok(cublasDgemm(blas, CUBLAS_OP_N, CUBLAS_OP_N, N, Mr, N, &one, g.S, N, X64.p, N, &zero, Z64.p, N),
-                "Dgemm");
+        if (g_clock)
+            g_clock->begin("chfsi_refine", st, (round == 0 ? 2.0 * NN * Mr : 2.0 * NR * Mr) + 6.0 * NR * Mr);
+        if (round == 0) {
+            blas_ok(cublasDgemm(blas, CUBLAS_OP_N, CUBLAS_OP_N, N, Mr, N, &one, g.S, N, X64.p, N, &zero, Z64.p, N),
+                    "Dgemm");
+            s.refine_gemms += 1;
+        }
         blas_ok(cublasDgemm(blas, CUBLAS_OP_T, CUBLAS_OP_N, Mr, Mr, N, &one, X64.p, N, Z64.p, N, &zero, U64.p, Mr),
                 "Dgemm");
         symmetrize_kernel<double><<<blocks((size_t)Mr * Mr), 256, 0, st>>>(Mr, U64.p, Hs.p);
@@ -522,12 +535,12 @@ void chfsi_eigensolve(const ChfsiArgs& g, cublasHandle_t blas, cusolverDnHandle_
                 "Dgemm");
         blas_ok(cublasDgemm(blas, CUBLAS_OP_N, CUBLAS_OP_N, N, Mr, Mr, &one, Z64.p, N, Hs.p, Mr, &zero, X64.p, N),
                 "Dgemm");
-        // X64 <- S u - theta u (the residual vectors), rd <- their norms
-        residual_vectors_kernel<<<Mr, 256, 0, st>>>(N, X64.p, U64.p, Wd.p, rd.p);
+        // X64 = S U kept; Z64 <- S u - theta u (the residual vectors), rd <- their norms
+        residual_vectors_kernel<<<Mr, 256, 0, st>>>(N, X64.p, U64.p, Wd.p, Z64.p, rd.p);
         OPSEC_CUDA(cudaGetLastError());
         if (g_clock) g_clock->end(st);
         *launches += 2;
-        s.refine_gemms += 1;
+        s.rounds += 1;
         OPSEC_CUDA(cudaMemcpyAsync(w64.data(), Wd.p, sizeof(double) * Mr, cudaMemcpyDeviceToHost, st));
         OPSEC_CUDA(cudaMemcpyAsync(r64.data(), rd.p, sizeof(double) * Mr, cudaMemcpyDeviceToHost, st));
         check_info("Dsyevd");
@@ -544,7 +557,7 @@ void chfsi_eigensolve(const ChfsiArgs& g, cublasHandle_t blas, cusolverDnHandle_
         }
         OPSEC_CUDA(cudaMemcpyAsync(colv.p, hv.data(), sizeof(double) * 2 * Mr, cudaMemcpyHostToDevice, st));
         narrow_kernel<<<blocks(NR), 256, 0, st>>>(NR, U64.p, U32.p);
-        scaled_narrow_kernel<<<blocks(NR), 256, 0, st>>>(N, Mr, X64.p, colv.p + Mr, R32.p);  // b_j = r_j / |r_j|
+        scaled_narrow_kernel<<<blocks(NR), 256, 0, st>>>(N, Mr, Z64.p, colv.p + Mr, R32.p);  // b_j = r_j / |r_j|
         OPSEC_CUDA(cudaGetLastError());
         *launches += 2;
         auto project = [&](float* V) {  // V <- V - U (U^T V)
@@ -595,10 +608,12 @@ void chfsi_eigensolve(const ChfsiArgs& g, cublasHandle_t blas, cusolverDnHandle_
             OPSEC_CUDA(cudaGetLastError());
             ++*launches;
         }
-        // X = U + |r| d
+        // Z = S U + |r| S d (S d by an FP32 GEMM), then X = U + |r| d
+        gemm(CUBLAS_OP_N, CUBLAS_OP_N, N, Mr, N, 1.f, S32.p, N, D32.p, N, 0.f, Q32.p, N);
+        correct_kernel<<<blocks(NR), 256, 0, st>>>(N, Mr, X64.p, colv.p + Mr, Q32.p, Z64.p);
         correct_kernel<<<blocks(NR), 256, 0, st>>>(N, Mr, U64.p, colv.p + Mr, D32.p, X64.p);
         OPSEC_CUDA(cudaGetLastError());
-        ++*launches;
+        *launches += 2;
         if (g_clock) g_clock->end(st);
     }
     reverse_kernel<<<blocks((size_t)N * M), 256, 0, st>>>(N, M, U64.p + (size_t)(Mr - M) * N, Wd.p + (Mr - M), g.modes,

@@ -1389,7 +1389,7 @@ int eigensolve(opsec_gpu* c, int ncells, const opsec_cell* cells, int M) {
         ChfsiStats st;
         chfsi_eigensolve(ca, c->blas, c->solver, c->stream, &c->launches, &st);
         const double v[10] = {2.0,   (double)st.iterations, (double)st.degree, (double)st.gemms, (double)st.block,
-                              st.lo, st.hi, st.resid, (double)st.refine_gemms, (double)st.cg_steps};
+                              st.lo, st.hi, st.resid, (double)st.rounds, (double)st.cg_steps};
         std::copy(v, v + 10, c->eig_stats);
         return M;
     }
