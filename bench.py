@@ -109,6 +109,65 @@ def bench_mocks(args):
     print(json.dumps(line), flush=True)
 
 
+EIG_BOXES = {"eig-box24": (24, 500), "eig-box32": (32, 1000), "eig-box40": (40, 1000)}
+
+
+def bench_eig(args):
+    """Top-M eigenpairs of the dense signal matrix of an open Cartesian box (50 Mpc/h cells, an
+    anisotropic selection) by the iterative eigensolver: seconds per klt call (cells in, modes and
+    eigenvalues out, so the host copies are inside), after warm-up calls on the same context."""
+    from opsec_gpu import api, synth
+
+    n, M = EIG_BOXES[args.workload]
+    sv, cells = synth.tilted_box_survey(n, 50.0 * n)
+    bands = synth.band_edges(6, 0.0, 0.12)
+    k, P = synth.pk_table()
+    out = {}
+    for solver in (("chfsi", "dense") if args.compare_dense else ("chfsi",)):
+        e = api.Engine(api.make_config(sv, bands=bands, nmodes=M, extra=(f"klt.solver = {solver}", "profile = 1")))
+        e.set_pk(k, P)
+        for _ in range(args.warmup):
+            e.klt(cells, M)
+        base = {name: e.kernel_stats(name) for name in ("chfsi_filter", "chfsi_rayleigh_ritz", "chfsi_refine",
+                                                        "chfsi_correct")}
+        launches0 = e.launch_count()
+        times = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            e.klt(cells, M)  # synchronous: returns with the modes on the host
+            times.append(time.perf_counter() - t0)
+        out[solver] = {"s": float(np.median(times)), "stats": e.eig_stats(), "launches": e.launch_count() - launches0,
+                       "kernels": {}}
+        for name, b in base.items():
+            a = e.kernel_stats(name)
+            dn = a["count"] - b["count"]
+            if dn:
+                ms = a["ms"] - b["ms"]
+                out[solver]["kernels"][name] = {"ms_per_solve": ms / args.steps,
+                                                "tflops": (a["flops"] - b["flops"]) / ms / 1e9}
+        e.close()
+    c = out["chfsi"]
+    _, bf16, kind = peaks()
+    filt = c["kernels"].get("chfsi_filter", {"tflops": 0.0})
+    line = {"metric": f"top {M} eigenpairs of a dense {cells.size}-cell box (iterative eigensolver)",
+            "value": c["s"], "unit": "s/solve", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": c["s"] * 1000, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 (bf16x9 tensor) + f64", "data": "synthetic",
+            "config": {"workload": args.workload, "cells": int(cells.size), "modes": M, "bands": 6,
+                       "grid": f"{n}^3 open box, 50 Mpc/h cells, anisotropic Gaussian selection",
+                       "l2": f"inputs larger than L2 (S: {cells.size ** 2 * 8 / 1e9:.1f} GB FP64)"},
+            "eig_stats": c["stats"], "kernels": c["kernels"], "gpu_launches": c["launches"],
+            "roofline": {"kernel": "chfsi_filter (cuBLAS BF16x9 GEMMs)", "bound": "tensor",
+                         "achieved": filt["tflops"], "unit": "TFLOP/s (FP32-equivalent)",
+                         "peak": bf16 / 9.0, "peak_kind": f"{kind} bf16 GEMM / 9 (BF16x9: nine BF16 products per FP32 one)",
+                         "frac": filt["tflops"] / (bf16 / 9.0), "traffic": None},
+            "e2e": {"value": c["s"], "unit": "s/solve", "h2d_bytes_per_step": int(cells.nbytes),
+                    "d2h_bytes_per_step": int(8 * M * (cells.size + 1))}}
+    if "dense" in out:
+        line["dense_s"] = out["dense"]["s"]
+    print(json.dumps(line), flush=True)
+
+
 def q_table_gb(w):
     """FP64 Q table bytes of a workload: tables x symmetry keys."""
     sv = w["survey"]
@@ -375,6 +434,8 @@ def main():
     ap.add_argument("--surrogate-epochs", type=int, default=3)
     ap.add_argument("--no-tc-roofline", action="store_true",
                     help="skip the one-band dense tensor-core projection run after the timed builds")
+    ap.add_argument("--compare-dense", action="store_true",
+                    help="eig-box workloads: also time the dense FP64 eigensolve")
     ap.add_argument("--set", action="append", default=[], metavar="KEY=VALUE",
                     help="extra configuration line for the engine, e.g. cubature.precision=fast")
     args = ap.parse_args()
@@ -386,6 +447,13 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
 
+    if args.workload in EIG_BOXES:
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the iterative-eigensolver workload has no reference CPU arm"}))
+            return
+        if rank != 0:
+            return
+        return bench_eig(args)
     if args.workload == "c5":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the batched-mock workload has no reference CPU arm"}))

@@ -27,11 +27,10 @@ struct Error {
 };
 
 [[noreturn]] void fail(int code, const std::string& msg);
-// Largest dynamic shared memory a block may opt in to on the current device.  Kernels
-// whose launches need different amounts set their attribute to this one value, so that
-// host threads launching them concurrently never lower it under one another.
-// Largest dynamic shared-memory size a launch of `func` may request on the
-// current device (opt-in ceiling less the kernel's static shared memory).
+// Largest dynamic shared-memory size a launch of `func` may request on the current device
+// (the opt-in ceiling less the kernel's static shared memory).  Kernels whose launches need
+// different amounts set their attribute to this one value, so that host threads launching
+// them concurrently never lower it under one another.
 int max_dynamic_smem(const void* func);
 void cuda_check(cudaError_t e, const char* what);
 #define OPSEC_CUDA(x) ::opsec::cuda_check((x), #x)

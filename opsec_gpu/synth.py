@@ -162,6 +162,18 @@ def box_survey(n: int = 12, side: float = 600.0, n0: float = 3e-4, scale: float 
     return sv, make_cells(sv, nbar)
 
 
+def tilted_box_survey(n: int, side: float, periodic: bool = False, n0: float = 3e-4):
+    """Cartesian box with an off-centre, anisotropic Gaussian selection: no symmetry of the grid
+    survives in S, so its eigenvalues are not degenerate."""
+    sv = Survey(COORD_CARTESIAN, (0.0, side, 0.0, side, 0.0, side), (n, n, n), L=side if periodic else 0.0)
+
+    def sel(x, y, z):
+        q = (x - 0.42 * side) ** 2 + 1.3 * (y - 0.57 * side) ** 2 + 0.8 * (z - 0.5 * side) ** 2 + 0.2 * x * y
+        return n0 * np.exp(-q / (0.5 * side) ** 2)
+
+    return sv, make_cells(sv, sel, nquad=4)
+
+
 def shell_survey(nr: int = 32, nmu: int = 32, nphi: int = 32, rmin: float = 200.0, rmax: float = 1000.0,
                  rc: float = 600.0, width: float = 250.0, mean_density: float = 3e-4, nquad: int = 24):
     """Full-sky spherical shell with a Gaussian radial selection.

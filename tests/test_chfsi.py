@@ -12,14 +12,13 @@ BANDS = synth.band_edges(6, 0.0, 0.12)
 
 
 def _box(n, side, periodic, tilt=True):
+    if tilt:
+        return synth.tilted_box_survey(n, side, periodic=periodic)
     sv = synth.Survey(synth.COORD_CARTESIAN, (0.0, side, 0.0, side, 0.0, side), (n, n, n),
                       L=side if periodic else 0.0)
 
-    def sel(x, y, z):  # an off-centre, anisotropic selection: no symmetry of the grid survives
-        if not tilt:
-            return 3e-4 * np.exp(-((x - side / 2) ** 2 + (y - side / 2) ** 2 + (z - side / 2) ** 2) / (side / 2) ** 2)
-        q = (x - 0.42 * side) ** 2 + 1.3 * (y - 0.57 * side) ** 2 + 0.8 * (z - 0.5 * side) ** 2 + 0.2 * x * y
-        return 3e-4 * np.exp(-q / (0.5 * side) ** 2)
+    def sel(x, y, z):  # centred and isotropic: the grid's symmetries make eigenvalues degenerate
+        return 3e-4 * np.exp(-((x - side / 2) ** 2 + (y - side / 2) ** 2 + (z - side / 2) ** 2) / (side / 2) ** 2)
 
     return sv, synth.make_cells(sv, sel, nquad=4)
 
