@@ -14,7 +14,7 @@
 //               Tiago, Chelikowsky, J. Comput. Phys. 219 (2006) 172-184): d GEMMs
 //               N x N x B in FP32 arithmetic on the tensor cores (cuBLAS BF16x9: each FP32
 //               operand as three BF16 terms, FP32 accumulation).  d is the largest degree
-//               (up to klt.degree) whose gain p(hi) / p(theta_M) stays below kMaxGain, so
+//               (up to klt.degree) whose gain p(hi) / p(theta_M) stays below 1e4, so
 //               that the wanted columns keep FP32 precision beside the top ones
 //   basis       Householder QR of Y (FP32)
 //   Rayleigh-   H = Y^T S Y, its eigenpairs in FP64, X = Y V, residuals |S x - theta x|;
@@ -38,13 +38,13 @@
 #include <string>
 #include <vector>
 
+#include "chfsi_host.h"
 #include "engine.h"
 
 namespace opsec {
 namespace {
 
-constexpr double kMaxGain = 1e4;  // largest filter gain between the top and the M-th Ritz value
-constexpr int kLanczos = 32;      // Lanczos steps for the spectrum bounds
+constexpr int kLanczos = 32;  // Lanczos steps for the spectrum bounds
 
 void blas_ok(cublasStatus_t st, const char* what) {
     if (st != CUBLAS_STATUS_SUCCESS) fail(OPSEC_ERR_CUDA, std::string(what) + ": cuBLAS status " + std::to_string((int)st));
@@ -232,40 +232,6 @@ __global__ void correct_kernel(int n, int m, const double* U, const double* scal
         X[e] = U[e] + scale[e / n] * (double)D[e];
 }
 
-// the extreme eigenvalues of the symmetric tridiagonal (alpha, beta) by Sturm bisection
-int sturm_count(const std::vector<double>& a, const std::vector<double>& b, double x) {
-    int cnt = 0;
-    double q = 1.0;
-    for (size_t i = 0; i < a.size(); i++) {
-        const double bb = i ? b[i - 1] * b[i - 1] : 0.0;
-        q = a[i] - x - (i ? bb / q : 0.0);
-        if (q == 0.0) q = -1e-300;
-        if (q < 0.0) cnt++;
-    }
-    return cnt;  // eigenvalues below x
-}
-
-double tridiag_eig(const std::vector<double>& a, const std::vector<double>& b, int k) {  // k-th smallest, 0-based
-    double lo = 1e300, hi = -1e300;
-    for (size_t i = 0; i < a.size(); i++) {
-        const double r = (i ? fabs(b[i - 1]) : 0.0) + (i + 1 < a.size() ? fabs(b[i]) : 0.0);
-        lo = std::min(lo, a[i] - r);
-        hi = std::max(hi, a[i] + r);
-    }
-    for (int it = 0; it < 200 && hi - lo > 1e-15 * std::max(fabs(lo), fabs(hi)); it++) {
-        const double mid = 0.5 * (lo + hi);
-        if (sturm_count(a, b, mid) > k)
-            hi = mid;
-        else
-            lo = mid;
-    }
-    return 0.5 * (lo + hi);
-}
-
-double cheb(int d, double t) {  // T_d(t) for t >= 1
-    return cosh(d * acosh(std::max(t, 1.0)));
-}
-
 struct Gemm32 {
     cublasHandle_t h;
     bool emulate;
@@ -284,8 +250,7 @@ struct Gemm32 {
 void chfsi_eigensolve(const ChfsiArgs& g, cublasHandle_t blas, cusolverDnHandle_t solver, cudaStream_t st,
                       long long* launches, ChfsiStats* stats) {
     const int N = g.N, M = g.M;
-    int B = std::min(N, M + std::max(g.guard, 8));
-    B = std::min(N, (B + 31) / 32 * 32);
+    const int B = chfsi::block_size(N, M, g.guard);
     const int Mr = std::min(B, M + 8);  // columns of the FP64 refinement
     if (M < 1 || M > N) fail(OPSEC_ERR_ARG, "iterative eigensolver: Nmodes must be in [1, Ncells]");
     const size_t NN = (size_t)N * N, NB = (size_t)N * B;
@@ -327,7 +292,7 @@ void chfsi_eigensolve(const ChfsiArgs& g, cublasHandle_t blas, cusolverDnHandle_
         OPSEC_CUDA(cudaMemcpyAsync(v1, w, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
         blas_ok(cublasDscal(blas, N, &inv, v1, 1), "Dscal");
     }
-    const double tmin = tridiag_eig(al, be, 0), tmax = tridiag_eig(al, be, (int)al.size() - 1);
+    const double tmin = chfsi::tridiag_eig(al, be, 0), tmax = chfsi::tridiag_eig(al, be, (int)al.size() - 1);
     double hi = tmax + std::fabs(beta);
     const double lo = tmin - 0.02 * (hi - tmin);
     lz.release();
@@ -410,11 +375,7 @@ void chfsi_eigensolve(const ChfsiArgs& g, cublasHandle_t blas, cusolverDnHandle_
         hi = std::max(hi, theta[B - 1] * (1.0 + 1e-9));
         const double cut = std::max(theta[0], lo + 1e-3 * (hi - lo));
         const double e = 0.5 * (cut - lo), c0 = 0.5 * (cut + lo);
-        // the degree: largest d <= g.degree with T_d(t(hi)) / T_d(t(theta_M)) <= kMaxGain
-        const double tM = (theta[B - M] - c0) / e, th = (hi - c0) / e;
-        degree = 1;
-        for (int d = 2; d <= g.degree; d++)
-            if (cheb(d, th) / std::max(cheb(d, tM), 1.0) <= kMaxGain) degree = d;
+        degree = chfsi::filter_degree(lo, cut, hi, theta[B - M], g.degree, chfsi::kMaxGain);
         if (g_clock) g_clock->begin("chfsi_filter", st, 2.0 * NN * B * degree);
         // X holds the Ritz vectors.  Y = (S X - c0 X) sigma1 / e
         const double sigma1 = e / (hi - c0);
