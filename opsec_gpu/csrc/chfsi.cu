@@ -467,9 +467,9 @@ void chfsi_eigensolve(const ChfsiArgs& g, cublasHandle_t blas, cusolverDnHandle_
     const double one = 1.0, zero = 0.0;
     const double target = 0.1 * g.tol;  // refine until the residuals are a tenth of the tolerance
     for (int round = 0;; round++) {
-        // orthonormal basis Q of the current vectors and Z = S Q.  Round 0: Z by a DGEMM with the
-        // FP64 S.  Later rounds: X = U + D and Z = S U + S D are carried in (S U from the last
-        // round in FP64, S D by an FP32 GEMM: D is small, so FP32 costs it nothing), and X = Q R
+        // orthonormal basis Q of the current vectors and Z = S Q.  First pass: Z by a DGEMM with
+        // the FP64 S.  Later passes: X = U + D and Z = S U + S D are carried in (S U from the last
+        // pass in FP64, S D by an FP32 GEMM: D is small, so FP32 costs it nothing), and X = Q R
         // turns Z into Z R^-1 = S Q by a triangular solve before R is overwritten
         solver_ok(cusolverDnDgeqrf(solver, N, Mr, X64.p, N, tau64.p, wsd.p, lmax, info.p), "Dgeqrf");
         if (round > 0)
@@ -483,7 +483,6 @@ void chfsi_eigensolve(const ChfsiArgs& g, cublasHandle_t blas, cusolverDnHandle_
         if (round == 0) {
             blas_ok(cublasDgemm(blas, CUBLAS_OP_N, CUBLAS_OP_N, N, Mr, N, &one, g.S, N, X64.p, N, &zero, Z64.p, N),
                     "Dgemm");
-            s.refine_gemms += 1;
         }
         blas_ok(cublasDgemm(blas, CUBLAS_OP_T, CUBLAS_OP_N, Mr, Mr, N, &one, X64.p, N, Z64.p, N, &zero, U64.p, Mr),
                 "Dgemm");

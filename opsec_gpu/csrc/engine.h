@@ -300,7 +300,7 @@ struct ChfsiArgs {
     double* evals = nullptr;    // out: M, descending
 };
 struct ChfsiStats {
-    int iterations = 0, degree = 0, gemms = 0, block = 0, rounds = 0, refine_gemms = 0, cg_steps = 0;
+    int iterations = 0, degree = 0, gemms = 0, block = 0, rounds = 0, cg_steps = 0;
     double lo = 0, hi = 0, resid = 0;  // spectrum bounds; largest relative FP64 residual of the top M
 };
 void chfsi_eigensolve(const ChfsiArgs& a, cublasHandle_t blas, cusolverDnHandle_t solver, cudaStream_t s,
