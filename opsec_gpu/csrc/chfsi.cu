@@ -295,6 +295,8 @@ void chfsi_eigensolve(const ChfsiArgs& g, cublasHandle_t blas, cusolverDnHandle_
     const double tmin = chfsi::tridiag_eig(al, be, 0), tmax = chfsi::tridiag_eig(al, be, (int)al.size() - 1);
     double hi = tmax + std::fabs(beta);
     const double lo = tmin - 0.02 * (hi - tmin);
+    if (!(hi > lo) || !std::isfinite(hi) || !std::isfinite(lo))
+        fail(OPSEC_ERR_NUMERIC, "iterative eigensolver: the signal matrix has no spread of eigenvalues (zero or not finite)");
     lz.release();
 
     // ---- FP32 copy of S and the block buffers
