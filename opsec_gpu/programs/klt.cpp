@@ -15,7 +15,9 @@ static const char* usage =
     "  Nmodes=NUM     Compute NUM mode functions of greatest S/N (required)\n"
     "  modefile=FILE  Write mode function coefficients to FILE (required)\n"
     "  evalfile=FILE  Write S/N eigenvalues to FILE (required)\n"
-    "  model=NAME     Use specified model (required)\n";
+    "  model=NAME     Use specified model (required)\n"
+    "  solver=NAME    parpack or anasazi: accepted for the reference's configurations; the\n"
+    "                 engine picks its eigensolver (klt.solver = auto|dense|chfsi)\n";
 
 int main(int argc, char** argv) {
     using namespace progs;
@@ -25,6 +27,11 @@ int main(int argc, char** argv) {
         std::fputs(usage, stderr);
         die("klt", "missing configuration options " + miss);
     }
+    // klt.cpp:167-193 selects PARPACK or Anasazi by `solver`: both find the top Nmodes
+    // eigenpairs, which the engine does by the azimuthal reduction, a dense solve or its own
+    // iterative solver
+    if (cfg.has("solver") && cfg.get("solver") != "parpack" && cfg.get("solver") != "anasazi")
+        die("klt", "unrecognized solver: " + cfg.get("solver"));
     std::string err;
     std::vector<opsec_cell> cells = read_cells(cfg.get("cellfile"), err);
     if (cells.empty()) die("klt", err.empty() ? "no cells" : err);
@@ -38,6 +45,14 @@ int main(int argc, char** argv) {
     int nconv = 0;
     if (opsec_gpu_klt(g, Ncells, cells.data(), Nmodes, evals.data(), modes.data(), &nconv) != OPSEC_OK)
         die("klt", opsec_gpu_last_error(g));
+    double st[10];
+    if (opsec_gpu_eig_stats(g, st) == OPSEC_OK) {  // in place of ParpackSolver.cpp:140-190's report
+        static const char* names[] = {"dense", "azimuthal blocks", "subspace iteration"};
+        std::fprintf(stderr, "klt: %d modes by the %s eigensolver", nconv, names[(int)st[0] % 3]);
+        if ((int)st[0] == 2)
+            std::fprintf(stderr, ", %d iterations, largest relative residual %.2e", (int)st[1], st[7]);
+        std::fprintf(stderr, "\n");
+    }
     // headers as klt.cpp:209-225
     Config opts;
     opts.set("cellfile", cfg.get("cellfile"));

@@ -30,7 +30,7 @@ def test_pipeline_programs(tmp_path):
     synth.write_pkfile(str(pk), k, P)
     bands = synth.band_edges(3, 0.0, 0.15)
     nmodes = 40
-    cfg = api.make_config(sv, bands=bands, nmodes=nmodes, pkfile=str(pk))
+    cfg = api.make_config(sv, bands=bands, nmodes=nmodes, pkfile=str(pk), extra=("solver = parpack",))
     files = {n: tmp_path / f"{n}.abn" for n in ("cells", "modes", "evals", "cov", "counts", "pix", "est")}
     cfg += "".join(f"{n}file = {p}\n" for n, p in [("cell", files["cells"]), ("mode", files["modes"]),
                                                     ("eval", files["evals"]), ("cov", files["cov"]),
@@ -81,6 +81,11 @@ def test_programs_reject_missing_options(tmp_path):
     assert res.returncode == 1 and "missing configuration options" in res.stderr
     res = subprocess.run([os.path.join(BIN, "klt"), "-h"], capture_output=True, text=True)
     assert res.returncode == 0 and "Usage: klt" in res.stdout
+    # the reference's solver key: parpack and anasazi are accepted, anything else refused (klt.cpp:167-193)
+    bad = tmp_path / "badsolver.cfg"
+    bad.write_text("cellfile = none.abn\nNmodes = 2\nmodefile = m.abn\nevalfile = e.abn\nsolver = lanczos\n")
+    res = subprocess.run([os.path.join(BIN, "klt"), "-c", str(bad)], capture_output=True, text=True)
+    assert res.returncode == 1 and "unrecognized solver: lanczos" in res.stderr
 
 
 def test_basis_and_mockcounts_programs(tmp_path):
