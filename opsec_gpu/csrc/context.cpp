@@ -1783,11 +1783,12 @@ int opsec_gpu_create(opsec_gpu** out, const char* cfg_text) {
     if (!c) return OPSEC_ERR_NOMEM;
     c->device = -1;
     int rc = guard(c, [&] {
+        // the configuration first (host only: its errors do not depend on a device), then the device
+        configure(c, parse_config(cfg_text));
+        c->cfg_text = cfg_text ? cfg_text : "";
         int dev = 0;
         OPSEC_CUDA(cudaGetDevice(&dev));
         c->device = dev;
-        configure(c, parse_config(cfg_text));
-        c->cfg_text = cfg_text ? cfg_text : "";
         OPSEC_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     });
     *out = c;  // returned even on error so that opsec_gpu_last_error can report it

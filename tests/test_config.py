@@ -1,0 +1,71 @@
+"""Configuration checks of opsec_gpu_create.  The configuration is parsed before the device
+is touched, so these run without a GPU: every out-of-range or unknown value is refused with
+OPSEC_ERR_CONFIG and a message naming the key; a valid configuration gets past the parser
+(OPSEC_OK on a GPU host, a CUDA error without one)."""
+import ctypes as C
+
+import pytest
+
+from opsec_gpu import api, build, synth
+
+
+@pytest.fixture(scope="module")
+def create():
+    build.build()
+    L = api.load()
+
+    def run(text):
+        h = C.c_void_p()
+        rc = L.opsec_gpu_create(C.byref(h), text.encode())
+        msg = L.opsec_gpu_last_error(h).decode() if h else ""
+        L.opsec_gpu_destroy(h)
+        return rc, msg
+
+    return run
+
+
+def _base(coordsys=1):
+    if coordsys == 1:
+        sv, _ = synth.box_survey(4)
+    else:
+        sv = synth.Survey(2, (200.0, 1000.0, -1.0, 1.0, 0.0, 6.283185307179586), (4, 4, 8))
+    return api.make_config(sv, bands=synth.band_edges(2, 0.0, 0.2))
+
+
+CONFIG = -1
+BAD = [
+    ("klt.solver = lanczos", "klt.solver"),
+    ("klt.degree = 0", "klt.degree"),
+    ("klt.tol = -1", "klt.tol"),
+    ("klt.gemm = tf32", "klt.gemm"),
+    ("klt.refine = -1", "klt.refine"),
+    ("sig.gauss = 7", "sig.gauss"),
+    ("mixing = bogus", "mixing"),
+    ("azimuthal.split = 17", "azimuthal.split"),
+    ("azimuthal.gemm = f16", "azimuthal.gemm"),
+    ("cubature.window_bins = 8", "cubature.window_bins"),
+    ("cubature.symmetry = half", "cubature.symmetry"),
+    ("basis.samples = 0", "basis.samples"),
+    ("xi.n1 = 0", "xi table layout"),
+    ("projection.chunk = 0", "projection.chunk"),
+]
+
+
+@pytest.mark.parametrize("line,key", BAD)
+def test_bad_values_are_refused(create, line, key):
+    rc, msg = create(_base() + line + "\n")
+    assert rc == CONFIG and key in msg, (rc, msg)
+
+
+def test_survey_type_is_required(create):
+    rc, msg = create("")
+    assert rc == CONFIG and "survey.type" in msg
+
+
+@pytest.mark.parametrize("coordsys", [1, 2])
+def test_valid_configurations_pass_the_parser(create, coordsys):
+    text = _base(coordsys)
+    for extra in ("", "klt.solver = chfsi\nklt.gemm = f32\nklt.degree = 6\n", "mixing = inverse-sqrt\n",
+                  "solver = parpack\n"):
+        rc, msg = create(text + extra)
+        assert rc in (api.OK, -3), (rc, msg)  # -3: OPSEC_ERR_CUDA, no device on this host
