@@ -75,13 +75,18 @@ def read(path: str):
 
 
 def write(f, array, fmt: str, opts: dict | None = None, comment: str = ""):
-    """Append one block to an open binary file (abn_write, abn.c:247-270)."""
+    """Append one block to an open binary file (abn_write, abn.c:186-220): `comment`, the text
+    the programs print before the block (its lines ending in a newline), then the block's
+    header -- an empty line, the options, the data-block line -- and the data."""
     a = np.ascontiguousarray(array)
     size = a.dtype.itemsize
     endian = "L" if sys.byteorder == "little" else "B"
     head = comment + "\n"
-    for k, v in (opts or {}).items():
-        head += f"{k} = {v}\n"
+    # keys in strcmp order with the quoting rule of cfg_write (cfg.c:292-312): the reference's
+    # Config keeps its entries sorted
+    for k in sorted((opts or {}), key=lambda x: str(x).encode()):
+        v = str(opts[k])
+        head += f'{k} = "{v}"\n' if v and (v[0].isspace() or v[-1].isspace()) else f"{k} = {v}\n"
     head += f"#!Begin data block: n = {a.size}, size = {size}, endian = {endian}, format = {fmt}\n"
     f.write(head.encode())
     f.write(a.tobytes())

@@ -3,6 +3,7 @@
 
 #include <unistd.h>
 
+#include <algorithm>
 #include <cctype>
 #include <cerrno>
 #include <cstdint>
@@ -192,8 +193,13 @@ bool abn_read(FILE* f, AbnHeader& h, std::vector<char>& data) {
 
 void abn_write_header(FILE* f, size_t n, const char* fmt, const Config* opts) {
     std::fprintf(f, "\n");
+    // keys in strcmp order: the reference's Config is a list kept sorted (cfg.c:49-132), and
+    // cfg_write walks it (cfg.c:297-312), so its headers list their keys sorted
+    std::vector<std::string> keys;
+    if (opts) keys = opts->order;
+    std::sort(keys.begin(), keys.end());
     if (opts)
-        for (const auto& k : opts->order) {
+        for (const auto& k : keys) {
             const std::string& v = opts->kv.at(k);
             bool quote = !v.empty() && (std::isspace((unsigned char)v.front()) || std::isspace((unsigned char)v.back()));
             std::fprintf(f, quote ? "%s = \"%s\"\n" : "%s = %s\n", k.c_str(), v.c_str());

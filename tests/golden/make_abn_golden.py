@@ -1,0 +1,80 @@
+"""Generate tests/golden/abn_ref.npz: ABN blocks written by the reference's own cfg.c and abn.c.
+
+Run where the reference checkout is present (it is absent on GPU hosts):
+
+    make -C oracle ref            # builds oracle/_ref/libopsecref.so
+    python tests/golden/make_abn_golden.py
+
+Each case is a comment written first (as the programs do with fprintf), then one
+abn_write of data under a Config filled with cfg_set in the given order
+(abn.c:186-220, cfg.c:297-312): the header of klt's evalfile (klt.cpp:209-218),
+comma's covfile (comma-scalapack.cpp:216-223), and a cell block whose options
+need quotes and mix upper- and lower-case keys.  Stored: the bytes of the file,
+the options in insertion order, the format, the comment and the data bytes.
+"""
+import ctypes as C
+import ctypes.util
+import json
+import os
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+L = C.CDLL(os.path.join(ROOT, "oracle", "_ref", "libopsecref.so"))
+libc = C.CDLL(ctypes.util.find_library("c"))
+libc.fopen.restype = C.c_void_p
+libc.fopen.argtypes = [C.c_char_p, C.c_char_p]
+libc.fputs.argtypes = [C.c_char_p, C.c_void_p]
+libc.fclose.argtypes = [C.c_void_p]
+L.cfg_new.restype = C.c_void_p
+L.cfg_set.argtypes = [C.c_void_p, C.c_char_p, C.c_char_p]
+L.cfg_destroy.argtypes = [C.c_void_p]
+L.abn_write.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_char_p, C.c_void_p]
+L.abn_write.restype = C.c_size_t
+
+
+def ref_write(comment, opts, data, n, fmt):
+    fd, path = tempfile.mkstemp()
+    os.close(fd)
+    f = libc.fopen(path.encode(), b"wb")
+    libc.fputs(comment.encode(), f)
+    cfg = L.cfg_new()
+    for k, v in opts:
+        L.cfg_set(cfg, k.encode(), v.encode())
+    L.abn_write(f, data.ctypes.data, n, fmt.encode(), cfg)
+    L.cfg_destroy(cfg)
+    libc.fclose(f)
+    raw = open(path, "rb").read()
+    os.remove(path)
+    return raw
+
+
+def main():
+    rng = np.random.default_rng(20261203)
+    cases = {
+        "klt_eval": ("# Signal matrix eigenvalues\n",
+                     [("cellfile", "cells.abn"), ("Ncells", "1728"), ("Nmodes", "5"), ("nconv", "5")],
+                     rng.standard_normal(5), 5, "d"),
+        "comma_cov": ("# Derivatives of the covariance matrix in KL basis, C_{ij,m}.\n",
+                      [("Nmodes", "3"), ("Nparams", "2"), ("packed", "1")], rng.standard_normal(12), 12, "d"),
+        "cells_quoted": ("",
+                         [("survey.type", "BoxSurvey"), ("zeta", " padded "), ("Ncells", "2"), ("alpha", "x y"),
+                          ("Beta", "tab\t")],
+                         rng.integers(0, 255, 160, dtype=np.uint8), 2, "4i8d"),
+    }
+    out = {}
+    for name, (comment, opts, data, n, fmt) in cases.items():
+        data = np.ascontiguousarray(data)
+        out[name + "_file"] = np.frombuffer(ref_write(comment, opts, data, n, fmt), dtype=np.uint8)
+        out[name + "_meta"] = np.frombuffer(json.dumps({"comment": comment, "opts": opts, "n": n, "fmt": fmt}).encode(),
+                                            dtype=np.uint8)
+        out[name + "_data"] = np.frombuffer(data.tobytes(), dtype=np.uint8)
+    np.savez_compressed(os.path.join(HERE, "abn_ref.npz"), **out)
+    for name in cases:
+        print(name, out[name + "_file"].tobytes()[:400])
+
+
+if __name__ == "__main__":
+    main()

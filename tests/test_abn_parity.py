@@ -1,0 +1,75 @@
+"""ABN files byte for byte as the reference writes them: the programs' writer
+(opsec_gpu/programs/progs.cpp, compiled here with g++) and the Python one
+(opsec_gpu/formats.py) against blocks written by the reference's own cfg.c / abn.c
+(tests/golden/abn_ref.npz, made by tests/golden/make_abn_golden.py): comment, the
+options sorted as the reference's Config keeps them, quoting, the data-block line and
+the data."""
+import ctypes as C
+import io
+import json
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+from opsec_gpu import formats
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+G = np.load(os.path.join(HERE, "golden", "abn_ref.npz"))
+CASES = ("klt_eval", "comma_cov", "cells_quoted")
+
+
+def _case(name):
+    meta = json.loads(G[name + "_meta"].tobytes())
+    return meta, G[name + "_data"].tobytes(), G[name + "_file"].tobytes()
+
+
+@pytest.fixture(scope="module")
+def writer(tmp_path_factory):
+    from opsec_gpu import build
+
+    build.build()
+    libdir = os.path.join(ROOT, "opsec_gpu")
+    so = str(tmp_path_factory.mktemp("abn") / "libabn_check.so")
+    subprocess.check_call(["g++", "-O1", "-std=c++17", "-shared", "-fPIC", "-o", so,
+                           os.path.join(HERE, "abn_check.cpp"), os.path.join(ROOT, "opsec_gpu", "programs", "progs.cpp"),
+                           f"-L{libdir}", "-lopsec_gpu", f"-Wl,-rpath,{libdir}"])
+    L = C.CDLL(so)
+    L.chk_abn_write.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.POINTER(C.c_char_p), C.POINTER(C.c_char_p),
+                                C.c_void_p, C.c_size_t, C.c_char_p]
+    return L
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_program_writer_matches_reference_bytes(writer, tmp_path, name):
+    meta, data, ref = _case(name)
+    keys = (C.c_char_p * len(meta["opts"]))(*[k.encode() for k, _ in meta["opts"]])
+    vals = (C.c_char_p * len(meta["opts"]))(*[v.encode() for _, v in meta["opts"]])
+    buf = C.create_string_buffer(data, len(data))
+    path = tmp_path / "out.abn"
+    assert writer.chk_abn_write(str(path).encode(), meta["comment"].encode(), len(meta["opts"]), keys, vals,
+                                C.cast(buf, C.c_void_p), meta["n"], meta["fmt"].encode()) == 0
+    assert path.read_bytes() == ref
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_python_writer_matches_reference_bytes(name):
+    meta, data, ref = _case(name)
+    rec = {"d": np.float64, "4i8d": np.dtype((np.void, 80))}[meta["fmt"]]
+    arr = np.frombuffer(data, dtype=rec)
+    f = io.BytesIO()
+    formats.write(f, arr, meta["fmt"], dict(meta["opts"]), comment=meta["comment"])  # the comment keeps its newline
+    assert f.getvalue() == ref
+
+
+def test_reader_round_trip_of_reference_bytes(tmp_path):
+    for name in CASES:
+        meta, data, ref = _case(name)
+        p = tmp_path / f"{name}.abn"
+        p.write_bytes(ref)
+        opts, arr = formats.read(str(p))
+        for k, v in meta["opts"]:
+            assert opts[k] == v, (name, k)
+        assert arr.tobytes() == data
