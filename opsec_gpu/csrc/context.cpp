@@ -9,6 +9,7 @@
 #include <atomic>
 #include <chrono>
 #include <cerrno>
+#include <cctype>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -125,26 +126,34 @@ bool Geometry::mu_symmetric() const {
 bool Geometry::full_sky() const { return coordsys == 2 && std::fabs(b[5] - b[4] - 2 * M_PI) < 1e-12; }
 
 // ---------------------------------------------------------------- config
-// key = value lines, '#' comments, surrounding quotes stripped (cfg.c:238-295).
+// key = value lines, '#' comments, C isspace trimmed, one pair of surrounding quotes stripped,
+// the last value of a key kept (cfg.c:238-295).  A line that is not key = value is an error
+// here: the reference stops reading its file there (cfg.c:200-214), a text handed to the
+// library is refused instead.
+static bool cspace(char c) { return std::isspace((unsigned char)c) != 0; }
+
 static std::map<std::string, std::string> parse_config(const char* text) {
     std::map<std::string, std::string> kv;
     if (!text) return kv;
     std::istringstream in(text);
     std::string line;
     while (std::getline(in, line)) {
-        size_t p = line.find_first_not_of(" \t\r\n");
-        if (p == std::string::npos || line[p] == '#') continue;
-        size_t eq = line.find('=', p);
+        size_t p = 0, end = line.size();
+        while (p < end && cspace(line[p])) p++;
+        if (p == end || line[p] == '#') continue;
+        const size_t eq = line.find('=', p);
         if (eq == std::string::npos || eq == p) fail(OPSEC_ERR_CONFIG, "not a key = value line: '" + line + "'");
-        std::string key = line.substr(p, eq - p);
-        key.erase(key.find_last_not_of(" \t") + 1);
-        std::string val = line.substr(eq + 1);
-        size_t vb = val.find_first_not_of(" \t\r\n");
-        val = (vb == std::string::npos) ? std::string() : val.substr(vb);
-        val.erase(val.find_last_not_of(" \t\r\n") + 1);
-        if (val.size() >= 2 && ((val.front() == '"' && val.back() == '"') || (val.front() == '\'' && val.back() == '\'')))
-            val = val.substr(1, val.size() - 2);
-        kv[key] = val;
+        size_t ke = eq;
+        while (ke > p && cspace(line[ke - 1])) ke--;
+        size_t vb = eq + 1;
+        while (vb < end && cspace(line[vb])) vb++;
+        size_t ve = end;
+        while (ve > vb && cspace(line[ve - 1])) ve--;
+        if (ve - vb >= 2 && ((line[vb] == '"' && line[ve - 1] == '"') || (line[vb] == '\'' && line[ve - 1] == '\''))) {
+            vb++;
+            ve--;
+        }
+        kv[line.substr(p, ke - p)] = line.substr(vb, ve - vb);
     }
     return kv;
 }

@@ -20,19 +20,38 @@ _BEGIN = re.compile(rb"#!Begin data block: n = (\d+), size = (\d+), endian = (\S
 _DTYPES = {"d": "f8", "f": "f4", "i": "i4", "q": "i8", "4i8d": None}
 
 
-def parse_config(text: str) -> dict:
-    """cfg_read_line semantics: '#' comments, key = value, quotes stripped."""
+_CSPACE = " \t\n\v\f\r"  # C isspace
+
+
+def parse_line(line: str):
+    """cfg_read_line (cfg.c:238-295): (key, value), None for a blank or '#' line, False for a
+    line that is not key = value.  Whitespace is C isspace; one pair of quotes is stripped."""
+    s = line.lstrip(_CSPACE)
+    if not s or s[0] == "#":
+        return None
+    eq = s.find("=")
+    if eq <= 0:
+        return False
+    k = s[:eq].rstrip(_CSPACE)
+    v = s[eq + 1:].strip(_CSPACE)
+    if len(v) >= 2 and v[0] == v[-1] and v[0] in "\"'":
+        v = v[1:-1]
+    return k, v
+
+
+def parse_config(text: str, stop_at_invalid: bool = True) -> dict:
+    """A configuration file as cfg_read reads it (cfg.c:200-214): key = value lines, the last
+    value of a key kept, reading stopped by the first invalid line (stop_at_invalid; ABN
+    headers, read line by line by abn_read_header, abn.c:221-247, skip it instead)."""
     out = {}
-    for line in text.splitlines():
-        s = line.strip()
-        if not s or s.startswith("#") or "=" not in s:
+    for line in text.split("\n"):
+        r = parse_line(line)
+        if r is False:
+            if stop_at_invalid:
+                break
             continue
-        k, v = s.split("=", 1)
-        k, v = k.strip(), v.strip()
-        if len(v) >= 2 and v[0] == v[-1] and v[0] in "\"'":
-            v = v[1:-1]
-        if k:
-            out[k] = v
+        if r is not None:
+            out[r[0]] = r[1]
     return out
 
 
@@ -61,7 +80,7 @@ def read_blocks(path: str):
         start = data.index(b"\n", m.end()) + 1
         dt = _dtype(fmt, size, endian)
         arr = np.frombuffer(data[start:start + n * size], dtype=dt, count=n).copy()
-        blocks.append((parse_config(header), arr))
+        blocks.append((parse_config(header, stop_at_invalid=False), arr))
         pos = start + n * size
     return blocks
 

@@ -27,32 +27,42 @@ void Config::set(const std::string& k, const std::string& v) {
     kv[k] = v;
 }
 
-// cfg_read_line (cfg.c:238-295): blank and '#' lines ignored, key = value,
-// whitespace trimmed, one pair of surrounding quotes stripped
-void Config::read_line(const std::string& line) {
-    size_t p = line.find_first_not_of(" \t\r\n");
-    if (p == std::string::npos || line[p] == '#') return;
-    size_t eq = line.find('=', p);
+// cfg_read_line (cfg.c:238-295): blank and '#' lines ignored, key = value, whitespace (C
+// isspace) trimmed, one pair of surrounding quotes stripped; false for a line that is not
+// key = value (no '=', or nothing before it)
+static bool cspace(char c) { return std::isspace((unsigned char)c) != 0; }
+
+bool Config::read_line(const std::string& line) {
+    size_t p = 0, end = line.size();
+    while (p < end && cspace(line[p])) p++;
+    if (p == end || line[p] == '#') return true;
+    const size_t eq = line.find('=', p);
     if (eq == std::string::npos || eq == p) {
         std::fprintf(stderr, "cfg_read_line: '%s' is not a valid configuration line\n", line.c_str());
-        return;
+        return false;
     }
-    std::string key = line.substr(p, eq - p);
-    key.erase(key.find_last_not_of(" \t") + 1);
-    std::string val = line.substr(eq + 1);
-    size_t vb = val.find_first_not_of(" \t\r\n");
-    val = vb == std::string::npos ? std::string() : val.substr(vb);
-    val.erase(val.find_last_not_of(" \t\r\n") + 1);
-    if (val.size() >= 2 && ((val.front() == '"' && val.back() == '"') || (val.front() == '\'' && val.back() == '\'')))
-        val = val.substr(1, val.size() - 2);
-    set(key, val);
+    size_t ke = eq;
+    while (ke > p && cspace(line[ke - 1])) ke--;
+    size_t vb = eq + 1;
+    while (vb < end && cspace(line[vb])) vb++;
+    size_t ve = end;
+    while (ve > vb && cspace(line[ve - 1])) ve--;
+    if (ve - vb >= 2 && ((line[vb] == '"' && line[ve - 1] == '"') || (line[vb] == '\'' && line[ve - 1] == '\''))) {
+        vb++;
+        ve--;
+    }
+    set(line.substr(p, ke - p), line.substr(vb, ve - vb));
+    return true;
 }
 
+// cfg_read (cfg.c:200-214): lines until the first one that is not key = value, which ends
+// the file's reading (what was read before it is kept)
 bool Config::read_file(const std::string& path) {
     std::ifstream in(path);
     if (!in) return false;
     std::string line;
-    while (std::getline(in, line)) read_line(line);
+    while (std::getline(in, line))
+        if (!read_line(line)) break;
     return true;
 }
 

@@ -20,7 +20,7 @@ struct Config {
     const std::string& get(const std::string& k) const;
     int get_int(const std::string& k) const;
     void set(const std::string& k, const std::string& v);
-    void read_line(const std::string& line);
+    bool read_line(const std::string& line);  // false (and a message) for an invalid line
     bool read_file(const std::string& path);
     std::string missing(const std::string& comma_keys) const;  // "" when all present
     std::string text() const;                                   // key = value lines

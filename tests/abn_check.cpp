@@ -15,3 +15,15 @@ extern "C" int chk_abn_write(const char* path, const char* comment, int nkeys, c
     std::fclose(f);
     return 0;
 }
+
+// a configuration file read by the programs' reader, written back as an ABN header of
+// n = 0 doubles (its options sorted, cfg_write's quoting)
+extern "C" int chk_cfg_dump(const char* in, const char* out) {
+    progs::Config c;
+    if (!c.read_file(in)) return 1;
+    FILE* f = std::fopen(out, "wb");
+    if (!f) return 1;
+    progs::abn_write_header(f, 0, "d", &c);
+    std::fclose(f);
+    return 0;
+}

@@ -1,9 +1,11 @@
-"""ABN files byte for byte as the reference writes them: the programs' writer
-(opsec_gpu/programs/progs.cpp, compiled here with g++) and the Python one
-(opsec_gpu/formats.py) against blocks written by the reference's own cfg.c / abn.c
-(tests/golden/abn_ref.npz, made by tests/golden/make_abn_golden.py): comment, the
-options sorted as the reference's Config keeps them, quoting, the data-block line and
-the data."""
+"""ABN files and configuration files as the reference writes and reads them: the
+programs' code (opsec_gpu/programs/progs.cpp, compiled here with g++) and the Python
+one (opsec_gpu/formats.py) against the reference's own cfg.c / abn.c:
+- blocks it wrote (tests/golden/abn_ref.npz, tests/golden/make_abn_golden.py): comment,
+  the options sorted as its Config keeps them, quoting, the data-block line, the data;
+- configuration texts it read (tests/golden/cfg_ref.npz, tests/golden/make_cfg_golden.py):
+  comments, whitespace, quotes, repeated keys, and the end of reading at the first line
+  that is not key = value."""
 import ctypes as C
 import io
 import json
@@ -19,6 +21,8 @@ from opsec_gpu import formats
 HERE = os.path.dirname(os.path.abspath(__file__))
 G = np.load(os.path.join(HERE, "golden", "abn_ref.npz"))
 CASES = ("klt_eval", "comma_cov", "cells_quoted")
+GC = np.load(os.path.join(HERE, "golden", "cfg_ref.npz"))
+CFG_CASES = sorted({k[:-3] for k in GC.files if k.endswith("_in")})
 
 
 def _case(name):
@@ -39,6 +43,7 @@ def writer(tmp_path_factory):
     L = C.CDLL(so)
     L.chk_abn_write.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.POINTER(C.c_char_p), C.POINTER(C.c_char_p),
                                 C.c_void_p, C.c_size_t, C.c_char_p]
+    L.chk_cfg_dump.argtypes = [C.c_char_p, C.c_char_p]
     return L
 
 
@@ -73,3 +78,23 @@ def test_reader_round_trip_of_reference_bytes(tmp_path):
         for k, v in meta["opts"]:
             assert opts[k] == v, (name, k)
         assert arr.tobytes() == data
+
+
+def test_cfg_cases_cover_the_rules():
+    assert {"plain", "whitespace", "quotes", "values", "stop", "stop_eq"} <= set(CFG_CASES)
+
+
+@pytest.mark.parametrize("name", CFG_CASES)
+def test_program_config_reader_matches_reference(writer, tmp_path, name):
+    src, dst = tmp_path / "in.cfg", tmp_path / "out.abn"
+    src.write_bytes(GC[name + "_in"].tobytes())
+    assert writer.chk_cfg_dump(str(src).encode(), str(dst).encode()) == 0
+    assert dst.read_bytes() == GC[name + "_out"].tobytes()
+
+
+@pytest.mark.parametrize("name", CFG_CASES)
+def test_python_config_reader_matches_reference(name):
+    opts = formats.parse_config(GC[name + "_in"].tobytes().decode("latin-1"))
+    f = io.BytesIO()
+    formats.write(f, np.zeros(0), "d", opts)
+    assert f.getvalue() == GC[name + "_out"].tobytes()

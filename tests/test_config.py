@@ -69,3 +69,19 @@ def test_valid_configurations_pass_the_parser(create, coordsys):
                   "solver = parpack\n"):
         rc, msg = create(text + extra)
         assert rc in (api.OK, -3), (rc, msg)  # -3: OPSEC_ERR_CUDA, no device on this host
+
+
+def test_parser_rules_of_the_library(create):
+    """The library reads key = value lines as cfg_read_line does (C isspace trimmed, quotes
+    stripped, the last value kept) and refuses a text with a line that is not key = value."""
+    base = _base()
+    # trimmed \t, \v, \f, \r and quotes: these values reach the option checks as '7' and 'bogus'
+    for line in ("sig.gauss =\t7\x0c", "\x0b sig.gauss = '7' \r", 'mixing = "bogus"'):
+        rc, msg = create(base + line + "\n")
+        assert rc == CONFIG and ("sig.gauss" in msg or "mixing" in msg), (line, rc, msg)
+    # ... and these are valid after trimming and unquoting
+    for line in ("mixing = 'inverse'", "sig.gauss\t=\t3\r", "sig.gauss = 9\nsig.gauss = 4"):
+        rc, msg = create(base + line + "\n")
+        assert rc in (api.OK, -3), (line, rc, msg)
+    rc, msg = create(base + "this is not key value\n")
+    assert rc == CONFIG and "not a key = value line" in msg

@@ -45,5 +45,7 @@ def test_cellfile_round_trip(tmp_path):
 
 def test_config_parsing_rules():
     text = "# comment\n  key = value  \nq = \"  spaced  \"\nbad line\nk2=v2\nkey = override\n"
-    cfg = formats.parse_config(text)
-    assert cfg == {"key": "override", "q": "  spaced  ", "k2": "v2"}
+    # a configuration file stops at its first invalid line (cfg.c:200-214) ...
+    assert formats.parse_config(text) == {"key": "value", "q": "  spaced  "}
+    # ... an ABN header reads on past it (abn.c:221-247)
+    assert formats.parse_config(text, stop_at_invalid=False) == {"key": "override", "q": "  spaced  ", "k2": "v2"}
