@@ -55,15 +55,39 @@ def parse_config(text: str, stop_at_invalid: bool = True) -> dict:
     return out
 
 
+_CODES = {"x": "V1", "c": "S1", "b": "i1", "B": "u1", "h": "i2", "H": "u2", "i": "i4", "I": "u4", "l": "i8",
+          "L": "u8", "q": "i8", "Q": "u8", "f": "f4", "d": "f8"}
+
+
+def _fields(fmt: str):
+    """Field codes of an ABN struct format, repeat counts expanded (abn.c:96-176)."""
+    out, num = [], ""
+    for ch in fmt:
+        if ch.isspace():
+            continue
+        if ch.isdigit():
+            num += ch
+            continue
+        out += [ch] * (int(num) if num else 1)
+        num = ""
+    return out
+
+
 def _dtype(fmt: str, size: int, endian: str):
+    """numpy dtype of one record in the file's byte order; values read through it come out
+    as abn_read returns them after abn_byte_swap."""
     e = "<" if endian == "L" else ">"
     if fmt == "4i8d":
         dt = CELL_DTYPE if e == "<" else CELL_DTYPE.newbyteorder(">")
         return dt
     code = _DTYPES.get(fmt)
-    if code is None:
+    if code is not None:
+        return np.dtype(e + code)
+    fl = _fields(fmt)
+    if not fl or any(c not in _CODES for c in fl):
         return np.dtype(f"V{size}")
-    return np.dtype(e + code)
+    dt = np.dtype([(f"f{k}", (e if _CODES[c][0] not in "VS" else "") + _CODES[c]) for k, c in enumerate(fl)])
+    return dt if dt.itemsize == size else np.dtype(f"V{size}")
 
 
 def read_blocks(path: str):

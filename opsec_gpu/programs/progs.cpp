@@ -150,6 +150,8 @@ static std::vector<int> field_sizes(const std::string& fmt) {
     std::vector<int> f;
     size_t i = 0;
     while (i < fmt.size()) {
+        while (i < fmt.size() && std::isspace((unsigned char)fmt[i])) i++;  // as abn_byte_swap (abn.c:113-115)
+        if (i >= fmt.size()) break;
         int num = 0;
         bool have = false;
         while (i < fmt.size() && std::isdigit((unsigned char)fmt[i])) {

@@ -1,6 +1,9 @@
 // C entry point over the programs' ABN writer (opsec_gpu/programs/progs.cpp) for
 // tests/test_abn_parity.py: one comment, then one abn_write under options set in order.
+#include <algorithm>
 #include <cstdio>
+#include <cstring>
+#include <vector>
 
 #include "../opsec_gpu/programs/progs.h"
 
@@ -26,4 +29,19 @@ extern "C" int chk_cfg_dump(const char* in, const char* out) {
     progs::abn_write_header(f, 0, "d", &c);
     std::fclose(f);
     return 0;
+}
+
+// the first data block of an ABN file as the programs read it (host byte order); returns
+// the byte count copied into out (at most cap), -1 when the file has no block
+extern "C" long long chk_abn_read(const char* path, void* out, size_t cap) {
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return -1;
+    progs::AbnHeader h;
+    std::vector<char> data;
+    const bool ok = progs::abn_read(f, h, data);
+    std::fclose(f);
+    if (!ok) return -1;
+    const size_t n = std::min(cap, data.size());
+    std::memcpy(out, data.data(), n);
+    return (long long)data.size();
 }

@@ -11,6 +11,11 @@ abn_write of data under a Config filled with cfg_set in the given order
 comma's covfile (comma-scalapack.cpp:216-223), and a cell block whose options
 need quotes and mix upper- and lower-case keys.  Stored: the bytes of the file,
 the options in insertion order, the format, the comment and the data bytes.
+
+Read cases: blocks of several formats in both byte orders (header written here, data
+laid out field by field in that order), read back by the reference's abn_read
+(abn.c:249-283, byte-swapped by abn_byte_swap, abn.c:96-183, when the order is not the
+host's).  Stored: the file bytes and the data as abn_read returns it.
 """
 import ctypes as C
 import ctypes.util
@@ -51,6 +56,63 @@ def ref_write(comment, opts, data, n, fmt):
     return raw
 
 
+L.abn_read.argtypes = [C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_size_t), C.POINTER(C.c_size_t),
+                       C.c_char_p, C.c_char_p, C.c_void_p]
+libc.free.argtypes = [C.c_void_p]
+CODES = {"c": "S1", "b": "i1", "B": "u1", "h": "i2", "H": "u2", "i": "i4", "I": "u4", "q": "i8", "Q": "u8",
+         "l": "i8", "f": "f4", "d": "f8"}
+
+
+def fields(fmt):
+    out, num = [], ""
+    for ch in fmt:
+        if ch.isdigit():
+            num += ch
+            continue
+        out += [ch] * (int(num) if num else 1)
+        num = ""
+    return out
+
+
+def ref_read(raw):
+    fd, path = tempfile.mkstemp()
+    os.write(fd, raw)
+    os.close(fd)
+    f = libc.fopen(path.encode(), b"rb")
+    ptr, n, size = C.c_void_p(), C.c_size_t(), C.c_size_t()
+    endian, fmt = C.create_string_buffer(4), C.create_string_buffer(64)
+    assert L.abn_read(f, C.byref(ptr), C.byref(n), C.byref(size), endian, fmt, None) == 0
+    data = C.string_at(ptr, n.value * size.value)
+    libc.free(ptr)
+    libc.fclose(f)
+    os.remove(path)
+    return data
+
+
+def read_cases(out):
+    rng = np.random.default_rng(7)
+    for fmt in ("d", "4f", "4i8d", "2h3q", "c2hfI"):
+        fl = fields(fmt)
+        n = 3
+        for endian, e in (("L", "<"), ("B", ">")):
+            dt = np.dtype([(f"f{k}", e + CODES[c]) for k, c in enumerate(fl)])
+            rec = np.zeros(n, dtype=dt)
+            for k, c in enumerate(fl):
+                if c in "fd":
+                    rec[f"f{k}"] = rng.standard_normal(n)
+                elif c == "c":
+                    rec[f"f{k}"] = [b"a", b"Z", b"!"]
+                else:
+                    info = np.iinfo(np.dtype(CODES[c]))
+                    rec[f"f{k}"] = rng.integers(info.min // 2, info.max // 2, n)
+            head = (f"\n# a {fmt} block\nNcells = {n}\n#!Begin data block: n = {n}, size = {dt.itemsize}, "
+                    f"endian = {endian}, format = {fmt}\n").encode()
+            raw = head + rec.tobytes()
+            name = f"read_{fmt}_{endian}"
+            out[name + "_file"] = np.frombuffer(raw, dtype=np.uint8)
+            out[name + "_data"] = np.frombuffer(ref_read(raw), dtype=np.uint8)
+
+
 def main():
     rng = np.random.default_rng(20261203)
     cases = {
@@ -71,6 +133,7 @@ def main():
         out[name + "_meta"] = np.frombuffer(json.dumps({"comment": comment, "opts": opts, "n": n, "fmt": fmt}).encode(),
                                             dtype=np.uint8)
         out[name + "_data"] = np.frombuffer(data.tobytes(), dtype=np.uint8)
+    read_cases(out)
     np.savez_compressed(os.path.join(HERE, "abn_ref.npz"), **out)
     for name in cases:
         print(name, out[name + "_file"].tobytes()[:400])

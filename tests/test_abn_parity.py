@@ -5,7 +5,9 @@ one (opsec_gpu/formats.py) against the reference's own cfg.c / abn.c:
   the options sorted as its Config keeps them, quoting, the data-block line, the data;
 - configuration texts it read (tests/golden/cfg_ref.npz, tests/golden/make_cfg_golden.py):
   comments, whitespace, quotes, repeated keys, and the end of reading at the first line
-  that is not key = value."""
+  that is not key = value;
+- blocks of several struct formats in both byte orders as its abn_read returns them
+  (byte-swapped field by field when the order is not the host's)."""
 import ctypes as C
 import io
 import json
@@ -23,6 +25,7 @@ G = np.load(os.path.join(HERE, "golden", "abn_ref.npz"))
 CASES = ("klt_eval", "comma_cov", "cells_quoted")
 GC = np.load(os.path.join(HERE, "golden", "cfg_ref.npz"))
 CFG_CASES = sorted({k[:-3] for k in GC.files if k.endswith("_in")})
+READ_CASES = sorted({k[:-5] for k in G.files if k.startswith("read_") and k.endswith("_file")})
 
 
 def _case(name):
@@ -44,6 +47,8 @@ def writer(tmp_path_factory):
     L.chk_abn_write.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.POINTER(C.c_char_p), C.POINTER(C.c_char_p),
                                 C.c_void_p, C.c_size_t, C.c_char_p]
     L.chk_cfg_dump.argtypes = [C.c_char_p, C.c_char_p]
+    L.chk_abn_read.argtypes = [C.c_char_p, C.c_void_p, C.c_size_t]
+    L.chk_abn_read.restype = C.c_longlong
     return L
 
 
@@ -98,3 +103,26 @@ def test_python_config_reader_matches_reference(name):
     f = io.BytesIO()
     formats.write(f, np.zeros(0), "d", opts)
     assert f.getvalue() == GC[name + "_out"].tobytes()
+
+
+def test_read_cases_cover_both_byte_orders():
+    assert len(READ_CASES) >= 10 and {c[-1] for c in READ_CASES} == {"L", "B"}
+
+
+@pytest.mark.parametrize("name", READ_CASES)
+def test_program_reader_matches_reference(writer, tmp_path, name):
+    p = tmp_path / "in.abn"
+    p.write_bytes(G[name + "_file"].tobytes())
+    want = G[name + "_data"].tobytes()
+    buf = C.create_string_buffer(len(want) + 16)
+    assert writer.chk_abn_read(str(p).encode(), buf, len(buf)) == len(want)
+    assert buf.raw[:len(want)] == want
+
+
+@pytest.mark.parametrize("name", READ_CASES)
+def test_python_reader_matches_reference(tmp_path, name):
+    p = tmp_path / "in.abn"
+    p.write_bytes(G[name + "_file"].tobytes())
+    opts, arr = formats.read(str(p))
+    assert opts["Ncells"] == "3"
+    assert arr.astype(arr.dtype.newbyteorder("=")).tobytes() == G[name + "_data"].tobytes()
