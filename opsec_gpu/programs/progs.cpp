@@ -187,19 +187,63 @@ bool abn_read_header(FILE* f, AbnHeader& h) {
     return false;
 }
 
+// abn_byte_swap (abn.c:96-183): every field of every record reversed when the block's byte
+// order is not the host's
+static void swap_block(const AbnHeader& h, std::vector<char>& data) {
+    if (h.endian == host_endian()) return;
+    std::vector<int> fs = field_sizes(h.format);
+    char* p = data.data();
+    for (size_t e = 0; e < h.n; e++)
+        for (int len : fs) {
+            for (int k = 0; k < len / 2; k++) std::swap(p[k], p[len - 1 - k]);
+            p += len;
+        }
+}
+
 bool abn_read(FILE* f, AbnHeader& h, std::vector<char>& data) {
     if (!abn_read_header(f, h)) return false;
     data.resize(h.n * h.size);
     if (h.n && std::fread(data.data(), h.size, h.n, f) != h.n) return false;
-    if (h.endian != host_endian()) {
-        std::vector<int> fs = field_sizes(h.format);
-        char* p = data.data();
-        for (size_t e = 0; e < h.n; e++)
-            for (int len : fs) {
-                for (int k = 0; k < len / 2; k++) std::swap(p[k], p[len - 1 - k]);
-                p += len;
-            }
+    swap_block(h, data);
+    return true;
+}
+
+// SplitFile (SplitFile.cpp:120-175): the data of a block may go on in the pieces of a file cut
+// by `split -d` -- when one piece ends, the next is the name with its last two characters
+// replaced by the two-digit index of the piece (cells.abn.00, cells.abn.01, ...).  The header
+// is read from the first piece.  A complete file opens no other piece.
+bool abn_read_split(const std::string& path, AbnHeader& h, std::vector<char>& data, std::string& err) {
+    FILE* f = std::fopen(path.c_str(), "rb");
+    if (!f) {
+        err = "could not open '" + path + "'";
+        return false;
     }
+    if (!abn_read_header(f, h)) {
+        std::fclose(f);
+        err = "error reading '" + path + "'";
+        return false;
+    }
+    data.resize(h.n * h.size);
+    std::string name = path;
+    size_t got = 0;
+    for (int index = 0; got < data.size() && f;) {
+        const size_t n = std::fread(data.data() + got, 1, data.size() - got, f);
+        got += n;
+        if (got < data.size()) {
+            if (!std::feof(f) || name.size() < 2) break;
+            index++;
+            const char suf[3] = {char('0' + (index / 10) % 10), char('0' + index % 10), 0};
+            name.replace(name.size() - 2, 2, suf);
+            f = std::freopen(name.c_str(), "rb", f);  // null (and closed) when there is no such piece
+        }
+    }
+    if (f) std::fclose(f);
+    if (got != data.size()) {
+        err = "error reading '" + path + "': " + std::to_string(got) + " of " + std::to_string(data.size()) +
+              " data bytes";
+        return false;
+    }
+    swap_block(h, data);
     return true;
 }
 
@@ -227,19 +271,9 @@ void abn_write(FILE* f, const void* data, size_t n, const char* fmt, const Confi
 
 std::vector<opsec_cell> read_cells(const std::string& path, std::string& err) {
     std::vector<opsec_cell> cells;
-    FILE* f = std::fopen(path.c_str(), "rb");
-    if (!f) {
-        err = "could not open '" + path + "'";
-        return cells;
-    }
     AbnHeader h;
     std::vector<char> data;
-    bool ok = abn_read(f, h, data);
-    std::fclose(f);
-    if (!ok) {
-        err = "error reading cells from '" + path + "'";
-        return cells;
-    }
+    if (!abn_read_split(path, h, data, err)) return cells;
     if (h.size != sizeof(opsec_cell) || abn_calcsize(h.format) != (int)sizeof(opsec_cell)) {
         err = "cell size mismatch in '" + path + "' (format " + h.format + ")";
         return cells;
@@ -254,15 +288,10 @@ std::vector<opsec_cell> read_cells(const std::string& path, std::string& err) {
 }
 
 bool read_modes(const std::string& path, int& nmodes, int& ncells, std::vector<double>& modes, std::string& err) {
-    FILE* f = std::fopen(path.c_str(), "rb");
-    if (!f) {
-        err = "could not open '" + path + "'";
-        return false;
-    }
     AbnHeader h;
     std::vector<char> data;
-    bool ok = abn_read(f, h, data);
-    std::fclose(f);
+    const bool ok = abn_read_split(path, h, data, err);
+    if (!ok && err.rfind("could not open", 0) == 0) return false;
     nmodes = h.opts.get_int("Nmodes");
     ncells = h.opts.get_int("Ncells");
     if (!ok || nmodes <= 0 || ncells <= 0 || h.n != (size_t)nmodes * ncells || h.size != sizeof(double)) {
@@ -275,15 +304,10 @@ bool read_modes(const std::string& path, int& nmodes, int& ncells, std::vector<d
 }
 
 bool read_doubles(const std::string& path, std::vector<double>& v, Config* opts, std::string& err) {
-    FILE* f = std::fopen(path.c_str(), "rb");
-    if (!f) {
-        err = "could not open '" + path + "'";
-        return false;
-    }
     AbnHeader h;
     std::vector<char> data;
-    bool ok = abn_read(f, h, data);
-    std::fclose(f);
+    const bool ok = abn_read_split(path, h, data, err);
+    if (!ok && err.rfind("could not open", 0) == 0) return false;
     if (!ok || h.size != sizeof(double)) {
         err = "error reading '" + path + "'";
         return false;

@@ -42,6 +42,8 @@ struct AbnHeader {
 bool abn_read_header(FILE* f, AbnHeader& h);
 // reads the whole data block (byte-swapped to host order for simple formats)
 bool abn_read(FILE* f, AbnHeader& h, std::vector<char>& data);
+// the first block of a file whose data may go on in split pieces (name.00, name.01, ...)
+bool abn_read_split(const std::string& path, AbnHeader& h, std::vector<char>& data, std::string& err);
 void abn_write_header(FILE* f, size_t n, const char* fmt, const Config* opts);
 void abn_write(FILE* f, const void* data, size_t n, const char* fmt, const Config* opts);
 int abn_calcsize(const std::string& fmt);

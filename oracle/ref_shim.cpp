@@ -21,6 +21,7 @@
 #include "QSpline.h"
 #include "SeparationFunc.h"
 #include "SphericalSurvey.h"
+#include "SplitFile.h"
 #include "Spline.h"
 #include "TestModel.h"
 #include "XiFunc.h"
@@ -275,6 +276,21 @@ void ref_count_galaxies(int coordsys, const double* grid, const int* n, long nga
         if (a >= 0) counts[a] += g[3];  // a = -1 (an empty grid cell) indexes before the array there
     }
     delete s;
+}
+
+// The data of the first ABN block of a file read through the reference's SplitFile, as
+// estimate reads its evalfile and covfile (estimate-mpi.cpp:152-200, SplitFile.cpp:120-175):
+// the header from the first piece, the data across the pieces that follow it.  Returns the
+// bytes read into out (at most cap), -1 without a header.
+long ref_split_read(const char* path, char* out, long cap) {
+    SplitFile f(path, "r");
+    if (!f.isopen()) return -1;
+    size_t n = 0, size = 0;
+    char endian = 0, fmt[ABN_MAX_FORMAT_LENGTH];
+    if (abn_read_header(f, &n, &size, &endian, fmt, NULL) != 0) return -1;
+    size_t want = n * size;
+    if ((long)want > cap) want = (size_t)cap;
+    return (long)f.read(out, want);
 }
 
 }  // extern "C"

@@ -45,3 +45,13 @@ extern "C" long long chk_abn_read(const char* path, void* out, size_t cap) {
     std::memcpy(out, data.data(), n);
     return (long long)data.size();
 }
+
+// the first block through the programs' split-file reader: bytes copied, -1 on an error
+extern "C" long long chk_abn_read_split(const char* path, void* out, size_t cap) {
+    progs::AbnHeader h;
+    std::vector<char> data;
+    std::string err;
+    if (!progs::abn_read_split(path, h, data, err)) return -1;
+    std::memcpy(out, data.data(), std::min(cap, data.size()));
+    return (long long)data.size();
+}

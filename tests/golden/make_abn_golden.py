@@ -12,6 +12,11 @@ comma's covfile (comma-scalapack.cpp:216-223), and a cell block whose options
 need quotes and mix upper- and lower-case keys.  Stored: the bytes of the file,
 the options in insertion order, the format, the comment and the data bytes.
 
+Split cases: one block cut into pieces name.00, name.01, ... (as `split -d -a 2` cuts a file)
+at byte offsets inside the data, read by the reference's SplitFile the way estimate reads its
+covfile (ref_split_read in oracle/ref_shim.cpp; SplitFile.cpp:120-175).  Stored: the pieces
+and the data as read; a case with its last piece missing stores the short read.
+
 Read cases: blocks of several formats in both byte orders (header written here, data
 laid out field by field in that order), read back by the reference's abn_read
 (abn.c:249-283, byte-swapped by abn_byte_swap, abn.c:96-183, when the order is not the
@@ -113,6 +118,42 @@ def read_cases(out):
             out[name + "_data"] = np.frombuffer(ref_read(raw), dtype=np.uint8)
 
 
+L.ref_split_read.argtypes = [C.c_char_p, C.c_void_p, C.c_long]
+L.ref_split_read.restype = C.c_long
+
+
+def split_cases(out):
+    rng = np.random.default_rng(11)
+    data = rng.standard_normal(500)
+    head = b"\n# Derivatives of the covariance matrix\nNmodes = 4\n" \
+           b"#!Begin data block: n = 500, size = 8, endian = L, format = d\n"
+    raw = head + data.tobytes()
+    for name, cuts, drop_last in (("three", (len(head) + 100, len(head) + 2501), False),
+                                  ("header_only", (len(head),), False),
+                                  ("whole", (), False),
+                                  ("missing", (len(head) + 800, len(head) + 2000), True)):
+        pieces, prev = [], 0
+        for c in list(cuts) + [len(raw)]:
+            pieces.append(raw[prev:c])
+            prev = c
+        d = tempfile.mkdtemp()
+        paths = [os.path.join(d, f"cov.abn.{i:02d}") for i in range(len(pieces))]
+        for i, (p, b) in enumerate(zip(paths, pieces)):
+            if drop_last and i == len(pieces) - 1:
+                continue
+            open(p, "wb").write(b)
+        buf = C.create_string_buffer(len(data) * 8 + 64)
+        got = L.ref_split_read(paths[0].encode(), buf, len(data) * 8)
+        for p in paths:
+            if os.path.exists(p):
+                os.remove(p)
+        os.rmdir(d)
+        out[f"split_{name}_npieces"] = np.array([len(pieces) - (1 if drop_last else 0)])
+        for i, b in enumerate(pieces[:len(pieces) - (1 if drop_last else 0)]):
+            out[f"split_{name}_piece{i}"] = np.frombuffer(b, dtype=np.uint8)
+        out[f"split_{name}_data"] = np.frombuffer(buf.raw[:got], dtype=np.uint8)
+
+
 def main():
     rng = np.random.default_rng(20261203)
     cases = {
@@ -134,6 +175,7 @@ def main():
                                             dtype=np.uint8)
         out[name + "_data"] = np.frombuffer(data.tobytes(), dtype=np.uint8)
     read_cases(out)
+    split_cases(out)
     np.savez_compressed(os.path.join(HERE, "abn_ref.npz"), **out)
     for name in cases:
         print(name, out[name + "_file"].tobytes()[:400])

@@ -7,7 +7,9 @@ one (opsec_gpu/formats.py) against the reference's own cfg.c / abn.c:
   comments, whitespace, quotes, repeated keys, and the end of reading at the first line
   that is not key = value;
 - blocks of several struct formats in both byte orders as its abn_read returns them
-  (byte-swapped field by field when the order is not the host's)."""
+  (byte-swapped field by field when the order is not the host's);
+- a block cut into pieces name.00, name.01, ... as its SplitFile reads it (estimate's
+  covfile and evalfile, comma's modefile)."""
 import ctypes as C
 import io
 import json
@@ -49,6 +51,8 @@ def writer(tmp_path_factory):
     L.chk_cfg_dump.argtypes = [C.c_char_p, C.c_char_p]
     L.chk_abn_read.argtypes = [C.c_char_p, C.c_void_p, C.c_size_t]
     L.chk_abn_read.restype = C.c_longlong
+    L.chk_abn_read_split.argtypes = [C.c_char_p, C.c_void_p, C.c_size_t]
+    L.chk_abn_read_split.restype = C.c_longlong
     return L
 
 
@@ -126,3 +130,18 @@ def test_python_reader_matches_reference(tmp_path, name):
     opts, arr = formats.read(str(p))
     assert opts["Ncells"] == "3"
     assert arr.astype(arr.dtype.newbyteorder("=")).tobytes() == G[name + "_data"].tobytes()
+
+
+@pytest.mark.parametrize("name", ["three", "header_only", "whole", "missing"])
+def test_split_file_reading_matches_reference(writer, tmp_path, name):
+    npieces = int(G[f"split_{name}_npieces"][0])
+    for i in range(npieces):
+        (tmp_path / f"cov.abn.{i:02d}").write_bytes(G[f"split_{name}_piece{i}"].tobytes())
+    want = G[f"split_{name}_data"].tobytes()
+    buf = C.create_string_buffer(4096)
+    got = writer.chk_abn_read_split(str(tmp_path / "cov.abn.00").encode(), buf, len(buf))
+    if name == "missing":
+        # the reference returns the 2,000 bytes it found; the programs refuse the short block
+        assert len(want) == 2000 and got == -1
+    else:
+        assert got == len(want) == 4000 and buf.raw[:got] == want
