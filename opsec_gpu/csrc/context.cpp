@@ -166,10 +166,12 @@ static double to_double(const std::string& key, const std::string& v) {
     return d;
 }
 
+// cfg_get_int (cfg.c:430-440) reads "%i": a leading integer in decimal, octal (0...) or hex
+// (0x...), whatever follows it ignored
 static int to_int(const std::string& key, const std::string& v) {
     char* end = nullptr;
-    long x = std::strtol(v.c_str(), &end, 10);
-    if (end == v.c_str() || *end != '\0') fail(OPSEC_ERR_CONFIG, "option " + key + " = '" + v + "' is not an integer");
+    long x = std::strtol(v.c_str(), &end, 0);
+    if (end == v.c_str()) fail(OPSEC_ERR_CONFIG, "option " + key + " = '" + v + "' is not an integer");
     return (int)x;
 }
 

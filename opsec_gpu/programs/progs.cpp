@@ -20,7 +20,8 @@ const std::string& Config::get(const std::string& k) const {
     return it == kv.end() ? empty : it->second;
 }
 
-int Config::get_int(const std::string& k) const { return std::atoi(get(k).c_str()); }
+// cfg_get_int (cfg.c:430-440): "%i", so octal and hex too, trailing text ignored
+int Config::get_int(const std::string& k) const { return (int)std::strtol(get(k).c_str(), nullptr, 0); }
 
 void Config::set(const std::string& k, const std::string& v) {
     if (!kv.count(k)) order.push_back(k);
@@ -274,11 +275,11 @@ std::vector<opsec_cell> read_cells(const std::string& path, std::string& err) {
     AbnHeader h;
     std::vector<char> data;
     if (!abn_read_split(path, h, data, err)) return cells;
-    if (h.size != sizeof(opsec_cell) || abn_calcsize(h.format) != (int)sizeof(opsec_cell)) {
+    if (h.size != sizeof(opsec_cell)) {  // Cell.cpp:52-55 checks the record size, not the format
         err = "cell size mismatch in '" + path + "' (format " + h.format + ")";
         return cells;
     }
-    if (h.opts.has("Ncells") && (size_t)h.opts.get_int("Ncells") != h.n) {
+    if ((size_t)h.opts.get_int("Ncells") != h.n) {  // ReadCells (Cell.cpp:47-51): the header's Ncells is required
         err = "consistency check fail for Ncells in '" + path + "'";
         return cells;
     }

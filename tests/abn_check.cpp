@@ -55,3 +55,17 @@ extern "C" long long chk_abn_read_split(const char* path, void* out, size_t cap)
     std::memcpy(out, data.data(), std::min(cap, data.size()));
     return (long long)data.size();
 }
+
+// an integer option as the programs read it (cfg_get_int's "%i")
+extern "C" int chk_get_int(const char* value) {
+    progs::Config c;
+    c.set("k", value);
+    return c.get_int("k");
+}
+
+// the cells of a cell file as the programs accept them: their count, -1 when refused
+extern "C" long long chk_read_cells(const char* path) {
+    std::string err;
+    std::vector<opsec_cell> cells = progs::read_cells(path, err);
+    return err.empty() ? (long long)cells.size() : -1;
+}

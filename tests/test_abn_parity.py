@@ -53,6 +53,9 @@ def writer(tmp_path_factory):
     L.chk_abn_read.restype = C.c_longlong
     L.chk_abn_read_split.argtypes = [C.c_char_p, C.c_void_p, C.c_size_t]
     L.chk_abn_read_split.restype = C.c_longlong
+    L.chk_get_int.argtypes = [C.c_char_p]
+    L.chk_read_cells.argtypes = [C.c_char_p]
+    L.chk_read_cells.restype = C.c_longlong
     return L
 
 
@@ -145,3 +148,30 @@ def test_split_file_reading_matches_reference(writer, tmp_path, name):
         assert len(want) == 2000 and got == -1
     else:
         assert got == len(want) == 4000 and buf.raw[:got] == want
+
+
+def test_integer_options_read_as_scanf_i(writer):
+    """cfg_get_int (cfg.c:430-440) reads "%i": octal and hex prefixes, trailing text ignored."""
+    for text, want in (("500", 500), ("010", 8), ("0x1F", 31), ("12abc", 12), ("500 # modes", 500), ("  -7", -7)):
+        assert writer.chk_get_int(text.encode()) == want, text
+
+
+def test_cell_file_checks_follow_read_cells(writer, tmp_path):
+    """ReadCells (Cell.cpp:16-56): the header's Ncells must equal the record count and the
+    record size must be 80 bytes; the format string itself is not checked."""
+    from opsec_gpu import synth
+
+    cells = np.zeros(3, dtype=synth.CELL_DTYPE)
+    cells["a"] = np.arange(3)
+
+    def put(name, opts, fmt="4i8d", arr=cells):
+        p = tmp_path / name
+        with open(p, "wb") as f:
+            formats.write(f, arr, fmt, opts)
+        return str(p).encode()
+
+    assert writer.chk_read_cells(put("ok.abn", {"Ncells": 3})) == 3
+    assert writer.chk_read_cells(put("other_fmt.abn", {"Ncells": 3}, fmt="10d")) == 3
+    assert writer.chk_read_cells(put("no_ncells.abn", {"survey.type": "BoxSurvey"})) == -1
+    assert writer.chk_read_cells(put("wrong_ncells.abn", {"Ncells": 4})) == -1
+    assert writer.chk_read_cells(put("small.abn", {"Ncells": 3}, fmt="9d", arr=np.zeros((3, 9)))) == -1

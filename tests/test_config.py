@@ -85,3 +85,15 @@ def test_parser_rules_of_the_library(create):
         assert rc in (api.OK, -3), (line, rc, msg)
     rc, msg = create(base + "this is not key value\n")
     assert rc == CONFIG and "not a key = value line" in msg
+
+
+def test_integer_options_read_as_scanf_i(create):
+    """Integer options are read as cfg_get_int reads them ("%i", cfg.c:430-440)."""
+    base = _base()
+    rc, msg = create(base + "sig.gauss = 010\n")  # octal 8: out of range
+    assert rc == CONFIG and "sig.gauss" in msg
+    for line in ("sig.gauss = 0x3", "sig.gauss = 3 # three points", "sig.gauss = 05"):
+        rc, msg = create(base + line + "\n")
+        assert rc in (api.OK, -3), (line, rc, msg)
+    rc, msg = create(base + "sig.gauss = three\n")
+    assert rc == CONFIG and "not an integer" in msg
