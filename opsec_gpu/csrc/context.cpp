@@ -554,11 +554,18 @@ void configure(opsec_gpu* c, const std::map<std::string, std::string>& kv) {
 
     if (has("Nmodes")) c->nmodes_cfg = to_int("Nmodes", get("Nmodes"));
     if (has("mixing")) {
+        // cfg_get_enum (cfg.c:486-501, estimate-mpi.cpp:369-372): the first of inverse,
+        // inverse-sqrt, identity that the value is a prefix of; no match is inverse
         const std::string& m = get("mixing");
-        if (m == "inverse") c->mixing = OPSEC_MIXING_INVERSE;
-        else if (m == "inverse-sqrt") c->mixing = OPSEC_MIXING_INVERSE_SQRT;
-        else if (m == "identity") c->mixing = OPSEC_MIXING_IDENTITY;
-        else fail(OPSEC_ERR_CONFIG, "mixing must be inverse, inverse-sqrt or identity");
+        static const std::pair<const char*, int> tags[] = {{"inverse", OPSEC_MIXING_INVERSE},
+                                                          {"inverse-sqrt", OPSEC_MIXING_INVERSE_SQRT},
+                                                          {"identity", OPSEC_MIXING_IDENTITY}};
+        c->mixing = OPSEC_MIXING_INVERSE;
+        for (const auto& t : tags)
+            if (std::string(t.first).compare(0, m.size(), m) == 0 && m.size() <= std::strlen(t.first)) {
+                c->mixing = t.second;
+                break;
+            }
     }
     if (has("xi.n1")) c->xl.n1 = to_int("xi.n1", get("xi.n1"));
     if (has("xi.n2")) c->xl.n2 = to_int("xi.n2", get("xi.n2"));

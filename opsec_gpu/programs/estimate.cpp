@@ -2,6 +2,7 @@
 // same options and estfile as the reference program at one rank
 // (code/opsec/src/estimate-mpi.cpp:340-660).
 #include <cstdio>
+#include <cstring>
 #include <cmath>
 #include <ctime>
 #include <vector>
@@ -33,8 +34,15 @@ int main(int argc, char** argv) {
     if (!fest) die("estimate", "cannot write to '" + cfg.get("estfile") + "'");
     int mixing = OPSEC_MIXING_INVERSE;
     if (cfg.has("mixing")) {
+        // cfg_get_enum (cfg.c:486-501): the first tag the value is a prefix of; no match is inverse
         const std::string& m = cfg.get("mixing");
-        mixing = m == "inverse-sqrt" ? OPSEC_MIXING_INVERSE_SQRT : m == "identity" ? OPSEC_MIXING_IDENTITY : OPSEC_MIXING_INVERSE;
+        const char* tags[] = {"inverse", "inverse-sqrt", "identity"};
+        const int modes[] = {OPSEC_MIXING_INVERSE, OPSEC_MIXING_INVERSE_SQRT, OPSEC_MIXING_IDENTITY};
+        for (int t = 0; t < 3; t++)
+            if (m.size() <= std::strlen(tags[t]) && std::string(tags[t]).compare(0, m.size(), m) == 0) {
+                mixing = modes[t];
+                break;
+            }
     }
     std::string err;
     std::vector<double> evals, cov, y;

@@ -40,7 +40,6 @@ BAD = [
     ("klt.gemm = tf32", "klt.gemm"),
     ("klt.refine = -1", "klt.refine"),
     ("sig.gauss = 7", "sig.gauss"),
-    ("mixing = bogus", "mixing"),
     ("azimuthal.split = 17", "azimuthal.split"),
     ("azimuthal.gemm = f16", "azimuthal.gemm"),
     ("cubature.window_bins = 8", "cubature.window_bins"),
@@ -75,10 +74,10 @@ def test_parser_rules_of_the_library(create):
     """The library reads key = value lines as cfg_read_line does (C isspace trimmed, quotes
     stripped, the last value kept) and refuses a text with a line that is not key = value."""
     base = _base()
-    # trimmed \t, \v, \f, \r and quotes: these values reach the option checks as '7' and 'bogus'
-    for line in ("sig.gauss =\t7\x0c", "\x0b sig.gauss = '7' \r", 'mixing = "bogus"'):
+    # trimmed \t, \v, \f, \r and quotes: these values reach the option checks as '7' and 'tf32'
+    for line in ("sig.gauss =\t7\x0c", "\x0b sig.gauss = '7' \r", 'klt.gemm = "tf32"'):
         rc, msg = create(base + line + "\n")
-        assert rc == CONFIG and ("sig.gauss" in msg or "mixing" in msg), (line, rc, msg)
+        assert rc == CONFIG and ("sig.gauss" in msg or "klt.gemm" in msg), (line, rc, msg)
     # ... and these are valid after trimming and unquoting
     for line in ("mixing = 'inverse'", "sig.gauss\t=\t3\r", "sig.gauss = 9\nsig.gauss = 4"):
         rc, msg = create(base + line + "\n")
@@ -97,3 +96,11 @@ def test_integer_options_read_as_scanf_i(create):
         assert rc in (api.OK, -3), (line, rc, msg)
     rc, msg = create(base + "sig.gauss = three\n")
     assert rc == CONFIG and "not an integer" in msg
+
+
+def test_mixing_is_read_as_cfg_get_enum(create):
+    """mixing is cfg_get_enum's (cfg.c:486-501): any prefix of inverse, inverse-sqrt or identity,
+    and a value matching none means inverse -- never an error, as in the reference."""
+    for v in ("inverse", "inverse-sqrt", "identity", "inv", "inverse-s", "id", "", "bogus"):
+        rc, msg = create(_base() + f"mixing = {v}\n")
+        assert rc in (api.OK, -3), (v, rc, msg)
