@@ -9,6 +9,7 @@ files from Python.
 """
 from __future__ import annotations
 
+import os
 import re
 import sys
 
@@ -90,9 +91,18 @@ def _dtype(fmt: str, size: int, endian: str):
     return dt if dt.itemsize == size else np.dtype(f"V{size}")
 
 
+def _next_piece(name: str, index: int) -> str:
+    """SplitFile's next piece (SplitFile.cpp:150-175): the last two characters replaced by the
+    two-digit index."""
+    return name[:-2] + f"{index % 100:02d}"
+
+
 def read_blocks(path: str):
-    """All data blocks of an ABN file: list of (opts, array)."""
+    """All data blocks of an ABN file: list of (opts, array).  A block whose data runs past the
+    end of the file goes on in the next pieces of a `split -d` series (name.00, name.01, ...),
+    as the reference's SplitFile reads it."""
     data = open(path, "rb").read()
+    name, index = path, 0
     pos = 0
     blocks = []
     while True:
@@ -102,6 +112,12 @@ def read_blocks(path: str):
         header = data[pos:m.start()].decode("ascii", "replace")
         n, size, endian, fmt = int(m.group(1)), int(m.group(2)), m.group(3).decode(), m.group(4).decode()
         start = data.index(b"\n", m.end()) + 1
+        while len(data) < start + n * size and len(name) >= 2:
+            index += 1
+            name = _next_piece(name, index)
+            if not os.path.exists(name):
+                break
+            data += open(name, "rb").read()
         dt = _dtype(fmt, size, endian)
         arr = np.frombuffer(data[start:start + n * size], dtype=dt, count=n).copy()
         blocks.append((parse_config(header, stop_at_invalid=False), arr))

@@ -148,6 +148,9 @@ def test_split_file_reading_matches_reference(writer, tmp_path, name):
         assert len(want) == 2000 and got == -1
     else:
         assert got == len(want) == 4000 and buf.raw[:got] == want
+        # the Python reader follows the pieces too
+        _, arr = formats.read(str(tmp_path / "cov.abn.00"))
+        assert arr.tobytes() == want
 
 
 def test_integer_options_read_as_scanf_i(writer):
