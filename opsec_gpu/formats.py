@@ -151,10 +151,53 @@ def write(f, array, fmt: str, opts: dict | None = None, comment: str = ""):
     f.write(a.tobytes())
 
 
+_C_INT = re.compile(r"\s*([+-]?)(0[xX][0-9a-fA-F]+|0[0-7]*|[1-9][0-9]*)")
+_C_DBL = re.compile(r"\s*[+-]?(\d+\.?\d*|\.\d+)([eE][+-]?\d+)?")
+
+
+def c_int(text: str) -> int:
+    """The leading integer of text as strtol(text, 0, 0) / "%i" reads it (0 when there is none)."""
+    m = _C_INT.match(text)
+    if not m:
+        return 0
+    sign, digits = m.groups()
+    v = int(digits, 16) if digits[:2] in ("0x", "0X") else int(digits, 8) if digits.startswith("0") else int(digits)
+    return -v if sign == "-" else v
+
+
+def c_double(text: str) -> float:
+    """The leading number of text as strtod reads it (0 when there is none)."""
+    m = _C_DBL.match(text)
+    return float(m.group(0)) if m else 0.0
+
+
+def survey_header(opts: dict, ncells: int) -> dict:
+    """The options basis writes on its cell file (basis.cpp:195-199): the survey's
+    GetConfigurationOptions (Survey.cpp:103-129, BoxSurvey.cpp:135-141,
+    SphericalSurvey.cpp:172-178) from `survey.*` options -- keys unprefixed, doubles "%g",
+    MuMin from MuMuin (Survey.cpp:39) -- and Ncells."""
+    g = lambda k: f"{c_double(opts.get('survey.' + k, '')):g}"
+    i = lambda k: str(c_int(opts.get("survey." + k, "")))
+    if opts.get("survey.type") == "BoxSurvey":
+        out = {"coordsys": "cartesian"}
+        out.update({k: g(k) for k in ("XMin", "XMax", "YMin", "YMax", "ZMin", "ZMax")})
+        out.update({k: i(k) for k in ("Nx", "Ny", "Nz")})
+        out.update(galfile=opts.get("survey.galfile", ""), nbar=g("nbar"), L=g("L"))
+    else:
+        out = {"coordsys": "spherical", "RMin": g("RMin"), "RMax": g("RMax"),
+               "MuMin": g("MuMuin" if "survey.MuMuin" in opts else "MuMin"), "MuMax": g("MuMax"),
+               "PhiMin": g("PhiMin"), "PhiMax": g("PhiMax")}
+        out.update({k: i(k) for k in ("Nr", "Nmu", "Nphi")})
+        out.update(galfile=opts.get("survey.galfile", ""), maskfile=opts.get("survey.maskfile", ""),
+                   radial=opts.get("survey.radial", ""))
+    out["Ncells"] = str(ncells)
+    return out
+
+
 def write_cells(path: str, cells, survey_lines=()):
-    """A cellfile as basis writes it (basis.cpp:197-201): survey options, Ncells, 4i8d records."""
-    opts = parse_config("\n".join(survey_lines))
-    opts["Ncells"] = str(len(cells))
+    """A cellfile as basis writes it (basis.cpp:195-201): the header of survey_header from the
+    `survey.*` configuration lines, then the 4i8d records."""
+    opts = survey_header(parse_config("\n".join(survey_lines)), len(cells))
     with open(path, "wb") as f:
         write(f, np.asarray(cells, dtype=CELL_DTYPE), "4i8d", opts)
 

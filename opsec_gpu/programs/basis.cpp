@@ -88,11 +88,7 @@ int main(int argc, char** argv) {
     std::vector<opsec_cell> cells(n);
     if (n && opsec_gpu_basis(g, n, cells.data(), &n) != OPSEC_OK) die("basis", opsec_gpu_last_error(g));
     std::fprintf(stderr, "basis: got %d non-empty cells\n", n);
-    // the survey options and Ncells in the header (basis.cpp:193-198)
-    Config opts;
-    for (const std::string& k : cfg.order)
-        if (k == "coordsys" || k.compare(0, 7, "survey.") == 0) opts.set(k, cfg.get(k));
-    opts.set("Ncells", std::to_string(n));
+    const Config opts = survey_header(cfg, n);  // the reference's header, byte for byte
     abn_write(fcells, cells.data(), (size_t)n, "4i8d", &opts);
     std::fclose(fcells);
     opsec_gpu_destroy(g);

@@ -319,6 +319,43 @@ bool read_doubles(const std::string& path, std::vector<double>& v, Config* opts,
     return true;
 }
 
+// The options basis writes on its cell file (basis.cpp:195-199): the survey's
+// GetConfigurationOptions (Survey.cpp:103-129, BoxSurvey.cpp:135-141,
+// SphericalSurvey.cpp:172-178) -- keys without the "survey." prefix, doubles printed "%g"
+// (cfg_set_double), MuMin read from MuMuin (Survey.cpp:39; MuMin without it) -- and Ncells.
+Config survey_header(const Config& cfg, int ncells) {
+    auto key = [&](const std::string& k) { return "survey." + k; };
+    auto dbl = [&](const std::string& k) {
+        char buf[64];
+        std::snprintf(buf, sizeof buf, "%g", std::strtod(cfg.get(key(k)).c_str(), nullptr));
+        return std::string(buf);
+    };
+    auto num = [&](const std::string& k) { return std::to_string((int)std::strtol(cfg.get(key(k)).c_str(), nullptr, 0)); };
+    Config o;
+    if (cfg.get("survey.type") == "BoxSurvey") {
+        o.set("coordsys", "cartesian");
+        for (const char* k : {"XMin", "XMax", "YMin", "YMax", "ZMin", "ZMax"}) o.set(k, dbl(k));
+        for (const char* k : {"Nx", "Ny", "Nz"}) o.set(k, num(k));
+        o.set("galfile", cfg.get("survey.galfile"));
+        o.set("nbar", dbl("nbar"));
+        o.set("L", dbl("L"));
+    } else {
+        o.set("coordsys", "spherical");
+        o.set("RMin", dbl("RMin"));
+        o.set("RMax", dbl("RMax"));
+        o.set("MuMin", dbl(cfg.has("survey.MuMuin") ? "MuMuin" : "MuMin"));
+        o.set("MuMax", dbl("MuMax"));
+        o.set("PhiMin", dbl("PhiMin"));
+        o.set("PhiMax", dbl("PhiMax"));
+        for (const char* k : {"Nr", "Nmu", "Nphi"}) o.set(k, num(k));
+        o.set("galfile", cfg.get("survey.galfile"));
+        o.set("maskfile", cfg.get("survey.maskfile"));
+        o.set("radial", cfg.get("survey.radial"));
+    }
+    o.set("Ncells", std::to_string(ncells));
+    return o;
+}
+
 opsec_gpu* make_context(const char* prog, const Config& cfg) {
     opsec_gpu* g = nullptr;
     int rc = opsec_gpu_create(&g, cfg.text().c_str());

@@ -57,6 +57,9 @@ bool read_modes(const std::string& path, int& nmodes, int& ncells, std::vector<d
 bool read_doubles(const std::string& path, std::vector<double>& v, Config* opts, std::string& err);
 
 // library context from the program's configuration; exits on error
+// the survey options and Ncells that basis writes on its cell file (basis.cpp:195-199)
+Config survey_header(const Config& cfg, int ncells);
+
 opsec_gpu* make_context(const char* prog, const Config& cfg);
 
 }  // namespace progs

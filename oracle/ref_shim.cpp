@@ -293,4 +293,23 @@ long ref_split_read(const char* path, char* out, long cap) {
     return (long)f.read(out, want);
 }
 
+// The header basis writes on its cell file (basis.cpp:195-199): the survey's
+// GetConfigurationOptions (Survey.cpp:103-129, BoxSurvey.cpp:135-141,
+// SphericalSurvey.cpp:172-178) plus Ncells, from the survey's sub-configuration in
+// cfgpath (keys without the "survey." prefix, as InitializeSurvey hands them over).
+int ref_survey_header(int coordsys, const char* cfgpath, int ncells, const char* outpath) {
+    Config cfg = cfg_new();
+    if (cfg_read_file(cfg, cfgpath) != 0) return 1;
+    Survey* s = coordsys == CoordSysCartesian ? (Survey*)new BoxSurvey(cfg) : (Survey*)new SphericalSurvey(cfg);
+    Config opts = s->GetConfigurationOptions();
+    cfg_set_int(opts, "Ncells", ncells);
+    FILE* f = fopen(outpath, "wb");
+    abn_write_header(f, ncells, CELL_FMT_STRING, opts);
+    fclose(f);
+    cfg_destroy(opts);
+    cfg_destroy(cfg);
+    delete s;
+    return 0;
+}
+
 }  // extern "C"

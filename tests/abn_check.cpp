@@ -69,3 +69,15 @@ extern "C" long long chk_read_cells(const char* path) {
     std::vector<opsec_cell> cells = progs::read_cells(path, err);
     return err.empty() ? (long long)cells.size() : -1;
 }
+
+// the cell-file header the basis program writes, for a program configuration file
+extern "C" int chk_survey_header(const char* cfgpath, int ncells, const char* outpath) {
+    progs::Config c;
+    if (!c.read_file(cfgpath)) return 1;
+    const progs::Config opts = progs::survey_header(c, ncells);
+    FILE* f = std::fopen(outpath, "wb");
+    if (!f) return 1;
+    progs::abn_write_header(f, (size_t)ncells, "4i8d", &opts);
+    std::fclose(f);
+    return 0;
+}

@@ -17,6 +17,10 @@ at byte offsets inside the data, read by the reference's SplitFile the way estim
 covfile (ref_split_read in oracle/ref_shim.cpp; SplitFile.cpp:120-175).  Stored: the pieces
 and the data as read; a case with its last piece missing stores the short read.
 
+Survey cases: the header the reference's basis writes on its cell file for a box and a
+shell (ref_survey_header in oracle/ref_shim.cpp: GetConfigurationOptions plus Ncells), from
+the survey's options; stored with the program configuration they come from.
+
 Read cases: blocks of several formats in both byte orders (header written here, data
 laid out field by field in that order), read back by the reference's abn_read
 (abn.c:249-283, byte-swapped by abn_byte_swap, abn.c:96-183, when the order is not the
@@ -154,6 +158,33 @@ def split_cases(out):
         out[f"split_{name}_data"] = np.frombuffer(buf.raw[:got], dtype=np.uint8)
 
 
+L.ref_survey_header.argtypes = [C.c_int, C.c_char_p, C.c_int, C.c_char_p]
+
+SURVEYS = {
+    "box": (1, "survey.type = BoxSurvey\nsurvey.XMin = 0\nsurvey.XMax = 600.0\nsurvey.YMin = -12.5\n"
+               "survey.YMax = 587.5\nsurvey.ZMin = 0.001\nsurvey.ZMax = 1234567.891\nsurvey.Nx = 12\n"
+               "survey.Ny = 0x0c\nsurvey.Nz = 12\nsurvey.galfile = gals.abn\nsurvey.nbar = 3e-4\nsurvey.L = 600\n"),
+    "sph": (2, "survey.type = SphericalSurvey\nsurvey.RMin = 200\nsurvey.RMax = 1000.0\nsurvey.MuMin = -1\n"
+               "survey.MuMuin = -1.0\nsurvey.MuMax = 1\nsurvey.PhiMin = 0\nsurvey.PhiMax = 6.283185307179586\n"
+               "survey.Nr = 32\nsurvey.Nmu = 32\nsurvey.Nphi = 32\nsurvey.galfile = none\n"
+               "survey.maskfile = none\nsurvey.radial = none\n"),
+}
+
+
+def survey_cases(out):
+    for name, (coordsys, text) in SURVEYS.items():
+        sub = "".join(line[len("survey."):] + "\n" for line in text.splitlines() if line.startswith("survey."))
+        d = tempfile.mkdtemp()
+        src, dst = os.path.join(d, "survey.cfg"), os.path.join(d, "head.abn")
+        open(src, "w").write(sub)
+        assert L.ref_survey_header(coordsys, src.encode(), 1728, dst.encode()) == 0
+        out[f"survey_{name}_cfg"] = np.frombuffer(text.encode(), dtype=np.uint8)
+        out[f"survey_{name}_head"] = np.frombuffer(open(dst, "rb").read(), dtype=np.uint8)
+        os.remove(src)
+        os.remove(dst)
+        os.rmdir(d)
+
+
 def main():
     rng = np.random.default_rng(20261203)
     cases = {
@@ -176,6 +207,7 @@ def main():
         out[name + "_data"] = np.frombuffer(data.tobytes(), dtype=np.uint8)
     read_cases(out)
     split_cases(out)
+    survey_cases(out)
     np.savez_compressed(os.path.join(HERE, "abn_ref.npz"), **out)
     for name in cases:
         print(name, out[name + "_file"].tobytes()[:400])

@@ -56,6 +56,7 @@ def writer(tmp_path_factory):
     L.chk_get_int.argtypes = [C.c_char_p]
     L.chk_read_cells.argtypes = [C.c_char_p]
     L.chk_read_cells.restype = C.c_longlong
+    L.chk_survey_header.argtypes = [C.c_char_p, C.c_int, C.c_char_p]
     return L
 
 
@@ -178,3 +179,28 @@ def test_cell_file_checks_follow_read_cells(writer, tmp_path):
     assert writer.chk_read_cells(put("no_ncells.abn", {"survey.type": "BoxSurvey"})) == -1
     assert writer.chk_read_cells(put("wrong_ncells.abn", {"Ncells": 4})) == -1
     assert writer.chk_read_cells(put("small.abn", {"Ncells": 3}, fmt="9d", arr=np.zeros((3, 9)))) == -1
+
+
+@pytest.mark.parametrize("name", ["box", "sph"])
+def test_basis_cell_file_header_matches_reference(writer, tmp_path, name):
+    """The basis program's cell-file header: the survey's GetConfigurationOptions (unprefixed
+    keys, doubles as "%g", MuMin from MuMuin) and Ncells, as the reference's basis writes it."""
+    cfg, out = tmp_path / "opsec.cfg", tmp_path / "head.abn"
+    cfg.write_bytes(G[f"survey_{name}_cfg"].tobytes())
+    assert writer.chk_survey_header(str(cfg).encode(), 1728, str(out).encode()) == 0
+    assert out.read_bytes() == G[f"survey_{name}_head"].tobytes()
+
+
+@pytest.mark.parametrize("name", ["box", "sph"])
+def test_python_cell_file_header_matches_reference(name):
+    opts = formats.survey_header(formats.parse_config(G[f"survey_{name}_cfg"].tobytes().decode()), 1728)
+    f = io.BytesIO()
+    formats.write(f, np.zeros(1728, dtype=np.dtype((np.void, 80))), "4i8d", opts)
+    assert f.getvalue()[:len(G[f"survey_{name}_head"])] == G[f"survey_{name}_head"].tobytes()
+
+
+def test_c_number_readers():
+    for text, want in (("12", 12), ("0x0c", 12), ("010", 8), ("0", 0), ("-7 # x", -7), ("abc", 0), ("  +5", 5)):
+        assert formats.c_int(text) == want, text
+    for text, want in (("3e-4", 3e-4), ("600.0", 600.0), (".5x", 0.5), ("-1", -1.0), ("", 0.0)):
+        assert formats.c_double(text) == want, text

@@ -39,7 +39,9 @@ def test_cellfile_round_trip(tmp_path):
     p = tmp_path / "cells.abn"
     formats.write_cells(str(p), cells, sv.config_lines())
     opts, back = formats.read(str(p))
-    assert int(opts["Ncells"]) == cells.size and opts["survey.type"] == "SphericalSurvey"
+    # the header basis writes: the survey's options unprefixed (Survey.cpp:103-129) and Ncells
+    assert int(opts["Ncells"]) == cells.size and opts["coordsys"] == "spherical"
+    assert (opts["Nr"], opts["Nmu"], opts["Nphi"]) == ("2", "3", "4") and opts["RMin"] == "200"
     assert back.tobytes() == cells.tobytes()
 
 
