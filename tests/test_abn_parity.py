@@ -204,3 +204,22 @@ def test_c_number_readers():
         assert formats.c_int(text) == want, text
     for text, want in (("3e-4", 3e-4), ("600.0", 600.0), (".5x", 0.5), ("-1", -1.0), ("", 0.0)):
         assert formats.c_double(text) == want, text
+
+
+def test_split_command_pieces_read_back(writer, tmp_path):
+    """After testSplitFile.cpp: a file cut by `split -d -b 999` (pieces name00, name01, ...)
+    reads back whole -- here an ABN block of 4,096 random bytes, by the programs' reader and
+    the Python reader."""
+    rng = np.random.default_rng(32)
+    data = rng.integers(0, 256, 4096, dtype=np.uint8)
+    full = tmp_path / "fullrandom"
+    with open(full, "wb") as f:
+        formats.write(f, data, "B", {"Nbytes": 4096})
+    subprocess.check_call(["split", "-d", "-b", "999", str(full), str(tmp_path / "splitrandom")])
+    first = tmp_path / "splitrandom00"
+    assert (tmp_path / "splitrandom04").exists()
+    buf = C.create_string_buffer(4096)
+    assert writer.chk_abn_read_split(str(first).encode(), buf, 4096) == 4096
+    assert buf.raw == data.tobytes()
+    opts, arr = formats.read(str(first))
+    assert opts["Nbytes"] == "4096" and arr.tobytes() == data.tobytes()

@@ -104,3 +104,20 @@ def test_mixing_is_read_as_cfg_get_enum(create):
     for v in ("inverse", "inverse-sqrt", "identity", "inv", "inverse-s", "id", "", "bogus"):
         rc, msg = create(_base() + f"mixing = {v}\n")
         assert rc in (api.OK, -3), (v, rc, msg)
+
+
+def test_band_lists_read_as_cfg_get_array(create):
+    """RealModel.bands is read as cfg_get_array_double reads it (space or comma separated,
+    empty fields skipped: testcfg.c:55-87); an odd trailing value is dropped (RealModel.cpp:49-52)."""
+    L = api.load()
+    L.opsec_gpu_num_params.argtypes = [C.c_void_p, C.POINTER(C.c_int)]
+    sv, _ = synth.box_survey(4)
+    for text, nb in (("0 0.1 0.1 0.2", 2), ("0, 0.1, 0.1, 0.2", 2), ("0, 0.1, 0.1, 0.2,", 2),
+                     ("0, 0.1, 0.1, 0.2,,", 2), ("0 0.1 0.1", 1)):
+        h = C.c_void_p()
+        text_cfg = "\n".join(sv.config_lines()) + f"\nmodel = RealModel\nRealModel.bands = {text}\n"
+        L.opsec_gpu_create(C.byref(h), text_cfg.encode())
+        n = C.c_int(-1)
+        rc = L.opsec_gpu_num_params(h, C.byref(n))  # host state: no device needed
+        L.opsec_gpu_destroy(h)
+        assert rc == api.OK and n.value == nb, (text, rc, n.value)
