@@ -223,3 +223,17 @@ def test_split_command_pieces_read_back(writer, tmp_path):
     assert buf.raw == data.tobytes()
     opts, arr = formats.read(str(first))
     assert opts["Nbytes"] == "4096" and arr.tobytes() == data.tobytes()
+
+
+def test_program_round_trip_after_testabn(writer, tmp_path):
+    """After testabn.c: 100 values cos(i) written with no options and read back -- count, record
+    size and values -- through the programs' writer and reader."""
+    data = np.cos(np.arange(100.0))
+    p = tmp_path / "cos.abn"
+    keys = (C.c_char_p * 0)()
+    assert writer.chk_abn_write(str(p).encode(), b"", 0, keys, keys, data.ctypes.data, 100, b"d") == 0
+    buf = C.create_string_buffer(800)
+    assert writer.chk_abn_read(str(p).encode(), buf, 800) == 800
+    assert np.array_equal(np.frombuffer(buf.raw, dtype=np.float64), data)
+    opts, arr = formats.read(str(p))
+    assert opts == {} and arr.dtype == np.float64 and np.array_equal(arr, data)
