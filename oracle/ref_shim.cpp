@@ -19,6 +19,7 @@
 #include "Cell.h"
 #include "Model.h"
 #include "QSpline.h"
+#include "RealModel.h"
 #include "SeparationFunc.h"
 #include "SphericalSurvey.h"
 #include "SplitFile.h"
@@ -309,6 +310,21 @@ int ref_survey_header(int coordsys, const char* cfgpath, int ncells, const char*
     cfg_destroy(opts);
     cfg_destroy(cfg);
     delete s;
+    return 0;
+}
+
+// Model::GetParam of RealModel for every band (RealModel.cpp:33-96): P(k) from pkfile,
+// Nbands regular bands on [kmin, kmax] (the values pass through cfg_set_double's "%g").
+int ref_band_params(const char* pkfile, int nbands, double kmin, double kmax, double* out) {
+    Config cfg = cfg_new();
+    cfg_set(cfg, "pkfile", pkfile);
+    cfg_set_int(cfg, "Nbands", nbands);
+    cfg_set_double(cfg, "kmin", kmin);
+    cfg_set_double(cfg, "kmax", kmax);
+    RealModel m(cfg);
+    cfg_destroy(cfg);
+    if (m.NumParams() != nbands) return 1;
+    for (int n = 0; n < nbands; n++) out[n] = m.GetParam(n);
     return 0;
 }
 

@@ -3,6 +3,7 @@ is touched, so these run without a GPU: every out-of-range or unknown value is r
 OPSEC_ERR_CONFIG and a message naming the key; a valid configuration gets past the parser
 (OPSEC_OK on a GPU host, a CUDA error without one)."""
 import ctypes as C
+import os
 
 import pytest
 
@@ -121,3 +122,36 @@ def test_band_lists_read_as_cfg_get_array(create):
         rc = L.opsec_gpu_num_params(h, C.byref(n))  # host state: no device needed
         L.opsec_gpu_destroy(h)
         assert rc == api.OK and n.value == nb, (text, rc, n.value)
+
+
+def test_band_priors_match_reference(tmp_path):
+    """Model::GetParam (RealModel.cpp:85-96), the prior estimate reads: the band powers of the
+    reference's own RealModel (tests/golden/params_ref.npz, tests/golden/make_params_golden.py)
+    against the oracle and against the library, which reads the same pkfile on the host."""
+    import numpy as np
+
+    import oracle as O
+
+    G = np.load(os.path.join(os.path.dirname(__file__), "golden", "params_ref.npz"))
+    pk = tmp_path / "pk.dat"
+    synth.write_pkfile(str(pk), G["pk_k"], G["pk_P"])
+    L = api.load()
+    L.opsec_gpu_get_params.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
+    sv, _ = synth.box_survey(4)
+    for name in ("c1", "c2", "narrow"):
+        nb, kmin, kmax = (float(x) for x in G[f"{name}_bands"])
+        nb = int(nb)
+        want = G[f"{name}_params"]
+        bands = [(kmin + n * (kmax - kmin) / nb, kmin + (n + 1) * (kmax - kmin) / nb) for n in range(nb)]
+        np.testing.assert_allclose(O.band_priors(G["pk_k"], G["pk_P"], bands), want, rtol=1e-13)
+        text = "\n".join(sv.config_lines()) + (f"\nmodel = RealModel\nRealModel.pkfile = {pk}\n"
+                                               f"RealModel.Nbands = {nb}\nRealModel.kmin = {kmin!r}\n"
+                                               f"RealModel.kmax = {kmax!r}\n")
+        h = C.c_void_p()
+        rc = L.opsec_gpu_create(C.byref(h), text.encode())
+        assert rc in (api.OK, -3), L.opsec_gpu_last_error(h)  # configuration parsed; -3: no device here
+        got = np.zeros(nb)
+        rc = L.opsec_gpu_get_params(h, got.ctypes.data_as(C.POINTER(C.c_double)))  # host only
+        L.opsec_gpu_destroy(h)
+        assert rc == api.OK
+        np.testing.assert_allclose(got, want, rtol=1e-13)
