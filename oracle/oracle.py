@@ -388,3 +388,120 @@ def subspace_sin(A, B):
     (rows orthonormal)."""
     s = np.linalg.svd(A @ B.T, compute_uv=False)
     return float(np.sqrt(max(0.0, 1.0 - min(s) ** 2)))
+
+
+# ---------------------------------------------------------------- full-sky shells at full size
+# On a full-sky spherical grid S depends on the two cells' arcs h = (i_r, j_mu) and on
+# |phi_a - phi_b| only (sig.cpp:150-207 keys it so), so S is block circulant in phi and its
+# eigenvectors are u_h * cos(2 pi m phi / N_phi) and u_h * sin(...) with u an eigenvector of the
+# arc-space matrix  S^(m)[h][g] = sum_d S[(h, 0), (g, d)] cos(2 pi m d / N_phi).
+# The restatement below runs klt.cpp:173-248 (top-M eigenpairs), comma-scalapack.cpp:228-252
+# (C_p = B^T S_p B) and estimate-mpi.cpp:480-546 (F, f, q) in that basis, in FP64, so that a
+# 32,768-cell build is checked without forming or diagonalising the 32,768^2 matrix.  It is the
+# same mathematics as the dense path (checked against it on small shells in tests/), not the
+# engine's algorithm: one FP64 eigh per order m over all arcs (no mu-parity split), FP64 GEMMs.
+def phi_basis(nphi):
+    """Orders m = 0..nphi/2, the cos / sin tables [phi][m] and the unit-norm scale per order."""
+    m = np.arange(nphi // 2 + 1)
+    ang = 2.0 * np.pi * np.outer(np.arange(nphi), m) / nphi
+    scale = np.where((m == 0) | (2 * m == nphi), 1.0 / np.sqrt(nphi), np.sqrt(2.0 / nphi))
+    return m, np.cos(ang), np.sin(ang), scale
+
+
+def azimuthal_blocks(srow, nphi):
+    """srow: [H][H * nphi], S[(h, phi=0), (g, d)] for every arc h (cell h * nphi) and cell (g, d).
+    Returns S^(m) [nm][H][H] (symmetrised)."""
+    H = srow.shape[0]
+    _, cosb, _, _ = phi_basis(nphi)
+    B = np.tensordot(srow.reshape(H, H, nphi), cosb, axes=([2], [0]))  # [h][g][m]
+    B = np.ascontiguousarray(np.moveaxis(B, 2, 0))
+    return 0.5 * (B + np.transpose(B, (0, 2, 1)))
+
+
+def klt_azimuthal(B0, nphi, nmodes):
+    """Top-nmodes eigenpairs of S from its order blocks.  Orders 0 < m < nphi/2 carry a cos and
+    a sin mode per block eigenvalue; the cos mode is ranked first (a cut inside such a pair
+    keeps the cos mode).  Returns the kept eigenvalues (descending) and, per (m, trig), the
+    block eigenvectors kept and their eigenvalues, and the largest eigenvalue left out."""
+    nm = B0.shape[0]
+    lam, mm, tt, ii, U = [], [], [], [], []
+    for m in range(nm):
+        w, V = np.linalg.eigh(B0[m])
+        U.append(V)
+        trigs = (0,) if (m == 0 or 2 * m == nphi) else (0, 1)
+        for t in trigs:
+            lam.append(w)
+            mm.append(np.full(w.size, m))
+            tt.append(np.full(w.size, t))
+            ii.append(np.arange(w.size))
+    lam, mm, tt, ii = (np.concatenate(a) for a in (lam, mm, tt, ii))
+    full = np.lexsort((ii, mm, tt, -lam))
+    order = full[:nmodes]
+    nxt = float(lam[full[nmodes]]) if full.size > nmodes else None
+    groups = {}
+    for m in range(nm):
+        for t in (0, 1):
+            sel = order[(mm[order] == m) & (tt[order] == t)]
+            if sel.size:
+                idx = ii[sel]
+                groups[(m, t)] = {"U": U[m][:, idx], "lam": lam[sel]}
+    return lam[order], groups, nxt
+
+
+def pixel_coefficients(x, H, nphi):
+    """X[h][m][trig] = sum_phi x[(h, phi)] * unit-norm cos / sin of order m."""
+    _, cosb, sinb, scale = phi_basis(nphi)
+    xs = x.reshape(H, nphi)
+    return np.stack([xs @ cosb * scale, xs @ sinb * scale], axis=2)
+
+
+def fisher_azimuthal(srow_of_table, nphi, nbands, nmodes, x, prior):
+    """F, f, q (estimate-mpi.cpp:480-546 at one rank) on the top-nmodes KL modes of a full-sky
+    shell.  srow_of_table(t): the [H][H * nphi] rows of S_t at phi = 0 (t = 0: xi, 1..nbands:
+    the band tables).  x: pixel values (N_a - Nbar_a)/sqrt(Nbar_a) per cell."""
+    B0 = srow_of_table(0)
+    H = B0.shape[0]
+    evals, groups, nxt = klt_azimuthal(azimuthal_blocks(B0, nphi), nphi, nmodes)
+    del B0
+    X = pixel_coefficients(np.asarray(x, dtype=np.float64), H, nphi)
+    keys = sorted(groups)
+    C = {g: np.zeros((nbands, groups[g]["U"].shape[1], groups[g]["U"].shape[1])) for g in keys}
+    for p in range(nbands):
+        Bp = azimuthal_blocks(srow_of_table(1 + p), nphi)
+        for (m, t) in keys:
+            U = groups[(m, t)]["U"]
+            if t == 1 and (m, 0) in groups and groups[(m, 0)]["U"].shape[1] >= U.shape[1]:
+                k = U.shape[1]  # the sin modes of an order are the first of its cos modes
+                C[(m, t)][p] = C[(m, 0)][p][:k, :k]
+                continue
+            C[(m, t)][p] = U.T @ Bp[m] @ U
+        del Bp
+    F = np.zeros((nbands, nbands))
+    f = np.zeros(nbands)
+    q = np.zeros(nbands)
+    for (m, t) in keys:
+        g = groups[(m, t)]
+        lam = g["lam"]
+        w = 1.0 / (1.0 + lam)
+        y = g["U"].T @ X[:, m, t]
+        Cg = C[(m, t)]
+        ww = np.outer(w, w)
+        Hg = (Cg * ww).reshape(nbands, -1)
+        F += 0.5 * Hg @ Cg.reshape(nbands, -1).T
+        R = np.diag(1.0 + lam) - np.tensordot(prior, Cg, axes=(0, 0))
+        f += 0.5 * Hg @ R.ravel()
+        wy = w * y
+        q += 0.5 * np.einsum("pij,i,j->p", Cg, wy, wy)
+    return {"evals": evals, "F": F, "f": f, "q": q, "groups": groups, "next_eval": nxt}
+
+
+def mode_projection_norms(modes, groups, H, nphi):
+    """For each row of modes [k][H * nphi] (unit vectors), the squared norm of its projection
+    onto the span of the kept azimuthal modes in groups."""
+    _, cosb, sinb, scale = phi_basis(nphi)
+    V = np.asarray(modes).reshape(-1, H, nphi)
+    coef = (np.tensordot(V, cosb, axes=([2], [0])) * scale, np.tensordot(V, sinb, axes=([2], [0])) * scale)
+    out = np.zeros(V.shape[0])
+    for (m, t), g in groups.items():
+        out += np.sum((coef[t][:, :, m] @ g["U"]) ** 2, axis=1)
+    return out

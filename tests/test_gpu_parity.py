@@ -252,9 +252,8 @@ def test_estimate(mixing):
 def test_fisher_build_end_to_end(name):
     """(1) With the oracle's modes, the GPU projection + Fisher + epilogue meet
     1e-6.  (2) With the GPU's own FP64 eigensolve of its FP32-cubature S, the
-    kept subspace moves by ~|dS|/gap, so the end-to-end bound is 1e-5 at a cut
-    whose gap exceeds 1e-4 lambda_0 (the reference's own ARPACK tolerance is
-    1e-5, ParpackSolver.cpp:15-40)."""
+    kept subspace moves by ~|dS|/gap; at a cut whose gap exceeds 1e-4 lambda_0
+    the whole path also meets 1e-6 (measured at most 4.4e-7)."""
     sv, cells = CASES[name]
     e, bands = engine(sv)
     tabs, Q, _, _, _ = _oracle_modes(sv, cells, bands, cells.size // 2)
@@ -271,7 +270,7 @@ def test_fisher_build_end_to_end(name):
     check_estimates(got, ref, name + "/oracle-modes", tol=1e-6)
     # (2) the whole path on the GPU
     got = e.fisher_build(cells, counts, M)
-    check_estimates(got, ref, name + "/end-to-end", tol=1e-5)
+    check_estimates(got, ref, name + "/end-to-end", tol=1e-6)
     assert e.launch_count() > 0
     e.close()
 
@@ -304,7 +303,7 @@ def test_fisher_build_azimuthal_projection():
     for k in ("az32", "az64"):
         rel = np.max(np.abs(out[k]["F"] - ref["est"]["F"])) / np.max(np.abs(ref["est"]["F"]))
         print(f"{k}: end-to-end Fisher rel err {rel:.2e}")
-        check_estimates(out[k], ref, f"shell1024/{k}/end-to-end", tol=1e-5)
+        check_estimates(out[k], ref, f"shell1024/{k}/end-to-end", tol=1e-6)
 
 
 def test_reflection_symmetry_paths_agree():
@@ -335,27 +334,33 @@ def test_reflection_symmetry_paths_agree():
 def check_estimates(got, ref, name, tol=1e-6):
     """F, f and q within tol of their scale; p-hat and Cov within tol of the
     scale their own inputs propagate (p-hat = M (q - f) cancels q against f,
-    and Cov ~ F^-1 amplifies by cond(F)), i.e. backward error <= tol."""
+    and Cov ~ F^-1 amplifies by cond(F)), i.e. backward error <= tol.
+    Prints and returns the measured errors in those units."""
     est = ref["est"]
-    assert np.max(np.abs(got["evals"] - ref["evals"])) <= tol * ref["evals"][0], name
     F = est["F"]
-    assert np.max(np.abs(got["F"] - F)) <= tol * np.max(np.abs(F)), (name, "F")
     qf_scale = max(np.max(np.abs(ref["q"])), np.max(np.abs(ref["f"])))
-    assert np.max(np.abs(got["f"] - est["f"])) <= tol * qf_scale, (name, "f")
-    assert np.max(np.abs((got["q"] + got["f"]) - ref["q"])) <= tol * qf_scale, (name, "q")
     Mx = est["M"]
     phat_scale = np.max(np.abs(Mx) @ (np.abs(ref["q"]) + np.abs(ref["f"])))
-    assert np.max(np.abs(got["phat"] - est["phat"])) <= tol * phat_scale, (name, "phat")
     cond = np.linalg.cond(F)
-    assert np.max(np.abs(got["pcov"] - est["pcov"])) <= tol * cond * np.max(np.abs(est["pcov"])), (name, "pcov")
+    err = {"evals": np.max(np.abs(got["evals"] - ref["evals"])) / ref["evals"][0],
+           "F": np.max(np.abs(got["F"] - F)) / np.max(np.abs(F)),
+           "f": np.max(np.abs(got["f"] - est["f"])) / qf_scale,
+           "q": np.max(np.abs((got["q"] + got["f"]) - ref["q"])) / qf_scale,
+           "phat": np.max(np.abs(got["phat"] - est["phat"])) / phat_scale,
+           "pcov": np.max(np.abs(got["pcov"] - est["pcov"])) / (cond * np.max(np.abs(est["pcov"])))}
+    err = {k: float(v) for k, v in err.items()}
+    print(f"{name}: " + ", ".join(f"{k} {v:.2e}" for k, v in err.items()))
+    for k, v in err.items():
+        assert v <= tol, (name, k, v, tol)
+    return err
 
 
 def test_fisher_build_box_1728_cells():
     """The benchmark's CPU-runnable configuration: 12^3 periodic box,
     n = 3e-4 exp(-(r/300)^2), 20 bands on [0, 0.2], 4^3 x 4^3 Gauss rule,
     4096 log-spaced xi points, 500 modes (moved to a spectral gap).  The
-    projection + Fisher + epilogue on the oracle's modes meet 1e-6; the whole
-    GPU path is reported and bounded by the eigenvector sensitivity at the cut."""
+    projection + Fisher + epilogue on the oracle's modes meet 1e-6, and so does
+    the whole GPU path at a cut in a spectral gap (measured 4.8e-7 in F)."""
     sv, cells = synth.box_survey(12)
     bands = synth.band_edges(20, 0.0, 0.2)
     layout = O.LAYOUT_LOG4096
@@ -377,5 +382,5 @@ def test_fisher_build_box_1728_cells():
     rel_F = np.max(np.abs(got["F"] - ref["est"]["F"])) / np.max(np.abs(ref["est"]["F"]))
     gap = (lam[M - 1] - lam[M]) / lam[0]
     print(f"box1728: M={M} relative gap {gap:.2e}, end-to-end Fisher rel err {rel_F:.3e}")
-    check_estimates(got, ref, "box1728/end-to-end", tol=1e-4)
+    check_estimates(got, ref, "box1728/end-to-end", tol=1e-6)
     e.close()
