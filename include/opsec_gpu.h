@@ -237,6 +237,25 @@ int opsec_gpu_ang2pix(opsec_gpu* ctx, long long nside, int nest, int n, const do
 int opsec_gpu_mock_counts(opsec_gpu* ctx, int ncells, const opsec_cell* cells, int ngrid, unsigned long long seed,
                           double bias, double* counts, double* delta);
 
+/* Failure handling.  The reference stops the whole job on any error (opsec_abort
+ * and MPI_Abort, opsec.c:88-116); here every call returns a status and leaves the
+ * context usable.  These two entry points exercise that without a GPU fault; they
+ * have no counterpart in the reference.
+ *
+ * opsec_gpu_fail_alloc: host-side fault injection.  With after >= 0 the device
+ * allocation after `after` more successful ones fails as if cudaMalloc had
+ * (OPSEC_ERR_NOMEM, message "... injected ..."); the call that meets it returns
+ * that status, forgets the context's cached device state, and the next call
+ * rebuilds it.  after = -1 switches injection off.
+ *
+ * opsec_gpu_wait_probe: the bounded mbarrier wait of the tensor-core projection
+ * kernels, run on a barrier that one thread completes after delay_cycles
+ * (arrive = 1) or that nothing completes (arrive = 0).  *timed_out = 1 when the
+ * wait gave up after limit_cycles; the kernel then returns normally (no copy is
+ * in flight), so the context stays usable.  Cycles in [1, 4e9]. */
+int opsec_gpu_fail_alloc(opsec_gpu* ctx, long long after);
+int opsec_gpu_wait_probe(opsec_gpu* ctx, long long limit_cycles, int arrive, long long delay_cycles, int* timed_out);
+
 /* Largest band count opsec_gpu_fisher_noalloc accepts. */
 #define OPSEC_NOALLOC_MAX_BANDS 64
 
@@ -256,13 +275,18 @@ int opsec_gpu_mock_counts(opsec_gpu* ctx, int ncells, const opsec_cell* cells, i
  * Scratch: one file-scope device array of 2.7 MB (152 x 2208 doubles) that
  * every GPU which loads this library holds until the process exits.  The
  * first call on a device, with that device current, looks up the array's
- * device address; make that first call before any stream capture.  Every call
- * shares the array and overwrites all of it that it reads, so no clearing is
- * needed -- but calls that overlap on the GPU (different streams, or
- * different host threads, running at once) race on it.
+ * device address (first calls from several host threads at once are safe);
+ * make that first call before any stream capture.  Every call shares the
+ * array and overwrites all of it that it reads, so no clearing is needed --
+ * but calls that overlap on the GPU (different streams, or different host
+ * threads, running at once) race on it.  The result equals the allocating
+ * path (opsec_gpu_estimate) within rounding, not bit for bit: the two sum
+ * their per-CTA partials over different CTA counts.
  *
  * Returns OPSEC_ERR_ARG for nbands > OPSEC_NOALLOC_MAX_BANDS (64), non-positive
- * sizes or null pointers, OPSEC_ERR_CUDA if a launch fails. */
+ * sizes or null pointers; OPSEC_ERR_CUDA, without launching, when a CUDA error
+ * is already pending on the calling thread (it is left for its owner), and
+ * when a launch fails. */
 int opsec_gpu_fisher_noalloc(int nmodes, int nbands, const float* cov_packed, const double* evals, const double* y,
                              const double* prior, double* out, void* stream);
 

@@ -19,6 +19,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libopsec_gpu.so")
 
 OK = 0
+ERR_ARG, ERR_CUDA, ERR_NOMEM = -2, -3, -4
 ERR = {-1: "CONFIG", -2: "ARG", -3: "CUDA", -4: "NOMEM", -5: "FILE", -6: "NUMERIC", -7: "STATE"}
 MIXING = {"inverse": 0, "inverse-sqrt": 1, "identity": 2}
 STAGES = ("xi_tables", "cubature", "eigensolve", "projection", "fisher")
@@ -74,6 +75,8 @@ def load():
     L.opsec_gpu_set_mask.argtypes = [vp, C.c_longlong, C.c_int, C.POINTER(C.c_float)]
     L.opsec_gpu_basis.argtypes = [vp, C.c_int, vp, ip]
     L.opsec_gpu_ang2pix.argtypes = [vp, C.c_longlong, C.c_int, C.c_int, dp, dp, C.POINTER(C.c_longlong)]
+    L.opsec_gpu_fail_alloc.argtypes = [vp, C.c_longlong]
+    L.opsec_gpu_wait_probe.argtypes = [vp, C.c_longlong, C.c_int, C.c_longlong, ip]
     _lib = L
     return L
 
@@ -378,6 +381,17 @@ class Engine:
         self._check(self._L.opsec_gpu_kernel_stats(self._h, name.encode(), C.byref(n), C.byref(ms), C.byref(fl),
                                                    C.byref(by)))
         return {"count": n.value, "ms": ms.value, "flops": fl.value, "bytes": by.value}
+
+    def fail_alloc(self, after):
+        """Host-side fault injection: the device allocation after `after` more fails (-1: off)."""
+        self._check(self._L.opsec_gpu_fail_alloc(self._h, C.c_longlong(after)))
+
+    def wait_probe(self, limit_cycles, arrive=False, delay_cycles=0):
+        """Run the projection kernels' bounded wait on a barrier; True when it timed out."""
+        out = C.c_int()
+        self._check(self._L.opsec_gpu_wait_probe(self._h, C.c_longlong(limit_cycles), int(bool(arrive)),
+                                                 C.c_longlong(delay_cycles), C.byref(out)))
+        return bool(out.value)
 
     def launch_count(self):
         return int(self._L.opsec_gpu_launch_count(self._h))

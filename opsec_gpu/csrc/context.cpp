@@ -5,6 +5,8 @@
 #include <cusolverDn.h>
 
 #include <algorithm>
+#include <cfloat>
+#include <functional>
 #include <array>
 #include <atomic>
 #include <chrono>
@@ -38,6 +40,7 @@ void launch_reverse_modes(int n, int m, int lda, const double* A, const double* 
 [[noreturn]] void fail(int code, const std::string& msg) { throw Error{code, msg}; }
 
 thread_local KernelClock* g_clock = nullptr;
+thread_local long long* g_fail_alloc = nullptr;
 
 void KernelClock::begin(const char* name, cudaStream_t s, double flops, double bytes) {
     if (!on) return;
@@ -96,6 +99,9 @@ void DevBuf<T>::alloc(size_t count) {
     if (count <= n && p) return;
     release();
     if (count == 0) return;
+    if (g_fail_alloc && *g_fail_alloc >= 0 && (*g_fail_alloc)-- == 0)
+        fail(OPSEC_ERR_NOMEM, "cudaMalloc of " + std::to_string(sizeof(T) * count) +
+                                  " bytes failed (injected by opsec_gpu_fail_alloc)");
     cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&p), sizeof(T) * count);
     if (e != cudaSuccess) {
         p = nullptr;
@@ -306,6 +312,8 @@ struct opsec_gpu {
     int mixing = OPSEC_MIXING_INVERSE;
     std::string projection = "auto";
     int proj_chunk = 1;
+    long long proj_wait = 2000000000LL;  // projection kernels: mbarrier wait bound in cycles
+    long long fail_alloc = -1;           // opsec_gpu_fail_alloc: device allocations left before one fails
     int cub_exact = 1;
     int az_gemm64 = 0;
     bool cub_reflect = true;
@@ -313,6 +321,7 @@ struct opsec_gpu {
     int win_key = 384, win_flush = 8, win_dot64 = 0;
     bool az_parity = true;
     bool az_batched = true;
+    bool az_own = true;     // the hand-written block eigensolver (blockeig.cu), else cuSOLVER
     int az_streams = 6;
     int az_split = 1;  // batched eigensolve calls in flight at once
     // the batched eigensolve as a CUDA graph, for builds that repeat the shapes and buffers
@@ -351,6 +360,9 @@ struct opsec_gpu {
     DevBuf<unsigned char> azws;  // azimuthal projection workspace
     DevBuf<double> nba_dev;      // Nbar per arc
     DevBuf<unsigned char> syev_ws;  // batched eigensolver workspace
+    DevBuf<double> bev_V, bev_T, bev_vec;  // hand-written block eigensolver: reflectors, T, vectors
+    DevBuf<int> bev_i;
+    DevBuf<int> probe;  // opsec_gpu_wait_probe's status word
     std::string cfg_text;        // the configuration the context was created with
     // learned far-field surrogate: 4 networks (FP32 master weights) and the target scale
     static constexpr int kMembers = 4;
@@ -425,15 +437,21 @@ void collect_clock(opsec_gpu* c) {
     c->clock.open.clear();
 }
 
+void forget_device_state(opsec_gpu* c);
+
 template <class F>
 int guard(opsec_gpu* ctx, F&& f) {
     if (!ctx) return OPSEC_ERR_ARG;
     struct ClockScope {
         opsec_gpu* c;
-        explicit ClockScope(opsec_gpu* cc) : c(cc) { g_clock = &cc->clock; }
+        explicit ClockScope(opsec_gpu* cc) : c(cc) {
+            g_clock = &cc->clock;
+            g_fail_alloc = &cc->fail_alloc;
+        }
         ~ClockScope() {
             collect_clock(c);
             g_clock = nullptr;
+            g_fail_alloc = nullptr;
         }
     } scope(ctx);
     try {
@@ -443,6 +461,7 @@ int guard(opsec_gpu* ctx, F&& f) {
         return OPSEC_OK;
     } catch (const Error& e) {
         ctx->err = e.msg;
+        if (e.code == OPSEC_ERR_NOMEM) forget_device_state(ctx);
         return e.code;
     } catch (const std::bad_alloc&) {
         ctx->err = "host allocation failed";
@@ -576,6 +595,13 @@ void configure(opsec_gpu* c, const std::map<std::string, std::string>& kv) {
     if (has("sig.gauss")) c->ng = to_int("sig.gauss", get("sig.gauss"));
     if (c->ng < 1 || c->ng > 6) fail(OPSEC_ERR_CONFIG, "sig.gauss must be between 1 and 6");
     if (has("projection")) c->projection = get("projection");
+    if (has("projection.wait_cycles")) {
+        const std::string& v = get("projection.wait_cycles");
+        char* end = nullptr;
+        c->proj_wait = std::strtoll(v.c_str(), &end, 10);
+        if (end == v.c_str() || c->proj_wait < 10000000LL)
+            fail(OPSEC_ERR_CONFIG, "projection.wait_cycles must be an integer >= 10000000");
+    }
     if (has("projection.chunk")) c->proj_chunk = to_int("projection.chunk", get("projection.chunk"));
     if (c->proj_chunk < 1) fail(OPSEC_ERR_CONFIG, "projection.chunk must be >= 1");
     if (has("azimuthal.gemm")) {
@@ -590,8 +616,10 @@ void configure(opsec_gpu* c, const std::map<std::string, std::string>& kv) {
     if (has("azimuthal.parity")) c->az_parity = get("azimuthal.parity") != "0";
     if (has("azimuthal.eig")) {
         const std::string& v = get("azimuthal.eig");
-        if (v != "streams" && v != "batched") fail(OPSEC_ERR_CONFIG, "azimuthal.eig must be streams or batched");
-        c->az_batched = v == "batched";
+        if (v != "own" && v != "streams" && v != "batched")
+            fail(OPSEC_ERR_CONFIG, "azimuthal.eig must be own, batched or streams");
+        c->az_own = v == "own";
+        c->az_batched = v != "streams";
     }
     if (has("klt.solver")) {
         c->eig_solver = get("klt.solver");
@@ -1179,6 +1207,106 @@ void drop_eig_graph(opsec_gpu* c) {
     c->eig_key = {};
 }
 
+// The hand-written block eigensolver (blockeig.cu) on the nblk blocks of order n in c->S:
+// every eigenvalue (ascending per block) into c->W, and the eigenvectors of the block
+// eigenvalues that can reach the global top-M cut as columns of c->S.  kc[b] = the number of
+// top eigenpairs of block b computed.  Returns false (and leaves a warning) when a check in the
+// kernels failed; the caller then solves the rebuilt blocks with the library.
+bool own_block_eigensolve(opsec_gpu* c, int n, int nblk, int npar, int Nphi, int M, std::vector<int>& kc) {
+    const size_t nn = (size_t)n * n;
+    c->bev_V.alloc((size_t)nblk * nn);
+    c->bev_T.alloc((size_t)nblk * (3 * n + 1));
+    double* tau = c->bev_T.p;
+    double* dg = tau + (size_t)nblk * n;
+    double* eg = dg + (size_t)nblk * n;
+    double* scale = eg + (size_t)nblk * n;
+    if (g_clock) g_clock->begin("blockeig_tridiag", c->stream, 4.0 / 3.0 * n * nn * nblk);
+    launch_blockeig_tridiag(n, nblk, c->S.p, c->bev_V.p, tau, dg, eg, c->stream, &c->launches);
+    if (g_clock) g_clock->end(c->stream);
+    launch_blockeig_spectrum(n, nblk, dg, eg, c->W.p, scale, c->stream, &c->launches);
+    std::vector<double> w((size_t)nblk * n), sc(nblk);
+    OPSEC_CUDA(cudaMemcpyAsync(w.data(), c->W.p, sizeof(double) * w.size(), cudaMemcpyDeviceToHost, c->stream));
+    OPSEC_CUDA(cudaMemcpyAsync(sc.data(), scale, sizeof(double) * nblk, cudaMemcpyDeviceToHost, c->stream));
+    sync(c);
+    // the M-th largest approximate eigenvalue, counting the (cos, sin) pairs of 0 < m < Nphi/2 twice
+    std::vector<double> all;
+    all.reserve((size_t)2 * nblk * n);
+    double smax = 0.0;
+    for (int b = 0; b < nblk; b++) {
+        const int m = b / npar, mult = (m == 0 || 2 * m == Nphi) ? 1 : 2;
+        smax = std::max(smax, sc[b]);
+        for (int j = 0; j < n; j++)
+            for (int k = 0; k < mult; k++) all.push_back(w[(size_t)b * n + j]);
+    }
+    const size_t mth = std::min(all.size(), (size_t)M) - 1;
+    std::nth_element(all.begin(), all.begin() + mth, all.end(), std::greater<double>());
+    // the FP32 bisection places every eigenvalue within ~4 eps32 of its block's scale; a
+    // candidate margin of 64 eps32 of the largest scale keeps every eigenvalue that can be
+    // among the top M once refined
+    const double cut = all[mth] - 64.0 * FLT_EPSILON * smax;
+    kc.assign(nblk, 0);
+    std::vector<int> koff(nblk);
+    int ktot = 0;
+    for (int b = 0; b < nblk; b++) {
+        int k = 0;
+        while (k < n && w[(size_t)b * n + n - 1 - k] >= cut) k++;
+        kc[b] = k;
+        koff[b] = ktot;
+        ktot += k;
+    }
+    c->eig_stats[1] = 1.0;
+    c->eig_stats[4] = ktot;
+    if (ktot == 0) return true;
+    c->bev_i.alloc((size_t)3 * nblk);
+    std::vector<int> hi(kc);
+    hi.insert(hi.end(), koff.begin(), koff.end());
+    OPSEC_CUDA(cudaMemcpyAsync(c->bev_i.p, hi.data(), sizeof(int) * 2 * nblk, cudaMemcpyHostToDevice, c->stream));
+    OPSEC_CUDA(cudaMemsetAsync(c->bev_i.p + 2 * nblk, 0, sizeof(int) * nblk, c->stream));
+    const size_t per = (size_t)n * ktot;
+    c->bev_vec.alloc(4 * per);
+    BlockEigVectors p{};
+    p.n = n;
+    p.nblk = nblk;
+    p.ktot = ktot;
+    p.kc = c->bev_i.p;
+    p.koff = c->bev_i.p + nblk;
+    p.status = c->bev_i.p + 2 * nblk;
+    p.dg = dg;
+    p.eg = eg;
+    p.scale = scale;
+    p.w = c->W.p;
+    p.Z = c->bev_vec.p;
+    p.L = p.Z + per;
+    p.U = p.L + per;
+    p.G = p.U + per;
+    p.V = c->bev_V.p;
+    p.tau = tau;
+    p.out = c->S.p;
+    if (g_clock) g_clock->begin("blockeig_vectors", c->stream, 2.0 * nn * ktot);
+    launch_blockeig_vectors(p, c->stream, &c->launches);
+    if (g_clock) g_clock->end(c->stream);
+    std::vector<int> st(nblk);
+    OPSEC_CUDA(cudaMemcpyAsync(st.data(), p.status, sizeof(int) * nblk, cudaMemcpyDeviceToHost, c->stream));
+    sync(c);
+    for (int b = 0; b < nblk; b++)
+        if (st[b]) {
+            c->warning = "block eigensolver check " + std::to_string(st[b]) + " failed on block " +
+                         std::to_string(b) + "; solved by cuSOLVER instead";
+            c->eig_stats[1] = 0.0;
+            return false;
+        }
+    return true;
+}
+
+// After a failed device allocation a buffer may have been released without being replaced:
+// nothing cached on the device is trusted, so the next call rebuilds what it needs.
+void forget_device_state(opsec_gpu* c) {
+    c->q_ok = c->qsq_ok = false;
+    if (!c->xi64.p || !c->xi32.p) c->tables_ok = false;
+    c->az_valid = false;
+    drop_eig_graph(c);
+}
+
 int eigensolve(opsec_gpu* c, int ncells, const opsec_cell* cells, int M) {
     build_q(c);
     load_cells(c, ncells, cells);
@@ -1211,127 +1339,134 @@ int eigensolve(opsec_gpu* c, int ncells, const opsec_cell* cells, int M) {
         launch_azimuthal_blocks(ks, c->Q.p, d_nba.p, nm, npar, c->S.p, c->stream, &c->launches);
         c->W.alloc((size_t)nblk * Hb);
         c->info.alloc(nblk);
-        int lwork = 0;
-        solver_check(cusolverDnDsyevd_bufferSize(c->solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, Hb,
-                                                 c->S.p, Hb, c->W.p, &lwork),
-                     "syevd_bufferSize");
-        bool batched_done = false;
-        if (c->az_batched) {
-            // Batched calls over the equal-size blocks, `azimuthal.split` of them on side
-            // streams at once (each is a chain of small launches, mostly latency); streams of
-            // single solves if a batched call is refused.
-            const int nsplit = std::max(1, std::min(c->az_split, nblk));
-            cusolverDnParams_t prm = nullptr;
-            solver_check(cusolverDnCreateParams(&prm), "cusolverDnCreateParams");
-            std::vector<cusolverDnHandle_t> hs(nsplit, c->solver);
-            if (nsplit > 1) {
-                for (int j = 0; j < nsplit; j++) {
-                    if (!c->side[j]) OPSEC_CUDA(cudaStreamCreateWithFlags(&c->side[j], cudaStreamNonBlocking));
-                    if (!c->side_solver[j]) solver_check(cusolverDnCreate(&c->side_solver[j]), "cusolverDnCreate");
-                    solver_check(cusolverDnSetStream(c->side_solver[j], c->side[j]), "cusolverDnSetStream");
-                    hs[j] = c->side_solver[j];
-                }
-                for (int j = 0; j <= nsplit; j++)
-                    if (!c->side_ev[j]) OPSEC_CUDA(cudaEventCreateWithFlags(&c->side_ev[j], cudaEventDisableTiming));
-            }
-            std::vector<int> b0(nsplit + 1);
-            for (int j = 0; j <= nsplit; j++) b0[j] = (int)((long long)j * nblk / nsplit);
-            std::vector<size_t> dbytes(nsplit, 0), hbytes(nsplit, 0), doff(nsplit + 1, 0);
-            cusolverStatus_t st = CUSOLVER_STATUS_SUCCESS;
-            for (int j = 0; j < nsplit && st == CUSOLVER_STATUS_SUCCESS; j++) {
-                st = cusolverDnXsyevBatched_bufferSize(hs[j], prm, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER,
-                                                       Hb, CUDA_R_64F, c->S.p + (size_t)b0[j] * Hb * Hb, Hb,
-                                                       CUDA_R_64F, c->W.p + (size_t)b0[j] * Hb, CUDA_R_64F,
-                                                       &dbytes[j], &hbytes[j], b0[j + 1] - b0[j]);
-                doff[j + 1] = doff[j] + ((std::max<size_t>(dbytes[j], 1) + 255) & ~size_t(255));
-            }
-            if (st == CUSOLVER_STATUS_SUCCESS) {
-                DevBuf<unsigned char>& dw = c->syev_ws;
-                dw.alloc(doff[nsplit]);
-                std::vector<std::vector<unsigned char>> hw(nsplit);
-                if (nsplit > 1) {
-                    OPSEC_CUDA(cudaEventRecord(c->side_ev[nsplit], c->stream));
-                    for (int j = 0; j < nsplit; j++) OPSEC_CUDA(cudaStreamWaitEvent(c->side[j], c->side_ev[nsplit], 0));
-                }
-                auto solve = [&](int j, std::vector<unsigned char>& host) {
-                    host.resize(std::max<size_t>(hbytes[j], 1));
-                    return cusolverDnXsyevBatched(hs[j], prm, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, Hb,
-                                                  CUDA_R_64F, c->S.p + (size_t)b0[j] * Hb * Hb, Hb, CUDA_R_64F,
-                                                  c->W.p + (size_t)b0[j] * Hb, CUDA_R_64F, dw.p + doff[j], dbytes[j],
-                                                  host.data(), hbytes[j], c->info.p + b0[j], b0[j + 1] - b0[j]);
-                };
-                // One call is a chain of thousands of small launches, bound by their host-side
-                // cost.  When a build repeats the previous one's shapes and buffers, the call is
-                // captured once into a CUDA graph and replayed; a capture the library refuses
-                // (a host synchronisation inside) falls back to the direct call for good.
-                const std::array<size_t, 6> key{(size_t)Hb, (size_t)nblk, (size_t)c->S.p, (size_t)c->W.p,
-                                                (size_t)c->info.p, (size_t)dw.p};
-                bool done = false;
-                if (nsplit == 1 && c->eig_graph_ok && key == c->eig_key) {
-                    if (!c->eig_exec) {
-                        cudaGraph_t g = nullptr;
-                        cudaError_t ce = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
-                        cusolverStatus_t cst = CUSOLVER_STATUS_INTERNAL_ERROR;
-                        if (ce == cudaSuccess) {
-                            cst = solve(0, c->eig_hw);  // kept while the graph lives: it may read it
-                            ce = cudaStreamEndCapture(c->stream, &g);
-                        }
-                        if (ce == cudaSuccess && cst == CUSOLVER_STATUS_SUCCESS && g)
-                            ce = cudaGraphInstantiate(&c->eig_exec, g, 0);
-                        if (g) cudaGraphDestroy(g);
-                        if (ce != cudaSuccess || cst != CUSOLVER_STATUS_SUCCESS) {
-                            (void)cudaGetLastError();
-                            c->eig_exec = nullptr;
-                            c->eig_graph_ok = false;
-                        }
-                    }
-                    if (c->eig_exec) {
-                        OPSEC_CUDA(cudaGraphLaunch(c->eig_exec, c->stream));
-                        done = true;
-                    }
-                }
-                if (!done) {
-                    if (key != c->eig_key) drop_eig_graph(c);
-                    for (int j = 0; j < nsplit && st == CUSOLVER_STATUS_SUCCESS; j++) st = solve(j, hw[j]);
-                    c->eig_key = key;
-                }
-                if (nsplit > 1)
-                    for (int j = 0; j < nsplit; j++) {
-                        OPSEC_CUDA(cudaEventRecord(c->side_ev[j], c->side[j]));
-                        OPSEC_CUDA(cudaStreamWaitEvent(c->stream, c->side_ev[j], 0));
-                    }
-                sync(c);
-            }
-            cusolverDnDestroyParams(prm);
-            batched_done = st == CUSOLVER_STATUS_SUCCESS;
-            if (!batched_done)  // the blocks may have been partly overwritten: rebuild them
+        std::vector<int> own_kc;
+        const bool own_try = c->az_own && blockeig_supported(Hb);
+        const bool own_done = own_try && own_block_eigensolve(c, Hb, nblk, npar, Nphi, M, own_kc);
+        if (!own_done) {
+            if (own_try)  // the reduction overwrote the blocks: rebuild them for the library solver
                 launch_azimuthal_blocks(ks, c->Q.p, d_nba.p, nm, npar, c->S.p, c->stream, &c->launches);
+            int lwork = 0;
+            solver_check(cusolverDnDsyevd_bufferSize(c->solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, Hb,
+                                                     c->S.p, Hb, c->W.p, &lwork),
+                         "syevd_bufferSize");
+            bool batched_done = false;
+            if (c->az_batched) {
+                // Batched calls over the equal-size blocks, `azimuthal.split` of them on side
+                // streams at once (each is a chain of small launches, mostly latency); streams of
+                // single solves if a batched call is refused.
+                const int nsplit = std::max(1, std::min(c->az_split, nblk));
+                cusolverDnParams_t prm = nullptr;
+                solver_check(cusolverDnCreateParams(&prm), "cusolverDnCreateParams");
+                std::vector<cusolverDnHandle_t> hs(nsplit, c->solver);
+                if (nsplit > 1) {
+                    for (int j = 0; j < nsplit; j++) {
+                        if (!c->side[j]) OPSEC_CUDA(cudaStreamCreateWithFlags(&c->side[j], cudaStreamNonBlocking));
+                        if (!c->side_solver[j]) solver_check(cusolverDnCreate(&c->side_solver[j]), "cusolverDnCreate");
+                        solver_check(cusolverDnSetStream(c->side_solver[j], c->side[j]), "cusolverDnSetStream");
+                        hs[j] = c->side_solver[j];
+                    }
+                    for (int j = 0; j <= nsplit; j++)
+                        if (!c->side_ev[j]) OPSEC_CUDA(cudaEventCreateWithFlags(&c->side_ev[j], cudaEventDisableTiming));
+                }
+                std::vector<int> b0(nsplit + 1);
+                for (int j = 0; j <= nsplit; j++) b0[j] = (int)((long long)j * nblk / nsplit);
+                std::vector<size_t> dbytes(nsplit, 0), hbytes(nsplit, 0), doff(nsplit + 1, 0);
+                cusolverStatus_t st = CUSOLVER_STATUS_SUCCESS;
+                for (int j = 0; j < nsplit && st == CUSOLVER_STATUS_SUCCESS; j++) {
+                    st = cusolverDnXsyevBatched_bufferSize(hs[j], prm, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER,
+                                                           Hb, CUDA_R_64F, c->S.p + (size_t)b0[j] * Hb * Hb, Hb,
+                                                           CUDA_R_64F, c->W.p + (size_t)b0[j] * Hb, CUDA_R_64F,
+                                                           &dbytes[j], &hbytes[j], b0[j + 1] - b0[j]);
+                    doff[j + 1] = doff[j] + ((std::max<size_t>(dbytes[j], 1) + 255) & ~size_t(255));
+                }
+                if (st == CUSOLVER_STATUS_SUCCESS) {
+                    DevBuf<unsigned char>& dw = c->syev_ws;
+                    dw.alloc(doff[nsplit]);
+                    std::vector<std::vector<unsigned char>> hw(nsplit);
+                    if (nsplit > 1) {
+                        OPSEC_CUDA(cudaEventRecord(c->side_ev[nsplit], c->stream));
+                        for (int j = 0; j < nsplit; j++) OPSEC_CUDA(cudaStreamWaitEvent(c->side[j], c->side_ev[nsplit], 0));
+                    }
+                    auto solve = [&](int j, std::vector<unsigned char>& host) {
+                        host.resize(std::max<size_t>(hbytes[j], 1));
+                        return cusolverDnXsyevBatched(hs[j], prm, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, Hb,
+                                                      CUDA_R_64F, c->S.p + (size_t)b0[j] * Hb * Hb, Hb, CUDA_R_64F,
+                                                      c->W.p + (size_t)b0[j] * Hb, CUDA_R_64F, dw.p + doff[j], dbytes[j],
+                                                      host.data(), hbytes[j], c->info.p + b0[j], b0[j + 1] - b0[j]);
+                    };
+                    // One call is a chain of thousands of small launches, bound by their host-side
+                    // cost.  When a build repeats the previous one's shapes and buffers, the call is
+                    // captured once into a CUDA graph and replayed; a capture the library refuses
+                    // (a host synchronisation inside) falls back to the direct call for good.
+                    const std::array<size_t, 6> key{(size_t)Hb, (size_t)nblk, (size_t)c->S.p, (size_t)c->W.p,
+                                                    (size_t)c->info.p, (size_t)dw.p};
+                    bool done = false;
+                    if (nsplit == 1 && c->eig_graph_ok && key == c->eig_key) {
+                        if (!c->eig_exec) {
+                            cudaGraph_t g = nullptr;
+                            cudaError_t ce = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
+                            cusolverStatus_t cst = CUSOLVER_STATUS_INTERNAL_ERROR;
+                            if (ce == cudaSuccess) {
+                                cst = solve(0, c->eig_hw);  // kept while the graph lives: it may read it
+                                ce = cudaStreamEndCapture(c->stream, &g);
+                            }
+                            if (ce == cudaSuccess && cst == CUSOLVER_STATUS_SUCCESS && g)
+                                ce = cudaGraphInstantiate(&c->eig_exec, g, 0);
+                            if (g) cudaGraphDestroy(g);
+                            if (ce != cudaSuccess || cst != CUSOLVER_STATUS_SUCCESS) {
+                                (void)cudaGetLastError();
+                                c->eig_exec = nullptr;
+                                c->eig_graph_ok = false;
+                            }
+                        }
+                        if (c->eig_exec) {
+                            OPSEC_CUDA(cudaGraphLaunch(c->eig_exec, c->stream));
+                            done = true;
+                        }
+                    }
+                    if (!done) {
+                        if (key != c->eig_key) drop_eig_graph(c);
+                        for (int j = 0; j < nsplit && st == CUSOLVER_STATUS_SUCCESS; j++) st = solve(j, hw[j]);
+                        c->eig_key = key;
+                    }
+                    if (nsplit > 1)
+                        for (int j = 0; j < nsplit; j++) {
+                            OPSEC_CUDA(cudaEventRecord(c->side_ev[j], c->side[j]));
+                            OPSEC_CUDA(cudaStreamWaitEvent(c->stream, c->side_ev[j], 0));
+                        }
+                    sync(c);
+                }
+                cusolverDnDestroyParams(prm);
+                batched_done = st == CUSOLVER_STATUS_SUCCESS;
+                if (!batched_done)  // the blocks may have been partly overwritten: rebuild them
+                    launch_azimuthal_blocks(ks, c->Q.p, d_nba.p, nm, npar, c->S.p, c->stream, &c->launches);
+            }
+            // the block eigenproblems are independent: spread them over side streams
+            const int ns = batched_done ? 0 : std::min(nblk, c->az_streams);
+            if (ns > 0) drop_eig_graph(c);
+            c->work.alloc((size_t)lwork * std::max(ns, 1));
+            for (int j = 0; j < ns; j++) {
+                if (!c->side[j]) OPSEC_CUDA(cudaStreamCreateWithFlags(&c->side[j], cudaStreamNonBlocking));
+                if (!c->side_solver[j]) solver_check(cusolverDnCreate(&c->side_solver[j]), "cusolverDnCreate");
+                solver_check(cusolverDnSetStream(c->side_solver[j], c->side[j]), "cusolverDnSetStream");
+            }
+            for (int j = 0; j <= ns; j++)
+                if (!c->side_ev[j]) OPSEC_CUDA(cudaEventCreateWithFlags(&c->side_ev[j], cudaEventDisableTiming));
+            OPSEC_CUDA(cudaEventRecord(c->side_ev[ns], c->stream));
+            for (int j = 0; j < ns; j++) OPSEC_CUDA(cudaStreamWaitEvent(c->side[j], c->side_ev[ns], 0));
+            for (int b = 0; b < nblk && ns > 0; b++) {
+                const int j = b % ns;
+                solver_check(cusolverDnDsyevd(c->side_solver[j], CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, Hb,
+                                              c->S.p + (size_t)b * Hb * Hb, Hb, c->W.p + (size_t)b * Hb,
+                                              c->work.p + (size_t)j * lwork, lwork, c->info.p + b),
+                             "syevd");
+            }
+            for (int j = 0; j < ns; j++) {
+                OPSEC_CUDA(cudaEventRecord(c->side_ev[j], c->side[j]));
+                OPSEC_CUDA(cudaStreamWaitEvent(c->stream, c->side_ev[j], 0));
+            }
+            check_info(c, nblk);
         }
-        // the block eigenproblems are independent: spread them over side streams
-        const int ns = batched_done ? 0 : std::min(nblk, c->az_streams);
-        if (ns > 0) drop_eig_graph(c);
-        c->work.alloc((size_t)lwork * std::max(ns, 1));
-        for (int j = 0; j < ns; j++) {
-            if (!c->side[j]) OPSEC_CUDA(cudaStreamCreateWithFlags(&c->side[j], cudaStreamNonBlocking));
-            if (!c->side_solver[j]) solver_check(cusolverDnCreate(&c->side_solver[j]), "cusolverDnCreate");
-            solver_check(cusolverDnSetStream(c->side_solver[j], c->side[j]), "cusolverDnSetStream");
-        }
-        for (int j = 0; j <= ns; j++)
-            if (!c->side_ev[j]) OPSEC_CUDA(cudaEventCreateWithFlags(&c->side_ev[j], cudaEventDisableTiming));
-        OPSEC_CUDA(cudaEventRecord(c->side_ev[ns], c->stream));
-        for (int j = 0; j < ns; j++) OPSEC_CUDA(cudaStreamWaitEvent(c->side[j], c->side_ev[ns], 0));
-        for (int b = 0; b < nblk && ns > 0; b++) {
-            const int j = b % ns;
-            solver_check(cusolverDnDsyevd(c->side_solver[j], CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, Hb,
-                                          c->S.p + (size_t)b * Hb * Hb, Hb, c->W.p + (size_t)b * Hb,
-                                          c->work.p + (size_t)j * lwork, lwork, c->info.p + b),
-                         "syevd");
-        }
-        for (int j = 0; j < ns; j++) {
-            OPSEC_CUDA(cudaEventRecord(c->side_ev[j], c->side[j]));
-            OPSEC_CUDA(cudaStreamWaitEvent(c->stream, c->side_ev[j], 0));
-        }
-        check_info(c, nblk);
         std::vector<double> w((size_t)nblk * Hb);
         OPSEC_CUDA(cudaMemcpyAsync(w.data(), c->W.p, sizeof(double) * w.size(), cudaMemcpyDeviceToHost, c->stream));
         sync(c);
@@ -1368,6 +1503,8 @@ int eigensolve(opsec_gpu* c, int ncells, const opsec_cell* cells, int M) {
         std::vector<int> sel((size_t)3 * M);
         std::vector<double> ev(M);
         for (int i = 0; i < M; i++) {
+            if (own_done && ent[i].idx < Hb - own_kc[ent[i].b])
+                fail(OPSEC_ERR_NUMERIC, "block eigensolver: a selected eigenpair lies outside the candidates");
             sel[i] = ent[i].b;
             sel[M + i] = ent[i].idx;
             sel[2 * M + i] = ent[i].kind;
@@ -1674,6 +1811,7 @@ void project_all(opsec_gpu* c, int ncells, int M, bool own_modes, bool packed = 
     a.Bs = c->Bs.p;
     a.Dp = c->Dp.p;
     a.chunk = c->proj_chunk;
+    a.wait_cycles = c->proj_wait;
     bool tc = (c->projection != "simt") && project_tc_supported(a);
     if (c->projection == "tc" && !tc) fail(OPSEC_ERR_CONFIG, "projection=tc requested but the shape is not supported");
     size_t wb = tc ? project_tc_work_bytes(a) : sizeof(float) * (size_t)M * ncells;
@@ -2439,6 +2577,27 @@ int opsec_gpu_eig_stats(const opsec_gpu* c, double* stats) {
     if (!c || !stats) return OPSEC_ERR_ARG;
     std::copy(c->eig_stats, c->eig_stats + 10, stats);
     return OPSEC_OK;
+}
+
+int opsec_gpu_fail_alloc(opsec_gpu* c, long long after) {
+    if (!c || after < -1) return OPSEC_ERR_ARG;
+    c->fail_alloc = after;
+    return OPSEC_OK;
+}
+
+int opsec_gpu_wait_probe(opsec_gpu* c, long long limit_cycles, int arrive, long long delay_cycles, int* timed_out) {
+    return guard(c, [&] {
+        if (!timed_out) fail(OPSEC_ERR_ARG, "null output");
+        if (limit_cycles < 1 || limit_cycles > 4000000000LL || delay_cycles < 0 || delay_cycles > 4000000000LL)
+            fail(OPSEC_ERR_ARG, "wait probe: cycles must be in [1, 4e9]");
+        c->probe.alloc(1);
+        OPSEC_CUDA(cudaMemsetAsync(c->probe.p, 0, sizeof(int), c->stream));
+        launch_wait_probe(limit_cycles, arrive ? 1 : 0, delay_cycles, c->probe.p, c->stream, &c->launches);
+        int h = 0;
+        OPSEC_CUDA(cudaMemcpyAsync(&h, c->probe.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+        sync(c);
+        *timed_out = h;
+    });
 }
 
 int opsec_gpu_kernel_stats(const opsec_gpu* c, const char* name, long long* count, double* total_ms, double* flops,

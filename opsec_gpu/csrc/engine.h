@@ -93,6 +93,9 @@ struct KernelClock {
     void end(cudaStream_t s);
 };
 extern thread_local KernelClock* g_clock;  // set by the context around its calls
+// Host-side fault injection: when >= 0, the device allocation after that many more fails as if
+// cudaMalloc had (set by the context around its calls; -1 = off).
+extern thread_local long long* g_fail_alloc;
 
 // ------------------------------------------------------------- kernels
 struct CubatureArgs {
@@ -182,6 +185,31 @@ void launch_azimuthal_scatter(int M, int nbands, const int* mode_m, const int* m
 void launch_assemble_modes(int H, int Nphi, int Nmu, int npar, int nmodes, const int* sel_b, const int* sel_idx,
                            const int* sel_kind, const double* U, double* modes, cudaStream_t st, long long* launches);
 
+// Hand-written batched symmetric eigensolver of equal-size blocks (blockeig.cu): Householder
+// tridiagonalisation (column-major blocks, lower triangle; the blocks are overwritten), every
+// eigenvalue to ~1e-6 of the block scale, then FP64 eigenpairs of the top kc[b] of each block
+// written as columns n-1-c of out (ascending order, as LAPACK's syevd).
+bool blockeig_supported(int n);
+void launch_blockeig_tridiag(int n, int nblk, double* A, double* V, double* tau, double* dg, double* eg,
+                             cudaStream_t s, long long* launches);
+void launch_blockeig_spectrum(int n, int nblk, const double* dg, const double* eg, double* w, double* scale,
+                              cudaStream_t s, long long* launches);
+struct BlockEigVectors {
+    int n, nblk, ktot;
+    const int* kc;        // [nblk] candidates per block
+    const int* koff;      // [nblk] prefix sums of kc
+    const double* dg;     // [nblk][n] diagonal of T
+    const double* eg;     // [nblk][n] off-diagonal of T
+    const double* scale;  // [nblk] power-of-two scale
+    double* w;            // [nblk][n] eigenvalues, ascending (candidates refined in place)
+    double *Z, *L, *U, *G;  // [n][ktot] each
+    int* status;          // [nblk], zeroed by the caller
+    const double* V;      // [nblk][n][n] reflectors
+    const double* tau;    // [nblk][n]
+    double* out;          // [nblk][n][n] eigenvector columns
+};
+void launch_blockeig_vectors(const BlockEigVectors& p, cudaStream_t s, long long* launches);
+
 // Projection C_p = B'^T Q_p B' for all bands; B' = diag(sqrt Nbar) B.
 struct ProjectArgs {
     KeySpace ks;
@@ -195,8 +223,12 @@ struct ProjectArgs {
     void* work;            // scratch
     size_t work_bytes;
     int chunk = 1;         // tensor-core path: K-slices of 64 per FP32 accumulator chunk
+    long long wait_cycles = 2000000000LL;  // bound of every mbarrier wait (~1 s at 2 GHz)
 };
 size_t project_work_bytes(const ProjectArgs& a);
+// The projection kernels' bounded mbarrier wait on a barrier that nothing (arrive = 0) or one
+// thread after `delay` cycles (arrive = 1) completes; *err (device) is raised on a timeout.
+void launch_wait_probe(long long limit, int arrive, long long delay, int* err, cudaStream_t s, long long* launches);
 void launch_project(const ProjectArgs& a, cudaStream_t s, long long* launches);
 
 // ------------------------------------------------------------- learned far-field surrogate

@@ -15,6 +15,7 @@
 // summed over the slice and FP64 across chunks; slices and per-CTA partials
 // are reduced in a fixed order, so reruns are bit-identical.
 #include <cmath>
+#include <mutex>
 
 #include "engine.h"
 
@@ -266,6 +267,8 @@ __global__ void __launch_bounds__(kMaxThreads) fisher_kernel(Src src, int nb, co
 #pragma unroll
             for (int b = 0; b < kTile; b++) red[(size_t)me * kTile * kTile + a * kTile + b] = acc[a][b];
     __syncthreads();
+    // Every CTA writes all nout outputs of its slot, zeros included when it had no chunk: the
+    // no-allocation entry point keeps its partials in a shared array that it never clears.
     if (me < tl.ntiles) {
         for (int e = 0; e < kTile * kTile; e++) {
             const int o = out_index(I * kTile + e / kTile, J * kTile + e % kTile, nb);
@@ -559,7 +562,31 @@ static __device__ __align__(256) double g_noalloc_partial[kNoallocBlocks * kNoal
 
 constexpr int kMaxDevices = 64;
 double* g_partial_addr[kMaxDevices] = {nullptr};
-bool g_attr_done[kMaxDevices] = {false};
+int g_setup_rc[kMaxDevices] = {0};
+std::once_flag g_setup_once[kMaxDevices];
+
+// Once per device, with that device current: the device address of the scratch array and the
+// kernel's shared-memory limit.  std::call_once makes concurrent first calls from several host
+// threads safe; a failed set-up is not retried.
+int noalloc_setup(int dev) {
+    std::call_once(g_setup_once[dev], [dev] {
+        void* p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_noalloc_partial) != cudaSuccess || !p) {
+            g_setup_rc[dev] = OPSEC_ERR_CUDA;
+            return;
+        }
+        size_t most = 0;  // the largest request of any band count this entry point accepts
+        for (int n = 1; n <= kNoallocMaxBands; n++) most = fisher_tiling(n).smem > most ? fisher_tiling(n).smem : most;
+        if (cudaFuncSetAttribute(fisher_kernel<PackedSource<float>>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)most) != cudaSuccess) {
+            g_setup_rc[dev] = OPSEC_ERR_CUDA;
+            return;
+        }
+        g_partial_addr[dev] = static_cast<double*>(p);
+        g_setup_rc[dev] = OPSEC_OK;
+    });
+    return g_setup_rc[dev];
+}
 
 }  // namespace
 
@@ -570,30 +597,22 @@ extern "C" int opsec_gpu_fisher_noalloc(int nmodes, int nbands, const float* cov
     using namespace opsec;
     if (nmodes <= 0 || nbands <= 0 || !cov_packed || !evals || !y || !prior || !out) return OPSEC_ERR_ARG;
     if (nbands > kNoallocMaxBands) return OPSEC_ERR_ARG;  // scratch holds at most 64 bands
+    // an error left pending by the caller's own launches is not taken for this call's
+    if (cudaPeekAtLastError() != cudaSuccess) return OPSEC_ERR_CUDA;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return OPSEC_ERR_CUDA;
-    // once per device, with that device current: the device address of the scratch array
-    if (!g_partial_addr[dev]) {
-        void* p = nullptr;
-        if (cudaGetSymbolAddress(&p, g_noalloc_partial) != cudaSuccess || !p) return OPSEC_ERR_CUDA;
-        g_partial_addr[dev] = static_cast<double*>(p);
-    }
+    const int rc = noalloc_setup(dev);
+    if (rc != OPSEC_OK) return rc;
     const int nb = nbands;
     const int nout = nb * (nb + 1) / 2 + 2 * nb;
     const FisherTiling tl = fisher_tiling(nb);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    if (!g_attr_done[dev]) {
-        size_t most = 0;  // the largest request of any band count this entry point accepts
-        for (int n = 1; n <= kNoallocMaxBands; n++) most = fisher_tiling(n).smem > most ? fisher_tiling(n).smem : most;
-        if (cudaFuncSetAttribute(fisher_kernel<PackedSource<float>>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)most) != cudaSuccess)
-            return OPSEC_ERR_CUDA;
-        g_attr_done[dev] = true;
-    }
-    // every CTA writes all nout partials of its slot, so nothing needs clearing
-    const PackedSource<float> src{cov_packed, (long long)nmodes * (nmodes + 1) / 2};
-    fisher_kernel<PackedSource<float>><<<kNoallocBlocks, tl.threads, tl.smem, s>>>(src, nb, evals, y, prior,
-                                                                                   g_partial_addr[dev]);
-    fisher_reduce_kernel<<<(nout + 255) / 256, 256, 0, s>>>(nb, kNoallocBlocks, g_partial_addr[dev], out);
+    const long long K = (long long)nmodes * (nmodes + 1) / 2;
+    const int nblocks = fisher_blocks_for(K) < kNoallocBlocks ? fisher_blocks_for(K) : kNoallocBlocks;
+    const PackedSource<float> src{cov_packed, K};
+    fisher_kernel<PackedSource<float>><<<nblocks, tl.threads, tl.smem, s>>>(src, nb, evals, y, prior,
+                                                                            g_partial_addr[dev]);
+    if (cudaGetLastError() != cudaSuccess) return OPSEC_ERR_CUDA;  // the reduction would read stale partials
+    fisher_reduce_kernel<<<(nout + 255) / 256, 256, 0, s>>>(nb, nblocks, g_partial_addr[dev], out);
     return cudaGetLastError() == cudaSuccess ? OPSEC_OK : OPSEC_ERR_CUDA;
 }

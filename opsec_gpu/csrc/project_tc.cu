@@ -39,7 +39,6 @@ constexpr uint32_t A_BYTES = BM * BK * 2;  // one FP16 operand tile, 16 KB
 constexpr uint32_t B_BYTES = BN * BK * 2;  // 32 KB
 constexpr uint32_t STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
 constexpr int TMEM_COLS = 512;  // [0,256) accumulator D, [256,512) running sum R
-constexpr long long kWaitCycles = 2000000000LL;  // ~1 s at 2 GHz
 
 // instruction descriptor: D=F32, A=B=F16, both K-major, M=128, N=256
 constexpr uint32_t kIdesc = (1u << 4) | (0u << 7) | (0u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
@@ -67,14 +66,15 @@ __device__ __forceinline__ bool mbar_try(uint32_t a, uint32_t parity) {
 }
 
 // Bounded wait.  Returns false (and raises the CTA's abort flag and the
-// global error word) when the barrier does not complete in time.
-__device__ __forceinline__ bool mbar_wait(uint32_t a, uint32_t parity, volatile int* abort_flag, int* err) {
+// global error word) when the barrier does not complete within `limit` cycles.
+__device__ __forceinline__ bool mbar_wait(uint32_t a, uint32_t parity, volatile int* abort_flag, int* err,
+                                          long long limit) {
     if (mbar_try(a, parity)) return true;
     const long long t0 = clock64();
     while (true) {
         if (mbar_try(a, parity)) return true;
         if (*abort_flag) return false;
-        if (clock64() - t0 > kWaitCycles) {
+        if (clock64() - t0 > limit) {
             *abort_flag = 1;
             atomicExch(err, 1);
             return false;
@@ -162,6 +162,7 @@ __device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.
 struct ChunkBars {
     uint32_t chunk_done;  // MMA -> drain warps (tcgen05.commit)
     uint32_t drained;     // drain warps -> MMA (4 arrivals)
+    long long wait_cycles;
 };
 
 template <class Store>
@@ -169,7 +170,7 @@ __device__ __forceinline__ void drain_loop(uint32_t tmem, int q, int lane, int n
                                            volatile int* abort_flag, int* err, Store store) {
     const uint32_t lane_base = (uint32_t)(32 * q) << 16;
     for (int c = 0; c < nchunks; c++) {
-        if (!mbar_wait(b.chunk_done, c & 1, abort_flag, err)) return;
+        if (!mbar_wait(b.chunk_done, c & 1, abort_flag, err, b.wait_cycles)) return;
         tc_fence_after();
         const bool last = (c == nchunks - 1);
         for (int cc = 0; cc < 8; cc++) {
@@ -239,6 +240,7 @@ struct Step1Params {
     float* Tf;                // [Mpad][Npad] T^T, FP32
     int chunk;                // K-slices per accumulator chunk
     int* err;
+    long long wait_cycles;  // bound of every mbarrier wait
 };
 
 __device__ __forceinline__ int pair_key(const KeySpace& ks, int4 a, int4 b) {
@@ -295,7 +297,7 @@ __global__ void __launch_bounds__(512, 1)
         if (lane == 0) {
             for (int k = 0; k < nk; k++) {
                 const int s = k % STAGES, n = k / STAGES;
-                if (n > 0 && !mbar_wait(smem_u32(&bar_empty[s]), (n - 1) & 1, &abort_flag, p.err)) break;
+                if (n > 0 && !mbar_wait(smem_u32(&bar_empty[s]), (n - 1) & 1, &abort_flag, p.err, p.wait_cycles)) break;
                 const uint32_t fb = smem_u32(&bar_full[s]);
                 mbar_arrive_tx(fb, 2 * B_BYTES);
                 tma_load_2d(smem_u32(B_hi(s)), &mBh, fb, k * BK, j0);
@@ -308,9 +310,9 @@ __global__ void __launch_bounds__(512, 1)
             const int s = k % STAGES, n = k / STAGES;
             const bool first = (k % chunk) == 0;
             if (first && k > 0) {  // the previous chunk's accumulator must be drained first
-                if (!mbar_wait(smem_u32(&bar_drained), ((k / chunk) - 1) & 1, &abort_flag, p.err)) break;
+                if (!mbar_wait(smem_u32(&bar_drained), ((k / chunk) - 1) & 1, &abort_flag, p.err, p.wait_cycles)) break;
             }
-            if (!mbar_wait(smem_u32(&bar_full[s]), n & 1, &abort_flag, p.err)) break;
+            if (!mbar_wait(smem_u32(&bar_full[s]), n & 1, &abort_flag, p.err, p.wait_cycles)) break;
             tc_fence_after();
             if (lane == 0) {
                 issue_slice(tmem, sdesc(smem_u32(A_hi(s))), sdesc(smem_u32(A_lo(s))), sdesc(smem_u32(B_hi(s))),
@@ -324,7 +326,7 @@ __global__ void __launch_bounds__(512, 1)
         // drain warps + epilogue: T^T[j][a] in natural units
         const int q = warp & 3;
         const int a = a0 + 32 * q + lane;
-        drain_loop(tmem, q, lane, nchunks, ChunkBars{smem_u32(&bar_chunk), smem_u32(&bar_drained)}, &abort_flag,
+        drain_loop(tmem, q, lane, nchunks, ChunkBars{smem_u32(&bar_chunk), smem_u32(&bar_drained), p.wait_cycles}, &abort_flag,
                    p.err, [&](int cc, const float* v) {
 #pragma unroll
                        for (int t = 0; t < 32; t++) p.Tf[(size_t)(j0 + 32 * cc + t) * p.Npad + a] = v[t] * p.out_scale;
@@ -348,7 +350,7 @@ __global__ void __launch_bounds__(512, 1)
         if (nk > 0) gather(0);
         for (int k = 0; k < nk; k++) {
             const int s = k % STAGES, n = k / STAGES;
-            if (n > 0 && !mbar_wait(smem_u32(&bar_empty[s]), (n - 1) & 1, &abort_flag, p.err)) break;
+            if (n > 0 && !mbar_wait(smem_u32(&bar_empty[s]), (n - 1) & 1, &abort_flag, p.err, p.wait_cycles)) break;
             unsigned char* ahi = A_hi(s);
             unsigned char* alo = A_lo(s);
 #pragma unroll
@@ -381,6 +383,7 @@ struct Step2Params {
     float* Dp;          // packed output of this band
     int chunk;          // K-slices per accumulator chunk
     int* err;
+    long long wait_cycles;  // bound of every mbarrier wait
 };
 
 __global__ void __launch_bounds__(256, 1)
@@ -424,7 +427,7 @@ __global__ void __launch_bounds__(256, 1)
         if (lane == 0) {
             for (int k = 0; k < nk; k++) {
                 const int s = k % STAGES, n = k / STAGES;
-                if (n > 0 && !mbar_wait(smem_u32(&bar_empty[s]), (n - 1) & 1, &abort_flag, p.err)) break;
+                if (n > 0 && !mbar_wait(smem_u32(&bar_empty[s]), (n - 1) & 1, &abort_flag, p.err, p.wait_cycles)) break;
                 const uint32_t fb = smem_u32(&bar_full[s]);
                 mbar_arrive_tx(fb, STAGE_BYTES);
                 tma_load_2d(smem_u32(A_hi(s)), &mAh, fb, k * BK, i0);
@@ -438,9 +441,9 @@ __global__ void __launch_bounds__(256, 1)
             const int s = k % STAGES, n = k / STAGES;
             const bool first = (k % chunk) == 0;
             if (first && k > 0) {
-                if (!mbar_wait(smem_u32(&bar_drained), ((k / chunk) - 1) & 1, &abort_flag, p.err)) break;
+                if (!mbar_wait(smem_u32(&bar_drained), ((k / chunk) - 1) & 1, &abort_flag, p.err, p.wait_cycles)) break;
             }
-            if (!mbar_wait(smem_u32(&bar_full[s]), n & 1, &abort_flag, p.err)) break;
+            if (!mbar_wait(smem_u32(&bar_full[s]), n & 1, &abort_flag, p.err, p.wait_cycles)) break;
             tc_fence_after();
             if (lane == 0) {
                 issue_slice(tmem, sdesc(smem_u32(A_hi(s))), sdesc(smem_u32(A_lo(s))), sdesc(smem_u32(B_hi(s))),
@@ -454,7 +457,7 @@ __global__ void __launch_bounds__(256, 1)
         const int q = warp & 3;
         const float out_scale = 1.0f / (p.sB * pow2_scale(__uint_as_float(*p.maxT)));
         const int i = i0 + 32 * q + lane;
-        drain_loop(tmem, q, lane, nchunks, ChunkBars{smem_u32(&bar_chunk), smem_u32(&bar_drained)}, &abort_flag,
+        drain_loop(tmem, q, lane, nchunks, ChunkBars{smem_u32(&bar_chunk), smem_u32(&bar_drained), p.wait_cycles}, &abort_flag,
                    p.err, [&](int cc, const float* v) {
 #pragma unroll
                        for (int t = 0; t < 32; t++) {
@@ -472,6 +475,29 @@ __global__ void __launch_bounds__(256, 1)
 }
 
 // ---------------------------------------------------------------- helpers
+// Self-check of the bounded wait used by the projection kernels: an mbarrier that expects one
+// arrival.  arrive = 1: a thread of the second warp arrives after `delay` cycles; arrive = 0:
+// nothing arrives and the wait gives up after `limit` cycles, raising *err.  No copy or MMA is
+// in flight, so the kernel simply returns either way.
+__global__ void wait_probe_kernel(long long limit, int arrive, long long delay, int* err) {
+    __shared__ __align__(8) unsigned long long bar;
+    __shared__ volatile int abort_flag;
+    if (threadIdx.x == 0) {
+        abort_flag = 0;
+        mbar_init(smem_u32(&bar), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 32 && arrive) {
+        const long long t0 = clock64();
+        while (clock64() - t0 < delay) {
+        }
+        mbar_arrive(smem_u32(&bar));
+    }
+    if (threadIdx.x == 0) mbar_wait(smem_u32(&bar), 0, &abort_flag, err, limit);
+    __syncthreads();
+}
+
 __global__ void cell_keys_kernel(KeySpace ks, int N, int Npad, const int* h, const int* f, const int* g, int4* out) {
     for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < Npad; a += gridDim.x * blockDim.x) {
         int4 k = make_int4(0, 0, 0, 0);
@@ -678,6 +704,7 @@ void launch_project_tc(const ProjectArgs& a, cudaStream_t s, long long* launches
         p1.Tf = Tf;
         p1.chunk = a.chunk;
         p1.err = err;
+        p1.wait_cycles = a.wait_cycles;
         if (g_clock) g_clock->begin("project_step1", s, 2.0 * N * (double)N * M);
         step1_kernel<<<n_at * n_jt, 512, smem, s>>>(mBh256, mBl256, p1);
         OPSEC_CUDA(cudaGetLastError());
@@ -694,6 +721,7 @@ void launch_project_tc(const ProjectArgs& a, cudaStream_t s, long long* launches
         p2.chunk = a.chunk;
         p2.Dp = a.Dp + (size_t)p * ((size_t)M * (M + 1) / 2);
         p2.err = err;
+        p2.wait_cycles = a.wait_cycles;
         if (g_clock) g_clock->begin("project_step2", s, (double)N * M * (double)(M + 1));
         step2_kernel<<<(unsigned)tl.size(), 256, smem, s>>>(mBh128, mBl128, mTh256, mTl256, p2);
         OPSEC_CUDA(cudaGetLastError());
@@ -704,6 +732,12 @@ void launch_project_tc(const ProjectArgs& a, cudaStream_t s, long long* launches
     OPSEC_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, s));
     OPSEC_CUDA(cudaStreamSynchronize(s));
     if (herr) fail(OPSEC_ERR_CUDA, "tensor-core projection timed out waiting on a pipeline barrier");
+}
+
+void launch_wait_probe(long long limit, int arrive, long long delay, int* err, cudaStream_t s, long long* launches) {
+    wait_probe_kernel<<<1, 64, 0, s>>>(limit, arrive, delay, err);
+    OPSEC_CUDA(cudaGetLastError());
+    ++*launches;
 }
 
 }  // namespace opsec

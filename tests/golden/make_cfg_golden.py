@@ -2,7 +2,7 @@
 
 Run where the reference checkout is present (it is absent on GPU hosts):
 
-    make -C oracle ref            # builds oracle/_ref/libopsecref.so
+    make -C oracle ref REF=<checkout>/code/opsec/src   # builds oracle/_ref/libopsecref.so
     python tests/golden/make_cfg_golden.py
 
 Each case is a configuration text, read with cfg_read_file (cfg.c:200-232; opsec_init

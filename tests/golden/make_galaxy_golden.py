@@ -2,7 +2,7 @@
 
 Run where the reference checkout is present (it is absent on GPU hosts):
 
-    make -C oracle ref            # builds oracle/_ref/libopsecref.so
+    make -C oracle ref REF=<checkout>/code/opsec/src   # builds oracle/_ref/libopsecref.so
     python tests/golden/make_galaxy_golden.py
 
 The library is the reference's unmodified sources plus oracle/ref_shim.cpp,

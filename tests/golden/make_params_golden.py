@@ -2,7 +2,7 @@
 
 Run where the reference checkout is present (it is absent on GPU hosts):
 
-    make -C oracle ref            # builds oracle/_ref/libopsecref.so
+    make -C oracle ref REF=<checkout>/code/opsec/src   # builds oracle/_ref/libopsecref.so
     python tests/golden/make_params_golden.py
 
 P(k) is the benchmark spectrum tabulated as a pkfile (opsec_gpu.synth.write_pkfile, 17

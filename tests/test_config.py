@@ -48,6 +48,9 @@ BAD = [
     ("basis.samples = 0", "basis.samples"),
     ("xi.n1 = 0", "xi table layout"),
     ("projection.chunk = 0", "projection.chunk"),
+    ("projection.wait_cycles = 1000", "projection.wait_cycles"),
+    ("projection.wait_cycles = soon", "projection.wait_cycles"),
+    ("azimuthal.eig = lapack", "azimuthal.eig"),
 ]
 
 
@@ -66,7 +69,8 @@ def test_survey_type_is_required(create):
 def test_valid_configurations_pass_the_parser(create, coordsys):
     text = _base(coordsys)
     for extra in ("", "klt.solver = chfsi\nklt.gemm = f32\nklt.degree = 6\n", "mixing = inverse-sqrt\n",
-                  "solver = parpack\n"):
+                  "solver = parpack\n", "azimuthal.eig = own\nprojection.wait_cycles = 20000000\n",
+                  "azimuthal.eig = batched\n"):
         rc, msg = create(text + extra)
         assert rc in (api.OK, -3), (rc, msg)  # -3: OPSEC_ERR_CUDA, no device on this host
 

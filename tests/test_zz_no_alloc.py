@@ -25,7 +25,9 @@ def _dev_ptr(t):
     return C.c_void_p(t.data_ptr())
 
 
-def test_fisher_noalloc_matches_allocating_path():
+@pytest.mark.parametrize("nb", [1, 6, 64])
+def test_fisher_noalloc_matches_allocating_path(nb):
+    """nb = 64 is the limit: the largest shared-memory request and partial stride."""
     import torch
 
     torch.cuda.init()
@@ -33,7 +35,7 @@ def test_fisher_noalloc_matches_allocating_path():
     L.opsec_gpu_fisher_noalloc.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                            C.c_void_p, C.c_void_p]
     rng = np.random.default_rng(3)
-    M, nb = 96, 6
+    M = 96
     K = M * (M + 1) // 2
     evals = np.ascontiguousarray(np.sort(rng.uniform(0.05, 4.0, M))[::-1])
     cov32 = np.stack([O.pack_upper((lambda A: A @ A.T / M)(rng.standard_normal((M, M)))) for _ in range(nb)]).astype(
