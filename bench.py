@@ -580,7 +580,8 @@ def main():
 
     for _ in range(args.warmup):
         res = eng.fisher_build(cells, counts, w["nmodes"])
-    names = ("cubature", "cubature_far", "surrogate", "blockeig_tridiag", "blockeig_vectors", "azimuthal_transform",
+    names = ("cubature", "cubature_far", "surrogate", "blockeig_tridiag", "blockeig_vectors", "blockeig_pairs",
+             "blockeig_back", "azimuthal_transform",
              "azimuthal_gemm", "project_step1", "project_step2", "fisher")
     base = {n: eng.kernel_stats(n) for n in names}
     launches0 = eng.launch_count()

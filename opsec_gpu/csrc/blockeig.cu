@@ -318,7 +318,62 @@ struct VecArgs {
     int* status;         // [nblk]: 0, or 1 when a bracket could not be confirmed, 2 when a cluster degenerated
 };
 
+// Twisted factorisation of T - s I (scaled T): the stationary top-down pivots G and multipliers
+// L, the bottom-up multipliers U, the twist index r where |gamma_r| is least, and the vector
+// z with z_r = 1 (rows i < r from L, rows i > r from U), written to column col of Z.
+// Returns the Rayleigh quotient correction gamma_r / |z|^2 (z^T (T - s I) z / z^T z) and
+// leaves |z|^2 in *nrm2.
+__device__ double twisted(int n, const double* d, const double* e, double s, double pivmin, size_t K, int col,
+                          double* G, double* L, double* U, double* Z, double* nrm2) {
+    double g = d[0] - s;
+    if (fabs(g) < pivmin) g = -pivmin;
+    for (int i = 0; i + 1 < n; i++) {
+        G[i * K + col] = g;
+        const double l = e[i] / g;
+        L[i * K + col] = l;
+        g = d[i + 1] - s - l * e[i];
+        if (fabs(g) < pivmin) g = -pivmin;
+    }
+    G[(size_t)(n - 1) * K + col] = g;
+    double h = d[n - 1] - s;
+    if (fabs(h) < pivmin) h = -pivmin;
+    int r = n - 1;
+    double gam_r = g, best = fabs(g);  // gamma_{n-1} = G_{n-1}
+    for (int i = n - 1; i >= 1; i--) {
+        const double u = e[i - 1] / h;
+        U[i * K + col] = u;
+        h = d[i - 1] - s - u * e[i - 1];
+        if (fabs(h) < pivmin) h = -pivmin;
+        // gamma_{i-1} = G_{i-1} + H_{i-1} - (d_{i-1} - s)
+        const double gam = G[(size_t)(i - 1) * K + col] + h - (d[i - 1] - s);
+        if (fabs(gam) < best) {
+            best = fabs(gam);
+            gam_r = gam;
+            r = i - 1;
+        }
+    }
+    double nrm = 1.0, z = 1.0;
+    Z[(size_t)r * K + col] = 1.0;
+    for (int i = r - 1; i >= 0; i--) {
+        z = -L[i * K + col] * z;
+        Z[i * K + col] = z;
+        nrm += z * z;
+    }
+    z = 1.0;
+    for (int i = r + 1; i < n; i++) {
+        z = -U[i * K + col] * z;
+        Z[i * K + col] = z;
+        nrm += z * z;
+    }
+    *nrm2 = nrm;
+    return gam_r / nrm;
+}
+
 // grid (nblk, ceil(n/32)), 32 threads: candidate c (0 = largest) of block b per thread.
+// The FP32 estimate's bracket is confirmed by two FP64 Sturm counts.  An eigenvalue alone in
+// its bracket is refined by Rayleigh-quotient iteration on twisted factorisations (cubic
+// convergence; the iterate must stay in the bracket); an eigenvalue sharing its bracket is
+// bisected to full precision first.  The last twisted factorisation gives the vector.
 __global__ void __launch_bounds__(32) vectors_kernel(VecArgs a) {
     __shared__ double d[kMaxN], e[kMaxN], e2[kMaxN];
     const int b = blockIdx.x, n = a.n;
@@ -337,72 +392,57 @@ __global__ void __launch_bounds__(32) vectors_kernel(VecArgs a) {
     const int col = a.koff[b] + c;
     const size_t K = (size_t)a.ktot;
     const double pivmin = 1e-290;
-    // FP64 bisection from the FP32 bracket, widened until the Sturm counts confirm it
     const double x = a.w[(size_t)b * n + j] * inv;
     double del = 64.0 * FLT_EPSILON, lo = x - del, hi = x + del;
+    int clo = 0, chi = 0;
     bool ok = false;
     for (int k = 0; k < 8 && !ok; k++) {
         lo = x - del;
         hi = x + del;
-        ok = sturm64(n, d, e2, lo, pivmin) <= j && sturm64(n, d, e2, hi, pivmin) > j;
+        clo = sturm64(n, d, e2, lo, pivmin);
+        chi = sturm64(n, d, e2, hi, pivmin);
+        ok = clo <= j && chi > j;
         del *= 8.0;
     }
     if (!ok) {
         lo = -1.0;
         hi = 1.0;
-        if (!(sturm64(n, d, e2, lo, pivmin) <= j && sturm64(n, d, e2, hi, pivmin) > j)) atomicMax(&a.status[b], 1);
+        clo = sturm64(n, d, e2, lo, pivmin);
+        chi = sturm64(n, d, e2, hi, pivmin);
+        if (!(clo <= j && chi > j)) atomicMax(&a.status[b], 1);
     }
-    for (int it = 0; it < 96; it++) {
-        const double mid = 0.5 * (lo + hi);
-        if (!(hi - lo > 2.0 * DBL_EPSILON * fmax(fabs(lo), fabs(hi)) + 4.0 * pivmin) || mid <= lo || mid >= hi) break;
-        if (sturm64(n, d, e2, mid, pivmin) > j) hi = mid;
-        else lo = mid;
-    }
-    const double lam = 0.5 * (lo + hi);
-    a.w[(size_t)b * n + j] = lam * sc;
-    // twisted factorisation of T - lam I: top-down pivots G and multipliers L, then bottom-up
-    double g = d[0] - lam;
-    if (fabs(g) < pivmin) g = -pivmin;
-    for (int i = 0; i + 1 < n; i++) {
-        a.G[i * K + col] = g;
-        const double l = e[i] / g;
-        a.L[i * K + col] = l;
-        g = d[i + 1] - lam - l * e[i];
-        if (fabs(g) < pivmin) g = -pivmin;
-    }
-    a.G[(size_t)(n - 1) * K + col] = g;
-    double h = d[n - 1] - lam;
-    if (fabs(h) < pivmin) h = -pivmin;
-    int r = n - 1;
-    double best = fabs(g);  // gamma_{n-1} = G_{n-1}
-    for (int i = n - 1; i >= 1; i--) {
-        const double u = e[i - 1] / h;
-        a.U[i * K + col] = u;
-        h = d[i - 1] - lam - u * e[i - 1];
-        if (fabs(h) < pivmin) h = -pivmin;
-        // gamma_{i-1} = G_{i-1} + H_{i-1} - (d_{i-1} - lam)
-        const double gam = a.G[(size_t)(i - 1) * K + col] + h - (d[i - 1] - lam);
-        if (fabs(gam) < best) {
-            best = fabs(gam);
-            r = i - 1;
+    double nrm2 = 1.0, lam = x;
+    bool done = false;
+    if (chi - clo == 1) {
+        // converged when the correction is below 1e-14 of the block scale (T is scaled to norm
+        // < 1), or when it stops shrinking at a level below 1e-10 (the rounding floor of gamma)
+        double s = fmin(fmax(x, lo), hi), prev = 1.0;
+        for (int it = 0; it < 8; it++) {
+            const double dl = twisted(n, d, e, s, pivmin, K, col, a.G, a.L, a.U, a.Z, &nrm2);
+            const double s1 = s + dl;
+            if (!(s1 > lo && s1 < hi)) break;  // left the bracket: bisect instead
+            if (fabs(dl) <= 1e-14 || (fabs(dl) <= 1e-10 && fabs(dl) > 0.25 * prev)) {
+                lam = s1;
+                done = true;
+                break;
+            }
+            prev = fabs(dl);
+            s = s1;
         }
     }
-    // z_r = 1, then outward: z_i = -L_i z_{i+1} above r, z_i = -U_i z_{i-1} below r
-    double nrm = 1.0;
-    a.Z[(size_t)r * K + col] = 1.0;
-    double z = 1.0;
-    for (int i = r - 1; i >= 0; i--) {
-        z = -a.L[i * K + col] * z;
-        a.Z[i * K + col] = z;
-        nrm += z * z;
+    if (!done) {
+        for (int it = 0; it < 96; it++) {
+            const double mid = 0.5 * (lo + hi);
+            if (!(hi - lo > 2.0 * DBL_EPSILON * fmax(fabs(lo), fabs(hi)) + 4.0 * pivmin) || mid <= lo || mid >= hi)
+                break;
+            if (sturm64(n, d, e2, mid, pivmin) > j) hi = mid;
+            else lo = mid;
+        }
+        lam = 0.5 * (lo + hi);
+        twisted(n, d, e, lam, pivmin, K, col, a.G, a.L, a.U, a.Z, &nrm2);
     }
-    z = 1.0;
-    for (int i = r + 1; i < n; i++) {
-        z = -a.U[i * K + col] * z;
-        a.Z[i * K + col] = z;
-        nrm += z * z;
-    }
-    const double s = 1.0 / sqrt(nrm);
+    a.w[(size_t)b * n + j] = lam * sc;
+    const double s = 1.0 / sqrt(nrm2);
     if (!isfinite(s) || !(s > 0.0)) atomicMax(&a.status[b], 3);
     for (int i = 0; i < n; i++) a.Z[i * K + col] *= s;
 }
@@ -442,45 +482,62 @@ __global__ void __launch_bounds__(256) cluster_kernel(VecArgs a, double tol) {
     }
 }
 
-// x = H_0 H_1 ... H_{n-3} z for 32 candidates of block b per CTA (one warp, a lane per
-// candidate); the vectors live in shared memory when n <= 512.  Writes column n-1-c of the
-// block (ascending order, column-major).
-template <bool kShared>
-__global__ void __launch_bounds__(32) backtransform_kernel(VecArgs a, const double* __restrict__ Vall,
-                                                           const double* __restrict__ tau, double* __restrict__ out) {
-    extern __shared__ double zs[];
+// x = H_0 H_1 ... H_{n-3} z for G candidates of block b per CTA (grid (nblk, ceil(n/G)), 256
+// threads).  The G vectors live in shared memory ([row][G]), each reflector row is staged once
+// per CTA, thread t works on vector t % G over the rows t / G + 8 k, and the G dot products are
+// summed over the 256 / G row groups in a fixed order.  Writes column n-1-c of the block
+// (ascending order, column-major).
+constexpr int kBT = 256;
+template <int G>
+__global__ void __launch_bounds__(kBT) backtransform_kernel(VecArgs a, const double* __restrict__ Vall,
+                                                            const double* __restrict__ tau, double* __restrict__ out) {
+    extern __shared__ double bsm[];
+    constexpr int R = kBT / G;  // row groups
     const int b = blockIdx.x, n = a.n, kc = a.kc[b];
-    if ((int)blockIdx.y * 32 >= kc) return;
-    const int c = blockIdx.y * 32 + threadIdx.x;
-    const bool act = c < kc;
+    const int c0 = blockIdx.y * G;
+    if (c0 >= kc) return;
+    double* z = bsm;                       // [n][G]
+    double* v = z + (size_t)n * G;         // [n] reflector row
+    double* part = v + n;                  // [R][G]
+    double* f = part + R * G;              // [G]
+    const int t = threadIdx.x, g = t % G, rg = t / G;
     const size_t K = (size_t)a.ktot;
-    const int col = a.koff[b] + (act ? c : 0);
-    double* zg = a.Z + col;  // stride K
-    double* z = kShared ? zs + threadIdx.x : zg;
-    const size_t st = kShared ? 32 : K;
-    if (kShared)
-        for (int i = 0; i < n; i++) z[i * st] = act ? zg[i * K] : 0.0;
-    const double* V = Vall + (size_t)b * n * n;
-    for (int c2 = n - 3; c2 >= 0; c2--) {
-        const double tc = tau[(size_t)b * n + c2];
-        if (tc == 0.0) continue;
-        const double* v = V + (size_t)c2 * n;
-        double s0 = z[(size_t)(c2 + 1) * st], s1 = 0.0, s2 = 0.0, s3 = 0.0;
-        int i = c2 + 2;
-        for (; i + 3 < n; i += 4) {
-            s0 = fma(v[i], z[(size_t)i * st], s0);
-            s1 = fma(v[i + 1], z[(size_t)(i + 1) * st], s1);
-            s2 = fma(v[i + 2], z[(size_t)(i + 2) * st], s2);
-            s3 = fma(v[i + 3], z[(size_t)(i + 3) * st], s3);
-        }
-        for (; i < n; i++) s0 = fma(v[i], z[(size_t)i * st], s0);
-        const double f = tc * ((s0 + s1) + (s2 + s3));
-        z[(size_t)(c2 + 1) * st] -= f;
-        for (i = c2 + 2; i < n; i++) z[(size_t)i * st] = fma(-f, v[i], z[(size_t)i * st]);
+    const int ng = min(G, kc - c0);
+    for (int idx = t; idx < n * G; idx += kBT) {
+        const int i = idx / G, gg = idx % G;
+        z[idx] = gg < ng ? a.Z[(size_t)i * K + a.koff[b] + c0 + gg] : 0.0;
     }
-    if (!act) return;
-    double* o = out + (size_t)b * n * n + (size_t)(n - 1 - c) * n;
-    for (int i = 0; i < n; i++) o[i] = z[(size_t)i * st];
+    const double* V = Vall + (size_t)b * n * n;
+    const double* tb = tau + (size_t)b * n;
+    for (int c2 = n - 3; c2 >= 0; c2--) {
+        const double tc = tb[c2];
+        if (tc == 0.0) continue;  // uniform over the CTA
+        __syncthreads();          // the previous update is done with v
+        for (int i = c2 + 1 + t; i < n; i += kBT) v[i] = V[(size_t)c2 * n + i];
+        __syncthreads();
+        double s0 = 0.0, s1 = 0.0;
+        int i = c2 + 1 + rg;
+        for (; i + R < n; i += 2 * R) {
+            s0 = fma(v[i], z[(size_t)i * G + g], s0);
+            s1 = fma(v[i + R], z[(size_t)(i + R) * G + g], s1);
+        }
+        if (i < n) s0 = fma(v[i], z[(size_t)i * G + g], s0);
+        part[rg * G + g] = s0 + s1;
+        __syncthreads();
+        if (t < G) {
+            double s = 0.0;
+            for (int r = 0; r < R; r++) s += part[r * G + t];
+            f[t] = tc * s;
+        }
+        __syncthreads();
+        const double fg = f[g];
+        for (i = c2 + 1 + rg; i < n; i += R) z[(size_t)i * G + g] = fma(-fg, v[i], z[(size_t)i * G + g]);
+    }
+    __syncthreads();
+    for (int gg = 0; gg < ng; gg++) {
+        double* o = out + (size_t)b * n * n + (size_t)(n - 1 - (c0 + gg)) * n;
+        for (int i2 = t; i2 < n; i2 += kBT) o[i2] = z[(size_t)i2 * G + gg];
+    }
 }
 
 }  // namespace
@@ -511,16 +568,25 @@ void launch_blockeig_spectrum(int n, int nblk, const double* dg, const double* e
 void launch_blockeig_vectors(const BlockEigVectors& p, cudaStream_t s, long long* launches) {
     VecArgs a{p.n, p.nblk, p.ktot, p.kc, p.koff, p.dg, p.eg, p.scale, p.w, p.Z, p.L, p.U, p.G, p.status};
     const dim3 grid(p.nblk, (p.n + 31) / 32);
+    if (g_clock) g_clock->begin("blockeig_pairs", s);
     vectors_kernel<<<grid, 32, 0, s>>>(a);
+    if (g_clock) g_clock->end(s);
     cluster_kernel<<<p.nblk, 256, 0, s>>>(a, 1e-6);
+    if (g_clock) g_clock->begin("blockeig_back", s, 2.0 * p.n * (double)p.n * p.ktot);
     if (p.n <= 512) {
-        const size_t smem = sizeof(double) * 32 * p.n;
-        OPSEC_CUDA(cudaFuncSetAttribute(backtransform_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        max_dynamic_smem((const void*)backtransform_kernel<true>)));
-        backtransform_kernel<true><<<grid, 32, smem, s>>>(a, p.V, p.tau, p.out);
+        constexpr int G = 32;
+        const size_t smem = sizeof(double) * ((size_t)p.n * G + p.n + kBT + G);
+        OPSEC_CUDA(cudaFuncSetAttribute(backtransform_kernel<G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        max_dynamic_smem((const void*)backtransform_kernel<G>)));
+        backtransform_kernel<G><<<dim3(p.nblk, (p.n + G - 1) / G), kBT, smem, s>>>(a, p.V, p.tau, p.out);
     } else {
-        backtransform_kernel<false><<<grid, 32, 0, s>>>(a, p.V, p.tau, p.out);
+        constexpr int G = 16;
+        const size_t smem = sizeof(double) * ((size_t)p.n * G + p.n + kBT + G);
+        OPSEC_CUDA(cudaFuncSetAttribute(backtransform_kernel<G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        max_dynamic_smem((const void*)backtransform_kernel<G>)));
+        backtransform_kernel<G><<<dim3(p.nblk, (p.n + G - 1) / G), kBT, smem, s>>>(a, p.V, p.tau, p.out);
     }
+    if (g_clock) g_clock->end(s);
     OPSEC_CUDA(cudaGetLastError());
     *launches += 3;
 }
