@@ -8,23 +8,27 @@
 //
 //   1. tridiag_kernel: Householder reduction A = Q T Q^T of every block, one cluster of four CTAs
 //      per block (the lower triangle stays in L2; each step is a fused pass that applies the
-//      previous reflector's rank-2 update and forms the next reflector's product A v).  FP64.
+//      previous reflector's rank-2 update and forms the next reflector's product A v).  The
+//      O(n^2) pass runs in double-FP32 (df64.h), the O(n) work of each step in FP64.
 //   2. spectrum_kernel: every eigenvalue of every T by bisection on FP32 Sturm counts of the
 //      power-of-two-scaled T (to ~1e-6 of the block norm): enough to decide which block
 //      eigenvalues can reach the global cut.
 //   3. (host) the candidates: per block, the eigenvalues within a safe margin of the cut.
-//   4. vectors_kernel: each candidate's eigenvalue by FP64 bisection from its FP32 bracket, then
-//      its eigenvector of T by a twisted factorisation (the stationary top-down and bottom-up
-//      LDL^T factorisations of T - lambda I meet at the index where the residual is smallest).
+//   4. vectors_kernel: each candidate's eigenvalue from its FP32 bracket (confirmed by two FP64
+//      Sturm counts, bisected until it holds this eigenvalue alone) by Rayleigh-quotient
+//      iteration on twisted factorisations (the stationary top-down and bottom-up LDL^T
+//      factorisations of T - s I meet at the index where the residual is smallest), then its
+//      eigenvector of T from the last one.
 //   5. cluster_kernel: Gram-Schmidt (twice) inside clusters of candidates closer than 1e-6 of the
 //      block norm, where separately computed vectors need not be orthogonal.
-//   6. backtransform_kernel: x = Q z by the stored reflectors, written as the block's eigenvector
-//      column (ascending eigenvalue order, the layout of LAPACK's syevd).
+//   6. backtransform_kernel: x = Q z by the stored reflectors (double-FP32), written as the
+//      block's eigenvector column (ascending eigenvalue order, the layout of LAPACK's syevd).
 #include <cooperative_groups.h>
 
 #include <cfloat>
 #include <cmath>
 
+#include "df64.h"
 #include "engine.h"
 
 namespace cg = cooperative_groups;
@@ -81,43 +85,62 @@ __device__ void householder(int n, int c, const double* col, double* v, double* 
     }
 }
 
-// One fused pass over the columns j in [j0, n) of the lower triangle: a -= v_i w_j + w_i v_j
-// (when upd), then the partial products p += A vn into this warp's row of pw (when sym).
-__device__ void fused_pass(int n, int j0, double* __restrict__ A, const double* vk, const double* wk,
-                           const double* vn, double* pw, bool upd, bool sym, int gwarp, int nwarps) {
+// One fused pass over the columns j in [j0, n) of the lower triangle, in double-FP32 (the
+// FP64 pipe is the bound otherwise): a -= v_i w_j + w_i v_j (when upd), then the partial
+// products p += A vn into this warp's row of pw (when sym).  conv: the column still holds FP64
+// values (the first pass), which are read as doubles and written back as (hi, lo) pairs in the
+// same 8 bytes.
+__device__ void fused_pass(int n, int j0, double* __restrict__ A, const float2* vk, const float2* wk,
+                           const float2* vn, float2* pw, bool upd, bool sym, bool conv, int gwarp, int nwarps) {
     const int lane = threadIdx.x & 31;
     const int L = n - j0;
+    float2* A2 = reinterpret_cast<float2*>(A);
     for (int q0 = 0; q0 < L; q0 += nwarps) {
         // snake order: the long columns at the front go to alternate ends of the warp list
         const int odd = (q0 / nwarps) & 1;
         const int q = q0 + (odd ? nwarps - 1 - gwarp : gwarp);
         if (q >= L) continue;
         const int j = j0 + q;
-        double* col = A + (size_t)j * n;
-        const double vkj = upd ? vk[j] : 0.0, wkj = upd ? wk[j] : 0.0, vnj = sym ? vn[j] : 0.0;
-        double cacc = 0.0;
+        const size_t cj = (size_t)j * n;
+        const df vkj = upd ? df_unpack(vk[j]) : df{0.f, 0.f}, wkj = upd ? df_unpack(wk[j]) : df{0.f, 0.f};
+        const df vnj = sym ? df_unpack(vn[j]) : df{0.f, 0.f};
+        df cacc{0.f, 0.f};
         for (int i = j + lane; i < n; i += 32) {
-            double a = col[i];
+            df a = conv ? df_from(A[cj + i]) : df_unpack(A2[cj + i]);
             if (upd) {
-                a = fma(-vk[i], wkj, a);
-                a = fma(-wk[i], vkj, a);
-                col[i] = a;
+                a = df_fms(a, df_unpack(vk[i]), wkj);
+                a = df_fms(a, df_unpack(wk[i]), vkj);
             }
+            if (upd || conv) A2[cj + i] = df_pack(a);
             if (sym) {
-                pw[i] = fma(a, vnj, pw[i]);
-                if (i != j) cacc = fma(a, vn[i], cacc);
+                pw[i] = df_pack(df_fma(df_unpack(pw[i]), a, vnj));
+                if (i != j) cacc = df_fma(cacc, a, df_unpack(vn[i]));
             }
         }
         if (sym) {
 #pragma unroll
-            for (int o = 16; o; o >>= 1) cacc += __shfl_xor_sync(0xffffffffu, cacc, o);
-            if (lane == 0) pw[j] += cacc;
+            for (int o = 16; o; o >>= 1) {
+                const df other{__shfl_xor_sync(0xffffffffu, cacc.h, o), __shfl_xor_sync(0xffffffffu, cacc.l, o)};
+                cacc = df_add(cacc, other);
+            }
+            if (lane == 0) pw[j] = df_pack(df_add(df_unpack(pw[j]), cacc));
         }
     }
 }
 
+// this CTA's partial A v for rows [i0, n): the warps' rows summed in a fixed order
+__device__ void reduce_warp_rows(int n, int i0, const float2* pw, float2* out) {
+    for (int i = i0 + (int)threadIdx.x; i < n; i += kTT) {
+        df s{0.f, 0.f};
+        for (int w = 0; w < kTW; w++) s = df_add(s, df_unpack(pw[(size_t)w * n + i]));
+        out[i] = df_pack(s);
+    }
+}
+
 // Householder tridiagonalisation of block b = blockIdx.x / kCl (column-major, lower triangle
-// read and updated; n >= 3).  Outputs T (dg, eg), the reflectors V[b][c][i] (v[c+1] = 1) and tau.
+// read and updated; n >= 3).  Outputs T (dg, eg), the reflectors V[b][c][i] as (hi, lo) float
+// pairs (v[c+1] = 1) and tau.  The O(n) work of each step (the reflector, w) is FP64; the
+// O(n^2) fused pass is double-FP32.
 __global__ void __cluster_dims__(kCl, 1, 1) __launch_bounds__(kTT, 1)
 tridiag_kernel(int n, double* __restrict__ Aall, double* __restrict__ Vall, double* __restrict__ tau,
                double* __restrict__ dg, double* __restrict__ eg) {
@@ -127,16 +150,19 @@ tridiag_kernel(int n, double* __restrict__ Aall, double* __restrict__ Vall, doub
     const int b = blockIdx.x / kCl;
     const int t = threadIdx.x, warp = t >> 5;
     double* A = Aall + (size_t)b * n * n;
-    double* V = Vall + (size_t)b * n * n;
-    double* vk = sm;
+    float2* V = reinterpret_cast<float2*>(Vall) + (size_t)b * n * n;
+    double* vk = sm;                  // FP64 copies for the O(n) work
     double* wk = vk + n;
     double* vn = wk + n;
     double* col = vn + n;
-    double* buf = col + n;           // [2][n] this CTA's partial A v, read by the whole cluster
-    double* pw = buf + 2 * n;        // [kTW][n] per-warp partial rows
-    double* red = pw + (size_t)kTW * n;  // 40 doubles
-    double* scal = red + 40;         // tau of the next reflector, beta
-    double* pw_mine = pw + (size_t)warp * n;
+    float2* vk2 = reinterpret_cast<float2*>(col + n);  // (hi, lo) copies for the fused pass
+    float2* wk2 = vk2 + n;
+    float2* vn2 = wk2 + n;
+    float2* buf = vn2 + n;            // [2][n] this CTA's partial A v, read by the whole cluster
+    float2* pw = buf + 2 * n;         // [kTW][n] per-warp partial rows
+    double* red = reinterpret_cast<double*>(pw + (size_t)kTW * n);  // 40 doubles
+    double* scal = red + 40;          // tau of the next reflector, beta
+    float2* pw_mine = pw + (size_t)warp * n;
     const int gwarp = rank * kTW + warp, nwarps = kCl * kTW;
 
     // pivot column 0 and the first reflector
@@ -144,49 +170,51 @@ tridiag_kernel(int n, double* __restrict__ Aall, double* __restrict__ Vall, doub
     __syncthreads();
     householder(n, 0, col, vn, &scal[0], &scal[1], red);
     __syncthreads();
+    for (int i = 1 + t; i < n; i += kTT) vn2[i] = df_pack(df_from(vn[i]));
     if (rank == 0) {
-        for (int i = 1 + t; i < n; i += kTT) V[i] = vn[i];
+        for (int i = 1 + t; i < n; i += kTT) V[i] = vn2[i];
         if (t == 0) {
             dg[(size_t)b * n] = col[0];
             eg[(size_t)b * n] = scal[1];
             tau[(size_t)b * n] = scal[0];
         }
     }
-    for (int i = 1 + (t & 31); i < n; i += 32) pw_mine[i] = 0.0;
-    __syncwarp();
-    fused_pass(n, 1, A, vk, wk, vn, pw_mine, false, true, gwarp, nwarps);
+    for (int i = 1 + (t & 31); i < n; i += 32) pw_mine[i] = make_float2(0.f, 0.f);
     __syncthreads();
-    for (int i = 1 + t; i < n; i += kTT) {
-        double s = 0.0;
-        for (int w = 0; w < kTW; w++) s += pw[(size_t)w * n + i];
-        buf[i] = s;  // parity 0
-    }
+    fused_pass(n, 1, A, vk2, wk2, vn2, pw_mine, false, true, true, gwarp, nwarps);
+    __syncthreads();
+    reduce_warp_rows(n, 1, pw, buf);  // parity 0
     cluster.sync();
 
     for (int c = 0; c <= n - 3; c++) {
         const double tc = scal[0];
         // (a) v_c, p_c = A v_c from the four CTAs (fixed order), w_c = y - (tau/2)(y.v) v
-        const double* rb[kCl];
+        const float2* rb[kCl];
 #pragma unroll
         for (int r = 0; r < kCl; r++) rb[r] = cluster.map_shared_rank(buf + (size_t)(c & 1) * n, r);
         double part = 0.0;
         for (int i = c + 1 + t; i < n; i += kTT) {
-            double p = 0.0;
+            df p = df_unpack(rb[0][i]);
 #pragma unroll
-            for (int r = 0; r < kCl; r++) p += rb[r][i];
-            const double y = tc * p;
+            for (int r = 1; r < kCl; r++) p = df_add(p, df_unpack(rb[r][i]));
+            const double y = tc * df_to(p);
             vk[i] = vn[i];
+            vk2[i] = vn2[i];
             wk[i] = y;
             part += y * vn[i];
         }
         const double alpha = 0.5 * tc * cta_sum(part, red);
-        for (int i = c + 1 + t; i < n; i += kTT) wk[i] -= alpha * vk[i];
+        for (int i = c + 1 + t; i < n; i += kTT) {
+            wk[i] -= alpha * vk[i];
+            wk2[i] = df_pack(df_from(wk[i]));
+        }
         __syncthreads();
         // (b) pivot column c+1 under the update, the next reflector
         const int c1 = c + 1;
         const double vkc = vk[c1], wkc = wk[c1];
+        const float2* A2 = reinterpret_cast<const float2*>(A);
         for (int i = c1 + t; i < n; i += kTT) {
-            double a = A[(size_t)c1 * n + i];
+            double a = df_to(df_unpack(A2[(size_t)c1 * n + i]));
             a = fma(-vk[i], wkc, a);
             a = fma(-wk[i], vkc, a);
             col[i] = a;
@@ -194,8 +222,9 @@ tridiag_kernel(int n, double* __restrict__ Aall, double* __restrict__ Vall, doub
         __syncthreads();
         householder(n, c1, col, vn, &scal[0], &scal[1], red);
         __syncthreads();
+        for (int i = c1 + 1 + t; i < n; i += kTT) vn2[i] = df_pack(df_from(vn[i]));
         if (rank == 0) {
-            for (int i = c1 + 1 + t; i < n; i += kTT) V[(size_t)c1 * n + i] = vn[i];
+            for (int i = c1 + 1 + t; i < n; i += kTT) V[(size_t)c1 * n + i] = vn2[i];
             if (t == 0) {
                 dg[(size_t)b * n + c1] = col[c1];
                 eg[(size_t)b * n + c1] = scal[1];
@@ -204,24 +233,17 @@ tridiag_kernel(int n, double* __restrict__ Aall, double* __restrict__ Vall, doub
         }
         // (c) columns c+2 .. n-1: update by (v_c, w_c); partial A v_{c+1} for the next step
         const bool sym = c1 <= n - 3;
-        if (sym) {
-            for (int i = c1 + 1 + (t & 31); i < n; i += 32) pw_mine[i] = 0.0;
-            __syncwarp();
-        }
-        fused_pass(n, c1 + 1, A, vk, wk, vn, pw_mine, true, sym, gwarp, nwarps);
+        if (sym)
+            for (int i = c1 + 1 + (t & 31); i < n; i += 32) pw_mine[i] = make_float2(0.f, 0.f);
         __syncthreads();
-        if (sym) {
-            double* bo = buf + (size_t)(c1 & 1) * n;
-            for (int i = c1 + 1 + t; i < n; i += kTT) {
-                double s = 0.0;
-                for (int w = 0; w < kTW; w++) s += pw[(size_t)w * n + i];
-                bo[i] = s;
-            }
-        }
+        fused_pass(n, c1 + 1, A, vk2, wk2, vn2, pw_mine, true, sym, false, gwarp, nwarps);
+        __syncthreads();
+        if (sym) reduce_warp_rows(n, c1 + 1, pw, buf + (size_t)(c1 & 1) * n);
         cluster.sync();
     }
     if (rank == 0 && t == 0) {
-        dg[(size_t)b * n + n - 1] = A[(size_t)(n - 1) * n + n - 1];
+        const float2* A2 = reinterpret_cast<const float2*>(A);
+        dg[(size_t)b * n + n - 1] = df_to(df_unpack(A2[(size_t)(n - 1) * n + n - 1]));
         eg[(size_t)b * n + n - 1] = 0.0;
         tau[(size_t)b * n + n - 1] = 0.0;
     }
@@ -318,55 +340,90 @@ struct VecArgs {
     int* status;         // [nblk]: 0, or 1 when a bracket could not be confirmed, 2 when a cluster degenerated
 };
 
-// Twisted factorisation of T - s I (scaled T): the stationary top-down pivots G and multipliers
-// L, the bottom-up multipliers U, the twist index r where |gamma_r| is least, and the vector
-// z with z_r = 1 (rows i < r from L, rows i > r from U), written to column col of Z.
-// Returns the Rayleigh quotient correction gamma_r / |z|^2 (z^T (T - s I) z / z^T z) and
-// leaves |z|^2 in *nrm2.
-__device__ double twisted(int n, const double* d, const double* e, double s, double pivmin, size_t K, int col,
-                          double* G, double* L, double* U, double* Z, double* nrm2) {
-    double g = d[0] - s;
+// Twisted factorisation of T - s I (scaled T).  The stationary top-down pivots G_i (with the
+// multipliers L_i = e_i / G_i) and the bottom-up pivots H_i (U_i = e_{i-1} / H_i) meet at the
+// twist index r where |gamma_r| = |G_r + H_r - (d_r - s)| is least; the vector with z_r = 1
+// has z_i = -L_i z_{i+1} above r and z_i = -U_i z_{i-1} below it.  Its squared norm at every
+// twist follows from two recurrences, S_{i+1} = L_i^2 (1 + S_i) from the top and
+// B_{i-1} = U_i^2 (1 + B_i) from the bottom, so |z|^2 = S_r + 1 + B_r without forming z.
+// rq_step: one pass each way; returns the Rayleigh-quotient correction gamma_r / |z|^2.  The
+// top-down pass keeps G and S in the scratch columns (they are read back, in an order that
+// does not depend on the recurrence, by the bottom-up pass).
+__device__ double rq_step(int n, const double* d, const double* e, double s, double pivmin, size_t K,
+                          double* __restrict__ Gc, double* __restrict__ Sc, int* r_out) {
+    double g = d[0] - s, sn = 0.0;
     if (fabs(g) < pivmin) g = -pivmin;
     for (int i = 0; i + 1 < n; i++) {
-        G[i * K + col] = g;
+        Gc[i * K] = g;
+        Sc[i * K] = sn;
         const double l = e[i] / g;
-        L[i * K + col] = l;
+        sn = l * l * (1.0 + sn);
         g = d[i + 1] - s - l * e[i];
         if (fabs(g) < pivmin) g = -pivmin;
     }
-    G[(size_t)(n - 1) * K + col] = g;
-    double h = d[n - 1] - s;
-    if (fabs(h) < pivmin) h = -pivmin;
+    // twist at n-1: gamma = G_{n-1}, |z|^2 = S_{n-1} + 1
     int r = n - 1;
-    double gam_r = g, best = fabs(g);  // gamma_{n-1} = G_{n-1}
+    double gam_r = g, best = fabs(g), nz = sn + 1.0;
+    double h = d[n - 1] - s, bn = 0.0;
+    if (fabs(h) < pivmin) h = -pivmin;
+    double gnext = Gc[(size_t)(n - 2) * K], snext = Sc[(size_t)(n - 2) * K];
     for (int i = n - 1; i >= 1; i--) {
+        const double gi = gnext, si = snext;  // G_{i-1}, S_{i-1}
+        if (i >= 2) {
+            gnext = Gc[(size_t)(i - 2) * K];
+            snext = Sc[(size_t)(i - 2) * K];
+        }
         const double u = e[i - 1] / h;
-        U[i * K + col] = u;
+        bn = u * u * (1.0 + bn);
         h = d[i - 1] - s - u * e[i - 1];
         if (fabs(h) < pivmin) h = -pivmin;
-        // gamma_{i-1} = G_{i-1} + H_{i-1} - (d_{i-1} - s)
-        const double gam = G[(size_t)(i - 1) * K + col] + h - (d[i - 1] - s);
+        const double gam = gi + h - (d[i - 1] - s);
         if (fabs(gam) < best) {
             best = fabs(gam);
             gam_r = gam;
             r = i - 1;
+            nz = si + 1.0 + bn;
         }
     }
+    *r_out = r;
+    return gam_r / nz;
+}
+
+// The eigenvector at s with twist r into column Zc (stride K), unnormalised, |z|^2 in *nrm_out;
+// Lc, Uc scratch columns.
+__device__ void twisted_vector(int n, const double* d, const double* e, double s, double pivmin, int r, size_t K,
+                               double* __restrict__ Lc, double* __restrict__ Uc, double* __restrict__ Zc,
+                               double* nrm_out) {
+    double g = d[0] - s;
+    if (fabs(g) < pivmin) g = -pivmin;
+    for (int i = 0; i < r; i++) {
+        const double l = e[i] / g;
+        Lc[i * K] = l;
+        g = d[i + 1] - s - l * e[i];
+        if (fabs(g) < pivmin) g = -pivmin;
+    }
+    double h = d[n - 1] - s;
+    if (fabs(h) < pivmin) h = -pivmin;
+    for (int i = n - 1; i > r; i--) {
+        const double u = e[i - 1] / h;
+        Uc[i * K] = u;
+        h = d[i - 1] - s - u * e[i - 1];
+        if (fabs(h) < pivmin) h = -pivmin;
+    }
     double nrm = 1.0, z = 1.0;
-    Z[(size_t)r * K + col] = 1.0;
+    Zc[(size_t)r * K] = 1.0;
     for (int i = r - 1; i >= 0; i--) {
-        z = -L[i * K + col] * z;
-        Z[i * K + col] = z;
+        z = -Lc[i * K] * z;
+        Zc[i * K] = z;
         nrm += z * z;
     }
     z = 1.0;
     for (int i = r + 1; i < n; i++) {
-        z = -U[i * K + col] * z;
-        Z[i * K + col] = z;
+        z = -Uc[i * K] * z;
+        Zc[i * K] = z;
         nrm += z * z;
     }
-    *nrm2 = nrm;
-    return gam_r / nrm;
+    *nrm_out = nrm;
 }
 
 // grid (nblk, ceil(n/32)), 32 threads: candidate c (0 = largest) of block b per thread.
@@ -393,7 +450,7 @@ __global__ void __launch_bounds__(32) vectors_kernel(VecArgs a) {
     const size_t K = (size_t)a.ktot;
     const double pivmin = 1e-290;
     const double x = a.w[(size_t)b * n + j] * inv;
-    double del = 64.0 * FLT_EPSILON, lo = x - del, hi = x + del;
+    double del = 8.0 * FLT_EPSILON, lo = x - del, hi = x + del;
     int clo = 0, chi = 0;
     bool ok = false;
     for (int k = 0; k < 8 && !ok; k++) {
@@ -411,18 +468,34 @@ __global__ void __launch_bounds__(32) vectors_kernel(VecArgs a) {
         chi = sturm64(n, d, e2, hi, pivmin);
         if (!(clo <= j && chi > j)) atomicMax(&a.status[b], 1);
     }
-    double nrm2 = 1.0, lam = x;
+    double* Gc = a.G + col;
+    double* Sc = a.L + col;
+    double lam = x, vs = x;  // the eigenvalue, and the shift whose twist r gives the vector
+    int r = n - 1;
     bool done = false;
+    // a bracket holding several eigenvalues is bisected until it holds this one alone
+    for (int it = 0; it < 60 && chi - clo > 1 && hi - lo > 4.0 * DBL_EPSILON; it++) {
+        const double mid = 0.5 * (lo + hi);
+        const int cm = sturm64(n, d, e2, mid, pivmin);
+        if (cm > j) {
+            hi = mid;
+            chi = cm;
+        } else {
+            lo = mid;
+            clo = cm;
+        }
+    }
     if (chi - clo == 1) {
         // converged when the correction is below 1e-14 of the block scale (T is scaled to norm
         // < 1), or when it stops shrinking at a level below 1e-10 (the rounding floor of gamma)
         double s = fmin(fmax(x, lo), hi), prev = 1.0;
         for (int it = 0; it < 8; it++) {
-            const double dl = twisted(n, d, e, s, pivmin, K, col, a.G, a.L, a.U, a.Z, &nrm2);
+            const double dl = rq_step(n, d, e, s, pivmin, K, Gc, Sc, &r);
             const double s1 = s + dl;
             if (!(s1 > lo && s1 < hi)) break;  // left the bracket: bisect instead
             if (fabs(dl) <= 1e-14 || (fabs(dl) <= 1e-10 && fabs(dl) > 0.25 * prev)) {
                 lam = s1;
+                vs = s;  // the twist r belongs to s
                 done = true;
                 break;
             }
@@ -438,9 +511,11 @@ __global__ void __launch_bounds__(32) vectors_kernel(VecArgs a) {
             if (sturm64(n, d, e2, mid, pivmin) > j) hi = mid;
             else lo = mid;
         }
-        lam = 0.5 * (lo + hi);
-        twisted(n, d, e, lam, pivmin, K, col, a.G, a.L, a.U, a.Z, &nrm2);
+        lam = vs = 0.5 * (lo + hi);
+        rq_step(n, d, e, vs, pivmin, K, Gc, Sc, &r);
     }
+    double nrm2 = 1.0;
+    twisted_vector(n, d, e, vs, pivmin, r, K, a.L + col, a.U + col, a.Z + col, &nrm2);
     a.w[(size_t)b * n + j] = lam * sc;
     const double s = 1.0 / sqrt(nrm2);
     if (!isfinite(s) || !(s > 0.0)) atomicMax(&a.status[b], 3);
@@ -483,10 +558,10 @@ __global__ void __launch_bounds__(256) cluster_kernel(VecArgs a, double tol) {
 }
 
 // x = H_0 H_1 ... H_{n-3} z for G candidates of block b per CTA (grid (nblk, ceil(n/G)), 256
-// threads).  The G vectors live in shared memory ([row][G]), each reflector row is staged once
-// per CTA, thread t works on vector t % G over the rows t / G + 8 k, and the G dot products are
-// summed over the 256 / G row groups in a fixed order.  Writes column n-1-c of the block
-// (ascending order, column-major).
+// threads), in double-FP32.  The G vectors live in shared memory ([row][G] (hi, lo) pairs),
+// each reflector row is staged once per CTA, thread t works on vector t % G over the rows
+// t / G + R k, and the G dot products are summed over the R = 256 / G row groups in a fixed
+// order.  Writes column n-1-c of the block in FP64 (ascending order, column-major).
 constexpr int kBT = 256;
 template <int G>
 __global__ void __launch_bounds__(kBT) backtransform_kernel(VecArgs a, const double* __restrict__ Vall,
@@ -496,53 +571,54 @@ __global__ void __launch_bounds__(kBT) backtransform_kernel(VecArgs a, const dou
     const int b = blockIdx.x, n = a.n, kc = a.kc[b];
     const int c0 = blockIdx.y * G;
     if (c0 >= kc) return;
-    double* z = bsm;                       // [n][G]
-    double* v = z + (size_t)n * G;         // [n] reflector row
-    double* part = v + n;                  // [R][G]
-    double* f = part + R * G;              // [G]
+    float2* z = reinterpret_cast<float2*>(bsm);  // [n][G]
+    float2* v = z + (size_t)n * G;                // [n] reflector row
+    float2* part = v + n;                         // [R][G]
+    float2* f = part + R * G;                     // [G]
     const int t = threadIdx.x, g = t % G, rg = t / G;
     const size_t K = (size_t)a.ktot;
     const int ng = min(G, kc - c0);
     for (int idx = t; idx < n * G; idx += kBT) {
         const int i = idx / G, gg = idx % G;
-        z[idx] = gg < ng ? a.Z[(size_t)i * K + a.koff[b] + c0 + gg] : 0.0;
+        z[idx] = df_pack(df_from(gg < ng ? a.Z[(size_t)i * K + a.koff[b] + c0 + gg] : 0.0));
     }
-    const double* V = Vall + (size_t)b * n * n;
+    const float2* V = reinterpret_cast<const float2*>(Vall) + (size_t)b * n * n;
     const double* tb = tau + (size_t)b * n;
     for (int c2 = n - 3; c2 >= 0; c2--) {
         const double tc = tb[c2];
         if (tc == 0.0) continue;  // uniform over the CTA
-        __syncthreads();          // the previous update is done with v
+        __syncthreads();          // the previous update is done with v and f
         for (int i = c2 + 1 + t; i < n; i += kBT) v[i] = V[(size_t)c2 * n + i];
         __syncthreads();
-        double s0 = 0.0, s1 = 0.0;
+        df s0{0.f, 0.f}, s1{0.f, 0.f};
         int i = c2 + 1 + rg;
         for (; i + R < n; i += 2 * R) {
-            s0 = fma(v[i], z[(size_t)i * G + g], s0);
-            s1 = fma(v[i + R], z[(size_t)(i + R) * G + g], s1);
+            s0 = df_fma(s0, df_unpack(v[i]), df_unpack(z[(size_t)i * G + g]));
+            s1 = df_fma(s1, df_unpack(v[i + R]), df_unpack(z[(size_t)(i + R) * G + g]));
         }
-        if (i < n) s0 = fma(v[i], z[(size_t)i * G + g], s0);
-        part[rg * G + g] = s0 + s1;
+        if (i < n) s0 = df_fma(s0, df_unpack(v[i]), df_unpack(z[(size_t)i * G + g]));
+        part[rg * G + g] = df_pack(df_add(s0, s1));
         __syncthreads();
         if (t < G) {
-            double s = 0.0;
-            for (int r = 0; r < R; r++) s += part[r * G + t];
-            f[t] = tc * s;
+            df s = df_unpack(part[t]);
+            for (int r = 1; r < R; r++) s = df_add(s, df_unpack(part[r * G + t]));
+            f[t] = df_pack(df_from(tc * df_to(s)));
         }
         __syncthreads();
-        const double fg = f[g];
-        for (i = c2 + 1 + rg; i < n; i += R) z[(size_t)i * G + g] = fma(-fg, v[i], z[(size_t)i * G + g]);
+        const df fg = df_unpack(f[g]);
+        for (i = c2 + 1 + rg; i < n; i += R)
+            z[(size_t)i * G + g] = df_pack(df_fms(df_unpack(z[(size_t)i * G + g]), fg, df_unpack(v[i])));
     }
     __syncthreads();
     for (int gg = 0; gg < ng; gg++) {
         double* o = out + (size_t)b * n * n + (size_t)(n - 1 - (c0 + gg)) * n;
-        for (int i2 = t; i2 < n; i2 += kBT) o[i2] = z[(size_t)i2 * G + gg];
+        for (int i2 = t; i2 < n; i2 += kBT) o[i2] = df_to(df_unpack(z[(size_t)i2 * G + gg]));
     }
 }
 
 }  // namespace
 
-size_t blockeig_tridiag_smem(int n) { return sizeof(double) * ((size_t)(6 + kTW) * n + 48); }
+size_t blockeig_tridiag_smem(int n) { return sizeof(double) * ((size_t)(9 + kTW) * n + 48); }
 
 bool blockeig_supported(int n) {
     return n >= 3 && n <= kMaxN && blockeig_tridiag_smem(n) <= (size_t)max_dynamic_smem((const void*)tridiag_kernel);

@@ -313,6 +313,8 @@ struct opsec_gpu {
     std::string projection = "auto";
     int proj_chunk = 1;
     long long proj_wait = 2000000000LL;  // projection kernels: mbarrier wait bound in cycles
+    bool proj_arcs = true;               // projection: arc-run tables for spherical cells in arc order
+    bool cells_arc_order = false;        // the loaded cells are in arc order (cell = h N3 + f)
     long long fail_alloc = -1;           // opsec_gpu_fail_alloc: device allocations left before one fails
     int cub_exact = 1;
     int az_gemm64 = 0;
@@ -601,6 +603,11 @@ void configure(opsec_gpu* c, const std::map<std::string, std::string>& kv) {
         c->proj_wait = std::strtoll(v.c_str(), &end, 10);
         if (end == v.c_str() || c->proj_wait < 10000000LL)
             fail(OPSEC_ERR_CONFIG, "projection.wait_cycles must be an integer >= 10000000");
+    }
+    if (has("projection.arc_tables")) {
+        const std::string& v = get("projection.arc_tables");
+        if (v != "0" && v != "1") fail(OPSEC_ERR_CONFIG, "projection.arc_tables must be 0 or 1");
+        c->proj_arcs = v == "1";
     }
     if (has("projection.chunk")) c->proj_chunk = to_int("projection.chunk", get("projection.chunk"));
     if (c->proj_chunk < 1) fail(OPSEC_ERR_CONFIG, "projection.chunk must be >= 1");
@@ -1155,6 +1162,9 @@ void load_cells(opsec_gpu* c, int ncells, const opsec_cell* cells) {
         }
         nb[a] = cl.Nbar;
     }
+    c->cells_arc_order = g.coordsys == 2;
+    for (int a = 0; a < ncells && c->cells_arc_order; a++)
+        if (idx[3 * (size_t)ncells + a] * g.n[2] + idx[4 * (size_t)ncells + a] != a) c->cells_arc_order = false;
     c->cell_i.alloc(idx.size());
     c->nbar.alloc(ncells);
     OPSEC_CUDA(cudaMemcpyAsync(c->cell_i.p, idx.data(), sizeof(int) * idx.size(), cudaMemcpyHostToDevice, c->stream));
@@ -1812,6 +1822,8 @@ void project_all(opsec_gpu* c, int ncells, int M, bool own_modes, bool packed = 
     a.Dp = c->Dp.p;
     a.chunk = c->proj_chunk;
     a.wait_cycles = c->proj_wait;
+    const int n3 = c->ks.N3;
+    if (c->proj_arcs && c->cells_arc_order && (n3 == 16 || n3 == 32 || n3 == 64)) a.arc_run = n3;
     bool tc = (c->projection != "simt") && project_tc_supported(a);
     if (c->projection == "tc" && !tc) fail(OPSEC_ERR_CONFIG, "projection=tc requested but the shape is not supported");
     size_t wb = tc ? project_tc_work_bytes(a) : sizeof(float) * (size_t)M * ncells;

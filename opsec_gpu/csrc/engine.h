@@ -224,6 +224,7 @@ struct ProjectArgs {
     size_t work_bytes;
     int chunk = 1;         // tensor-core path: K-slices of 64 per FP32 accumulator chunk
     long long wait_cycles = 2000000000LL;  // bound of every mbarrier wait (~1 s at 2 GHz)
+    int arc_run = 0;       // spherical cells in arc order (cell = h N3 + f): N3 when it is 16, 32 or 64
 };
 size_t project_work_bytes(const ProjectArgs& a);
 // The projection kernels' bounded mbarrier wait on a barrier that nothing (arrive = 0) or one

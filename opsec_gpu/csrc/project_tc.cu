@@ -241,7 +241,26 @@ struct Step1Params {
     int chunk;                // K-slices per accumulator chunk
     int* err;
     long long wait_cycles;  // bound of every mbarrier wait
+    int arcs;                 // > 0: cells in arc order with this many phi cells per arc (a divisor of BK)
 };
+
+// Arc-run tables of the spherical gather: when the cells are in arc order (cell = h N3 + f) and
+// N3 divides BK (and so BM), the 128 x 64 A tile of a K-slice spans BM/N3 row arcs and BK/N3
+// column arcs, and every element is Q(h_a, h_b, |f_a - f_b|): one run of nf consecutive words
+// of the square table per arc pair.  Each producer warp loads those runs (at most kArcTab words,
+// N3 >= 16) once per slice into its own buffer and expands its rows of the tile from there.
+constexpr int kArcTab = 288;  // (BM/16) (BK/16) 9 words at N3 = 16, the smallest arc run allowed
+
+__device__ __forceinline__ int arc_table_size(const KeySpace& ks, int n3) { return (BM / n3) * (BK / n3) * ks.nf; }
+
+__device__ __forceinline__ uint32_t arc_table_word(const KeySpace& ks, const uint32_t* Qhl, int n3, int a0, int k,
+                                                   int e) {
+    const int nca = BK / n3;
+    const int df = e % ks.nf, pr = e / ks.nf, ca = pr % nca, ra = pr / nca;
+    const int ha = a0 / n3 + ra, hb = (k * BK) / n3 + ca;
+    if (ha >= ks.H || hb >= ks.H) return 0u;  // padding rows and columns
+    return __ldg(Qhl + ((size_t)ha * ks.H + hb) * ks.nf + df);
+}
 
 __device__ __forceinline__ int pair_key(const KeySpace& ks, int4 a, int4 b) {
     if (ks.coordsys == 1) {
@@ -331,6 +350,60 @@ __global__ void __launch_bounds__(512, 1)
 #pragma unroll
                        for (int t = 0; t < 32; t++) p.Tf[(size_t)(j0 + 32 * cc + t) * p.Npad + a] = v[t] * p.out_scale;
                    });
+    } else if (warp < 10 && p.arcs > 0) {
+        // eight producers expanding arc-run tables (see arc_table_word): each warp loads slice
+        // k+1's table into registers while it expands slice k from its own shared buffer.
+        const int pw = warp - 2, n3 = p.arcs;
+        uint32_t* tab = reinterpret_cast<uint32_t*>(smem + STAGES * STAGE_BYTES) + pw * 2 * kArcTab;  // [2][kArcTab]
+        const int T = arc_table_size(p.ks, n3);
+        constexpr int kPer = kArcTab / 32;
+        uint32_t nxt[kPer];
+        auto load = [&](int k) {
+#pragma unroll
+            for (int q = 0; q < kPer; q++) {
+                const int e = lane + 32 * q;
+                nxt[q] = e < T ? arc_table_word(p.ks, p.Qhl, n3, a0, k, e) : 0u;
+            }
+        };
+        auto store = [&](int buf) {
+#pragma unroll
+            for (int q = 0; q < kPer; q++) tab[buf * kArcTab + lane + 32 * q] = nxt[q];
+        };
+        if (nk > 0) {
+            load(0);
+            store(0);
+        }
+        const int nca = BK / n3;
+        const int c0 = 2 * lane, c1 = c0 + 1;
+        const int ca0 = c0 / n3, fb0 = c0 % n3, ca1 = c1 / n3, fb1 = c1 % n3;
+        for (int k = 0; k < nk; k++) {
+            __syncwarp();  // table k complete in this warp's buffer
+            if (k + 1 < nk) load(k + 1);
+            const int s = k % STAGES, n = k / STAGES;
+            if (n > 0 && !mbar_wait(smem_u32(&bar_empty[s]), (n - 1) & 1, &abort_flag, p.err, p.wait_cycles)) break;
+            const uint32_t* tb = tab + (k & 1) * kArcTab;
+            unsigned char* ahi = A_hi(s);
+            unsigned char* alo = A_lo(s);
+#pragma unroll
+            for (int i = 0; i < BM / 8; i++) {
+                const int r = pw + 8 * i;
+                const int ra = r / n3, fa = r % n3;
+                int d0 = abs(fa - fb0), d1 = abs(fa - fb1);
+                if (p.ks.fold) {
+                    d0 = min(d0, n3 - d0);
+                    d1 = min(d1, n3 - d1);
+                }
+                const uint32_t x0 = tb[(ra * nca + ca0) * p.ks.nf + d0];
+                const uint32_t x1 = tb[(ra * nca + ca1) * p.ks.nf + d1];
+                const uint32_t off = (r >> 3) * 1024 + (r & 7) * 128 + ((((uint32_t)lane >> 2) ^ (r & 7)) << 4) + (lane & 3) * 4;
+                *reinterpret_cast<uint32_t*>(ahi + off) = __byte_perm(x0, x1, 0x5410);  // (hi0, hi1)
+                *reinterpret_cast<uint32_t*>(alo + off) = __byte_perm(x0, x1, 0x7632);  // (lo0, lo1)
+            }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            __syncwarp();  // also: every lane is done reading buffer k & 1 before it is refilled
+            if (lane == 0) mbar_arrive(smem_u32(&bar_full[s]));
+            if (k + 1 < nk) store((k + 1) & 1);
+        }
     } else if (warp < 10) {
         // eight gather producers: warp pw fills rows pw, pw+8, ...; lane covers columns 2 lane, 2 lane + 1.
         // Software-pipelined: the 32 gathers of K-slice k+1 are in flight while the warp waits for
@@ -682,7 +755,7 @@ void launch_project_tc(const ProjectArgs& a, cudaStream_t s, long long* launches
     const CUtensorMap mBh128 = make_map(Bh, L.Mpad, L.Npad, BM), mBl128 = make_map(Bl, L.Mpad, L.Npad, BM);
     const CUtensorMap mTh256 = make_map(Th, L.Mpad, L.Npad, BN), mTl256 = make_map(Tl, L.Mpad, L.Npad, BN);
 
-    const size_t smem = (size_t)STAGES * STAGE_BYTES + 1024;
+    const size_t smem = (size_t)STAGES * STAGE_BYTES + 1024 + sizeof(uint32_t) * 8 * 2 * kArcTab;
     OPSEC_CUDA(cudaFuncSetAttribute(step1_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     OPSEC_CUDA(cudaFuncSetAttribute(step2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
 
@@ -705,6 +778,7 @@ void launch_project_tc(const ProjectArgs& a, cudaStream_t s, long long* launches
         p1.chunk = a.chunk;
         p1.err = err;
         p1.wait_cycles = a.wait_cycles;
+        p1.arcs = a.arc_run;
         if (g_clock) g_clock->begin("project_step1", s, 2.0 * N * (double)N * M);
         step1_kernel<<<n_at * n_jt, 512, smem, s>>>(mBh256, mBl256, p1);
         OPSEC_CUDA(cudaGetLastError());

@@ -51,6 +51,7 @@ BAD = [
     ("projection.wait_cycles = 1000", "projection.wait_cycles"),
     ("projection.wait_cycles = soon", "projection.wait_cycles"),
     ("azimuthal.eig = lapack", "azimuthal.eig"),
+    ("projection.arc_tables = 2", "projection.arc_tables"),
 ]
 
 

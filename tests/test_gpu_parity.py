@@ -418,3 +418,25 @@ def test_block_eigensolver_matches_library(dims):
     print(f"{dims}: {st['block']} eigenvectors computed for {M} modes; eigenvalues {d_ev:.2e}, "
           f"span sin {sin:.2e}, F {d_F:.2e}")
     assert d_ev <= 1e-12 and sin <= 1e-8 and d_F <= 1e-9, (d_ev, sin, d_F)
+
+
+@pytest.mark.parametrize("dims", [(4, 4, 16), (3, 4, 32), (2, 2, 64)])
+def test_projection_arc_tables(dims):
+    """The tensor-core projection's arc-run gather (cells in arc order, 16, 32 or 64 phi cells
+    per arc: each K-slice's tile expanded from the runs of the square key table it spans)
+    against the general per-element gather: bit for bit, and both against the oracle."""
+    sv, cells = synth.shell_survey(*dims)
+    bands = synth.band_edges(3, 0.0, 0.3)
+    tabs = O.xi_tables(*PK, bands)
+    Q = O.qtable_keys(sv, O.keys_all(sv), tabs)
+    _, modes = O.klt(O.signal_matrix(sv, cells, Q[:, 0]), 40)
+    out = {}
+    for arcs in ("1", "0"):
+        e = api.Engine(api.make_config(sv, bands=bands, extra=["projection = tc", f"projection.arc_tables = {arcs}"]))
+        e.set_pk(*PK)
+        out[arcs] = e.comma(cells, modes)
+        e.close()
+    np.testing.assert_array_equal(out["1"], out["0"])
+    for p in range(len(bands)):
+        ref = O.project(modes, O.signal_matrix(sv, cells, Q[:, 1 + p]))
+        assert np.max(np.abs(out["1"][p] - ref)) <= 1e-5 * np.max(np.abs(ref)), p
