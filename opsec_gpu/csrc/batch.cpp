@@ -24,12 +24,11 @@ void run_mock(opsec_gpu* w, const opsec_mock& m, size_t i, int nb, double* F, do
     w->q_ok = w->qsq_ok = false;
     build_tables(w);  // no-op: the tables do not depend on the grid
     build_q(w);
-    const int n = eigensolve(w, m.ncells, m.cells, m.nmodes);
+    const int n = eigensolve(w, m.ncells, m.cells, m.nmodes, false);
     project_all(w, m.ncells, n, true, false);
     w->counts.alloc(m.ncells);
-    w->y.alloc(n);
     OPSEC_CUDA(cudaMemcpyAsync(w->counts.p, m.counts, sizeof(double) * m.ncells, cudaMemcpyHostToDevice, w->stream));
-    launch_dot(m.ncells, n, w->modes.p, w->counts.p, w->nbar.p, w->y.p, w->stream, &w->launches);
+    pixel_projection(w, m.ncells, n);
     const size_t n2 = (size_t)nb * nb;
     fisher_and_epilogue(w, n, w->az_blockF ? nullptr : w->Dp.p, nullptr, OPSEC_MIXING_INVERSE, phat ? phat + i * nb : nullptr,
                         pcov ? pcov + i * n2 : nullptr, F ? F + i * n2 : nullptr, nullptr, nullptr, nullptr, nullptr);

@@ -418,6 +418,7 @@ int opsec_gpu_comma(opsec_gpu* c, int ncells, const opsec_cell* cells, int nmode
         build_qsq(c);
         load_cells(c, ncells, cells);
         c->modes.alloc((size_t)nmodes * ncells);
+        c->modes_ok = false;  // the caller's modes, not the last eigensolve's
         OPSEC_CUDA(cudaMemcpyAsync(c->modes.p, modes, sizeof(double) * (size_t)nmodes * ncells, cudaMemcpyHostToDevice,
                                    c->stream));
         project_all(c, ncells, nmodes, false);
@@ -435,6 +436,7 @@ int opsec_gpu_dot(opsec_gpu* c, int ncells, const opsec_cell* cells, const doubl
         if (nmodes <= 0 || !counts || !modes || !y) fail(OPSEC_ERR_ARG, "invalid dot arguments");
         load_cells(c, ncells, cells);
         c->modes.alloc((size_t)nmodes * ncells);
+        c->modes_ok = false;  // the caller's modes, not the last eigensolve's
         c->counts.alloc(ncells);
         c->y.alloc(nmodes);
         OPSEC_CUDA(cudaMemcpyAsync(c->modes.p, modes, sizeof(double) * (size_t)nmodes * ncells, cudaMemcpyHostToDevice,
@@ -728,13 +730,12 @@ int opsec_gpu_fisher_build(opsec_gpu* c, int ncells, const opsec_cell* cells, co
         t.mark();
         build_q(c);
         t.mark();
-        int n = eigensolve(c, ncells, cells, nmodes);
+        int n = eigensolve(c, ncells, cells, nmodes, false);
         t.mark();
         project_all(c, ncells, n, true, false);
         c->counts.alloc(ncells);
-        c->y.alloc(n);
         OPSEC_CUDA(cudaMemcpyAsync(c->counts.p, counts, sizeof(double) * ncells, cudaMemcpyHostToDevice, c->stream));
-        launch_dot(ncells, n, c->modes.p, c->counts.p, c->nbar.p, c->y.p, c->stream, &c->launches);
+        pixel_projection(c, ncells, n);
         t.mark();
         if (evals) OPSEC_CUDA(cudaMemcpyAsync(evals, c->evals.p, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
         fisher_and_epilogue(c, n, c->az_blockF ? nullptr : c->Dp.p, nullptr, mixing, phat, pcov, F, W, M, q, f);

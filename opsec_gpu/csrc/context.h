@@ -87,6 +87,8 @@ struct opsec_gpu {
     long long proj_wait = 2000000000LL;  // projection kernels: mbarrier wait bound in cycles
     bool proj_arcs = true;               // projection: arc-run tables for spherical cells in arc order
     bool cells_arc_order = false;        // the loaded cells are in arc order (cell = h N3 + f)
+    bool modes_ok = false;               // c->modes holds the modes of the last eigensolve
+    DevBuf<double> arc_x;                // per-arc trig sums of the pixel values
     long long fail_alloc = -1;           // opsec_gpu_fail_alloc: device allocations left before one fails
     int cub_exact = 1;
     int az_gemm64 = 0;
@@ -207,7 +209,12 @@ void load_cells(opsec_gpu* c, int ncells, const opsec_cell* cells);
 CellKeyInfo cell_info(opsec_gpu* c);
 bool azimuthal_ok(opsec_gpu* c, int ncells, const opsec_cell* cells);
 void drop_eig_graph(opsec_gpu* c);
-int eigensolve(opsec_gpu* c, int ncells, const opsec_cell* cells, int M);
+// want_modes = false leaves the mode matrix unformed on the azimuthal path (ensure_modes forms it
+// from the kept block eigenvectors when a later step needs it)
+int eigensolve(opsec_gpu* c, int ncells, const opsec_cell* cells, int M, bool want_modes = true);
+void ensure_modes(opsec_gpu* c);
+// y = B^T (N - Nbar)/sqrt(Nbar) for the modes of the last eigensolve (counts already on the device)
+void pixel_projection(opsec_gpu* c, int ncells, int n);
 void project_all(opsec_gpu* c, int ncells, int M, bool own_modes, bool packed = true);
 std::vector<double> priors(opsec_gpu* c);
 void fisher_and_epilogue(opsec_gpu* c, int M, const float* Dp32, const double* Dp64, int mixing, double* phat,

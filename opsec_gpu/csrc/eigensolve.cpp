@@ -139,7 +139,7 @@ void forget_device_state(opsec_gpu* c) {
     drop_eig_graph(c);
 }
 
-int eigensolve(opsec_gpu* c, int ncells, const opsec_cell* cells, int M) {
+int eigensolve(opsec_gpu* c, int ncells, const opsec_cell* cells, int M, bool want_modes) {
     build_q(c);
     load_cells(c, ncells, cells);
     if (M <= 0 || M > ncells) fail(OPSEC_ERR_ARG, "Nmodes must be in [1, Ncells]");
@@ -345,8 +345,12 @@ int eigensolve(opsec_gpu* c, int ncells, const opsec_cell* cells, int M) {
         c->sel.alloc(sel.size());
         OPSEC_CUDA(cudaMemcpyAsync(c->sel.p, sel.data(), sizeof(int) * sel.size(), cudaMemcpyHostToDevice, c->stream));
         OPSEC_CUDA(cudaMemcpyAsync(c->evals.p, ev.data(), sizeof(double) * M, cudaMemcpyHostToDevice, c->stream));
-        launch_assemble_modes(H, Nphi, Nmu, npar, M, c->sel.p, c->sel.p + M, c->sel.p + 2 * M, c->S.p, c->modes.p,
-                              c->stream, &c->launches);
+        c->modes_ok = false;
+        if (want_modes) {
+            launch_assemble_modes(H, Nphi, Nmu, npar, M, c->sel.p, c->sel.p + M, c->sel.p + 2 * M, c->S.p,
+                                  c->modes.p, c->stream, &c->launches);
+            c->modes_ok = true;
+        }
         sync(c);
         c->az_m.assign(sel.begin(), sel.begin() + M);
         c->az_idx.assign(sel.begin() + M, sel.begin() + 2 * M);
@@ -355,6 +359,7 @@ int eigensolve(opsec_gpu* c, int ncells, const opsec_cell* cells, int M) {
         return M;
     }
     drop_eig_graph(c);
+    c->modes_ok = true;  // the dense and iterative solvers write the modes directly
     // dense path: S in FP64, top-M by syevdx or by subspace iteration (klt.cpp:173-248 via PARPACK there)
     const int N = ncells;
     c->S.alloc((size_t)N * N);
@@ -408,3 +413,27 @@ int eigensolve(opsec_gpu* c, int ncells, const opsec_cell* cells, int M) {
     sync(c);
     return M;
 }
+
+void ensure_modes(opsec_gpu* c) {
+    if (c->modes_ok) return;
+    if (!c->az_valid) fail(OPSEC_ERR_STATE, "no modes: run the eigensolve first");
+    const KeySpace& ks = c->ks;
+    const int M = (int)c->az_m.size();
+    launch_assemble_modes(ks.H, ks.N3, ks.N2, c->az_npar, M, c->sel.p, c->sel.p + M, c->sel.p + 2 * M, c->S.p,
+                          c->modes.p, c->stream, &c->launches);
+    c->modes_ok = true;
+}
+
+void pixel_projection(opsec_gpu* c, int ncells, int n) {
+    c->y.alloc(n);
+    if (!c->modes_ok && c->az_valid) {
+        const KeySpace& ks = c->ks;
+        c->arc_x.alloc((size_t)2 * ks.H * (ks.N3 / 2 + 1));
+        launch_dot_azimuthal(ks.H, ks.N3, ks.N2, c->az_npar, n, c->sel.p, c->sel.p + n, c->sel.p + 2 * n, c->S.p,
+                             c->counts.p, c->nbar.p, c->arc_x.p, c->y.p, c->stream, &c->launches);
+        return;
+    }
+    ensure_modes(c);
+    launch_dot(ncells, n, c->modes.p, c->counts.p, c->nbar.p, c->y.p, c->stream, &c->launches);
+}
+

@@ -145,7 +145,8 @@ struct XiTableArgs {
     double* r;              // [n] out
     double* xi64;           // [1+nbands][n] out
     float* xi32;            // [1+nbands][n] out
-    double* scratch;        // >= 2 (32769 + nbands*8193) doubles: Simpson weights, then weights / k
+    double* scratch;        // >= 3 (32769 + nbands*8193) doubles: Simpson weights, weights / k, and
+                            // weights / k as (hi, lo) float pairs
 };
 void launch_xi_tables(const XiTableArgs& a, cudaStream_t s, long long* launches);
 
@@ -306,6 +307,11 @@ void launch_epilogue(int nb, int mixing, const double* Fqf, double* out, int* st
 
 // y_i = sum_a B_ia (N_a - Nbar_a) / sqrt(Nbar_a)
 // y = B^T x with x = (N - Nbar) / sqrt(Nbar) formed in place of `counts`
+// y = B^T x on the azimuthal modes of the last block eigensolve, from the block eigenvectors U
+// (no mode matrix); X: 2 H (Nphi/2 + 1) doubles of scratch.  counts are read, not changed.
+void launch_dot_azimuthal(int H, int Nphi, int Nmu, int npar, int nmodes, const int* sel_b, const int* sel_idx,
+                          const int* sel_kind, const double* U, const double* counts, const double* nbar, double* X,
+                          double* y, cudaStream_t s, long long* l);
 void launch_dot(int ncells, int nmodes, const double* modes, double* counts, const double* nbar, double* y,
                 cudaStream_t s, long long* launches);
 

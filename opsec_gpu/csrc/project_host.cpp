@@ -219,6 +219,7 @@ void project_all(opsec_gpu* c, int ncells, int M, bool own_modes, bool packed) {
     if (c->projection == "azimuthal")
         fail(OPSEC_ERR_CONFIG, "projection=azimuthal needs a full-sky spherical build on its own modes");
     build_qsq(c);
+    if (own_modes) ensure_modes(c);
     const int nb = c->ntab() - 1;
     c->Bs.alloc((size_t)M * ncells);
     launch_scale_modes(ncells, M, c->modes.p, c->nbar.p, c->Bs.p, c->stream, &c->launches);

@@ -230,6 +230,57 @@ __global__ void dot_kernel(int ncells, int nmodes, const double* modes, const do
     if (lane == 0) y[warp] = acc;
 }
 
+// Pixel values on the azimuthal modes without forming them (dot.cpp:120-152 on the modes that
+// assemble_modes_kernel would write): a mode is u_b[x] (the block eigenvector, + or - on the
+// mu-reflected arcs) times cos or sin of order m over phi, so y_i = sum_h u(i, h) X(h, kind, m)
+// with X the per-arc trig sums of the pixel values x = (N - Nbar)/sqrt(Nbar).
+// Grid: one thread per (arc, order); X[h][m] = (cos sum, sin sum) with the modes' scales.
+__global__ void arc_trig_sums_kernel(int H, int Nphi, const double* counts, const double* nbar, double2* X) {
+    const int nm = Nphi / 2 + 1;
+    const double c0 = 1.0 / sqrt((double)Nphi), c1 = sqrt(2.0 / Nphi);
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < H * nm; e += gridDim.x * blockDim.x) {
+        const int h = e / nm, m = e % nm;
+        double sc = 0.0, ss = 0.0;
+        for (int f = 0; f < Nphi; f++) {
+            const int a = h * Nphi + f;
+            const double x = (counts[a] - nbar[a]) / sqrt(nbar[a]);
+            const int mf = (int)(((long long)m * f) % Nphi);
+            sc = fma(x, cospi(2.0 * mf / Nphi), sc);
+            ss = fma(x, sinpi(2.0 * mf / Nphi), ss);
+        }
+        const bool edge = m == 0 || 2 * m == Nphi;
+        X[e] = make_double2(sc * (edge ? c0 : c1), ss * c1);
+    }
+}
+
+// One warp per mode: y_i = sum over the block's arcs x of u_b[x] (X(h1) +/- X(h2)) / sqrt 2 with
+// h1, h2 the arc and its mu reflection (npar = 2), or sum_h u_b[h] X(h) (npar = 1).
+__global__ void azimuthal_dot_kernel(int H, int Nphi, int Nmu, int npar, int nmodes, const int* sel_b,
+                                     const int* sel_idx, const int* sel_kind, const double* U, const double2* X,
+                                     double* y) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (warp >= nmodes) return;
+    const int nm = Nphi / 2 + 1, Hb = H / npar, half = Nmu / npar;
+    const int b = sel_b[warp], m = b / npar, kind = sel_kind[warp];
+    const double* u = U + (size_t)b * Hb * Hb + (size_t)sel_idx[warp] * Hb;
+    const double cp = npar == 2 ? sqrt(0.5) : 1.0, sg = (npar == 2 && (b & 1)) ? -1.0 : 1.0;
+    double acc = 0.0;
+    for (int x = lane; x < Hb; x += 32) {
+        const int hr = x / half, j = x % half;
+        const int h1 = hr * Nmu + j;
+        const double2 a1 = X[(size_t)h1 * nm + m];
+        double v = kind == 2 ? a1.y : a1.x;  // kinds 0, 1, 3 use the cos sum (order 0 and Nphi/2 included)
+        if (npar == 2) {
+            const double2 a2 = X[(size_t)(hr * Nmu + (Nmu - 1 - j)) * nm + m];
+            v += sg * (kind == 2 ? a2.y : a2.x);
+        }
+        acc = fma(u[x] * cp, v, acc);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) y[warp] = acc;
+}
+
 // modes[i][a] = A[(M-1-i)*lda + a], evals[i] = w[M-1-i]: syevdx returns ascending order
 __global__ void reverse_modes_kernel(int n, int m, int lda, const double* A, const double* w, double* modes,
                                      double* evals) {
@@ -435,6 +486,18 @@ void launch_dot(int ncells, int nmodes, const double* modes, double* counts, con
                 cudaStream_t s, long long* l) {
     pixel_values_kernel<<<grid_for(ncells), 256, 0, s>>>(ncells, counts, nbar);
     dot_kernel<<<(nmodes * 32 + 255) / 256, 256, 0, s>>>(ncells, nmodes, modes, counts, y);
+    OPSEC_CUDA(cudaGetLastError());
+    *l += 2;
+}
+
+void launch_dot_azimuthal(int H, int Nphi, int Nmu, int npar, int nmodes, const int* sel_b, const int* sel_idx,
+                          const int* sel_kind, const double* U, const double* counts, const double* nbar, double* X,
+                          double* y, cudaStream_t s, long long* l) {
+    const int nm = Nphi / 2 + 1;
+    double2* X2 = reinterpret_cast<double2*>(X);
+    arc_trig_sums_kernel<<<grid_for((long long)H * nm), 256, 0, s>>>(H, Nphi, counts, nbar, X2);
+    azimuthal_dot_kernel<<<(nmodes * 32 + 255) / 256, 256, 0, s>>>(H, Nphi, Nmu, npar, nmodes, sel_b, sel_idx,
+                                                                     sel_kind, U, X2, y);
     OPSEC_CUDA(cudaGetLastError());
     *l += 2;
 }

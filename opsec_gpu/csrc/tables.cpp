@@ -26,7 +26,7 @@ void build_tables(opsec_gpu* c) {
     OPSEC_CUDA(cudaMemcpyAsync(c->r_grid.p, r.data(), sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
     c->xi64.alloc((size_t)ntab * n);
     c->xi32.alloc((size_t)ntab * n);
-    c->scratch.alloc(2 * ((size_t)32769 + (size_t)nb * 8193));
+    c->scratch.alloc(3 * ((size_t)32769 + (size_t)nb * 8193));  // weights, weights / k, (weights / k) as float pairs
     XiTableArgs a;
     a.xl = c->xl;
     a.nbands = nb;

@@ -9,6 +9,7 @@
 // band table contributes nothing, as in the reference.
 #include <cmath>
 
+#include "df64.h"
 #include "engine.h"
 
 namespace opsec {
@@ -66,12 +67,14 @@ __global__ void simpson_weights_kernel(XiTableArgs a) {
         mult *= P * (k * k) * exp(-k * k / (1.0 * 1.0));
         mult *= (dk / 3) / kTwoPi2;
         a.scratch[s.off + j] = mult;
-        a.scratch[s.off + j + scratch_half(a)] = (k > 0.0) ? mult / k : 0.0;  // for sin(kr)/(kr) = (1/k) sin(kr) / r
+        const double mk = (k > 0.0) ? mult / k : 0.0;  // for sin(kr)/(kr) = (1/k) sin(kr) / r
+        a.scratch[s.off + j + scratch_half(a)] = mk;
+        reinterpret_cast<float2*>(a.scratch + 2 * scratch_half(a))[s.off + j] = df_pack(df_from(mk));
     }
 }
 
 constexpr int kRPerWarp = 4;   // r values per warp; each weight load feeds all of them
-constexpr int kAnchor = 32;    // Chebyshev steps per lane between rotation anchors
+constexpr int kAnchor = 16;    // Chebyshev steps per lane between rotation anchors
 
 // One warp per (table, 4 consecutive r): sum_j mult_j j0(k_j r), FP64.
 //
@@ -97,15 +100,18 @@ __global__ void xi_sum_kernel(XiTableArgs a) {
     const double dk = (s.kmax - s.kmin) / s.nk;
     const double* mult = a.scratch + s.off;
     const double* minv = a.scratch + s.off + scratch_half(a);
+    const float2* minv2 = reinterpret_cast<const float2*>(a.scratch + 2 * scratch_half(a)) + s.off;
     const int nk = s.nk;
 
     double r[kRPerWarp], acc_series[kRPerWarp], acc_sin[kRPerWarp];
+    df acc_rec[kRPerWarp];
     int jc = 0;
 #pragma unroll
     for (int q = 0; q < kRPerWarp; q++) {
         r[q] = a.r[min(i0 + q, n - 1)];  // past the end: a copy of the last r, not stored
         acc_series[q] = 0.0;
         acc_sin[q] = 0.0;
+        acc_rec[q] = df{0.f, 0.f};
         // first j with (kmin + j dk) r >= 0.01, from below; the prefix loop tests each term exactly
         if (r[q] > 0.0) {
             const double jf = (0.01 / r[q] - s.kmin) / dk;
@@ -142,20 +148,25 @@ __global__ void xi_sum_kernel(XiTableArgs a) {
             c2[q] = 2.0 * cth[q];
             sincos((s.kmin + (jc + lane) * dk) * r[q], &sn[q], &cs[q]);
         }
+        df c2d[kRPerWarp];
+#pragma unroll
+        for (int q = 0; q < kRPerWarp; q++) c2d[q] = df_from(c2[q]);
         for (int j0 = jc + lane; j0 <= nk; j0 += 32 * kAnchor) {
-            double cur[kRPerWarp], prev[kRPerWarp];
+            // the recurrence and its sum in double-FP32 (FP64 instructions issue at 1/64 of the
+            // FP32 rate here); the anchors stay FP64
+            df cur[kRPerWarp], prev[kRPerWarp];
 #pragma unroll
             for (int q = 0; q < kRPerWarp; q++) {
-                cur[q] = sn[q];
-                prev[q] = sn[q] * cth[q] - cs[q] * sth[q];  // sin(x - theta)
+                cur[q] = df_from(sn[q]);
+                prev[q] = df_from(sn[q] * cth[q] - cs[q] * sth[q]);  // sin(x - theta)
             }
             const int steps = min(kAnchor, (nk - j0) / 32 + 1);
             for (int m = 0; m < steps; m++) {
-                const double w = minv[j0 + 32 * m];
+                const df w = df_unpack(minv2[j0 + 32 * m]);
 #pragma unroll
                 for (int q = 0; q < kRPerWarp; q++) {
-                    acc_sin[q] = fma(w, cur[q], acc_sin[q]);
-                    const double nxt = fma(c2[q], cur[q], -prev[q]);
+                    acc_rec[q] = df_fma(acc_rec[q], w, cur[q]);
+                    const df nxt = df_fma(df{-prev[q].h, -prev[q].l}, c2d[q], cur[q]);
                     prev[q] = cur[q];
                     cur[q] = nxt;
                 }
@@ -171,7 +182,8 @@ __global__ void xi_sum_kernel(XiTableArgs a) {
 
 #pragma unroll
     for (int q = 0; q < kRPerWarp; q++) {
-        double acc = (r[q] > 0.0) ? acc_series[q] + acc_sin[q] / r[q] : acc_series[q];
+        const double sins = acc_sin[q] + df_to(acc_rec[q]);
+        double acc = (r[q] > 0.0) ? acc_series[q] + sins / r[q] : acc_series[q];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
         if (lane == 0 && i0 + q < n) {
