@@ -42,12 +42,6 @@ constexpr int TMEM_COLS = 512;  // [0,256) accumulator D, [256,512) running sum 
 
 // instruction descriptor: D=F32, A=B=F16, both K-major, M=128, N=256
 constexpr uint32_t kIdesc = (1u << 4) | (0u << 7) | (0u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
-// step 1: N = 128 tiles, three stages, two TMEM accumulators (D0, D1) and the running sum R
-constexpr int BN1 = 128;
-constexpr int STAGES1 = 3;
-constexpr uint32_t B1_BYTES = BN1 * BK * 2;  // 16 KB
-constexpr uint32_t STAGE1_BYTES = 2 * A_BYTES + 2 * B1_BYTES;
-constexpr uint32_t kIdesc1 = (1u << 4) | ((uint32_t)(BN1 >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -107,11 +101,10 @@ __device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
     return d;
 }
 
-__device__ __forceinline__ void umma(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t accumulate,
-                                     uint32_t idesc = kIdesc) {
+__device__ __forceinline__ void umma(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t accumulate) {
     asm volatile(
         "{ .reg .pred p; setp.ne.b32 p, %4, 0; tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p; }" ::"r"(tmem_d),
-        "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+        "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate));
 }
 __device__ __forceinline__ void umma_commit(uint32_t mbar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar) : "memory");
@@ -209,17 +202,17 @@ __device__ __forceinline__ void drain_loop(uint32_t tmem, int q, int lane, int n
 // are issued first, while D is small, so only the four main-term MMAs of a
 // slice add bias at the scale of the result.
 __device__ __forceinline__ void issue_slice(uint32_t tmem, uint64_t ah, uint64_t al, uint64_t bh, uint64_t bl,
-                                            bool first_in_chunk, uint32_t idesc = kIdesc) {
+                                            bool first_in_chunk) {
 #pragma unroll
     for (int kk = 0; kk < BK / 16; kk++) {
         const uint64_t adv = (uint64_t)(kk * 32) >> 4;
-        umma(tmem, ah + adv, bl + adv, (!first_in_chunk || kk > 0) ? 1u : 0u, idesc);
-        umma(tmem, al + adv, bh + adv, 1u, idesc);
+        umma(tmem, ah + adv, bl + adv, (!first_in_chunk || kk > 0) ? 1u : 0u);
+        umma(tmem, al + adv, bh + adv, 1u);
     }
 #pragma unroll
     for (int kk = 0; kk < BK / 16; kk++) {
         const uint64_t adv = (uint64_t)(kk * 32) >> 4;
-        umma(tmem, ah + adv, bh + adv, 1u, idesc);
+        umma(tmem, ah + adv, bh + adv, 1u);
     }
 }
 
@@ -279,35 +272,31 @@ __device__ __forceinline__ int pair_key(const KeySpace& ks, int4 a, int4 b) {
     return a.x * ks.H + b.x + df;  // a.x = h_a nf, b.x = h_b nf
 }
 
-// warps: 0 TMA, 1 MMA, 2-9 gather producers, 10-11 idle, 12-15 drain + epilogue (lane quarters 0-3).
-// Tiles of 128 cells x 128 modes; two TMEM accumulators, so the MMAs of chunk c+1 (into D of
-// parity c+1) run while the drain warps add chunk c's D into the running sum R.
+// warps: 0 TMA, 1 MMA, 2-9 gather producers, 10-11 idle, 12-15 drain + epilogue (lane quarters 0-3)
 __global__ void __launch_bounds__(512, 1)
     step1_kernel(const __grid_constant__ CUtensorMap mBh, const __grid_constant__ CUtensorMap mBl, Step1Params p) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    __shared__ __align__(8) unsigned long long bar_full[STAGES1], bar_empty[STAGES1], bar_chunk[2], bar_drained[2];
+    __shared__ __align__(8) unsigned long long bar_full[STAGES], bar_empty[STAGES], bar_chunk, bar_drained;
     __shared__ uint32_t tmem_slot;
     __shared__ volatile int abort_flag;
     __shared__ int4 rowkey[BM];
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int jt = blockIdx.x / p.n_at, at = blockIdx.x % p.n_at;
-    const int a0 = at * BM, j0 = jt * BN1;
+    const int a0 = at * BM, j0 = jt * BN;
     const int nk = p.Npad / BK;
     const int chunk = p.chunk > 0 ? p.chunk : 1;
     const int nchunks = (nk + chunk - 1) / chunk;
 
     if (threadIdx.x == 0) {
         abort_flag = 0;
-        for (int s = 0; s < STAGES1; s++) {
+        for (int s = 0; s < STAGES; s++) {
             mbar_init(smem_u32(&bar_full[s]), 1 + 8);
             mbar_init(smem_u32(&bar_empty[s]), 1);
         }
-        for (int b = 0; b < 2; b++) {
-            mbar_init(smem_u32(&bar_chunk[b]), 1);
-            mbar_init(smem_u32(&bar_drained[b]), 4);
-        }
+        mbar_init(smem_u32(&bar_chunk), 1);
+        mbar_init(smem_u32(&bar_drained), 4);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (threadIdx.x < BM) rowkey[threadIdx.x] = p.ckey[a0 + threadIdx.x];
@@ -317,81 +306,55 @@ __global__ void __launch_bounds__(512, 1)
     tc_fence_after();
     const uint32_t tmem = tmem_slot;
 
-    auto A_hi = [&](int s) { return smem + s * STAGE1_BYTES; };
-    auto A_lo = [&](int s) { return smem + s * STAGE1_BYTES + A_BYTES; };
-    auto B_hi = [&](int s) { return smem + s * STAGE1_BYTES + 2 * A_BYTES; };
-    auto B_lo = [&](int s) { return smem + s * STAGE1_BYTES + 2 * A_BYTES + B1_BYTES; };
+    auto A_hi = [&](int s) { return smem + s * STAGE_BYTES; };
+    auto A_lo = [&](int s) { return smem + s * STAGE_BYTES + A_BYTES; };
+    auto B_hi = [&](int s) { return smem + s * STAGE_BYTES + 2 * A_BYTES; };
+    auto B_lo = [&](int s) { return smem + s * STAGE_BYTES + 2 * A_BYTES + B_BYTES; };
 
     if (warp == 0) {
         // TMA producer for B' hi/lo
         if (lane == 0) {
             for (int k = 0; k < nk; k++) {
-                const int s = k % STAGES1, n = k / STAGES1;
+                const int s = k % STAGES, n = k / STAGES;
                 if (n > 0 && !mbar_wait(smem_u32(&bar_empty[s]), (n - 1) & 1, &abort_flag, p.err, p.wait_cycles)) break;
                 const uint32_t fb = smem_u32(&bar_full[s]);
-                mbar_arrive_tx(fb, 2 * B1_BYTES);
+                mbar_arrive_tx(fb, 2 * B_BYTES);
                 tma_load_2d(smem_u32(B_hi(s)), &mBh, fb, k * BK, j0);
                 tma_load_2d(smem_u32(B_lo(s)), &mBl, fb, k * BK, j0);
             }
         }
     } else if (warp == 1) {
-        // MMA issuer: chunk c accumulates into D of parity c & 1
+        // MMA issuer
         for (int k = 0; k < nk; k++) {
-            const int s = k % STAGES1, n = k / STAGES1;
-            const int c = k / chunk, bf = c & 1;
+            const int s = k % STAGES, n = k / STAGES;
             const bool first = (k % chunk) == 0;
-            if (first && c >= 2) {  // this accumulator's previous chunk (c - 2) must be drained first
-                if (!mbar_wait(smem_u32(&bar_drained[bf]), ((c - 2) >> 1) & 1, &abort_flag, p.err, p.wait_cycles))
-                    break;
+            if (first && k > 0) {  // the previous chunk's accumulator must be drained first
+                if (!mbar_wait(smem_u32(&bar_drained), ((k / chunk) - 1) & 1, &abort_flag, p.err, p.wait_cycles)) break;
             }
             if (!mbar_wait(smem_u32(&bar_full[s]), n & 1, &abort_flag, p.err, p.wait_cycles)) break;
             tc_fence_after();
             if (lane == 0) {
-                issue_slice(tmem + (uint32_t)(bf * BN1), sdesc(smem_u32(A_hi(s))), sdesc(smem_u32(A_lo(s))),
-                            sdesc(smem_u32(B_hi(s))), sdesc(smem_u32(B_lo(s))), first, kIdesc1);
+                issue_slice(tmem, sdesc(smem_u32(A_hi(s))), sdesc(smem_u32(A_lo(s))), sdesc(smem_u32(B_hi(s))),
+                            sdesc(smem_u32(B_lo(s))), first);
                 umma_commit(smem_u32(&bar_empty[s]));
-                if ((k % chunk) == chunk - 1 || k == nk - 1) umma_commit(smem_u32(&bar_chunk[bf]));
+                if ((k % chunk) == chunk - 1 || k == nk - 1) umma_commit(smem_u32(&bar_chunk));
             }
             __syncwarp();
         }
     } else if (warp >= 12) {
-        // drain warps + epilogue: R += D of each chunk (round to nearest), T^T[j][a] at the end
+        // drain warps + epilogue: T^T[j][a] in natural units
         const int q = warp & 3;
         const int a = a0 + 32 * q + lane;
-        const uint32_t lane_base = (uint32_t)(32 * q) << 16;
-        for (int c = 0; c < nchunks; c++) {
-            const int bf = c & 1;
-            if (!mbar_wait(smem_u32(&bar_chunk[bf]), (c >> 1) & 1, &abort_flag, p.err, p.wait_cycles)) break;
-            tc_fence_after();
-            const bool last = (c == nchunks - 1);
-            for (int cc = 0; cc < BN1 / 32; cc++) {
-                float v[32];
-                tmem_ld32(tmem + lane_base + (uint32_t)(bf * BN1 + 32 * cc), v);
-                if (c > 0) {
-                    float r[32];
-                    tmem_ld32(tmem + lane_base + (uint32_t)(2 * BN1 + 32 * cc), r);
+        drain_loop(tmem, q, lane, nchunks, ChunkBars{smem_u32(&bar_chunk), smem_u32(&bar_drained), p.wait_cycles}, &abort_flag,
+                   p.err, [&](int cc, const float* v) {
 #pragma unroll
-                    for (int t = 0; t < 32; t++) v[t] += r[t];
-                }
-                if (last) {
-#pragma unroll
-                    for (int t = 0; t < 32; t++) p.Tf[(size_t)(j0 + 32 * cc + t) * p.Npad + a] = v[t] * p.out_scale;
-                } else {
-                    tmem_st32(tmem + lane_base + (uint32_t)(2 * BN1 + 32 * cc), v);
-                }
-            }
-            if (!last) {
-                tmem_wait_st();
-                tc_fence_before();
-                __syncwarp();
-                if (lane == 0) mbar_arrive(smem_u32(&bar_drained[bf]));
-            }
-        }
+                       for (int t = 0; t < 32; t++) p.Tf[(size_t)(j0 + 32 * cc + t) * p.Npad + a] = v[t] * p.out_scale;
+                   });
     } else if (warp < 10 && p.arcs > 0) {
         // eight producers expanding arc-run tables (see arc_table_word): each warp loads slice
         // k+1's table into registers while it expands slice k from its own shared buffer.
         const int pw = warp - 2, n3 = p.arcs;
-        uint32_t* tab = reinterpret_cast<uint32_t*>(smem + STAGES1 * STAGE1_BYTES) + pw * 2 * kArcTab;  // [2][kArcTab]
+        uint32_t* tab = reinterpret_cast<uint32_t*>(smem + STAGES * STAGE_BYTES) + pw * 2 * kArcTab;  // [2][kArcTab]
         const int T = arc_table_size(p.ks, n3);
         constexpr int kPer = kArcTab / 32;
         uint32_t nxt[kPer];
@@ -416,7 +379,7 @@ __global__ void __launch_bounds__(512, 1)
         for (int k = 0; k < nk; k++) {
             __syncwarp();  // table k complete in this warp's buffer
             if (k + 1 < nk) load(k + 1);
-            const int s = k % STAGES1, n = k / STAGES1;
+            const int s = k % STAGES, n = k / STAGES;
             if (n > 0 && !mbar_wait(smem_u32(&bar_empty[s]), (n - 1) & 1, &abort_flag, p.err, p.wait_cycles)) break;
             const uint32_t* tb = tab + (k & 1) * kArcTab;
             unsigned char* ahi = A_hi(s);
@@ -459,7 +422,7 @@ __global__ void __launch_bounds__(512, 1)
         };
         if (nk > 0) gather(0);
         for (int k = 0; k < nk; k++) {
-            const int s = k % STAGES1, n = k / STAGES1;
+            const int s = k % STAGES, n = k / STAGES;
             if (n > 0 && !mbar_wait(smem_u32(&bar_empty[s]), (n - 1) & 1, &abort_flag, p.err, p.wait_cycles)) break;
             unsigned char* ahi = A_hi(s);
             unsigned char* alo = A_lo(s);
@@ -788,15 +751,15 @@ void launch_project_tc(const ProjectArgs& a, cudaStream_t s, long long* launches
             if (ti * BM <= tj * BN + BN - 1 && ti * BM < M && tj * BN < M) tl.push_back(make_int2(ti, tj));
     OPSEC_CUDA(cudaMemcpyAsync(tiles, tl.data(), sizeof(int2) * tl.size(), cudaMemcpyHostToDevice, s));
 
+    const CUtensorMap mBh256 = make_map(Bh, L.Mpad, L.Npad, BN), mBl256 = make_map(Bl, L.Mpad, L.Npad, BN);
     const CUtensorMap mBh128 = make_map(Bh, L.Mpad, L.Npad, BM), mBl128 = make_map(Bl, L.Mpad, L.Npad, BM);
     const CUtensorMap mTh256 = make_map(Th, L.Mpad, L.Npad, BN), mTl256 = make_map(Tl, L.Mpad, L.Npad, BN);
 
-    const size_t smem = (size_t)STAGES * STAGE_BYTES + 1024;
-    const size_t smem1 = (size_t)STAGES1 * STAGE1_BYTES + 1024 + sizeof(uint32_t) * 8 * 2 * kArcTab;
-    OPSEC_CUDA(cudaFuncSetAttribute(step1_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1));
+    const size_t smem = (size_t)STAGES * STAGE_BYTES + 1024 + sizeof(uint32_t) * 8 * 2 * kArcTab;
+    OPSEC_CUDA(cudaFuncSetAttribute(step1_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     OPSEC_CUDA(cudaFuncSetAttribute(step2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
 
-    const int n_at = L.Npad / BM, n_jt = L.Mpad / BN1;
+    const int n_at = L.Npad / BM, n_jt = L.Mpad / BN;
     const size_t nT = (size_t)L.Mpad * L.Npad;
     for (int p = 0; p < nb; p++) {
         const float sQ = pow2_scale(asf(hm[1 + p]));
@@ -817,7 +780,7 @@ void launch_project_tc(const ProjectArgs& a, cudaStream_t s, long long* launches
         p1.wait_cycles = a.wait_cycles;
         p1.arcs = a.arc_run;
         if (g_clock) g_clock->begin("project_step1", s, 2.0 * N * (double)N * M);
-        step1_kernel<<<n_at * n_jt, 512, smem1, s>>>(mBh128, mBl128, p1);
+        step1_kernel<<<n_at * n_jt, 512, smem, s>>>(mBh256, mBl256, p1);
         OPSEC_CUDA(cudaGetLastError());
         if (g_clock) g_clock->end(s);
         absmax_f32_kernel<<<dim3(2048, 1), 256, 0, s>>>(1, nT, Tf, maxT + p);

@@ -137,28 +137,32 @@ __global__ void xi_sum_kernel(XiTableArgs a) {
         }
     }
 
-    // the rest, by the three-term recurrence
+    // the rest, by the three-term recurrence, in double-FP32 (FP64 instructions issue at 1/64 of
+    // the FP32 rate here): the angles' sines and cosines once per lane in FP64, then the
+    // recurrence, its sum and the anchor rotations as (hi, lo) float pairs
     if (jc <= nk) {
-        double c2[kRPerWarp], cth[kRPerWarp], sth[kRPerWarp], cT[kRPerWarp], sT[kRPerWarp];
-        double sn[kRPerWarp], cs[kRPerWarp];
+        df c2[kRPerWarp], cth[kRPerWarp], sth[kRPerWarp], cT[kRPerWarp], sT[kRPerWarp], sn[kRPerWarp], cs[kRPerWarp];
 #pragma unroll
         for (int q = 0; q < kRPerWarp; q++) {
-            sincos(32.0 * dk * r[q], &sth[q], &cth[q]);
-            sincos((32.0 * kAnchor) * dk * r[q], &sT[q], &cT[q]);
-            c2[q] = 2.0 * cth[q];
-            sincos((s.kmin + (jc + lane) * dk) * r[q], &sn[q], &cs[q]);
+            double a, b;
+            sincos(32.0 * dk * r[q], &a, &b);
+            sth[q] = df_from(a);
+            cth[q] = df_from(b);
+            c2[q] = df_from(2.0 * b);
+            sincos((32.0 * kAnchor) * dk * r[q], &a, &b);
+            sT[q] = df_from(a);
+            cT[q] = df_from(b);
+            sincos((s.kmin + (jc + lane) * dk) * r[q], &a, &b);
+            sn[q] = df_from(a);
+            cs[q] = df_from(b);
         }
-        df c2d[kRPerWarp];
-#pragma unroll
-        for (int q = 0; q < kRPerWarp; q++) c2d[q] = df_from(c2[q]);
+        const df zero{0.f, 0.f};
         for (int j0 = jc + lane; j0 <= nk; j0 += 32 * kAnchor) {
-            // the recurrence and its sum in double-FP32 (FP64 instructions issue at 1/64 of the
-            // FP32 rate here); the anchors stay FP64
             df cur[kRPerWarp], prev[kRPerWarp];
 #pragma unroll
             for (int q = 0; q < kRPerWarp; q++) {
-                cur[q] = df_from(sn[q]);
-                prev[q] = df_from(sn[q] * cth[q] - cs[q] * sth[q]);  // sin(x - theta)
+                cur[q] = sn[q];
+                prev[q] = df_fms(df_fma(zero, sn[q], cth[q]), cs[q], sth[q]);  // sin(x - theta)
             }
             const int steps = min(kAnchor, (nk - j0) / 32 + 1);
             for (int m = 0; m < steps; m++) {
@@ -166,15 +170,15 @@ __global__ void xi_sum_kernel(XiTableArgs a) {
 #pragma unroll
                 for (int q = 0; q < kRPerWarp; q++) {
                     acc_rec[q] = df_fma(acc_rec[q], w, cur[q]);
-                    const df nxt = df_fma(df{-prev[q].h, -prev[q].l}, c2d[q], cur[q]);
+                    const df nxt = df_fma(df{-prev[q].h, -prev[q].l}, c2[q], cur[q]);
                     prev[q] = cur[q];
                     cur[q] = nxt;
                 }
             }
 #pragma unroll
-            for (int q = 0; q < kRPerWarp; q++) {
-                const double sn2 = sn[q] * cT[q] + cs[q] * sT[q];
-                cs[q] = cs[q] * cT[q] - sn[q] * sT[q];
+            for (int q = 0; q < kRPerWarp; q++) {  // rotate the anchor by 32 kAnchor dk r
+                const df sn2 = df_fma(df_fma(zero, sn[q], cT[q]), cs[q], sT[q]);
+                cs[q] = df_fms(df_fma(zero, cs[q], cT[q]), sn[q], sT[q]);
                 sn[q] = sn2;
             }
         }
@@ -201,7 +205,8 @@ void launch_xi_tables(const XiTableArgs& a, cudaStream_t s, long long* launches)
     OPSEC_CUDA(cudaGetLastError());
     const int n = a.xl.n();
     const int warps = (n + kRPerWarp - 1) / kRPerWarp;
-    xi_sum_kernel<<<dim3((warps * 32 + 255) / 256, ntab), 256, 0, s>>>(a);
+    // 128-thread CTAs: three fit on an SM at this kernel's register count (12 warps in flight)
+    xi_sum_kernel<<<dim3((warps * 32 + 127) / 128, ntab), 128, 0, s>>>(a);
     OPSEC_CUDA(cudaGetLastError());
     *launches += 2;
 }
