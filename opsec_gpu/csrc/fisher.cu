@@ -46,7 +46,7 @@ __host__ __device__ inline FisherTiling fisher_tiling(int nb) {
     while (t.slices < 32 && t.ntiles * t.slices * 2 <= kMaxThreads) t.slices *= 2;
     t.threads = (t.ntiles * t.slices + 31) / 32 * 32;
     if (t.threads < kChunk) t.threads = kChunk;
-    const size_t stage = sizeof(float) * (size_t)t.rows * kStride;
+    const size_t stage = 2 * sizeof(float) * (size_t)t.rows * kStride;  // two chunk buffers
     const size_t red = sizeof(double) * (size_t)t.ntiles * t.slices * kTile * kTile;
     t.smem = stage > red ? stage : red;
     return t;
@@ -104,6 +104,7 @@ struct PackedSource {
         *off = k;
     }
     __device__ float value(int p, long long off) const { return (float)Dp[(size_t)p * K + off]; }
+    __device__ const T* addr(int p, long long off) const { return Dp + (size_t)p * K + off; }
 };
 
 // Block: only the pairs whose packed value can be nonzero on the azimuthal
@@ -128,8 +129,32 @@ struct BlockSource {
         const int blk = b.g_blk[lo];
         *off = b.off[blk] + (long long)b.mode_col[*j] * b.Km[blk] + b.mode_col[*i];
     }
-    __device__ float value(int p, long long off) const { return b.C[(size_t)p * b.csize + off]; }
+    __device__ const float* addr(int p, long long off) const { return b.C + (size_t)p * b.csize + off; }
 };
+
+// 4-byte asynchronous copy global -> shared (zero-filled when !valid; src must still be a
+// valid address then)
+__device__ __forceinline__ void cp_async4(float* dst, const float* src, bool valid) {
+    const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(d), "l"(src), "r"(valid ? 4 : 0) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+// Stage the raw D_p of one chunk: asynchronously for FP32 sources, by plain loads for FP64.
+template <class Src>
+__device__ __forceinline__ void stage_chunk(const Src& src, int nb, long long k0, long long K, const long long* offs,
+                                            float* h) {
+    for (int e = threadIdx.x; e < nb * kChunk; e += blockDim.x) {
+        const int p = e / kChunk, kk = e % kChunk;
+        const bool ok = k0 + kk < K;
+        if constexpr (sizeof(*src.addr(0, 0)) == sizeof(float))
+            cp_async4(h + p * kStride + kk, ok ? src.addr(p, offs[kk]) : src.addr(0, 0), ok);
+        else
+            h[p * kStride + kk] = ok ? src.value(p, offs[kk]) : 0.f;
+    }
+}
 
 template <class Src>
 __global__ void __launch_bounds__(kMaxThreads) fisher_kernel(Src src, int nb, const double* evals, const double* y,
@@ -137,8 +162,8 @@ __global__ void __launch_bounds__(kMaxThreads) fisher_kernel(Src src, int nb, co
     extern __shared__ __align__(16) unsigned char fisher_smem[];
     float* hs = reinterpret_cast<float*>(fisher_smem);  // [rows][kStride]
     __shared__ float p_hi[kMaxBands], p_lo[kMaxBands];   // prior p_n = p_hi + p_lo
-    __shared__ int s_i[kChunk], s_j[kChunk];            // the chunk's entries
-    __shared__ long long s_off[kChunk];
+    __shared__ int s_i[2 * kChunk], s_j[2 * kChunk];    // the entries of the two staged chunks
+    __shared__ long long s_off[2 * kChunk];
     const FisherTiling tl = fisher_tiling(nb);
     for (int n = threadIdx.x; n < nb; n += blockDim.x) {
         p_hi[n] = (float)prior[n];
@@ -172,26 +197,46 @@ __global__ void __launch_bounds__(kMaxThreads) fisher_kernel(Src src, int nb, co
             part[a][b] = 0.f;
         }
 
-    for (int e = me; e < (tl.rows - nb - 2) * kStride; e += blockDim.x) hs[(size_t)(nb + 2) * kStride + e] = 0.f;
-
-    for (long long k0 = (long long)blockIdx.x * kChunk; k0 < K; k0 += (long long)gridDim.x * kChunk) {
+    const size_t buf_floats = (size_t)tl.rows * kStride;
+    for (int b = 0; b < 2; b++)
+        for (int e = me; e < (tl.rows - nb - 2) * kStride; e += blockDim.x)
+            hs[b * buf_floats + (size_t)(nb + 2) * kStride + e] = 0.f;
+    auto entries = [&](long long k0, int b) {
         for (int kk = me; kk < kChunk; kk += blockDim.x) {
             const long long k = k0 + kk;
             int i = 0, j = 0;
             long long off = 0;
             if (k < K) src.entry(k, &i, &j, &off);
-            s_i[kk] = i;
-            s_j[kk] = j;
-            s_off[kk] = off;
+            s_i[b * kChunk + kk] = i;
+            s_j[b * kChunk + kk] = j;
+            s_off[b * kChunk + kk] = off;
         }
+    };
+    // two chunk buffers: the copies of chunk c+1 are in flight while chunk c is weighted and summed
+    const long long step = (long long)gridDim.x * kChunk;
+    long long k0 = (long long)blockIdx.x * kChunk;
+    if (k0 < K) {
+        entries(k0, 0);
         __syncthreads();
-        // stage raw D_p[k]
-        for (int e = me; e < nb * kChunk; e += blockDim.x) {
-            const int p = e / kChunk, kk = e % kChunk;
-            const long long k = k0 + kk;
-            hs[p * kStride + kk] = (k < K) ? src.value(p, s_off[kk]) : 0.f;
+        stage_chunk(src, nb, k0, K, s_off, hs);
+        cp_async_commit();
+    }
+    for (int it = 0; k0 < K; k0 += step, it++) {
+        const int bs = it & 1;  // this chunk's buffer
+        const long long k1 = k0 + step;
+        if (k1 < K) entries(k1, bs ^ 1);
+        __syncthreads();  // entries of chunk k1 visible; chunk it-1 no longer read from buffer b^1
+        if (k1 < K) {
+            stage_chunk(src, nb, k1, K, s_off + (bs ^ 1) * kChunk, hs + (bs ^ 1) * buf_floats);
+            cp_async_commit();
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
         }
-        __syncthreads();
+        __syncthreads();  // chunk k0's copies visible to every thread
+        float* const hb = hs + bs * buf_floats;
+        const int* const si = s_i + bs * kChunk;
+        const int* const sj = s_j + bs * kChunk;
         // per-k weights sqrt(m w_i w_j), residual row R, data row y_i y_j.  R's
         // diagonal is 1 + lambda_i less a sum close to lambda_i, so the sum runs
         // in compensated FP32 (a two-sum per term plus the exact rounding error
@@ -200,7 +245,7 @@ __global__ void __launch_bounds__(kMaxThreads) fisher_kernel(Src src, int nb, co
             const long long k = k0 + kk;
             float sc = 0.f, R = 0.f, yy = 0.f;
             if (k < K) {
-                const int i = s_i[kk], j = s_j[kk];
+                const int i = si[kk], j = sj[kk];
                 const float wi = 1.0f / (1.0f + (float)evals[i]), wj = 1.0f / (1.0f + (float)evals[j]);
                 sc = sqrtf((i == j ? 0.5f : 1.0f) * wi * wj);
                 float rs = 0.f, rc = 0.f;
@@ -210,7 +255,7 @@ __global__ void __launch_bounds__(kMaxThreads) fisher_kernel(Src src, int nb, co
                     rc = (float)(d - (double)rs);
                 }
                 for (int n = 0; n < nb; n++) {
-                    const float dn = hs[n * kStride + kk];
+                    const float dn = hb[n * kStride + kk];
                     const float t = -p_hi[n] * dn;
                     const float te = fmaf(-p_hi[n], dn, -t);  // exact: -p_hi dn = t + te
                     const float u = rs + t;                    // two-sum: rs + t = u + ue
@@ -222,9 +267,9 @@ __global__ void __launch_bounds__(kMaxThreads) fisher_kernel(Src src, int nb, co
                 R = rs + rc;
                 yy = (float)(y[i] * y[j]);
             }
-            for (int p = 0; p < nb; p++) hs[p * kStride + kk] *= sc;
-            hs[nb * kStride + kk] = R * sc;
-            hs[(nb + 1) * kStride + kk] = yy * sc;
+            for (int p = 0; p < nb; p++) hb[p * kStride + kk] *= sc;
+            hb[nb * kStride + kk] = R * sc;
+            hb[(nb + 1) * kStride + kk] = yy * sc;
         }
         __syncthreads();
         if (worker) {
@@ -233,8 +278,8 @@ __global__ void __launch_bounds__(kMaxThreads) fisher_kernel(Src src, int nb, co
                 float va[kTile], vb[kTile];
 #pragma unroll
                 for (int a = 0; a < kTile; a++) {
-                    va[a] = ra[a * kStride + kk];
-                    vb[a] = rb[a * kStride + kk];
+                    va[a] = ra[bs * buf_floats + a * kStride + kk];
+                    vb[a] = rb[bs * buf_floats + a * kStride + kk];
                 }
 #pragma unroll
                 for (int a = 0; a < kTile; a++)
