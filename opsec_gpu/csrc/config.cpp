@@ -202,6 +202,11 @@ void configure(opsec_gpu* c, const std::map<std::string, std::string>& kv) {
     if (has("cubature.flush")) c->win_flush = to_int("cubature.flush", get("cubature.flush"));
     if (c->win_flush < 0) fail(OPSEC_ERR_CONFIG, "cubature.flush must be >= 0");
     if (has("cubature.dot")) c->win_dot64 = get("cubature.dot") != "f32";
+    if (has("cubature.log_keys")) {
+        const std::string& v = get("cubature.log_keys");
+        if (v != "0" && v != "1") fail(OPSEC_ERR_CONFIG, "cubature.log_keys must be 0 or 1");
+        c->win_logkeys = v == "1";
+    }
     if (has("cubature.symmetry")) {
         const std::string& v = get("cubature.symmetry");
         if (v == "reflect")

@@ -417,6 +417,7 @@ struct WinPlan {
     float4* arc;      // [H][ng^2]: rho hi, rho lo, z hi, z lo of node pair P = i_r ng + i_mu
     float* wrm;       // [ng^2]: w_r w_mu of node pair P
     float4* sph;      // [nf][ng(ng+1)/2]: sin^2(theta/2) hi, lo, phi-node weight (x2 off the diagonal), 0
+    int logkeys;      // one-pass keys in the log section take the specialised loop
 };
 
 // Tables of the spherical window kernel, from the cubature nodes (FP64 products,
@@ -571,7 +572,7 @@ __global__ void bucket_scatter_kernel(long long nkeys, WinPlan w) {
 // Histogram bins hold sum w_p w_q (1-fr) and sum w_p w_q fr, in fixed point:
 // each contribution is scaled so that the largest pair weight is 2^k coarse
 // units (k = 18 for 4^3 x 4^3 points), rounded once in FP32 (the product),
-// split into its integer part and its fraction in 2^-k units, and added with
+// split into its nearest integer and the rest in 2^-k units, and added with
 // two native 32-bit integer shared-memory atomics; neither partial sum can
 // overflow within a pass, at whose end they move into a 64-bit integer
 // histogram.  The sums are exact and independent of the order of the atomics.
@@ -586,17 +587,45 @@ __global__ void bucket_scatter_kernel(long long nkeys, WinPlan w) {
 // from L1/L2, so the tables take no shared memory and two 16-warp CTAs fit on
 // an SM.
 
-// round-to-nearest integer of |v| < 2^22 by the FP32 magic-number addition (FMA/ALU pipes)
-__device__ __forceinline__ int fix_round(float v) { return __float_as_int(v + 12582912.f) - 0x4B400000; }
+// 1.5 * 2^23: an FP32 sum with it that lands in [2^23, 2^24), where the FP32 values are the
+// integers, is the integer rounding of the other addend, read from the sum's bits (FMA/ALU
+// pipes, no conversion instruction)
+constexpr float kMagic = 12582912.f;
+constexpr int kMagicBits = 0x4B400000;
 
-// Add x (in units of the coarse quantum) to bin b of the fixed-point partial histogram:
-// the integer part into hqa, the fraction in units of 1/frac (a power of two) into hqb
-// (both native integer shared atomics, exact and order-independent).  x - floor(x) is
-// exact in FP32.
+// Add x (in units of the coarse quantum, |x| < 2^21) to bin b of the fixed-point partial
+// histogram: its nearest integer a into hqa, x - a (exact, |x - a| <= 1/2) in units of 1/frac
+// (a power of two), rounded to nearest, into hqb (both native integer shared atomics, exact
+// and order-independent).  a frac + rn((x - a) frac) is the nearest integer to x frac whatever
+// the integer a, so the sums are those of any other integer split.
 __device__ __forceinline__ void add_fixed(int* hqa, int* hqb, int b, float x, float frac) {
-    const float a = floorf(x);
-    atomicAdd(&hqa[b], fix_round(a));
-    atomicAdd(&hqb[b], fix_round((x - a) * frac));
+    const float s = __fadd_rn(x, kMagic);
+    const float f = __fsub_rn(x, __fsub_rn(s, kMagic));
+    atomicAdd(&hqa[b], __float_as_int(s) - kMagicBits);
+    atomicAdd(&hqb[b], __float_as_int(fmaf(f, frac, kMagic)) - kMagicBits);
+}
+
+// Table index (i, fr) of r^2 = r2 + r2l when r^2 >= r1^2 is known (every pair of a key whose
+// window starts above the linear section): index_r2's log branch with the same operations
+// and roundings, its exponent clamp and 2^-E folded into a table indexed by the biased
+// exponent, s_ce[eb] = (2^(127-eb), fraction of c_e, integer part of c_e - kMagicBits, 0),
+// and floor(y) from an FP32 addition rounded down.
+__device__ __forceinline__ void index_log(const Lookup& lk, const float4* s_ce, const float4* s_kt, float r2,
+                                          float r2l, int& i, float& fr) {
+    const unsigned u = __float_as_uint(r2) >> (23 - kLogBits);  // exponent and top mantissa bits
+    const float4 ce = s_ce[(u >> kLogBits) & 255];
+    const float4 kt = s_kt[u & (kLogN - 1)];
+    const float Rk = __uint_as_float(u << (23 - kLogBits));
+    const float delta = ((r2 - Rk) + r2l) * (kt.x * ce.x);
+    const float ln1p = delta * fmaf(-delta, fmaf(-delta, fmaf(-delta, 0.25f, 1.f / 3.f), 0.5f), 1.f);
+    const float y = fmaf(ln1p, lk.cp, ce.y + kt.y);
+    const float s = __fadd_rd(y, kMagic);  // kMagic + floor(y), |y| < 2^22
+    i = __float_as_int(ce.z) + __float_as_int(kt.z) + __float_as_int(s);
+    fr = __fsub_rn(y, __fsub_rn(s, kMagic));
+    if (i > lk.imax) {
+        i = lk.imax;
+        fr = 1.0f;
+    }
 }
 
 // Move the partial sums into the 64-bit histogram (units of 2^-fbits of the coarse quantum:
@@ -853,12 +882,18 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
     __shared__ float s_cf[kMaxExp];
     __shared__ float4 s_kt[kLogN];
     __shared__ float s_wrm[NG2];
+    __shared__ float4 s_ce[256];  // index_log's exponent table
     for (int i = threadIdx.x; i < lk.ne; i += blockDim.x) {
         s_ci[i] = lk.ci[i];
         s_cf[i] = lk.cf[i];
     }
     for (int i = threadIdx.x; i < kLogN; i += blockDim.x) s_kt[i] = lk.kt[i];
     for (int i = threadIdx.x; i < NG2; i += blockDim.x) s_wrm[i] = w.wrm[i];
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) {
+        const int e = min(max(i - 127 - lk.e0, 0), lk.ne - 1);
+        s_ce[i] = make_float4(__uint_as_float((unsigned)(254 - i) << 23), lk.cf[e],
+                              __int_as_float(lk.ci[e] - kMagicBits), 0.f);
+    }
     __syncthreads();
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -903,6 +938,10 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
                 hqb[j] = 0;
             }
             __syncwarp();
+            // One pass whose window starts above the linear section of the table (most far
+            // keys): every pair has r^2 >= r1^2 and its bin is in the histogram, so the loop
+            // below needs neither the linear branch nor the pass filter.
+            const bool logkeys = w.logkeys && npass == 1 && wn.x > lk.n1;
             // lanes take the (P, Q) node pairs; every lane runs the same trip counts
             for (int c0 = 0; c0 < NG2 * NG2; c0 += 32) {
                 const int c = c0 + lane;
@@ -921,6 +960,30 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
                     const float B4h = 4.f * t0;
                     const float B4l = 4.f * (fmaf(A.x, B.x, -t0) + fmaf(A.x, B.y, A.y * B.x));
                     const float wpq = s_wrm[P] * s_wrm[Q];
+                    if (logkeys) {
+#pragma unroll
+                        for (int j = 0; j < NC; j++) {
+                            const float4 sp = SP[j];
+                            const float t = __fmul_rn(B4h, sp.x);
+                            const float tl = fmaf(B4h, sp.x, -t) + fmaf(B4h, sp.y, B4l * sp.x);
+                            float e;
+                            const float r2 = two_sum(Dh, t, &e);
+                            const float r2l = e + Dl + tl;
+                            int i;
+                            float fr;
+                            index_log(lk, s_ce, s_kt, r2, r2l, i, fr);
+                            int bi = i - wn.x;
+                            if ((unsigned)bi > (unsigned)(wl - 2)) {  // outside the window: cannot happen for a sound window
+                                ++bad;
+                                bi = min(max(bi, 0), wl - 2);
+                            }
+                            const float ww = wpq * sp.z;
+                            const float wq = ww * w.qinv;
+                            add_fixed(hqa, hqb, bi, fmaf(-wq, fr, wq), w.qfrac);
+                            add_fixed(hqa, hqb, bi + 1, wq * fr, w.qfrac);
+                        }
+                        continue;
+                    }
 #pragma unroll 2
                     for (int j = 0; j < NC; j++) {
                         const float4 sp = SP[j];
@@ -1080,6 +1143,7 @@ bool run_window(const CubatureArgs& a, const Lookup& lk, cudaStream_t s, long lo
     w.Wmax = std::min(kMaxPasses * (w.Wkey - 1) + 1, nx);
     w.flush = a.win_flush;
     w.dot64 = a.win_dot64;
+    w.logkeys = a.win_logkeys;
     const bool sph = a.coordsys == 2;
     {
         // Fixed-point partial histograms, summed over a whole pass: at most `pairs`

@@ -121,6 +121,8 @@ struct CubatureArgs {
     int win_key = 384;   // widest key window (bins) on the window path
     int win_flush = 8;   // Cartesian window kernel: second-cell points per loop chunk (0: all)
     int win_dot64 = 0;   // window dot products in FP64 (1) or FP32 chunks of 8 bins added in FP64 (0)
+    int win_logkeys = 1;  // spherical window kernel: one-pass keys in the log section of the table take
+                          // the specialised loop (1) or the general one (0); the results are the same bits
     void* work = nullptr;  // cubature_work_bytes() of scratch for the window path
     size_t work_bytes = 0;
     // list mode (set internally): integrate the keys list[0 .. *list_count) only

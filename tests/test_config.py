@@ -52,6 +52,7 @@ BAD = [
     ("projection.wait_cycles = soon", "projection.wait_cycles"),
     ("azimuthal.eig = lapack", "azimuthal.eig"),
     ("projection.arc_tables = 2", "projection.arc_tables"),
+    ("cubature.log_keys = yes", "cubature.log_keys"),
 ]
 
 
