@@ -207,6 +207,11 @@ void configure(opsec_gpu* c, const std::map<std::string, std::string>& kv) {
         if (v != "0" && v != "1") fail(OPSEC_ERR_CONFIG, "cubature.log_keys must be 0 or 1");
         c->win_logkeys = v == "1";
     }
+    if (has("cubature.order")) {
+        const std::string& v = get("cubature.order");
+        if (v != "key" && v != "window") fail(OPSEC_ERR_CONFIG, "cubature.order must be key or window");
+        c->win_keyorder = v == "key";
+    }
     if (has("cubature.symmetry")) {
         const std::string& v = get("cubature.symmetry");
         if (v == "reflect")

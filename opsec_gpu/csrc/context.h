@@ -94,7 +94,7 @@ struct opsec_gpu {
     int az_gemm64 = 0;
     bool cub_reflect = true;
     int cub_window = 1;
-    int win_key = 384, win_flush = 8, win_dot64 = 0, win_logkeys = 1;
+    int win_key = 384, win_flush = 8, win_dot64 = 0, win_logkeys = 1, win_keyorder = 1;
     bool az_parity = true;
     bool az_batched = true;
     bool az_own = true;     // the hand-written block eigensolver (blockeig.cu), else cuSOLVER

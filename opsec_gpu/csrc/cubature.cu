@@ -31,6 +31,7 @@
 //  * FP32 sums over the ng^3 points of the second cell; FP64 for the outer
 //    sum and the warp reduction.
 // Periodic boxes wrap each pair difference into [-L/2, L/2) (BoxSurvey.cpp:26-30).
+#include <climits>
 #include <cmath>
 #include <algorithm>
 #include <cstring>
@@ -79,6 +80,18 @@ struct Shape {
     static constexpr int kWarps = NG <= 4 ? 16 : 8;
 };
 
+// Row ha of entry tri of the packed upper triangle of an H x H matrix (row ha starts at
+// ha H - ha (ha - 1) / 2): the FP32 root of the quadratic (FP64 issues at 1/64 of the FP32
+// rate on this part), then exact integer corrections.
+__device__ __forceinline__ int tri_row(int H, long long tri) {
+    const float H2 = 2.f * (float)H + 1.f;
+    int ha = (int)floorf((H2 - sqrtf(fmaxf(H2 * H2 - 8.f * (float)tri, 0.f))) * 0.5f);
+    ha = min(max(ha, 0), H - 1);
+    while (ha > 0 && (long long)ha * H - (long long)ha * (ha - 1) / 2 > tri) --ha;
+    while ((long long)(ha + 1) * H - (long long)(ha + 1) * ha / 2 <= tri) ++ha;
+    return ha;
+}
+
 __device__ __forceinline__ void decode_key(const KeySpace& ks, long long key, int* c1, int* c2) {
     if (ks.coordsys == 1) {
         int kz = (int)(key % ks.N3);
@@ -91,12 +104,7 @@ __device__ __forceinline__ void decode_key(const KeySpace& ks, long long key, in
     }
     const int df = (int)(key % ks.nf);
     const long long tri = key / ks.nf;
-    // rows of the upper triangle: row ha starts at ha*H - ha(ha-1)/2
-    const double H2 = 2.0 * ks.H + 1.0;
-    int ha = (int)floor((H2 - sqrt(H2 * H2 - 8.0 * (double)tri)) * 0.5);
-    if (ha < 0) ha = 0;
-    while (ha > 0 && (long long)ha * ks.H - (long long)ha * (ha - 1) / 2 > tri) --ha;
-    while ((long long)(ha + 1) * ks.H - (long long)(ha + 1) * ha / 2 <= tri) ++ha;
+    const int ha = tri_row(ks.H, tri);
     const int hb = ha + (int)(tri - ((long long)ha * ks.H - (long long)ha * (ha - 1) / 2));
     c1[0] = ha / ks.N2; c1[1] = ha % ks.N2; c1[2] = 0;
     c2[0] = hb / ks.N2; c2[1] = hb % ks.N2; c2[2] = df;
@@ -110,11 +118,7 @@ __device__ __forceinline__ void decode_key(const KeySpace& ks, long long key, in
 __device__ __forceinline__ long long reflect_partner(const KeySpace& ks, long long key) {
     const int df = (int)(key % ks.nf);
     const long long tri = key / ks.nf;
-    const double H2 = 2.0 * ks.H + 1.0;
-    int ha = (int)floor((H2 - sqrt(H2 * H2 - 8.0 * (double)tri)) * 0.5);
-    if (ha < 0) ha = 0;
-    while (ha > 0 && (long long)ha * ks.H - (long long)ha * (ha - 1) / 2 > tri) --ha;
-    while ((long long)(ha + 1) * ks.H - (long long)(ha + 1) * ha / 2 <= tri) ++ha;
+    const int ha = tri_row(ks.H, tri);
     const int hb = ha + (int)(tri - ((long long)ha * ks.H - (long long)ha * (ha - 1) / 2));
     const int pa = (ha / ks.N2) * ks.N2 + (ks.N2 - 1 - ha % ks.N2);
     const int pb = (hb / ks.N2) * ks.N2 + (ks.N2 - 1 - hb % ks.N2);
@@ -405,9 +409,12 @@ struct WinPlan {
     float qfine;  // pair weight per unit of the 64-bit histogram (2^-fbits / qinv)
     int nbucket;  // nx + 1: bucket nx holds the near keys
     int2* win;        // [nkeys]: (bucket, width); bucket -1 = key copied by the reflection fill
-    int* order;       // [2 nkeys]: far keys by bucket, then near keys, then overflows
+    int* order;       // [2 nkeys]: far keys, then near keys (incl. windows too wide for the far kernels)
     int* count;       // [nbucket + 1]
     int* cursor;      // [nbucket + 1]
+    int keyorder;     // far and near keys each in ascending key order (1) or by window start (0)
+    int4* tiles;      // key order: per tile of kPartTile keys, the counts of the three classes, then
+                      // the tile's first slot in order[] for each
     int* nfar;        // far keys
     int* nnear;       // near keys incl. overflows (list length from order + nfar)
     int* violations;  // pairs that fell outside their key's window (must stay 0)
@@ -418,6 +425,8 @@ struct WinPlan {
     float* wrm;       // [ng^2]: w_r w_mu of node pair P
     float4* sph;      // [nf][ng(ng+1)/2]: sin^2(theta/2) hi, lo, phi-node weight (x2 off the diagonal), 0
     int logkeys;      // one-pass keys in the log section take the specialised loop
+    double* arcbox;   // [H][4]: rho min, rho max, z min, z max over the arc's node pairs
+    double* sphbox;   // [nf][2]: min and max of sin^2(theta/2) over the canonical phi-node pairs
 };
 
 // Tables of the spherical window kernel, from the cubature nodes (FP64 products,
@@ -454,6 +463,40 @@ __global__ void sph_tables_kernel(CubatureArgs a, WinPlan w) {
             const float sh = (float)s2;
             const double wphi = a.w[lp] * a.w[lq] * (lp + lq < ng - 1 ? 2.0 : 1.0);
             w.sph[t] = make_float4(sh, (float)(s2 - (double)sh), (float)wphi, 0.f);
+        }
+    }
+}
+
+// Ranges of the spherical kernel's pair terms: per arc, the (rho, z) box of its node pairs;
+// per azimuthal offset, the range of sin^2(theta/2) over its canonical phi-node pairs (FP64
+// from the FP32 pairs).  key_window_kernel bounds r^2 = (rho_P - rho_Q)^2 + (z_P - z_Q)^2 +
+// 4 rho_P rho_Q sin^2(theta/2) of a key's pairs by them.
+__global__ void sph_box_kernel(CubatureArgs a, WinPlan w) {
+    const int ng2 = a.ng * a.ng, nc = a.ng * (a.ng + 1) / 2;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < (long long)a.ks.H + a.ks.nf;
+         e += (long long)gridDim.x * blockDim.x) {
+        if (e < a.ks.H) {
+            double b[4] = {INFINITY, -INFINITY, INFINITY, -INFINITY};
+            for (int P = 0; P < ng2; P++) {
+                const float4 v = w.arc[e * ng2 + P];
+                const double rho = (double)v.x + v.y, z = (double)v.z + v.w;
+                b[0] = fmin(b[0], rho);
+                b[1] = fmax(b[1], rho);
+                b[2] = fmin(b[2], z);
+                b[3] = fmax(b[3], z);
+            }
+            for (int k = 0; k < 4; k++) w.arcbox[4 * e + k] = b[k];
+        } else {
+            const long long df = e - a.ks.H;
+            double lo = INFINITY, hi = -INFINITY;
+            for (int c = 0; c < nc; c++) {
+                const float4 v = w.sph[df * nc + c];
+                const double s2 = (double)v.x + v.y;
+                lo = fmin(lo, s2);
+                hi = fmax(hi, s2);
+            }
+            w.sphbox[2 * df] = lo;
+            w.sphbox[2 * df + 1] = hi;
         }
     }
 }
@@ -520,12 +563,29 @@ __global__ void key_window_kernel(CubatureArgs a, WinPlan w) {
             }
         }
         const double dist = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
-        const int blo = max(bin_floor(a.xl, fmax(dist - R, 0.0)) - 1, 0);
-        const int bhi = min(bin_floor(a.xl, dist + R) + 3, nx);
+        double rlo = fmax(dist - R, 0.0), rhi = dist + R;
+        if (w.arcbox) {
+            // spherical grids: the bounding spheres of cells long in phi are loose; bound r^2
+            // term by term from the arcs' (rho, z) boxes and the offset's sin^2 range, and keep
+            // the tighter of the two bounds (both hold for every node pair of the key)
+            const double* ba = w.arcbox + 4 * (c1[0] * a.ks.N2 + c1[1]);
+            const double* bb = w.arcbox + 4 * (c2[0] * a.ks.N2 + c2[1]);
+            const double s2lo = w.sphbox[2 * c2[2]], s2hi = w.sphbox[2 * c2[2] + 1];
+            const double grho = fmax(0.0, fmax(bb[0] - ba[1], ba[0] - bb[1]));
+            const double gz = fmax(0.0, fmax(bb[2] - ba[3], ba[2] - bb[3]));
+            const double drho = fmax(bb[1] - ba[0], ba[1] - bb[0]);
+            const double dz = fmax(bb[3] - ba[2], ba[3] - bb[2]);
+            const double r2lo = grho * grho + gz * gz + 4.0 * ba[0] * bb[0] * s2lo;
+            const double r2hi = drho * drho + dz * dz + 4.0 * ba[1] * bb[1] * s2hi;
+            rlo = fmax(rlo, sqrt(r2lo) * (1.0 - 1e-9));
+            rhi = fmin(rhi, sqrt(r2hi) * (1.0 + 1e-9));
+        }
+        const int blo = max(bin_floor(a.xl, rlo) - 1, 0);
+        const int bhi = min(bin_floor(a.xl, rhi) + 3, nx);
         const int width = bhi - blo;
         const int bucket = (near || width > w.Wmax) ? nx : blo;
         w.win[key] = make_int2(bucket, width);
-        atomicAdd(&w.count[bucket], 1);
+        if (!w.keyorder) atomicAdd(&w.count[bucket], 1);
     }
 }
 
@@ -569,6 +629,127 @@ __global__ void bucket_scatter_kernel(long long nkeys, WinPlan w) {
     }
 }
 
+// Key order: a stable partition of the keys into three classes, each in ascending key order:
+// far keys that the spherical kernel's log-section loop takes (one pass, window above the
+// linear section), the other far keys, the near keys.  Consecutive warps of the far kernels
+// then integrate consecutive keys (mostly the same arc pair at consecutive azimuthal
+// offsets, or neighbouring Cartesian offsets), so the Q values they write for one table fall
+// into the same 32-byte sectors, which L2 merges before they reach DRAM (in window-start order
+// every Q value was an isolated 8-byte write to its own sector), and the warps of an SM run
+// the same loop at the same time.  Three launches: per-tile class counts, a scan over the
+// tiles, a scatter in key order.
+constexpr int kPartTile = 1024;  // keys per tile
+constexpr int kPartThreads = 256;
+
+// 0: reflected or skipped key, 1: far, log-section loop, 2: other far, 3: near.  n1log: the
+// window start above which one-pass keys take the log-section loop (INT_MAX: none).
+__device__ __forceinline__ int part_class(const WinPlan& w, long long key, int n1log) {
+    const int2 wn = w.win[key];
+    if (wn.x < 0) return 0;
+    if (wn.x == w.nbucket - 1) return 3;
+    const int S = w.Wkey - 1;
+    return (wn.y - 1 <= S && wn.x > n1log) ? 1 : 2;
+}
+
+__global__ void __launch_bounds__(kPartThreads) part_count_kernel(long long nkeys, WinPlan w, int n1log) {
+    __shared__ int s_n[3][kPartThreads / 32];
+    const long long k0 = (long long)blockIdx.x * kPartTile;
+    int n[3] = {0, 0, 0};
+    for (int t = threadIdx.x; t < kPartTile && k0 + t < nkeys; t += kPartThreads) {
+        const int c = part_class(w, k0 + t, n1log);
+        if (c > 0) ++n[c - 1];
+    }
+    for (int o = 16; o > 0; o >>= 1)
+        for (int c = 0; c < 3; c++) n[c] += __shfl_xor_sync(0xffffffffu, n[c], o);
+    if ((threadIdx.x & 31) == 0)
+        for (int c = 0; c < 3; c++) s_n[c][threadIdx.x >> 5] = n[c];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int4 v = make_int4(0, 0, 0, 0);
+        for (int i = 0; i < kPartThreads / 32; i++) {
+            v.x += s_n[0][i];
+            v.y += s_n[1][i];
+            v.z += s_n[2][i];
+        }
+        w.tiles[blockIdx.x] = v;
+    }
+}
+
+// exclusive scan of the tile counts (one block) into the tiles' first slots in order[]: class 1
+// from 0, class 2 after all of class 1, class 3 (near keys) after all far keys
+__global__ void part_scan_kernel(int ntiles, WinPlan w) {
+    __shared__ int4 part[1024];
+    const int per = (ntiles + blockDim.x - 1) / blockDim.x;
+    const int t0 = threadIdx.x * per, t1 = min(ntiles, t0 + per);
+    int4 sum = make_int4(0, 0, 0, 0);
+    for (int t = t0; t < t1; t++) {
+        const int4 v = w.tiles[t];
+        sum.x += v.x;
+        sum.y += v.y;
+        sum.z += v.z;
+    }
+    part[threadIdx.x] = sum;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int4 run = make_int4(0, 0, 0, 0);
+        for (int i = 0; i < (int)blockDim.x; i++) {
+            const int4 v = part[i];
+            part[i] = run;
+            run.x += v.x;
+            run.y += v.y;
+            run.z += v.z;
+        }
+        *w.nfar = run.x + run.y;
+        *w.nnear = run.z;
+        part[0].w = run.x;  // class 1 total, read below (after the barrier)
+    }
+    __syncthreads();
+    const int n1 = part[0].w, nfar = *w.nfar;
+    int4 run = part[threadIdx.x];
+    for (int t = t0; t < t1; t++) {
+        const int4 v = w.tiles[t];
+        w.tiles[t] = make_int4(run.x, n1 + run.y, nfar + run.z, 0);
+        run.x += v.x;
+        run.y += v.y;
+        run.z += v.z;
+    }
+}
+
+// each thread classifies kPartTile / kPartThreads consecutive keys; a block-wide scan of the
+// per-thread counts gives every key its slot
+__global__ void __launch_bounds__(kPartThreads) part_scatter_kernel(long long nkeys, WinPlan w, int n1log) {
+    constexpr int kPer = kPartTile / kPartThreads;
+    constexpr int kW = kPartThreads / 32;
+    __shared__ int s_n[3][kW];
+    const long long k0 = (long long)blockIdx.x * kPartTile + (long long)threadIdx.x * kPer;
+    int cls[kPer];
+    int cnt[3] = {0, 0, 0};
+#pragma unroll
+    for (int u = 0; u < kPer; u++) {
+        cls[u] = k0 + u < nkeys ? part_class(w, k0 + u, n1log) : 0;
+        for (int c = 0; c < 3; c++) cnt[c] += cls[u] == c + 1;
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int inc[3] = {cnt[0], cnt[1], cnt[2]};  // inclusive scans over the warp
+    for (int o = 1; o < 32; o <<= 1)
+        for (int c = 0; c < 3; c++) {
+            const int v = __shfl_up_sync(0xffffffffu, inc[c], o);
+            if (lane >= o) inc[c] += v;
+        }
+    if (lane == 31)
+        for (int c = 0; c < 3; c++) s_n[c][warp] = inc[c];
+    __syncthreads();
+    const int4 base = w.tiles[blockIdx.x];
+    int slot[3] = {base.x, base.y, base.z};
+    for (int c = 0; c < 3; c++) {
+        for (int i = 0; i < warp; i++) slot[c] += s_n[c][i];
+        slot[c] += inc[c] - cnt[c];
+    }
+#pragma unroll
+    for (int u = 0; u < kPer; u++)
+        if (cls[u] > 0) w.order[slot[cls[u] - 1]++] = (int)(k0 + u);
+}
+
 // Histogram bins hold sum w_p w_q (1-fr) and sum w_p w_q fr, in fixed point:
 // each contribution is scaled so that the largest pair weight is 2^k coarse
 // units (k = 18 for 4^3 x 4^3 points), rounded once in FP32 (the product),
@@ -609,18 +790,21 @@ __device__ __forceinline__ void add_fixed(int* hqa, int* hqb, int b, float x, fl
 // window starts above the linear section): index_r2's log branch with the same operations
 // and roundings, its exponent clamp and 2^-E folded into a table indexed by the biased
 // exponent, s_ce[eb] = (2^(127-eb), fraction of c_e, integer part of c_e - kMagicBits, 0),
-// and floor(y) from an FP32 addition rounded down.
-__device__ __forceinline__ void index_log(const Lookup& lk, const float4* s_ce, const float4* s_kt, float r2,
-                                          float r2l, int& i, float& fr) {
+// the mantissa table split into (1/T_k, fraction of z_k) pairs and the integer parts of z_k
+// (8 + 2 bytes per entry instead of 16: the lanes' random entries cost fewer shared-memory
+// wavefronts), and floor(y) from an FP32 addition rounded down.
+__device__ __forceinline__ void index_log(const Lookup& lk, const float4* s_ce, const float2* s_kt2,
+                                          const unsigned short* s_kz, float r2, float r2l, int& i, float& fr) {
     const unsigned u = __float_as_uint(r2) >> (23 - kLogBits);  // exponent and top mantissa bits
     const float4 ce = s_ce[(u >> kLogBits) & 255];
-    const float4 kt = s_kt[u & (kLogN - 1)];
+    const int k = u & (kLogN - 1);
+    const float2 kt = s_kt2[k];
     const float Rk = __uint_as_float(u << (23 - kLogBits));
     const float delta = ((r2 - Rk) + r2l) * (kt.x * ce.x);
     const float ln1p = delta * fmaf(-delta, fmaf(-delta, fmaf(-delta, 0.25f, 1.f / 3.f), 0.5f), 1.f);
     const float y = fmaf(ln1p, lk.cp, ce.y + kt.y);
     const float s = __fadd_rd(y, kMagic);  // kMagic + floor(y), |y| < 2^22
-    i = __float_as_int(ce.z) + __float_as_int(kt.z) + __float_as_int(s);
+    i = __float_as_int(ce.z) + (int)s_kz[k] + __float_as_int(s);
     fr = __fsub_rn(y, __fsub_rn(s, kMagic));
     if (i > lk.imax) {
         i = lk.imax;
@@ -641,12 +825,13 @@ __device__ __forceinline__ void flush_fixed(int* hqa, int* hqb, long long* hm, i
 }
 
 constexpr int kMaxPasses = 8;  // passes over the point pairs for windows wider than one histogram
-constexpr int kDotChunk = 16;  // bins summed in FP32 per FP64 addition in the window dot products
+constexpr int kDotChunk = 16;  // bins summed in FP32 per compensated addition in the window dot products
 
 // Dot products of one pass's histogram (64-bit, bins s0 .. s0 + segw - 1 of the key's window)
 // with every table, added into Q.  Two work items per table, alternate chunks of kDotChunk
 // bins, spread over the lanes (table t: items 2t and 2t+1 on neighbouring lanes, combined by
-// one shuffle).  Far keys: FP32 within a chunk, FP64 across chunks.  Keys whose window
+// one shuffle).  Far keys: FP32 within a chunk, the chunk sums added by two-sum into an FP32
+// pair (as exact as FP64 additions of them, without the FP64 pipe).  Keys whose window
 // reaches the linear section of the table or needs several passes (self and adjacent
 // cells, whose integrals cancel strongly over several periods of a band table) and every
 // key with `dot64`: compensated FP32 -- exact products by FMA, two-sum accumulation, the bin
@@ -685,11 +870,30 @@ __device__ __forceinline__ void window_dots(const CubatureArgs& a, const WinPlan
                     }
                 acc = (double)sh + (double)sl;
             } else {
+                float sh = 0.f, sl = 0.f;
                 for (int b0 = kDotChunk * h; b0 < segw; b0 += 2 * kDotChunk) {
                     float pt = 0.f;
-                    for (int b = b0; b < min(b0 + kDotChunk, segw); b++) pt = fmaf(tr[(size_t)b * ntab], hp[b], pt);
-                    acc += (double)pt;
+                    if (b0 + kDotChunk <= segw) {
+                        // a whole chunk: the histogram values four at a time (one broadcast
+                        // 16-byte shared load; hp is 16-byte aligned, Wkey a multiple of 4)
+                        const float* trb = tr + (size_t)b0 * ntab;
+#pragma unroll
+                        for (int u = 0; u < kDotChunk; u += 4) {
+                            const float4 hv = *reinterpret_cast<const float4*>(hp + b0 + u);
+                            pt = fmaf(trb[0], hv.x, pt);
+                            pt = fmaf(trb[ntab], hv.y, pt);
+                            pt = fmaf(trb[2 * ntab], hv.z, pt);
+                            pt = fmaf(trb[3 * ntab], hv.w, pt);
+                            trb += 4 * ntab;
+                        }
+                    } else {
+                        for (int b = b0; b < segw; b++) pt = fmaf(tr[(size_t)b * ntab], hp[b], pt);
+                    }
+                    float e;
+                    sh = two_sum(sh, pt, &e);
+                    sl += e;
                 }
+                acc = (double)sh + (double)sl;
             }
         }
         acc += __shfl_xor_sync(0xffffffffu, acc, 1);
@@ -715,7 +919,6 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
     constexpr int NG2 = NG * NG;
     constexpr int kWarps = FarShape<NG>::kWarps;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int ntab = a.ntab;
     float4* pts = reinterpret_cast<float4*>(smem_raw);                  // [kWarps][2][NP]
     long long* mas = reinterpret_cast<long long*>(pts + kWarps * 2 * NP);  // [kWarps][Wkey]: 64-bit histogram
     int* pa = reinterpret_cast<int*>(mas + kWarps * w.Wkey);               // [kWarps][Wkey]: partial sums, integer part
@@ -740,8 +943,7 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
     const bool periodic = (a.coordsys == 1 && a.L > 0);
     const float Lh = (float)a.L, Ll = (float)(a.L - (double)Lh), hL = 0.5f * Lh;
     const int nfar = *w.nfar;
-    // consecutive warps take consecutive keys of the window-start order: the
-    // keys in flight at any time read neighbouring rows of the tables
+    // consecutive warps take consecutive keys of the order (see part_scatter_kernel)
     for (int kk = blockIdx.x * kWarps + warp; kk < nfar; kk += gridDim.x * kWarps) {
         const int key = w.order[kk];
         const int2 wn = w.win[key];
@@ -873,7 +1075,6 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
     constexpr int NC = NG * (NG + 1) / 2;
     constexpr int kWarps = FarShape<NG>::kWarps;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int ntab = a.ntab;
     float4* sphw = reinterpret_cast<float4*>(smem_raw);        // [kWarps][NC]: the key's phi-node pairs
     long long* mas = reinterpret_cast<long long*>(sphw + kWarps * NC);  // [kWarps][Wkey]: 64-bit histogram
     int* pa = reinterpret_cast<int*>(mas + kWarps * w.Wkey);            // [kWarps][Wkey]: partial sums, integer part
@@ -883,11 +1084,18 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
     __shared__ float4 s_kt[kLogN];
     __shared__ float s_wrm[NG2];
     __shared__ float4 s_ce[256];  // index_log's exponent table
+    __shared__ float2 s_kt2[kLogN];          // index_log: 1/T_k, fraction of z_k
+    __shared__ unsigned short s_kz[kLogN];   // index_log: integer part of z_k
     for (int i = threadIdx.x; i < lk.ne; i += blockDim.x) {
         s_ci[i] = lk.ci[i];
         s_cf[i] = lk.cf[i];
     }
-    for (int i = threadIdx.x; i < kLogN; i += blockDim.x) s_kt[i] = lk.kt[i];
+    for (int i = threadIdx.x; i < kLogN; i += blockDim.x) {
+        const float4 kt = lk.kt[i];
+        s_kt[i] = kt;
+        s_kt2[i] = make_float2(kt.x, kt.y);
+        s_kz[i] = (unsigned short)__float_as_int(kt.z);  // < 2^16: checked on the host
+    }
     for (int i = threadIdx.x; i < NG2; i += blockDim.x) s_wrm[i] = w.wrm[i];
     for (int i = threadIdx.x; i < 256; i += blockDim.x) {
         const int e = min(max(i - 127 - lk.e0, 0), lk.ne - 1);
@@ -961,7 +1169,7 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
                     const float B4l = 4.f * (fmaf(A.x, B.x, -t0) + fmaf(A.x, B.y, A.y * B.x));
                     const float wpq = s_wrm[P] * s_wrm[Q];
                     if (logkeys) {
-#pragma unroll
+#pragma unroll 2
                         for (int j = 0; j < NC; j++) {
                             const float4 sp = SP[j];
                             const float t = __fmul_rn(B4h, sp.x);
@@ -971,7 +1179,7 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
                             const float r2l = e + Dl + tl;
                             int i;
                             float fr;
-                            index_log(lk, s_ce, s_kt, r2, r2l, i, fr);
+                            index_log(lk, s_ce, s_kt2, s_kz, r2, r2l, i, fr);
                             int bi = i - wn.x;
                             if ((unsigned)bi > (unsigned)(wl - 2)) {  // outside the window: cannot happen for a sound window
                                 ++bad;
@@ -1103,7 +1311,7 @@ size_t cubature_point_count(const KeySpace& ks, int ng) {
 namespace {
 // scratch layout of the window path
 struct WinLayout {
-    size_t win, order, count, cursor, scal, cen, tabT, arc, wrm, sph, total;
+    size_t win, order, count, cursor, scal, cen, tabT, arc, wrm, sph, arcbox, sphbox, tiles, total;
 };
 WinLayout win_layout(const KeySpace& ks, int nx, int ntab, int ng) {
     auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
@@ -1120,7 +1328,10 @@ WinLayout win_layout(const KeySpace& ks, int nx, int ntab, int ng) {
     const bool sph = ks.coordsys == 2;
     L.wrm = L.arc + (sph ? al(sizeof(float4) * (size_t)ks.H * ng * ng) : 0);
     L.sph = L.wrm + (sph ? al(sizeof(float) * (size_t)ng * ng) : 0);
-    L.total = L.sph + (sph ? al(sizeof(float4) * (size_t)ks.nf * (ng * (ng + 1) / 2)) : 0);
+    L.arcbox = L.sph + (sph ? al(sizeof(float4) * (size_t)ks.nf * (ng * (ng + 1) / 2)) : 0);
+    L.sphbox = L.arcbox + (sph ? al(sizeof(double) * 4 * (size_t)ks.H) : 0);
+    L.tiles = L.sphbox + (sph ? al(sizeof(double) * 2 * (size_t)ks.nf) : 0);
+    L.total = L.tiles + al(sizeof(int4) * (size_t)((ks.nkeys + kPartTile - 1) / kPartTile));
     return L;
 }
 
@@ -1139,11 +1350,21 @@ bool run_window(const CubatureArgs& a, const Lookup& lk, cudaStream_t s, long lo
     WinPlan w{};
     // Cartesian grids also keep the second cell's points per warp: narrower histograms so
     // that two CTAs still fit on an SM
-    w.Wkey = std::min(a.coordsys == 2 ? a.win_key : std::min(a.win_key, 256), nx);
+    w.Wkey = std::min(a.coordsys == 2 ? a.win_key : std::min(a.win_key, 256), nx) & ~3;  // 16-byte rows
     w.Wmax = std::min(kMaxPasses * (w.Wkey - 1) + 1, nx);
     w.flush = a.win_flush;
     w.dot64 = a.win_dot64;
     w.logkeys = a.win_logkeys;
+    {
+        int zmax = 0;  // index_log keeps the integer parts of z_k in 16 bits
+        for (int k = 0; k < kLogN; k++) {
+            int zi = 0;
+            std::memcpy(&zi, &lk.kt[k].z, sizeof zi);
+            zmax = std::max(zmax, zi);
+        }
+        if (zmax > 65535) w.logkeys = 0;
+    }
+    w.keyorder = a.win_keyorder;
     const bool sph = a.coordsys == 2;
     {
         // Fixed-point partial histograms, summed over a whole pass: at most `pairs`
@@ -1170,6 +1391,7 @@ bool run_window(const CubatureArgs& a, const Lookup& lk, cudaStream_t s, long lo
     w.order = reinterpret_cast<int*>(base + L.order);
     w.count = reinterpret_cast<int*>(base + L.count);
     w.cursor = reinterpret_cast<int*>(base + L.cursor);
+    w.tiles = reinterpret_cast<int4*>(base + L.tiles);
     int* scal = reinterpret_cast<int*>(base + L.scal);
     w.nfar = scal;
     w.nnear = scal + 1;
@@ -1180,6 +1402,8 @@ bool run_window(const CubatureArgs& a, const Lookup& lk, cudaStream_t s, long lo
         w.arc = reinterpret_cast<float4*>(base + L.arc);
         w.wrm = reinterpret_cast<float*>(base + L.wrm);
         w.sph = reinterpret_cast<float4*>(base + L.sph);
+        w.arcbox = reinterpret_cast<double*>(base + L.arcbox);
+        w.sphbox = reinterpret_cast<double*>(base + L.sphbox);
     }
     OPSEC_CUDA(cudaMemsetAsync(w.count, 0, sizeof(int) * (nx + 2), s));
     OPSEC_CUDA(cudaMemsetAsync(scal, 0, 256, s));
@@ -1187,21 +1411,36 @@ bool run_window(const CubatureArgs& a, const Lookup& lk, cudaStream_t s, long lo
     auto blocks = [](long long n) { return (unsigned)std::min<long long>((n + 255) / 256, 65536); };
     cell_sphere_kernel<<<blocks(ncell), 256, 0, s>>>(a.pts, a.np, ncell, w.cen);
     OPSEC_CUDA(cudaGetLastError());
-    key_window_kernel<<<blocks(a.ks.nkeys), 256, 0, s>>>(a, w);
-    OPSEC_CUDA(cudaGetLastError());
-    bucket_scan_kernel<<<1, 1024, 0, s>>>(w);
-    OPSEC_CUDA(cudaGetLastError());
-    bucket_scatter_kernel<<<blocks(a.ks.nkeys), 256, 0, s>>>(a.ks.nkeys, w);
-    OPSEC_CUDA(cudaGetLastError());
-    transpose_tables_kernel<<<blocks((long long)a.ntab * nx), 256, 0, s>>>(a.tab32, a.ntab, nx, w.tabT);
-    OPSEC_CUDA(cudaGetLastError());
-    *launches += 5;
     if (sph) {
         const long long n = (long long)a.ks.H * a.ng * a.ng + a.ng * a.ng + (long long)a.ks.nf * (a.ng * (a.ng + 1) / 2);
         sph_tables_kernel<<<blocks(n), 256, 0, s>>>(a, w);
         OPSEC_CUDA(cudaGetLastError());
-        ++*launches;
+        sph_box_kernel<<<blocks((long long)a.ks.H + a.ks.nf), 256, 0, s>>>(a, w);
+        OPSEC_CUDA(cudaGetLastError());
+        *launches += 2;
     }
+    key_window_kernel<<<blocks(a.ks.nkeys), 256, 0, s>>>(a, w);
+    OPSEC_CUDA(cudaGetLastError());
+    if (w.keyorder) {
+        const long long ntiles = (a.ks.nkeys + kPartTile - 1) / kPartTile;
+        if (ntiles > INT_MAX) fail(OPSEC_ERR_CONFIG, "cubature: too many keys");
+        const int n1log = sph && w.logkeys ? lk.n1 : INT_MAX;
+        part_count_kernel<<<(unsigned)ntiles, kPartThreads, 0, s>>>(a.ks.nkeys, w, n1log);
+        OPSEC_CUDA(cudaGetLastError());
+        part_scan_kernel<<<1, 1024, 0, s>>>((int)ntiles, w);
+        OPSEC_CUDA(cudaGetLastError());
+        part_scatter_kernel<<<(unsigned)ntiles, kPartThreads, 0, s>>>(a.ks.nkeys, w, n1log);
+        OPSEC_CUDA(cudaGetLastError());
+        ++*launches;
+    } else {
+        bucket_scan_kernel<<<1, 1024, 0, s>>>(w);
+        OPSEC_CUDA(cudaGetLastError());
+        bucket_scatter_kernel<<<blocks(a.ks.nkeys), 256, 0, s>>>(a.ks.nkeys, w);
+        OPSEC_CUDA(cudaGetLastError());
+    }
+    transpose_tables_kernel<<<blocks((long long)a.ntab * nx), 256, 0, s>>>(a.tab32, a.ntab, nx, w.tabT);
+    OPSEC_CUDA(cudaGetLastError());
+    *launches += 5;
     int h_nfar = 0;
     OPSEC_CUDA(cudaMemcpyAsync(&h_nfar, w.nfar, sizeof(int), cudaMemcpyDeviceToHost, s));
     OPSEC_CUDA(cudaStreamSynchronize(s));

@@ -123,6 +123,7 @@ struct CubatureArgs {
     int win_dot64 = 0;   // window dot products in FP64 (1) or FP32 chunks of 8 bins added in FP64 (0)
     int win_logkeys = 1;  // spherical window kernel: one-pass keys in the log section of the table take
                           // the specialised loop (1) or the general one (0); the results are the same bits
+    int win_keyorder = 1;  // far keys integrated in key order (1) or by window start (0); same results
     void* work = nullptr;  // cubature_work_bytes() of scratch for the window path
     size_t work_bytes = 0;
     // list mode (set internally): integrate the keys list[0 .. *list_count) only

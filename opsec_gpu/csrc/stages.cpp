@@ -80,6 +80,7 @@ void build_q(opsec_gpu* c) {
     a.win_flush = c->win_flush;
     a.win_dot64 = c->win_dot64;
     a.win_logkeys = c->win_logkeys;
+    a.win_keyorder = c->win_keyorder;
     if (a.exact && a.window) {
         a.work_bytes = cubature_work_bytes(c->ks, c->xl.n(), a.ntab, a.ng);
         c->cubwork.alloc(a.work_bytes);

@@ -53,6 +53,7 @@ BAD = [
     ("azimuthal.eig = lapack", "azimuthal.eig"),
     ("projection.arc_tables = 2", "projection.arc_tables"),
     ("cubature.log_keys = yes", "cubature.log_keys"),
+    ("cubature.order = random", "cubature.order"),
 ]
 
 

@@ -128,23 +128,26 @@ def test_cubature_window_path(name):
         assert e_win <= 3e-7 and e_grp <= 3e-7, (name, t, e_win, e_grp)
 
 
-def test_cubature_log_section_loop_is_bitwise_the_general_one():
+def test_cubature_window_variants_are_bitwise_equal():
     """The spherical window kernel's loop for one-pass keys above the linear section of the
     table (exponent table, floor by a rounded-down addition, no linear branch or pass filter)
-    performs the general loop's operations and roundings: the signal matrix is the same bits
-    with it on and off, on a shell whose far keys take it and whose self and neighbour keys
-    (windows reaching below r1 = 10) do not."""
+    performs the general loop's operations and roundings, and every key is integrated by one
+    warp whatever order the keys are taken in: the signal matrix is the same bits with the
+    loop on and off and with the far keys in key order and in window-start order, on a shell
+    whose far keys take the loop and whose self and neighbour keys (windows reaching below
+    r1 = 10) do not."""
     sv, cells = synth.shell_survey(8, 8, 16)
     bands = synth.band_edges(20, 0.0, 0.4)
     got = {}
-    for on in ("1", "0"):
+    for opts in (("1", "key"), ("0", "key"), ("1", "window")):
         e = api.Engine(api.make_config(sv, bands=bands, layout=O.LAYOUT_LOG4096,
-                                       extra=[f"cubature.log_keys = {on}"]))
+                                       extra=[f"cubature.log_keys = {opts[0]}", f"cubature.order = {opts[1]}"]))
         e.set_pk(*PK)
-        got[on] = [e.signal_block(cells, table=t) for t in (0, 10, 20)]
+        got[opts] = [e.signal_block(cells, table=t) for t in (0, 10, 20)]
         e.close()
-    for j in range(3):
-        assert np.array_equal(got["1"][j], got["0"][j]), j
+    for opts in (("0", "key"), ("1", "window")):
+        for j in range(3):
+            assert np.array_equal(got[("1", "key")][j], got[opts][j]), (opts, j)
 
 
 @pytest.mark.parametrize("gauss", [2, 3, 5])
