@@ -8,8 +8,8 @@
 //
 //   1. tridiag_kernel: Householder reduction A = Q T Q^T of every block, one cluster of four CTAs
 //      per block (the lower triangle stays in L2; each step is a fused pass that applies the
-//      previous reflector's rank-2 update and forms the next reflector's product A v).  The
-//      O(n^2) pass runs in double-FP32 (df64.h), the O(n) work of each step in FP64.
+//      previous reflector's rank-2 update and forms the next reflector's product A v).  It runs
+//      in double-FP32 (df64.h) but the reflectors' scalars (FP64, one warp).
 //   2. spectrum_kernel: every eigenvalue of every T by bisection on FP32 Sturm counts of the
 //      power-of-two-scaled T (to ~1e-6 of the block norm): enough to decide which block
 //      eigenvalues can reach the global cut.
@@ -60,29 +60,61 @@ __device__ double cta_sum(double x, double* red) {
     return r;
 }
 
-// Householder reflector of the pivot column c held in col[c..n): d_c = col[c], and
-// H = I - tau v v^T with v[c+1] = 1 maps col[c+1..n) onto beta e_{c+1}.  Every CTA of the
-// cluster computes it from the same data and gets the same bits.
-__device__ void householder(int n, int c, const double* col, double* v, double* tau_out, double* beta_out,
-                            double* red) {
+// Deterministic CTA-wide double-FP32 sum (lane 0's butterfly result of each warp, then warp
+// 0's): the same inputs give the same bits in every CTA of the cluster.
+__device__ df cta_sum_df(df x, float2* red) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o; o >>= 1)
+        x = df_add(x, df{__shfl_xor_sync(0xffffffffu, x.h, o), __shfl_xor_sync(0xffffffffu, x.l, o)});
+    if (lane == 0) red[warp] = df_pack(x);
+    __syncthreads();
+    if (warp == 0) {
+        df y = lane < (int)(blockDim.x >> 5) ? df_unpack(red[lane]) : df{0.f, 0.f};
+#pragma unroll
+        for (int o = 16; o; o >>= 1)
+            y = df_add(y, df{__shfl_xor_sync(0xffffffffu, y.h, o), __shfl_xor_sync(0xffffffffu, y.l, o)});
+        if (lane == 0) red[32] = df_pack(y);
+    }
+    __syncthreads();
+    const df r = df_unpack(red[32]);
+    __syncthreads();
+    return r;
+}
+
+// Householder reflector of the pivot column c held in col[c..n) (double-FP32): H = I - tau v v^T
+// with v[c+1] = 1 maps col[c+1..n) onto beta e_{c+1}.  The sum of squares and v in double-FP32,
+// the scalars in FP64 by warp 0 alone (the FP64 pipe issues at 1/64 of the FP32 rate: once per
+// CTA, not in every warp).  sc: tau, beta (FP64); sc2: tau, 1/(x0 - beta) as (hi, lo) pairs.
+// Every CTA of the cluster computes it from the same data and gets the same bits.
+__device__ void householder_df(int n, int c, const float2* col, float2* v, double* sc, float2* sc2, float2* red) {
     const int t = threadIdx.x;
-    double s = 0.0;
-    for (int i = c + 2 + t; i < n; i += blockDim.x) s += col[i] * col[i];
-    const double s2 = cta_sum(s, red);
-    const double x0 = col[c + 1];
-    double tau = 0.0, beta = x0, scal = 0.0;
-    if (s2 > 0.0) {
-        const double nrm = sqrt(x0 * x0 + s2);
-        beta = x0 >= 0.0 ? -nrm : nrm;
-        tau = (beta - x0) / beta;
-        scal = 1.0 / (x0 - beta);
+    df s{0.f, 0.f};
+    for (int i = c + 2 + t; i < n; i += blockDim.x) {
+        const df x = df_unpack(col[i]);
+        s = df_fma(s, x, x);
     }
-    for (int i = c + 2 + t; i < n; i += blockDim.x) v[i] = col[i] * scal;
-    if (t == 0) {
-        v[c + 1] = 1.0;
-        *tau_out = tau;
-        *beta_out = beta;
+    const df s2 = cta_sum_df(s, red);
+    if (t < 32) {
+        const double x0 = df_to(df_unpack(col[c + 1])), s2d = df_to(s2);
+        double tau = 0.0, beta = x0, scal = 0.0;
+        if (s2d > 0.0) {
+            const double nrm = sqrt(x0 * x0 + s2d);
+            beta = x0 >= 0.0 ? -nrm : nrm;
+            tau = (beta - x0) / beta;
+            scal = 1.0 / (x0 - beta);
+        }
+        if (t == 0) {
+            sc[0] = tau;
+            sc[1] = beta;
+            sc2[0] = df_pack(df_from(tau));
+            sc2[1] = df_pack(df_from(scal));
+        }
     }
+    __syncthreads();
+    const df scal = df_unpack(sc2[1]);
+    for (int i = c + 2 + t; i < n; i += blockDim.x) v[i] = df_pack(df_mul(df_unpack(col[i]), scal));
+    if (t == 0) v[c + 1] = make_float2(1.f, 0.f);
 }
 
 // One fused pass over the columns j in [j0, n) of the lower triangle, in double-FP32 (the
@@ -139,8 +171,9 @@ __device__ void reduce_warp_rows(int n, int i0, const float2* pw, float2* out) {
 
 // Householder tridiagonalisation of block b = blockIdx.x / kCl (column-major, lower triangle
 // read and updated; n >= 3).  Outputs T (dg, eg), the reflectors V[b][c][i] as (hi, lo) float
-// pairs (v[c+1] = 1) and tau.  The O(n) work of each step (the reflector, w) is FP64; the
-// O(n^2) fused pass is double-FP32.
+// pairs (v[c+1] = 1) and tau.  Everything runs in double-FP32 but the reflector's scalars
+// (FP64, one warp): the O(n^2) fused pass and the O(n) work of each step (p = A v from the
+// cluster, w, the pivot column, v).
 __global__ void __cluster_dims__(kCl, 1, 1) __launch_bounds__(kTT, 1)
 tridiag_kernel(int n, double* __restrict__ Aall, double* __restrict__ Vall, double* __restrict__ tau,
                double* __restrict__ dg, double* __restrict__ eg) {
@@ -151,32 +184,30 @@ tridiag_kernel(int n, double* __restrict__ Aall, double* __restrict__ Vall, doub
     const int t = threadIdx.x, warp = t >> 5;
     double* A = Aall + (size_t)b * n * n;
     float2* V = reinterpret_cast<float2*>(Vall) + (size_t)b * n * n;
-    double* vk = sm;                  // FP64 copies for the O(n) work
-    double* wk = vk + n;
-    double* vn = wk + n;
-    double* col = vn + n;
-    float2* vk2 = reinterpret_cast<float2*>(col + n);  // (hi, lo) copies for the fused pass
-    float2* wk2 = vk2 + n;
+    float2* vk2 = reinterpret_cast<float2*>(sm);  // (hi, lo): v and w of the step being applied,
+    float2* wk2 = vk2 + n;                        // the next reflector, the pivot column
     float2* vn2 = wk2 + n;
-    float2* buf = vn2 + n;            // [2][n] this CTA's partial A v, read by the whole cluster
+    float2* col2 = vn2 + n;
+    float2* buf = col2 + n;           // [2][n] this CTA's partial A v, read by the whole cluster
     float2* pw = buf + 2 * n;         // [kTW][n] per-warp partial rows
-    double* red = reinterpret_cast<double*>(pw + (size_t)kTW * n);  // 40 doubles
-    double* scal = red + 40;          // tau of the next reflector, beta
+    float2* red = pw + (size_t)kTW * n;  // 40 pairs
+    double* sc = reinterpret_cast<double*>(red + 40);  // tau, beta of the next reflector
+    float2* sc2 = reinterpret_cast<float2*>(sc + 2);   // tau, 1/(x0 - beta) as pairs
     float2* pw_mine = pw + (size_t)warp * n;
     const int gwarp = rank * kTW + warp, nwarps = kCl * kTW;
+    const float2* A2 = reinterpret_cast<const float2*>(A);
 
     // pivot column 0 and the first reflector
-    for (int i = t; i < n; i += kTT) col[i] = A[i];
+    for (int i = t; i < n; i += kTT) col2[i] = df_pack(df_from(A[i]));
     __syncthreads();
-    householder(n, 0, col, vn, &scal[0], &scal[1], red);
+    householder_df(n, 0, col2, vn2, sc, sc2, red);
     __syncthreads();
-    for (int i = 1 + t; i < n; i += kTT) vn2[i] = df_pack(df_from(vn[i]));
     if (rank == 0) {
         for (int i = 1 + t; i < n; i += kTT) V[i] = vn2[i];
         if (t == 0) {
-            dg[(size_t)b * n] = col[0];
-            eg[(size_t)b * n] = scal[1];
-            tau[(size_t)b * n] = scal[0];
+            dg[(size_t)b * n] = df_to(df_unpack(col2[0]));
+            eg[(size_t)b * n] = sc[1];
+            tau[(size_t)b * n] = sc[0];
         }
     }
     for (int i = 1 + (t & 31); i < n; i += 32) pw_mine[i] = make_float2(0.f, 0.f);
@@ -187,48 +218,45 @@ tridiag_kernel(int n, double* __restrict__ Aall, double* __restrict__ Vall, doub
     cluster.sync();
 
     for (int c = 0; c <= n - 3; c++) {
-        const double tc = scal[0];
+        const df tc = df_unpack(sc2[0]);
         // (a) v_c, p_c = A v_c from the four CTAs (fixed order), w_c = y - (tau/2)(y.v) v
         const float2* rb[kCl];
 #pragma unroll
         for (int r = 0; r < kCl; r++) rb[r] = cluster.map_shared_rank(buf + (size_t)(c & 1) * n, r);
-        double part = 0.0;
+        df part{0.f, 0.f};
         for (int i = c + 1 + t; i < n; i += kTT) {
             df p = df_unpack(rb[0][i]);
 #pragma unroll
             for (int r = 1; r < kCl; r++) p = df_add(p, df_unpack(rb[r][i]));
-            const double y = tc * df_to(p);
-            vk[i] = vn[i];
-            vk2[i] = vn2[i];
-            wk[i] = y;
-            part += y * vn[i];
+            const df y = df_mul(tc, p);
+            const float2 v = vn2[i];
+            vk2[i] = v;
+            wk2[i] = df_pack(y);
+            part = df_fma(part, y, df_unpack(v));
         }
-        const double alpha = 0.5 * tc * cta_sum(part, red);
-        for (int i = c + 1 + t; i < n; i += kTT) {
-            wk[i] -= alpha * vk[i];
-            wk2[i] = df_pack(df_from(wk[i]));
-        }
+        const df yv = cta_sum_df(part, red);
+        const df alpha = df_mul(tc, df{0.5f * yv.h, 0.5f * yv.l});
+        for (int i = c + 1 + t; i < n; i += kTT)
+            wk2[i] = df_pack(df_fms(df_unpack(wk2[i]), alpha, df_unpack(vk2[i])));
         __syncthreads();
         // (b) pivot column c+1 under the update, the next reflector
         const int c1 = c + 1;
-        const double vkc = vk[c1], wkc = wk[c1];
-        const float2* A2 = reinterpret_cast<const float2*>(A);
+        const df vkc = df_unpack(vk2[c1]), wkc = df_unpack(wk2[c1]);
         for (int i = c1 + t; i < n; i += kTT) {
-            double a = df_to(df_unpack(A2[(size_t)c1 * n + i]));
-            a = fma(-vk[i], wkc, a);
-            a = fma(-wk[i], vkc, a);
-            col[i] = a;
+            df a = df_unpack(A2[(size_t)c1 * n + i]);
+            a = df_fms(a, df_unpack(vk2[i]), wkc);
+            a = df_fms(a, df_unpack(wk2[i]), vkc);
+            col2[i] = df_pack(a);
         }
         __syncthreads();
-        householder(n, c1, col, vn, &scal[0], &scal[1], red);
+        householder_df(n, c1, col2, vn2, sc, sc2, red);
         __syncthreads();
-        for (int i = c1 + 1 + t; i < n; i += kTT) vn2[i] = df_pack(df_from(vn[i]));
         if (rank == 0) {
             for (int i = c1 + 1 + t; i < n; i += kTT) V[(size_t)c1 * n + i] = vn2[i];
             if (t == 0) {
-                dg[(size_t)b * n + c1] = col[c1];
-                eg[(size_t)b * n + c1] = scal[1];
-                tau[(size_t)b * n + c1] = scal[0];
+                dg[(size_t)b * n + c1] = df_to(df_unpack(col2[c1]));
+                eg[(size_t)b * n + c1] = sc[1];
+                tau[(size_t)b * n + c1] = sc[0];
             }
         }
         // (c) columns c+2 .. n-1: update by (v_c, w_c); partial A v_{c+1} for the next step
@@ -242,7 +270,6 @@ tridiag_kernel(int n, double* __restrict__ Aall, double* __restrict__ Vall, doub
         cluster.sync();
     }
     if (rank == 0 && t == 0) {
-        const float2* A2 = reinterpret_cast<const float2*>(A);
         dg[(size_t)b * n + n - 1] = df_to(df_unpack(A2[(size_t)(n - 1) * n + n - 1]));
         eg[(size_t)b * n + n - 1] = 0.0;
         tau[(size_t)b * n + n - 1] = 0.0;
@@ -618,7 +645,7 @@ __global__ void __launch_bounds__(kBT) backtransform_kernel(VecArgs a, const dou
 
 }  // namespace
 
-size_t blockeig_tridiag_smem(int n) { return sizeof(double) * ((size_t)(9 + kTW) * n + 48); }
+size_t blockeig_tridiag_smem(int n) { return sizeof(double) * ((size_t)(6 + kTW) * n + 48); }
 
 bool blockeig_supported(int n) {
     return n >= 3 && n <= kMaxN && blockeig_tridiag_smem(n) <= (size_t)max_dynamic_smem((const void*)tridiag_kernel);

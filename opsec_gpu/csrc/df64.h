@@ -47,6 +47,14 @@ __device__ __forceinline__ df df_fma(df acc, df x, df y) {
 }
 // acc - x * y
 __device__ __forceinline__ df df_fms(df acc, df x, df y) { return df_fma(acc, {-x.h, -x.l}, y); }
+// x * y
+__device__ __forceinline__ df df_mul(df x, df y) {
+    const float p = x.h * y.h;
+    float e = fmaf(x.h, y.h, -p);
+    e = fmaf(x.h, y.l, e);
+    e = fmaf(x.l, y.h, e);
+    return fast_two_sum(p, e);
+}
 // x + y
 __device__ __forceinline__ df df_add(df x, df y) {
     float t;
