@@ -755,8 +755,13 @@ __global__ void __launch_bounds__(kPartThreads) part_scatter_kernel(long long nk
 // units (k = 18 for 4^3 x 4^3 points), rounded once in FP32 (the product),
 // split into its nearest integer and the rest in 2^-k units, and added with
 // two native 32-bit integer shared-memory atomics; neither partial sum can
-// overflow within a pass, at whose end they move into a 64-bit integer
-// histogram.  The sums are exact and independent of the order of the atomics.
+// overflow within a pass, at whose end the dot products combine them into the
+// 64-bit value.  The sums are exact and independent of the order of the atomics.
+// Each warp keeps two copies of its histogram, one per half-warp, interleaved
+// (copy c of bin b at word 2b + c): the lanes' bins collide in shared-memory
+// banks, and the copies cut the wavefronts per atomic from 3.6 to 2.7 (a model
+// of the 32k-cell shell's bins; no extra memory: the 64-bit staging histogram
+// is gone).
 // (64-bit integer shared atomics instead: cubature 90 ms against 66 ms at 32k
 // cells.)
 // (FP32 shared-memory atomics were slower -- the counters showed them retried
@@ -812,14 +817,11 @@ __device__ __forceinline__ void index_log(const Lookup& lk, const float4* s_ce, 
     }
 }
 
-// Move the partial sums into the 64-bit histogram (units of 2^-fbits of the coarse quantum:
-// exact) and clear them.  Warp-wide.
-__device__ __forceinline__ void flush_fixed(int* hqa, int* hqb, long long* hm, int n, int lane, int fbits) {
-    __syncwarp();
-    for (int b = lane; b < n; b += 32) {
-        hm[b] += ((long long)hqa[b] << fbits) + hqb[b];
-        hqa[b] = 0;
-        hqb[b] = 0;
+// Clear bins [0, n) of both copies.  Warp-wide.
+__device__ __forceinline__ void clear_fixed(int* hqa, int* hqb, int n, int lane) {
+    for (int j = lane; j < 2 * n; j += 32) {
+        hqa[j] = 0;
+        hqb[j] = 0;
     }
     __syncwarp();
 }
@@ -827,7 +829,7 @@ __device__ __forceinline__ void flush_fixed(int* hqa, int* hqb, long long* hm, i
 constexpr int kMaxPasses = 8;  // passes over the point pairs for windows wider than one histogram
 constexpr int kDotChunk = 16;  // bins summed in FP32 per compensated addition in the window dot products
 
-// Dot products of one pass's histogram (64-bit, bins s0 .. s0 + segw - 1 of the key's window)
+// Dot products of one pass's histogram (bins s0 .. s0 + segw - 1 of the key's window)
 // with every table, added into Q.  Two work items per table, alternate chunks of kDotChunk
 // bins, spread over the lanes (table t: items 2t and 2t+1 on neighbouring lanes, combined by
 // one shuffle).  Far keys: FP32 within a chunk, the chunk sums added by two-sum into an FP32
@@ -835,20 +837,31 @@ constexpr int kDotChunk = 16;  // bins summed in FP32 per compensated addition i
 // reaches the linear section of the table or needs several passes (self and adjacent
 // cells, whose integrals cancel strongly over several periods of a band table) and every
 // key with `dot64`: compensated FP32 -- exact products by FMA, two-sum accumulation, the bin
-// values as FP32 high + low parts -- about FP64 accuracy.  hp and hl are the words of the
-// (now zero) partial sums.  Warp-wide.
-__device__ __forceinline__ void window_dots(const CubatureArgs& a, const WinPlan& w, const long long* hm, float* hp,
-                                            float* hl, int key, int wx, int s0, int segw, int pass, bool precise,
-                                            int lane) {
+// values as FP32 high + low parts -- about FP64 accuracy.  The bin values replace the partial
+// sums in place: hp[b] is word b of hqa, hl[b] word b of hqb.  Warp-wide.
+__device__ __forceinline__ void window_dots(const CubatureArgs& a, const WinPlan& w, int* hqa, int* hqb, int key,
+                                            int wx, int s0, int segw, int pass, bool precise, int lane) {
     const int ntab = a.ntab;
-    for (int b = lane; b < segw; b += 32) {
-        if (precise) {
-            const double v = (double)hm[b] * (double)w.qfine;
-            const float hi = (float)v;
-            hp[b] = hi;
-            hl[b] = (float)(v - (double)hi);
-        } else {
-            hp[b] = (float)hm[b] * w.qfine;
+    float* hp = reinterpret_cast<float*>(hqa);
+    float* hl = reinterpret_cast<float*>(hqb);
+    // bin b's two copies are words 2b, 2b+1, and its value goes to word b: the 32 bins of a
+    // sweep read words [64k, 64k + 64) and write [32k, 32k + 32), whose inputs earlier sweeps
+    // (or this one, before the barrier) have read
+    for (int b0 = 0; b0 < segw; b0 += 32) {
+        const int b = b0 + lane;
+        long long v = 0;
+        if (b < segw)
+            v = (((long long)hqa[2 * b] + hqa[2 * b + 1]) << w.fbits) + (long long)hqb[2 * b] + hqb[2 * b + 1];
+        __syncwarp();
+        if (b < segw) {
+            if (precise) {
+                const double x = (double)v * (double)w.qfine;
+                const float hi = (float)x;
+                hp[b] = hi;
+                hl[b] = (float)(x - (double)hi);
+            } else {
+                hp[b] = (float)v * w.qfine;
+            }
         }
     }
     __syncwarp();
@@ -920,9 +933,8 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
     constexpr int kWarps = FarShape<NG>::kWarps;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float4* pts = reinterpret_cast<float4*>(smem_raw);                  // [kWarps][2][NP]
-    long long* mas = reinterpret_cast<long long*>(pts + kWarps * 2 * NP);  // [kWarps][Wkey]: 64-bit histogram
-    int* pa = reinterpret_cast<int*>(mas + kWarps * w.Wkey);               // [kWarps][Wkey]: partial sums, integer part
-    int* pb = pa + kWarps * w.Wkey;                                        // [kWarps][Wkey]: partial sums, fraction
+    int* pa = reinterpret_cast<int*>(pts + kWarps * 2 * NP);  // [kWarps][Wkey][2]: partial sums, integer part
+    int* pb = pa + 2 * kWarps * w.Wkey;                       // [kWarps][Wkey][2]: partial sums, fraction
     __shared__ int s_ci[kMaxExp];
     __shared__ float s_cf[kMaxExp];
     __shared__ float4 s_kt[kLogN];
@@ -936,10 +948,9 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     float4* P2 = pts + warp * 2 * NP;
     float4* P2l = P2 + NP;
-    long long* hm = mas + warp * w.Wkey;
-    int* hqa = pa + warp * w.Wkey;
-    int* hqb = pb + warp * w.Wkey;
-    float* hp = reinterpret_cast<float*>(hqa);  // the same words: FP32 histogram values for the dot products
+    int* hqa = pa + 2 * warp * w.Wkey;
+    int* hqb = pb + 2 * warp * w.Wkey;
+    const int cpy = lane >> 4;  // this lane's histogram copy
     const bool periodic = (a.coordsys == 1 && a.L > 0);
     const float Lh = (float)a.L, Ll = (float)(a.L - (double)Lh), hL = 0.5f * Lh;
     const int nfar = *w.nfar;
@@ -991,12 +1002,7 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
                     f_hi = r * r;
                 }
             }
-            for (int j = lane; j < segw; j += 32) {
-                hm[j] = 0;
-                hqa[j] = 0;
-                hqb[j] = 0;
-            }
-            __syncwarp();
+            clear_fixed(hqa, hqb, segw, lane);
             // Mirror symmetry of the innermost axis (phi on spherical grids, z on Cartesian
             // ones): the Gauss nodes are symmetric about each cell's centre, so the pair of
             // innermost nodes (l_p, l_q) and (NG-1-l_q, NG-1-l_p) have the same separation
@@ -1042,15 +1048,15 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
                                 bad += out;
                                 const float ww = (lsum < NG - 1 ? 2.f : 1.f) * Ah.w * B.w;
                                 const float wq = ww * w.qinv;  // fixed point: the largest pair weight -> 2^k units
-                                add_fixed(hqa, hqb, bi, fmaf(-wq, fr, wq), w.qfrac);
-                                add_fixed(hqa, hqb, bi + 1, wq * fr, w.qfrac);
+                                add_fixed(hqa, hqb, 2 * bi + cpy, fmaf(-wq, fr, wq), w.qfrac);
+                                add_fixed(hqa, hqb, 2 * bi + 2 + cpy, wq * fr, w.qfrac);
                             }
                         }
                     }
                 }
             }
-            flush_fixed(hqa, hqb, hm, segw, lane, w.fbits);
-            window_dots(a, w, hm, hp, reinterpret_cast<float*>(hqb), key, wn.x, s0, segw, pass,
+            __syncwarp();
+            window_dots(a, w, hqa, hqb, key, wn.x, s0, segw, pass,
                         w.dot64 || npass > 1 || wn.x < lk.n1, lane);
         }
         if (bad) atomicAdd(w.violations, bad);
@@ -1076,9 +1082,8 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
     constexpr int kWarps = FarShape<NG>::kWarps;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float4* sphw = reinterpret_cast<float4*>(smem_raw);        // [kWarps][NC]: the key's phi-node pairs
-    long long* mas = reinterpret_cast<long long*>(sphw + kWarps * NC);  // [kWarps][Wkey]: 64-bit histogram
-    int* pa = reinterpret_cast<int*>(mas + kWarps * w.Wkey);            // [kWarps][Wkey]: partial sums, integer part
-    int* pb = pa + kWarps * w.Wkey;                                     // [kWarps][Wkey]: partial sums, fraction
+    int* pa = reinterpret_cast<int*>(sphw + kWarps * NC);  // [kWarps][Wkey][2]: partial sums, integer part
+    int* pb = pa + 2 * kWarps * w.Wkey;                    // [kWarps][Wkey][2]: partial sums, fraction
     __shared__ int s_ci[kMaxExp];
     __shared__ float s_cf[kMaxExp];
     __shared__ float4 s_kt[kLogN];
@@ -1106,10 +1111,9 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     float4* SP = sphw + warp * NC;
-    long long* hm = mas + warp * w.Wkey;
-    int* hqa = pa + warp * w.Wkey;
-    int* hqb = pb + warp * w.Wkey;
-    float* hp = reinterpret_cast<float*>(hqa);  // the same words: FP32 histogram values for the dot products
+    int* hqa = pa + 2 * warp * w.Wkey;
+    int* hqb = pb + 2 * warp * w.Wkey;
+    const int cpy = lane >> 4;  // this lane's histogram copy
     const int nfar = *w.nfar;
     for (int kk = blockIdx.x * kWarps + warp; kk < nfar; kk += gridDim.x * kWarps) {
         const int key = w.order[kk];
@@ -1140,12 +1144,7 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
                     f_hi = r * r;
                 }
             }
-            for (int j = lane; j < segw; j += 32) {
-                hm[j] = 0;
-                hqa[j] = 0;
-                hqb[j] = 0;
-            }
-            __syncwarp();
+            clear_fixed(hqa, hqb, segw, lane);
             // One pass whose window starts above the linear section of the table (most far
             // keys): every pair has r^2 >= r1^2 and its bin is in the histogram, so the loop
             // below needs neither the linear branch nor the pass filter.
@@ -1187,8 +1186,8 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
                             }
                             const float ww = wpq * sp.z;
                             const float wq = ww * w.qinv;
-                            add_fixed(hqa, hqb, bi, fmaf(-wq, fr, wq), w.qfrac);
-                            add_fixed(hqa, hqb, bi + 1, wq * fr, w.qfrac);
+                            add_fixed(hqa, hqb, 2 * bi + cpy, fmaf(-wq, fr, wq), w.qfrac);
+                            add_fixed(hqa, hqb, 2 * bi + 2 + cpy, wq * fr, w.qfrac);
                         }
                         continue;
                     }
@@ -1214,14 +1213,14 @@ __global__ void __launch_bounds__(FarShape<NG>::kWarps * 32, 2)
                             bad += out;
                             const float ww = wpq * sp.z;
                             const float wq = ww * w.qinv;  // fixed point: the largest pair weight -> 2^k units
-                            add_fixed(hqa, hqb, bi, fmaf(-wq, fr, wq), w.qfrac);
-                            add_fixed(hqa, hqb, bi + 1, wq * fr, w.qfrac);
+                            add_fixed(hqa, hqb, 2 * bi + cpy, fmaf(-wq, fr, wq), w.qfrac);
+                            add_fixed(hqa, hqb, 2 * bi + 2 + cpy, wq * fr, w.qfrac);
                         }
                     }
                 }
             }
-            flush_fixed(hqa, hqb, hm, segw, lane, w.fbits);
-            window_dots(a, w, hm, hp, reinterpret_cast<float*>(hqb), key, wn.x, s0, segw, pass,
+            __syncwarp();
+            window_dots(a, w, hqa, hqb, key, wn.x, s0, segw, pass,
                         w.dot64 || npass > 1 || wn.x < lk.n1, lane);
         }
         if (bad) atomicAdd(w.violations, bad);
@@ -1338,7 +1337,7 @@ WinLayout win_layout(const KeySpace& ks, int nx, int ntab, int ng) {
 template <int NG>
 size_t far_smem(const WinPlan& w, bool sph) {
     const size_t pts = sph ? sizeof(float4) * (NG * (NG + 1) / 2) : sizeof(float4) * 2 * FarShape<NG>::NP;
-    return FarShape<NG>::kWarps * (pts + (sizeof(long long) + 2 * sizeof(int)) * w.Wkey);
+    return FarShape<NG>::kWarps * (pts + 4 * sizeof(int) * w.Wkey);
 }
 
 // Far keys by windows, near keys by table groups in list mode.  Returns false (nothing
