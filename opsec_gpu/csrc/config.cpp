@@ -140,12 +140,12 @@ void configure(opsec_gpu* c, const std::map<std::string, std::string>& kv) {
     if (c->proj_chunk < 1) fail(OPSEC_ERR_CONFIG, "projection.chunk must be >= 1");
     if (has("azimuthal.gemm")) {
         const std::string& v = get("azimuthal.gemm");
-        if (v == "f64")
-            c->az_gemm64 = 1;
-        else if (v == "f32")
-            c->az_gemm64 = 0;
-        else
-            fail(OPSEC_ERR_CONFIG, "azimuthal.gemm must be f64 or f32");
+        if (v == "f64" || v == "f32" || v == "tc") {
+            c->az_gemm64 = v == "f64";
+            c->az_tc = v == "tc";
+        } else {
+            fail(OPSEC_ERR_CONFIG, "azimuthal.gemm must be tc, f32 or f64");
+        }
     }
     if (has("azimuthal.parity")) c->az_parity = get("azimuthal.parity") != "0";
     if (has("azimuthal.eig")) {

@@ -92,6 +92,7 @@ struct opsec_gpu {
     long long fail_alloc = -1;           // opsec_gpu_fail_alloc: device allocations left before one fails
     int cub_exact = 1;
     int az_gemm64 = 0;
+    int az_tc = 1;  // block projection GEMMs on the tensor cores (az_tc.cu); 0: cuBLAS SGEMM
     bool cub_reflect = true;
     int cub_window = 1;
     int win_key = 384, win_flush = 8, win_dot64 = 0, win_logkeys = 1, win_keyorder = 1;

@@ -185,6 +185,16 @@ void launch_azimuthal_scatter(int M, int nbands, const int* mode_m, const int* m
 void launch_azimuthal_scatter(int M, int nbands, const int* mode_m, const int* mode_cls, const int* mode_col,
                               const long long* blk_off, const int* blk_K, long long csize, const float* C, float* Dp,
                               cudaStream_t st, long long* launches);
+// The block projection on the tensor cores (az_tc.cu): T = S_p(m) U_m and C_m = U_m^T T for np
+// bands, 3-term TF32 products.  S [np][nblk][H][H], U [ncol][H], T scratch [np][ncol][H], C
+// [np][csize]; Km, base, off device tables (kmh: Km on the host); work: az_tc_work_bytes; err: a
+// device word raised when a bounded wait gives up.
+bool az_tc_supported(int H);
+size_t az_tc_work_bytes(int nblk, int np, const std::vector<int>& kmh, int H);
+void launch_az_tc(int H, int nblk, int ncol, int np, const float* S, const float* U, float* T, float* C,
+                  long long csize, const int* Km, const int* base, const long long* off, const std::vector<int>& kmh,
+                  void* work, size_t work_bytes, int* err, long long wait_cycles, cudaStream_t s,
+                  long long* launches);
 // Modes from block eigenvectors: B[mode][h*Nphi + f] = U_m[h][idx] * trig(m f)
 void launch_assemble_modes(int H, int Nphi, int Nmu, int npar, int nmodes, const int* sel_b, const int* sel_idx,
                            const int* sel_kind, const double* U, double* modes, cudaStream_t st, long long* launches);

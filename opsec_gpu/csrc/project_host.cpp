@@ -7,7 +7,7 @@ struct AzPlan {
     long long csize;
     int Kmax;
     double flops;
-    const int *col_m, *col_idx, *mode_m, *mode_cls, *mode_col, *Km_dev;
+    const int *col_m, *col_idx, *mode_m, *mode_cls, *mode_col, *Km_dev, *base_dev;
     const std::vector<int>* Km;
     const std::vector<int>* base;
     const std::vector<long long>* off;
@@ -48,11 +48,20 @@ T* az_blocks(opsec_gpu* c, const AzPlan& a) {
     const size_t nU = (size_t)a.ncol * H, nS = (size_t)nblk * H * H, nT = (size_t)H * std::max(a.Kmax, 1),
                  nC = (size_t)std::max(a.csize, 1LL) * a.nb;
     const int bpp = (int)std::max<size_t>(1, std::min<size_t>(a.nb, (size_t(2) << 30) / (sizeof(T) * nS)));
-    ws.alloc(sizeof(T) * (nU + nS * bpp + nT * bpp + nC));
+    // tensor-core products (FP32 path): T of every band of a batch, [band][ncol][H], then the
+    // tiles and the error word
+    const bool tcg = sizeof(T) == sizeof(float) && c->az_tc && az_tc_supported(H);
+    const size_t nTb = tcg ? (size_t)a.ncol * H * bpp : nT * bpp;
+    const size_t tc_bytes = tcg ? az_tc_work_bytes(nblk, bpp, *a.Km, H) : 0;
+    ws.alloc(sizeof(T) * (nU + nS * bpp + nTb + nC) + tc_bytes + 512);
     T* U = reinterpret_cast<T*>(ws.p);
     T* Sb = U + nU;
     T* Tm = Sb + nS * bpp;
-    T* Cm = Tm + nT * bpp;
+    T* Cm = Tm + nTb;
+    unsigned char* tcw = reinterpret_cast<unsigned char*>(Cm + nC);
+    tcw = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(tcw) + 255) & ~uintptr_t(255));
+    int* tc_err = reinterpret_cast<int*>(tcw);
+    if (tcg) OPSEC_CUDA(cudaMemsetAsync(tc_err, 0, sizeof(int), c->stream));
     // the block eigenvectors the modes use
     launch_gather_block_vectors(H, a.ncol, a.col_m, a.col_idx, c->S.p, U, c->stream, &c->launches);
     for (int p0 = 0; p0 < a.nb; p0 += bpp) {
@@ -64,6 +73,14 @@ T* az_blocks(opsec_gpu* c, const AzPlan& a) {
             if (g_clock) g_clock->end(c->stream);
         }
         if (g_clock) g_clock->begin("azimuthal_gemm", c->stream, a.flops * np);
+        if (tcg) {
+            launch_az_tc(H, nblk, a.ncol, np, reinterpret_cast<const float*>(Sb), reinterpret_cast<const float*>(U),
+                         reinterpret_cast<float*>(Tm), reinterpret_cast<float*>(Cm + (size_t)p0 * a.csize), a.csize,
+                         a.Km_dev, a.base_dev, c->az_off.p, *a.Km, tcw + 256, tc_bytes, tc_err,
+                         c->proj_wait, c->stream, &c->launches);
+            if (g_clock) g_clock->end(c->stream);
+            continue;
+        }
         for (int m = 0; m < nblk; m++) {
             const int K = (*a.Km)[m];
             if (K == 0) continue;
@@ -78,6 +95,12 @@ T* az_blocks(opsec_gpu* c, const AzPlan& a) {
             c->launches += 2;
         }
         if (g_clock) g_clock->end(c->stream);
+    }
+    if (tcg) {
+        int e = 0;
+        OPSEC_CUDA(cudaMemcpyAsync(&e, tc_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+        OPSEC_CUDA(cudaStreamSynchronize(c->stream));
+        if (e) fail(OPSEC_ERR_CUDA, "tensor-core block projection: a pipeline wait timed out");
     }
     return Cm;
 }
@@ -133,6 +156,7 @@ void project_azimuthal(opsec_gpu* c, int ncells, int M, bool packed) {
     ti.insert(ti.end(), mode_cls.begin(), mode_cls.end());
     ti.insert(ti.end(), mode_col.begin(), mode_col.end());
     ti.insert(ti.end(), Km.begin(), Km.end());
+    ti.insert(ti.end(), base.begin(), base.end());
     c->az_i.alloc(ti.size());
     OPSEC_CUDA(cudaMemcpyAsync(c->az_i.p, ti.data(), sizeof(int) * ti.size(), cudaMemcpyHostToDevice, c->stream));
     c->az_off.alloc(nblk);
@@ -143,6 +167,7 @@ void project_azimuthal(opsec_gpu* c, int ncells, int M, bool packed) {
     const int* d_mode_cls = d_mode_m + M;
     const int* d_mode_col = d_mode_cls + M;
     const int* d_Km = d_mode_col + M;
+    const int* d_base = d_Km + nblk;
     if (!c->blas) blas_check(cublasCreate(&c->blas), "cublasCreate");
     blas_check(cublasSetStream(c->blas, c->stream), "cublasSetStream");
     std::vector<double> nba(c->nbar_arc);
@@ -151,8 +176,8 @@ void project_azimuthal(opsec_gpu* c, int ncells, int M, bool packed) {
     OPSEC_CUDA(cudaMemcpyAsync(d_nba.p, nba.data(), sizeof(double) * nba.size(), cudaMemcpyHostToDevice, c->stream));
     double fl = 0;
     for (int m = 0; m < nblk; m++) fl += 2.0 * H * H * Km[m] + 2.0 * H * (double)Km[m] * Km[m];
-    AzPlan plan{H, nm, npar, nb, ncol, csize, Kmax, fl, d_col_m, d_col_idx, d_mode_m, d_mode_cls, d_mode_col, d_Km, &Km,
-                &base, &off, d_nba.p};
+    AzPlan plan{H,      nm,        npar,       nb,         ncol,       csize, Kmax,  fl, d_col_m,
+                d_col_idx, d_mode_m, d_mode_cls, d_mode_col, d_Km, d_base, &Km, &base, &off, d_nba.p};
     c->az_blockF = false;
     if (!packed && !c->az_gemm64) {
         // the Fisher sums read the block matrices directly: groups (block, trig class)

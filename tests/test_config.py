@@ -43,6 +43,7 @@ BAD = [
     ("sig.gauss = 7", "sig.gauss"),
     ("azimuthal.split = 17", "azimuthal.split"),
     ("azimuthal.gemm = f16", "azimuthal.gemm"),
+    ("azimuthal.gemm = tf32", "azimuthal.gemm"),
     ("cubature.window_bins = 8", "cubature.window_bins"),
     ("cubature.symmetry = half", "cubature.symmetry"),
     ("basis.samples = 0", "basis.samples"),

@@ -299,8 +299,9 @@ def test_fisher_build_end_to_end(name):
 
 def test_fisher_build_azimuthal_projection():
     """Full-sky shell, 8 x 8 x 16 = 1024 cells, 10 bands: the build projects
-    onto its own azimuthal modes block by block (FP64 GEMMs on the H x H
-    cosine transforms of each band).  Against the dense tensor-core projection
+    onto its own azimuthal modes block by block (the block GEMMs on the H x H
+    cosine transforms of each band: 3-term TF32 on the tensor cores, the
+    default, FP32 and FP64 by cuBLAS).  Against the dense tensor-core projection
     of the same modes (projection = tc) and against the oracle end to end."""
     sv, cells = synth.shell_survey(8, 8, 16)
     bands = synth.band_edges(10, 0.0, 0.2)
@@ -311,18 +312,19 @@ def test_fisher_build_azimuthal_projection():
     lam = np.sort(np.linalg.eigvalsh(S))[::-1]
     M = O.gap_nmodes(lam, 256, rel_gap=1e-4, span=64)
     out = {}
-    for name, extra in (("az32", ["azimuthal.gemm = f32"]), ("az64", ["azimuthal.gemm = f64"]),
-                        ("tc", ["projection = tc"]), ("simt", ["projection = simt"])):
+    for name, extra in (("aztc", ["azimuthal.gemm = tc"]), ("az32", ["azimuthal.gemm = f32"]),
+                        ("az64", ["azimuthal.gemm = f64"]), ("tc", ["projection = tc"]),
+                        ("simt", ["projection = simt"])):
         e = api.Engine(api.make_config(sv, bands=bands, extra=extra))
         e.set_pk(*PK)
         out[name] = e.fisher_build(cells, counts, M)
         e.close()
     scale = np.max(np.abs(out["simt"]["F"]))
-    d = {k: np.max(np.abs(out[k]["F"] - out["az64"]["F"])) / scale for k in ("az32", "tc", "simt")}
+    d = {k: np.max(np.abs(out[k]["F"] - out["az64"]["F"])) / scale for k in ("aztc", "az32", "tc", "simt")}
     print("F against the FP64 azimuthal projection: " + ", ".join(f"{k} {v:.2e}" for k, v in d.items()))
     assert max(d.values()) <= 1e-6, d
     ref = O.fisher_build(sv, cells, counts, *PK, bands, M)
-    for k in ("az32", "az64"):
+    for k in ("aztc", "az32", "az64"):
         rel = np.max(np.abs(out[k]["F"] - ref["est"]["F"])) / np.max(np.abs(ref["est"]["F"]))
         print(f"{k}: end-to-end Fisher rel err {rel:.2e}")
         check_estimates(out[k], ref, f"shell1024/{k}/end-to-end", tol=1e-6)
