@@ -257,12 +257,11 @@ __global__ void __launch_bounds__(kAzThreads, 1)
                     break;
                 }
                 tc_fence_after();
+                {
+                    float v[64];
+                    tmem_ld64(tmem + lane_base + (uint32_t)(b * AN), v);
 #pragma unroll
-                for (int cc = 0; cc < 2; cc++) {
-                    float v[32];
-                    tmem_ld32(tmem + lane_base + (uint32_t)(b * AN + 32 * cc), v);
-#pragma unroll
-                    for (int u = 0; u < 32; u++) R[32 * cc + u] += v[u];
+                    for (int u = 0; u < 64; u++) R[u] += v[u];
                 }
                 tc_fence_before();
                 __syncwarp();
