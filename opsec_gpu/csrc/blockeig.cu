@@ -602,6 +602,7 @@ __global__ void __launch_bounds__(kBT) backtransform_kernel(VecArgs a, const dou
     float2* v = z + (size_t)n * G;                // [n] reflector row
     float2* part = v + n;                         // [R][G]
     float2* f = part + R * G;                     // [G]
+    float2* tau2 = f + G;                         // [n] tau as (hi, lo) pairs
     const int t = threadIdx.x, g = t % G, rg = t / G;
     const size_t K = (size_t)a.ktot;
     const int ng = min(G, kc - c0);
@@ -611,9 +612,11 @@ __global__ void __launch_bounds__(kBT) backtransform_kernel(VecArgs a, const dou
     }
     const float2* V = reinterpret_cast<const float2*>(Vall) + (size_t)b * n * n;
     const double* tb = tau + (size_t)b * n;
+    for (int i = t; i < n; i += kBT) tau2[i] = df_pack(df_from(tb[i]));
+    __syncthreads();
     for (int c2 = n - 3; c2 >= 0; c2--) {
-        const double tc = tb[c2];
-        if (tc == 0.0) continue;  // uniform over the CTA
+        const float2 tc2 = tau2[c2];
+        if (tc2.x == 0.f) continue;  // uniform over the CTA
         __syncthreads();          // the previous update is done with v and f
         for (int i = c2 + 1 + t; i < n; i += kBT) v[i] = V[(size_t)c2 * n + i];
         __syncthreads();
@@ -629,7 +632,7 @@ __global__ void __launch_bounds__(kBT) backtransform_kernel(VecArgs a, const dou
         if (t < G) {
             df s = df_unpack(part[t]);
             for (int r = 1; r < R; r++) s = df_add(s, df_unpack(part[r * G + t]));
-            f[t] = df_pack(df_from(tc * df_to(s)));
+            f[t] = df_pack(df_mul(df_unpack(tc2), s));
         }
         __syncthreads();
         const df fg = df_unpack(f[g]);
@@ -676,15 +679,15 @@ void launch_blockeig_vectors(const BlockEigVectors& p, cudaStream_t s, long long
     if (g_clock) g_clock->end(s);
     cluster_kernel<<<p.nblk, 256, 0, s>>>(a, 1e-6);
     if (g_clock) g_clock->begin("blockeig_back", s, 2.0 * p.n * (double)p.n * p.ktot);
-    if (p.n <= 512) {
+    if (p.n <= 256) {  // 16 vectors per CTA above: twice the CTAs, two per SM
         constexpr int G = 32;
-        const size_t smem = sizeof(double) * ((size_t)p.n * G + p.n + kBT + G);
+        const size_t smem = sizeof(double) * ((size_t)p.n * G + 2 * p.n + kBT + G);
         OPSEC_CUDA(cudaFuncSetAttribute(backtransform_kernel<G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         max_dynamic_smem((const void*)backtransform_kernel<G>)));
         backtransform_kernel<G><<<dim3(p.nblk, (p.n + G - 1) / G), kBT, smem, s>>>(a, p.V, p.tau, p.out);
     } else {
         constexpr int G = 16;
-        const size_t smem = sizeof(double) * ((size_t)p.n * G + p.n + kBT + G);
+        const size_t smem = sizeof(double) * ((size_t)p.n * G + 2 * p.n + kBT + G);
         OPSEC_CUDA(cudaFuncSetAttribute(backtransform_kernel<G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         max_dynamic_smem((const void*)backtransform_kernel<G>)));
         backtransform_kernel<G><<<dim3(p.nblk, (p.n + G - 1) / G), kBT, smem, s>>>(a, p.V, p.tau, p.out);
