@@ -207,19 +207,17 @@ def tensor_roofline(s1, bf16, peak_kind):
             "avg_launch_ms": avg_s * 1000, "launches": int(s1["count"])}
 
 
-# Instructions one point pair costs in the far-key window kernel's inner loop, counted from
-# the source (opsec_gpu/csrc/cubature.cu, exact_index and the histogram update): two shared
-# loads of the second point, three FP32-pair differences (24), r^2 as an FP32 pair (27), the
-# log2(r^2) split into exponent, table slot and series (about 30 with three shared loads and
-# the clamps), the window offset and its check (4), the two weights and two shared atomics (7),
-# loop control (about 2).
-FAR_OPS_PER_PAIR = 100
+# Lane instructions the spherical far-key window kernel executes per algorithmic point pair (the
+# 4096 Gauss-point pairs of a key; the phi-node mirror symmetry evaluates 10 of every 16),
+# everything included (pair loop, histograms, dot products, key decode), from one ncu capture on
+# the inner half of the 32k-cell shell (profiles/cubature_far_sph_c2inner.md: 1.0759e10 warp
+# instructions x 32 lanes over 1,118,464 keys x 4096 pairs).
+FAR_OPS_PER_PAIR = 1.0758645e10 * 32 / (1118464 * 4096)
 
-# DRAM bytes (read + written) per canonical key of the spherical window kernel, from one ncu
-# capture on the inner half of the 32k-cell shell (profiles/cubature_far_sph_c2inner.md:
-# 1.114 GB + 1.239 GB over 1,118,464 keys); the kernel's traffic grows with the keys it
+# DRAM bytes (read + written) per canonical key of the spherical window kernel, from the same
+# capture (101.5 MB + 376.8 MB over 1,118,464 keys); the kernel's traffic grows with the keys it
 # integrates (Q written per key and table), so a launch's traffic is this x its keys.
-FAR_TRAFFIC_PER_KEY = (1.114271e9 + 1.239336e9) / 1118464
+FAR_TRAFFIC_PER_KEY = (101.491968e6 + 376.818944e6) / 1118464
 
 
 def roofline(stats, clk, hbm, bf16, peak_kind, ntab):
@@ -231,13 +229,12 @@ def roofline(stats, clk, hbm, bf16, peak_kind, ntab):
     if dom in ("cubature", "cubature_far") and stats.get("cubature_far", {}).get("count", 0) > 0:
         # The cubature stage's dominant kernel is the far-key window kernel: per key one pass over
         # the 4096 Gauss-point pairs scatters interpolation weights into a bin histogram, then one
-        # dot product per table.  Against HBM (the roofline bound reported): its algorithmic bytes
-        # are the Q values it must write, 8 bytes per key and table (its inputs -- per-arc node
-        # tables, the bin-major xi tables -- are a few MB and stay in L2); it is far from that
-        # bound.  What bounds it is instruction issue (roofline_issue below): point pairs, each
-        # FAR_OPS_PER_PAIR instructions of the direct exact method, against 4 schedulers x 32
-        # lanes per clock per SM (no measured figure exists for issue: derived from the SM count
-        # and the sampled clock).
+        # dot product per table.  Against HBM (roofline_hbm): its algorithmic bytes are the Q
+        # values it must write, 8 bytes per key and table (its inputs -- per-arc node tables, the
+        # bin-major xi tables -- are a few MB and stay in L2); it is far from that bound.  What
+        # bounds it is instruction issue together with the shared-memory pipe: point pairs, each
+        # FAR_OPS_PER_PAIR lane instructions, against 4 schedulers x 32 lanes per clock per SM (no
+        # measured figure exists for issue: derived from the SM count and the sampled clock).
         f = stats["cubature_far"]
         avg_s = f["ms"] / 1000.0 / f["count"]
         keys = f["flops"] / f["count"] / 4096.0  # algorithmic pairs per launch / pairs per key (4^3 x 4^3 rule)
@@ -251,8 +248,9 @@ def roofline(stats, clk, hbm, bf16, peak_kind, ntab):
         return {"kernel": "cubature_far_sph_kernel / cubature_far_kernel (window histograms)", "bound": "issue",
                 "achieved": iach, "peak": ipeak, "unit": "G point pairs/s", "frac": iach / ipeak,
                 "peak_kind": f"derived, not measured: 128 lane instructions/clk/SM x {nsm} SMs x {mhz:.0f} MHz "
-                             f"(sampled median) / {FAR_OPS_PER_PAIR} instructions per point pair of the direct "
-                             f"exact method; ncu measured issue active 75 % of peak on the 16x32x32 inner shell",
+                             f"(sampled median) / {FAR_OPS_PER_PAIR:.1f} lane instructions per point pair (ncu "
+                             f"instruction count of this kernel); ncu measured issue active 81 % of peak on the "
+                             f"16x32x32 inner shell",
                 "algorithmic_unit": "one Gauss-point pair (all xi tables at once)",
                 "traffic": FAR_TRAFFIC_PER_KEY * keys,
                 "traffic_note": "DRAM bytes per launch: ncu bytes per key on the 16x32x32 shell x this launch's keys",
