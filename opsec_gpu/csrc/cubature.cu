@@ -425,8 +425,8 @@ struct WinPlan {
     float* wrm;       // [ng^2]: w_r w_mu of node pair P
     float4* sph;      // [nf][ng(ng+1)/2]: sin^2(theta/2) hi, lo, phi-node weight (x2 off the diagonal), 0
     int logkeys;      // one-pass keys in the log section take the specialised loop
-    double* arcbox;   // [H][4]: rho min, rho max, z min, z max over the arc's node pairs
-    double* sphbox;   // [nf][2]: min and max of sin^2(theta/2) over the canonical phi-node pairs
+    float4* arcbox;   // [H]: rho min, rho max, z min, z max over the arc's node pairs (rounded outward)
+    float2* sphbox;   // [nf]: min and max of sin^2(theta/2) over the canonical phi-node pairs (outward)
 };
 
 // Tables of the spherical window kernel, from the cubature nodes (FP64 products,
@@ -485,7 +485,8 @@ __global__ void sph_box_kernel(CubatureArgs a, WinPlan w) {
                 b[2] = fmin(b[2], z);
                 b[3] = fmax(b[3], z);
             }
-            for (int k = 0; k < 4; k++) w.arcbox[4 * e + k] = b[k];
+            w.arcbox[e] = make_float4(__double2float_rd(b[0]), __double2float_ru(b[1]), __double2float_rd(b[2]),
+                                      __double2float_ru(b[3]));
         } else {
             const long long df = e - a.ks.H;
             double lo = INFINITY, hi = -INFINITY;
@@ -495,8 +496,7 @@ __global__ void sph_box_kernel(CubatureArgs a, WinPlan w) {
                 lo = fmin(lo, s2);
                 hi = fmax(hi, s2);
             }
-            w.sphbox[2 * df] = lo;
-            w.sphbox[2 * df + 1] = hi;
+            w.sphbox[df] = make_float2(__double2float_rd(lo), __double2float_ru(hi));
         }
     }
 }
@@ -534,16 +534,20 @@ __global__ void cell_sphere_kernel(const float4* pts, int np, long long ncell, f
     }
 }
 
-// table bin of a distance (the QSpline grid), FP64: the index the pair kernels compute, up to rounding
-__device__ __forceinline__ int bin_floor(const XiLayout& xl, double r) {
-    if (r < xl.r1) return (int)floor(r * xl.n1 / xl.r1);
-    if (r >= xl.r2) return xl.n() - 1;
-    return xl.n1 + (int)floor(log(r / xl.r1) * (xl.n2 - 1) / log(xl.r2 / xl.r1));
+// table bin of a distance (the QSpline grid) in FP32: the index the pair kernels compute to
+// ~1e-3 of a bin (the windows carry a bin of margin below and three above)
+// (per_oct: bins per octave of r in the log section, (n2 - 1) / log2(r2 / r1))
+__device__ __forceinline__ int bin_floor(const XiLayout& xl, float per_oct, float r) {
+    const float r1 = (float)xl.r1;
+    if (r < r1) return (int)floorf(r * ((float)xl.n1 / r1));
+    if (r >= (float)xl.r2) return xl.n() - 1;
+    return xl.n1 + (int)floorf(log2f(r / r1) * per_oct);
 }
 
 __global__ void key_window_kernel(CubatureArgs a, WinPlan w) {
     const bool periodic = (a.coordsys == 1 && a.L > 0);
     const int nx = a.xl.n();
+    const float per_oct = (float)((a.xl.n2 - 1) / log2(a.xl.r2 / a.xl.r1));
     for (long long key = blockIdx.x * (long long)blockDim.x + threadIdx.x; key < a.ks.nkeys;
          key += (long long)gridDim.x * blockDim.x) {
         if ((a.ks.coordsys == 2 && a.ks.mu_reflect && reflect_partner(a.ks, key) < key) || (a.skip && a.skip[key])) {
@@ -552,36 +556,39 @@ __global__ void key_window_kernel(CubatureArgs a, WinPlan w) {
         }
         int c1[3], c2[3];
         decode_key(a.ks, key, c1, c2);
+        // FP32 (FP64 issues at 1/64 of the FP32 rate here), every bound widened by 1e-5 of
+        // itself: far beyond the FP32 rounding of these few operations
         const float4 A = w.cen[cell_id(a.ks, c1)], B = w.cen[cell_id(a.ks, c2)];
-        double d[3] = {(double)B.x - A.x, (double)B.y - A.y, (double)B.z - A.z};
-        const double R = (double)A.w + B.w;
+        float d[3] = {B.x - A.x, B.y - A.y, B.z - A.z};
+        const float R = A.w + B.w;
         bool near = false;
         if (periodic) {
+            const float L = (float)a.L;
             for (int k = 0; k < 3; k++) {
-                d[k] -= a.L * floor(d[k] / a.L + 0.5);
-                if (fabs(d[k]) + R >= 0.5 * a.L) near = true;  // pair differences may wrap differently
+                d[k] -= L * floorf(d[k] / L + 0.5f);
+                if (fabsf(d[k]) + R >= 0.5f * L * (1.f - 1e-5f)) near = true;  // pair differences may wrap differently
             }
         }
-        const double dist = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
-        double rlo = fmax(dist - R, 0.0), rhi = dist + R;
+        const float dist = sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+        float rlo = fmaxf(dist - R, 0.f) * (1.f - 1e-5f), rhi = (dist + R) * (1.f + 1e-5f);
         if (w.arcbox) {
             // spherical grids: the bounding spheres of cells long in phi are loose; bound r^2
             // term by term from the arcs' (rho, z) boxes and the offset's sin^2 range, and keep
             // the tighter of the two bounds (both hold for every node pair of the key)
-            const double* ba = w.arcbox + 4 * (c1[0] * a.ks.N2 + c1[1]);
-            const double* bb = w.arcbox + 4 * (c2[0] * a.ks.N2 + c2[1]);
-            const double s2lo = w.sphbox[2 * c2[2]], s2hi = w.sphbox[2 * c2[2] + 1];
-            const double grho = fmax(0.0, fmax(bb[0] - ba[1], ba[0] - bb[1]));
-            const double gz = fmax(0.0, fmax(bb[2] - ba[3], ba[2] - bb[3]));
-            const double drho = fmax(bb[1] - ba[0], ba[1] - bb[0]);
-            const double dz = fmax(bb[3] - ba[2], ba[3] - bb[2]);
-            const double r2lo = grho * grho + gz * gz + 4.0 * ba[0] * bb[0] * s2lo;
-            const double r2hi = drho * drho + dz * dz + 4.0 * ba[1] * bb[1] * s2hi;
-            rlo = fmax(rlo, sqrt(r2lo) * (1.0 - 1e-9));
-            rhi = fmin(rhi, sqrt(r2hi) * (1.0 + 1e-9));
+            const float4 ba = w.arcbox[c1[0] * a.ks.N2 + c1[1]];
+            const float4 bb = w.arcbox[c2[0] * a.ks.N2 + c2[1]];
+            const float2 s2 = w.sphbox[c2[2]];
+            const float grho = fmaxf(0.f, fmaxf(bb.x - ba.y, ba.x - bb.y));
+            const float gz = fmaxf(0.f, fmaxf(bb.z - ba.w, ba.z - bb.w));
+            const float drho = fmaxf(bb.y - ba.x, ba.y - bb.x);
+            const float dz = fmaxf(bb.w - ba.z, ba.w - bb.z);
+            const float r2lo = grho * grho + gz * gz + 4.f * ba.x * bb.x * s2.x;
+            const float r2hi = drho * drho + dz * dz + 4.f * ba.y * bb.y * s2.y;
+            rlo = fmaxf(rlo, sqrtf(r2lo) * (1.f - 1e-5f));
+            rhi = fminf(rhi, sqrtf(r2hi) * (1.f + 1e-5f));
         }
-        const int blo = max(bin_floor(a.xl, rlo) - 1, 0);
-        const int bhi = min(bin_floor(a.xl, rhi) + 3, nx);
+        const int blo = max(bin_floor(a.xl, per_oct, rlo) - 1, 0);
+        const int bhi = min(bin_floor(a.xl, per_oct, rhi) + 3, nx);
         const int width = bhi - blo;
         const int bucket = (near || width > w.Wmax) ? nx : blo;
         w.win[key] = make_int2(bucket, width);
@@ -1328,8 +1335,8 @@ WinLayout win_layout(const KeySpace& ks, int nx, int ntab, int ng) {
     L.wrm = L.arc + (sph ? al(sizeof(float4) * (size_t)ks.H * ng * ng) : 0);
     L.sph = L.wrm + (sph ? al(sizeof(float) * (size_t)ng * ng) : 0);
     L.arcbox = L.sph + (sph ? al(sizeof(float4) * (size_t)ks.nf * (ng * (ng + 1) / 2)) : 0);
-    L.sphbox = L.arcbox + (sph ? al(sizeof(double) * 4 * (size_t)ks.H) : 0);
-    L.tiles = L.sphbox + (sph ? al(sizeof(double) * 2 * (size_t)ks.nf) : 0);
+    L.sphbox = L.arcbox + (sph ? al(sizeof(float4) * (size_t)ks.H) : 0);
+    L.tiles = L.sphbox + (sph ? al(sizeof(float2) * (size_t)ks.nf) : 0);
     L.total = L.tiles + al(sizeof(int4) * (size_t)((ks.nkeys + kPartTile - 1) / kPartTile));
     return L;
 }
@@ -1401,8 +1408,8 @@ bool run_window(const CubatureArgs& a, const Lookup& lk, cudaStream_t s, long lo
         w.arc = reinterpret_cast<float4*>(base + L.arc);
         w.wrm = reinterpret_cast<float*>(base + L.wrm);
         w.sph = reinterpret_cast<float4*>(base + L.sph);
-        w.arcbox = reinterpret_cast<double*>(base + L.arcbox);
-        w.sphbox = reinterpret_cast<double*>(base + L.sphbox);
+        w.arcbox = reinterpret_cast<float4*>(base + L.arcbox);
+        w.sphbox = reinterpret_cast<float2*>(base + L.sphbox);
     }
     OPSEC_CUDA(cudaMemsetAsync(w.count, 0, sizeof(int) * (nx + 2), s));
     OPSEC_CUDA(cudaMemsetAsync(scal, 0, 256, s));
