@@ -138,23 +138,50 @@ __global__ void xi_sum_kernel(XiTableArgs a) {
     }
 
     // the rest, by the three-term recurrence, in double-FP32 (FP64 instructions issue at 1/64 of
-    // the FP32 rate here): the angles' sines and cosines once per lane in FP64, then the
-    // recurrence, its sum and the anchor rotations as (hi, lo) float pairs
+    // the FP32 rate here).  The sines and cosines it starts from: one FP64 sincos per lane --
+    // lane 8 q + u, for r_q, of the warp's first angle (kmin + jc dk) r_q (u = 0), of 2^(u-1)
+    // dk r_q (u = 1..5), of 32 dk r_q (u = 6) and of 32 kAnchor dk r_q (u = 7) -- split into
+    // (hi, lo) pairs and shared by shuffles; each lane turns the first angle into its own,
+    // (kmin + (jc + lane) dk) r_q, by rotations through the powers of two in its lane number;
+    // then the recurrence, its sum and the anchor rotations as (hi, lo) float pairs
+    static_assert(kRPerWarp * 8 == 32, "one FP64 sincos per lane");
     if (jc <= nk) {
         df c2[kRPerWarp], cth[kRPerWarp], sth[kRPerWarp], cT[kRPerWarp], sT[kRPerWarp], sn[kRPerWarp], cs[kRPerWarp];
+        df sl, cl;  // this lane's sincos
+        {
+            const int q = lane >> 3, u = lane & 7;
+            const double rq = a.r[min(i0 + q, n - 1)];
+            const double ang = u == 0   ? (s.kmin + jc * dk) * rq
+                               : u <= 5 ? (double)(1 << (u - 1)) * dk * rq
+                               : u == 6 ? 32.0 * dk * rq
+                                        : (32.0 * kAnchor) * dk * rq;
+            double sa, ca;
+            sincos(ang, &sa, &ca);
+            sl = df_from(sa);
+            cl = df_from(ca);
+        }
+        auto shfl = [&](df v, int src) {
+            return df{__shfl_sync(0xffffffffu, v.h, src), __shfl_sync(0xffffffffu, v.l, src)};
+        };
 #pragma unroll
         for (int q = 0; q < kRPerWarp; q++) {
-            double a, b;
-            sincos(32.0 * dk * r[q], &a, &b);
-            sth[q] = df_from(a);
-            cth[q] = df_from(b);
-            c2[q] = df_from(2.0 * b);
-            sincos((32.0 * kAnchor) * dk * r[q], &a, &b);
-            sT[q] = df_from(a);
-            cT[q] = df_from(b);
-            sincos((s.kmin + (jc + lane) * dk) * r[q], &a, &b);
-            sn[q] = df_from(a);
-            cs[q] = df_from(b);
+            df sq = shfl(sl, 8 * q), cq = shfl(cl, 8 * q);
+#pragma unroll
+            for (int bit = 0; bit < 5; bit++) {
+                const df sb = shfl(sl, 8 * q + 1 + bit), cb = shfl(cl, 8 * q + 1 + bit);
+                if ((lane >> bit) & 1) {  // rotate by 2^bit dk r_q
+                    const df s1 = df_fma(df_mul(sq, cb), cq, sb);
+                    cq = df_fms(df_mul(cq, cb), sq, sb);
+                    sq = s1;
+                }
+            }
+            sn[q] = sq;
+            cs[q] = cq;
+            sth[q] = shfl(sl, 8 * q + 6);
+            cth[q] = shfl(cl, 8 * q + 6);
+            c2[q] = df{2.f * cth[q].h, 2.f * cth[q].l};
+            sT[q] = shfl(sl, 8 * q + 7);
+            cT[q] = shfl(cl, 8 * q + 7);
         }
         const df zero{0.f, 0.f};
         for (int j0 = jc + lane; j0 <= nk; j0 += 32 * kAnchor) {
