@@ -58,6 +58,13 @@ int opsec_gpu_batch_fisher(opsec_gpu* c, int nmocks, const opsec_mock* mocks, in
             ctx[k]->surr_on = false;
             build_tables(ctx[k]);
         }
+        // largest mocks first: a worker's buffers then reach their final size on its first mocks,
+        // and later mocks reuse them (a reallocation frees device memory, which waits for the
+        // whole device, every worker's work included)
+        std::vector<int> order(nmocks);
+        for (int i = 0; i < nmocks; i++) order[i] = i;
+        std::stable_sort(order.begin(), order.end(),
+                         [&](int x, int y) { return mocks[x].ncells > mocks[y].ncells; });
         std::atomic<int> next{0};
         std::atomic<int> err_code{OPSEC_OK};
         std::string err_msg;
@@ -70,7 +77,7 @@ int opsec_gpu_batch_fisher(opsec_gpu* c, int nmocks, const opsec_mock* mocks, in
                     int i;
                     while (err_code.load() == OPSEC_OK && (i = next.fetch_add(1)) < end) {
                         try {
-                            run_mock(ctx[k], mocks[i], (size_t)i, nb, F, phat, pcov);
+                            run_mock(ctx[k], mocks[order[i]], (size_t)order[i], nb, F, phat, pcov);
                         } catch (const Error& e) {
                             std::lock_guard<std::mutex> lk(err_mu);
                             if (err_code.load() == OPSEC_OK) {
