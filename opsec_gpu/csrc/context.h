@@ -93,6 +93,7 @@ struct opsec_gpu {
     int cub_exact = 1;
     int az_gemm64 = 0;
     int az_tc = 1;  // block projection GEMMs on the tensor cores (az_tc.cu); 0: cuBLAS SGEMM
+    int az_tiled = 1;  // FP32 band blocks by staged tiles (1) or one thread per output (0); same bits
     bool cub_reflect = true;
     int cub_window = 1;
     int win_key = 384, win_flush = 8, win_dot64 = 0, win_logkeys = 1, win_keyorder = 1;

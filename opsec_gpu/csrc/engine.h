@@ -172,7 +172,7 @@ void launch_signal_block(const KeySpace& ks, const CellKeyInfo& ci, const double
 void launch_azimuthal_blocks(const KeySpace& ks, const double* Qtab, const double* nbar_arc, int nm, int npar,
                              double* Sm, cudaStream_t st, long long* launches);
 void launch_azimuthal_blocks(const KeySpace& ks, const double* Qtab, const double* nbar_arc, int nm, int npar,
-                             float* Sm, cudaStream_t st, long long* launches);
+                             float* Sm, cudaStream_t st, long long* launches, bool tiled = true);
 // Block eigenvector columns (m, idx) gathered into Ucat[col][h]
 void launch_gather_block_vectors(int H, int ncol, const int* col_m, const int* col_idx, const double* U, double* Ucat,
                                  cudaStream_t st, long long* launches);

@@ -1,5 +1,7 @@
 // project_host.cpp -- C_p = B^T S_p B (comma-scalapack.cpp:228-265): azimuthal blocks or the fused
 // tensor-core projection.
+#include <type_traits>
+
 #include "context.h"
 
 struct AzPlan {
@@ -68,8 +70,12 @@ T* az_blocks(opsec_gpu* c, const AzPlan& a) {
         const int np = std::min(bpp, a.nb - p0);
         for (int p = p0; p < p0 + np; p++) {
             if (g_clock) g_clock->begin("azimuthal_transform", c->stream, 2.0 * nblk * (double)H * H * c->ks.nf);
-            launch_azimuthal_blocks(c->ks, c->Q.p + (size_t)(1 + p) * c->ks.nkeys, a.nbar_arc, a.nm, a.npar,
-                                    Sb + (size_t)(p - p0) * nS, c->stream, &c->launches);
+            if constexpr (std::is_same<T, float>::value)
+                launch_azimuthal_blocks(c->ks, c->Q.p + (size_t)(1 + p) * c->ks.nkeys, a.nbar_arc, a.nm, a.npar,
+                                        Sb + (size_t)(p - p0) * nS, c->stream, &c->launches, c->az_tiled != 0);
+            else
+                launch_azimuthal_blocks(c->ks, c->Q.p + (size_t)(1 + p) * c->ks.nkeys, a.nbar_arc, a.nm, a.npar,
+                                        Sb + (size_t)(p - p0) * nS, c->stream, &c->launches);
             if (g_clock) g_clock->end(c->stream);
         }
         if (g_clock) g_clock->begin("azimuthal_gemm", c->stream, a.flops * np);

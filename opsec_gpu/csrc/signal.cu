@@ -371,13 +371,132 @@ __global__ void azimuthal_blocks_f32_kernel(KeySpace ks, const double* Q, const 
     }
 }
 
+// The same FP32 blocks by tiles of 16 (x) x 32 (y) outputs with y >= x, written at [x][y] and,
+// mirrored through shared memory, at [y][x] (the blocks are symmetric).  In such a tile every
+// key row the block needs -- (h_x, h_y) and (h_x, P h_y) -- has its smaller arc first (the arcs
+// of the x half grow with x; P h_y lies in the upper mu half of h_y's shell), so for each x the
+// rows of consecutive y are runs of consecutive keys: the tile's rows are staged in shared memory
+// by coalesced loads (in the per-thread kernel above, one thread in two read a row of its own,
+// ~H keys from its neighbour's).
+constexpr int kTX = 16, kTY = 32;
+
+template <int NFM>
+__global__ void __launch_bounds__(256) azimuthal_blocks_tiled_kernel(KeySpace ks, const double* Q,
+                                                                     const double* nbar_arc, int nm, int npar,
+                                                                     float* Sm) {
+    // tile (blockIdx.x, blockIdx.y); tiles entirely below the diagonal have nothing to do
+    const int x0 = blockIdx.x * kTX, y0 = blockIdx.y * kTY;
+    if (y0 + kTY - 1 < x0) return;
+    extern __shared__ __align__(16) float tsm[];
+    float* cwf = tsm;                     // [nm][NFM]
+    float* q1s = cwf + nm * NFM;          // [kTX][kTY][NFM]
+    float* q2s = q1s + kTX * kTY * NFM;   // [kTX][kTY][NFM]
+    float* st = q2s + kTX * kTY * NFM;    // [2][kTY][kTX + 1]: one order's mirrored outputs
+    const int H = ks.H, Nphi = ks.N3, nf = ks.nf, Nmu = ks.N2;
+    const int Hb = H / npar, half = Nmu / npar;
+    const long long HH = (long long)Hb * Hb;
+    for (int t = threadIdx.x; t < nm * NFM; t += blockDim.x) {
+        const int m = t / NFM, df = t % NFM;
+        const int md = (int)(((long long)m * df) % Nphi);
+        const double w = (df == 0 || 2 * df == Nphi) ? 1.0 : 2.0;
+        cwf[t] = df < nf ? (float)(w * cospi(2.0 * md / Nphi)) : 0.f;
+    }
+    auto arc = [&](int v) { return (v / half) * Nmu + v % half; };
+    auto refl = [&](int h) { return (h / Nmu) * Nmu + (Nmu - 1 - h % Nmu); };
+    // stage the tile's key rows (pairs outside the block or below the diagonal: zeros)
+    for (int e = threadIdx.x; e < kTX * kTY * NFM; e += blockDim.x) {
+        const int xi = e / (kTY * NFM), r = e % (kTY * NFM), yi = r / NFM, df = r % NFM;
+        const int x = x0 + xi, y = y0 + yi;
+        float v1 = 0.f, v2 = 0.f;
+        if (x < Hb && y < Hb && y >= x && df < nf) {
+            const int ha = arc(x), hb = arc(y);
+            v1 = (float)Q[tri_index(min(ha, hb), max(ha, hb), H) * nf + df];
+            if (npar == 2) {
+                const int pb = refl(hb);
+                v2 = (float)Q[tri_index(min(ha, pb), max(ha, pb), H) * nf + df];
+            }
+        }
+        q1s[e] = v1;
+        q2s[e] = v2;
+    }
+    __syncthreads();
+    // two pairs per thread, y fastest: p = threadIdx.x + 256 k -> (xi, yi) = (p / kTY, p % kTY)
+    float q1[2][NFM], q2[2][NFM], dd[2];
+    int xs[2], ys[2];
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+        const int p = threadIdx.x + 256 * k, xi = p / kTY, yi = p % kTY;
+        xs[k] = x0 + xi;
+        ys[k] = y0 + yi;
+#pragma unroll
+        for (int df = 0; df < NFM; df++) {
+            q1[k][df] = q1s[p * NFM + df];
+            q2[k][df] = q2s[p * NFM + df];
+        }
+        const bool ok = xs[k] < Hb && ys[k] < Hb && ys[k] >= xs[k];
+        dd[k] = ok ? sqrtf((float)nbar_arc[arc(xs[k])]) * sqrtf((float)nbar_arc[arc(ys[k])]) : 0.f;
+    }
+    for (int m = 0; m < nm; m++) {
+        const float* c = cwf + m * NFM;
+        float o[2][2];
+#pragma unroll
+        for (int k = 0; k < 2; k++) {
+            float a1 = 0.f, a2 = 0.f;
+#pragma unroll
+            for (int df = 0; df < NFM; df++) {
+                a1 = fmaf(q1[k][df], c[df], a1);
+                a2 = fmaf(q2[k][df], c[df], a2);
+            }
+            o[k][0] = npar == 1 ? dd[k] * a1 : dd[k] * (a1 + a2);
+            o[k][1] = dd[k] * (a1 - a2);
+            const bool ok = xs[k] < Hb && ys[k] < Hb && ys[k] >= xs[k];
+            if (ok) {
+                if (npar == 1) {
+                    Sm[(size_t)m * HH + (size_t)xs[k] * Hb + ys[k]] = o[k][0];
+                } else {
+                    Sm[(size_t)(2 * m) * HH + (size_t)xs[k] * Hb + ys[k]] = o[k][0];
+                    Sm[(size_t)(2 * m + 1) * HH + (size_t)xs[k] * Hb + ys[k]] = o[k][1];
+                }
+            }
+            const int p = threadIdx.x + 256 * k, xi = p / kTY, yi = p % kTY;
+            st[yi * (kTX + 1) + xi] = o[k][0];
+            st[kTY * (kTX + 1) + yi * (kTX + 1) + xi] = o[k][1];
+        }
+        __syncthreads();
+        // mirror: [y][x] for y > x, x fastest
+#pragma unroll
+        for (int k = 0; k < 2; k++) {
+            const int p = threadIdx.x + 256 * k, yi = p / kTX, xi = p % kTX;
+            const int x = x0 + xi, y = y0 + yi;
+            if (x < Hb && y < Hb && y > x) {
+                if (npar == 1) {
+                    Sm[(size_t)m * HH + (size_t)y * Hb + x] = st[yi * (kTX + 1) + xi];
+                } else {
+                    Sm[(size_t)(2 * m) * HH + (size_t)y * Hb + x] = st[yi * (kTX + 1) + xi];
+                    Sm[(size_t)(2 * m + 1) * HH + (size_t)y * Hb + x] = st[kTY * (kTX + 1) + yi * (kTX + 1) + xi];
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
 template <int NFM>
 void launch_azimuthal_f32(const KeySpace& ks, const double* Q, const double* nbar_arc, int nm, int npar, float* Sm,
-                          cudaStream_t st) {
+                          cudaStream_t st, bool tiled) {
+    const int Hb = ks.H / npar;
+    if (tiled) {
+        const size_t smem = sizeof(float) * ((size_t)nm * NFM + 2 * (size_t)kTX * kTY * NFM + 2 * kTY * (kTX + 1));
+        OPSEC_CUDA(cudaFuncSetAttribute(azimuthal_blocks_tiled_kernel<NFM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)smem));
+        const dim3 grid((unsigned)((Hb + kTX - 1) / kTX), (unsigned)((Hb + kTY - 1) / kTY));
+        azimuthal_blocks_tiled_kernel<NFM><<<grid, 256, smem, st>>>(ks, Q, nbar_arc, nm, npar, Sm);
+        return;
+    }
     const size_t smem = sizeof(float) * (size_t)nm * NFM;
     OPSEC_CUDA(cudaFuncSetAttribute(azimuthal_blocks_f32_kernel<NFM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     max_dynamic_smem((const void*)azimuthal_blocks_f32_kernel<NFM>)));
-    const long long HH = (long long)(ks.H / npar) * (ks.H / npar);
+    const long long HH = (long long)Hb * Hb;
     long long gx = (HH + 255) / 256;
     if (gx > 65535) gx = 65535;
     azimuthal_blocks_f32_kernel<NFM><<<(unsigned)gx, 256, smem, st>>>(ks, Q, nbar_arc, nm, npar, Sm);
@@ -385,17 +504,17 @@ void launch_azimuthal_f32(const KeySpace& ks, const double* Q, const double* nba
 
 template <typename T>
 void launch_azimuthal_blocks_t(const KeySpace& ks, const double* Q, const double* nbar_arc, int nm, int npar, T* Sm,
-                               cudaStream_t st, long long* l) {
+                               cudaStream_t st, long long* l, bool tiled = false) {
     if (npar != 1 && !(npar == 2 && ks.N2 % 2 == 0)) fail(OPSEC_ERR_ARG, "parity split needs an even mu grid");
     if (!ks.fold) fail(OPSEC_ERR_CONFIG, "azimuthal blocks need a full-sky grid");
     if constexpr (std::is_same<T, float>::value) {
         if (ks.nf <= 33) {
             if (ks.nf <= 9)
-                launch_azimuthal_f32<9>(ks, Q, nbar_arc, nm, npar, Sm, st);
+                launch_azimuthal_f32<9>(ks, Q, nbar_arc, nm, npar, Sm, st, tiled);
             else if (ks.nf <= 17)
-                launch_azimuthal_f32<17>(ks, Q, nbar_arc, nm, npar, Sm, st);
+                launch_azimuthal_f32<17>(ks, Q, nbar_arc, nm, npar, Sm, st, tiled);
             else
-                launch_azimuthal_f32<33>(ks, Q, nbar_arc, nm, npar, Sm, st);
+                launch_azimuthal_f32<33>(ks, Q, nbar_arc, nm, npar, Sm, st, tiled);
             OPSEC_CUDA(cudaGetLastError());
             ++*l;
             return;
@@ -419,8 +538,8 @@ void launch_azimuthal_blocks(const KeySpace& ks, const double* Q, const double* 
 }
 
 void launch_azimuthal_blocks(const KeySpace& ks, const double* Q, const double* nbar_arc, int nm, int npar, float* Sm,
-                             cudaStream_t st, long long* l) {
-    launch_azimuthal_blocks_t(ks, Q, nbar_arc, nm, npar, Sm, st, l);
+                             cudaStream_t st, long long* l, bool tiled) {
+    launch_azimuthal_blocks_t(ks, Q, nbar_arc, nm, npar, Sm, st, l, tiled);
 }
 
 template <typename T>

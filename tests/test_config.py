@@ -55,6 +55,7 @@ BAD = [
     ("projection.arc_tables = 2", "projection.arc_tables"),
     ("cubature.log_keys = yes", "cubature.log_keys"),
     ("cubature.order = random", "cubature.order"),
+    ("azimuthal.transform = cols", "azimuthal.transform"),
 ]
 
 
