@@ -270,7 +270,9 @@ void project_all(opsec_gpu* c, int ncells, int M, bool own_modes, bool packed) {
     a.chunk = c->proj_chunk;
     a.wait_cycles = c->proj_wait;
     const int n3 = c->ks.N3;
-    if (c->proj_arcs && c->cells_arc_order && (n3 == 16 || n3 == 32 || n3 == 64)) a.arc_run = n3;
+    if (c->proj_arcs && c->cells_arc_order && (n3 == 16 || n3 == 32 || n3 == 64) &&
+        (long long)(128 / n3) * c->ks.H * c->ks.nf < (1LL << 23))
+        a.arc_run = n3;
     bool tc = (c->projection != "simt") && project_tc_supported(a);
     if (c->projection == "tc" && !tc) fail(OPSEC_ERR_CONFIG, "projection=tc requested but the shape is not supported");
     size_t wb = tc ? project_tc_work_bytes(a) : sizeof(float) * (size_t)M * ncells;

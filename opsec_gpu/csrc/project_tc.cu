@@ -115,6 +115,26 @@ __device__ __forceinline__ void issue_slice(uint32_t tmem, uint64_t ah, uint64_t
     }
 }
 
+// Step 1 issues each K-slice as two N = 128 halves into two accumulators, so that one half's
+// drain (into its running sum) overlaps the tensor core's work on the other half.
+constexpr uint32_t kIdesc128 =
+    (1u << 4) | (0u << 7) | (0u << 10) | ((uint32_t)(128 >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+
+__device__ __forceinline__ void issue_slice_n128(uint32_t tmem, uint64_t ah, uint64_t al, uint64_t bh, uint64_t bl,
+                                                 bool first_in_chunk) {
+#pragma unroll
+    for (int kk = 0; kk < BK / 16; kk++) {
+        const uint64_t adv = (uint64_t)(kk * 32) >> 4;
+        umma_f16(tmem, ah + adv, bl + adv, kIdesc128, (!first_in_chunk || kk > 0) ? 1u : 0u);
+        umma_f16(tmem, al + adv, bh + adv, kIdesc128, 1u);
+    }
+#pragma unroll
+    for (int kk = 0; kk < BK / 16; kk++) {
+        const uint64_t adv = (uint64_t)(kk * 32) >> 4;
+        umma_f16(tmem, ah + adv, bh + adv, kIdesc128, 1u);
+    }
+}
+
 __device__ __forceinline__ void split_half(float x, __half& h, __half& l) {
     h = __float2half_rn(x);
     l = __float2half_rn(x - __half2float(h));
@@ -148,18 +168,11 @@ struct Step1Params {
 // column arcs, and every element is Q(h_a, h_b, |f_a - f_b|): one run of nf consecutive words
 // of the square table per arc pair.  Each producer warp loads those runs (at most kArcTab words,
 // N3 >= 16) once per slice into its own buffer and expands its rows of the tile from there.
+// Entry e = ((ra (BK/N3) + ca) nf + df) of slice k's table is the word of row arc a0/N3 + ra,
+// column arc k BK/N3 + ca and offset df (zero past the last arc: padding rows and columns).
 constexpr int kArcTab = 288;  // (BM/16) (BK/16) 9 words at N3 = 16, the smallest arc run allowed
 
 __device__ __forceinline__ int arc_table_size(const KeySpace& ks, int n3) { return (BM / n3) * (BK / n3) * ks.nf; }
-
-__device__ __forceinline__ uint32_t arc_table_word(const KeySpace& ks, const uint32_t* Qhl, int n3, int a0, int k,
-                                                   int e) {
-    const int nca = BK / n3;
-    const int df = e % ks.nf, pr = e / ks.nf, ca = pr % nca, ra = pr / nca;
-    const int ha = a0 / n3 + ra, hb = (k * BK) / n3 + ca;
-    if (ha >= ks.H || hb >= ks.H) return 0u;  // padding rows and columns
-    return __ldg(Qhl + ((size_t)ha * ks.H + hb) * ks.nf + df);
-}
 
 __device__ __forceinline__ int pair_key(const KeySpace& ks, int4 a, int4 b) {
     if (ks.coordsys == 1) {
@@ -172,11 +185,14 @@ __device__ __forceinline__ int pair_key(const KeySpace& ks, int4 a, int4 b) {
 }
 
 // warps: 0 TMA, 1 MMA, 2-9 gather producers, 10-11 idle, 12-15 drain + epilogue (lane quarters 0-3)
+// N3A: 0 for the key gather, else the phi cells per arc of the arc-run tables (p.arcs), a
+// compile-time constant so that the producers' row and column splits are shifts
+template <int N3A>
 __global__ void __launch_bounds__(512, 1)
     step1_kernel(const __grid_constant__ CUtensorMap mBh, const __grid_constant__ CUtensorMap mBl, Step1Params p) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    __shared__ __align__(8) unsigned long long bar_full[STAGES], bar_empty[STAGES], bar_chunk, bar_drained;
+    __shared__ __align__(8) unsigned long long bar_full[STAGES], bar_empty[STAGES], bar_chunk[2], bar_drained[2];
     __shared__ uint32_t tmem_slot;
     __shared__ volatile int abort_flag;
     __shared__ int4 rowkey[BM];
@@ -194,8 +210,10 @@ __global__ void __launch_bounds__(512, 1)
             mbar_init(smem_u32(&bar_full[s]), 1 + 8);
             mbar_init(smem_u32(&bar_empty[s]), 1);
         }
-        mbar_init(smem_u32(&bar_chunk), 1);
-        mbar_init(smem_u32(&bar_drained), 4);
+        for (int h = 0; h < 2; h++) {
+            mbar_init(smem_u32(&bar_chunk[h]), 1);
+            mbar_init(smem_u32(&bar_drained[h]), 4);
+        }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (threadIdx.x < BM) rowkey[threadIdx.x] = p.ckey[a0 + threadIdx.x];
@@ -223,45 +241,100 @@ __global__ void __launch_bounds__(512, 1)
             }
         }
     } else if (warp == 1) {
-        // MMA issuer
-        for (int k = 0; k < nk; k++) {
+        // MMA issuer: accumulator halves D0 = columns [0, 128) of TMEM for output columns
+        // j0 .. j0 + 127, D1 = [128, 256) for j0 + 128 ..; running sums R0, R1 at [256, 512)
+        bool ok = true;
+        for (int k = 0; k < nk && ok; k++) {
             const int s = k % STAGES, n = k / STAGES;
-            const bool first = (k % chunk) == 0;
-            if (first && k > 0) {  // the previous chunk's accumulator must be drained first
-                if (!mbar_wait(smem_u32(&bar_drained), ((k / chunk) - 1) & 1, &abort_flag, p.err, p.wait_cycles)) break;
-            }
+            const bool first = (k % chunk) == 0, last = (k % chunk) == chunk - 1 || k == nk - 1;
             if (!mbar_wait(smem_u32(&bar_full[s]), n & 1, &abort_flag, p.err, p.wait_cycles)) break;
-            tc_fence_after();
-            if (lane == 0) {
-                issue_slice(tmem, sdesc(smem_u32(A_hi(s))), sdesc(smem_u32(A_lo(s))), sdesc(smem_u32(B_hi(s))),
-                            sdesc(smem_u32(B_lo(s))), first);
-                umma_commit(smem_u32(&bar_empty[s]));
-                if ((k % chunk) == chunk - 1 || k == nk - 1) umma_commit(smem_u32(&bar_chunk));
+            for (int h = 0; h < 2; h++) {
+                // this half's previous chunk must be drained before it restarts
+                if (first && k > 0 &&
+                    !mbar_wait(smem_u32(&bar_drained[h]), ((k / chunk) - 1) & 1, &abort_flag, p.err, p.wait_cycles)) {
+                    ok = false;
+                    break;
+                }
+                tc_fence_after();
+                if (lane == 0) {
+                    const uint32_t boff = (uint32_t)h * (128 * 128);  // rows 128 h of the B tiles (8-row atoms of 1 KB)
+                    issue_slice_n128(tmem + (uint32_t)(128 * h), sdesc(smem_u32(A_hi(s))), sdesc(smem_u32(A_lo(s))),
+                                     sdesc(smem_u32(B_hi(s)) + boff), sdesc(smem_u32(B_lo(s)) + boff), first);
+                    if (h == 1) umma_commit(smem_u32(&bar_empty[s]));
+                    if (last) umma_commit(smem_u32(&bar_chunk[h]));
+                }
+                __syncwarp();
             }
-            __syncwarp();
         }
     } else if (warp >= 12) {
-        // drain warps + epilogue: T^T[j][a] in natural units
+        // drain warps + epilogue: T^T[j][a] in natural units; per chunk, half 0 then half 1,
+        // each drained while the tensor core works on the other
         const int q = warp & 3;
         const int a = a0 + 32 * q + lane;
-        drain_loop(tmem, q, lane, nchunks, ChunkBars{smem_u32(&bar_chunk), smem_u32(&bar_drained), p.wait_cycles}, &abort_flag,
-                   p.err, [&](int cc, const float* v) {
+        const uint32_t lane_base = (uint32_t)(32 * q) << 16;
+        bool ok = true;
+        for (int c = 0; c < nchunks && ok; c++) {
+            const bool last = (c == nchunks - 1);
+            for (int h = 0; h < 2; h++) {
+                if (!mbar_wait(smem_u32(&bar_chunk[h]), c & 1, &abort_flag, p.err, p.wait_cycles)) {
+                    ok = false;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t dcol = lane_base + (uint32_t)(128 * h), rcol = lane_base + 256u + (uint32_t)(128 * h);
+                for (int cc = 0; cc < 4; cc++) {
+                    float v[32];
+                    tmem_ld32(tmem + dcol + (uint32_t)(32 * cc), v);
+                    if (c > 0) {
+                        float r[32];
+                        tmem_ld32(tmem + rcol + (uint32_t)(32 * cc), r);
 #pragma unroll
-                       for (int t = 0; t < 32; t++) p.Tf[(size_t)(j0 + 32 * cc + t) * p.Npad + a] = v[t] * p.out_scale;
-                   });
-    } else if (warp < 10 && p.arcs > 0) {
-        // eight producers expanding arc-run tables (see arc_table_word): each warp loads slice
-        // k+1's table into registers while it expands slice k from its own shared buffer.
-        const int pw = warp - 2, n3 = p.arcs;
+                        for (int t = 0; t < 32; t++) v[t] += r[t];
+                    }
+                    if (last) {
+#pragma unroll
+                        for (int t = 0; t < 32; t++)
+                            p.Tf[(size_t)(j0 + 128 * h + 32 * cc + t) * p.Npad + a] = v[t] * p.out_scale;
+                    } else {
+                        tmem_st32(tmem + rcol + (uint32_t)(32 * cc), v);
+                    }
+                }
+                if (!last) tmem_wait_st();
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(smem_u32(&bar_drained[h]));
+            }
+        }
+    } else if (N3A > 0 && warp < 10) {
+        // eight producers expanding arc-run tables: each warp loads slice k+1's table into
+        // registers while it expands slice k from its own shared buffer.
+        constexpr int n3 = N3A > 0 ? N3A : 1;
+        const int pw = warp - 2;
         uint32_t* tab = reinterpret_cast<uint32_t*>(smem + STAGES * STAGE_BYTES) + pw * 2 * kArcTab;  // [2][kArcTab]
         const int T = arc_table_size(p.ks, n3);
         constexpr int kPer = kArcTab / 32;
+        constexpr int nca = BK / n3;
+        // the table entries' index split, once per lane: entry e of every slice's table is word
+        // (ha0 + ra) H nf + (kb + ca) nf + df of the key table, kb = k BK / n3; packed as
+        // rel = (ra H + ca) nf + df, ca and whether row arc ha0 + ra exists (the host keeps
+        // (BM / n3) H nf below 2^23)
+        const int H = p.ks.H, nf = p.ks.nf, ha0 = a0 / n3;
+        int packed[kPer];
+#pragma unroll
+        for (int q = 0; q < kPer; q++) {
+            const int e = lane + 32 * q;
+            const int df = e % nf, pr = e / nf, ca = pr % nca, ra = pr / nca;
+            const int rel = (ra * H + ca) * nf + df;
+            packed[q] = e < T && ha0 + ra < H ? (rel << 8) | (ca << 1) | 1 : 0;
+        }
         uint32_t nxt[kPer];
         auto load = [&](int k) {
+            const int kb = (k * BK) / n3;
+            const uint32_t* base = p.Qhl + ((size_t)ha0 * H + kb) * nf;
 #pragma unroll
             for (int q = 0; q < kPer; q++) {
-                const int e = lane + 32 * q;
-                nxt[q] = e < T ? arc_table_word(p.ks, p.Qhl, n3, a0, k, e) : 0u;
+                const int pk = packed[q];
+                nxt[q] = (pk & 1) && kb + ((pk >> 1) & 127) < H ? __ldg(base + (pk >> 8)) : 0u;
             }
         };
         auto store = [&](int buf) {
@@ -272,7 +345,6 @@ __global__ void __launch_bounds__(512, 1)
             load(0);
             store(0);
         }
-        const int nca = BK / n3;
         const int c0 = 2 * lane, c1 = c0 + 1;
         const int ca0 = c0 / n3, fb0 = c0 % n3, ca1 = c1 / n3, fb1 = c1 % n3;
         for (int k = 0; k < nk; k++) {
@@ -303,7 +375,7 @@ __global__ void __launch_bounds__(512, 1)
             if (lane == 0) mbar_arrive(smem_u32(&bar_full[s]));
             if (k + 1 < nk) store((k + 1) & 1);
         }
-    } else if (warp < 10) {
+    } else if (N3A == 0 && warp < 10) {
         // eight gather producers: warp pw fills rows pw, pw+8, ...; lane covers columns 2 lane, 2 lane + 1.
         // Software-pipelined: the 32 gathers of K-slice k+1 are in flight while the warp waits for
         // its stage to drain and while the tensor core works on slice k.
@@ -639,7 +711,10 @@ void launch_project_tc(const ProjectArgs& a, cudaStream_t s, long long* launches
     const CUtensorMap mTh256 = make_map(Th, L.Mpad, L.Npad, BN), mTl256 = make_map(Tl, L.Mpad, L.Npad, BN);
 
     const size_t smem = (size_t)STAGES * STAGE_BYTES + 1024 + sizeof(uint32_t) * 8 * 2 * kArcTab;
-    OPSEC_CUDA(cudaFuncSetAttribute(step1_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    OPSEC_CUDA(cudaFuncSetAttribute(step1_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    OPSEC_CUDA(cudaFuncSetAttribute(step1_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    OPSEC_CUDA(cudaFuncSetAttribute(step1_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    OPSEC_CUDA(cudaFuncSetAttribute(step1_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     OPSEC_CUDA(cudaFuncSetAttribute(step2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
 
     const int n_at = L.Npad / BM, n_jt = L.Mpad / BN;
@@ -663,7 +738,15 @@ void launch_project_tc(const ProjectArgs& a, cudaStream_t s, long long* launches
         p1.wait_cycles = a.wait_cycles;
         p1.arcs = a.arc_run;
         if (g_clock) g_clock->begin("project_step1", s, 2.0 * N * (double)N * M);
-        step1_kernel<<<n_at * n_jt, 512, smem, s>>>(mBh256, mBl256, p1);
+        const unsigned g1 = (unsigned)(n_at * n_jt);
+        if (p1.arcs == 16)
+            step1_kernel<16><<<g1, 512, smem, s>>>(mBh256, mBl256, p1);
+        else if (p1.arcs == 32)
+            step1_kernel<32><<<g1, 512, smem, s>>>(mBh256, mBl256, p1);
+        else if (p1.arcs == 64)
+            step1_kernel<64><<<g1, 512, smem, s>>>(mBh256, mBl256, p1);
+        else
+            step1_kernel<0><<<g1, 512, smem, s>>>(mBh256, mBl256, p1);
         OPSEC_CUDA(cudaGetLastError());
         if (g_clock) g_clock->end(s);
         absmax_f32_kernel<<<dim3(2048, 1), 256, 0, s>>>(1, nT, Tf, maxT + p);
