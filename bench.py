@@ -627,7 +627,8 @@ def main():
     roof_tc = None
     if not args.no_tc_roofline:
         e2 = api.Engine(api.make_config(sv, bands=bands[:1], nmodes=w["nmodes"], layout=w["layout"],
-                                        gauss=w["gauss"], extra=["profile = 1", "projection = tc"]))
+                                        gauss=w["gauss"], extra=["profile = 1", "projection = tc"] +
+                                        [kv.replace("=", " = ", 1) for kv in args.set]))
         e2.set_pk(k, P)
         e2.fisher_build(cells, counts, w["nmodes"])
         b2 = e2.kernel_stats("project_step1")
