@@ -254,6 +254,19 @@ int opsec_gpu_mock_counts(opsec_gpu* ctx, int ncells, const opsec_cell* cells, i
  * wait gave up after limit_cycles; the kernel then returns normally (no copy is
  * in flight), so the context stays usable.  Cycles in [1, 4e9]. */
 int opsec_gpu_fail_alloc(opsec_gpu* ctx, long long after);
+
+/* The block product of the iterative eigensolver (klt.solver = chfsi): the product
+ * of the signal matrix with a block of vectors that replaces the reference's one
+ * matrix-vector product per ARPACK step (the OP * x of the reverse-communication
+ * loop, ParpackSolver.cpp:111-123), on the engine's tcgen05 kernel:
+ *   C = alpha S X + beta C + gamma D
+ * S: N x N symmetric (FP64, both triangles); X, C, D: N x ncols FP32, column-major
+ * (leading dimension N); host buffers.  S and X are split into FP16 hi + lo after
+ * a power-of-two scaling (~22 significant bits); the result is accurate to a few
+ * 1e-7 of sum_k |S_ik X_kj|.  D may be null when gamma = 0; C is not read when
+ * beta = 0.  The kernel's output tiles follow the configuration's klt.tile. */
+int opsec_gpu_block_product(opsec_gpu* ctx, int N, int ncols, const double* S, const float* X, float alpha,
+                            float beta, float* C, float gamma, const float* D);
 int opsec_gpu_wait_probe(opsec_gpu* ctx, long long limit_cycles, int arrive, long long delay_cycles, int* timed_out);
 
 /* Largest band count opsec_gpu_fisher_noalloc accepts. */

@@ -77,6 +77,7 @@ def load():
     L.opsec_gpu_ang2pix.argtypes = [vp, C.c_longlong, C.c_int, C.c_int, dp, dp, C.POINTER(C.c_longlong)]
     L.opsec_gpu_fail_alloc.argtypes = [vp, C.c_longlong]
     L.opsec_gpu_wait_probe.argtypes = [vp, C.c_longlong, C.c_int, C.c_longlong, ip]
+    L.opsec_gpu_block_product.argtypes = [vp, C.c_int, C.c_int, dp, fp, C.c_float, C.c_float, fp, C.c_float, fp]
     _lib = L
     return L
 
@@ -392,6 +393,19 @@ class Engine:
         self._check(self._L.opsec_gpu_wait_probe(self._h, C.c_longlong(limit_cycles), int(bool(arrive)),
                                                  C.c_longlong(delay_cycles), C.byref(out)))
         return bool(out.value)
+
+    def block_product(self, S, X, alpha=1.0, beta=0.0, Cin=None, gamma=0.0, D=None):
+        """alpha S X + beta Cin + gamma D on the tensor-core block-product kernel of the
+        iterative eigensolver: S (N x N, symmetric) FP64, X / Cin / D (N x ncols) FP32."""
+        S = np.ascontiguousarray(S, dtype=np.float64)
+        N = S.shape[0]
+        Xf = np.asfortranarray(X, dtype=np.float32)
+        ncols = Xf.shape[1]
+        out = np.asfortranarray(Cin if Cin is not None else np.zeros((N, ncols)), dtype=np.float32).copy(order="F")
+        Df = None if D is None else np.asfortranarray(D, dtype=np.float32)
+        self._check(self._L.opsec_gpu_block_product(self._h, N, ncols, _d(S), _fp(Xf), C.c_float(alpha),
+                                                    C.c_float(beta), _fp(out), C.c_float(gamma), _fp(Df)))
+        return out
 
     def launch_count(self):
         return int(self._L.opsec_gpu_launch_count(self._h))

@@ -12,8 +12,12 @@
 //   filter      Y = p_d(S) X with p_d the degree-d Chebyshev polynomial of [lo, cut],
 //               scaled to 1 at hi, by the scaled three-term recurrence (Zhou, Saad,
 //               Tiago, Chelikowsky, J. Comput. Phys. 219 (2006) 172-184): d GEMMs
-//               N x N x B in FP32 arithmetic on the tensor cores (cuBLAS BF16x9: each FP32
-//               operand as three BF16 terms, FP32 accumulation).  d is the largest degree
+//               N x N x B on the tensor cores, by the engine's tcgen05 kernel (gemm_tc.cu:
+//               S split once into FP16 hi + lo, the block at every step, three FP16
+//               products, the recurrence's axpy fused into the epilogue; `klt.gemm = tc`)
+//               or cuBLAS (BF16x9: each FP32 operand as three BF16 terms; or FP32 SIMT).
+//               Every product with S (filter, Rayleigh-Ritz, correction solve) takes
+//               the same route.  d is the largest degree
 //               (up to klt.degree) whose gain p(hi) / p(theta_M) stays below 1e4, so
 //               that the wanted columns keep FP32 precision beside the top ones
 //   basis       Householder QR of Y (FP32)
@@ -21,7 +25,8 @@
 //   Ritz        cut = the smallest Ritz value; stop when the top M residuals are below
 //               tol theta_i or the FP32 floor, or stop improving
 //   refinement  on the top Mr = M + 8 vectors, up to klt.refine rounds of: Rayleigh-Ritz
-//               in FP64 (DGEMMs with the FP64 S), the FP64 residuals r_j = S u_j -
+//               in FP64 (products with the FP64 S in double-FP32 on the FP32 pipes,
+//               gemm_df.cu, or cuBLAS DGEMM: `klt.fp64`), the FP64 residuals r_j = S u_j -
 //               theta_j u_j, and the correction equation of Jacobi-Davidson,
 //               (I - U U^T)(theta_j - S)(I - U U^T) d_j = r_j, positive definite on the
 //               complement of U, solved by CG with FP32 GEMMs (klt.cg steps), x_j = u_j +
@@ -40,6 +45,8 @@
 
 #include "chfsi_host.h"
 #include "engine.h"
+#include "gemm_df.h"
+#include "gemm_tc.h"
 
 namespace opsec {
 namespace {
@@ -299,11 +306,36 @@ void chfsi_eigensolve(const ChfsiArgs& g, cublasHandle_t blas, cusolverDnHandle_
         fail(OPSEC_ERR_NUMERIC, "iterative eigensolver: the signal matrix has no spread of eigenvalues (zero or not finite)");
     lz.release();
 
-    // ---- FP32 copy of S and the block buffers
+    // ---- S for the block products (an FP32 copy for cuBLAS, or the FP16 hi/lo split of the
+    // FP64 S for the tensor-core kernel) and the block buffers
     DevBuf<float> S32, Xb, Yb, Zb, Hb, Vf;
-    S32.alloc(NN);
-    narrow_kernel<<<blocks(NN), 256, 0, st>>>(NN, g.S, S32.p);
-    OPSEC_CUDA(cudaGetLastError());
+    TcOperand Stc, Btc;
+    DevBuf<int> tc_err;
+    if (g.tc) {
+        Stc.shape(N, N);
+        tc_split(g.S, N, Stc, st, launches);
+        tc_err.alloc(1);
+        OPSEC_CUDA(cudaMemsetAsync(tc_err.p, 0, sizeof(int), st));
+    } else {
+        S32.alloc(NN);
+        narrow_kernel<<<blocks(NN), 256, 0, st>>>(NN, g.S, S32.p);
+        OPSEC_CUDA(cudaGetLastError());
+    }
+    // C = alpha S X + beta C + gamma D for an N x ncols block X (C, D: N x ncols, leading dimension N)
+    auto sprod = [&](int ncols, float alpha, const float* X, float beta, float* C, float gamma, const float* D) {
+        if (g.tc) {
+            Btc.shape(ncols, N);
+            tc_split(X, N, Btc, st, launches);
+            tc_gemm(Stc, Btc, alpha, beta, C, N, gamma, D, N, 1, g.tile, tc_err.p, g.wait_cycles, st, launches);
+        } else {
+            gemm(CUBLAS_OP_N, CUBLAS_OP_N, N, ncols, N, alpha, S32.p, N, X, N, beta, C, N);
+            if (gamma != 0.f) {
+                axpy_kernel<<<blocks((size_t)N * ncols), 256, 0, st>>>((size_t)N * ncols, gamma, D, C);
+                OPSEC_CUDA(cudaGetLastError());
+                ++*launches;
+            }
+        }
+    };
     Xb.alloc(NB);
     Yb.alloc(NB);
     Zb.alloc(NB);
@@ -328,9 +360,11 @@ void chfsi_eigensolve(const ChfsiArgs& g, cublasHandle_t blas, cusolverDnHandle_
     DevBuf<double> wsd;
     wsd.alloc((size_t)std::max(lw_ev, 1));
     auto check_info = [&](const char* what) {
-        int h = 0;
+        int h = 0, te = 0;
         OPSEC_CUDA(cudaMemcpyAsync(&h, info.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+        if (g.tc) OPSEC_CUDA(cudaMemcpyAsync(&te, tc_err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
         OPSEC_CUDA(cudaStreamSynchronize(st));
+        if (te != 0) fail(OPSEC_ERR_CUDA, "iterative eigensolver: tensor-core GEMM timed out waiting on a pipeline barrier");
         if (h != 0) fail(OPSEC_ERR_NUMERIC, std::string("iterative eigensolver: ") + what + " failed (info " + std::to_string(h) + ")");
     };
     auto orthonormalize = [&](float* Y) {
@@ -341,7 +375,7 @@ void chfsi_eigensolve(const ChfsiArgs& g, cublasHandle_t blas, cusolverDnHandle_
     // Rayleigh-Ritz on the orthonormal Y: X = Y V, Y <- S X, theta and residuals on the host
     auto rayleigh_ritz = [&]() {
         if (g_clock) g_clock->begin("chfsi_rayleigh_ritz", st, 2.0 * NN * B + 2.0 * NB * B * 3);
-        gemm(CUBLAS_OP_N, CUBLAS_OP_N, N, B, N, 1.f, S32.p, N, Yb.p, N, 0.f, Zb.p, N);            // Z = S Y
+        sprod(B, 1.f, Yb.p, 0.f, Zb.p, 0.f, nullptr);                                           // Z = S Y
         gemm(CUBLAS_OP_T, CUBLAS_OP_N, B, B, N, 1.f, Yb.p, N, Zb.p, N, 0.f, Hb.p, B);              // H = Y^T Z
         symmetrize_kernel<float><<<blocks((size_t)B * B), 256, 0, st>>>(B, Hb.p, Hd.p);
         OPSEC_CUDA(cudaGetLastError());
@@ -382,20 +416,13 @@ void chfsi_eigensolve(const ChfsiArgs& g, cublasHandle_t blas, cusolverDnHandle_
         // X holds the Ritz vectors.  Y = (S X - c0 X) sigma1 / e
         const double sigma1 = e / (hi - c0);
         double sigma = sigma1;
-        gemm(CUBLAS_OP_N, CUBLAS_OP_N, N, B, N, (float)(sigma1 / e), S32.p, N, Xb.p, N, 0.f, Yb.p, N);
-        axpy_kernel<<<blocks(NB), 256, 0, st>>>(NB, (float)(-c0 * sigma1 / e), Xb.p, Yb.p);
-        OPSEC_CUDA(cudaGetLastError());
-        ++*launches;
+        sprod(B, (float)(sigma1 / e), Xb.p, 0.f, Yb.p, (float)(-c0 * sigma1 / e), Xb.p);
         float* Xp = Xb.p;
         float* Yp = Yb.p;
         for (int k = 2; k <= degree; k++) {
             const double sn = 1.0 / (2.0 / sigma1 - sigma);
             // X <- (2 sn / e)(S Y - c0 Y) - sigma sn X, then swap so that Y is the newest
-            gemm(CUBLAS_OP_N, CUBLAS_OP_N, N, B, N, (float)(2.0 * sn / e), S32.p, N, Yp, N, (float)(-sigma * sn), Xp,
-                 N);
-            axpy_kernel<<<blocks(NB), 256, 0, st>>>(NB, (float)(-2.0 * sn * c0 / e), Yp, Xp);
-            OPSEC_CUDA(cudaGetLastError());
-            ++*launches;
+            sprod(B, (float)(2.0 * sn / e), Yp, (float)(-sigma * sn), Xp, (float)(-2.0 * sn * c0 / e), Yp);
             std::swap(Xp, Yp);
             sigma = sn;
         }
@@ -482,21 +509,25 @@ void chfsi_eigensolve(const ChfsiArgs& g, cublasHandle_t blas, cusolverDnHandle_
         check_info("Dgeqrf/Dorgqr");
         if (g_clock)
             g_clock->begin("chfsi_refine", st, (round == 0 ? 2.0 * NN * Mr : 2.0 * NR * Mr) + 6.0 * NR * Mr);
-        if (round == 0) {
-            blas_ok(cublasDgemm(blas, CUBLAS_OP_N, CUBLAS_OP_N, N, Mr, N, &one, g.S, N, X64.p, N, &zero, Z64.p, N),
-                    "Dgemm");
-        }
-        blas_ok(cublasDgemm(blas, CUBLAS_OP_T, CUBLAS_OP_N, Mr, Mr, N, &one, X64.p, N, Z64.p, N, &zero, U64.p, Mr),
-                "Dgemm");
+        // the FP64-accurate products: double-FP32 on the FP32 pipes (gemm_df.cu), or cuBLAS DGEMM
+        auto dgemm = [&](bool at, int m, int n, int k, const double* A, int lda, const double* Bm, int ldb, double* Cm,
+                         int ldc) {
+            if (g.df64)
+                df_gemm(at, m, n, k, A, lda, Bm, ldb, Cm, ldc, st, launches);
+            else
+                blas_ok(cublasDgemm(blas, at ? CUBLAS_OP_T : CUBLAS_OP_N, CUBLAS_OP_N, m, n, k, &one, A, lda, Bm, ldb,
+                                    &zero, Cm, ldc),
+                        "Dgemm");
+        };
+        if (round == 0) dgemm(true, N, Mr, N, g.S, N, X64.p, N, Z64.p, N);  // Z = S X (S symmetric)
+        dgemm(true, Mr, Mr, N, X64.p, N, Z64.p, N, U64.p, Mr);              // X^T Z
         symmetrize_kernel<double><<<blocks((size_t)Mr * Mr), 256, 0, st>>>(Mr, U64.p, Hs.p);
         OPSEC_CUDA(cudaGetLastError());
         solver_ok(cusolverDnDsyevd(solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, Mr, Hs.p, Mr, Wd.p, wsd.p,
                                    lmax, info.p),
                   "Dsyevd");
-        blas_ok(cublasDgemm(blas, CUBLAS_OP_N, CUBLAS_OP_N, N, Mr, Mr, &one, X64.p, N, Hs.p, Mr, &zero, U64.p, N),
-                "Dgemm");
-        blas_ok(cublasDgemm(blas, CUBLAS_OP_N, CUBLAS_OP_N, N, Mr, Mr, &one, Z64.p, N, Hs.p, Mr, &zero, X64.p, N),
-                "Dgemm");
+        dgemm(false, N, Mr, Mr, X64.p, N, Hs.p, Mr, U64.p, N);  // U = X V
+        dgemm(false, N, Mr, Mr, Z64.p, N, Hs.p, Mr, X64.p, N);  // S U = Z V
         // X64 = S U kept; Z64 <- S u - theta u (the residual vectors), rd <- their norms
         residual_vectors_kernel<<<Mr, 256, 0, st>>>(N, X64.p, U64.p, Wd.p, Z64.p, rd.p);
         OPSEC_CUDA(cudaGetLastError());
@@ -537,7 +568,7 @@ void chfsi_eigensolve(const ChfsiArgs& g, cublasHandle_t blas, cusolverDnHandle_
         rho0 = rho;
         for (int k = 0; k < g.cg_steps; k++) {
             // Q = (I - P)(theta P - S P)
-            gemm(CUBLAS_OP_N, CUBLAS_OP_N, N, Mr, N, 1.f, S32.p, N, P32.p, N, 0.f, Q32.p, N);
+            sprod(Mr, 1.f, P32.p, 0.f, Q32.p, 0.f, nullptr);
             shift_sub_kernel<<<blocks(NR), 256, 0, st>>>(N, Mr, colv.p, P32.p, Q32.p);
             OPSEC_CUDA(cudaGetLastError());
             project(Q32.p);
@@ -571,7 +602,7 @@ void chfsi_eigensolve(const ChfsiArgs& g, cublasHandle_t blas, cusolverDnHandle_
             ++*launches;
         }
         // Z = S U + |r| S d (S d by an FP32 GEMM), then X = U + |r| d
-        gemm(CUBLAS_OP_N, CUBLAS_OP_N, N, Mr, N, 1.f, S32.p, N, D32.p, N, 0.f, Q32.p, N);
+        sprod(Mr, 1.f, D32.p, 0.f, Q32.p, 0.f, nullptr);
         correct_kernel<<<blocks(NR), 256, 0, st>>>(N, Mr, X64.p, colv.p + Mr, Q32.p, Z64.p);
         correct_kernel<<<blocks(NR), 256, 0, st>>>(N, Mr, U64.p, colv.p + Mr, D32.p, X64.p);
         OPSEC_CUDA(cudaGetLastError());

@@ -178,8 +178,19 @@ void configure(opsec_gpu* c, const std::map<std::string, std::string>& kv) {
     if (has("klt.seed")) c->chfsi.seed = (unsigned long long)to_int("klt.seed", get("klt.seed"));
     if (has("klt.gemm")) {
         const std::string& v = get("klt.gemm");
-        if (v != "bf16x9" && v != "f32") fail(OPSEC_ERR_CONFIG, "klt.gemm must be bf16x9 or f32");
-        c->chfsi.emulate = v == "bf16x9";
+        if (v != "tc" && v != "bf16x9" && v != "f32") fail(OPSEC_ERR_CONFIG, "klt.gemm must be tc, bf16x9 or f32");
+        c->chfsi.tc = v == "tc";
+        c->chfsi.emulate = v != "f32";
+    }
+    if (has("klt.fp64")) {
+        const std::string& v = get("klt.fp64");
+        if (v != "df32" && v != "native") fail(OPSEC_ERR_CONFIG, "klt.fp64 must be df32 or native");
+        c->chfsi.df64 = v == "df32";
+    }
+    if (has("klt.tile")) {
+        const std::string& v = get("klt.tile");
+        if (v != "auto" && v != "128" && v != "256") fail(OPSEC_ERR_CONFIG, "klt.tile must be auto, 128 or 256");
+        c->chfsi.tile = v == "auto" ? 0 : std::atoi(v.c_str());
     }
     if (!(c->chfsi.tol > 0) || c->chfsi.degree < 1 || c->chfsi.degree > 64 || c->chfsi.maxit < 1 || c->chfsi.guard < 0)
         fail(OPSEC_ERR_CONFIG, "klt.tol must be > 0, klt.degree in [1, 64], klt.maxit >= 1, klt.guard >= 0");

@@ -1,6 +1,7 @@
 // context.cpp -- the engine's utilities (errors, device buffers, kernel clocks) and the C ABI of
 // include/opsec_gpu.h, which drives the host-side stages that context.h lists.
 #include "context.h"
+#include "gemm_tc.h"
 
 namespace opsec {
 
@@ -846,6 +847,41 @@ int opsec_gpu_wait_probe(opsec_gpu* c, long long limit_cycles, int arrive, long 
         OPSEC_CUDA(cudaMemcpyAsync(&h, c->probe.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
         sync(c);
         *timed_out = h;
+    });
+}
+
+int opsec_gpu_block_product(opsec_gpu* c, int N, int ncols, const double* S, const float* X, float alpha, float beta,
+                            float* C, float gamma, const float* D) {
+    return guard(c, [&] {
+        if (N < 1 || ncols < 1 || !S || !X || !C || (gamma != 0.f && !D))
+            fail(OPSEC_ERR_ARG, "block product: N, ncols >= 1 and S, X, C (and D when gamma != 0) required");
+        const size_t NN = (size_t)N * N, NX = (size_t)N * ncols;
+        DevBuf<double> dS;
+        DevBuf<float> dX, dC, dD;
+        dS.alloc(NN);
+        dX.alloc(NX);
+        dC.alloc(NX);
+        OPSEC_CUDA(cudaMemcpyAsync(dS.p, S, sizeof(double) * NN, cudaMemcpyHostToDevice, c->stream));
+        OPSEC_CUDA(cudaMemcpyAsync(dX.p, X, sizeof(float) * NX, cudaMemcpyHostToDevice, c->stream));
+        if (beta != 0.f) OPSEC_CUDA(cudaMemcpyAsync(dC.p, C, sizeof(float) * NX, cudaMemcpyHostToDevice, c->stream));
+        if (gamma != 0.f) {
+            dD.alloc(NX);
+            OPSEC_CUDA(cudaMemcpyAsync(dD.p, D, sizeof(float) * NX, cudaMemcpyHostToDevice, c->stream));
+        }
+        TcOperand a, b;
+        a.shape(N, N);
+        b.shape(ncols, N);
+        c->probe.alloc(1);
+        OPSEC_CUDA(cudaMemsetAsync(c->probe.p, 0, sizeof(int), c->stream));
+        tc_split(dS.p, N, a, c->stream, &c->launches);
+        tc_split(dX.p, N, b, c->stream, &c->launches);
+        tc_gemm(a, b, alpha, beta, dC.p, N, gamma, dD.p, N, 1, c->chfsi.tile, c->probe.p, c->proj_wait, c->stream,
+                &c->launches);
+        int h = 0;
+        OPSEC_CUDA(cudaMemcpyAsync(C, dC.p, sizeof(float) * NX, cudaMemcpyDeviceToHost, c->stream));
+        OPSEC_CUDA(cudaMemcpyAsync(&h, c->probe.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+        sync(c);
+        if (h) fail(OPSEC_ERR_CUDA, "block product: tensor-core GEMM timed out waiting on a pipeline barrier");
     });
 }
 

@@ -375,6 +375,7 @@ int eigensolve(opsec_gpu* c, int ncells, const opsec_cell* cells, int M, bool wa
         if (!c->blas) blas_check(cublasCreate(&c->blas), "cublasCreate");
         ca.N = N;
         ca.M = M;
+        ca.wait_cycles = c->proj_wait;
         ca.S = c->S.p;
         ca.modes = c->modes.p;
         ca.evals = c->evals.p;

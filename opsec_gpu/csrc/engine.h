@@ -344,7 +344,11 @@ struct ChfsiArgs {
     int degree = 12;            // largest Chebyshev degree
     int maxit = 100;            // filter iterations at most
     double tol = 1e-5;          // |S x - theta x| <= tol |theta| for the top M
-    int emulate = 1;            // FP32 GEMMs as BF16x9 on the tensor cores (1) or FP32 SIMT (0)
+    int tc = 1;                 // products with S by the engine's tcgen05 kernel (gemm_tc.cu)
+    int tile = 0;               // its output tiles: 128 or 256 columns (0: by the SMs' waves)
+    int df64 = 1;               // refinement products in double-FP32 (gemm_df.cu, 1) or cuBLAS DGEMM (0)
+    int emulate = 1;            // other FP32 GEMMs (and S products when tc = 0) as cuBLAS BF16x9 (1) or FP32 SIMT (0)
+    long long wait_cycles = 2000000000LL;  // bound of the tcgen05 kernel's barrier waits
     int refine = 2;             // FP64 refinement rounds (correction solves) at most
     int cg_steps = 20;          // CG steps per correction solve at most
     unsigned long long seed = 1;

@@ -112,3 +112,40 @@ def test_chfsi_rejects_bad_options():
     for bad in ("klt.solver = lanczos", "klt.degree = 0", "klt.tol = -1", "klt.gemm = tf32"):
         with pytest.raises(api.OpsecError):
             api.Engine(api.make_config(sv, bands=BANDS, extra=(bad,)))
+
+
+def test_block_product_tensor_cores():
+    """The eigensolver's block product C = alpha S X + beta C + gamma D on the tcgen05 kernel
+    against FP64 numpy: ragged N (K padding) and column counts (partial 256-column tiles),
+    rows and columns of S spread over 2^+-8 (FP16 scaling and subnormal low parts).  The
+    split keeps ~22 bits of each operand and the FP32 running sums round once per 64 of K,
+    so the error is a few 1e-7 of sum_k |alpha S_ik X_kj| + |beta C| + |gamma D|."""
+    sv, _ = _box(4, 100.0, periodic=False)
+    rng = np.random.default_rng(5)
+    for N, nc, tile in ((333, 37, "auto"), (1024, 300, "256"), (1500, 640, "128"), (1500, 640, "256")):
+        e = api.Engine(api.make_config(sv, bands=BANDS, extra=(f"klt.tile = {tile}",)))
+        A = rng.standard_normal((N, N))
+        w = np.exp2(rng.uniform(-8, 8, N))
+        S = (A + A.T) * w[:, None] * w[None, :]
+        X = rng.standard_normal((N, nc)).astype(np.float32)
+        C0 = rng.standard_normal((N, nc)).astype(np.float32)
+        D = rng.standard_normal((N, nc)).astype(np.float32)
+        for alpha, beta, gamma in ((1.0, 0.0, 0.0), (0.75, -0.5, 0.25)):
+            out = e.block_product(S, X, alpha, beta, C0, gamma, D if gamma else None)
+            X64 = X.astype(np.float64)
+            ref = alpha * (S @ X64) + beta * C0 + gamma * D
+            bound = abs(alpha) * (np.abs(S) @ np.abs(X64)) + abs(beta) * np.abs(C0) + abs(gamma) * np.abs(D)
+            rel = np.abs(out - ref) / bound
+            print(f"N {N} ncols {nc} tile {tile} beta {beta}: max {rel.max():.2e}, median {np.median(rel):.2e}")
+            assert rel.max() <= 2e-6 and np.median(rel) <= 2e-7, (N, nc, rel.max(), np.median(rel))
+        e.close()
+
+
+def test_chfsi_cublas_route_matches_dense():
+    """klt.gemm = bf16x9, klt.fp64 = native: the products with S through cuBLAS (BF16x9 and
+    DGEMM) instead of the engine's tcgen05 and double-FP32 kernels."""
+    sv, cells = _box(12, 600.0, periodic=False)
+    d, c = _pair(sv, 200, extra=("klt.gemm = bf16x9", "klt.fp64 = native"))
+    _compare(d, c, cells, 200)
+    d.close()
+    c.close()

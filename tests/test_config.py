@@ -39,6 +39,8 @@ BAD = [
     ("klt.degree = 0", "klt.degree"),
     ("klt.tol = -1", "klt.tol"),
     ("klt.gemm = tf32", "klt.gemm"),
+    ("klt.tile = 64", "klt.tile"),
+    ("klt.fp64 = f64", "klt.fp64"),
     ("klt.refine = -1", "klt.refine"),
     ("sig.gauss = 7", "sig.gauss"),
     ("azimuthal.split = 17", "azimuthal.split"),
@@ -73,7 +75,8 @@ def test_survey_type_is_required(create):
 @pytest.mark.parametrize("coordsys", [1, 2])
 def test_valid_configurations_pass_the_parser(create, coordsys):
     text = _base(coordsys)
-    for extra in ("", "klt.solver = chfsi\nklt.gemm = f32\nklt.degree = 6\n", "mixing = inverse-sqrt\n",
+    for extra in ("", "klt.solver = chfsi\nklt.gemm = f32\nklt.degree = 6\n", "klt.gemm = tc\nklt.tile = 256\n",
+                  "klt.gemm = bf16x9\nklt.tile = auto\nklt.fp64 = native\n", "mixing = inverse-sqrt\n",
                   "solver = parpack\n", "azimuthal.eig = own\nprojection.wait_cycles = 20000000\n",
                   "azimuthal.eig = batched\n"):
         rc, msg = create(text + extra)
