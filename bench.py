@@ -129,11 +129,14 @@ def bench_eig(args):
     k, P = synth.pk_table()
     out = {}
     for solver in (("chfsi", "dense") if args.compare_dense else ("chfsi",)):
-        e = api.Engine(api.make_config(sv, bands=bands, nmodes=M, extra=(f"klt.solver = {solver}", "profile = 1")))
+        e = api.Engine(api.make_config(sv, bands=bands, nmodes=M,
+                                       extra=(f"klt.solver = {solver}", "profile = 1") +
+                                       tuple(kv.replace("=", " = ", 1) for kv in args.set)))
         e.set_pk(k, P)
         for _ in range(args.warmup):
             e.klt(cells, M)
-        base = {name: e.kernel_stats(name) for name in ("chfsi_filter", "chfsi_rayleigh_ritz", "chfsi_refine",
+        base = {name: e.kernel_stats(name) for name in ("chfsi_bounds", "chfsi_filter", "chfsi_qr32",
+                                                        "chfsi_rayleigh_ritz", "chfsi_qr64", "chfsi_refine",
                                                         "chfsi_correct")}
         launches0 = e.launch_count()
         times = []
@@ -157,15 +160,20 @@ def bench_eig(args):
     line = {"metric": f"top {M} eigenpairs of a dense {cells.size}-cell box (iterative eigensolver)",
             "value": c["s"], "unit": "s/solve", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": c["s"] * 1000, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32 (bf16x9 tensor) + f64", "data": "synthetic",
+            "dtype": "f16x3 (tcgen05) + double-f32", "data": "synthetic",
             "config": {"workload": args.workload, "cells": int(cells.size), "modes": M, "bands": 6,
                        "grid": f"{n}^3 open box, 50 Mpc/h cells, anisotropic Gaussian selection",
                        "l2": f"inputs larger than L2 (S: {cells.size ** 2 * 8 / 1e9:.1f} GB FP64)"},
             "eig_stats": c["stats"], "kernels": c["kernels"], "gpu_launches": c["launches"],
-            "roofline": {"kernel": "chfsi_filter (cuBLAS BF16x9 GEMMs)", "bound": "tensor",
-                         "achieved": filt["tflops"], "unit": "TFLOP/s (FP32-equivalent)",
-                         "peak": bf16 / 9.0, "peak_kind": f"{kind} bf16 GEMM / 9 (BF16x9: nine BF16 products per FP32 one)",
-                         "frac": filt["tflops"] / (bf16 / 9.0), "traffic": None},
+            "roofline": {"kernel": "chfsi_filter (tn_gemm_kernel: tcgen05 FP16 hi/lo, three products)",
+                         "bound": "tensor", "achieved": filt["tflops"], "unit": "TFLOP/s (FP32-equivalent)",
+                         "peak": bf16 / 3.0,
+                         "peak_kind": f"{kind} bf16 dense GEMM / 3 (three FP16 products per FP32-equivalent one; "
+                                      "FP16 and BF16 share the tensor rate)",
+                         "frac": filt["tflops"] / (bf16 / 3.0), "traffic": None,
+                         "refine": c["kernels"].get("chfsi_refine", {}),
+                         "refine_note": "FP64-accurate products in double-FP32 on the FP32 pipes (df_gemm_kernel); "
+                                        "tflops counts FP64 flop"},
             "e2e": {"value": c["s"], "unit": "s/solve", "h2d_bytes_per_step": int(cells.nbytes),
                     "d2h_bytes_per_step": int(8 * M * (cells.size + 1))}}
     if "dense" in out:

@@ -80,6 +80,13 @@ __global__ void narrow_kernel(size_t n, const double* in, float* out) {
         out[e] = (float)in[e];
 }
 
+// A = I (n x n)
+__global__ void identity_kernel(int n, double* A) {
+    const size_t total = (size_t)n * n;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x)
+        A[e] = (e % n == e / n) ? 1.0 : 0.0;
+}
+
 __global__ void widen_kernel(size_t n, const float* in, double* out) {
     for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x)
         out[e] = (double)in[e];
@@ -282,6 +289,7 @@ void chfsi_eigensolve(const ChfsiArgs& g, cublasHandle_t blas, cusolverDnHandle_
     std::vector<double> al, be;
     double beta = 0.0;
     const int steps = std::min(kLanczos, N);
+    if (g_clock) g_clock->begin("chfsi_bounds", st, 2.0 * NN * steps);
     for (int j = 0; j < steps; j++) {
         const double one = 1.0, zero = 0.0;
         blas_ok(cublasDgemv(blas, CUBLAS_OP_N, N, N, &one, g.S, N, v1, 1, &zero, w, 1), "Dgemv");
@@ -299,6 +307,7 @@ void chfsi_eigensolve(const ChfsiArgs& g, cublasHandle_t blas, cusolverDnHandle_
         OPSEC_CUDA(cudaMemcpyAsync(v1, w, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
         blas_ok(cublasDscal(blas, N, &inv, v1, 1), "Dscal");
     }
+    if (g_clock) g_clock->end(st);
     const double tmin = chfsi::tridiag_eig(al, be, 0), tmax = chfsi::tridiag_eig(al, be, (int)al.size() - 1);
     double hi = tmax + std::fabs(beta);
     const double lo = tmin - 0.02 * (hi - tmin);
@@ -429,7 +438,9 @@ void chfsi_eigensolve(const ChfsiArgs& g, cublasHandle_t blas, cusolverDnHandle_
         if (g_clock) g_clock->end(st);
         s.gemms += degree;
         if (Yp != Yb.p) OPSEC_CUDA(cudaMemcpyAsync(Yb.p, Yp, sizeof(float) * NB, cudaMemcpyDeviceToDevice, st));
+        if (g_clock) g_clock->begin("chfsi_qr32", st, 4.0 * NB * B);
         orthonormalize(Yb.p);
+        if (g_clock) g_clock->end(st);
         rayleigh_ritz();
         // convergence of the top M: residual below tol theta_i or the FP32 floor
         double worst = 0.0;
@@ -483,14 +494,18 @@ void chfsi_eigensolve(const ChfsiArgs& g, cublasHandle_t blas, cusolverDnHandle_
     DevBuf<double> colv;  // per-column scalars: theta, scale, alpha, beta
     colv.alloc((size_t)4 * Mr);
     tau64.alloc(Mr);
-    int lq = 0, lo2 = 0, le = 0;
+    int lq = 0, lo2 = 0, le = 0, lc = 0;
+    DevBuf<double> G64, Ri64;  // CholeskyQR: the Gram matrix / its Cholesky factor, the factor's inverse
+    G64.alloc((size_t)Mr * Mr);
+    Ri64.alloc((size_t)Mr * Mr);
+    solver_ok(cusolverDnDpotrf_bufferSize(solver, CUBLAS_FILL_MODE_UPPER, Mr, G64.p, Mr, &lc), "Dpotrf_bufferSize");
     solver_ok(cusolverDnDgeqrf_bufferSize(solver, N, Mr, X64.p, N, &lq), "Dgeqrf_bufferSize");
     solver_ok(cusolverDnDorgqr_bufferSize(solver, N, Mr, Mr, X64.p, N, tau64.p, &lo2), "Dorgqr_bufferSize");
     solver_ok(cusolverDnDsyevd_bufferSize(solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, Mr, Hs.p, Mr,
                                           Wd.p, &le),
               "Dsyevd_bufferSize");
     wsd.release();
-    wsd.alloc((size_t)std::max(std::max(lq, lo2), std::max(le, 1)));
+    wsd.alloc((size_t)std::max(std::max(std::max(lq, lo2), std::max(le, 1)), lc));
     const int lmax = (int)wsd.n;
     std::vector<double> w64(Mr), r64(Mr), hv(4 * (size_t)Mr), pq(Mr), rho(Mr), rho0(Mr);
     const double one = 1.0, zero = 0.0;
@@ -500,12 +515,51 @@ void chfsi_eigensolve(const ChfsiArgs& g, cublasHandle_t blas, cusolverDnHandle_
         // the FP64 S.  Later passes: X = U + D and Z = S U + S D are carried in (S U from the last
         // pass in FP64, S D by an FP32 GEMM: D is small, so FP32 costs it nothing), and X = Q R
         // turns Z into Z R^-1 = S Q by a triangular solve before R is overwritten
-        solver_ok(cusolverDnDgeqrf(solver, N, Mr, X64.p, N, tau64.p, wsd.p, lmax, info.p), "Dgeqrf");
-        if (round > 0)
-            blas_ok(cublasDtrsm(blas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, N, Mr,
-                                &one, X64.p, N, Z64.p, N),
-                    "Dtrsm");
-        solver_ok(cusolverDnDorgqr(solver, N, Mr, Mr, X64.p, N, tau64.p, wsd.p, lmax, info.p), "Dorgqr");
+        if (g_clock) g_clock->begin("chfsi_qr64", st, 4.0 * NR * Mr);
+        bool qr_done = false;
+        if (g.cholqr && g.df64) {
+            // CholeskyQR2 (Fukaya, Nakatsukasa, Yanagisawa, Yamamoto 2014): twice G = X^T X,
+            // G = R^T R (Cholesky), X <- X R^-1 (and Z <- Z R^-1); the products in double-FP32,
+            // R^-1 from a triangular solve on the identity.  The refinement's X has nearly
+            // orthonormal columns, so the first pass already leaves X orthonormal to ~eps64 cond^2
+            // and the second to ~eps64.  A failed factorisation falls back to Householder QR.
+            qr_done = true;
+            for (int pass = 0; pass < 2 && qr_done; pass++) {
+                df_gemm(true, Mr, Mr, N, X64.p, N, X64.p, N, G64.p, Mr, st, launches);
+                solver_ok(cusolverDnDpotrf(solver, CUBLAS_FILL_MODE_UPPER, Mr, G64.p, Mr, wsd.p, lmax, info.p),
+                          "Dpotrf");
+                int h = 0;
+                OPSEC_CUDA(cudaMemcpyAsync(&h, info.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+                OPSEC_CUDA(cudaStreamSynchronize(st));
+                if (h != 0) {
+                    qr_done = false;
+                    break;
+                }
+                identity_kernel<<<blocks((size_t)Mr * Mr), 256, 0, st>>>(Mr, Ri64.p);
+                OPSEC_CUDA(cudaGetLastError());
+                ++*launches;
+                blas_ok(cublasDtrsm(blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT,
+                                    Mr, Mr, &one, G64.p, Mr, Ri64.p, Mr),
+                        "Dtrsm");
+                df_gemm(false, N, Mr, Mr, X64.p, N, Ri64.p, Mr, U64.p, N, st, launches);
+                OPSEC_CUDA(cudaMemcpyAsync(X64.p, U64.p, sizeof(double) * NR, cudaMemcpyDeviceToDevice, st));
+                if (round > 0) {
+                    df_gemm(false, N, Mr, Mr, Z64.p, N, Ri64.p, Mr, U64.p, N, st, launches);
+                    OPSEC_CUDA(cudaMemcpyAsync(Z64.p, U64.p, sizeof(double) * NR, cudaMemcpyDeviceToDevice, st));
+                }
+            }
+            // a failure in the second pass leaves X and Z transformed consistently by the first:
+            // Householder below starts from there
+        }
+        if (!qr_done) {
+            solver_ok(cusolverDnDgeqrf(solver, N, Mr, X64.p, N, tau64.p, wsd.p, lmax, info.p), "Dgeqrf");
+            if (round > 0)
+                blas_ok(cublasDtrsm(blas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, N,
+                                    Mr, &one, X64.p, N, Z64.p, N),
+                        "Dtrsm");
+            solver_ok(cusolverDnDorgqr(solver, N, Mr, Mr, X64.p, N, tau64.p, wsd.p, lmax, info.p), "Dorgqr");
+        }
+        if (g_clock) g_clock->end(st);
         check_info("Dgeqrf/Dorgqr");
         if (g_clock)
             g_clock->begin("chfsi_refine", st, (round == 0 ? 2.0 * NN * Mr : 2.0 * NR * Mr) + 6.0 * NR * Mr);

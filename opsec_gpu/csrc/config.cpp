@@ -187,6 +187,11 @@ void configure(opsec_gpu* c, const std::map<std::string, std::string>& kv) {
         if (v != "df32" && v != "native") fail(OPSEC_ERR_CONFIG, "klt.fp64 must be df32 or native");
         c->chfsi.df64 = v == "df32";
     }
+    if (has("klt.qr")) {
+        const std::string& v = get("klt.qr");
+        if (v != "cholesky2" && v != "householder") fail(OPSEC_ERR_CONFIG, "klt.qr must be cholesky2 or householder");
+        c->chfsi.cholqr = v == "cholesky2";
+    }
     if (has("klt.tile")) {
         const std::string& v = get("klt.tile");
         if (v != "auto" && v != "128" && v != "256") fail(OPSEC_ERR_CONFIG, "klt.tile must be auto, 128 or 256");

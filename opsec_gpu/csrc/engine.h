@@ -347,6 +347,7 @@ struct ChfsiArgs {
     int tc = 1;                 // products with S by the engine's tcgen05 kernel (gemm_tc.cu)
     int tile = 0;               // its output tiles: 128 or 256 columns (0: by the SMs' waves)
     int df64 = 1;               // refinement products in double-FP32 (gemm_df.cu, 1) or cuBLAS DGEMM (0)
+    int cholqr = 1;             // refinement QR: CholeskyQR2 with double-FP32 products (1) or Householder (0)
     int emulate = 1;            // other FP32 GEMMs (and S products when tc = 0) as cuBLAS BF16x9 (1) or FP32 SIMT (0)
     long long wait_cycles = 2000000000LL;  // bound of the tcgen05 kernel's barrier waits
     int refine = 2;             // FP64 refinement rounds (correction solves) at most

@@ -142,10 +142,11 @@ def test_block_product_tensor_cores():
 
 
 def test_chfsi_cublas_route_matches_dense():
-    """klt.gemm = bf16x9, klt.fp64 = native: the products with S through cuBLAS (BF16x9 and
-    DGEMM) instead of the engine's tcgen05 and double-FP32 kernels."""
+    """klt.gemm = bf16x9, klt.fp64 = native, klt.qr = householder: the products with S through
+    cuBLAS (BF16x9 and DGEMM) and the refinement's QR by cuSOLVER's Householder, instead of the
+    engine's tcgen05 and double-FP32 kernels and CholeskyQR2."""
     sv, cells = _box(12, 600.0, periodic=False)
-    d, c = _pair(sv, 200, extra=("klt.gemm = bf16x9", "klt.fp64 = native"))
+    d, c = _pair(sv, 200, extra=("klt.gemm = bf16x9", "klt.fp64 = native", "klt.qr = householder"))
     _compare(d, c, cells, 200)
     d.close()
     c.close()

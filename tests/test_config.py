@@ -41,6 +41,7 @@ BAD = [
     ("klt.gemm = tf32", "klt.gemm"),
     ("klt.tile = 64", "klt.tile"),
     ("klt.fp64 = f64", "klt.fp64"),
+    ("klt.qr = lq", "klt.qr"),
     ("klt.refine = -1", "klt.refine"),
     ("sig.gauss = 7", "sig.gauss"),
     ("azimuthal.split = 17", "azimuthal.split"),
@@ -76,7 +77,7 @@ def test_survey_type_is_required(create):
 def test_valid_configurations_pass_the_parser(create, coordsys):
     text = _base(coordsys)
     for extra in ("", "klt.solver = chfsi\nklt.gemm = f32\nklt.degree = 6\n", "klt.gemm = tc\nklt.tile = 256\n",
-                  "klt.gemm = bf16x9\nklt.tile = auto\nklt.fp64 = native\n", "mixing = inverse-sqrt\n",
+                  "klt.gemm = bf16x9\nklt.tile = auto\nklt.fp64 = native\nklt.qr = householder\n", "mixing = inverse-sqrt\n",
                   "solver = parpack\n", "azimuthal.eig = own\nprojection.wait_cycles = 20000000\n",
                   "azimuthal.eig = batched\n"):
         rc, msg = create(text + extra)
