@@ -509,6 +509,34 @@ void chfsi_eigensolve(const ChfsiArgs& g, cublasHandle_t blas, cusolverDnHandle_
     const int lmax = (int)wsd.n;
     std::vector<double> w64(Mr), r64(Mr), hv(4 * (size_t)Mr), pq(Mr), rho(Mr), rho0(Mr);
     const double one = 1.0, zero = 0.0;
+    // The FP64-accurate products: double-FP32 on the FP32 pipes (gemm_df.cu; operands split into
+    // float pairs first, S once per solve), or cuBLAS DGEMM.  A is K-major (C = A^T B) when at.
+    DevBuf<float> dfS, dfA, dfB;
+    DevBuf<double> dwork;
+    if (g.df64) {
+        dfS.alloc(2 * NN);
+        df_split(NN, g.S, dfS.p, st, launches);
+    }
+    auto dprod = [&](bool at, int m, int n, int k, const double* A, int lda, const double* Bm, int ldb, double* Cm,
+                     int ldc) {
+        if (!g.df64) {
+            blas_ok(cublasDgemm(blas, at ? CUBLAS_OP_T : CUBLAS_OP_N, CUBLAS_OP_N, m, n, k, &one, A, lda, Bm, ldb, &zero,
+                                Cm, ldc),
+                    "Dgemm");
+            return;
+        }
+        const float* a = dfS.p;
+        if (A != g.S) {
+            const size_t na = (size_t)lda * (at ? m : k);
+            dfA.alloc(2 * na);
+            df_split(na, A, dfA.p, st, launches);
+            a = dfA.p;
+        }
+        const size_t nb = (size_t)ldb * n;
+        dfB.alloc(2 * nb);
+        df_split(nb, Bm, dfB.p, st, launches);
+        df_gemm(at, m, n, k, a, lda, dfB.p, ldb, Cm, ldc, dwork, st, launches);
+    };
     const double target = 0.1 * g.tol;  // refine until the residuals are a tenth of the tolerance
     for (int round = 0;; round++) {
         // orthonormal basis Q of the current vectors and Z = S Q.  First pass: Z by a DGEMM with
@@ -525,7 +553,7 @@ void chfsi_eigensolve(const ChfsiArgs& g, cublasHandle_t blas, cusolverDnHandle_
             // and the second to ~eps64.  A failed factorisation falls back to Householder QR.
             qr_done = true;
             for (int pass = 0; pass < 2 && qr_done; pass++) {
-                df_gemm(true, Mr, Mr, N, X64.p, N, X64.p, N, G64.p, Mr, st, launches);
+                dprod(true, Mr, Mr, N, X64.p, N, X64.p, N, G64.p, Mr);
                 solver_ok(cusolverDnDpotrf(solver, CUBLAS_FILL_MODE_UPPER, Mr, G64.p, Mr, wsd.p, lmax, info.p),
                           "Dpotrf");
                 int h = 0;
@@ -541,10 +569,10 @@ void chfsi_eigensolve(const ChfsiArgs& g, cublasHandle_t blas, cusolverDnHandle_
                 blas_ok(cublasDtrsm(blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT,
                                     Mr, Mr, &one, G64.p, Mr, Ri64.p, Mr),
                         "Dtrsm");
-                df_gemm(false, N, Mr, Mr, X64.p, N, Ri64.p, Mr, U64.p, N, st, launches);
+                dprod(false, N, Mr, Mr, X64.p, N, Ri64.p, Mr, U64.p, N);
                 OPSEC_CUDA(cudaMemcpyAsync(X64.p, U64.p, sizeof(double) * NR, cudaMemcpyDeviceToDevice, st));
                 if (round > 0) {
-                    df_gemm(false, N, Mr, Mr, Z64.p, N, Ri64.p, Mr, U64.p, N, st, launches);
+                    dprod(false, N, Mr, Mr, Z64.p, N, Ri64.p, Mr, U64.p, N);
                     OPSEC_CUDA(cudaMemcpyAsync(Z64.p, U64.p, sizeof(double) * NR, cudaMemcpyDeviceToDevice, st));
                 }
             }
@@ -563,25 +591,15 @@ void chfsi_eigensolve(const ChfsiArgs& g, cublasHandle_t blas, cusolverDnHandle_
         check_info("Dgeqrf/Dorgqr");
         if (g_clock)
             g_clock->begin("chfsi_refine", st, (round == 0 ? 2.0 * NN * Mr : 2.0 * NR * Mr) + 6.0 * NR * Mr);
-        // the FP64-accurate products: double-FP32 on the FP32 pipes (gemm_df.cu), or cuBLAS DGEMM
-        auto dgemm = [&](bool at, int m, int n, int k, const double* A, int lda, const double* Bm, int ldb, double* Cm,
-                         int ldc) {
-            if (g.df64)
-                df_gemm(at, m, n, k, A, lda, Bm, ldb, Cm, ldc, st, launches);
-            else
-                blas_ok(cublasDgemm(blas, at ? CUBLAS_OP_T : CUBLAS_OP_N, CUBLAS_OP_N, m, n, k, &one, A, lda, Bm, ldb,
-                                    &zero, Cm, ldc),
-                        "Dgemm");
-        };
-        if (round == 0) dgemm(true, N, Mr, N, g.S, N, X64.p, N, Z64.p, N);  // Z = S X (S symmetric)
-        dgemm(true, Mr, Mr, N, X64.p, N, Z64.p, N, U64.p, Mr);              // X^T Z
+        if (round == 0) dprod(true, N, Mr, N, g.S, N, X64.p, N, Z64.p, N);  // Z = S X (S symmetric)
+        dprod(true, Mr, Mr, N, X64.p, N, Z64.p, N, U64.p, Mr);              // X^T Z
         symmetrize_kernel<double><<<blocks((size_t)Mr * Mr), 256, 0, st>>>(Mr, U64.p, Hs.p);
         OPSEC_CUDA(cudaGetLastError());
         solver_ok(cusolverDnDsyevd(solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, Mr, Hs.p, Mr, Wd.p, wsd.p,
                                    lmax, info.p),
                   "Dsyevd");
-        dgemm(false, N, Mr, Mr, X64.p, N, Hs.p, Mr, U64.p, N);  // U = X V
-        dgemm(false, N, Mr, Mr, Z64.p, N, Hs.p, Mr, X64.p, N);  // S U = Z V
+        dprod(false, N, Mr, Mr, X64.p, N, Hs.p, Mr, U64.p, N);  // U = X V
+        dprod(false, N, Mr, Mr, Z64.p, N, Hs.p, Mr, X64.p, N);  // S U = Z V
         // X64 = S U kept; Z64 <- S u - theta u (the residual vectors), rd <- their norms
         residual_vectors_kernel<<<Mr, 256, 0, st>>>(N, X64.p, U64.p, Wd.p, Z64.p, rd.p);
         OPSEC_CUDA(cudaGetLastError());

@@ -11,7 +11,7 @@
 // bits and the tensor core forms Ah Bh + Ah Bl + Al Bh (the dropped Al Bl is ~2^-22 of each
 // product).  One CTA per 128 x 256 output tile:
 //   - warp 0 loads A (128 rows) and B (256 rows) hi/lo slices of 64 along K by TMA (128-byte
-//     swizzle), two stages;
+//     swizzle), two stages (three for 128-column tiles);
 //   - warp 1 (one lane) issues tcgen05.mma kind::f16 M = 128, N = 128, K = 16 for the two
 //     halves of the 256 columns into two TMEM accumulators, the cross terms of a slice first
 //     (while the accumulator is small);
@@ -41,15 +41,19 @@ namespace {
 using namespace tc;
 
 constexpr int GM = 128, GN = 256, GK = 64;  // output tile (GN: the widest), K slice (64 FP16 = one 128-byte row)
-constexpr int GSTAGES = 2;
 constexpr uint32_t GA_BYTES = GM * GK * 2;  // 16 KB
-// NH halves of 128 columns per tile: B tiles of 128 NH rows
+// NH halves of 128 columns per tile: B tiles of 128 NH rows; as many stages as fit beside the
+// barriers (the slices in flight must cover the TMA latency: a 128 x 128 tile consumes a 64 KB
+// stage in ~800 tensor-core cycles)
 template <int NH>
 struct TileShape {
     static constexpr int N = 128 * NH;
     static constexpr uint32_t B_BYTES = N * GK * 2;
     static constexpr uint32_t STAGE_BYTES = 2 * GA_BYTES + 2 * B_BYTES;
+    static constexpr int STAGES = NH == 1 ? 3 : 2;
+    static constexpr size_t SMEM = (size_t)STAGES * STAGE_BYTES + 1024;
 };
+constexpr int kMaxStages = 3;
 constexpr uint32_t G_TMEM_COLS = 512;  // D0, D1 (128 each), R0, R1
 constexpr int kDrain = 8;              // warps 4-11: TMEM lane quarter x column half of a half
 constexpr int kGThreads = 32 * (4 + kDrain);
@@ -103,7 +107,8 @@ __global__ void __launch_bounds__(kGThreads, 1)
                    const __grid_constant__ CUtensorMap mBh, const __grid_constant__ CUtensorMap mBl, GemmParams p) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    __shared__ __align__(8) unsigned long long bar_full[GSTAGES], bar_empty[GSTAGES], bar_chunk[2], bar_drained[2];
+    constexpr int GSTAGES = TileShape<NH>::STAGES;
+    __shared__ __align__(8) unsigned long long bar_full[kMaxStages], bar_empty[kMaxStages], bar_chunk[2], bar_drained[2];
     __shared__ uint32_t tmem_slot;
     __shared__ volatile int abort_flag;
 
@@ -353,7 +358,7 @@ void tc_gemm(const TcOperand& A, const TcOperand& B, float alpha, float beta, fl
     const CUtensorMap mAh = make_map(h(A.hi()), A.rows_pad, A.kpad, GM), mAl = make_map(h(A.lo()), A.rows_pad, A.kpad, GM);
     const CUtensorMap mBh = make_map(h(B.hi()), B.rows_pad, B.kpad, 128 * NH);
     const CUtensorMap mBl = make_map(h(B.lo()), B.rows_pad, B.kpad, 128 * NH);
-    const size_t smem = (size_t)GSTAGES * (NH == 1 ? TileShape<1>::STAGE_BYTES : TileShape<2>::STAGE_BYTES) + 1024;
+    const size_t smem = NH == 1 ? TileShape<1>::SMEM : TileShape<2>::SMEM;
     GemmParams p;
     p.ntj = (B.rows + 128 * NH - 1) / (128 * NH);
     p.nk = A.kpad / GK;
