@@ -257,8 +257,8 @@ int opsec_gpu_fail_alloc(opsec_gpu* ctx, long long after);
 
 /* The block product of the iterative eigensolver (klt.solver = chfsi): the product
  * of the signal matrix with a block of vectors that replaces the reference's one
- * matrix-vector product per ARPACK step (the OP * x of the reverse-communication
- * loop, ParpackSolver.cpp:111-123), on the engine's tcgen05 kernel:
+ * matrix-vector product per ARPACK step (y = A x of the reverse-communication
+ * loop, ParpackSolver.cpp:116-122), on the engine's tcgen05 kernel:
  *   C = alpha S X + beta C + gamma D
  * S: N x N symmetric (FP64, both triangles); X, C, D: N x ncols FP32, column-major
  * (leading dimension N); host buffers.  S and X are split into FP16 hi + lo after
