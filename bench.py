@@ -287,12 +287,30 @@ class ClockSampler:
         self.out = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
 
     def start(self):
+        """Start sampling and wait (up to 10 s) for the first sample, so that the timed region that
+        follows is covered; the rows written before mark() are left out of the record."""
+        self.skip = 0
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
                                           "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.out,
                                          stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
+            return
+        t0 = time.time()
+        while time.time() - t0 < 10.0 and self.proc.poll() is None and self._rows() == 0:
+            time.sleep(0.05)
+
+    def _rows(self):
+        try:
+            with open(self.out.name) as f:
+                return sum(1 for l in f if l.strip())
+        except OSError:
+            return 0
+
+    def mark(self):
+        """The timed region starts: earlier rows are not part of its record."""
+        self.skip = self._rows()
 
     def stop(self):
         if self.proc is None:
@@ -305,6 +323,8 @@ class ClockSampler:
         self.out.flush()
         rows = [l.strip().split(",") for l in open(self.out.name) if l.strip()]
         os.unlink(self.out.name)
+        if len(rows) > self.skip:  # keep the rows of the timed region (all of them if it saw none)
+            rows = rows[self.skip:]
         sm = [float(r[1]) for r in rows if len(r) >= 9 and r[1].strip().replace(".", "").isdigit()]
         mx = [float(r[2]) for r in rows if len(r) >= 9 and r[2].strip().replace(".", "").isdigit()]
         reasons = set()
@@ -596,6 +616,7 @@ def main():
     clocks = ClockSampler(local)
     clocks.start()
     barrier()
+    clocks.mark()
     t0 = time.perf_counter()
     dev_ms = 0.0
     stage_tot = None
