@@ -107,7 +107,9 @@ def bench_mocks(args):
                        "modes": "Ncells / 4", "grid": "nr x 16 x 16 full-sky shells",
                        "selection": "Gaussian shell, centre U[300, 900], width U[100, 300]"},
             "sequential_mocks_per_s": 256 / seq["seconds"], "workers": auto["workers"],
-            "autotune_mocks_per_s": auto["autotune_mocks_per_s"], "max_fisher_diff_batched_vs_sequential": dF,
+            "autotune_rates": auto["autotune_mocks_per_s"],
+            "autotune_rates_unit": "mocks of the batch's mean cost (ncells^1.5) per second, per worker count",
+            "max_fisher_diff_batched_vs_sequential": dF,
             "mock_generation_s": gen_s,
             "e2e": {"value": rate, "unit": "mocks/s", "h2d_bytes_per_step": int(sum(m["cells"].nbytes + m["counts"].nbytes for m in mocks)),
                     "d2h_bytes_per_step": int(256 * 8 * (2 * 20 * 20 + 20))}}

@@ -184,11 +184,12 @@ typedef struct {
  * `ctx`: worker contexts (each with its own stream, solver handles and xi
  * tables, computed once) take mocks in turn from host threads, so that the
  * builds of small surveys overlap on the GPU.  workers = 1 runs them one after
- * the other; workers <= 0 autotunes the count on the first mocks (1, 2, 4 and 8
- * workers, two mocks each) and runs the rest with the fastest.  Outputs per
- * mock i (mixing = inverse): F + i nb^2, phat + i nb, pcov + i nb^2 (any may be
- * NULL).  stats (6, may be NULL): seconds, workers used, then the mocks per
- * second measured for 1, 2, 4 and 8 workers while autotuning. */
+ * the other; workers <= 0 autotunes the count on the first mocks (1, 2, 4, 8, 12
+ * and 16 workers, two mocks each) and runs the rest with the fastest.  Outputs
+ * per mock i (mixing = inverse): F + i nb^2, phat + i nb, pcov + i nb^2 (any may
+ * be NULL).  stats (8, may be NULL): seconds, workers used, then the rate of
+ * each candidate while autotuning, in mocks of the batch's mean cost per second
+ * (a mock's cost taken as ncells^1.5: the largest mocks run first). */
 int opsec_gpu_batch_fisher(opsec_gpu* ctx, int nmocks, const opsec_mock* mocks, int workers, double* F,
                            double* phat, double* pcov, double* stats);
 

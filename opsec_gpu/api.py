@@ -347,11 +347,11 @@ class Engine:
         F = np.zeros((len(mocks), nb, nb))
         phat = np.zeros((len(mocks), nb))
         pcov = np.zeros((len(mocks), nb, nb))
-        st = np.zeros(6)
+        st = np.zeros(8)
         self._check(self._L.opsec_gpu_batch_fisher(self._h, len(mocks), C.cast(arr, C.c_void_p), int(workers), _d(F),
                                                    _d(phat), _d(pcov), _d(st)))
         return {"F": F, "phat": phat, "pcov": pcov, "seconds": st[0], "workers": int(st[1]),
-                "autotune_mocks_per_s": {k: st[2 + i] for i, k in enumerate((1, 2, 4, 8))}}
+                "autotune_mocks_per_s": {k: st[2 + i] for i, k in enumerate((1, 2, 4, 8, 12, 16))}}
 
     def fisher_build(self, cells, counts, nmodes, mixing="inverse", want_evals=True):
         cells = _cells(cells)

@@ -1,6 +1,8 @@
 // batch.cpp -- many independent mock surveys on worker contexts (opsec_gpu_batch_fisher).
 #include "context.h"
 
+#include <cmath>
+
 // ---------------------------------------------------------------- batched mocks
 namespace {
 // One mock on a worker context whose xi tables are already built: the survey
@@ -41,7 +43,7 @@ int opsec_gpu_batch_fisher(opsec_gpu* c, int nmocks, const opsec_mock* mocks, in
         if (nmocks <= 0 || !mocks) fail(OPSEC_ERR_ARG, "no mocks");
         if (workers > 16) fail(OPSEC_ERR_ARG, "at most 16 workers");
         const int nb = c->ntab() - 1;
-        const int maxw = workers > 0 ? workers : 8;
+        const int maxw = workers > 0 ? workers : 16;
         // worker contexts: the template's configuration and P(k), tables built once each
         std::vector<opsec_gpu*> ctx(maxw, nullptr);
         struct Cleanup {
@@ -94,14 +96,22 @@ int opsec_gpu_batch_fisher(opsec_gpu* c, int nmocks, const opsec_mock* mocks, in
         const auto t0 = now();
         int best = maxw;
         if (workers <= 0) {
-            // autotune the concurrency on the first mocks: 1, 2, 4, 8 workers, 2 per worker each
-            const int cand[4] = {1, 2, 4, 8};
+            // autotune the concurrency on the first mocks: 1, 2, 4, 8, 12, 16 workers, 2 mocks per
+            // worker each.  The mocks run largest first, so each candidate sees smaller mocks than
+            // the one before: its rate counts mocks of the batch's mean cost per second, a mock's
+            // cost taken as ncells^1.5 (the cubature's key count grows as ncells^2 / nphi)
+            const int cand[6] = {1, 2, 4, 8, 12, 16};
+            auto cost = [&](int i) { return std::pow((double)mocks[order[i]].ncells, 1.5); };
+            double mean = 0;
+            for (int i = 0; i < nmocks; i++) mean += cost(i) / nmocks;
             double best_rate = 0;
-            for (int ci = 0; ci < 4 && next.load() < nmocks; ci++) {
+            for (int ci = 0; ci < 6 && next.load() < nmocks; ci++) {
                 const int start = next.load(), end = std::min(nmocks, start + 2 * cand[ci]);
                 const auto ta = now();
                 run_range(cand[ci], end);
-                const double rate = (end - start) / std::chrono::duration<double>(now() - ta).count();
+                double work = 0;
+                for (int i = start; i < end; i++) work += cost(i) / mean;
+                const double rate = work / std::chrono::duration<double>(now() - ta).count();
                 if (stats) stats[2 + ci] = rate;
                 if (rate > best_rate) {
                     best_rate = rate;

@@ -23,7 +23,7 @@ def test_batch_matches_single_builds(workers):
     if workers > 0:
         assert out["workers"] == workers
     else:
-        assert out["workers"] in (1, 2, 4, 8)
+        assert out["workers"] in (1, 2, 4, 8, 12, 16)
     for i, m in enumerate(mocks):
         s = api.Engine(api.make_config(m["survey"], bands=bands))
         s.set_pk(*PK)
