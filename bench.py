@@ -294,7 +294,7 @@ class ClockSampler:
         self.skip = 0
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.out,
+                                          "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.out,
                                          stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
@@ -511,7 +511,7 @@ def whole_job_seconds_per_build(per_build_max, world):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="c2")
