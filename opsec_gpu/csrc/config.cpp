@@ -148,6 +148,7 @@ void configure(opsec_gpu* c, const std::map<std::string, std::string>& kv) {
         }
     }
     if (has("azimuthal.parity")) c->az_parity = get("azimuthal.parity") != "0";
+    if (has("azimuthal.overlap")) c->az_overlap = to_int("azimuthal.overlap", get("azimuthal.overlap")) != 0;
     if (has("azimuthal.transform")) {
         const std::string& v = get("azimuthal.transform");
         if (v != "tiled" && v != "rows") fail(OPSEC_ERR_CONFIG, "azimuthal.transform must be tiled or rows");

@@ -305,7 +305,11 @@ int opsec_gpu_create(opsec_gpu** out, const char* cfg_text) {
         int dev = 0;
         OPSEC_CUDA(cudaGetDevice(&dev));
         c->device = dev;
-        OPSEC_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+        // the main stream at the highest priority: work overlapped on the band stream (lowest)
+        // takes the SMs the main stream's kernels leave free
+        int least = 0, greatest = 0;
+        OPSEC_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        OPSEC_CUDA(cudaStreamCreateWithPriority(&c->stream, cudaStreamNonBlocking, greatest));
     });
     *out = c;  // returned even on error so that opsec_gpu_last_error can report it
     return rc;
@@ -730,6 +734,7 @@ int opsec_gpu_fisher_build(opsec_gpu* c, int ncells, const opsec_cell* cells, co
         build_tables(c);
         t.mark();
         build_q(c);
+        prefetch_band_blocks(c, ncells, cells);
         t.mark();
         int n = eigensolve(c, ncells, cells, nmodes, false);
         t.mark();
@@ -913,6 +918,12 @@ void opsec_gpu_destroy(opsec_gpu* c) {
     }
     for (int j = 0; j <= opsec_gpu::kSide; j++)
         if (c->side_ev[j]) cudaEventDestroy(c->side_ev[j]);
+    if (c->band_stream) {
+        cudaStreamSynchronize(c->band_stream);
+        cudaStreamDestroy(c->band_stream);
+    }
+    for (auto& e : c->band_ev)
+        if (e) cudaEventDestroy(e);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }

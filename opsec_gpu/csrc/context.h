@@ -72,6 +72,13 @@ struct opsec_gpu {
     cudaStream_t side[kSide] = {};
     cusolverDnHandle_t side_solver[kSide] = {};
     cudaEvent_t side_ev[kSide + 1] = {};
+    // FP32 band blocks of the block projection, transformed on their own stream while the
+    // eigensolve runs (they depend on the Q tables only): prefetch_band_blocks, az_blocks
+    cudaStream_t band_stream = nullptr;
+    cudaEvent_t band_ev[2] = {};       // [0] Q tables ready on the main stream, [1] blocks done
+    bool band_pending = false;         // band_stream holds work the host has not waited for
+    int band_batch = 0;                // bands prefetched into azSb for this build (0: none)
+    int band_nblk = 0, band_H = 0;     // their block count and order
     long long launches = 0;
     double stage_ms[5] = {0, 0, 0, 0, 0};
     std::string warning;
@@ -94,6 +101,7 @@ struct opsec_gpu {
     int az_gemm64 = 0;
     int az_tc = 1;  // block projection GEMMs on the tensor cores (az_tc.cu); 0: cuBLAS SGEMM
     int az_tiled = 1;  // FP32 band blocks by staged tiles (1) or one thread per output (0); same bits
+    int az_overlap = 1;  // FP32 band blocks transformed during the eigensolve (1) or after it (0); same bits
     bool cub_reflect = true;
     int cub_window = 1;
     int win_key = 384, win_flush = 8, win_dot64 = 0, win_logkeys = 1, win_keyorder = 1;
@@ -136,6 +144,8 @@ struct opsec_gpu {
     std::vector<int> az_m, az_idx, az_kind;
     std::vector<double> nbar_arc;
     DevBuf<unsigned char> azws;  // azimuthal projection workspace
+    DevBuf<unsigned char> azSb;  // FP32 band blocks of one batch of bands
+    DevBuf<double> nba_band;     // per-arc Nbar read by the band-block transforms
     DevBuf<double> nba_dev;      // Nbar per arc
     DevBuf<unsigned char> syev_ws;  // batched eigensolver workspace
     DevBuf<double> bev_V, bev_T, bev_vec;  // hand-written block eigensolver: reflectors, T, vectors
@@ -210,6 +220,15 @@ void build_qsq(opsec_gpu* c);
 void load_cells(opsec_gpu* c, int ncells, const opsec_cell* cells);
 CellKeyInfo cell_info(opsec_gpu* c);
 bool azimuthal_ok(opsec_gpu* c, int ncells, const opsec_cell* cells);
+// the per-arc Nbar of a full-sky build (nba) and its mu-parity split of the azimuthal blocks: 2
+// when the mu grid and Nbar are symmetric under mu -> -mu (each order m then splits into even and
+// odd blocks), else 1
+int az_parity_split(opsec_gpu* c, const opsec_cell* cells, std::vector<double>& nba);
+// the FP32 band blocks of the block projection, transformed on the band stream while the
+// eigensolve runs (a no-op when the build will not project by blocks in FP32); band_wait: the
+// host waits for that stream
+void prefetch_band_blocks(opsec_gpu* c, int ncells, const opsec_cell* cells);
+void band_wait(opsec_gpu* c);
 void drop_eig_graph(opsec_gpu* c);
 // want_modes = false leaves the mode matrix unformed on the azimuthal path (ensure_modes forms it
 // from the kept block eigenvectors when a later step needs it)

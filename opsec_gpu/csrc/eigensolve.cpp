@@ -16,6 +16,19 @@ bool azimuthal_ok(opsec_gpu* c, int ncells, const opsec_cell* cells) {
     return true;
 }
 
+int az_parity_split(opsec_gpu* c, const opsec_cell* cells, std::vector<double>& nba) {
+    const KeySpace& ks = c->ks;
+    const int H = ks.H, Nphi = ks.N3, Nmu = ks.N2;
+    nba.assign(H, 0.0);
+    for (int h = 0; h < H; h++) nba[h] = cells[(size_t)h * Nphi].Nbar;
+    bool par = c->az_parity && c->geo.mu_symmetric() && Nmu % 2 == 0;
+    for (int h = 0; par && h < H; h++) {
+        const int ph = (h / Nmu) * Nmu + (Nmu - 1 - h % Nmu);
+        if (std::fabs(nba[h] - nba[ph]) > 1e-12 * nba[h]) par = false;
+    }
+    return par ? 2 : 1;
+}
+
 void cusolver_stream(opsec_gpu* c) {
     if (!c->solver) solver_check(cusolverDnCreate(&c->solver), "cusolverDnCreate");
     solver_check(cusolverDnSetStream(c->solver, c->stream), "cusolverDnSetStream");
@@ -133,6 +146,8 @@ bool own_block_eigensolve(opsec_gpu* c, int n, int nblk, int npar, int Nphi, int
 // After a failed device allocation a buffer may have been released without being replaced:
 // nothing cached on the device is trusted, so the next call rebuilds what it needs.
 void forget_device_state(opsec_gpu* c) {
+    band_wait(c);
+    c->band_batch = 0;
     c->q_ok = c->qsq_ok = false;
     if (!c->xi64.p || !c->xi32.p) c->tables_ok = false;
     c->az_valid = false;
@@ -153,16 +168,10 @@ int eigensolve(opsec_gpu* c, int ncells, const opsec_cell* cells, int M, bool wa
         c->eig_stats[0] = 1.0;
         const KeySpace& ks = c->ks;
         const int H = ks.H, Nphi = ks.N3, Nmu = ks.N2, nm = Nphi / 2 + 1;
-        std::vector<double> nba(H);
-        for (int h = 0; h < H; h++) nba[h] = cells[(size_t)h * Nphi].Nbar;
-        c->nbar_arc = nba;
+        std::vector<double> nba;
         // mu parity split: reflection-symmetric mu grid, even N_mu, Nbar symmetric under j -> N_mu-1-j
-        bool par = c->az_parity && c->geo.mu_symmetric() && Nmu % 2 == 0;
-        for (int h = 0; par && h < H; h++) {
-            const int ph = (h / Nmu) * Nmu + (Nmu - 1 - h % Nmu);
-            if (std::fabs(nba[h] - nba[ph]) > 1e-12 * nba[h]) par = false;
-        }
-        const int npar = par ? 2 : 1, Hb = H / npar, nblk = nm * npar;
+        const int npar = az_parity_split(c, cells, nba), Hb = H / npar, nblk = nm * npar;
+        c->nbar_arc = nba;
         c->az_npar = npar;
         DevBuf<double>& d_nba = c->nba_dev;
         d_nba.alloc(H);

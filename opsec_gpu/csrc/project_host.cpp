@@ -36,6 +36,11 @@ cublasStatus_t gemm_sb<float>(cublasHandle_t h, cublasOperation_t ta, cublasOper
     return cublasSgemmStridedBatched(h, ta, tb, m, n, k, &one, A, lda, sa, B, ldb, sb, &zero, C, ldc, sc, batch);
 }
 
+// Bands per batch of band blocks: as many as fit in ~2 GB
+int band_batch_of(int nb, size_t nS, size_t elem) {
+    return (int)std::max<size_t>(1, std::min<size_t>(nb, (size_t(2) << 30) / (elem * nS)));
+}
+
 // Band blocks and block GEMMs, in FP64 or FP32, for every band: the blocks of
 // up to ~2 GB of bands at a time are transformed, then for each block one
 // batched GEMM over those bands forms T = S_p(b) U_b and one more
@@ -49,16 +54,27 @@ T* az_blocks(opsec_gpu* c, const AzPlan& a) {
     const int nblk = a.nm * a.npar;
     const size_t nU = (size_t)a.ncol * H, nS = (size_t)nblk * H * H, nT = (size_t)H * std::max(a.Kmax, 1),
                  nC = (size_t)std::max(a.csize, 1LL) * a.nb;
-    const int bpp = (int)std::max<size_t>(1, std::min<size_t>(a.nb, (size_t(2) << 30) / (sizeof(T) * nS)));
+    const int bpp = band_batch_of(a.nb, nS, sizeof(T));
+    // FP32 band blocks live in their own buffer, whose first batch may already be under way on
+    // the band stream (prefetch_band_blocks, for this build and these blocks)
+    constexpr bool f32 = std::is_same<T, float>::value;
+    const bool pre = f32 && c->band_batch > 0 && c->band_batch == std::min(bpp, a.nb) && c->band_nblk == nblk &&
+                     c->band_H == H;
+    c->band_batch = 0;
+    if (f32 && !pre) {
+        band_wait(c);
+        c->azSb.alloc(sizeof(float) * nS * bpp);
+    }
     // tensor-core products (FP32 path): T of every band of a batch, [band][ncol][H], then the
     // tiles and the error word
     const bool tcg = sizeof(T) == sizeof(float) && c->az_tc && az_tc_supported(H);
     const size_t nTb = tcg ? (size_t)a.ncol * H * bpp : nT * bpp;
     const size_t tc_bytes = tcg ? az_tc_work_bytes(nblk, bpp, *a.Km, H) : 0;
-    ws.alloc(sizeof(T) * (nU + nS * bpp + nTb + nC) + tc_bytes + 512);
+    const size_t nSw = f32 ? 0 : nS * bpp;
+    ws.alloc(sizeof(T) * (nU + nSw + nTb + nC) + tc_bytes + 512);
     T* U = reinterpret_cast<T*>(ws.p);
-    T* Sb = U + nU;
-    T* Tm = Sb + nS * bpp;
+    T* Sb = f32 ? reinterpret_cast<T*>(c->azSb.p) : U + nU;
+    T* Tm = U + nU + nSw;
     T* Cm = Tm + nTb;
     unsigned char* tcw = reinterpret_cast<unsigned char*>(Cm + nC);
     tcw = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(tcw) + 255) & ~uintptr_t(255));
@@ -68,7 +84,12 @@ T* az_blocks(opsec_gpu* c, const AzPlan& a) {
     launch_gather_block_vectors(H, a.ncol, a.col_m, a.col_idx, c->S.p, U, c->stream, &c->launches);
     for (int p0 = 0; p0 < a.nb; p0 += bpp) {
         const int np = std::min(bpp, a.nb - p0);
-        for (int p = p0; p < p0 + np; p++) {
+        if (pre && p0 == 0) {
+            // the first batch was transformed on the band stream
+            OPSEC_CUDA(cudaStreamWaitEvent(c->stream, c->band_ev[1], 0));
+            c->band_pending = false;
+        }
+        for (int p = (pre && p0 == 0) ? p0 + np : p0; p < p0 + np; p++) {
             if (g_clock) g_clock->begin("azimuthal_transform", c->stream, 2.0 * nblk * (double)H * H * c->ks.nf);
             if constexpr (std::is_same<T, float>::value)
                 launch_azimuthal_blocks(c->ks, c->Q.p + (size_t)(1 + p) * c->ks.nkeys, a.nbar_arc, a.nm, a.npar,
@@ -241,6 +262,50 @@ void project_azimuthal(opsec_gpu* c, int ncells, int M, bool packed) {
 
 // packed = false: the caller needs only the Fisher sums, which on the azimuthal
 // path then read the block matrices (az_blockF) instead of the packed triangle.
+void band_wait(opsec_gpu* c) {
+    if (c->band_pending && c->band_stream) OPSEC_CUDA(cudaStreamSynchronize(c->band_stream));
+    c->band_pending = false;
+}
+
+void prefetch_band_blocks(opsec_gpu* c, int ncells, const opsec_cell* cells) {
+    c->band_batch = 0;
+    if (!c->az_overlap || c->az_gemm64 || !(c->projection == "auto" || c->projection == "azimuthal")) return;
+    if (c->ntab() < 2 || !azimuthal_ok(c, ncells, cells)) return;
+    const KeySpace& ks = c->ks;
+    std::vector<double> nba;
+    const int npar = az_parity_split(c, cells, nba);
+    const int H = ks.H / npar, nm = ks.N3 / 2 + 1, nblk = nm * npar, nb = c->ntab() - 1;
+    const size_t nS = (size_t)nblk * H * H;
+    const int np = std::min(band_batch_of(nb, nS, sizeof(float)), nb);
+    band_wait(c);
+    if (!c->band_stream) {
+        int least = 0, greatest = 0;
+        OPSEC_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        OPSEC_CUDA(cudaStreamCreateWithPriority(&c->band_stream, cudaStreamNonBlocking, least));
+        for (auto& e : c->band_ev) OPSEC_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    c->azSb.alloc(sizeof(float) * nS * band_batch_of(nb, nS, sizeof(float)));
+    c->nba_band.alloc(nba.size());
+    // the Q tables (and the per-arc Nbar) are complete on the main stream; the blocks depend on
+    // nothing else
+    OPSEC_CUDA(cudaMemcpyAsync(c->nba_band.p, nba.data(), sizeof(double) * nba.size(), cudaMemcpyHostToDevice,
+                               c->stream));
+    OPSEC_CUDA(cudaEventRecord(c->band_ev[0], c->stream));
+    OPSEC_CUDA(cudaStreamWaitEvent(c->band_stream, c->band_ev[0], 0));
+    float* Sb = reinterpret_cast<float*>(c->azSb.p);
+    for (int p = 0; p < np; p++) {
+        if (g_clock) g_clock->begin("azimuthal_transform", c->band_stream, 2.0 * nblk * (double)H * H * ks.nf);
+        launch_azimuthal_blocks(ks, c->Q.p + (size_t)(1 + p) * ks.nkeys, c->nba_band.p, nm, npar, Sb + (size_t)p * nS,
+                                c->band_stream, &c->launches, c->az_tiled != 0);
+        if (g_clock) g_clock->end(c->band_stream);
+    }
+    OPSEC_CUDA(cudaEventRecord(c->band_ev[1], c->band_stream));
+    c->band_pending = true;
+    c->band_batch = np;
+    c->band_nblk = nblk;
+    c->band_H = H;
+}
+
 void project_all(opsec_gpu* c, int ncells, int M, bool own_modes, bool packed) {
     c->az_blockF = false;
     if (own_modes && c->az_valid && (c->projection == "auto" || c->projection == "azimuthal")) {

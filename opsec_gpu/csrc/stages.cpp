@@ -3,6 +3,8 @@
 
 void build_q(opsec_gpu* c) {
     if (c->q_ok) return;
+    band_wait(c);  // band-block transforms still reading the old Q tables
+    c->band_batch = 0;
     build_tables(c);
     setup_keys(c);
     const int ng = c->ng;

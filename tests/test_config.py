@@ -59,6 +59,7 @@ BAD = [
     ("cubature.log_keys = yes", "cubature.log_keys"),
     ("cubature.order = random", "cubature.order"),
     ("azimuthal.transform = cols", "azimuthal.transform"),
+    ("azimuthal.overlap = yes", "azimuthal.overlap"),
 ]
 
 
