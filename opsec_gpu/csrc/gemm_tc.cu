@@ -42,9 +42,8 @@ using namespace tc;
 
 constexpr int GM = 128, GN = 256, GK = 64;  // output tile (GN: the widest), K slice (64 FP16 = one 128-byte row)
 constexpr uint32_t GA_BYTES = GM * GK * 2;  // 16 KB
-// NH halves of 128 columns per tile: B tiles of 128 NH rows; as many stages as fit beside the
-// barriers (the slices in flight must cover the TMA latency: a 128 x 128 tile consumes a 64 KB
-// stage in ~800 tensor-core cycles)
+// NH halves of 128 columns per tile: B tiles of 128 NH rows; as many stages as fit in shared
+// memory (three of 64 KB for 128-column tiles, two of 96 KB for 256-column ones)
 template <int NH>
 struct TileShape {
     static constexpr int N = 128 * NH;
