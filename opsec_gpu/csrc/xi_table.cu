@@ -89,7 +89,7 @@ constexpr int kAnchor = 16;    // Chebyshev steps per lane between rotation anch
 // the angle-addition rotation through 1024 dk r from one sincos per lane, so
 // the error stays within a few hundred ulps of the largest term (the error of
 // the three-term recurrence grows at most quadratically in its length).
-__global__ void xi_sum_kernel(XiTableArgs a) {
+__global__ void __launch_bounds__(128, 6) xi_sum_kernel(XiTableArgs a) {
     const int n = a.xl.n();
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
