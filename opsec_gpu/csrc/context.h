@@ -262,6 +262,7 @@ inline int guard(opsec_gpu* ctx, F&& f) {
     } scope(ctx);
     try {
         ctx->err.clear();
+        ctx->band_batch = 0;  // band blocks prefetched by an earlier call (one that failed) are not this call's
         if (ctx->device >= 0) OPSEC_CUDA(cudaSetDevice(ctx->device));
         f();
         return OPSEC_OK;
